@@ -1,0 +1,358 @@
+"""GB300-native sphere tracing for ForgedThoughts scenes.
+
+Python host layer over the C ABI (``include/forgedthoughts_gb300.h``).  Names
+and argument meanings mirror the reference crate's public API
+(crates/forgedthoughts/src/renderer.rs, "R"):
+
+* :class:`RenderOptions`            -- ``struct RenderOptions`` (R:32-56)
+* :class:`AccelMode`                -- ``enum AccelMode`` (R:58-63)
+* :func:`parse_and_eval`            -- ``parse_program`` + ``eval_program``
+* :func:`load_and_eval_scene`       -- ``load_and_eval_scene`` (lib.rs:280-284)
+* :func:`extract_scene_render_settings` -- R:1316-1354
+* :func:`render_depth_png_with_accel`   -- R:1139-1156
+* :func:`render_preview_progressive_with_accel` -- R:1238-1277
+* :class:`RenderError` and subclasses -- ``enum RenderError`` (R:159-168)
+
+All rendering runs in the sm_103a kernels of the native library; there is no
+CPU path in this package.
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import enum
+import struct
+import zlib
+from pathlib import Path
+from typing import Callable, Optional
+
+import numpy as np
+
+from . import _native
+
+__all__ = [
+    "AccelMode", "RenderOptions", "SceneState", "GpuScene", "DepthImage", "PreviewProgress", "RenderError",
+    "MissingSceneRoot", "UnsupportedObjectType", "ExpectedObject", "ParseError", "EvalError", "CudaError",
+    "parse_and_eval", "load_and_eval_scene", "extract_scene_render_settings", "render_depth",
+    "render_depth_png_with_accel", "render_preview_progressive_with_accel", "write_png", "read_png",
+]
+
+
+class AccelMode(enum.IntEnum):
+    Naive = 0
+    Bvh = 1
+    Bricks = 2
+
+
+@dataclasses.dataclass
+class RenderOptions:
+    """``RenderOptions`` with the reference defaults (R:43-55)."""
+
+    width: int = 800
+    height: int = 800
+    max_steps: int = 128
+    max_dist: float = 40.0
+    epsilon: float = 0.001
+    step_scale: float = 0.7
+    camera_z: float = 6.0
+    fov_y_degrees: float = 45.0
+
+    def to_c(self) -> _native.RenderOptionsC:
+        return _native.RenderOptionsC(int(self.width), int(self.height), int(self.max_steps), float(self.max_dist),
+                                      float(self.epsilon), float(self.step_scale), float(self.camera_z),
+                                      float(self.fov_y_degrees))
+
+
+# ---------------------------------------------------------------- errors
+class RenderError(RuntimeError):
+    """Base of the renderer's errors (``enum RenderError``, R:159-168)."""
+
+    status = -1
+
+
+class MissingSceneRoot(RenderError):
+    status = _native.FT_ERR_MISSING_SCENE_ROOT
+
+
+class UnsupportedObjectType(RenderError):
+    status = _native.FT_ERR_UNSUPPORTED_OBJECT
+
+
+class ExpectedObject(RenderError):
+    status = _native.FT_ERR_EXPECTED_OBJECT
+
+
+class ParseError(RenderError):
+    status = _native.FT_ERR_PARSE
+
+
+class EvalError(RenderError):
+    status = _native.FT_ERR_EVAL
+
+
+class CudaError(RenderError):
+    status = _native.FT_ERR_CUDA
+
+
+_ERRORS = {cls.status: cls for cls in (MissingSceneRoot, UnsupportedObjectType, ExpectedObject, ParseError,
+                                       EvalError, CudaError)}
+
+
+def _check(status: int) -> None:
+    if status != _native.FT_OK:
+        cls = _ERRORS.get(status, RenderError)
+        err = cls(_native.last_error() or f"native call failed with status {status}")
+        err.status = status
+        raise err
+
+
+# ---------------------------------------------------------------- scenes
+@dataclasses.dataclass
+class SceneRenderSettings:
+    """``SceneRenderSettings`` (R:66-81), render-option part."""
+
+    width: Optional[int] = None
+    height: Optional[int] = None
+    max_steps: Optional[int] = None
+    max_dist: Optional[float] = None
+    epsilon: Optional[float] = None
+    step_scale: Optional[float] = None
+    camera_z: Optional[float] = None
+    fov_y_degrees: Optional[float] = None
+    accel: Optional[AccelMode] = None
+
+
+class SceneState:
+    """An evaluated and lowered `.ft` scene (the role of ``EvalState``).
+
+    Holds the flat scene description produced by the native front-end.  The
+    GPU copy is created on first use and cached.
+    """
+
+    def __init__(self, source: str):
+        lib = _native.lib()
+        ptr = ctypes.POINTER(_native.SceneDescC)()
+        _check(lib.ft_scene_desc_from_source(source.encode("utf-8"), ctypes.byref(ptr)))
+        self._desc = ptr
+        self._gpu: Optional[GpuScene] = None
+        self.source = source
+
+    @property
+    def desc_ptr(self):
+        return self._desc
+
+    @property
+    def desc(self) -> _native.SceneDescC:
+        return self._desc.contents
+
+    def gpu(self) -> "GpuScene":
+        if self._gpu is None:
+            self._gpu = GpuScene(self)
+        return self._gpu
+
+    def close(self) -> None:
+        if self._gpu is not None:
+            self._gpu.close()
+            self._gpu = None
+        if self._desc:
+            _native.lib().ft_scene_desc_free(self._desc)
+            self._desc = ctypes.POINTER(_native.SceneDescC)()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def parse_and_eval(source: str) -> SceneState:
+    return SceneState(source)
+
+
+def load_and_eval_scene(path) -> SceneState:
+    return SceneState(Path(path).read_text())
+
+
+def extract_scene_render_settings(state: SceneState) -> SceneRenderSettings:
+    d = state.desc
+    s = d.settings
+    m = d.settings_mask
+    out = SceneRenderSettings()
+    names = ["width", "height", "max_steps", "max_dist", "epsilon", "step_scale", "camera_z", "fov_y_degrees"]
+    for bit, name in enumerate(names):
+        if m & (1 << bit):
+            setattr(out, name, getattr(s, name))
+    if d.settings_accel >= 0:
+        out.accel = AccelMode(d.settings_accel)
+    return out
+
+
+class GpuScene:
+    """A scene resident on the current CUDA device (``ft_scene``)."""
+
+    def __init__(self, state: SceneState):
+        lib = _native.lib()
+        h = ctypes.c_void_p()
+        _check(lib.ft_scene_create(state.desc_ptr, ctypes.byref(h)))
+        self._h = h
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._h
+
+    def close(self) -> None:
+        if self._h:
+            _native.lib().ft_scene_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+@dataclasses.dataclass
+class DepthImage:
+    width: int
+    height: int
+    aa: int
+    t: Optional[np.ndarray]         # (H, W, aa) float32 refined hit distance, 0 on miss
+    mask: Optional[np.ndarray]      # (H, W, aa) uint8
+    material: Optional[np.ndarray]  # (H, W, aa) uint32
+    normal: Optional[np.ndarray]    # (H, W, aa, 3) float32
+    rgb8: Optional[np.ndarray]      # (H, W, 3) uint8 depth preview
+
+
+def _ptr(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def render_depth(state: SceneState, options: RenderOptions, accel: AccelMode = AccelMode.Bvh, aa_samples: int = 1,
+                 *, want_t: bool = True, want_mask: bool = True, want_material: bool = False,
+                 want_normal: bool = False, want_rgb8: bool = True) -> DepthImage:
+    """Depth preview of ``state`` on the GPU (host output buffers)."""
+    aa = max(int(aa_samples), 1)
+    h, w = int(options.height), int(options.width)
+    t = np.empty((h, w, aa), np.float32) if want_t else None
+    mask = np.empty((h, w, aa), np.uint8) if want_mask else None
+    mat = np.empty((h, w, aa), np.uint32) if want_material else None
+    nrm = np.empty((h, w, aa, 3), np.float32) if want_normal else None
+    rgb = np.empty((h, w, 3), np.uint8) if want_rgb8 else None
+    opts = options.to_c()
+    _check(_native.lib().ft_render_depth(state.gpu().handle, ctypes.byref(opts), int(accel), aa, _ptr(t), _ptr(mask),
+                                         _ptr(mat), _ptr(nrm), _ptr(rgb), 0, None))
+    return DepthImage(w, h, aa, t, mask, mat, nrm, rgb)
+
+
+@dataclasses.dataclass
+class PreviewProgress:
+    """``PreviewProgress`` (R:96-101)."""
+
+    tiles_done: int
+    tiles_total: int
+    elapsed_ms: int
+
+
+def _tile_jobs(width: int, height: int, tile: int):
+    # tile_jobs (R:3849-3862)
+    for ty in range(0, height, tile):
+        for tx in range(0, width, tile):
+            yield tx, ty, min(tile, width - tx), min(tile, height - ty)
+
+
+def render_preview_progressive_with_accel(state: SceneState, options: RenderOptions, accel: AccelMode,
+                                          tile_size: int, aa_samples: int,
+                                          on_tile: Callable[[PreviewProgress, np.ndarray], None]) -> np.ndarray:
+    """Depth preview with the reference's per-tile progress callback.
+
+    The GPU renders the frame in one launch; ``on_tile`` then sees the image
+    with tiles revealed in the reference's tile order.  An exception raised by
+    the callback aborts the call, as a callback ``Err`` does (R:3815-3830).
+    """
+    import time
+
+    start = time.monotonic()
+    img = render_depth(state, options, accel, aa_samples, want_t=False, want_mask=False).rgb8
+    out = np.zeros_like(img)
+    jobs = list(_tile_jobs(options.width, options.height, max(int(tile_size), 1)))
+    for done, (tx, ty, tw, th) in enumerate(jobs, 1):
+        out[ty:ty + th, tx:tx + tw] = img[ty:ty + th, tx:tx + tw]
+        on_tile(PreviewProgress(done, len(jobs), int((time.monotonic() - start) * 1000)), out.copy())
+    return out
+
+
+def render_depth_png_with_accel(state: SceneState, output_path, options: RenderOptions,
+                                accel: AccelMode = AccelMode.Naive) -> None:
+    img = render_depth(state, options, accel, 1, want_t=False, want_mask=False).rgb8
+    write_png(output_path, img)
+
+
+# ---------------------------------------------------------------- PNG I/O
+def write_png(path, rgb: np.ndarray) -> None:
+    """Write an 8-bit RGB image (H, W, 3) as PNG."""
+    rgb = np.ascontiguousarray(rgb, dtype=np.uint8)
+    h, w, c = rgb.shape
+    if c != 3:
+        raise ValueError("write_png expects an RGB image")
+    raw = b"".join(b"\x00" + rgb[y].tobytes() for y in range(h))
+
+    def chunk(tag: bytes, data: bytes) -> bytes:
+        return struct.pack(">I", len(data)) + tag + data + struct.pack(">I", zlib.crc32(tag + data) & 0xFFFFFFFF)
+
+    png = b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 2, 0, 0, 0))
+    png += chunk(b"IDAT", zlib.compress(raw, 6)) + chunk(b"IEND", b"")
+    Path(path).write_bytes(png)
+
+
+def read_png(path) -> np.ndarray:
+    """Read an 8-bit non-interlaced gray/RGB/RGBA PNG as (H, W, 3) uint8."""
+    data = Path(path).read_bytes()
+    if data[:8] != b"\x89PNG\r\n\x1a\n":
+        raise ValueError("not a PNG file")
+    pos, idat, hdr = 8, b"", None
+    while pos < len(data):
+        (n,) = struct.unpack(">I", data[pos:pos + 4])
+        tag = data[pos + 4:pos + 8]
+        body = data[pos + 8:pos + 8 + n]
+        pos += 12 + n
+        if tag == b"IHDR":
+            hdr = struct.unpack(">IIBBBBB", body)
+        elif tag == b"IDAT":
+            idat += body
+        elif tag == b"IEND":
+            break
+    w, h, depth, ctype, _, _, interlace = hdr
+    if depth != 8 or interlace != 0 or ctype not in (0, 2, 6):
+        raise ValueError("unsupported PNG format")
+    ch = {0: 1, 2: 3, 6: 4}[ctype]
+    raw = zlib.decompress(idat)
+    stride = w * ch
+    out = np.zeros((h, stride), np.int32)
+    prev = np.zeros(stride, np.int32)
+    for y in range(h):
+        f = raw[y * (stride + 1)]
+        line = np.frombuffer(raw, np.uint8, stride, y * (stride + 1) + 1).astype(np.int32)
+        cur = np.zeros(stride, np.int32)
+        for x in range(stride):
+            a = cur[x - ch] if x >= ch else 0
+            b = prev[x]
+            c = prev[x - ch] if x >= ch else 0
+            if f == 0:
+                p = 0
+            elif f == 1:
+                p = a
+            elif f == 2:
+                p = b
+            elif f == 3:
+                p = (a + b) // 2
+            else:
+                pa, pb, pc = abs(b - c), abs(a - c), abs(a + b - 2 * c)
+                p = a if pa <= pb and pa <= pc else (b if pb <= pc else c)
+            cur[x] = (line[x] + p) & 0xFF
+        out[y] = cur
+        prev = cur
+    img = out.reshape(h, w, ch).astype(np.uint8)
+    if ch == 1:
+        img = np.repeat(img, 3, axis=2)
+    return img[:, :, :3]

@@ -1,0 +1,136 @@
+"""ctypes binding of the C ABI in ``include/forgedthoughts_gb300.h``.
+
+The library is built in-tree (``forgedthoughts_gb300/_build``); importing this
+module never falls back to another implementation: a missing library raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "_build" / "libforgedthoughts_gb300.so"
+
+FT_OK = 0
+FT_ERR_INVALID_ARGUMENT = 1
+FT_ERR_MISSING_SCENE_ROOT = 2
+FT_ERR_UNSUPPORTED_OBJECT = 3
+FT_ERR_EXPECTED_OBJECT = 4
+FT_ERR_PARSE = 5
+FT_ERR_EVAL = 6
+FT_ERR_CUDA = 7
+FT_ERR_TIMEOUT = 8
+FT_ERR_OUT_OF_MEMORY = 9
+FT_ERR_UNSUPPORTED = 10
+FT_ERR_NO_DEVICE = 11
+
+FT_FLAG_DEVICE_POINTERS = 1
+FT_ABI_VERSION = 1
+FT_MAX_PROGRAM_REGS = 64
+
+
+class RenderOptionsC(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("max_steps", ctypes.c_uint32),
+                ("max_dist", ctypes.c_float), ("epsilon", ctypes.c_float), ("step_scale", ctypes.c_float),
+                ("camera_z", ctypes.c_float), ("fov_y_degrees", ctypes.c_float)]
+
+
+class NodeC(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("a", ctypes.c_int32), ("b", ctypes.c_int32),
+                ("program", ctypes.c_int32), ("object_id", ctypes.c_uint32), ("material_id", ctypes.c_uint32),
+                ("ival", ctypes.c_int32), ("reserved", ctypes.c_int32), ("center", ctypes.c_float * 3),
+                ("rot_deg", ctypes.c_float * 3), ("f", ctypes.c_float * 6), ("bounds_min", ctypes.c_float * 3),
+                ("bounds_max", ctypes.c_float * 3)]
+
+
+class InstrC(ctypes.Structure):
+    _fields_ = [("op", ctypes.c_uint8), ("flags", ctypes.c_uint8), ("dst", ctypes.c_uint8), ("a", ctypes.c_uint8),
+                ("b", ctypes.c_uint8), ("c", ctypes.c_uint8), ("pad", ctypes.c_uint8 * 2),
+                ("imm", ctypes.c_float * 3)]
+
+
+class ProgramC(ctypes.Structure):
+    _fields_ = [("first_instr", ctypes.c_uint32), ("n_instr", ctypes.c_uint32), ("n_regs", ctypes.c_uint32),
+                ("n_params", ctypes.c_uint32), ("param_is_vec3", ctypes.c_uint32),
+                ("result_is_vec3", ctypes.c_uint32)]
+
+
+class LightC(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("samples", ctypes.c_uint32), ("position", ctypes.c_float * 3),
+                ("radius", ctypes.c_float), ("intensity", ctypes.c_float * 3)]
+
+
+class MaterialC(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("has_medium", ctypes.c_int32), ("thin_walled", ctypes.c_int32),
+                ("color_program", ctypes.c_int32), ("color", ctypes.c_float * 3), ("roughness", ctypes.c_float),
+                ("metallic", ctypes.c_float), ("ior", ctypes.c_float), ("transmission", ctypes.c_float),
+                ("emission_strength", ctypes.c_float), ("emission_color", ctypes.c_float * 3),
+                ("medium_ior", ctypes.c_float), ("medium_absorption", ctypes.c_float * 3),
+                ("medium_density", ctypes.c_float)]
+
+
+class CameraC(ctypes.Structure):
+    _fields_ = [("origin", ctypes.c_float * 3), ("target", ctypes.c_float * 3), ("up", ctypes.c_float * 3),
+                ("fov_y_degrees", ctypes.c_float)]
+
+
+class SceneDescC(ctypes.Structure):
+    _fields_ = [("abi_version", ctypes.c_uint32), ("root", ctypes.c_int32), ("nodes", ctypes.POINTER(NodeC)),
+                ("n_nodes", ctypes.c_uint32), ("n_instrs", ctypes.c_uint32), ("instrs", ctypes.POINTER(InstrC)),
+                ("programs", ctypes.POINTER(ProgramC)), ("n_programs", ctypes.c_uint32),
+                ("n_lights", ctypes.c_uint32), ("lights", ctypes.POINTER(LightC)),
+                ("materials", ctypes.POINTER(MaterialC)), ("n_materials", ctypes.c_uint32),
+                ("environment_program", ctypes.c_int32), ("camera", CameraC), ("has_camera", ctypes.c_int32),
+                ("scene_center", ctypes.c_float * 3), ("settings_mask", ctypes.c_uint32),
+                ("settings", RenderOptionsC), ("settings_accel", ctypes.c_int32)]
+
+
+class RenderStatsC(ctypes.Structure):
+    _fields_ = [("rays", ctypes.c_uint64), ("distance_evals", ctypes.c_uint64), ("primitive_evals", ctypes.c_uint64),
+                ("box_tests", ctypes.c_uint64), ("hook_instrs", ctypes.c_uint64), ("march_steps", ctypes.c_uint64)]
+
+
+# Every symbol include/forgedthoughts_gb300.h declares, with its signature.
+SIGNATURES = {
+    "ft_abi_version": (ctypes.c_uint32, []),
+    "ft_last_error": (ctypes.c_char_p, []),
+    "ft_scene_desc_from_source": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.POINTER(SceneDescC))]),
+    "ft_scene_desc_free": (None, [ctypes.POINTER(SceneDescC)]),
+    "ft_scene_create": (ctypes.c_int, [ctypes.POINTER(SceneDescC), ctypes.POINTER(ctypes.c_void_p)]),
+    "ft_scene_destroy": (None, [ctypes.c_void_p]),
+    "ft_render_depth": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RenderOptionsC), ctypes.c_int,
+                                       ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p]),
+    "ft_render_depth_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RenderOptionsC), ctypes.c_int,
+                                             ctypes.c_uint32, ctypes.POINTER(RenderStatsC)]),
+    "ft_measure_fp32_peak": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double)]),
+}
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """Load the native library (built by ``forgedthoughts_gb300.build``)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = Path(os.environ.get("FT_GB300_LIB", LIB_PATH))
+    if not path.exists():
+        raise RuntimeError(
+            f"native library {path} is missing; build it with `python -m forgedthoughts_gb300.build` "
+            "(there is no non-native fallback)")
+    handle = ctypes.CDLL(str(path), mode=ctypes.RTLD_GLOBAL)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(handle, name)
+        fn.restype = res
+        fn.argtypes = args
+    if handle.ft_abi_version() != FT_ABI_VERSION:
+        raise RuntimeError("native library ABI version mismatch")
+    _lib = handle
+    return _lib
+
+
+def last_error() -> str:
+    msg = lib().ft_last_error()
+    return msg.decode("utf-8", "replace") if msg else ""

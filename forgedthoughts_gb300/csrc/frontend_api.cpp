@@ -1,0 +1,90 @@
+// C ABI of the `.ft` front-end: ft_scene_desc_from_source / ft_scene_desc_free
+// and the thread-local error string shared by every entry point.
+#include <pthread.h>
+
+#include <cstring>
+#include <new>
+
+#include "common.h"
+#include "frontend.h"
+
+namespace ftcommon {
+namespace {
+thread_local std::string g_last_error;
+}
+void set_last_error(const std::string& message) { g_last_error = message; }
+void clear_last_error() { g_last_error.clear(); }
+const char* last_error_cstr() { return g_last_error.c_str(); }
+}  // namespace ftcommon
+
+namespace {
+
+struct FrontendJob {
+  const char* source = nullptr;
+  std::unique_ptr<ftfe::OwnedSceneDesc> result;
+  ft_status status = FT_OK;
+  std::string error;
+};
+
+void* run_frontend(void* arg) {
+  auto* job = static_cast<FrontendJob*>(arg);
+  try {
+    std::vector<ftfe::Stmt> program = ftfe::parse_program(job->source);
+    ftfe::EvalState state = ftfe::eval_program(program);
+    job->result = ftfe::lower_scene(state);
+  } catch (const ftfe::FrontendError& e) {
+    job->status = e.status;
+    job->error = e.what();
+  } catch (const std::bad_alloc&) {
+    job->status = FT_ERR_OUT_OF_MEMORY;
+    job->error = "out of host memory in the scene front-end";
+  } catch (const std::exception& e) {
+    job->status = FT_ERR_EVAL;
+    job->error = e.what();
+  }
+  return nullptr;
+}
+
+}  // namespace
+
+extern "C" {
+
+uint32_t ft_abi_version(void) { return FT_ABI_VERSION; }
+
+// The string lives in thread-local storage and stays valid until the next
+// call on this thread that sets or clears it.
+const char* ft_last_error(void) { return ftcommon::last_error_cstr(); }
+
+ft_status ft_scene_desc_from_source(const char* source, ft_scene_desc** out) {
+  if (!source || !out) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "source and out must be non-null");
+  *out = nullptr;
+  FrontendJob job;
+  job.source = source;
+  // Scenes such as `a + b + c + ...` over thousands of objects nest deeply;
+  // the recursive evaluator runs on a thread with a large stack.
+  pthread_attr_t attr;
+  pthread_attr_init(&attr);
+  pthread_attr_setstacksize(&attr, size_t(512) << 20);
+  pthread_t th;
+  if (pthread_create(&th, &attr, run_frontend, &job) != 0) {
+    pthread_attr_destroy(&attr);
+    return ftcommon::fail(FT_ERR_OUT_OF_MEMORY, "could not start the front-end thread");
+  }
+  pthread_join(th, nullptr);
+  pthread_attr_destroy(&attr);
+  if (job.status != FT_OK) return ftcommon::fail(job.status, job.error);
+  ftfe::OwnedSceneDesc* owned = job.result.release();
+  // desc is the first member: the C handle points at it.
+  *out = &owned->desc;
+  ftcommon::clear_last_error();
+  return FT_OK;
+}
+
+void ft_scene_desc_free(ft_scene_desc* desc) {
+  if (!desc) return;
+  auto* owned = reinterpret_cast<ftfe::OwnedSceneDesc*>(reinterpret_cast<char*>(desc) -
+                                                         offsetof(ftfe::OwnedSceneDesc, desc));
+  delete owned;
+}
+
+}  // extern "C"

@@ -1,0 +1,812 @@
+// sm_103a sphere-tracing kernels and the C ABI around them.
+//
+// One thread marches one primary sample (pixel x AA offset).  Threads of a
+// warp cover a compact 8x4-pixel tile so their rays stay coherent.  The scene
+// distance is the minimum over hard-union leaves found by walking the leaf
+// BVH in the reference's order (R:743-786, R = crates/forgedthoughts/src/
+// renderer.rs); each leaf is evaluated with a cutoff, the running best, below
+// which its value must be exact.  The march itself (raymarch_hit R:4091-4139,
+// refine_hit_distance R:4180-4200, estimate_normal R:4202-4215) and the depth
+// preview (R:3931-3971, R:5215-5227) follow the reference step for step.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "common.h"
+#include "ft_device.cuh"
+#include "scene_build.h"
+
+using ftd::DevNode;
+using ftd::F3;
+using ftd::f3;
+using ftd::Info;
+
+namespace {
+
+constexpr float kInf = __builtin_huge_valf();
+
+struct DevLeaf {
+  float bmin[3], bmax[3];
+  int32_t kind, node, first, count;
+};
+struct DevBvhNode {
+  float bmin[3], bmax[3];
+  int32_t lhs, rhs, leaf, pad;
+};
+struct DevUrTree {
+  float r;
+  int32_t n_prims, prim_first, bvh_root, inner_root, depth, fallback_first, fallback_count;
+};
+struct DevUrBvh {
+  float bmin[3], bmax[3];
+  int32_t left, right, prim_begin, prim_count;
+};
+struct DevUrInner {
+  int32_t child[2];
+  int32_t lo, hi;
+};
+static_assert(sizeof(DevLeaf) == sizeof(ftgpu::HostLeaf), "leaf layout");
+static_assert(sizeof(DevBvhNode) == sizeof(ftgpu::HostBvhNode), "bvh layout");
+static_assert(sizeof(DevUrTree) == sizeof(ftgpu::HostUrTree), "urtree layout");
+static_assert(sizeof(DevUrBvh) == sizeof(ftgpu::HostUrBvh), "urbvh layout");
+static_assert(sizeof(DevUrInner) == sizeof(ftgpu::HostUrInner), "urinner layout");
+
+struct DevScene {
+  const DevNode* __restrict__ nodes;
+  const DevLeaf* __restrict__ leaves;
+  const DevBvhNode* __restrict__ bvh;
+  const uint32_t* __restrict__ gops;
+  const DevUrTree* __restrict__ urtrees;
+  const DevUrBvh* __restrict__ ur_bvh;
+  const int32_t* __restrict__ ur_bvh_prims;
+  const int32_t* __restrict__ ur_prims;
+  const DevUrInner* __restrict__ ur_inner;
+  const ft_program* __restrict__ programs;
+  const ft_instr* __restrict__ instrs;
+  int32_t bvh_root;
+  float smin[3], smax[3];
+};
+
+struct RayParams {
+  float origin[3], fwd[3], right[3], up[3];
+  float tan_fov, aspect;
+  uint32_t width, height, aa, grid, max_steps;
+  float max_dist, eps, step_scale;
+  uint32_t tiles_x;
+  uint64_t n_items;
+};
+
+// Per-thread work counters (only compiled into the statistics variant).
+struct Counters {
+  unsigned long long evals, prims, boxes, hook_instrs, steps;
+};
+
+template <bool kStats>
+struct Ctx {
+  Counters c;
+  __device__ void eval() {
+    if (kStats) ++c.evals;
+  }
+  __device__ void prim() {
+    if (kStats) ++c.prims;
+  }
+  __device__ void box() {
+    if (kStats) ++c.boxes;
+  }
+  __device__ void step() {
+    if (kStats) ++c.steps;
+  }
+  __device__ unsigned long long* hooks() { return kStats ? &c.hook_instrs : nullptr; }
+};
+
+__device__ __forceinline__ float node_lb(F3 p, const float* mn, const float* mx) { return ftd::aabb_lb(p, mn, mx); }
+
+// Generic leaf: postfix program over the leaf's node tree (exact).
+template <bool kStats>
+__device__ Info eval_generic(const DevScene& S, int first, int count, F3 p, Ctx<kStats>& cx) {
+  Info vs[ftgpu::kMaxGenericValueStack];
+  F3 ps[ftgpu::kMaxGenericPointStack];
+  int vsp = 0, psp = 0;
+  ps[0] = p;
+  for (int k = 0; k < count; ++k) {
+    uint32_t w = S.gops[first + k];
+    uint32_t op = w >> ftgpu::kGOpShift;
+    const DevNode& n = S.nodes[w & ftgpu::kGNodeMask];
+    switch (op) {
+      case ftgpu::kGPrim:
+        cx.prim();
+        vs[vsp++] = Info{ftd::prim_distance(n, ps[psp]), n.object_id, n.material_id};
+        break;
+      case ftgpu::kGDomainPush: {
+        F3 q = ftd::to_local(ps[psp], n);
+        ps[psp + 1] = ftd::run_program(S.programs[n.program], S.instrs, &q, cx.hooks());
+        ++psp;
+        break;
+      }
+      case ftgpu::kGLocalPush:
+        ps[psp + 1] = ftd::to_local(ps[psp], n);
+        ++psp;
+        break;
+      case ftgpu::kGPostPop: {
+        float d = vs[vsp - 1].d;
+        F3 args[2] = {f3(d, d, d), ps[psp]};
+        vs[vsp - 1].d = ftd::run_program(S.programs[n.program], S.instrs, args, cx.hooks()).x;
+        --psp;
+        break;
+      }
+      case ftgpu::kGNoisePop:
+        vs[vsp - 1].d = ftd::apply_noise(ps[psp], vs[vsp - 1].d, n.ival, n.f[0], n.f[1]);
+        --psp;
+        break;
+      case ftgpu::kGPop: --psp; break;
+      case ftgpu::kGBinary: {
+        Info r = vs[--vsp];
+        Info l = vs[--vsp];
+        vs[vsp++] = ftd::combine(n.kind, n.f[0], n.f[1], l, r);
+        break;
+      }
+      case ftgpu::kGSlice: {
+        F3 q = ps[psp];
+        float coord = n.ival == 0 ? q.x : (n.ival == 1 ? q.y : q.z);
+        float slab = ftd::rmax(n.f[0] - coord, coord - n.f[1]);
+        vs[vsp - 1].d = ftd::rmax(vs[vsp - 1].d, slab);
+        break;
+      }
+      case ftgpu::kGSmooth: vs[vsp - 1].d -= n.f[0] * 0.1f; break;
+    }
+  }
+  return vs[0];
+}
+
+// union_round tree of primitives with a single radius r.
+//
+// For every primitive with exact distance >= r each union_round it feeds is
+// in its min(a, b) regime (op_union_round, R:6024-6029), so the tree value
+// only depends on the set N of primitives closer than r:
+//   * N empty: the value is the minimum primitive distance, exactly;
+//   * otherwise: evaluate the tree restricted to subtrees containing an
+//     N-primitive, treating every other subtree as +inf, which reproduces
+//     op_union_round(a, b, r) bit for bit for any b >= r.
+// N is gathered through a BVH over the tree's primitives with pruning bound
+// max(r, min(best so far, cutoff)); primitive AABBs bound their distances from
+// below, so no primitive that can change the result is skipped.
+template <bool kStats>
+__device__ Info eval_urtree(const DevScene& S, const DevUrTree& t, F3 p, float cutoff, Ctx<kStats>& cx) {
+  const float r = t.r;
+  int near_pos[ftgpu::kUrNear];
+  Info near_info[ftgpu::kUrNear];
+  int nn = 0;
+  bool overflow = false;
+  Info best{kInf, 0u, 0u};
+  int stack[48];
+  int sp = 0;
+  stack[sp++] = t.bvh_root;
+  while (sp > 0) {
+    const DevUrBvh& bn = S.ur_bvh[stack[--sp]];
+    cx.box();
+    float bound = ftd::rmax(r, fminf(best.d, cutoff));
+    if (node_lb(p, bn.bmin, bn.bmax) >= bound) continue;
+    if (bn.prim_count > 0) {
+      for (int k = 0; k < bn.prim_count; ++k) {
+        int pos = S.ur_bvh_prims[bn.prim_begin + k];
+        const DevNode& pn = S.nodes[S.ur_prims[t.prim_first + pos]];
+        cx.box();
+        float lim = ftd::rmax(r, fminf(best.d, cutoff));
+        if (node_lb(p, pn.bmin, pn.bmax) >= lim) continue;
+        cx.prim();
+        float d = ftd::prim_distance(pn, p);
+        if (d < best.d) best = Info{d, pn.object_id, pn.material_id};
+        if (d < r) {
+          if (nn < ftgpu::kUrNear) {
+            near_pos[nn] = pos;
+            near_info[nn] = Info{d, pn.object_id, pn.material_id};
+            ++nn;
+          } else {
+            overflow = true;
+          }
+        }
+      }
+      continue;
+    }
+    const DevUrBvh& L = S.ur_bvh[bn.left];
+    const DevUrBvh& R = S.ur_bvh[bn.right];
+    float ll = node_lb(p, L.bmin, L.bmax), rl = node_lb(p, R.bmin, R.bmax);
+    if (sp + 2 > 48) {
+      overflow = true;
+      break;
+    }
+    if (ll <= rl) {
+      stack[sp++] = bn.right;
+      stack[sp++] = bn.left;
+    } else {
+      stack[sp++] = bn.left;
+      stack[sp++] = bn.right;
+    }
+  }
+  if (overflow) return eval_generic(S, t.fallback_first, t.fallback_count, p, cx);
+  if (nn == 0) return best;
+  // Restricted tree fold; frames hold partially combined inner nodes.
+  struct Frame {
+    int inner, stage;
+    Info slot[2];
+  };
+  Frame fr[ftgpu::kMaxUrDepth + 1];
+  int fp = 0;
+  fr[0].inner = t.inner_root;
+  fr[0].stage = 0;
+  for (;;) {
+    Frame& F = fr[fp];
+    if (F.stage < 2) {
+      const DevUrInner& in = S.ur_inner[F.inner];
+      int c = in.child[F.stage];
+      if (c < 0) {
+        int pos = -c - 1;
+        Info v{kInf, 0u, 0u};
+        for (int k = 0; k < nn; ++k)
+          if (near_pos[k] == pos) v = near_info[k];
+        F.slot[F.stage++] = v;
+        continue;
+      }
+      const DevUrInner& ci = S.ur_inner[c];
+      bool has = false;
+      for (int k = 0; k < nn; ++k) has |= (near_pos[k] >= ci.lo && near_pos[k] < ci.hi);
+      if (!has) {
+        F.slot[F.stage++] = Info{kInf, 0u, 0u};
+        continue;
+      }
+      ++F.stage;
+      ++fp;
+      fr[fp].inner = c;
+      fr[fp].stage = 0;
+      continue;
+    }
+    Info res = ftd::combine(FT_NODE_UNION_ROUND, r, 0.0f, F.slot[0], F.slot[1]);
+    if (fp == 0) return res;
+    --fp;
+    fr[fp].slot[fr[fp].stage - 1] = res;
+  }
+}
+
+template <bool kStats>
+__device__ __forceinline__ Info eval_leaf(const DevScene& S, const DevLeaf& lf, F3 p, float cutoff, Ctx<kStats>& cx) {
+  if (lf.kind == ftgpu::kLeafPrim) {
+    const DevNode& n = S.nodes[lf.node];
+    cx.prim();
+    return Info{ftd::prim_distance(n, p), n.object_id, n.material_id};
+  }
+  if (lf.kind == ftgpu::kLeafUrTree) return eval_urtree(S, S.urtrees[lf.first], p, cutoff, cx);
+  return eval_generic(S, lf.first, lf.count, p, cx);
+}
+
+// Accelerator::distance_info over the leaf BVH (bvh_distance_info,
+// R:743-786): nearest-first, a node is skipped when its box bound exceeds the
+// best distance so far, a later leaf replaces the result only when strictly
+// closer.
+template <bool kStats>
+__device__ __noinline__ Info scene_distance(const DevScene& S, F3 p, Ctx<kStats>& cx) {
+  cx.eval();
+  float best = kInf;
+  Info cur{kInf, 0u, 0u};
+  int stack[64];
+  float stack_lb[64];
+  int sp = 0;
+  stack[sp] = S.bvh_root;
+  stack_lb[sp] = node_lb(p, S.bvh[S.bvh_root].bmin, S.bvh[S.bvh_root].bmax);
+  ++sp;
+  cx.box();
+  while (sp > 0) {
+    --sp;
+    int ni = stack[sp];
+    if (stack_lb[sp] > best) continue;
+    const DevBvhNode& n = S.bvh[ni];
+    if (n.leaf >= 0) {
+      Info in = eval_leaf(S, S.leaves[n.leaf], p, best, cx);
+      if (in.d < best) {
+        best = in.d;
+        cur = in;
+      }
+      continue;
+    }
+    const DevBvhNode& L = S.bvh[n.lhs];
+    const DevBvhNode& R = S.bvh[n.rhs];
+    float ll = node_lb(p, L.bmin, L.bmax), rl = node_lb(p, R.bmin, R.bmax);
+    cx.box();
+    cx.box();
+    if (sp + 2 > 64) break;  // depth is bounded by the median-split build
+    if (ll <= rl) {
+      stack[sp] = n.rhs; stack_lb[sp] = rl; ++sp;
+      stack[sp] = n.lhs; stack_lb[sp] = ll; ++sp;
+    } else {
+      stack[sp] = n.lhs; stack_lb[sp] = ll; ++sp;
+      stack[sp] = n.rhs; stack_lb[sp] = rl; ++sp;
+    }
+  }
+  return cur;
+}
+
+template <bool kStats>
+__device__ __forceinline__ float scene_d(const DevScene& S, F3 p, Ctx<kStats>& cx) {
+  return scene_distance(S, p, cx).d;
+}
+
+// ray_aabb_intersection (R:4141-4173)
+__device__ bool ray_aabb(F3 o, F3 d, const float* mn, const float* mx, float* t0o, float* t1o) {
+  float tmin = -kInf, tmax = kInf;
+  float os[3] = {o.x, o.y, o.z}, ds[3] = {d.x, d.y, d.z};
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    if (fabsf(ds[k]) <= 1.0e-8f) {
+      if (os[k] < mn[k] || os[k] > mx[k]) return false;
+      continue;
+    }
+    float inv = 1.0f / ds[k];
+    float t0 = (mn[k] - os[k]) * inv, t1 = (mx[k] - os[k]) * inv;
+    if (t0 > t1) {
+      float tt = t0;
+      t0 = t1;
+      t1 = tt;
+    }
+    tmin = fmaxf(tmin, t0);
+    tmax = fminf(tmax, t1);
+    if (tmax < tmin) return false;
+  }
+  *t0o = tmin;
+  *t1o = tmax;
+  return true;
+}
+
+struct HitOut {
+  float t;
+  uint32_t mat;
+  bool hit;
+  F3 normal;
+};
+
+template <bool kStats>
+__device__ HitOut march(const DevScene& S, const RayParams& P, F3 o, F3 d, bool want_normal, Ctx<kStats>& cx) {
+  HitOut h{0.0f, 0u, false, f3(0.0f, 0.0f, 0.0f)};
+  float t0, t1;
+  if (!ray_aabb(o, d, S.smin, S.smax, &t0, &t1)) return h;
+  float max_t = fminf(P.max_dist, t1);
+  float traveled = fmaxf(0.0f, fmaxf(t0, 0.0f));
+  float prev = traveled;
+  const float eps = P.eps;
+  const float scale = ftd::rclamp(P.step_scale, 0.05f, 1.0f);
+  const float min_step = fmaxf(eps * 0.5f, 1.0e-5f);
+  for (uint32_t s = 0; s < P.max_steps; ++s) {
+    if (traveled > max_t) return h;
+    cx.step();
+    Info info = scene_distance(S, o + d * traveled, cx);
+    if (fabsf(info.d) < eps) {
+      float lo = prev, hi = traveled;
+      for (int k = 0; k < 10; ++k) {
+        float mid = 0.5f * (lo + hi);
+        float dm = fabsf(scene_d(S, o + d * mid, cx));
+        if (dm < eps) hi = mid;
+        else lo = mid;
+      }
+      F3 pos = o + d * hi;
+      if (want_normal) {
+        // estimate_normal (R:4202-4215)
+        float e = fmaxf(eps * 4.0f, 1.0e-5f);
+        float dx = scene_d(S, f3(pos.x + e, pos.y, pos.z), cx) - scene_d(S, f3(pos.x - e, pos.y, pos.z), cx);
+        float dy = scene_d(S, f3(pos.x, pos.y + e, pos.z), cx) - scene_d(S, f3(pos.x, pos.y - e, pos.z), cx);
+        float dz = scene_d(S, f3(pos.x, pos.y, pos.z + e), cx) - scene_d(S, f3(pos.x, pos.y, pos.z - e), cx);
+        F3 nn = f3(dx, dy, dz);
+        h.normal = ftd::len3(nn) > 1.0e-8f ? ftd::normalize3(nn) : f3(0.0f, 1.0f, 0.0f);
+      }
+      Info fin = scene_distance(S, pos, cx);
+      h.t = hi;
+      h.mat = fin.mat;
+      h.hit = true;
+      return h;
+    }
+    prev = traveled;
+    traveled += fmaxf(fabsf(info.d) * scale, min_step);
+  }
+  return h;
+}
+
+__device__ __forceinline__ void item_coords(const RayParams& P, uint64_t i, uint32_t* px, uint32_t* py, uint32_t* s) {
+  uint32_t per_tile = 32u * P.aa;
+  uint64_t tile = i / per_tile;
+  uint32_t k = static_cast<uint32_t>(i - tile * per_tile);
+  *s = k % P.aa;
+  uint32_t j = k / P.aa;
+  *px = static_cast<uint32_t>(tile % P.tiles_x) * 8u + (j & 7u);
+  *py = static_cast<uint32_t>(tile / P.tiles_x) * 4u + (j >> 3);
+}
+
+template <bool kStats>
+__global__ void __launch_bounds__(128) march_depth_kernel(DevScene S, RayParams P, float* __restrict__ t_out,
+                                                          uint8_t* __restrict__ mask_out,
+                                                          uint32_t* __restrict__ mat_out,
+                                                          float* __restrict__ normal_out,
+                                                          unsigned long long* __restrict__ stats) {
+  uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  Ctx<kStats> cx;
+  cx.c = Counters{0, 0, 0, 0, 0};
+  bool active = i < P.n_items;
+  uint32_t px = 0, py = 0, s = 0;
+  if (active) {
+    item_coords(P, i, &px, &py, &s);
+    active = px < P.width && py < P.height;
+  }
+  if (active) {
+    // pixel_sample_offsets (R:4838-4854) and the NDC map of render_depth_tile.
+    float sx = (static_cast<float>(s % P.grid) + 0.5f) / static_cast<float>(P.grid);
+    float sy = (static_cast<float>(s / P.grid) + 0.5f) / static_cast<float>(P.grid);
+    float ndc_x = ((static_cast<float>(px) + sx) / static_cast<float>(P.width)) * 2.0f - 1.0f;
+    float ndc_y = 1.0f - ((static_cast<float>(py) + sy) / static_cast<float>(P.height)) * 2.0f;
+    ndc_x *= P.aspect;
+    F3 fwd = f3(P.fwd[0], P.fwd[1], P.fwd[2]), rt = f3(P.right[0], P.right[1], P.right[2]);
+    F3 up = f3(P.up[0], P.up[1], P.up[2]);
+    F3 dir = ftd::normalize3(fwd + rt * (ndc_x * P.tan_fov) + up * (ndc_y * P.tan_fov));
+    dir = ftd::normalize3(dir);
+    F3 o = f3(P.origin[0], P.origin[1], P.origin[2]);
+    HitOut h = march(S, P, o, dir, normal_out != nullptr, cx);
+    size_t idx = (static_cast<size_t>(py) * P.width + px) * P.aa + s;
+    t_out[idx] = h.hit ? h.t : 0.0f;
+    mask_out[idx] = h.hit ? 1 : 0;
+    if (mat_out) mat_out[idx] = h.hit ? h.mat : 0u;
+    if (normal_out) {
+      normal_out[3 * idx] = h.normal.x;
+      normal_out[3 * idx + 1] = h.normal.y;
+      normal_out[3 * idx + 2] = h.normal.z;
+    }
+  }
+  if (kStats) {
+    unsigned long long v[5] = {cx.c.evals, cx.c.prims, cx.c.boxes, cx.c.hook_instrs, cx.c.steps};
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      unsigned long long x = v[k];
+      for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+      if ((threadIdx.x & 31) == 0 && x) atomicAdd(&stats[k], x);
+    }
+  }
+}
+
+// Depth preview pixels (render_depth_tile R:3931-3971, depth_preview_value
+// R:5215-5219, spectrum_to_rgb8 R:5221-5227).
+__global__ void depth_rgb8_kernel(const float* __restrict__ t, const uint8_t* __restrict__ mask, uint32_t n_pixels,
+                                  uint32_t aa, float max_dist, uint8_t* __restrict__ rgb) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_pixels) return;
+  float sum = 0.0f;
+  float md = fmaxf(max_dist, 1.0e-6f);
+  for (uint32_t s = 0; s < aa; ++s) {
+    size_t k = static_cast<size_t>(i) * aa + s;
+    float depth = 0.0f;
+    if (mask[k]) {
+      float d = ftd::rclamp(t[k] / md, 0.0f, 1.0f);
+      float shaped = 1.0f - d;
+      depth = shaped * shaped;
+    }
+    sum += depth;
+  }
+  float v = sum * (1.0f / static_cast<float>(aa));
+  float mapped = fminf(powf(fmaxf(v, 0.0f), 1.0f / 2.2f), 1.0f);
+  uint8_t g = static_cast<uint8_t>(mapped * 255.0f);
+  rgb[3 * static_cast<size_t>(i)] = g;
+  rgb[3 * static_cast<size_t>(i) + 1] = g;
+  rgb[3 * static_cast<size_t>(i) + 2] = g;
+}
+
+// Dependent-FMA chains, 8 per thread, for the FP32 roofline denominator.
+__global__ void fma_peak_kernel(float* out, int iters, float a, float b) {
+  float x0 = threadIdx.x * 1e-3f, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6,
+        x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fmaf(x0, a, b); x1 = fmaf(x1, a, b); x2 = fmaf(x2, a, b); x3 = fmaf(x3, a, b);
+    x4 = fmaf(x4, a, b); x5 = fmaf(x5, a, b); x6 = fmaf(x6, a, b); x7 = fmaf(x7, a, b);
+  }
+  float s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+  if (s == 12345.678f) out[0] = s;
+}
+
+std::string cuda_msg(cudaError_t e, const char* what) {
+  return std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+}
+
+#define FT_CUDA_TRY(expr, what)                                                    \
+  do {                                                                             \
+    cudaError_t _e = (expr);                                                       \
+    if (_e != cudaSuccess) return ftcommon::fail(FT_ERR_CUDA, cuda_msg(_e, what)); \
+  } while (0)
+
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+}  // namespace
+
+struct ft_scene {
+  int device = 0;
+  ftgpu::SceneImage img;
+  void* arena = nullptr;
+  DevScene dev{};
+  // Per-render buffers, grown on demand and reused across calls.
+  float* d_t = nullptr;
+  uint8_t* d_mask = nullptr;
+  uint32_t* d_mat = nullptr;
+  float* d_normal = nullptr;
+  uint8_t* d_rgb = nullptr;
+  size_t cap_items = 0, cap_pixels = 0;
+  unsigned long long* d_stats = nullptr;
+  std::mutex mu;
+};
+
+namespace {
+
+ft_status upload_scene(ft_scene* sc) {
+  const ftgpu::SceneImage& im = sc->img;
+  struct Part {
+    const void* src;
+    size_t bytes;
+    size_t off;
+  };
+  std::vector<Part> parts = {
+      {im.nodes.data(), im.nodes.size() * sizeof(DevNode), 0},
+      {im.leaves.data(), im.leaves.size() * sizeof(DevLeaf), 0},
+      {im.bvh.data(), im.bvh.size() * sizeof(DevBvhNode), 0},
+      {im.gops.data(), im.gops.size() * sizeof(uint32_t), 0},
+      {im.urtrees.data(), im.urtrees.size() * sizeof(DevUrTree), 0},
+      {im.ur_bvh.data(), im.ur_bvh.size() * sizeof(DevUrBvh), 0},
+      {im.ur_bvh_prims.data(), im.ur_bvh_prims.size() * sizeof(int32_t), 0},
+      {im.ur_prims.data(), im.ur_prims.size() * sizeof(int32_t), 0},
+      {im.ur_inner.data(), im.ur_inner.size() * sizeof(DevUrInner), 0},
+      {im.programs.data(), im.programs.size() * sizeof(ft_program), 0},
+      {im.instrs.data(), im.instrs.size() * sizeof(ft_instr), 0},
+  };
+  size_t total = 0;
+  for (Part& p : parts) {
+    p.off = total;
+    total = align_up(total + std::max<size_t>(p.bytes, 16), 256);
+  }
+  std::vector<unsigned char> staging(total, 0);
+  for (const Part& p : parts)
+    if (p.bytes) std::memcpy(staging.data() + p.off, p.src, p.bytes);
+  FT_CUDA_TRY(cudaMalloc(&sc->arena, total), "cudaMalloc(scene)");
+  FT_CUDA_TRY(cudaMemcpy(sc->arena, staging.data(), total, cudaMemcpyHostToDevice), "cudaMemcpy(scene)");
+  unsigned char* base = static_cast<unsigned char*>(sc->arena);
+  DevScene& d = sc->dev;
+  d.nodes = reinterpret_cast<const DevNode*>(base + parts[0].off);
+  d.leaves = reinterpret_cast<const DevLeaf*>(base + parts[1].off);
+  d.bvh = reinterpret_cast<const DevBvhNode*>(base + parts[2].off);
+  d.gops = reinterpret_cast<const uint32_t*>(base + parts[3].off);
+  d.urtrees = reinterpret_cast<const DevUrTree*>(base + parts[4].off);
+  d.ur_bvh = reinterpret_cast<const DevUrBvh*>(base + parts[5].off);
+  d.ur_bvh_prims = reinterpret_cast<const int32_t*>(base + parts[6].off);
+  d.ur_prims = reinterpret_cast<const int32_t*>(base + parts[7].off);
+  d.ur_inner = reinterpret_cast<const DevUrInner*>(base + parts[8].off);
+  d.programs = reinterpret_cast<const ft_program*>(base + parts[9].off);
+  d.instrs = reinterpret_cast<const ft_instr*>(base + parts[10].off);
+  d.bvh_root = im.bvh_root;
+  std::memcpy(d.smin, im.scene_min, sizeof(d.smin));
+  std::memcpy(d.smax, im.scene_max, sizeof(d.smax));
+  FT_CUDA_TRY(cudaMalloc(&sc->d_stats, 8 * sizeof(unsigned long long)), "cudaMalloc(stats)");
+  return FT_OK;
+}
+
+ft_status ensure_buffers(ft_scene* sc, size_t items, size_t pixels) {
+  if (items > sc->cap_items) {
+    cudaFree(sc->d_t);
+    cudaFree(sc->d_mask);
+    cudaFree(sc->d_mat);
+    cudaFree(sc->d_normal);
+    sc->d_t = nullptr;
+    sc->d_mask = nullptr;
+    sc->d_mat = nullptr;
+    sc->d_normal = nullptr;
+    sc->cap_items = 0;
+    FT_CUDA_TRY(cudaMalloc(&sc->d_t, items * sizeof(float)), "cudaMalloc(depth)");
+    FT_CUDA_TRY(cudaMalloc(&sc->d_mask, items), "cudaMalloc(mask)");
+    FT_CUDA_TRY(cudaMalloc(&sc->d_mat, items * sizeof(uint32_t)), "cudaMalloc(material)");
+    FT_CUDA_TRY(cudaMalloc(&sc->d_normal, items * 3 * sizeof(float)), "cudaMalloc(normal)");
+    sc->cap_items = items;
+  }
+  if (pixels > sc->cap_pixels) {
+    cudaFree(sc->d_rgb);
+    sc->d_rgb = nullptr;
+    sc->cap_pixels = 0;
+    FT_CUDA_TRY(cudaMalloc(&sc->d_rgb, pixels * 3), "cudaMalloc(rgb)");
+    sc->cap_pixels = pixels;
+  }
+  return FT_OK;
+}
+
+ft_status check_options(const ft_render_options* o, uint32_t aa) {
+  if (!o) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "options must be non-null");
+  if (o->width == 0 || o->height == 0) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "width and height must be >= 1");
+  if (o->width > 32768 || o->height > 32768)
+    return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "width and height must be <= 32768");
+  if (aa > 256) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "aa_samples must be <= 256");
+  if (!(o->epsilon > 0.0f) || !std::isfinite(o->max_dist))
+    return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "epsilon must be > 0 and max_dist finite");
+  return FT_OK;
+}
+
+RayParams make_params(const ft_scene* sc, const ft_render_options& o, uint32_t aa) {
+  RayParams P{};
+  ftgpu::CameraBasis cb = ftgpu::resolve_camera(sc->img, o);
+  std::memcpy(P.origin, cb.origin, sizeof(P.origin));
+  std::memcpy(P.fwd, cb.forward, sizeof(P.fwd));
+  std::memcpy(P.right, cb.right, sizeof(P.right));
+  std::memcpy(P.up, cb.up, sizeof(P.up));
+  P.tan_fov = cb.tan_fov;
+  P.aspect = static_cast<float>(o.width) / static_cast<float>(o.height);
+  P.width = o.width;
+  P.height = o.height;
+  P.aa = aa;
+  P.grid = static_cast<uint32_t>(std::ceil(std::sqrt(static_cast<float>(aa))));
+  P.max_steps = o.max_steps;
+  P.max_dist = o.max_dist;
+  P.eps = o.epsilon;
+  P.step_scale = o.step_scale;
+  P.tiles_x = (o.width + 7) / 8;
+  uint64_t tiles_y = (o.height + 3) / 4;
+  P.n_items = static_cast<uint64_t>(P.tiles_x) * tiles_y * 32u * aa;
+  return P;
+}
+
+ft_status launch_depth(ft_scene* sc, const RayParams& P, cudaStream_t st, bool stats, float* t, uint8_t* mask,
+                       uint32_t* mat, float* normal) {
+  uint64_t blocks = (P.n_items + 127) / 128;
+  if (blocks > 0x7fffffffull) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "image too large");
+  if (stats) {
+    FT_CUDA_TRY(cudaMemsetAsync(sc->d_stats, 0, 8 * sizeof(unsigned long long), st), "cudaMemsetAsync(stats)");
+    march_depth_kernel<true><<<static_cast<unsigned>(blocks), 128, 0, st>>>(sc->dev, P, t, mask, mat, normal,
+                                                                          sc->d_stats);
+  } else {
+    march_depth_kernel<false><<<static_cast<unsigned>(blocks), 128, 0, st>>>(sc->dev, P, t, mask, mat, normal,
+                                                                           nullptr);
+  }
+  FT_CUDA_TRY(cudaGetLastError(), "march_depth_kernel launch");
+  return FT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+ft_status ft_scene_create(const ft_scene_desc* desc, ft_scene** out) {
+  if (!desc || !out) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "desc and out must be non-null");
+  *out = nullptr;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0)
+    return ftcommon::fail(FT_ERR_NO_DEVICE, e != cudaSuccess ? cuda_msg(e, "cudaGetDeviceCount") : "no CUDA device");
+  auto* sc = new (std::nothrow) ft_scene();
+  if (!sc) return ftcommon::fail(FT_ERR_OUT_OF_MEMORY, "out of host memory");
+  std::string err;
+  if (!ftgpu::build_scene_image(*desc, &sc->img, &err)) {
+    delete sc;
+    return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, err);
+  }
+  FT_CUDA_TRY(cudaGetDevice(&sc->device), "cudaGetDevice");
+  ft_status s = upload_scene(sc);
+  if (s != FT_OK) {
+    ft_scene_destroy(sc);
+    return s;
+  }
+  *out = sc;
+  ftcommon::clear_last_error();
+  return FT_OK;
+}
+
+void ft_scene_destroy(ft_scene* sc) {
+  if (!sc) return;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(sc->device);
+  cudaFree(sc->arena);
+  cudaFree(sc->d_t);
+  cudaFree(sc->d_mask);
+  cudaFree(sc->d_mat);
+  cudaFree(sc->d_normal);
+  cudaFree(sc->d_rgb);
+  cudaFree(sc->d_stats);
+  cudaSetDevice(prev);
+  delete sc;
+}
+
+ft_status ft_render_depth(ft_scene* sc, const ft_render_options* options, ft_accel_mode accel, uint32_t aa_samples,
+                          float* t_out, uint8_t* mask_out, uint32_t* material_out, float* normal_out,
+                          uint8_t* rgb8_out, uint32_t flags, void* stream) {
+  if (!sc) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "scene must be non-null");
+  if (accel < FT_ACCEL_NAIVE || accel > FT_ACCEL_BRICKS) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "unknown accel mode");
+  uint32_t aa = std::max(aa_samples, 1u);
+  if (ft_status s = check_options(options, aa)) return s;
+  std::lock_guard<std::mutex> lock(sc->mu);
+  FT_CUDA_TRY(cudaSetDevice(sc->device), "cudaSetDevice");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const bool dev_ptrs = (flags & FT_FLAG_DEVICE_POINTERS) != 0;
+  size_t pixels = static_cast<size_t>(options->width) * options->height;
+  size_t items = pixels * aa;
+  if (ft_status s = ensure_buffers(sc, items, pixels)) return s;
+  RayParams P = make_params(sc, *options, aa);
+  float* t = dev_ptrs && t_out ? t_out : sc->d_t;
+  uint8_t* mask = dev_ptrs && mask_out ? mask_out : sc->d_mask;
+  uint32_t* mat = material_out ? (dev_ptrs ? material_out : sc->d_mat) : nullptr;
+  float* nrm = normal_out ? (dev_ptrs ? normal_out : sc->d_normal) : nullptr;
+  if (ft_status s = launch_depth(sc, P, st, false, t, mask, mat, nrm)) return s;
+  if (rgb8_out) {
+    uint8_t* rgb = dev_ptrs ? rgb8_out : sc->d_rgb;
+    uint32_t np = static_cast<uint32_t>(pixels);
+    depth_rgb8_kernel<<<(np + 255) / 256, 256, 0, st>>>(t, mask, np, aa, options->max_dist, rgb);
+    FT_CUDA_TRY(cudaGetLastError(), "depth_rgb8_kernel launch");
+    if (!dev_ptrs)
+      FT_CUDA_TRY(cudaMemcpyAsync(rgb8_out, rgb, pixels * 3, cudaMemcpyDeviceToHost, st), "copy rgb8");
+  }
+  if (!dev_ptrs) {
+    if (t_out) FT_CUDA_TRY(cudaMemcpyAsync(t_out, t, items * sizeof(float), cudaMemcpyDeviceToHost, st), "copy depth");
+    if (mask_out) FT_CUDA_TRY(cudaMemcpyAsync(mask_out, mask, items, cudaMemcpyDeviceToHost, st), "copy mask");
+    if (material_out)
+      FT_CUDA_TRY(cudaMemcpyAsync(material_out, mat, items * sizeof(uint32_t), cudaMemcpyDeviceToHost, st),
+                  "copy material");
+    if (normal_out)
+      FT_CUDA_TRY(cudaMemcpyAsync(normal_out, nrm, items * 3 * sizeof(float), cudaMemcpyDeviceToHost, st),
+                  "copy normal");
+  }
+  FT_CUDA_TRY(cudaStreamSynchronize(st), "render");
+  ftcommon::clear_last_error();
+  return FT_OK;
+}
+
+ft_status ft_render_depth_stats(ft_scene* sc, const ft_render_options* options, ft_accel_mode accel,
+                                uint32_t aa_samples, ft_render_stats* stats) {
+  if (!sc || !stats) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "scene and stats must be non-null");
+  if (accel < FT_ACCEL_NAIVE || accel > FT_ACCEL_BRICKS) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "unknown accel mode");
+  uint32_t aa = std::max(aa_samples, 1u);
+  if (ft_status s = check_options(options, aa)) return s;
+  std::lock_guard<std::mutex> lock(sc->mu);
+  FT_CUDA_TRY(cudaSetDevice(sc->device), "cudaSetDevice");
+  size_t pixels = static_cast<size_t>(options->width) * options->height;
+  if (ft_status s = ensure_buffers(sc, pixels * aa, pixels)) return s;
+  RayParams P = make_params(sc, *options, aa);
+  if (ft_status s = launch_depth(sc, P, nullptr, true, sc->d_t, sc->d_mask, nullptr, sc->d_normal)) return s;
+  unsigned long long h[8] = {0};
+  FT_CUDA_TRY(cudaMemcpy(h, sc->d_stats, sizeof(h), cudaMemcpyDeviceToHost), "copy stats");
+  stats->rays = pixels * aa;
+  stats->distance_evals = h[0];
+  stats->primitive_evals = h[1];
+  stats->box_tests = h[2];
+  stats->hook_instrs = h[3];
+  stats->march_steps = h[4];
+  ftcommon::clear_last_error();
+  return FT_OK;
+}
+
+ft_status ft_measure_fp32_peak(double* tflops) {
+  if (!tflops) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "tflops must be non-null");
+  int dev = 0, sms = 0;
+  FT_CUDA_TRY(cudaGetDevice(&dev), "cudaGetDevice");
+  FT_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "sm count");
+  float* out = nullptr;
+  FT_CUDA_TRY(cudaMalloc(&out, sizeof(float)), "cudaMalloc");
+  const int iters = 1 << 16, threads = 256, blocks = sms * 8;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  fma_peak_kernel<<<blocks, threads>>>(out, iters, 0.999f, 0.001f);
+  cudaEventRecord(a);
+  const int reps = 5;
+  for (int r = 0; r < reps; ++r) fma_peak_kernel<<<blocks, threads>>>(out, iters, 0.999f, 0.001f);
+  cudaEventRecord(b);
+  cudaError_t e = cudaEventSynchronize(b);
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(out);
+  if (e != cudaSuccess) return ftcommon::fail(FT_ERR_CUDA, cuda_msg(e, "fma_peak_kernel"));
+  double flops = 2.0 * 8.0 * iters * double(threads) * blocks * reps;
+  *tflops = flops / (ms * 1e-3) / 1e12;
+  return FT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,504 @@
+// Host-side construction of the GPU scene image (see scene_build.h).
+//
+// Leaves are the operands of hard unions, collected as collect_accel_leaves
+// does (R:659-670, R = crates/forgedthoughts/src/renderer.rs); the leaf BVH
+// is built exactly as build_bvh (R:693-732): median split of leaf-AABB
+// centroids along the longest axis with a stable sort, so a GPU traversal in
+// the reference's order (R:743-786) visits leaves in the same sequence.
+#include "scene_build.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <functional>
+#include <limits>
+#include <numeric>
+
+namespace ftgpu {
+namespace {
+
+struct Box {
+  float mn[3], mx[3];
+};
+
+Box box_union(const Box& a, const Box& b) {
+  Box o;
+  for (int k = 0; k < 3; ++k) {
+    o.mn[k] = std::min(a.mn[k], b.mn[k]);
+    o.mx[k] = std::max(a.mx[k], b.mx[k]);
+  }
+  return o;
+}
+
+bool is_prim(int k) { return k >= FT_NODE_SPHERE && k <= FT_NODE_EXTRUDE_POLYGON; }
+bool is_binary(int k) { return k >= FT_NODE_UNION && k <= FT_NODE_TONGUE; }
+bool is_unary(int k) {
+  return k == FT_NODE_DOMAIN || k == FT_NODE_DISTANCE_POST || k == FT_NODE_NOISE || k == FT_NODE_SLICE ||
+         k == FT_NODE_SMOOTH;
+}
+
+float deg_to_rad(float d) { return d * (3.14159265358979323846f / 180.0f); }
+
+class Builder {
+ public:
+  Builder(const ft_scene_desc& d, SceneImage* img, std::string* err) : d_(d), img_(img), err_(err) {}
+
+  bool run() {
+    if (!validate()) return false;
+    convert_nodes();
+    bounds_.assign(d_.n_nodes, Box{});
+    have_bounds_.assign(d_.n_nodes, 0);
+    for (uint32_t i = 0; i < d_.n_nodes; ++i) node_bounds(static_cast<int>(i));
+    // Primitive nodes carry their culling box in bmin/bmax.
+    for (uint32_t i = 0; i < d_.n_nodes; ++i) {
+      if (is_prim(d_.nodes[i].kind)) {
+        std::memcpy(img_->nodes[i].bmin, bounds_[i].mn, sizeof(float) * 3);
+        std::memcpy(img_->nodes[i].bmax, bounds_[i].mx, sizeof(float) * 3);
+      }
+    }
+    const Box& sb = bounds_[d_.root];
+    std::memcpy(img_->scene_min, sb.mn, sizeof(sb.mn));
+    std::memcpy(img_->scene_max, sb.mx, sizeof(sb.mx));
+    std::memcpy(img_->scene_center, d_.scene_center, sizeof(d_.scene_center));
+    img_->camera = d_.camera;
+    img_->has_camera = d_.has_camera;
+    img_->programs.assign(d_.programs, d_.programs + d_.n_programs);
+    img_->instrs.assign(d_.instrs, d_.instrs + d_.n_instrs);
+
+    collect_leaves(d_.root);
+    std::vector<size_t> idx(img_->leaves.size());
+    std::iota(idx.begin(), idx.end(), 0);
+    img_->bvh_root = build_bvh(idx);
+    for (size_t li = 0; li < img_->leaves.size(); ++li)
+      if (!classify(li)) return false;
+    return true;
+  }
+
+ private:
+  const ft_scene_desc& d_;
+  SceneImage* img_;
+  std::string* err_;
+  std::vector<Box> bounds_;
+  std::vector<char> have_bounds_;
+
+  bool fail(const std::string& m) {
+    *err_ = m;
+    return false;
+  }
+
+  // Every index that a kernel dereferences is checked here, on the host.
+  bool validate() {
+    if (d_.abi_version != FT_ABI_VERSION) return fail("scene description has a different ABI version");
+    if (d_.n_nodes == 0 || !d_.nodes) return fail("scene has no nodes");
+    if (d_.root < 0 || static_cast<uint32_t>(d_.root) >= d_.n_nodes) return fail("scene root index out of range");
+    for (uint32_t i = 0; i < d_.n_programs; ++i) {
+      const ft_program& p = d_.programs[i];
+      if (p.n_regs > FT_MAX_PROGRAM_REGS || p.n_params > p.n_regs || p.n_instr == 0)
+        return fail("hook program " + std::to_string(i) + " has an invalid register/instruction count");
+      if (static_cast<uint64_t>(p.first_instr) + p.n_instr > d_.n_instrs)
+        return fail("hook program " + std::to_string(i) + " instruction range out of bounds");
+      for (uint32_t k = 0; k < p.n_instr; ++k) {
+        const ft_instr& in = d_.instrs[p.first_instr + k];
+        if (in.op >= FT_OP_COUNT) return fail("hook program has an unknown opcode");
+        if (in.dst >= p.n_regs || in.a >= p.n_regs || in.b >= p.n_regs || in.c >= p.n_regs)
+          return fail("hook program register index out of range");
+      }
+      if (d_.instrs[p.first_instr + p.n_instr - 1].op != FT_OP_RET)
+        return fail("hook program does not end with a return");
+    }
+    for (uint32_t i = 0; i < d_.n_nodes; ++i) {
+      const ft_node& n = d_.nodes[i];
+      if (n.kind < 0 || n.kind >= FT_NODE_KIND_COUNT) return fail("node " + std::to_string(i) + " has an unknown kind");
+      auto child_ok = [&](int c) { return c >= 0 && static_cast<uint32_t>(c) < d_.n_nodes && c != static_cast<int>(i); };
+      if (is_binary(n.kind) && (!child_ok(n.a) || !child_ok(n.b)))
+        return fail("node " + std::to_string(i) + " has an invalid child index");
+      if (is_unary(n.kind) && !child_ok(n.a)) return fail("node " + std::to_string(i) + " has an invalid base index");
+      if (n.kind == FT_NODE_DOMAIN || n.kind == FT_NODE_DISTANCE_POST) {
+        if (n.program < 0 || static_cast<uint32_t>(n.program) >= d_.n_programs)
+          return fail("modifier node " + std::to_string(i) + " has an invalid program index");
+        const ft_program& p = d_.programs[n.program];
+        bool dom = n.kind == FT_NODE_DOMAIN;
+        if (dom && (p.n_params != 1 || p.param_is_vec3 != 1u || !p.result_is_vec3))
+          return fail("domain hook must map vec3 -> vec3");
+        if (!dom && (p.n_params != 2 || p.param_is_vec3 != 2u || p.result_is_vec3))
+          return fail("distance_post hook must map (f32, vec3) -> f32");
+      }
+      if (n.kind == FT_NODE_SLICE && (n.ival < 0 || n.ival > 2)) return fail("slice axis out of range");
+    }
+    // The node graph must be a DAG reachable from the root (no cycles).
+    std::vector<char> state(d_.n_nodes, 0);
+    std::function<bool(int, int)> dfs = [&](int i, int depth) -> bool {
+      if (depth > 100000) return false;
+      if (state[i] == 1) return false;
+      if (state[i] == 2) return true;
+      state[i] = 1;
+      const ft_node& n = d_.nodes[i];
+      if ((is_binary(n.kind) || is_unary(n.kind)) && !dfs(n.a, depth + 1)) return false;
+      if (is_binary(n.kind) && !dfs(n.b, depth + 1)) return false;
+      state[i] = 2;
+      return true;
+    };
+    if (!dfs(d_.root, 0)) return fail("scene node graph has a cycle or is too deep");
+    return true;
+  }
+
+  void convert_nodes() {
+    img_->nodes.resize(d_.n_nodes);
+    for (uint32_t i = 0; i < d_.n_nodes; ++i) {
+      const ft_node& s = d_.nodes[i];
+      HostNode& n = img_->nodes[i];
+      std::memset(&n, 0, sizeof(n));
+      n.kind = s.kind;
+      n.a = s.a;
+      n.b = s.b;
+      n.program = s.program;
+      n.object_id = s.object_id;
+      n.material_id = s.material_id;
+      n.ival = s.ival;
+      std::memcpy(n.c, s.center, sizeof(n.c));
+      n.has_rot = (s.rot_deg[0] != 0.0f || s.rot_deg[1] != 0.0f || s.rot_deg[2] != 0.0f) ? 1 : 0;
+      // to_local rotates by the negated angles (R:6216-6222).
+      float rz = deg_to_rad(-s.rot_deg[2]), ry = deg_to_rad(-s.rot_deg[1]), rx = deg_to_rad(-s.rot_deg[0]);
+      n.sz = std::sin(rz); n.cz = std::cos(rz);
+      n.sy = std::sin(ry); n.cy = std::cos(ry);
+      n.sx = std::sin(rx); n.cx = std::cos(rx);
+      std::memcpy(n.f, s.f, sizeof(n.f));
+      std::memcpy(n.bmin, s.bounds_min, sizeof(n.bmin));
+      std::memcpy(n.bmax, s.bounds_max, sizeof(n.bmax));
+    }
+  }
+
+  // sdf_bounds (R:5242-5386) in f32.
+  const Box& node_bounds(int i) {
+    if (have_bounds_[i]) return bounds_[i];
+    const ft_node& n = d_.nodes[i];
+    Box b{};
+    auto cube = [&](float r) {
+      for (int k = 0; k < 3; ++k) {
+        b.mn[k] = n.center[k] - r;
+        b.mx[k] = n.center[k] + r;
+      }
+    };
+    switch (n.kind) {
+      case FT_NODE_SPHERE: cube(n.f[0]); break;
+      case FT_NODE_BOX: cube(std::sqrt(n.f[0] * n.f[0] + n.f[1] * n.f[1] + n.f[2] * n.f[2])); break;
+      case FT_NODE_CYLINDER:
+      case FT_NODE_EXTRUDE_POLYGON: cube(std::sqrt(n.f[0] * n.f[0] + n.f[1] * n.f[1])); break;
+      case FT_NODE_TORUS: cube(n.f[0] + n.f[1]); break;
+      case FT_NODE_DOMAIN:
+      case FT_NODE_DISTANCE_POST:
+      case FT_NODE_NOISE:
+        std::memcpy(b.mn, n.bounds_min, sizeof(b.mn));
+        std::memcpy(b.mx, n.bounds_max, sizeof(b.mx));
+        break;
+      case FT_NODE_SUBTRACT: b = node_bounds(n.a); break;
+      case FT_NODE_SLICE: {
+        b = node_bounds(n.a);
+        int ax = n.ival;
+        b.mn[ax] = std::max(b.mn[ax], n.f[0]);
+        b.mx[ax] = std::min(b.mx[ax], n.f[1]);
+        if (b.mx[ax] < b.mn[ax]) b.mx[ax] = b.mn[ax];
+        break;
+      }
+      case FT_NODE_SMOOTH: {
+        b = node_bounds(n.a);
+        float e = n.f[0] * 0.1f;
+        for (int k = 0; k < 3; ++k) {
+          b.mn[k] -= e;
+          b.mx[k] += e;
+        }
+        break;
+      }
+      default: b = box_union(node_bounds(n.a), node_bounds(n.b)); break;
+    }
+    bounds_[i] = b;
+    have_bounds_[i] = 1;
+    return bounds_[i];
+  }
+
+  void collect_leaves(int i) {
+    const ft_node& n = d_.nodes[i];
+    if (n.kind == FT_NODE_UNION) {
+      collect_leaves(n.a);
+      collect_leaves(n.b);
+      return;
+    }
+    HostLeaf l;
+    std::memset(&l, 0, sizeof(l));
+    const Box& b = bounds_[i];
+    std::memcpy(l.bmin, b.mn, sizeof(b.mn));
+    std::memcpy(l.bmax, b.mx, sizeof(b.mx));
+    l.node = i;
+    img_->leaves.push_back(l);
+  }
+
+  int build_bvh(const std::vector<size_t>& indices) {
+    if (indices.empty()) return -1;
+    auto& leaves = img_->leaves;
+    HostBvhNode node;
+    std::memset(&node, 0, sizeof(node));
+    node.lhs = node.rhs = node.leaf = -1;
+    if (indices.size() == 1) {
+      std::memcpy(node.bmin, leaves[indices[0]].bmin, sizeof(node.bmin));
+      std::memcpy(node.bmax, leaves[indices[0]].bmax, sizeof(node.bmax));
+      node.leaf = static_cast<int32_t>(indices[0]);
+      img_->bvh.push_back(node);
+      return static_cast<int>(img_->bvh.size()) - 1;
+    }
+    Box b;
+    std::memcpy(b.mn, leaves[indices[0]].bmin, sizeof(b.mn));
+    std::memcpy(b.mx, leaves[indices[0]].bmax, sizeof(b.mx));
+    for (size_t k = 1; k < indices.size(); ++k) {
+      Box o;
+      std::memcpy(o.mn, leaves[indices[k]].bmin, sizeof(o.mn));
+      std::memcpy(o.mx, leaves[indices[k]].bmax, sizeof(o.mx));
+      b = box_union(b, o);
+    }
+    float ex = b.mx[0] - b.mn[0], ey = b.mx[1] - b.mn[1], ez = b.mx[2] - b.mn[2];
+    int axis = (ex >= ey && ex >= ez) ? 0 : (ey >= ez ? 1 : 2);
+    auto centroid = [&](size_t li) { return (leaves[li].bmin[axis] + leaves[li].bmax[axis]) * 0.5f; };
+    std::vector<size_t> sorted = indices;
+    std::stable_sort(sorted.begin(), sorted.end(), [&](size_t x, size_t y) { return centroid(x) < centroid(y); });
+    size_t mid = sorted.size() / 2;
+    int l = build_bvh(std::vector<size_t>(sorted.begin(), sorted.begin() + mid));
+    int r = build_bvh(std::vector<size_t>(sorted.begin() + mid, sorted.end()));
+    std::memcpy(node.bmin, b.mn, sizeof(node.bmin));
+    std::memcpy(node.bmax, b.mx, sizeof(node.bmax));
+    node.lhs = l;
+    node.rhs = r;
+    img_->bvh.push_back(node);
+    return static_cast<int>(img_->bvh.size()) - 1;
+  }
+
+  // Postfix program over a leaf's node tree; tracks stack depths.
+  bool emit_generic(int i, int vdepth, int pdepth, int* vmax, int* pmax) {
+    const ft_node& n = d_.nodes[i];
+    auto op = [&](uint32_t code) { img_->gops.push_back((code << kGOpShift) | static_cast<uint32_t>(i)); };
+    *pmax = std::max(*pmax, pdepth);
+    if (static_cast<uint32_t>(i) > kGNodeMask) return fail("scene has too many nodes for the generic evaluator");
+    if (is_prim(n.kind)) {
+      op(kGPrim);
+      *vmax = std::max(*vmax, vdepth + 1);
+      return true;
+    }
+    switch (n.kind) {
+      case FT_NODE_DOMAIN:
+        op(kGDomainPush);
+        if (!emit_generic(n.a, vdepth, pdepth + 1, vmax, pmax)) return false;
+        op(kGPop);
+        return true;
+      case FT_NODE_DISTANCE_POST:
+        op(kGLocalPush);
+        if (!emit_generic(n.a, vdepth, pdepth + 1, vmax, pmax)) return false;
+        op(kGPostPop);
+        return true;
+      case FT_NODE_NOISE:
+        op(kGLocalPush);
+        if (!emit_generic(n.a, vdepth, pdepth + 1, vmax, pmax)) return false;
+        op(kGNoisePop);
+        return true;
+      case FT_NODE_SLICE:
+        if (!emit_generic(n.a, vdepth, pdepth, vmax, pmax)) return false;
+        op(kGSlice);
+        return true;
+      case FT_NODE_SMOOTH:
+        if (!emit_generic(n.a, vdepth, pdepth, vmax, pmax)) return false;
+        op(kGSmooth);
+        return true;
+      default:
+        if (!emit_generic(n.a, vdepth, pdepth, vmax, pmax)) return false;
+        if (!emit_generic(n.b, vdepth + 1, pdepth, vmax, pmax)) return false;
+        op(kGBinary);
+        return true;
+    }
+  }
+
+  bool emit_program(int root, int32_t* first, int32_t* count) {
+    *first = static_cast<int32_t>(img_->gops.size());
+    int vmax = 0, pmax = 0;
+    if (!emit_generic(root, 0, 0, &vmax, &pmax)) return false;
+    *count = static_cast<int32_t>(img_->gops.size()) - *first;
+    if (vmax > kMaxGenericValueStack || pmax >= kMaxGenericPointStack)
+      return fail("scene leaf nests operators deeper than the generic evaluator supports (" +
+                  std::to_string(vmax) + " values, " + std::to_string(pmax) + " points)");
+    img_->max_value_stack = std::max(img_->max_value_stack, vmax);
+    img_->max_point_stack = std::max(img_->max_point_stack, pmax);
+    return true;
+  }
+
+  static float processed_r(float r) { return std::max(std::fabs(r), 1.0e-6f); }
+
+  // A leaf qualifies for the culled union_round path if every inner node is
+  // union_round with one radius and every leaf is a plain primitive.
+  bool is_urtree(int root, float* r, int* nprims, int* depth) {
+    const ft_node& rn = d_.nodes[root];
+    if (rn.kind != FT_NODE_UNION_ROUND) return false;
+    *r = processed_r(rn.f[0]);
+    *nprims = 0;
+    *depth = 0;
+    std::function<bool(int, int)> walk = [&](int i, int dep) -> bool {
+      const ft_node& n = d_.nodes[i];
+      *depth = std::max(*depth, dep);
+      if (is_prim(n.kind)) {
+        ++*nprims;
+        return true;
+      }
+      if (n.kind != FT_NODE_UNION_ROUND || processed_r(n.f[0]) != *r) return false;
+      return walk(n.a, dep + 1) && walk(n.b, dep + 1);
+    };
+    return walk(root, 1) && *nprims >= 4 && *depth <= kMaxUrDepth;
+  }
+
+  int build_ur_bvh(std::vector<int32_t>& pos, size_t lo, size_t hi, int32_t prim_first) {
+    HostUrBvh node;
+    std::memset(&node, 0, sizeof(node));
+    node.left = node.right = -1;
+    Box b;
+    bool first = true;
+    for (size_t k = lo; k < hi; ++k) {
+      const HostNode& pn = img_->nodes[img_->ur_prims[prim_first + pos[k]]];
+      Box o;
+      std::memcpy(o.mn, pn.bmin, sizeof(o.mn));
+      std::memcpy(o.mx, pn.bmax, sizeof(o.mx));
+      b = first ? o : box_union(b, o);
+      first = false;
+    }
+    std::memcpy(node.bmin, b.mn, sizeof(node.bmin));
+    std::memcpy(node.bmax, b.mx, sizeof(node.bmax));
+    int self = static_cast<int>(img_->ur_bvh.size());
+    img_->ur_bvh.push_back(node);
+    if (hi - lo <= static_cast<size_t>(kUrBvhLeafSize)) {
+      img_->ur_bvh[self].prim_begin = static_cast<int32_t>(img_->ur_bvh_prims.size());
+      img_->ur_bvh[self].prim_count = static_cast<int32_t>(hi - lo);
+      for (size_t k = lo; k < hi; ++k) img_->ur_bvh_prims.push_back(pos[k]);
+      return self;
+    }
+    // Median split of primitive-box centroids along the longest centroid axis.
+    float cmn[3] = {std::numeric_limits<float>::infinity(), std::numeric_limits<float>::infinity(),
+                    std::numeric_limits<float>::infinity()};
+    float cmx[3] = {-cmn[0], -cmn[1], -cmn[2]};
+    auto cen = [&](int32_t p, int ax) {
+      const HostNode& pn = img_->nodes[img_->ur_prims[prim_first + p]];
+      return (pn.bmin[ax] + pn.bmax[ax]) * 0.5f;
+    };
+    for (size_t k = lo; k < hi; ++k)
+      for (int ax = 0; ax < 3; ++ax) {
+        cmn[ax] = std::min(cmn[ax], cen(pos[k], ax));
+        cmx[ax] = std::max(cmx[ax], cen(pos[k], ax));
+      }
+    int axis = 0;
+    for (int ax = 1; ax < 3; ++ax)
+      if (cmx[ax] - cmn[ax] > cmx[axis] - cmn[axis]) axis = ax;
+    size_t mid = (lo + hi) / 2;
+    std::nth_element(pos.begin() + lo, pos.begin() + mid, pos.begin() + hi,
+                     [&](int32_t x, int32_t y) { return cen(x, axis) < cen(y, axis); });
+    int l = build_ur_bvh(pos, lo, mid, prim_first);
+    int r = build_ur_bvh(pos, mid, hi, prim_first);
+    img_->ur_bvh[self].left = l;
+    img_->ur_bvh[self].right = r;
+    return self;
+  }
+
+  bool build_urtree(HostLeaf& leaf, float r, int depth) {
+    HostUrTree t;
+    std::memset(&t, 0, sizeof(t));
+    t.r = r;
+    t.depth = depth;
+    t.prim_first = static_cast<int32_t>(img_->ur_prims.size());
+    // In-order positions and inner nodes.
+    std::function<int(int)> walk = [&](int i) -> int {
+      const ft_node& n = d_.nodes[i];
+      if (is_prim(n.kind)) {
+        int posn = static_cast<int>(img_->ur_prims.size()) - t.prim_first;
+        img_->ur_prims.push_back(i);
+        return -(posn + 1);
+      }
+      int self = static_cast<int>(img_->ur_inner.size());
+      img_->ur_inner.push_back(HostUrInner{{0, 0}, 0, 0});
+      int lo = static_cast<int>(img_->ur_prims.size()) - t.prim_first;
+      int a = walk(n.a);
+      int b = walk(n.b);
+      int hi = static_cast<int>(img_->ur_prims.size()) - t.prim_first;
+      img_->ur_inner[self] = HostUrInner{{a, b}, lo, hi};
+      return self;
+    };
+    t.inner_root = walk(leaf.node);
+    t.n_prims = static_cast<int32_t>(img_->ur_prims.size()) - t.prim_first;
+    std::vector<int32_t> pos(t.n_prims);
+    std::iota(pos.begin(), pos.end(), 0);
+    t.bvh_root = build_ur_bvh(pos, 0, pos.size(), t.prim_first);
+    if (!emit_program(leaf.node, &t.fallback_first, &t.fallback_count)) return false;
+    leaf.kind = kLeafUrTree;
+    leaf.first = static_cast<int32_t>(img_->urtrees.size());
+    leaf.count = t.n_prims;
+    img_->urtrees.push_back(t);
+    return true;
+  }
+
+  bool classify(size_t li) {
+    HostLeaf& leaf = img_->leaves[li];
+    const ft_node& n = d_.nodes[leaf.node];
+    if (is_prim(n.kind)) {
+      leaf.kind = kLeafPrim;
+      leaf.first = leaf.count = 0;
+      return true;
+    }
+    float r;
+    int np, depth;
+    if (is_urtree(leaf.node, &r, &np, &depth)) return build_urtree(leaf, r, depth);
+    leaf.kind = kLeafGeneric;
+    return emit_program(leaf.node, &leaf.first, &leaf.count);
+  }
+};
+
+}  // namespace
+
+bool build_scene_image(const ft_scene_desc& desc, SceneImage* out, std::string* error) {
+  *out = SceneImage{};
+  Builder b(desc, out, error);
+  return b.run();
+}
+
+// parse_camera (R:6263-6286) + PinholeCamera::generate_ray basis
+// (crates/forgedthoughts/src/render_api.rs:132-144), all in f32.
+CameraBasis resolve_camera(const SceneImage& img, const ft_render_options& opt) {
+  auto normalize = [](float v[3]) {
+    float l = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    if (l <= std::numeric_limits<float>::epsilon()) return;
+    float s = 1.0f / l;
+    v[0] *= s;
+    v[1] *= s;
+    v[2] *= s;
+  };
+  auto cross = [](const float a[3], const float b[3], float o[3]) {
+    o[0] = a[1] * b[2] - a[2] * b[1];
+    o[1] = a[2] * b[0] - a[0] * b[2];
+    o[2] = a[0] * b[1] - a[1] * b[0];
+  };
+  CameraBasis cb;
+  float org[3] = {img.scene_center[0], img.scene_center[1], img.scene_center[2] + opt.camera_z};
+  float tgt[3] = {img.scene_center[0], img.scene_center[1], img.scene_center[2]};
+  float fov = opt.fov_y_degrees;
+  if (img.has_camera) {
+    if (!std::isnan(img.camera.origin[0])) std::memcpy(org, img.camera.origin, sizeof(org));
+    if (!std::isnan(img.camera.target[0])) std::memcpy(tgt, img.camera.target, sizeof(tgt));
+    if (!std::isnan(img.camera.fov_y_degrees)) fov = img.camera.fov_y_degrees;
+  }
+  std::memcpy(cb.origin, org, sizeof(org));
+  float up0[3] = {0.0f, 1.0f, 0.0f};
+  float f[3] = {tgt[0] - org[0], tgt[1] - org[1], tgt[2] - org[2]};
+  normalize(f);
+  float r[3];
+  cross(f, up0, r);
+  normalize(r);
+  float u[3];
+  cross(r, f, u);
+  normalize(u);
+  std::memcpy(cb.forward, f, sizeof(f));
+  std::memcpy(cb.right, r, sizeof(r));
+  std::memcpy(cb.up, u, sizeof(u));
+  cb.tan_fov = std::tan(0.5f * deg_to_rad(fov));
+  return cb;
+}
+
+}  // namespace ftgpu

@@ -1,0 +1,118 @@
+// Host-side construction of the GPU scene image: device node table, hard-union
+// leaves, the leaf BVH, generic leaf programs and the culled union_round-tree
+// structures.  Pure C++ (no CUDA) so it is shared by the renderer and the
+// structure tests.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "forgedthoughts_gb300.h"
+
+namespace ftgpu {
+
+// Leaf kinds.
+enum LeafKind : int32_t {
+  kLeafPrim = 0,     // a single primitive node: inline evaluation
+  kLeafGeneric = 1,  // postfix program over the leaf's node tree
+  kLeafUrTree = 2    // union_round tree of primitives with one radius
+};
+
+// Generic-program opcodes (top 5 bits of a uint32 op word, node index below).
+enum GenericOp : uint32_t {
+  kGPrim = 0,        // push primitive distance at the current point
+  kGDomainPush = 1,  // q = domain(to_local(p)); push point
+  kGLocalPush = 2,   // q = to_local(p); push point (distance_post / noise)
+  kGPostPop = 3,     // d = distance_post(d, p); pop point
+  kGNoisePop = 4,    // d = noise(p, d); pop point
+  kGPop = 5,         // pop point (after a domain base)
+  kGBinary = 6,      // combine the two top values with the node's operator
+  kGSlice = 7,
+  kGSmooth = 8
+};
+constexpr uint32_t kGOpShift = 27;
+constexpr uint32_t kGNodeMask = (1u << kGOpShift) - 1u;
+constexpr int kMaxGenericValueStack = 16;
+constexpr int kMaxGenericPointStack = 8;
+constexpr int kMaxUrDepth = 40;
+constexpr int kUrNear = 8;       // near-set capacity of the union_round tree path
+constexpr int kUrBvhLeafSize = 4;
+
+struct HostNode {  // mirrors ftd::DevNode (128 bytes)
+  int32_t kind, a, b, program;
+  uint32_t object_id, material_id;
+  int32_t ival, has_rot;
+  float c[3];
+  float sz, cz, sy, cy, sx, cx;
+  float f[6];
+  float bmin[3], bmax[3];
+  float pad[3];
+};
+static_assert(sizeof(HostNode) == 128, "HostNode layout");
+
+struct HostLeaf {
+  float bmin[3], bmax[3];
+  int32_t kind;
+  int32_t node;
+  int32_t first;
+  int32_t count;
+};
+
+struct HostBvhNode {  // leaf BVH in the reference's build order (R:693-732)
+  float bmin[3], bmax[3];
+  int32_t lhs, rhs, leaf, pad;
+};
+
+struct HostUrTree {
+  float r;
+  int32_t n_prims;
+  int32_t prim_first;   // into ur_prims (in-order position -> node index)
+  int32_t bvh_root;     // into ur_bvh
+  int32_t inner_root;   // into ur_inner
+  int32_t depth;
+  int32_t fallback_first, fallback_count;  // generic program of the whole tree
+};
+
+struct HostUrBvh {
+  float bmin[3], bmax[3];
+  int32_t left, right;
+  int32_t prim_begin, prim_count;  // into ur_bvh_prims (in-order positions)
+};
+
+struct HostUrInner {
+  int32_t child[2];  // >= 0: ur_inner index; < 0: -(position + 1) of a primitive
+  int32_t lo, hi;    // in-order primitive range covered (relative to the tree)
+};
+
+struct SceneImage {
+  std::vector<HostNode> nodes;
+  std::vector<HostLeaf> leaves;
+  std::vector<HostBvhNode> bvh;
+  int32_t bvh_root = -1;
+  std::vector<uint32_t> gops;
+  std::vector<HostUrTree> urtrees;
+  std::vector<HostUrBvh> ur_bvh;
+  std::vector<int32_t> ur_bvh_prims;
+  std::vector<int32_t> ur_prims;
+  std::vector<HostUrInner> ur_inner;
+  std::vector<ft_program> programs;
+  std::vector<ft_instr> instrs;
+  float scene_min[3], scene_max[3];
+  float scene_center[3];
+  ft_camera camera;
+  int32_t has_camera = 0;
+  int32_t max_value_stack = 0, max_point_stack = 0;
+};
+
+// Build the image; returns false with `error` set on an invalid description.
+bool build_scene_image(const ft_scene_desc& desc, SceneImage* out, std::string* error);
+
+// Camera basis (R:6263-6286, render_api.rs:132-144) in f32.
+struct CameraBasis {
+  float origin[3], forward[3], right[3], up[3];
+  float tan_fov;
+};
+CameraBasis resolve_camera(const SceneImage& img, const ft_render_options& opt);
+
+}  // namespace ftgpu

@@ -1,0 +1,91 @@
+"""CPU oracle for the sphere-tracing hot path — TEST INFRASTRUCTURE ONLY.
+
+ctypes binding of ``oracle/_build/libftoracle.so`` (a C++ restatement of the
+reference renderer's depth path, see ``oracle/oracle.cpp``).  Only the tests,
+``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg import this
+package; the product never does.
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+import numpy as np
+
+_HERE = Path(__file__).resolve().parent
+LIB_PATH = _HERE / "_build" / "libftoracle.so"
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"{LIB_PATH} missing; run `python -m forgedthoughts_gb300.build`")
+        h = ctypes.CDLL(str(LIB_PATH))
+        vp = ctypes.c_void_p
+        h.oracle_render_depth.restype = ctypes.c_int
+        h.oracle_render_depth.argtypes = [vp, vp, ctypes.c_int, ctypes.c_uint32, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, vp, vp, vp, vp,
+                                          ctypes.POINTER(ctypes.c_uint64)]
+        h.oracle_distance.restype = ctypes.c_int
+        h.oracle_distance.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, ctypes.c_size_t, vp, vp, vp]
+        h.oracle_eval_program.restype = ctypes.c_int
+        h.oracle_eval_program.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, ctypes.c_size_t, vp]
+        h.oracle_last_error.restype = ctypes.c_char_p
+        _lib = h
+    return _lib
+
+
+def _vp(x):
+    return ctypes.cast(x, ctypes.c_void_p)
+
+
+def _arr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _check(rc: int) -> None:
+    if rc != 0:
+        raise RuntimeError("oracle failed: " + (lib().oracle_last_error() or b"").decode())
+
+
+def render_depth(state, options, accel: int, aa: int = 1, precision: int = 32, threads: int = 0,
+                 rows: tuple[int, int, int] | None = None):
+    """Oracle depth preview.  Returns (t, mask, material, rgb8, evals)."""
+    from forgedthoughts_gb300 import _native  # scene description structs only
+
+    aa = max(int(aa), 1)
+    h, w = int(options.height), int(options.width)
+    t = np.zeros((h, w, aa), np.float32)
+    mask = np.zeros((h, w, aa), np.uint8)
+    mat = np.zeros((h, w, aa), np.uint32)
+    rgb = np.zeros((h, w, 3), np.uint8)
+    opts = options.to_c() if hasattr(options, "to_c") else options
+    assert isinstance(opts, _native.RenderOptionsC)
+    r0, r1, rs = rows if rows is not None else (0, h, 1)
+    evals = ctypes.c_uint64(0)
+    _check(lib().oracle_render_depth(_vp(state.desc_ptr), ctypes.cast(ctypes.pointer(opts), ctypes.c_void_p),
+                                     int(accel), aa, int(precision), int(threads), r0, r1, rs, _arr(t), _arr(mask),
+                                     _arr(mat), _arr(rgb), ctypes.byref(evals)))
+    return t, mask, mat, rgb, int(evals.value)
+
+
+def distance(state, points: np.ndarray, accel: int = 1, precision: int = 32):
+    pts = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+    n = pts.shape[0]
+    d = np.zeros(n, np.float64)
+    obj = np.zeros(n, np.uint32)
+    mat = np.zeros(n, np.uint32)
+    _check(lib().oracle_distance(_vp(state.desc_ptr), int(accel), int(precision), _arr(pts), n, _arr(d), _arr(obj),
+                                 _arr(mat)))
+    return d, obj, mat
+
+
+def eval_program(state, program: int, args: np.ndarray, precision: int = 32) -> np.ndarray:
+    """Run hook program ``program`` on ``args`` of shape (n, n_params, 3)."""
+    a = np.ascontiguousarray(args, np.float32)
+    n = a.shape[0]
+    out = np.zeros((n, 3), np.float64)
+    _check(lib().oracle_eval_program(_vp(state.desc_ptr), int(program), int(precision), _arr(a), n, _arr(out)))
+    return out

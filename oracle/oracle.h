@@ -1,0 +1,54 @@
+/*
+ * CPU oracle for the sphere-tracing hot path — TEST INFRASTRUCTURE ONLY.
+ *
+ * A C++ restatement of the reference renderer's depth path
+ * (crates/forgedthoughts/src/renderer.rs), templated on the arithmetic type:
+ * precision 32 follows the reference's f32 arithmetic step for step, precision
+ * 64 is the FP64 oracle march.  It consumes the same flat scene IR the GPU
+ * library consumes (include/forgedthoughts_gb300.h).
+ *
+ * Only the tests, the smoke check and the benchmark's CPU-baseline leg may
+ * load this library; the product never links or calls it.
+ */
+#ifndef FT_ORACLE_H
+#define FT_ORACLE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "forgedthoughts_gb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Depth preview over rows row_begin, row_begin + row_step, ... < row_end.
+ * Output layouts match ft_render_depth; rows not rendered are left untouched.
+ * `threads` <= 0 uses std::thread::hardware_concurrency().  `evals_out`
+ * (nullable) receives the number of distance evaluations performed.
+ * Returns 0 on success, a non-zero ft_status otherwise. */
+int oracle_render_depth(const ft_scene_desc* desc, const ft_render_options* options,
+                        int accel, uint32_t aa_samples, int precision, int threads,
+                        uint32_t row_begin, uint32_t row_end, uint32_t row_step,
+                        float* t_out, uint8_t* mask_out, uint32_t* material_out,
+                        uint8_t* rgb8_out, uint64_t* evals_out);
+
+/* Accelerator distance query (`Accelerator::distance_info`) at n points
+ * (xyz triples).  Outputs are nullable. */
+int oracle_distance(const ft_scene_desc* desc, int accel, int precision,
+                    const float* points, size_t n, double* distance_out,
+                    uint32_t* object_out, uint32_t* material_out);
+
+/* Evaluate hook program `program` of the scene on n argument sets.  args
+ * holds, per call, the parameters packed as 3 floats each (scalars use the
+ * first lane).  out receives 3 floats per call. */
+int oracle_eval_program(const ft_scene_desc* desc, int program, int precision,
+                        const float* args, size_t n, double* out);
+
+const char* oracle_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FT_ORACLE_H */
