@@ -99,6 +99,7 @@ SIGNATURES = {
     "ft_scene_desc_free": (None, [ctypes.POINTER(SceneDescC)]),
     "ft_scene_create": (ctypes.c_int, [ctypes.POINTER(SceneDescC), ctypes.POINTER(ctypes.c_void_p)]),
     "ft_scene_destroy": (None, [ctypes.c_void_p]),
+    "ft_scene_device_bytes": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]),
     "ft_render_depth": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RenderOptionsC), ctypes.c_int,
                                        ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p]),

@@ -528,6 +528,7 @@ struct ft_scene {
   int device = 0;
   ftgpu::SceneImage img;
   void* arena = nullptr;
+  size_t arena_bytes = 0;
   DevScene dev{};
   // Per-render buffers, grown on demand and reused across calls.
   float* d_t = nullptr;
@@ -571,6 +572,7 @@ ft_status upload_scene(ft_scene* sc) {
   for (const Part& p : parts)
     if (p.bytes) std::memcpy(staging.data() + p.off, p.src, p.bytes);
   FT_CUDA_TRY(cudaMalloc(&sc->arena, total), "cudaMalloc(scene)");
+  sc->arena_bytes = total;
   FT_CUDA_TRY(cudaMemcpy(sc->arena, staging.data(), total, cudaMemcpyHostToDevice), "cudaMemcpy(scene)");
   unsigned char* base = static_cast<unsigned char*>(sc->arena);
   DevScene& d = sc->dev;
@@ -695,6 +697,12 @@ ft_status ft_scene_create(const ft_scene_desc* desc, ft_scene** out) {
   }
   *out = sc;
   ftcommon::clear_last_error();
+  return FT_OK;
+}
+
+ft_status ft_scene_device_bytes(const ft_scene* sc, uint64_t* bytes) {
+  if (!sc || !bytes) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "scene and bytes must be non-null");
+  *bytes = sc->arena_bytes;
   return FT_OK;
 }
 

@@ -289,6 +289,9 @@ void ft_scene_desc_free(ft_scene_desc* desc);
 ft_status ft_scene_create(const ft_scene_desc* desc, ft_scene** out);
 void ft_scene_destroy(ft_scene* scene);
 
+/* Bytes of scene data the last ft_scene_create copied host -> device. */
+ft_status ft_scene_device_bytes(const ft_scene* scene, uint64_t* bytes);
+
 /* Depth preview: `render_depth_png_with_accel` (R:1139-1156) /
  * `render_preview_progressive_with_accel` (R:1238-1277) without the PNG step.
  * One primary ray per (pixel, AA offset) with the reference's deterministic

@@ -26,7 +26,7 @@ def lib() -> ctypes.CDLL:
         vp = ctypes.c_void_p
         h.oracle_render_depth.restype = ctypes.c_int
         h.oracle_render_depth.argtypes = [vp, vp, ctypes.c_int, ctypes.c_uint32, ctypes.c_int, ctypes.c_int,
-                                          ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, vp, vp, vp, vp,
+                                          ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, vp, vp, vp, vp, vp,
                                           ctypes.POINTER(ctypes.c_uint64)]
         h.oracle_distance.restype = ctypes.c_int
         h.oracle_distance.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, ctypes.c_size_t, vp, vp, vp]
@@ -51,8 +51,8 @@ def _check(rc: int) -> None:
 
 
 def render_depth(state, options, accel: int, aa: int = 1, precision: int = 32, threads: int = 0,
-                 rows: tuple[int, int, int] | None = None):
-    """Oracle depth preview.  Returns (t, mask, material, rgb8, evals)."""
+                 rows: tuple[int, int, int] | None = None, normals: bool = False):
+    """Oracle depth preview.  Returns (t, mask, material, rgb8, evals[, normal])."""
     from forgedthoughts_gb300 import _native  # scene description structs only
 
     aa = max(int(aa), 1)
@@ -61,13 +61,16 @@ def render_depth(state, options, accel: int, aa: int = 1, precision: int = 32, t
     mask = np.zeros((h, w, aa), np.uint8)
     mat = np.zeros((h, w, aa), np.uint32)
     rgb = np.zeros((h, w, 3), np.uint8)
+    nrm = np.zeros((h, w, aa, 3), np.float32) if normals else None
     opts = options.to_c() if hasattr(options, "to_c") else options
     assert isinstance(opts, _native.RenderOptionsC)
     r0, r1, rs = rows if rows is not None else (0, h, 1)
     evals = ctypes.c_uint64(0)
     _check(lib().oracle_render_depth(_vp(state.desc_ptr), ctypes.cast(ctypes.pointer(opts), ctypes.c_void_p),
                                      int(accel), aa, int(precision), int(threads), r0, r1, rs, _arr(t), _arr(mask),
-                                     _arr(mat), _arr(rgb), ctypes.byref(evals)))
+                                     _arr(mat), _arr(nrm), _arr(rgb), ctypes.byref(evals)))
+    if normals:
+        return t, mask, mat, rgb, int(evals.value), nrm
     return t, mask, mat, rgb, int(evals.value)
 
 

@@ -882,7 +882,7 @@ Opts resolve(const ft_render_options* o) {
 template <class R>
 int render_depth(const ft_scene_desc* desc, const ft_render_options* options, int accel, uint32_t aa, int threads,
                  uint32_t row_begin, uint32_t row_end, uint32_t row_step, float* t_out, uint8_t* mask_out,
-                 uint32_t* mat_out, uint8_t* rgb_out, uint64_t* evals_out) {
+                 uint32_t* mat_out, float* normal_out, uint8_t* rgb_out, uint64_t* evals_out) {
   Opts op = resolve(options);
   Scene<R> scene(*desc);
   Accel<R> acc(scene, accel);
@@ -925,6 +925,11 @@ int render_depth(const ft_scene_desc* desc, const ft_render_options* options, in
           if (t_out) t_out[idx] = hit ? static_cast<float>(h.t) : 0.0f;
           if (mask_out) mask_out[idx] = hit ? 1 : 0;
           if (mat_out) mat_out[idx] = hit ? h.mat : 0;
+          if (normal_out) {
+            normal_out[3 * idx] = hit ? static_cast<float>(h.normal.x) : 0.0f;
+            normal_out[3 * idx + 1] = hit ? static_cast<float>(h.normal.y) : 0.0f;
+            normal_out[3 * idx + 2] = hit ? static_cast<float>(h.normal.z) : 0.0f;
+          }
         }
         if (rgb_out) {
           uint8_t g = depth_to_u8(sum * (1.0f / static_cast<float>(aa)));
@@ -959,8 +964,8 @@ const char* oracle_last_error(void) { return g_error.c_str(); }
 
 int oracle_render_depth(const ft_scene_desc* desc, const ft_render_options* options, int accel, uint32_t aa_samples,
                         int precision, int threads, uint32_t row_begin, uint32_t row_end, uint32_t row_step,
-                        float* t_out, uint8_t* mask_out, uint32_t* material_out, uint8_t* rgb8_out,
-                        uint64_t* evals_out) {
+                        float* t_out, uint8_t* mask_out, uint32_t* material_out, float* normal_out,
+                        uint8_t* rgb8_out, uint64_t* evals_out) {
   if (int e = check_desc(desc)) return e;
   if (!options || options->width == 0 || options->height == 0) {
     g_error = "invalid render options";
@@ -968,9 +973,9 @@ int oracle_render_depth(const ft_scene_desc* desc, const ft_render_options* opti
   }
   if (precision == 64)
     return render_depth<double>(desc, options, accel, aa_samples, threads, row_begin, row_end, row_step, t_out,
-                                mask_out, material_out, rgb8_out, evals_out);
+                                mask_out, material_out, normal_out, rgb8_out, evals_out);
   return render_depth<float>(desc, options, accel, aa_samples, threads, row_begin, row_end, row_step, t_out,
-                             mask_out, material_out, rgb8_out, evals_out);
+                             mask_out, material_out, normal_out, rgb8_out, evals_out);
 }
 
 int oracle_distance(const ft_scene_desc* desc, int accel, int precision, const float* points, size_t n,

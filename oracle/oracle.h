@@ -31,7 +31,7 @@ int oracle_render_depth(const ft_scene_desc* desc, const ft_render_options* opti
                         int accel, uint32_t aa_samples, int precision, int threads,
                         uint32_t row_begin, uint32_t row_end, uint32_t row_step,
                         float* t_out, uint8_t* mask_out, uint32_t* material_out,
-                        uint8_t* rgb8_out, uint64_t* evals_out);
+                        float* normal_out, uint8_t* rgb8_out, uint64_t* evals_out);
 
 /* Accelerator distance query (`Accelerator::distance_info`) at n points
  * (xyz triples).  Outputs are nullable. */

@@ -1,0 +1,118 @@
+"""`.ft` front-end: the reference's own parse/eval error fixtures, hook KATs,
+scene lowering details (lights, camera, settings, modifiers)."""
+import numpy as np
+import pytest
+
+import forgedthoughts_gb300 as ft
+import oracle
+from conftest import FIXTURES
+from forgedthoughts_gb300 import _native, workloads
+
+
+@pytest.mark.parametrize("name", sorted(p.stem for p in (FIXTURES / "parse_err").glob("*.ft")))
+def test_parse_error_fixtures(name):
+    src = (FIXTURES / "parse_err" / f"{name}.ft").read_text()
+    want = (FIXTURES / "parse_err" / f"{name}.err").read_text().strip()
+    with pytest.raises(ft.ParseError) as e:
+        ft.parse_and_eval(src)
+    assert str(e.value) == want
+
+
+@pytest.mark.parametrize("name", sorted(p.stem for p in (FIXTURES / "eval_err").glob("*.ft")))
+def test_eval_error_fixtures(name):
+    src = (FIXTURES / "eval_err" / f"{name}.ft").read_text()
+    want = (FIXTURES / "eval_err" / f"{name}.err").read_text().strip()
+    with pytest.raises(ft.RenderError) as e:
+        ft.parse_and_eval(src + "\nlet scene = Sphere {};\n")
+    assert str(e.value) == want
+
+
+def test_missing_scene_root():
+    with pytest.raises(ft.MissingSceneRoot):
+        ft.parse_and_eval("let a = Sphere {};")
+
+
+def test_unsupported_object_type():
+    with pytest.raises(ft.UnsupportedObjectType):
+        ft.parse_and_eval("let scene = Teapot {};")
+
+
+def test_expected_object():
+    with pytest.raises(ft.ExpectedObject):
+        ft.parse_and_eval("let scene = 3.0;")
+
+
+def test_distance_post_kat():
+    # crates/forgedthoughts/src/lib.rs:1919: abs(d) - 0.05 at d = 0.2 is 0.15
+    st = ft.parse_and_eval("let scene = Sphere { radius: 1.0, distance_post: fn(d, p) { return abs(d) - 0.05; } };")
+    assert st.desc.n_programs == 1
+    out = oracle.eval_program(st, 0, np.array([[[0.2, 0.2, 0.2], [0.0, 0.0, 0.0]]], np.float32))
+    assert np.float32(out[0, 0]) == np.float32(0.15)
+
+
+def test_hook_program_matches_builtin_semantics():
+    src = ("let k = 3.0;\n"
+           "let scene = Sphere { radius: 1.0, domain: fn(p) {\n"
+           "  let q = rotate_y(p, p.y * 18.0);\n"
+           "  return vec3(clamp(q.x, -1.0, 1.0), mix(q.y, k, 0.25), smoothstep(0.0, 1.0, q.z)) + normalize(p) * 0.5;\n"
+           "} };")
+    st = ft.parse_and_eval(src)
+    rng = np.random.default_rng(3)
+    p = rng.uniform(-2, 2, (64, 3)).astype(np.float32)
+    got = oracle.eval_program(st, 0, p[:, None, :], precision=64)
+    for i in range(len(p)):
+        x, y, z = map(float, p[i])
+        a = np.radians(y * 18.0)
+        q = (np.cos(a) * x + np.sin(a) * z, y, -np.sin(a) * x + np.cos(a) * z)
+        t = min(max(q[2], 0.0), 1.0)
+        n = np.array([x, y, z]) / np.linalg.norm([x, y, z])
+        want = np.array([min(max(q[0], -1), 1), q[1] * 0.75 + 3.0 * 0.25, t * t * (3 - 2 * t)]) + n * 0.5
+        np.testing.assert_allclose(got[i], want, rtol=1e-6, atol=1e-6)
+
+
+def test_scene_lowering_records_lights_camera_settings():
+    src = (FIXTURES / "render_regression" / "ray_boolean_union_round.ft").read_text()
+    src += "\nlet render = RenderSettings { width: 64, height: 48, max_steps: 99, accel: Bricks {} };\n"
+    st = ft.parse_and_eval(src)
+    d = st.desc
+    assert d.n_lights == 2  # fill, key: ordered by binding name
+    assert d.lights[0].kind == 0 and abs(d.lights[0].intensity[0] - 34.0 * 0xc9 / 255.0) < 1e-4
+    assert d.has_camera == 1 and abs(d.camera.fov_y_degrees - 25.0) < 1e-6
+    s = ft.extract_scene_render_settings(st)
+    assert (s.width, s.height, s.max_steps, s.accel) == (64, 48, 99, ft.AccelMode.Bricks)
+    assert d.environment_program >= 0
+
+
+def test_union_round_tree_and_modifiers_lower():
+    st = ft.parse_and_eval(workloads.union_round_field(n=16, width=8, height=8).source)
+    kinds = [st.desc.nodes[i].kind for i in range(st.desc.n_nodes)]
+    assert kinds.count(11) == 15  # union_round nodes
+    st2 = ft.parse_and_eval(workloads.twisted_shells(n=4, width=8, height=8).source)
+    kinds2 = [st2.desc.nodes[i].kind for i in range(st2.desc.n_nodes)]
+    # one DOMAIN and one DISTANCE_POST wrapper per sphere, hooks compiled once
+    assert kinds2.count(5) == 4 and kinds2.count(6) == 4 and st2.desc.n_programs == 2
+
+
+def test_double_transform_of_domain_plus_distance_post():
+    # Both hooks keep the primitive's transform (split_modifier_base, R:1750-1780).
+    st = ft.parse_and_eval("let scene = Sphere { radius: 0.5, pos: vec3(1, 0, 0), "
+                           "domain: fn(p) { return p; }, distance_post: fn(d, p) { return d; } };")
+    d, _, _ = oracle.distance(st, np.array([[2.0, 0.0, 0.0]]), accel=0)
+    # p - c applied twice: |2 - 1 - 1| - 0.5 = -0.5
+    assert abs(d[0] + 0.5) < 1e-6
+
+
+def test_mirror_and_repeat_expand():
+    st = ft.parse_and_eval("let b = Sphere { radius: 0.25, pos: vec3(1, 0, 0) };\n"
+                           "let scene = b.mirror_x().repeat_z(2.0, 3);")
+    prims = [n for n in (st.desc.nodes[i] for i in range(st.desc.n_nodes)) if n.kind == 0]
+    centers = sorted((round(p.center[0], 3), round(p.center[2], 3)) for p in prims)
+    # the final copies are the remapped ones; each compile also leaves its base node
+    assert (-1.0, -2.0) in centers and (1.0, 2.0) in centers and (-1.0, 0.0) in centers
+
+
+def test_workload_generators_are_deterministic():
+    a = workloads.union_round_field(n=32, width=16, height=16).source
+    b = workloads.union_round_field(n=32, width=16, height=16).source
+    assert a == b
+    assert "e-" not in a and "e+" not in a  # the lexer has no exponent syntax
