@@ -524,6 +524,37 @@ size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 }  // namespace
 
+// Scratch of ft_render_depth_preview_noalloc: FT_NOALLOC_MAX_SAMPLES refined
+// distances (f32) followed by as many hit-mask bytes.  A file-scope device
+// array, so the entry point needs no allocation; every device that loads the
+// library holds it until the process exits.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[FT_NOALLOC_MAX_SAMPLES * (sizeof(float) + 1)];
+
+namespace {
+
+constexpr int kMaxNoallocDevices = 64;
+std::mutex g_noalloc_mu;
+unsigned char* g_noalloc_address[kMaxNoallocDevices] = {};
+
+// In host code `g_noalloc_scratch` names a host-side stand-in, not device
+// memory: the device address is looked up once per device, with that device
+// current, and then passed to the kernels.
+ft_status noalloc_scratch_address(int device, unsigned char** out) {
+  if (device < 0 || device >= kMaxNoallocDevices)
+    return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "device ordinal out of range for the no-allocation path");
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_address[device]) {
+    void* ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess || !ptr) return ftcommon::fail(FT_ERR_CUDA, cuda_msg(e, "cudaGetSymbolAddress(scratch)"));
+    g_noalloc_address[device] = static_cast<unsigned char*>(ptr);
+  }
+  *out = g_noalloc_address[device];
+  return FT_OK;
+}
+
+}  // namespace
+
 struct ft_scene {
   int device = 0;
   ftgpu::SceneImage img;
@@ -761,6 +792,37 @@ ft_status ft_render_depth(ft_scene* sc, const ft_render_options* options, ft_acc
                   "copy normal");
   }
   FT_CUDA_TRY(cudaStreamSynchronize(st), "render");
+  ftcommon::clear_last_error();
+  return FT_OK;
+}
+
+ft_status ft_render_depth_preview_noalloc(ft_scene* sc, const ft_render_options* options, ft_accel_mode accel,
+                                          uint32_t aa_samples, uint8_t* rgb8_out, void* stream) {
+  if (!sc || !rgb8_out) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "scene and rgb8_out must be non-null");
+  if (accel < FT_ACCEL_NAIVE || accel > FT_ACCEL_BRICKS) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "unknown accel mode");
+  uint32_t aa = std::max(aa_samples, 1u);
+  if (ft_status s = check_options(options, aa)) return s;
+  uint64_t pixels = static_cast<uint64_t>(options->width) * options->height;
+  uint64_t items = pixels * aa;
+  if (items > FT_NOALLOC_MAX_SAMPLES)
+    return ftcommon::fail(FT_ERR_INVALID_ARGUMENT,
+                          "width*height*aa = " + std::to_string(items) + " samples exceeds the no-allocation scratch "
+                          "limit of " + std::to_string(FT_NOALLOC_MAX_SAMPLES) + " samples");
+  std::lock_guard<std::mutex> lock(sc->mu);
+  FT_CUDA_TRY(cudaSetDevice(sc->device), "cudaSetDevice");
+  unsigned char* scratch = nullptr;
+  if (ft_status s = noalloc_scratch_address(sc->device, &scratch)) return s;
+  float* t = reinterpret_cast<float*>(scratch);
+  uint8_t* mask = scratch + sizeof(float) * FT_NOALLOC_MAX_SAMPLES;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  RayParams P = make_params(sc, *options, aa);
+  uint64_t blocks = (P.n_items + 127) / 128;
+  march_depth_kernel<false><<<static_cast<unsigned>(blocks), 128, 0, st>>>(sc->dev, P, t, mask, nullptr, nullptr,
+                                                                           nullptr);
+  FT_CUDA_TRY(cudaGetLastError(), "march_depth_kernel launch");
+  uint32_t np = static_cast<uint32_t>(pixels);
+  depth_rgb8_kernel<<<(np + 255) / 256, 256, 0, st>>>(t, mask, np, aa, options->max_dist, rgb8_out);
+  FT_CUDA_TRY(cudaGetLastError(), "depth_rgb8_kernel launch");
   ftcommon::clear_last_error();
   return FT_OK;
 }

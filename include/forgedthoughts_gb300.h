@@ -324,6 +324,32 @@ typedef struct ft_render_stats {
   uint64_t march_steps;
 } ft_render_stats;
 
+/* Depth preview for callers that cannot allocate device memory.
+ *
+ * No counterpart in the reference: it exists for hosts that must not call
+ * cudaMalloc while rendering, such as an engine whose allocator owns all
+ * device memory, a real-time loop that cannot afford the implicit device
+ * synchronisation of cudaMalloc/cudaFree, or a plugin running inside another
+ * framework's memory budget.  Output is the same gray preview as
+ * ft_render_depth's rgb8_out, written to `rgb8_out`, a DEVICE pointer of
+ * width*height*3 bytes owned by the caller.
+ *
+ * The per-sample depth and hit mask live in one fixed scratch array inside the
+ * library (FT_NOALLOC_MAX_SAMPLES samples, 5 bytes each, about 10 MiB), which
+ * every GPU that loads the library holds until the process exits.  Calls with
+ * width*height*max(aa,1) above FT_NOALLOC_MAX_SAMPLES fail with
+ * FT_ERR_INVALID_ARGUMENT and launch nothing.  The first call on a device
+ * looks up that array's device address (a one-time set-up); make that first
+ * call before any stream capture.  The call allocates nothing, enqueues its
+ * two kernels on `stream` and returns without waiting: the image is ready
+ * when the stream's work completes.  All calls share the scratch array and it
+ * keeps the last call's contents, so calls whose work can overlap on the GPU
+ * (other streams, other threads) race with each other; serialise them. */
+#define FT_NOALLOC_MAX_SAMPLES (1u << 21)
+ft_status ft_render_depth_preview_noalloc(ft_scene* scene, const ft_render_options* options,
+                                          ft_accel_mode accel, uint32_t aa_samples,
+                                          uint8_t* rgb8_out, void* stream);
+
 ft_status ft_render_depth_stats(ft_scene* scene, const ft_render_options* options,
                                 ft_accel_mode accel, uint32_t aa_samples,
                                 ft_render_stats* stats);

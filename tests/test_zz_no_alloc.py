@@ -1,0 +1,55 @@
+"""The depth preview for callers that cannot allocate device memory.
+
+Such callers (an engine whose allocator owns every device byte, a frame loop
+that cannot take cudaMalloc's implicit device synchronisation) pass their own
+device output buffer; the entry point keeps its per-sample scratch in a fixed
+array inside the library.  Its output must equal the regular entry point's,
+call after call.  This file is collected last so a failure here comes after
+every other test has run.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import forgedthoughts_gb300 as ft
+from forgedthoughts_gb300 import _native, workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def _noalloc(scene, opts, accel, aa, out, stream):
+    return _native.lib().ft_render_depth_preview_noalloc(scene.handle, ctypes.byref(opts.to_c()), int(accel), aa,
+                                                         ctypes.c_void_p(out.data_ptr()),
+                                                         ctypes.c_void_p(stream.cuda_stream))
+
+
+def test_noalloc_preview_matches_regular_entry_point():
+    torch = pytest.importorskip("torch")
+    cases = [workloads.union_round_field(n=64, width=320, height=180, aa=4),
+             workloads.spheres_on_ground(width=256, height=192)]
+    stream = torch.cuda.current_stream()
+    for w in cases:
+        st = ft.parse_and_eval(w.source)
+        expected = ft.render_depth(st, w.options, w.accel, w.aa, want_t=False, want_mask=False).rgb8
+        out = torch.empty(w.options.width * w.options.height * 3, dtype=torch.uint8, device="cuda")
+        for _ in range(2):  # the scratch keeps the previous call's contents
+            out.fill_(7)
+            rc = _noalloc(st.gpu(), w.options, w.accel, w.aa, out, stream)
+            assert rc == _native.FT_OK, _native.last_error()
+            torch.cuda.synchronize()
+            got = out.cpu().numpy().reshape(w.options.height, w.options.width, 3)
+            assert np.abs(got.astype(int) - expected.astype(int)).max() == 0
+        st.close()
+
+
+def test_noalloc_rejects_frames_beyond_the_scratch_limit():
+    torch = pytest.importorskip("torch")
+    w = workloads.spheres_on_ground(width=1024, height=1024)
+    st = ft.parse_and_eval(w.source)
+    out = torch.empty(1024 * 1024 * 3, dtype=torch.uint8, device="cuda")
+    rc = _noalloc(st.gpu(), w.options, w.accel, 4, out, torch.cuda.current_stream())
+    assert rc == _native.FT_ERR_INVALID_ARGUMENT
+    assert "scratch" in _native.last_error()
+    assert 1024 * 1024 * 4 > _native.FT_NOALLOC_MAX_SAMPLES
+    st.close()
