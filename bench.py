@@ -181,6 +181,10 @@ def main() -> None:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="union_round")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--width", type=int, default=0, help="override the workload's width (profiling runs)")
+    ap.add_argument("--height", type=int, default=0)
+    ap.add_argument("--aa", type=int, default=0)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
 
@@ -188,6 +192,12 @@ def main() -> None:
 
     build_all()
     w = workload(args.workload)
+    if args.width:
+        w.options.width = args.width
+    if args.height:
+        w.options.height = args.height
+    if args.aa:
+        w.aa = args.aa
     if args.impl == "reference":
         run_reference(args, w)
         return
@@ -287,7 +297,7 @@ def main() -> None:
     h_n, h_rgb = pin(items * 3, torch.float32), pin(pixels * 3, torch.uint8)
     e2e_times = []
     h2d = 0
-    for k in range(args.steps + 1):
+    for k in range(0 if args.no_e2e else args.steps + 1):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         handle = ctypes.c_void_p()
@@ -305,7 +315,7 @@ def main() -> None:
             e2e_times.append(time.perf_counter() - t0)
         h2d = int(nbytes.value) + ctypes.sizeof(opts)
     d2h = items * (4 + 1 + 4 + 12) + pixels * 3
-    e2e_value = items / statistics.mean(e2e_times) / 1e6
+    e2e_value = items / statistics.mean(e2e_times) / 1e6 if e2e_times else None
 
     # Traffic of the dominant kernel from an ncu capture (small case scaled
     # to a full launch), committed under profiles/.
