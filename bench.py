@@ -320,12 +320,11 @@ def main() -> None:
     # Traffic of the dominant kernel from an ncu capture (small case scaled
     # to a full launch), committed under profiles/.
     traffic = None
-    prof = ROOT / "profiles" / "march_depth_union_round_traffic.json"
-    if prof.exists():
-        try:
-            traffic = json.loads(prof.read_text()).get("bytes_per_full_launch")
-        except (OSError, ValueError):
-            traffic = None
+    prof = ROOT / "profiles" / "march_depth_traffic.txt"
+    if prof.exists() and w.name.startswith("union_round512") and items == 8294400:
+        for ln in prof.read_text().splitlines():
+            if ln.startswith("bytes_per_full_launch:"):
+                traffic = int(ln.split(":", 1)[1])
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
