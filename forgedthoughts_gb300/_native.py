@@ -86,6 +86,13 @@ class SceneDescC(ctypes.Structure):
                 ("settings", RenderOptionsC), ("settings_accel", ctypes.c_int32)]
 
 
+class BuildInfoC(ctypes.Structure):
+    _fields_ = [("leaves", ctypes.c_uint32), ("primitive_leaves", ctypes.c_uint32),
+                ("generic_leaves", ctypes.c_uint32), ("union_round_leaves", ctypes.c_uint32),
+                ("bvh_nodes", ctypes.c_uint32), ("grid_cells", ctypes.c_uint64), ("grid_entries", ctypes.c_uint64),
+                ("grid_max_list", ctypes.c_uint32), ("generic_ops", ctypes.c_uint32), ("build_ms", ctypes.c_double)]
+
+
 class RenderStatsC(ctypes.Structure):
     _fields_ = [("rays", ctypes.c_uint64), ("distance_evals", ctypes.c_uint64), ("primitive_evals", ctypes.c_uint64),
                 ("box_tests", ctypes.c_uint64), ("hook_instrs", ctypes.c_uint64), ("march_steps", ctypes.c_uint64)]
@@ -100,6 +107,7 @@ SIGNATURES = {
     "ft_scene_create": (ctypes.c_int, [ctypes.POINTER(SceneDescC), ctypes.POINTER(ctypes.c_void_p)]),
     "ft_scene_destroy": (None, [ctypes.c_void_p]),
     "ft_scene_device_bytes": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]),
+    "ft_scene_build_info": (ctypes.c_int, [ctypes.POINTER(SceneDescC), ctypes.POINTER(BuildInfoC)]),
     "ft_render_depth": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RenderOptionsC), ctypes.c_int,
                                        ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p]),

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -42,6 +43,10 @@ struct DevBvhNode {
 struct DevUrTree {
   float r;
   int32_t n_prims, prim_first, bvh_root, inner_root, depth, fallback_first, fallback_count;
+  float gmin[3];
+  float cell, inv_cell;
+  int32_t dims[3];
+  int32_t cell_first, pad;
 };
 struct DevUrBvh {
   float bmin[3], bmax[3];
@@ -67,6 +72,8 @@ struct DevScene {
   const int32_t* __restrict__ ur_bvh_prims;
   const int32_t* __restrict__ ur_prims;
   const DevUrInner* __restrict__ ur_inner;
+  const uint32_t* __restrict__ ur_cell_offsets;
+  const int32_t* __restrict__ ur_cell_prims;
   const ft_program* __restrict__ programs;
   const ft_instr* __restrict__ instrs;
   int32_t bvh_root;
@@ -109,7 +116,7 @@ __device__ __forceinline__ float node_lb(F3 p, const float* mn, const float* mx)
 
 // Generic leaf: postfix program over the leaf's node tree (exact).
 template <bool kStats>
-__device__ Info eval_generic(const DevScene& S, int first, int count, F3 p, Ctx<kStats>& cx) {
+__device__ __noinline__ Info eval_generic(const DevScene& S, int first, int count, F3 p, Ctx<kStats>& cx) {
   Info vs[ftgpu::kMaxGenericValueStack];
   F3 ps[ftgpu::kMaxGenericPointStack];
   int vsp = 0, psp = 0;
@@ -176,42 +183,58 @@ __device__ Info eval_generic(const DevScene& S, int first, int count, F3 p, Ctx<
 // N is gathered through a BVH over the tree's primitives with pruning bound
 // max(r, min(best so far, cutoff)); primitive AABBs bound their distances from
 // below, so no primitive that can change the result is skipped.
+__device__ __noinline__ Info ur_fold(const DevScene& S, const DevUrTree& t, const int* near_pos,
+                                     const Info* near_info, int nn);
+
 template <bool kStats>
-__device__ Info eval_urtree(const DevScene& S, const DevUrTree& t, F3 p, float cutoff, Ctx<kStats>& cx) {
+__device__ __forceinline__ Info eval_urtree(const DevScene& S, const DevUrTree& t, F3 p, float cutoff,
+                                            Ctx<kStats>& cx) {
   const float r = t.r;
   int near_pos[ftgpu::kUrNear];
   Info near_info[ftgpu::kUrNear];
   int nn = 0;
   bool overflow = false;
   Info best{kInf, 0u, 0u};
+  // Test one primitive against the running bound; evaluate it if it can
+  // matter and record it in the near set when closer than r.
+  auto consider = [&](int pos) {
+    const DevNode& pn = S.nodes[S.ur_prims[t.prim_first + pos]];
+    cx.box();
+    float lim = ftd::rmax(r, fminf(best.d, cutoff));
+    if (node_lb(p, pn.bmin, pn.bmax) >= lim) return;
+    cx.prim();
+    float d = ftd::prim_distance(pn, p);
+    if (d < best.d) best = Info{d, pn.object_id, pn.material_id};
+    if (d < r) {
+      if (nn < ftgpu::kUrNear) {
+        near_pos[nn] = pos;
+        near_info[nn] = Info{d, pn.object_id, pn.material_id};
+        ++nn;
+      } else {
+        overflow = true;
+      }
+    }
+  };
   int stack[48];
   int sp = 0;
-  stack[sp++] = t.bvh_root;
+  // Inside the candidate grid one cell list replaces the BVH walk.
+  float gx = (p.x - t.gmin[0]) * t.inv_cell, gy = (p.y - t.gmin[1]) * t.inv_cell, gz = (p.z - t.gmin[2]) * t.inv_cell;
+  if (t.dims[0] > 0 && gx >= 0.0f && gy >= 0.0f && gz >= 0.0f && gx < (float)t.dims[0] && gy < (float)t.dims[1] &&
+      gz < (float)t.dims[2]) {
+    int ix = min((int)gx, t.dims[0] - 1), iy = min((int)gy, t.dims[1] - 1), iz = min((int)gz, t.dims[2] - 1);
+    int cell = t.cell_first + ix + t.dims[0] * (iy + t.dims[1] * iz);
+    uint32_t beg = S.ur_cell_offsets[cell], end = S.ur_cell_offsets[cell + 1];
+    for (uint32_t k = beg; k < end; ++k) consider(S.ur_cell_prims[k]);
+  } else {
+    stack[sp++] = t.bvh_root;
+  }
   while (sp > 0) {
     const DevUrBvh& bn = S.ur_bvh[stack[--sp]];
     cx.box();
     float bound = ftd::rmax(r, fminf(best.d, cutoff));
     if (node_lb(p, bn.bmin, bn.bmax) >= bound) continue;
     if (bn.prim_count > 0) {
-      for (int k = 0; k < bn.prim_count; ++k) {
-        int pos = S.ur_bvh_prims[bn.prim_begin + k];
-        const DevNode& pn = S.nodes[S.ur_prims[t.prim_first + pos]];
-        cx.box();
-        float lim = ftd::rmax(r, fminf(best.d, cutoff));
-        if (node_lb(p, pn.bmin, pn.bmax) >= lim) continue;
-        cx.prim();
-        float d = ftd::prim_distance(pn, p);
-        if (d < best.d) best = Info{d, pn.object_id, pn.material_id};
-        if (d < r) {
-          if (nn < ftgpu::kUrNear) {
-            near_pos[nn] = pos;
-            near_info[nn] = Info{d, pn.object_id, pn.material_id};
-            ++nn;
-          } else {
-            overflow = true;
-          }
-        }
-      }
+      for (int k = 0; k < bn.prim_count; ++k) consider(S.ur_bvh_prims[bn.prim_begin + k]);
       continue;
     }
     const DevUrBvh& L = S.ur_bvh[bn.left];
@@ -231,7 +254,15 @@ __device__ Info eval_urtree(const DevScene& S, const DevUrTree& t, F3 p, float c
   }
   if (overflow) return eval_generic(S, t.fallback_first, t.fallback_count, p, cx);
   if (nn == 0) return best;
-  // Restricted tree fold; frames hold partially combined inner nodes.
+  return ur_fold(S, t, near_pos, near_info, nn);
+}
+
+// Restricted union_round fold over the subtrees holding near primitives
+// (out of line: only points within r of a primitive take it).
+__device__ __noinline__ Info ur_fold(const DevScene& S, const DevUrTree& t, const int* near_pos,
+                                     const Info* near_info, int nn) {
+  const float r = t.r;
+  // Frames hold partially combined inner nodes.
   struct Frame {
     int inner, stage;
     Info slot[2];
@@ -289,8 +320,7 @@ __device__ __forceinline__ Info eval_leaf(const DevScene& S, const DevLeaf& lf, 
 // best distance so far, a later leaf replaces the result only when strictly
 // closer.
 template <bool kStats>
-__device__ __noinline__ Info scene_distance(const DevScene& S, F3 p, Ctx<kStats>& cx) {
-  cx.eval();
+__device__ __noinline__ Info scene_distance_bvh(const DevScene& S, F3 p, Ctx<kStats>& cx) {
   float best = kInf;
   Info cur{kInf, 0u, 0u};
   int stack[64];
@@ -328,6 +358,35 @@ __device__ __noinline__ Info scene_distance(const DevScene& S, F3 p, Ctx<kStats>
     }
   }
   return cur;
+}
+
+// Same traversal, with the one- and two-leaf BVHs (a single object, or a
+// ground plus one composite object) walked without a stack.
+template <bool kStats>
+__device__ __forceinline__ Info scene_distance_inl(const DevScene& S, F3 p, Ctx<kStats>& cx) {
+  cx.eval();
+  const DevBvhNode& root = S.bvh[S.bvh_root];
+  if (root.leaf >= 0) return eval_leaf(S, S.leaves[root.leaf], p, kInf, cx);
+  const DevBvhNode& L = S.bvh[root.lhs];
+  const DevBvhNode& R = S.bvh[root.rhs];
+  if (L.leaf < 0 || R.leaf < 0) return scene_distance_bvh(S, p, cx);
+  cx.box();
+  cx.box();
+  float ll = node_lb(p, L.bmin, L.bmax), rl = node_lb(p, R.bmin, R.bmax);
+  const bool lfirst = ll <= rl;
+  const DevLeaf& first = S.leaves[lfirst ? L.leaf : R.leaf];
+  const DevLeaf& second = S.leaves[lfirst ? R.leaf : L.leaf];
+  Info cur = eval_leaf(S, first, p, kInf, cx);
+  if ((lfirst ? rl : ll) <= cur.d) {
+    Info in = eval_leaf(S, second, p, cur.d, cx);
+    if (in.d < cur.d) cur = in;
+  }
+  return cur;
+}
+
+template <bool kStats>
+__device__ __noinline__ Info scene_distance(const DevScene& S, F3 p, Ctx<kStats>& cx) {
+  return scene_distance_inl(S, p, cx);
 }
 
 template <bool kStats>
@@ -472,6 +531,189 @@ __global__ void __launch_bounds__(128) march_depth_kernel(DevScene S, RayParams 
   }
 }
 
+// Primary ray of work item i (pixel_sample_offsets R:4838-4854, NDC map of
+// render_depth_tile R:3951-3955, generate_ray render_api.rs:132-144 and the
+// second normalisation of the tile loop).
+__device__ __forceinline__ bool item_ray(const RayParams& P, uint64_t i, F3* dir, size_t* out_idx) {
+  uint32_t px, py, s;
+  item_coords(P, i, &px, &py, &s);
+  if (px >= P.width || py >= P.height) return false;
+  float sx = (static_cast<float>(s % P.grid) + 0.5f) / static_cast<float>(P.grid);
+  float sy = (static_cast<float>(s / P.grid) + 0.5f) / static_cast<float>(P.grid);
+  float ndc_x = ((static_cast<float>(px) + sx) / static_cast<float>(P.width)) * 2.0f - 1.0f;
+  float ndc_y = 1.0f - ((static_cast<float>(py) + sy) / static_cast<float>(P.height)) * 2.0f;
+  ndc_x *= P.aspect;
+  F3 fwd = f3(P.fwd[0], P.fwd[1], P.fwd[2]), rt = f3(P.right[0], P.right[1], P.right[2]);
+  F3 up = f3(P.up[0], P.up[1], P.up[2]);
+  F3 d = ftd::normalize3(fwd + rt * (ndc_x * P.tan_fov) + up * (ndc_y * P.tan_fov));
+  *dir = ftd::normalize3(d);
+  *out_idx = (static_cast<size_t>(py) * P.width + px) * P.aa + s;
+  return true;
+}
+
+// Persistent march with per-lane state machines.
+//
+// Every loop iteration performs exactly one scene distance evaluation per
+// live lane, whatever the lane is doing: a march step (R:4100-4137), one of
+// the ten bisection steps (refine_hit_distance, R:4180-4200), one of the six
+// estimate_normal taps (R:4202-4215) or the final material lookup.  Lanes
+// whose ray finished pick up the next work item from a global counter once a
+// quarter of the warp is idle, so divergent march lengths do not leave lanes
+// idle for the rest of the warp's life.  The sequence of evaluation points of
+// each ray is exactly the reference's.
+enum Phase : int { kMarch = 0, kRefine = 1, kNormal = 2, kFinal = 3 };
+
+template <bool kStats>
+__global__ void __launch_bounds__(128) march_depth_persistent(DevScene S, RayParams P, float* __restrict__ t_out,
+                                                              uint8_t* __restrict__ mask_out,
+                                                              uint32_t* __restrict__ mat_out,
+                                                              float* __restrict__ normal_out,
+                                                              unsigned long long* __restrict__ stats,
+                                                              unsigned long long* __restrict__ next_item) {
+  const unsigned lane = threadIdx.x & 31u;
+  const F3 o = f3(P.origin[0], P.origin[1], P.origin[2]);
+  const float eps = P.eps;
+  const float scale = ftd::rclamp(P.step_scale, 0.05f, 1.0f);
+  const float min_step = fmaxf(eps * 0.5f, 1.0e-5f);
+  const float ne = fmaxf(eps * 4.0f, 1.0e-5f);
+  const bool want_normal = normal_out != nullptr;
+  Ctx<kStats> cx;
+  cx.c = Counters{0, 0, 0, 0, 0};
+
+  bool live = false;
+  bool queue_done = false;
+  size_t idx = 0;
+  F3 d = f3(0.0f, 0.0f, 0.0f), pos = f3(0.0f, 0.0f, 0.0f);
+  float traveled = 0.0f, prev = 0.0f, max_t = 0.0f, lo = 0.0f, hi = 0.0f;
+  float nx = 0.0f, ny = 0.0f, nz = 0.0f;  // estimate_normal differences
+  uint32_t steps = 0;
+  int phase = kMarch, k = 0;
+
+  for (;;) {
+    // Refill idle lanes when enough of the warp is idle (or all of it).
+    unsigned idle = __ballot_sync(0xffffffffu, !live);
+    if (!queue_done && (__popc(idle) >= 8 || idle == 0xffffffffu)) {
+      unsigned n = __popc(idle);
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(next_item, static_cast<unsigned long long>(n));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (base >= P.n_items) queue_done = true;
+      if (!live) {
+        unsigned rank = __popc(idle & ((1u << lane) - 1u));
+        uint64_t item = base + rank;
+        if (item < P.n_items && item_ray(P, item, &d, &idx)) {
+          float t0, t1;
+          bool inside = ray_aabb(o, d, S.smin, S.smax, &t0, &t1);
+          traveled = fmaxf(0.0f, fmaxf(t0, 0.0f));
+          max_t = fminf(P.max_dist, t1);
+          if (inside && P.max_steps > 0 && !(traveled > max_t)) {
+            live = true;
+            prev = traveled;
+            steps = 0;
+            phase = kMarch;
+          } else {
+            t_out[idx] = 0.0f;
+            mask_out[idx] = 0;
+            if (mat_out) mat_out[idx] = 0u;
+            if (normal_out) {
+              normal_out[3 * idx] = 0.0f;
+              normal_out[3 * idx + 1] = 0.0f;
+              normal_out[3 * idx + 2] = 0.0f;
+            }
+          }
+        }
+      }
+    }
+    if (__ballot_sync(0xffffffffu, live) == 0u) {
+      if (queue_done) break;
+      continue;
+    }
+    if (!live) continue;
+
+    // The point this lane evaluates in this iteration.
+    F3 q;
+    float mid = 0.0f;
+    if (phase == kMarch) {
+      q = o + d * traveled;
+      cx.step();
+    } else if (phase == kRefine) {
+      mid = 0.5f * (lo + hi);
+      q = o + d * mid;
+    } else if (phase == kNormal) {
+      float sgn = (k & 1) ? -ne : ne;
+      q = pos;
+      if (k < 2) q.x += sgn;
+      else if (k < 4) q.y += sgn;
+      else q.z += sgn;
+    } else {
+      q = pos;
+    }
+    Info info = scene_distance_inl(S, q, cx);
+
+    if (phase == kMarch) {
+      if (fabsf(info.d) < eps) {
+        phase = kRefine;
+        lo = prev;
+        hi = traveled;
+        k = 0;
+      } else {
+        prev = traveled;
+        traveled += fmaxf(fabsf(info.d) * scale, min_step);
+        ++steps;
+        if (steps >= P.max_steps || traveled > max_t) {  // miss
+          live = false;
+          t_out[idx] = 0.0f;
+          mask_out[idx] = 0;
+          if (mat_out) mat_out[idx] = 0u;
+          if (normal_out) {
+            normal_out[3 * idx] = 0.0f;
+            normal_out[3 * idx + 1] = 0.0f;
+            normal_out[3 * idx + 2] = 0.0f;
+          }
+        }
+      }
+    } else if (phase == kRefine) {
+      if (fabsf(info.d) < eps) hi = mid;
+      else lo = mid;
+      if (++k == 10) {
+        pos = o + d * hi;
+        phase = want_normal ? kNormal : kFinal;
+        k = 0;
+      }
+    } else if (phase == kNormal) {
+      // dx = d(p + e x) - d(p - e x), one subtraction as in the reference
+      if (k == 0) nx = info.d;
+      else if (k == 1) nx = nx - info.d;
+      else if (k == 2) ny = info.d;
+      else if (k == 3) ny = ny - info.d;
+      else if (k == 4) nz = info.d;
+      else nz = nz - info.d;
+      if (++k == 6) phase = kFinal;
+    } else {
+      live = false;
+      t_out[idx] = hi;
+      mask_out[idx] = 1;
+      if (mat_out) mat_out[idx] = info.mat;
+      if (normal_out) {
+        F3 nn = f3(nx, ny, nz);
+        F3 nr = ftd::len3(nn) > 1.0e-8f ? ftd::normalize3(nn) : f3(0.0f, 1.0f, 0.0f);
+        normal_out[3 * idx] = nr.x;
+        normal_out[3 * idx + 1] = nr.y;
+        normal_out[3 * idx + 2] = nr.z;
+      }
+    }
+  }
+  if (kStats) {
+    unsigned long long v[5] = {cx.c.evals, cx.c.prims, cx.c.boxes, cx.c.hook_instrs, cx.c.steps};
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+      unsigned long long x = v[j];
+      for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+      if (lane == 0 && x) atomicAdd(&stats[j], x);
+    }
+  }
+}
+
 // Depth preview pixels (render_depth_tile R:3931-3971, depth_preview_value
 // R:5215-5219, spectrum_to_rgb8 R:5221-5227).
 __global__ void depth_rgb8_kernel(const float* __restrict__ t, const uint8_t* __restrict__ mask, uint32_t n_pixels,
@@ -569,6 +811,7 @@ struct ft_scene {
   uint8_t* d_rgb = nullptr;
   size_t cap_items = 0, cap_pixels = 0;
   unsigned long long* d_stats = nullptr;
+  int persistent_blocks = 1;
   std::mutex mu;
 };
 
@@ -593,6 +836,8 @@ ft_status upload_scene(ft_scene* sc) {
       {im.ur_inner.data(), im.ur_inner.size() * sizeof(DevUrInner), 0},
       {im.programs.data(), im.programs.size() * sizeof(ft_program), 0},
       {im.instrs.data(), im.instrs.size() * sizeof(ft_instr), 0},
+      {im.ur_cell_offsets.data(), im.ur_cell_offsets.size() * sizeof(uint32_t), 0},
+      {im.ur_cell_prims.data(), im.ur_cell_prims.size() * sizeof(int32_t), 0},
   };
   size_t total = 0;
   for (Part& p : parts) {
@@ -618,10 +863,18 @@ ft_status upload_scene(ft_scene* sc) {
   d.ur_inner = reinterpret_cast<const DevUrInner*>(base + parts[8].off);
   d.programs = reinterpret_cast<const ft_program*>(base + parts[9].off);
   d.instrs = reinterpret_cast<const ft_instr*>(base + parts[10].off);
+  d.ur_cell_offsets = reinterpret_cast<const uint32_t*>(base + parts[11].off);
+  d.ur_cell_prims = reinterpret_cast<const int32_t*>(base + parts[12].off);
   d.bvh_root = im.bvh_root;
   std::memcpy(d.smin, im.scene_min, sizeof(d.smin));
   std::memcpy(d.smax, im.scene_max, sizeof(d.smax));
-  FT_CUDA_TRY(cudaMalloc(&sc->d_stats, 8 * sizeof(unsigned long long)), "cudaMalloc(stats)");
+  // [0, 8): statistics counters; [8]: work-item counter of the persistent march
+  FT_CUDA_TRY(cudaMalloc(&sc->d_stats, 16 * sizeof(unsigned long long)), "cudaMalloc(stats)");
+  int sms = 0, per_sm = 0;
+  FT_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, sc->device), "sm count");
+  FT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, march_depth_persistent<false>, 128, 0),
+              "occupancy");
+  sc->persistent_blocks = std::max(1, sms * std::max(per_sm, 1));
   return FT_OK;
 }
 
@@ -690,15 +943,16 @@ ft_status launch_depth(ft_scene* sc, const RayParams& P, cudaStream_t st, bool s
                        uint32_t* mat, float* normal) {
   uint64_t blocks = (P.n_items + 127) / 128;
   if (blocks > 0x7fffffffull) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "image too large");
+  unsigned grid = static_cast<unsigned>(std::min<uint64_t>(blocks, static_cast<uint64_t>(sc->persistent_blocks)));
+  unsigned long long* counter = sc->d_stats + 8;
   if (stats) {
-    FT_CUDA_TRY(cudaMemsetAsync(sc->d_stats, 0, 8 * sizeof(unsigned long long), st), "cudaMemsetAsync(stats)");
-    march_depth_kernel<true><<<static_cast<unsigned>(blocks), 128, 0, st>>>(sc->dev, P, t, mask, mat, normal,
-                                                                          sc->d_stats);
+    FT_CUDA_TRY(cudaMemsetAsync(sc->d_stats, 0, 16 * sizeof(unsigned long long), st), "cudaMemsetAsync(stats)");
+    march_depth_persistent<true><<<grid, 128, 0, st>>>(sc->dev, P, t, mask, mat, normal, sc->d_stats, counter);
   } else {
-    march_depth_kernel<false><<<static_cast<unsigned>(blocks), 128, 0, st>>>(sc->dev, P, t, mask, mat, normal,
-                                                                           nullptr);
+    FT_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st), "cudaMemsetAsync(counter)");
+    march_depth_persistent<false><<<grid, 128, 0, st>>>(sc->dev, P, t, mask, mat, normal, nullptr, counter);
   }
-  FT_CUDA_TRY(cudaGetLastError(), "march_depth_kernel launch");
+  FT_CUDA_TRY(cudaGetLastError(), "march_depth_persistent launch");
   return FT_OK;
 }
 
@@ -728,6 +982,38 @@ ft_status ft_scene_create(const ft_scene_desc* desc, ft_scene** out) {
   }
   *out = sc;
   ftcommon::clear_last_error();
+  return FT_OK;
+}
+
+ft_status ft_scene_build_info(const ft_scene_desc* desc, ft_build_info* info) {
+  if (!desc || !info) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "desc and info must be non-null");
+  ftgpu::SceneImage img;
+  std::string err;
+  auto t0 = std::chrono::steady_clock::now();
+  if (!ftgpu::build_scene_image(*desc, &img, &err)) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, err);
+  auto t1 = std::chrono::steady_clock::now();
+  std::memset(info, 0, sizeof(*info));
+  info->leaves = static_cast<uint32_t>(img.leaves.size());
+  for (const auto& l : img.leaves) {
+    info->primitive_leaves += l.kind == ftgpu::kLeafPrim;
+    info->generic_leaves += l.kind == ftgpu::kLeafGeneric;
+    info->union_round_leaves += l.kind == ftgpu::kLeafUrTree;
+  }
+  info->bvh_nodes = static_cast<uint32_t>(img.bvh.size());
+  if (!img.ur_cell_offsets.empty()) {
+    for (const auto& t : img.urtrees) {
+      if (t.dims[0] <= 0) continue;
+      uint64_t cells = static_cast<uint64_t>(t.dims[0]) * t.dims[1] * t.dims[2];
+      info->grid_cells += cells;
+      for (uint64_t c = 0; c < cells; ++c) {
+        uint32_t len = img.ur_cell_offsets[t.cell_first + c + 1] - img.ur_cell_offsets[t.cell_first + c];
+        info->grid_entries += len;
+        info->grid_max_list = std::max(info->grid_max_list, len);
+      }
+    }
+  }
+  info->generic_ops = static_cast<uint32_t>(img.gops.size());
+  info->build_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
   return FT_OK;
 }
 

@@ -13,6 +13,8 @@
 #include <functional>
 #include <limits>
 #include <numeric>
+#include <atomic>
+#include <thread>
 
 namespace ftgpu {
 namespace {
@@ -341,7 +343,9 @@ class Builder {
       *depth = std::max(*depth, dep);
       if (is_prim(n.kind)) {
         ++*nprims;
-        return true;
+        // Extruded polygons evaluate a distance to an edge line, which can lie
+        // below their box bound; such trees take the exact generic path.
+        return n.kind != FT_NODE_EXTRUDE_POLYGON;
       }
       if (n.kind != FT_NODE_UNION_ROUND || processed_r(n.f[0]) != *r) return false;
       return walk(n.a, dep + 1) && walk(n.b, dep + 1);
@@ -399,6 +403,121 @@ class Builder {
     return self;
   }
 
+  // Radius of a ball around the primitive's centre that lies inside the solid
+  // (its distance is at most |p - c| - radius everywhere), or a negative value
+  // when the shape has no such ball and the loose bound |p - c| + R applies.
+  float inscribed_radius(const HostNode& n) const {
+    switch (n.kind) {
+      case FT_NODE_SPHERE: return n.f[1] > 0.0f ? -1.0f : n.f[0];
+      case FT_NODE_BOX: return n.f[4] > 0.0f ? -1.0f : std::min(n.f[0], std::min(n.f[1], n.f[2]));
+      default: return -1.0f;
+    }
+  }
+
+  // Candidate grid over the tree's primitives.  For a cell C and primitive i,
+  //   lb(i, C) = distance between i's AABB and C  (<= d_i(p) for p in C, p
+  //              outside the AABB; the only case where lb > 0)
+  //   ub(i, C) = max_{p in C} |p - c_i| - rho_i  (>= d_i(p), rho_i the
+  //              inscribed radius; + R_i for shapes without one)
+  // and C lists {i : lb(i, C) < max(r, min_j ub(j, C))}.  A primitive left out
+  // has d >= r at every point of C (so it is inert in every union_round it
+  // feeds) and d >= the cell's nearest distance, so evaluating only the list
+  // gives the tree's exact value.  Cells are padded by a thousandth of their
+  // size against rounding in the device's cell lookup.
+  void build_ur_grid(HostUrTree& t) {
+    const int np = t.n_prims;
+    std::vector<Box> pb(np);
+    std::vector<float> cx(np), cy(np), cz(np), rho(np), rad(np);
+    Box all{};
+    for (int k = 0; k < np; ++k) {
+      const HostNode& n = img_->nodes[img_->ur_prims[t.prim_first + k]];
+      std::memcpy(pb[k].mn, n.bmin, sizeof(pb[k].mn));
+      std::memcpy(pb[k].mx, n.bmax, sizeof(pb[k].mx));
+      all = k ? box_union(all, pb[k]) : pb[k];
+      cx[k] = n.c[0];
+      cy[k] = n.c[1];
+      cz[k] = n.c[2];
+      rho[k] = inscribed_radius(n);
+      rad[k] = 0.5f * (n.bmax[0] - n.bmin[0]);
+    }
+    for (int a = 0; a < 3; ++a) {
+      all.mn[a] -= 2.0f * t.r;
+      all.mx[a] += 2.0f * t.r;
+    }
+    double ext[3] = {double(all.mx[0]) - all.mn[0], double(all.mx[1]) - all.mn[1], double(all.mx[2]) - all.mn[2]};
+    double target = std::min(262144.0, std::max(4096.0, 64.0 * np));
+    double cell = std::cbrt(ext[0] * ext[1] * ext[2] / target);
+    if (!(cell > 0.0) || !std::isfinite(cell)) return;
+    int dims[3];
+    for (int a = 0; a < 3; ++a) dims[a] = std::max(1, static_cast<int>(std::ceil(ext[a] / cell)));
+    if (static_cast<int64_t>(dims[0]) * dims[1] * dims[2] > 2 * 262144) return;
+    t.cell = static_cast<float>(cell);
+    t.inv_cell = 1.0f / t.cell;
+    std::memcpy(t.gmin, all.mn, sizeof(t.gmin));
+    std::memcpy(t.dims, dims, sizeof(dims));
+    t.cell_first = static_cast<int32_t>(img_->ur_cell_offsets.size());
+    const double pad = double(t.cell) * 1.0e-3;
+    // Cells are independent: z-slabs are built on worker threads and
+    // concatenated in cell order.  Each list is sorted by its box gap so the
+    // device meets the likely nearest primitive first and prunes the rest.
+    const int nz = dims[2];
+    std::vector<std::vector<uint32_t>> slab_offsets(nz);
+    std::vector<std::vector<int32_t>> slab_prims(nz);
+    auto work = [&](int z) {
+      std::vector<std::pair<double, int32_t>> cand;
+      cand.reserve(64);
+      auto& offs = slab_offsets[z];
+      auto& prims = slab_prims[z];
+      for (int y = 0; y < dims[1]; ++y)
+        for (int x = 0; x < dims[0]; ++x) {
+          double mn[3], mx[3];
+          int idx[3] = {x, y, z};
+          for (int a = 0; a < 3; ++a) {
+            mn[a] = double(t.gmin[a]) + double(idx[a]) * double(t.cell) - pad;
+            mx[a] = double(t.gmin[a]) + double(idx[a] + 1) * double(t.cell) + pad;
+          }
+          double min_ub = std::numeric_limits<double>::infinity();
+          for (int k = 0; k < np; ++k) {
+            double fx = std::max(std::fabs(double(cx[k]) - mn[0]), std::fabs(double(cx[k]) - mx[0]));
+            double fy = std::max(std::fabs(double(cy[k]) - mn[1]), std::fabs(double(cy[k]) - mx[1]));
+            double fz = std::max(std::fabs(double(cz[k]) - mn[2]), std::fabs(double(cz[k]) - mx[2]));
+            double far = std::sqrt(fx * fx + fy * fy + fz * fz);
+            double u = rho[k] >= 0.0f ? far - rho[k] : far + 2.0 * rad[k];
+            min_ub = std::min(min_ub, u);
+          }
+          // slack of 1e-5 keeps float rounding of the device-side bound on the safe side
+          double thr = std::max(double(t.r), min_ub) * (1.0 + 1e-5) + 1e-6;
+          double thr2 = thr * thr;
+          cand.clear();
+          for (int k = 0; k < np; ++k) {
+            double g2 = 0.0;
+            for (int a = 0; a < 3; ++a) {
+              double gap = std::max({0.0, double(pb[k].mn[a]) - mx[a], mn[a] - double(pb[k].mx[a])});
+              g2 += gap * gap;
+            }
+            if (g2 < thr2) cand.emplace_back(g2, k);
+          }
+          std::sort(cand.begin(), cand.end());
+          offs.push_back(static_cast<uint32_t>(prims.size()));
+          for (const auto& c : cand) prims.push_back(c.second);
+        }
+    };
+    unsigned nthreads = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    std::atomic<int> next{0};
+    std::vector<std::thread> pool;
+    for (unsigned i = 0; i < nthreads; ++i)
+      pool.emplace_back([&]() {
+        for (int z = next.fetch_add(1); z < nz; z = next.fetch_add(1)) work(z);
+      });
+    for (auto& th : pool) th.join();
+    for (int z = 0; z < nz; ++z) {
+      uint32_t base = static_cast<uint32_t>(img_->ur_cell_prims.size());
+      for (uint32_t o : slab_offsets[z]) img_->ur_cell_offsets.push_back(base + o);
+      img_->ur_cell_prims.insert(img_->ur_cell_prims.end(), slab_prims[z].begin(), slab_prims[z].end());
+    }
+    img_->ur_cell_offsets.push_back(static_cast<uint32_t>(img_->ur_cell_prims.size()));
+  }
+
   bool build_urtree(HostLeaf& leaf, float r, int depth) {
     HostUrTree t;
     std::memset(&t, 0, sizeof(t));
@@ -427,6 +546,7 @@ class Builder {
     std::vector<int32_t> pos(t.n_prims);
     std::iota(pos.begin(), pos.end(), 0);
     t.bvh_root = build_ur_bvh(pos, 0, pos.size(), t.prim_first);
+    build_ur_grid(t);
     if (!emit_program(leaf.node, &t.fallback_first, &t.fallback_count)) return false;
     leaf.kind = kLeafUrTree;
     leaf.first = static_cast<int32_t>(img_->urtrees.size());

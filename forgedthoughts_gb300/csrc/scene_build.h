@@ -72,6 +72,13 @@ struct HostUrTree {
   int32_t inner_root;   // into ur_inner
   int32_t depth;
   int32_t fallback_first, fallback_count;  // generic program of the whole tree
+  // Candidate grid: cell c lists every primitive that can be the nearest or
+  // lie within r of some point of c.  dims[0] == 0 disables the grid.
+  float gmin[3];
+  float cell, inv_cell;
+  int32_t dims[3];
+  int32_t cell_first;  // into ur_cell_offsets (dims product + 1 entries)
+  int32_t pad;
 };
 
 struct HostUrBvh {
@@ -96,6 +103,8 @@ struct SceneImage {
   std::vector<int32_t> ur_bvh_prims;
   std::vector<int32_t> ur_prims;
   std::vector<HostUrInner> ur_inner;
+  std::vector<uint32_t> ur_cell_offsets;  // per grid cell: begin into ur_cell_prims
+  std::vector<int32_t> ur_cell_prims;     // in-order primitive positions
   std::vector<ft_program> programs;
   std::vector<ft_instr> instrs;
   float scene_min[3], scene_max[3];

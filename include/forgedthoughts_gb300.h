@@ -289,6 +289,24 @@ void ft_scene_desc_free(ft_scene_desc* desc);
 ft_status ft_scene_create(const ft_scene_desc* desc, ft_scene** out);
 void ft_scene_destroy(ft_scene* scene);
 
+/* Host-only summary of the culling structures ft_scene_create would build for
+ * `desc` (no device needed): hard-union leaves by evaluation kind, the
+ * union_round trees and their candidate grids. */
+typedef struct ft_build_info {
+  uint32_t leaves;
+  uint32_t primitive_leaves;
+  uint32_t generic_leaves;
+  uint32_t union_round_leaves;
+  uint32_t bvh_nodes;
+  uint64_t grid_cells;
+  uint64_t grid_entries;      /* sum of candidate-list lengths */
+  uint32_t grid_max_list;
+  uint32_t generic_ops;
+  double build_ms;            /* host time to build the structures */
+} ft_build_info;
+
+ft_status ft_scene_build_info(const ft_scene_desc* desc, ft_build_info* info);
+
 /* Bytes of scene data the last ft_scene_create copied host -> device. */
 ft_status ft_scene_device_bytes(const ft_scene* scene, uint64_t* bytes);
 
