@@ -67,7 +67,9 @@ class MaterialC(ctypes.Structure):
                 ("metallic", ctypes.c_float), ("ior", ctypes.c_float), ("transmission", ctypes.c_float),
                 ("emission_strength", ctypes.c_float), ("emission_color", ctypes.c_float * 3),
                 ("medium_ior", ctypes.c_float), ("medium_absorption", ctypes.c_float * 3),
-                ("medium_density", ctypes.c_float)]
+                ("medium_density", ctypes.c_float), ("specular", ctypes.c_float),
+                ("specular_weight", ctypes.c_float), ("specular_color", ctypes.c_float * 3),
+                ("clearcoat", ctypes.c_float), ("clearcoat_roughness", ctypes.c_float)]
 
 
 class CameraC(ctypes.Structure):

@@ -161,6 +161,12 @@ ft_material material_defaults(int kind) {
   m.color[0] = m.color[1] = m.color[2] = 0.8f;
   m.roughness = 0.5f;
   m.ior = 1.5f;
+  // MaterialParams constructors (crates/forgedthoughts/src/materials/mod.rs:90-212)
+  m.specular = 0.5f;
+  m.specular_weight = 1.0f;
+  m.specular_color[0] = m.specular_color[1] = m.specular_color[2] = 1.0f;
+  m.clearcoat = 0.0f;
+  m.clearcoat_roughness = 0.1f;
   return m;
 }
 
@@ -652,6 +658,7 @@ class Lowerer {
       set_color(m, v3(0.9f, 0.9f, 0.9f));
       m.roughness = clampf(number_or(o, {"roughness"}, 0.1f), 0.0f, 1.0f);
       m.metallic = 1.0f;
+      m.specular = 1.0f;
       emission(m);
       return m;
     }
@@ -674,6 +681,14 @@ class Lowerer {
     m.ior = clampf(number_or(o, {"ior", "specular_ior"}, 1.5f), 1.0f, 3.0f);
     m.transmission = clampf(number_or(o, {"transmission", "transmission_weight"}, 0.0f), 0.0f, 1.0f);
     m.thin_walled = number_or(o, {"thin_walled"}, 0.0f) >= 0.5f;
+    m.specular = clampf(number_or(o, {"specular"}, 0.5f), 0.0f, 1.0f);
+    m.specular_weight = clampf(number_or(o, {"specular_weight"}, 1.0f), 0.0f, 1.0f);
+    V3 sc;
+    if (read_spectrum(o, "specular_color", &sc)) {
+      m.specular_color[0] = sc.x; m.specular_color[1] = sc.y; m.specular_color[2] = sc.z;
+    }
+    m.clearcoat = clampf(number_or(o, {"clearcoat"}, 0.0f), 0.0f, 1.0f);
+    m.clearcoat_roughness = clampf(number_or(o, {"clearcoat_roughness"}, 0.1f), 0.0f, 1.0f);
     emission(m);
     return m;
   }

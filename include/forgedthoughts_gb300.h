@@ -228,6 +228,11 @@ typedef struct ft_material {
   float medium_ior;
   float medium_absorption[3];
   float medium_density;
+  float specular;
+  float specular_weight;
+  float specular_color[3];
+  float clearcoat;
+  float clearcoat_roughness;
 } ft_material;
 
 typedef struct ft_camera {

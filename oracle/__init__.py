@@ -32,6 +32,10 @@ def lib() -> ctypes.CDLL:
         h.oracle_distance.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, ctypes.c_size_t, vp, vp, vp]
         h.oracle_eval_program.restype = ctypes.c_int
         h.oracle_eval_program.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, ctypes.c_size_t, vp]
+        h.oracle_render_trace.restype = ctypes.c_int
+        h.oracle_render_trace.argtypes = [vp, vp, ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int,
+                                          ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, vp, vp,
+                                          ctypes.POINTER(ctypes.c_uint64)]
         h.oracle_last_error.restype = ctypes.c_char_p
         _lib = h
     return _lib
@@ -72,6 +76,24 @@ def render_depth(state, options, accel: int, aa: int = 1, precision: int = 32, t
     if normals:
         return t, mask, mat, rgb, int(evals.value), nrm
     return t, mask, mat, rgb, int(evals.value)
+
+
+def render_trace(state, options, accel: int, aa: int = 1, max_depth: int = 8, precision: int = 32,
+                 threads: int = 0, rows: tuple[int, int, int] | None = None):
+    """Oracle Whitted trace.  Returns (rgb linear float (H, W, 3), rgb8, evals)."""
+    from forgedthoughts_gb300 import _native
+
+    h, w = int(options.height), int(options.width)
+    rgb = np.zeros((h, w, 3), np.float32)
+    rgb8 = np.zeros((h, w, 3), np.uint8)
+    opts = options.to_c() if hasattr(options, "to_c") else options
+    assert isinstance(opts, _native.RenderOptionsC)
+    r0, r1, rs = rows if rows is not None else (0, h, 1)
+    evals = ctypes.c_uint64(0)
+    _check(lib().oracle_render_trace(_vp(state.desc_ptr), ctypes.cast(ctypes.pointer(opts), ctypes.c_void_p),
+                                     int(accel), max(int(aa), 1), int(max_depth), int(precision), int(threads), r0,
+                                     r1, rs, _arr(rgb), _arr(rgb8), ctypes.byref(evals)))
+    return rgb, rgb8, int(evals.value)
 
 
 def distance(state, points: np.ndarray, accel: int = 1, precision: int = 32):

@@ -742,6 +742,25 @@ struct Accel {
   }
 
   R distance(V<R> p) const { return distance_info(p).d; }
+
+  // Accelerator::lower_bound (R:1040-1042, R:1078-1084, R:1118-1124, R:924-963)
+  R lower_bound(V<R> p) const {
+    int root = scene.desc().root;
+    if (mode == FT_ACCEL_NAIVE) return scene.lower_bound(root, p);
+    if (mode == FT_ACCEL_BVH) {
+      R best = std::numeric_limits<R>::infinity();
+      R out;
+      if (bvh_root >= 0 && bvh_lb(bvh_root, p, best, out)) return out;
+      return scene.lower_bound(root, p);
+    }
+    if (!has_grid) return scene.lower_bound(root, p);
+    R best = std::numeric_limits<R>::infinity();
+    grid_walk(p, best, [&](size_t li) {
+      R lb = point_aabb_lb(p, leaves[li].bounds);
+      if (lb < best) best = lb;
+    });
+    return best;
+  }
 };
 
 // ------------------------------------------------------------ march
@@ -948,6 +967,755 @@ int render_depth(const ft_scene_desc* desc, const ft_render_options* options, in
   return 0;
 }
 
+// ============================================================ Whitted trace
+// Restates crates/forgedthoughts/src/renderer/ray.rs:3-222 (trace_ray_recursive,
+// trace_hit_with_material) with the shading helpers of renderer.rs, the
+// materials of materials/{mod,lambert,metal,dielectric,standard}.rs and the
+// lights of render_api.rs.  Dynamic material hooks and rough-dielectric lobes
+// (roughness > 0.06 on transmissive materials) are not restated.
+
+template <class R>
+struct Sp {
+  R r, g, b;
+};
+template <class R> Sp<R> sp(R r, R g, R b) { return Sp<R>{r, g, b}; }
+template <class R> Sp<R> operator+(Sp<R> a, Sp<R> b) { return sp(a.r + b.r, a.g + b.g, a.b + b.b); }
+template <class R> Sp<R> operator*(Sp<R> a, Sp<R> b) { return sp(a.r * b.r, a.g * b.g, a.b * b.b); }
+template <class R> Sp<R> scale(Sp<R> a, R s) { return sp(a.r * s, a.g * s, a.b * s); }
+template <class R> Sp<R> black() { return sp(R(0), R(0), R(0)); }
+// lerp_spectrum (R:5205-5213): clamped t, a*(1-t) + b*t
+template <class R> Sp<R> lerp_sp(Sp<R> a, Sp<R> b, R t) {
+  R tt = rclamp(t, R(0), R(1));
+  return sp(a.r * (R(1) - tt) + b.r * tt, a.g * (R(1) - tt) + b.g * tt, a.b * (R(1) - tt) + b.b * tt);
+}
+
+enum Model { kStandard = 0, kLambert = 1, kMetal = 2, kDielectric = 3, kBlend = 4 };
+
+template <class R>
+struct Params {  // MaterialParams (materials/mod.rs:66-86), render-relevant fields
+  Sp<R> color;
+  R roughness, metallic, specular, specular_weight;
+  Sp<R> specular_color;
+  R ior, clearcoat, clearcoat_roughness, transmission;
+  bool thin_walled;
+  Sp<R> emission_color;
+  R emission_strength;
+};
+
+template <class R>
+struct Mat {  // Material enum incl. Blend (materials/mod.rs:214-230)
+  int kind = kStandard;  // Model
+  Params<R> p;           // Standard/Lambert/Metal/Dielectric params, or blend's a
+  int b_model = 0, a_model = 0;
+  Params<R> pb;
+  R t = 0;
+};
+
+template <class R> Params<R> params_from(const ft_material& m) {
+  Params<R> p;
+  p.color = sp(R(m.color[0]), R(m.color[1]), R(m.color[2]));
+  p.roughness = R(m.roughness);
+  p.metallic = R(m.metallic);
+  p.specular = R(m.specular);
+  p.specular_weight = R(m.specular_weight);
+  p.specular_color = sp(R(m.specular_color[0]), R(m.specular_color[1]), R(m.specular_color[2]));
+  p.ior = R(m.ior);
+  p.clearcoat = R(m.clearcoat);
+  p.clearcoat_roughness = R(m.clearcoat_roughness);
+  p.transmission = R(m.transmission);
+  p.thin_walled = m.thin_walled != 0;
+  p.emission_color = sp(R(m.emission_color[0]), R(m.emission_color[1]), R(m.emission_color[2]));
+  p.emission_strength = R(m.emission_strength);
+  return p;
+}
+
+// material_for_id (R:6895-6900)
+template <class R> Mat<R> material_for_id(const ft_scene_desc& d, uint32_t id) {
+  Mat<R> m;
+  if (d.n_materials == 0) {
+    m.kind = kStandard;
+    ft_material dm;
+    std::memset(&dm, 0, sizeof(dm));
+    dm.color[0] = dm.color[1] = dm.color[2] = 0.8f;
+    dm.roughness = 0.5f; dm.ior = 1.5f; dm.specular = 0.5f; dm.specular_weight = 1.0f;
+    dm.specular_color[0] = dm.specular_color[1] = dm.specular_color[2] = 1.0f; dm.clearcoat_roughness = 0.1f;
+    m.p = params_from<R>(dm);
+    return m;
+  }
+  const ft_material& fm = d.materials[id < d.n_materials ? id : 0];
+  m.kind = fm.kind;
+  m.p = params_from<R>(fm);
+  return m;
+}
+
+template <class R> int dominant_model(const Mat<R>& m) {
+  if (m.kind != kBlend) return m.kind;
+  return m.t < R(0.5) ? m.a_model : m.b_model;
+}
+template <class R> Params<R> dominant_params(const Mat<R>& m) {
+  if (m.kind != kBlend) return m.p;
+  return m.t < R(0.5) ? m.p : m.pb;
+}
+
+// blend_params / blend_materials (R:7602-7651)
+template <class R> Params<R> blend_params(Params<R> a, const Params<R>& b, R t) {
+  a.color = lerp_sp(a.color, b.color, t);
+  a.roughness = a.roughness + (b.roughness - a.roughness) * t;
+  a.metallic = a.metallic + (b.metallic - a.metallic) * t;
+  a.specular = a.specular + (b.specular - a.specular) * t;
+  a.specular_weight = a.specular_weight + (b.specular_weight - a.specular_weight) * t;
+  a.specular_color = lerp_sp(a.specular_color, b.specular_color, t);
+  a.ior = a.ior + (b.ior - a.ior) * t;
+  a.clearcoat = a.clearcoat + (b.clearcoat - a.clearcoat) * t;
+  a.clearcoat_roughness = a.clearcoat_roughness + (b.clearcoat_roughness - a.clearcoat_roughness) * t;
+  a.transmission = a.transmission + (b.transmission - a.transmission) * t;
+  a.thin_walled = t < R(0.5) ? a.thin_walled : b.thin_walled;
+  a.emission_color = lerp_sp(a.emission_color, b.emission_color, t);
+  a.emission_strength = a.emission_strength + (b.emission_strength - a.emission_strength) * t;
+  return a;
+}
+template <class R> Mat<R> blend_materials(const Mat<R>& a, const Mat<R>& b, R t) {
+  if (a.kind != kBlend && a.kind == b.kind) {
+    Mat<R> m;
+    m.kind = a.kind;
+    m.p = blend_params(a.p, b.p, t);
+    return m;
+  }
+  Mat<R> m;
+  m.kind = kBlend;
+  m.a_model = dominant_model(a);
+  m.p = dominant_params(a);
+  m.b_model = dominant_model(b);
+  m.pb = dominant_params(b);
+  m.t = rclamp(t, R(0), R(1));
+  return m;
+}
+
+// Material::emission (materials/mod.rs:284-296)
+template <class R> Sp<R> emission(const Mat<R>& m) {
+  auto e = [](const Params<R>& p) { return scale(p.emission_color, rmax(p.emission_strength, R(0))); };
+  if (m.kind != kBlend) return e(m.p);
+  return lerp_sp(e(m.p), e(m.pb), m.t);
+}
+
+template <class R> R pi_() { return R(3.14159265358979323846); }
+
+// metal.rs:7-20, 84-102
+template <class R> R ggx_d(R ndoth, R alpha) {
+  R a2 = alpha * alpha, n2 = ndoth * ndoth;
+  R denom = rmax(n2 * (a2 - R(1)) + R(1), R(1.0e-5));
+  return a2 / (pi_<R>() * denom * denom);
+}
+template <class R> R smith_g1(R ndotx, R alpha) {
+  R k = (alpha * alpha) * R(0.5);
+  return ndotx / rmax(ndotx * (R(1) - k) + k, R(1.0e-5));
+}
+template <class R> Sp<R> fresnel_schlick_sp(Sp<R> f0, R c) {
+  R x = R(1) - rclamp(c, R(0), R(1));
+  R m = x * x * x * x * x;
+  return f0 + scale(sp(R(1), R(1), R(1)), m) + scale(f0, -m);
+}
+template <class R> Sp<R> metal_eval(const Params<R>& m, V<R> n, V<R> wi, V<R> wo) {
+  R ndotl = rmax(dot(n, wi), R(0)), ndotv = rmax(dot(n, wo), R(0));
+  if (ndotl <= R(0) || ndotv <= R(0)) return black<R>();
+  V<R> h = normalize(wi + wo);
+  R ndoth = rmax(dot(n, h), R(0)), vdoth = rmax(dot(wo, h), R(0));
+  R rr = rclamp(m.roughness, R(0.02), R(1));
+  R alpha = rr * rr;
+  R d = ggx_d(ndoth, alpha);
+  R g = smith_g1(ndotl, alpha) * smith_g1(ndotv, alpha);
+  Sp<R> f = fresnel_schlick_sp(m.color, vdoth);
+  return scale(f, (d * g) / rmax(R(4) * ndotl * ndotv, R(1.0e-5)));
+}
+// lambert.rs:7-13
+template <class R> Sp<R> lambert_eval(const Params<R>& m, V<R> n, V<R> wi) {
+  if (dot(n, wi) <= R(0)) return black<R>();
+  return scale(m.color, R(1) / pi_<R>());
+}
+template <class R> R f0_from_ior(R ior) {
+  R i = rmax(ior, R(1.0e-3));
+  R r = (i - R(1)) / (i + R(1));
+  return r * r;
+}
+// standard.rs:6-43, 170-183
+template <class R> Sp<R> standard_eval(const Params<R>& m, V<R> n, V<R> wi, V<R> wo) {
+  R ndotl = rmax(dot(n, wi), R(0)), ndotv = rmax(dot(n, wo), R(0));
+  if (ndotl <= R(0) || ndotv <= R(0)) return black<R>();
+  R metallic = rclamp(m.metallic, R(0), R(1));
+  R transmission = rclamp(m.transmission, R(0), R(1));
+  R clearcoat = rclamp(m.clearcoat, R(0), R(1));
+  R cx = rclamp(R(1) - rclamp(ndotv, R(0), R(1)), R(0), R(1));
+  R x2 = cx * cx;
+  R schlick_w = x2 * x2 * cx;
+  R coat_cover = rclamp(clearcoat * (R(0.2) + R(0.8) * schlick_w) * R(0.65), R(0), R(0.95));
+  R base_kd = rclamp((R(1) - metallic) * (R(1) - transmission), R(0), R(1)) * (R(1) - coat_cover);
+  Sp<R> diffuse = scale(m.color, base_kd / pi_<R>());
+  R f0d = rclamp(f0_from_ior(m.ior), R(0), R(1));
+  Sp<R> base_f0 = scale(sp(f0d, f0d, f0d), rclamp(m.specular, R(0), R(1)) * rclamp(m.specular_weight, R(0), R(1))) *
+                  m.specular_color;
+  // standard.rs lerp_spectrum: a.scale(1 - t) + b.scale(t), unclamped
+  Sp<R> spec_f0 = scale(base_f0, R(1) - metallic) + scale(m.color, metallic);
+  Params<R> sparams = m;
+  sparams.color = spec_f0;
+  Sp<R> specular = scale(metal_eval(sparams, n, wi, wo), R(1) - coat_cover * R(0.85));
+  Sp<R> cc = black<R>();
+  if (clearcoat > R(1.0e-5)) {
+    Params<R> cp = m;
+    cp.color = sp(R(1), R(1), R(1));
+    cp.roughness = rclamp(m.clearcoat_roughness, R(0.02), R(1));
+    cc = scale(metal_eval(cp, n, wi, wo), clearcoat * R(0.18));
+  }
+  return diffuse + specular + cc;
+}
+template <class R> Sp<R> model_eval(int model, const Params<R>& p, V<R> n, V<R> wi, V<R> wo) {
+  switch (model) {
+    case kStandard: return standard_eval(p, n, wi, wo);
+    case kLambert: return lambert_eval(p, n, wi);
+    case kMetal: return metal_eval(p, n, wi, wo);
+    default: return black<R>();  // dielectric.rs:5-7
+  }
+}
+// Material::eval (materials/mod.rs:298-310)
+template <class R> Sp<R> mat_eval(const Mat<R>& m, V<R> n, V<R> wi, V<R> wo) {
+  if (m.kind != kBlend) return model_eval(m.kind, m.p, n, wi, wo);
+  return lerp_sp(model_eval(m.a_model, m.p, n, wi, wo), model_eval(m.b_model, m.pb, n, wi, wo), m.t);
+}
+
+template <class R> R smoothstepf(R e0, R e1, R x) {  // R:7538-7541
+  R t = rclamp((x - e0) / rmax(e1 - e0, R(1.0e-6)), R(0), R(1));
+  return t * t * (R(3) - R(2) * t);
+}
+
+template <class R>
+struct Medium {  // MediumState (R:4372-4387)
+  R ior;
+  Sp<R> absorption;
+  R density;
+  static Medium air() { return Medium{R(1), sp(R(1), R(1), R(1)), R(0)}; }
+};
+
+template <class R>
+class Tracer {
+ public:
+  Tracer(const Scene<R>& s, const Accel<R>& a, const Opts& op, uint32_t max_depth)
+      : S(s), A(a), op_(op), max_depth_(std::max(max_depth, 1u)) {}
+
+  // trace_ray_recursive (ray.rs:3-39)
+  Sp<R> trace(V<R> o, V<R> d, Medium<R> med, uint32_t depth, uint64_t* evals) const {
+    if (depth >= max_depth_) return black<R>();
+    R min_t = depth == 0 ? R(0) : R(op_.epsilon) * R(2);
+    Hit<R> h;
+    if (!raymarch(A, o, d, op_, min_t, R(op_.max_dist), &h, evals)) {
+      return attenuate(environment(d), med, R(op_.max_dist));
+    }
+    V<R> view = normalize(d * R(-1));
+    Mat<R> ma, mb;
+    R t;
+    int root = S.desc().root;
+    if (split_material(root, h.pos, &ma, &mb, &t)) {
+      Sp<R> a = trace_hit(h, d, med, depth, ma, evals);
+      Sp<R> b = trace_hit(h, d, med, depth, mb, evals);
+      return lerp_sp(a, b, t);
+    }
+    Mat<R> m;
+    if (!material_from_node(root, h.pos, &m)) m = material_for_id<R>(S.desc(), h.mat);
+    (void)view;
+    return trace_hit(h, d, med, depth, m, evals);
+  }
+
+ private:
+  const Scene<R>& S;
+  const Accel<R>& A;
+  Opts op_;
+  uint32_t max_depth_;
+
+  Sp<R> env_radiance() const {  // R:4318-4326 over path lights
+    Sp<R> s = black<R>();
+    const ft_scene_desc& d = S.desc();
+    bool any = false;
+    for (uint32_t i = 0; i < d.n_lights; ++i)
+      if (d.lights[i].kind == FT_LIGHT_ENV) {
+        s = s + sp(R(d.lights[i].intensity[0]), R(d.lights[i].intensity[1]), R(d.lights[i].intensity[2]));
+        any = true;
+      }
+    (void)any;
+    return s;
+  }
+
+  // environment_color (R:4328-4333) with the env_radiance fallback
+  Sp<R> environment(V<R> dir) const {
+    const ft_scene_desc& d = S.desc();
+    if (d.environment_program >= 0) {
+      V<R> out;
+      S.run_program(d.environment_program, &dir, &out);
+      return sp(out.x, out.y, out.z);
+    }
+    return env_radiance();
+  }
+
+  static Sp<R> attenuate(Sp<R> c, const Medium<R>& m, R dist) {  // R:5109-5123
+    if (m.density <= R(0) || dist <= R(0)) return c;
+    R e = m.density * rmax(dist, R(0));
+    return c * sp(std::pow(rclamp(m.absorption.r, R(0), R(1)), e), std::pow(rclamp(m.absorption.g, R(0), R(1)), e),
+                  std::pow(rclamp(m.absorption.b, R(0), R(1)), e));
+  }
+
+  // estimate_node_normal (R:4554-4570)
+  V<R> node_normal(int idx, V<R> p, R eps) const {
+    R e = rmax(eps, R(1.0e-5));
+    V<R> k1 = mk(R(1), R(-1), R(-1)), k2 = mk(R(-1), R(-1), R(1)), k3 = mk(R(-1), R(1), R(-1)),
+         k4 = mk(R(1), R(1), R(1));
+    V<R> n = k1 * S.info(idx, p + k1 * e).d + k2 * S.info(idx, p + k2 * e).d + k3 * S.info(idx, p + k3 * e).d +
+             k4 * S.info(idx, p + k4 * e).d;
+    return len(n) > R(1.0e-6) ? normalize(n) : mk(R(0), R(1), R(0));
+  }
+
+  static bool blend_kind(int k, bool* diff, R* radius, const ft_node& n) {
+    *diff = false;
+    switch (k) {
+      case FT_NODE_UNION_ROUND: case FT_NODE_UNION_CHAMFER: case FT_NODE_UNION_SOFT: case FT_NODE_INTERSECT_ROUND:
+      case FT_NODE_INTERSECT_CHAMFER: case FT_NODE_UNION_COLUMNS: case FT_NODE_UNION_STAIRS:
+      case FT_NODE_INTERSECT_COLUMNS: case FT_NODE_INTERSECT_STAIRS:
+        *radius = R(n.f[0]);
+        return true;
+      case FT_NODE_DIFF_ROUND: case FT_NODE_DIFF_CHAMFER: case FT_NODE_DIFF_COLUMNS: case FT_NODE_DIFF_STAIRS:
+      case FT_NODE_PIPE: case FT_NODE_ENGRAVE:
+        *diff = true;
+        *radius = R(n.f[0]);
+        return true;
+      case FT_NODE_GROOVE: case FT_NODE_TONGUE:
+        *diff = true;
+        *radius = rmax(R(n.f[0]), R(n.f[1]));
+        return true;
+      default: return false;
+    }
+  }
+
+  R blend_t(const ft_node& n, V<R> p, bool diff, R radius) const {
+    Info<R> l = S.info(n.a, p), r = S.info(n.b, p);
+    R k = rmax(std::fabs(radius), R(1.0e-6));
+    if (diff) return smoothstepf(R(0), R(1), R(0.5) + R(0.5) * (((-r.d) - l.d) / k));
+    return smoothstepf(R(0), R(1), R(0.5) + R(0.5) * ((l.d - r.d) / k));
+  }
+
+  // resolve_surface_normal_from_node (R:4462-4527) / blend_surface_normals (R:4529-4552)
+  bool surface_normal(int idx, V<R> p, R eps, V<R>* out) const {
+    const ft_node& n = S.node(idx);
+    if (n.kind <= FT_NODE_NOISE) {  // primitives and modifiers
+      *out = node_normal(idx, p, eps);
+      return true;
+    }
+    switch (n.kind) {
+      case FT_NODE_UNION: {
+        Info<R> l = S.info(n.a, p), r = S.info(n.b, p);
+        return surface_normal(l.d <= r.d ? n.a : n.b, p, eps, out);
+      }
+      case FT_NODE_INTERSECT: {
+        Info<R> l = S.info(n.a, p), r = S.info(n.b, p);
+        return surface_normal(l.d >= r.d ? n.a : n.b, p, eps, out);
+      }
+      case FT_NODE_SUBTRACT: {
+        Info<R> l = S.info(n.a, p), r = S.info(n.b, p);
+        if (l.d >= -r.d) return surface_normal(n.a, p, eps, out);
+        if (!surface_normal(n.b, p, eps, out)) return false;
+        *out = *out * R(-1);
+        return true;
+      }
+      case FT_NODE_SLICE:
+      case FT_NODE_SMOOTH: return surface_normal(n.a, p, eps, out);
+      default: break;
+    }
+    bool diff;
+    R radius;
+    blend_kind(n.kind, &diff, &radius, n);
+    Info<R> l = S.info(n.a, p), r = S.info(n.b, p);
+    (void)l;
+    (void)r;
+    V<R> left, right;
+    if (!surface_normal(n.a, p, eps, &left) || !surface_normal(n.b, p, eps, &right)) return false;
+    R t = blend_t(n, p, diff, radius);
+    if (diff) right = right * R(-1);
+    V<R> m = left * (R(1) - t) + right * t;
+    if (len(m) > R(1.0e-6)) *out = normalize(m);
+    else *out = t < R(0.5) ? left : right;
+    return true;
+  }
+
+  // resolve_material_from_node (R:6945-7050) / blend_node_materials (R:7093-7113)
+  bool material_from_node(int idx, V<R> p, Mat<R>* out) const {
+    const ft_node& n = S.node(idx);
+    if (n.kind <= FT_NODE_EXTRUDE_POLYGON) {
+      *out = material_for_id<R>(S.desc(), n.material_id);
+      return true;
+    }
+    switch (n.kind) {
+      case FT_NODE_DOMAIN: case FT_NODE_DISTANCE_POST: case FT_NODE_NOISE: case FT_NODE_SLICE: case FT_NODE_SMOOTH:
+        return material_from_node(n.a, p, out);
+      case FT_NODE_UNION: {
+        Info<R> l = S.info(n.a, p), r = S.info(n.b, p);
+        return material_from_node(l.d <= r.d ? n.a : n.b, p, out);
+      }
+      case FT_NODE_INTERSECT: {
+        Info<R> l = S.info(n.a, p), r = S.info(n.b, p);
+        return material_from_node(l.d >= r.d ? n.a : n.b, p, out);
+      }
+      case FT_NODE_SUBTRACT: {
+        Info<R> l = S.info(n.a, p), r = S.info(n.b, p);
+        return material_from_node(l.d >= -r.d ? n.a : n.b, p, out);
+      }
+      default: break;
+    }
+    bool diff;
+    R radius;
+    blend_kind(n.kind, &diff, &radius, n);
+    Mat<R> left, right;
+    if (!material_from_node(n.a, p, &left) || !material_from_node(n.b, p, &right)) return false;
+    *out = blend_materials(left, right, blend_t(n, p, diff, radius));
+    return true;
+  }
+
+  // resolve_split_material_from_node (R:7052-7091)
+  bool split_material(int idx, V<R> p, Mat<R>* a, Mat<R>* b, R* t) const {
+    const ft_node& n = S.node(idx);
+    switch (n.kind) {
+      case FT_NODE_UNION: {
+        Info<R> l = S.info(n.a, p), r = S.info(n.b, p);
+        return split_material(l.d <= r.d ? n.a : n.b, p, a, b, t);
+      }
+      case FT_NODE_INTERSECT: {
+        Info<R> l = S.info(n.a, p), r = S.info(n.b, p);
+        return split_material(l.d >= r.d ? n.a : n.b, p, a, b, t);
+      }
+      case FT_NODE_SUBTRACT: {
+        Info<R> l = S.info(n.a, p), r = S.info(n.b, p);
+        return split_material(l.d >= -r.d ? n.a : n.b, p, a, b, t);
+      }
+      case FT_NODE_SMOOTH:
+      case FT_NODE_NOISE: return split_material(n.a, p, a, b, t);
+      default: break;
+    }
+    bool diff;
+    R radius;
+    if (!blend_kind(n.kind, &diff, &radius, n)) return false;
+    if (!material_from_node(n.a, p, a) || !material_from_node(n.b, p, b)) return false;
+    *t = blend_t(n, p, diff, radius);
+    return true;
+  }
+
+  // offset_ray_origin (R:5067-5078)
+  static V<R> offset_origin(V<R> pos, V<R> gn, V<R> dir, R eps) {
+    V<R> n = len(gn) > R(1.0e-8) ? normalize(gn) : normalize(dir);
+    R sign = dot(dir, n) >= R(0) ? R(1) : R(-1);
+    V<R> no = n * (sign * rmax(eps * R(16), R(2.0e-4)));
+    R step = rmax(eps * R(8), R(1.0e-4));
+    return pos + no + normalize(dir) * step;
+  }
+
+  // shadow_visibility (R:4706-4733)
+  R shadow(V<R> o, V<R> d, R max_t, uint64_t* evals) const {
+    R eps = R(op_.epsilon);
+    R t = eps * R(2);
+    R vis = R(1);
+    for (int i = 0; i < 80; ++i) {
+      if (t >= max_t) return rclamp(vis, R(0), R(1));
+      V<R> p = o + d * t;
+      R lower = std::fabs(A.lower_bound(p));
+      R h;
+      if (lower > rmax(eps * R(8), R(0.02))) {
+        h = lower;
+      } else {
+        h = std::fabs(A.distance(p));
+        ++*evals;
+      }
+      if (h < eps * R(4)) return R(0);
+      vis = rmin(vis, rclamp(R(10) * h / t, R(0), R(1)));
+      t += rmax(h, eps * R(2));
+    }
+    return rclamp(vis, R(0), R(1));
+  }
+
+  // Light::sample_li_indexed (render_api.rs:172-259)
+  void sample_light(const ft_light& L, V<R> p, uint32_t idx, uint32_t count, V<R>* wi, Sp<R>* rad, R* dist) const {
+    Sp<R> inten = sp(R(L.intensity[0]), R(L.intensity[1]), R(L.intensity[2]));
+    V<R> lp = mk(R(L.position[0]), R(L.position[1]), R(L.position[2]));
+    if (L.kind == FT_LIGHT_ENV) {
+      *wi = mk(R(0), R(1), R(0));
+      *rad = inten;
+      *dist = std::numeric_limits<R>::infinity();
+      return;
+    }
+    V<R> target = lp;
+    if (L.kind == FT_LIGHT_SPHERE && R(L.radius) > R(1.0e-5)) {
+      V<R> nrm = normalize(p - lp);
+      V<R> up = std::fabs(nrm.y) < R(0.99) ? mk(R(0), R(1), R(0)) : mk(R(1), R(0), R(0));
+      V<R> tangent = normalize(cross(nrm, up));
+      V<R> bit = normalize(cross(tangent, nrm));
+      uint32_t n = std::max(count, 1u);
+      R u = (R(idx) + R(0.5)) / R(n);
+      uint32_t bits = idx;
+      bits = (bits >> 16) | (bits << 16);
+      bits = ((bits & 0x55555555u) << 1) | ((bits & 0xAAAAAAAAu) >> 1);
+      bits = ((bits & 0x33333333u) << 2) | ((bits & 0xCCCCCCCCu) >> 2);
+      bits = ((bits & 0x0F0F0F0Fu) << 4) | ((bits & 0xF0F0F0F0u) >> 4);
+      bits = ((bits & 0x00FF00FFu) << 8) | ((bits & 0xFF00FF00u) >> 8);
+      R v = R(float(bits) * 2.3283064e-10f);
+      R sx = R(2) * u - R(1), sy = R(2) * v - R(1);
+      R dx = 0, dy = 0;
+      if (!(std::fabs(sx) <= R(1.1920929e-7) && std::fabs(sy) <= R(1.1920929e-7))) {
+        R rr, th;
+        if (std::fabs(sx) > std::fabs(sy)) {
+          rr = sx;
+          th = R(0.78539816339744830962) * (sy / sx);
+        } else {
+          rr = sy;
+          th = R(1.57079632679489661923) - R(0.78539816339744830962) * (sx / sy);
+        }
+        dx = rr * std::cos(th);
+        dy = rr * std::sin(th);
+      }
+      target = lp + tangent * (dx * R(L.radius)) + bit * (dy * R(L.radius));
+    }
+    V<R> to = target - p;
+    R dd = rmax(len(to), R(1.0e-4));
+    R att = R(1) / (dd * dd);
+    *wi = to * (R(1) / dd);
+    *rad = scale(inten, att);
+    *dist = dd;
+  }
+
+  // shade_color (R:4217-4276)
+  Sp<R> shade(const Mat<R>& mat, const Hit<R>& h, bool front, V<R> n_shade, V<R> wo, uint64_t* evals) const {
+    const ft_scene_desc& d = S.desc();
+    if (d.n_lights == 0) return sp(R(1), R(1), R(1));
+    V<R> n = normalize(n_shade);
+    V<R> gn = front ? normalize(h.normal) : normalize(h.normal * R(-1));
+    Sp<R> color = black<R>();
+    R eps = R(op_.epsilon);
+    for (uint32_t li = 0; li < d.n_lights; ++li) {
+      const ft_light& L = d.lights[li];
+      uint32_t samples = L.kind == FT_LIGHT_SPHERE ? std::max(L.samples, 1u) : 1u;
+      R inv = R(1) / R(samples);
+      for (uint32_t s = 0; s < samples; ++s) {
+        V<R> wi;
+        Sp<R> rad;
+        R dist;
+        sample_light(L, h.pos, s, samples, &wi, &rad, &dist);
+        wi = normalize(wi);
+        R ndotl = n.x * wi.x + n.y * wi.y + n.z * wi.z;
+        if (ndotl <= R(0)) continue;
+        V<R> so = offset_origin(h.pos, gn, wi, eps);
+        R max_t = std::isfinite(dist) ? rmax(dist - eps * R(8), R(0)) : R(op_.max_dist);
+        if (max_t <= R(0)) continue;
+        R vis = shadow(so, wi, max_t, evals);
+        if (vis <= R(0)) continue;
+        // eval_bsdf passes the context normal as stored (R:4905-4919)
+        Sp<R> f = mat_eval(mat, n_shade, wi, wo);
+        color = color + scale(f * rad, ndotl * vis * inv);
+      }
+    }
+    return color;
+  }
+
+  static R fresnel_dielectric(R ci, R eta_i, R eta_t) {  // R:5188-5204
+    R ei = rmax(eta_i, R(1.0e-4)), et = rmax(eta_t, R(1.0e-4));
+    if (std::fabs(ei - et) < R(1.0e-6)) return R(0);
+    ci = rclamp(ci, R(0), R(1));
+    R eta = ei / et;
+    R sin2 = eta * eta * (R(1) - ci * ci);
+    if (sin2 >= R(1)) return R(1);
+    R ct = std::sqrt(R(1) - sin2);
+    R rs = ((ei * ci) - (et * ct)) / rmax((ei * ci) + (et * ct), R(1.0e-6));
+    R rp = ((et * ci) - (ei * ct)) / rmax((et * ci) + (ei * ct), R(1.0e-6));
+    return R(0.5) * (rs * rs + rp * rp);
+  }
+
+  // trace_hit_with_material (ray.rs:41-222)
+  Sp<R> trace_hit(const Hit<R>& h, V<R> dir, Medium<R> med, uint32_t depth, const Mat<R>& mat,
+                  uint64_t* evals) const {
+    bool front = dot(h.normal, dir) < R(0);
+    V<R> normal = front ? normalize(h.normal) : normalize(h.normal * R(-1));
+    V<R> wo = normalize(dir * R(-1));
+    // build_bsdf_context: tree-resolved geometric normal (epsilon 1e-4)
+    V<R> gnode;
+    V<R> shading_n = normal;
+    if (surface_normal(S.desc().root, h.pos, R(1.0e-4), &gnode)) {
+      gnode = front ? gnode : gnode * R(-1);
+      shading_n = normalize(gnode);
+    }
+    Params<R> P = dominant_params(mat);
+    R rough = rclamp(P.roughness, R(0), R(1));
+    int model = dominant_model(mat);
+    R transmission, ior, specular_strength, metallic, clearcoat;
+    bool thin;
+    Sp<R> spec_color, base_color;
+    switch (model) {
+      case kStandard:
+        transmission = rclamp(P.transmission, R(0), R(1));
+        ior = rclamp(P.ior, R(1), R(3));
+        thin = P.thin_walled;
+        spec_color = P.specular_color;
+        base_color = P.color;
+        metallic = rclamp(P.metallic, R(0), R(1));
+        clearcoat = rclamp(P.clearcoat, R(0), R(1));
+        specular_strength = rclamp(P.specular * P.specular_weight, R(0), R(1));
+        break;
+      case kLambert:
+        transmission = 0; ior = 1; thin = false; spec_color = black<R>(); base_color = P.color;
+        metallic = 0; clearcoat = 0; specular_strength = 0;
+        break;
+      case kMetal:
+        transmission = 0; ior = 1; thin = false; spec_color = P.color; base_color = P.color;
+        metallic = 1; clearcoat = 0; specular_strength = 1;
+        break;
+      default:  // dielectric
+        transmission = 1; ior = rclamp(P.ior, R(1), R(3)); thin = P.thin_walled; spec_color = sp(R(1), R(1), R(1));
+        base_color = P.color; metallic = 0; clearcoat = 0; specular_strength = 1;
+        break;
+    }
+    R eta_i, eta_t, next_ior;
+    if (thin) { eta_i = 1; eta_t = 1; next_ior = med.ior; }
+    else if (front) { eta_i = med.ior; eta_t = ior; next_ior = ior; }
+    else { eta_i = med.ior; eta_t = 1; next_ior = 1; }
+    V<R> gn = normal;  // geometric normal (hit normal oriented to the viewer)
+    R cosv = std::fabs(dot(normal, wo));
+    R fresnel;
+    if (transmission > R(1.0e-4)) {
+      fresnel = fresnel_dielectric(cosv, eta_i, eta_t);
+    } else {
+      R f0 = rclamp(f0_from_ior(ior), R(0), R(1));
+      R x = R(1) - rclamp(cosv, R(0), R(1));
+      R m5 = x * x * x * x * x;
+      fresnel = rclamp(f0 + (R(1) - f0) * m5, R(0), R(1));
+    }
+    R reflect_w;
+    if (transmission > R(1.0e-4)) {
+      reflect_w = rclamp(fresnel, R(0), R(1));
+    } else {
+      R base = metallic > R(0.5) ? R(1) : rclamp(specular_strength, R(0), R(1));
+      reflect_w = rclamp(base * fresnel + metallic * R(0.8) + clearcoat * R(0.2), R(0), R(1));
+    }
+    R local_w = rclamp((R(1) - transmission) * (R(1) - reflect_w), R(0), R(1));
+    Sp<R> color = scale(shade(mat, h, front, shading_n, wo, evals), local_w);
+    color = color + emission(mat);
+    R eps = R(op_.epsilon);
+    if (reflect_w > R(1.0e-4)) {
+      // trace_rough_dielectric_reflection is not restated (roughness <= 0.06 here)
+      V<R> rd = normalize(dir - normal * (R(2) * dot(dir, normal)));
+      V<R> ro = offset_origin(h.pos, gn, rd, eps * (R(1) + rough * R(6)));
+      Sp<R> refl = trace(ro, rd, med, depth + 1, evals);
+      Sp<R> tint = lerp_sp(spec_color, base_color, rclamp(metallic, R(0), R(1)));
+      color = color + scale(refl * tint, reflect_w);
+    }
+    if (transmission > R(1.0e-4)) {
+      Medium<R> next = med;
+      if (!thin) next = transition(mat, front, med);
+      next.ior = rclamp(next_ior, R(1), R(3));
+      Sp<R> refr = black<R>();
+      V<R> td;
+      if (refract_dir(dir, normal, eta_i / eta_t, &td)) {
+        V<R> to = offset_origin(h.pos, gn, td, eps * (R(8) + rough * R(12)));
+        refr = trace(to, normalize(td), next, depth + 1, evals);
+      }
+      if (!(refr.r == R(0) && refr.g == R(0) && refr.b == R(0))) {
+        R tt = rclamp(transmission, R(0), R(1));
+        Sp<R> tint = sp(R(1) - (R(1) - rclamp(base_color.r, R(0), R(1))) * tt,
+                        R(1) - (R(1) - rclamp(base_color.g, R(0), R(1))) * tt,
+                        R(1) - (R(1) - rclamp(base_color.b, R(0), R(1))) * tt);
+        color = color + scale(refr * tint, transmission * (R(1) - fresnel));
+      }
+    }
+    return attenuate(color, med, h.t);
+  }
+
+  static bool refract_dir(V<R> inc, V<R> nrm, R eta, V<R>* out) {  // R:5080-5095
+    V<R> i = normalize(inc);
+    V<R> n = normalize(nrm);
+    R cosi = rclamp(dot(i, n), R(-1), R(1));
+    if (cosi > R(0)) n = n * R(-1);
+    else cosi = -cosi;
+    R sin2 = eta * eta * (R(1) - cosi * cosi);
+    if (sin2 > R(1)) return false;
+    R cost = std::sqrt(R(1) - sin2);
+    *out = normalize(i * eta + n * (eta * cosi - cost));
+    return true;
+  }
+
+  static Medium<R> transition(const Mat<R>& m, bool front, Medium<R> cur) {  // R:5125-5175
+    int model = dominant_model(m);
+    Params<R> p = dominant_params(m);
+    bool transmissive = model == kDielectric || (model == kStandard && p.transmission > R(0.01));
+    if (!transmissive) return cur;
+    if (front) return Medium<R>{rclamp(p.ior, R(1), R(3)), sp(R(1), R(1), R(1)), R(0)};
+    return Medium<R>::air();
+  }
+};
+
+// spectrum_to_rgb8_reinhard (R:5229-5239)
+uint8_t reinhard_u8(float v) {
+  float x = std::fmax(v, 0.0f);
+  float t = x / (1.0f + x);
+  float mapped = std::min(std::pow(t, 1.0f / 2.2f), 1.0f);
+  return static_cast<uint8_t>(mapped * 255.0f);
+}
+
+template <class R>
+int render_trace(const ft_scene_desc* desc, const ft_render_options* options, int accel, uint32_t aa,
+                 uint32_t max_depth, int threads, uint32_t row_begin, uint32_t row_end, uint32_t row_step,
+                 float* rgb_out, uint8_t* rgb8_out, uint64_t* evals_out) {
+  Opts op = resolve(options);
+  Scene<R> scene(*desc);
+  Accel<R> acc(scene, accel);
+  Camera<R> cam(*desc, op);
+  Tracer<R> tracer(scene, acc, op, max_depth);
+  aa = std::max(aa, 1u);
+  auto offs = sample_offsets(aa);
+  float aspect = static_cast<float>(op.width) / static_cast<float>(op.height);
+  if (threads <= 0) threads = static_cast<int>(std::max(1u, std::thread::hardware_concurrency()));
+  row_step = std::max(row_step, 1u);
+  row_end = std::min(row_end, op.height);
+  std::vector<uint32_t> rows;
+  for (uint32_t y = row_begin; y < row_end; y += row_step) rows.push_back(y);
+  std::atomic<size_t> next{0};
+  std::atomic<uint64_t> total{0};
+  auto worker = [&]() {
+    uint64_t evals = 0;
+    for (;;) {
+      size_t k = next.fetch_add(1);
+      if (k >= rows.size()) break;
+      uint32_t y = rows[k];
+      for (uint32_t x = 0; x < op.width; ++x) {
+        Sp<float> sum = sp(0.0f, 0.0f, 0.0f);
+        for (uint32_t s = 0; s < aa; ++s) {
+          float px = ((static_cast<float>(x) + offs[s].first) / static_cast<float>(op.width)) * 2.0f - 1.0f;
+          float py = 1.0f - ((static_cast<float>(y) + offs[s].second) / static_cast<float>(op.height)) * 2.0f;
+          V<R> d = cam.dir(R(px * aspect), R(py));
+          Sp<R> c = tracer.trace(cam.origin, d, Medium<R>::air(), 0, &evals);
+          sum = sum + sp(float(c.r), float(c.g), float(c.b));
+        }
+        Sp<float> avg = scale(sum, 1.0f / static_cast<float>(aa));
+        size_t pi = (static_cast<size_t>(y) * op.width + x) * 3;
+        if (rgb_out) {
+          rgb_out[pi] = avg.r;
+          rgb_out[pi + 1] = avg.g;
+          rgb_out[pi + 2] = avg.b;
+        }
+        if (rgb8_out) {
+          rgb8_out[pi] = reinhard_u8(avg.r);
+          rgb8_out[pi + 1] = reinhard_u8(avg.g);
+          rgb8_out[pi + 2] = reinhard_u8(avg.b);
+        }
+      }
+    }
+    total.fetch_add(evals);
+  };
+  std::vector<std::thread> pool;
+  for (int i = 1; i < threads; ++i) pool.emplace_back(worker);
+  worker();
+  for (auto& t : pool) t.join();
+  if (evals_out) *evals_out = total.load();
+  return 0;
+}
+
 int check_desc(const ft_scene_desc* d) {
   if (!d || d->abi_version != FT_ABI_VERSION || d->root < 0 || static_cast<uint32_t>(d->root) >= d->n_nodes) {
     g_error = "invalid scene description";
@@ -1027,3 +1795,19 @@ int oracle_eval_program(const ft_scene_desc* desc, int program, int precision, c
 }
 
 }  // extern "C"
+
+extern "C" int oracle_render_trace(const ft_scene_desc* desc, const ft_render_options* options, int accel,
+                                   uint32_t aa_samples, uint32_t max_depth, int precision, int threads,
+                                   uint32_t row_begin, uint32_t row_end, uint32_t row_step, float* rgb_out,
+                                   uint8_t* rgb8_out, uint64_t* evals_out) {
+  if (int e = check_desc(desc)) return e;
+  if (!options || options->width == 0 || options->height == 0) {
+    g_error = "invalid render options";
+    return FT_ERR_INVALID_ARGUMENT;
+  }
+  if (precision == 64)
+    return render_trace<double>(desc, options, accel, aa_samples, max_depth, threads, row_begin, row_end, row_step,
+                                rgb_out, rgb8_out, evals_out);
+  return render_trace<float>(desc, options, accel, aa_samples, max_depth, threads, row_begin, row_end, row_step,
+                             rgb_out, rgb8_out, evals_out);
+}

@@ -33,6 +33,14 @@ int oracle_render_depth(const ft_scene_desc* desc, const ft_render_options* opti
                         float* t_out, uint8_t* mask_out, uint32_t* material_out,
                         float* normal_out, uint8_t* rgb8_out, uint64_t* evals_out);
 
+/* Whitted trace (trace_ray_recursive, crates/forgedthoughts/src/renderer/ray.rs:3-222)
+ * over the same rows; rgb_out receives width*height*3 linear floats (the AA
+ * average), rgb8_out the Reinhard + gamma bytes (renderer.rs:5229-5239). */
+int oracle_render_trace(const ft_scene_desc* desc, const ft_render_options* options,
+                        int accel, uint32_t aa_samples, uint32_t max_depth, int precision,
+                        int threads, uint32_t row_begin, uint32_t row_end, uint32_t row_step,
+                        float* rgb_out, uint8_t* rgb8_out, uint64_t* evals_out);
+
 /* Accelerator distance query (`Accelerator::distance_info`) at n points
  * (xyz triples).  Outputs are nullable. */
 int oracle_distance(const ft_scene_desc* desc, int accel, int precision,

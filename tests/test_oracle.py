@@ -54,3 +54,31 @@ def test_empty_sample_rows_are_untouched():
     rendered = np.zeros(32, bool)
     rendered[::8] = True
     assert not m[~rendered].any()
+
+
+# crates/forgedthoughts/tests/render_regression.rs:48-90 (Whitted, depth 4, aa 1, Bvh)
+TRACE_CASES = {
+    "ray_metal": dict(width=96, height=96, max_steps=360, max_dist=50.0, epsilon=0.0002, step_scale=0.7,
+                      camera_z=6.0, fov_y_degrees=35.0),
+    "ray_boolean_union_round": dict(width=96, height=96, max_steps=520, max_dist=60.0, epsilon=0.0002,
+                                    step_scale=0.7, camera_z=6.0, fov_y_degrees=25.0),
+}
+
+
+@pytest.mark.parametrize("name", sorted(TRACE_CASES))
+@pytest.mark.parametrize("precision", [32, 64])
+def test_oracle_matches_reference_trace_golden(name, precision):
+    st = ft.load_and_eval_scene(FIXTURES / "render_regression" / f"{name}.ft")
+    _, rgb8, _ = oracle.render_trace(st, ft.RenderOptions(**TRACE_CASES[name]), ft.AccelMode.Bvh, 1, 4, precision)
+    gold = ft.read_png(FIXTURES / "render_regression" / f"{name}.png")
+    diff = np.abs(rgb8.astype(int) - gold.astype(int))
+    # the reference's own regression tolerance (render_regression.rs:139-145)
+    assert diff.max() <= 8 and diff.mean() <= 0.35, (diff.max(), diff.mean())
+
+
+def test_trace_f32_tracks_f64():
+    st = ft.load_and_eval_scene(FIXTURES / "render_regression" / "ray_boolean_union_round.ft")
+    opts = ft.RenderOptions(**TRACE_CASES["ray_boolean_union_round"])
+    a, _, _ = oracle.render_trace(st, opts, 1, 1, 4, 32)
+    b, _, _ = oracle.render_trace(st, opts, 1, 1, 4, 64)
+    assert np.sqrt(np.mean((a - b) ** 2)) <= 1e-3
