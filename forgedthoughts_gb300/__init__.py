@@ -246,6 +246,43 @@ def render_depth(state: SceneState, options: RenderOptions, accel: AccelMode = A
 
 
 @dataclasses.dataclass
+class RaySettings:
+    """``RaySettings`` (R:124-141)."""
+
+    max_depth: int = 8
+    tile_size: int = 64
+    aa_samples: int = 1
+
+
+def render_trace(state: SceneState, options: RenderOptions, accel: AccelMode = AccelMode.Bvh, aa_samples: int = 1,
+                 max_depth: int = 8, *, want_linear: bool = True) -> tuple:
+    """Whitted trace of ``state`` on the GPU: (linear rgb (H, W, 3) float32 or
+    None, rgb8 (H, W, 3) uint8)."""
+    h, w = int(options.height), int(options.width)
+    lin = np.empty((h, w, 3), np.float32) if want_linear else None
+    rgb8 = np.empty((h, w, 3), np.uint8)
+    opts = options.to_c()
+    _check(_native.lib().ft_render_trace(state.gpu().handle, ctypes.byref(opts), int(accel), max(int(aa_samples), 1),
+                                         int(max_depth), _ptr(lin), _ptr(rgb8), 0, None))
+    return lin, rgb8
+
+
+def render_ray_progressive_with_accel(state: SceneState, options: RenderOptions, accel: AccelMode,
+                                      settings: RaySettings, on_tile) -> np.ndarray:
+    """Whitted render with the reference's per-tile progress callback (R:1201-1236)."""
+    import time
+
+    start = time.monotonic()
+    _, img = render_trace(state, options, accel, settings.aa_samples, settings.max_depth, want_linear=False)
+    out = np.zeros_like(img)
+    jobs = list(_tile_jobs(options.width, options.height, max(int(settings.tile_size), 1)))
+    for done, (tx, ty, tw, th) in enumerate(jobs, 1):
+        out[ty:ty + th, tx:tx + tw] = img[ty:ty + th, tx:tx + tw]
+        on_tile(PreviewProgress(done, len(jobs), int((time.monotonic() - start) * 1000)), out.copy())
+    return out
+
+
+@dataclasses.dataclass
 class PreviewProgress:
     """``PreviewProgress`` (R:96-101)."""
 

@@ -113,6 +113,9 @@ SIGNATURES = {
     "ft_render_depth": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RenderOptionsC), ctypes.c_int,
                                        ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p]),
+    "ft_render_trace": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RenderOptionsC), ctypes.c_int, ctypes.c_uint32,
+                                       ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
+                                       ctypes.c_void_p]),
     "ft_render_depth_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RenderOptionsC), ctypes.c_int,
                                              ctypes.c_uint32, ctypes.POINTER(RenderStatsC)]),
     "ft_measure_fp32_peak": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double)]),

@@ -76,6 +76,12 @@ struct DevScene {
   const int32_t* __restrict__ ur_cell_prims;
   const ft_program* __restrict__ programs;
   const ft_instr* __restrict__ instrs;
+  const ft_material* __restrict__ materials;
+  const ft_light* __restrict__ lights;
+  const int32_t* __restrict__ node_op_begin;
+  const int32_t* __restrict__ node_op_end;
+  const int32_t* __restrict__ ur_inner_blend;
+  int32_t n_materials, n_lights, env_program;
   int32_t bvh_root;
   float smin[3], smax[3];
 };
@@ -392,6 +398,48 @@ __device__ __noinline__ Info scene_distance(const DevScene& S, F3 p, Ctx<kStats>
 template <bool kStats>
 __device__ __forceinline__ float scene_d(const DevScene& S, F3 p, Ctx<kStats>& cx) {
   return scene_distance(S, p, cx).d;
+}
+
+// The same leaf-BVH walk reporting the winning hard-union leaf: the leaf whose
+// subtree the reference's Union walks descend into when resolving a hit's
+// normal and material (R:4471-4478, R:6995-7002).
+template <bool kStats>
+__device__ __noinline__ Info scene_distance_leaf(const DevScene& S, F3 p, int* leaf, Ctx<kStats>& cx) {
+  cx.eval();
+  float best = kInf;
+  Info cur{kInf, 0u, 0u};
+  *leaf = 0;
+  int stack[64];
+  float stack_lb[64];
+  int sp = 0;
+  stack[sp] = S.bvh_root;
+  stack_lb[sp] = node_lb(p, S.bvh[S.bvh_root].bmin, S.bvh[S.bvh_root].bmax);
+  ++sp;
+  while (sp > 0) {
+    --sp;
+    int ni = stack[sp];
+    if (stack_lb[sp] > best) continue;
+    const DevBvhNode& n = S.bvh[ni];
+    if (n.leaf >= 0) {
+      Info in = eval_leaf(S, S.leaves[n.leaf], p, best, cx);
+      if (in.d < best) {
+        best = in.d;
+        cur = in;
+        *leaf = n.leaf;
+      }
+      continue;
+    }
+    float ll = node_lb(p, S.bvh[n.lhs].bmin, S.bvh[n.lhs].bmax), rl = node_lb(p, S.bvh[n.rhs].bmin, S.bvh[n.rhs].bmax);
+    if (sp + 2 > 64) break;
+    if (ll <= rl) {
+      stack[sp] = n.rhs; stack_lb[sp] = rl; ++sp;
+      stack[sp] = n.lhs; stack_lb[sp] = ll; ++sp;
+    } else {
+      stack[sp] = n.lhs; stack_lb[sp] = ll; ++sp;
+      stack[sp] = n.rhs; stack_lb[sp] = rl; ++sp;
+    }
+  }
+  return cur;
 }
 
 // ray_aabb_intersection (R:4141-4173)
@@ -740,6 +788,220 @@ __global__ void depth_rgb8_kernel(const float* __restrict__ t, const uint8_t* __
   rgb[3 * static_cast<size_t>(i) + 2] = g;
 }
 
+#include "ft_trace.cuh"
+
+struct TraceHit {
+  float t;
+  F3 pos, normal;
+  uint32_t mat;
+  int leaf;
+};
+
+// raymarch_hit (R:4091-4139) from min_t, with the six-tap normal and the
+// winning leaf of the final evaluation.
+template <bool kStats>
+__device__ bool march_hit(const DevScene& S, const RayParams& P, F3 o, F3 d, float min_t, TraceHit* h,
+                          Ctx<kStats>& cx) {
+  float t0, t1;
+  if (!ray_aabb(o, d, S.smin, S.smax, &t0, &t1)) return false;
+  float max_t = fminf(P.max_dist, t1);
+  float traveled = fmaxf(min_t, fmaxf(t0, 0.0f));
+  float prev = traveled;
+  const float eps = P.eps;
+  const float scale = ftd::rclamp(P.step_scale, 0.05f, 1.0f);
+  const float min_step = fmaxf(eps * 0.5f, 1.0e-5f);
+  for (uint32_t s = 0; s < P.max_steps; ++s) {
+    if (traveled > max_t) return false;
+    cx.step();
+    Info info = scene_distance(S, o + d * traveled, cx);
+    if (fabsf(info.d) < eps) {
+      float lo = prev, hi = traveled;
+      for (int k = 0; k < 10; ++k) {
+        float mid = 0.5f * (lo + hi);
+        if (fabsf(scene_d(S, o + d * mid, cx)) < eps) hi = mid;
+        else lo = mid;
+      }
+      F3 pos = o + d * hi;
+      float e = fmaxf(eps * 4.0f, 1.0e-5f);
+      float dx = scene_d(S, f3(pos.x + e, pos.y, pos.z), cx) - scene_d(S, f3(pos.x - e, pos.y, pos.z), cx);
+      float dy = scene_d(S, f3(pos.x, pos.y + e, pos.z), cx) - scene_d(S, f3(pos.x, pos.y - e, pos.z), cx);
+      float dz = scene_d(S, f3(pos.x, pos.y, pos.z + e), cx) - scene_d(S, f3(pos.x, pos.y, pos.z - e), cx);
+      F3 nn = f3(dx, dy, dz);
+      h->normal = ftd::len3(nn) > 1.0e-8f ? ftd::normalize3(nn) : f3(0.0f, 1.0f, 0.0f);
+      Info fin = scene_distance_leaf(S, pos, &h->leaf, cx);
+      h->t = hi;
+      h->pos = pos;
+      h->mat = fin.mat;
+      return true;
+    }
+    prev = traveled;
+    traveled += fmaxf(fabsf(info.d) * scale, min_step);
+  }
+  return false;
+}
+
+// environment_color (R:4328-4333), falling back to the sum of EnvLight
+// radiances (env_radiance, R:4318-4326).
+__device__ F3 environment(const DevScene& S, F3 dir) {
+  if (S.env_program >= 0) return ftd::run_program(S.programs[S.env_program], S.instrs, &dir, nullptr);
+  F3 s = f3(0.0f, 0.0f, 0.0f);
+  for (int i = 0; i < S.n_lights; ++i)
+    if (S.lights[i].kind == FT_LIGHT_ENV) s = s + f3(S.lights[i].intensity[0], S.lights[i].intensity[1], S.lights[i].intensity[2]);
+  return s;
+}
+
+// One thread per (pixel, AA sample): the full Whitted tree of the sample.
+template <bool kStats>
+__global__ void __launch_bounds__(128) trace_kernel(DevScene S, RayParams P, uint32_t max_depth,
+                                                    float* __restrict__ sample_rgb,
+                                                    unsigned long long* __restrict__ stats) {
+  uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  Ctx<kStats> cx;
+  cx.c = Counters{0, 0, 0, 0, 0};
+  F3 dir;
+  size_t idx = 0;
+  bool active = i < P.n_items && item_ray(P, i, &dir, &idx);
+  if (active) {
+    const float eps = P.eps;
+    RayJob stack[kTraceStack];
+    int sp = 0;
+    stack[sp++] = RayJob{f3(P.origin[0], P.origin[1], P.origin[2]), dir, f3(1.0f, 1.0f, 1.0f), air(), 0};
+    F3 acc = f3(0.0f, 0.0f, 0.0f);
+    while (sp > 0) {
+      RayJob J = stack[--sp];
+      if (static_cast<uint32_t>(J.depth) >= max_depth) continue;
+      float min_t = J.depth == 0 ? 0.0f : eps * 2.0f;  // secondary_min_t (R:4175-4178)
+      TraceHit h;
+      if (!march_hit(S, P, J.o, J.d, min_t, &h, cx)) {
+        acc = acc + mul3(J.w, mul3(environment(S, J.d), transmittance(J.med, P.max_dist)));
+        continue;
+      }
+      Resolved rs;
+      resolve_hit(S, h.leaf, h.pos, &rs, cx);
+      bool front = ftd::dot3(h.normal, J.d) < 0.0f;
+      F3 normal = front ? ftd::normalize3(h.normal) : ftd::normalize3(h.normal * -1.0f);
+      F3 shading_n = normal;
+      if (rs.ok) shading_n = ftd::normalize3(front ? rs.normal : rs.normal * -1.0f);
+      DMat mats[2];
+      float ws[2];
+      int nm = 0;
+      if (rs.ok && rs.split) {
+        float tt = clamp01(rs.t);  // lerp_spectrum(a, b, t): a (1 - t) + b t
+        if (tt != 1.0f) { mats[nm] = rs.m; ws[nm++] = 1.0f - tt; }
+        if (tt != 0.0f) { mats[nm] = rs.mb; ws[nm++] = tt; }
+      } else {
+        mats[0] = rs.ok ? rs.m : mat_of_id(S, h.mat);
+        ws[0] = 1.0f;
+        nm = 1;
+      }
+      F3 att = transmittance(J.med, h.t);
+      F3 wo = ftd::normalize3(J.d * -1.0f);
+      for (int mi = 0; mi < nm; ++mi) {
+        const DMat& mat = mats[mi];
+        F3 W = mul3(J.w * ws[mi], att);
+        // trace_hit_with_material (ray.rs:41-222)
+        const DParams& Pm = dom_params(mat);
+        float rough = clamp01(Pm.roughness);
+        int model = dom_model(mat);
+        float transmission, ior, metallic, clearcoat, specular_strength;
+        bool thin;
+        F3 spec_color, base_color;
+        if (model == FT_MAT_STANDARD) {
+          transmission = clamp01(Pm.transmission); ior = ftd::rclamp(Pm.ior, 1.0f, 3.0f); thin = Pm.thin != 0;
+          spec_color = Pm.spec_color; base_color = Pm.color; metallic = clamp01(Pm.metallic);
+          clearcoat = clamp01(Pm.clearcoat); specular_strength = clamp01(Pm.specular * Pm.specular_weight);
+        } else if (model == FT_MAT_LAMBERT) {
+          transmission = 0.0f; ior = 1.0f; thin = false; spec_color = f3(0.0f, 0.0f, 0.0f); base_color = Pm.color;
+          metallic = 0.0f; clearcoat = 0.0f; specular_strength = 0.0f;
+        } else if (model == FT_MAT_METAL) {
+          transmission = 0.0f; ior = 1.0f; thin = false; spec_color = Pm.color; base_color = Pm.color;
+          metallic = 1.0f; clearcoat = 0.0f; specular_strength = 1.0f;
+        } else {
+          transmission = 1.0f; ior = ftd::rclamp(Pm.ior, 1.0f, 3.0f); thin = Pm.thin != 0;
+          spec_color = f3(1.0f, 1.0f, 1.0f); base_color = Pm.color; metallic = 0.0f; clearcoat = 0.0f;
+          specular_strength = 1.0f;
+        }
+        float eta_i, eta_t, next_ior;
+        if (thin) { eta_i = 1.0f; eta_t = 1.0f; next_ior = J.med.ior; }
+        else if (front) { eta_i = J.med.ior; eta_t = ior; next_ior = ior; }
+        else { eta_i = J.med.ior; eta_t = 1.0f; next_ior = 1.0f; }
+        float cosv = fabsf(ftd::dot3(normal, wo));
+        float fresnel;
+        if (transmission > 1.0e-4f) {
+          fresnel = fresnel_dielectric(cosv, eta_i, eta_t);
+        } else {
+          float f0 = clamp01(f0_from_ior(ior));
+          float x = 1.0f - clamp01(cosv);
+          float m5 = x * x * x * x * x;
+          fresnel = clamp01(f0 + (1.0f - f0) * m5);
+        }
+        float reflect_w;
+        if (transmission > 1.0e-4f) {
+          reflect_w = clamp01(fresnel);
+        } else {
+          float base = metallic > 0.5f ? 1.0f : clamp01(specular_strength);
+          reflect_w = clamp01(base * fresnel + metallic * 0.8f + clearcoat * 0.2f);
+        }
+        float local_w = clamp01((1.0f - transmission) * (1.0f - reflect_w));
+        F3 local = shade_color(S, mat, h.pos, normal, shading_n, wo, eps, P.max_dist, cx) * local_w;
+        acc = acc + mul3(W, local + mat_emission(mat));
+        if (reflect_w > 1.0e-4f && sp < kTraceStack) {
+          F3 rd = ftd::normalize3(J.d - normal * (2.0f * ftd::dot3(J.d, normal)));
+          F3 ro = offset_origin(h.pos, normal, rd, eps * (1.0f + rough * 6.0f));
+          F3 tint = lerp_sp(spec_color, base_color, clamp01(metallic));
+          stack[sp++] = RayJob{ro, rd, mul3(W, tint * reflect_w), J.med, J.depth + 1};
+        }
+        if (transmission > 1.0e-4f && sp < kTraceStack) {
+          MediumD next = thin ? J.med : transition(mat, front, J.med);
+          next.ior = ftd::rclamp(next_ior, 1.0f, 3.0f);
+          F3 td;
+          if (refract_dir(J.d, normal, eta_i / eta_t, &td)) {
+            F3 to = offset_origin(h.pos, normal, td, eps * (8.0f + rough * 12.0f));
+            float tt = clamp01(transmission);
+            F3 tint = f3(1.0f - (1.0f - clamp01(base_color.x)) * tt, 1.0f - (1.0f - clamp01(base_color.y)) * tt,
+                         1.0f - (1.0f - clamp01(base_color.z)) * tt);
+            stack[sp++] = RayJob{to, ftd::normalize3(td), mul3(W, tint * (transmission * (1.0f - fresnel))), next,
+                                 J.depth + 1};
+          }
+        }
+      }
+    }
+    sample_rgb[3 * idx] = acc.x;
+    sample_rgb[3 * idx + 1] = acc.y;
+    sample_rgb[3 * idx + 2] = acc.z;
+  }
+  if (kStats) {
+    unsigned long long v[5] = {cx.c.evals, cx.c.prims, cx.c.boxes, cx.c.hook_instrs, cx.c.steps};
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      unsigned long long x = v[k];
+      for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+      if ((threadIdx.x & 31) == 0 && x) atomicAdd(&stats[k], x);
+    }
+  }
+}
+
+// AA average per pixel and spectrum_to_rgb8_reinhard (R:3908-3921, R:5229-5239).
+__global__ void trace_pixels_kernel(const float* __restrict__ sample_rgb, uint32_t n_pixels, uint32_t aa,
+                                    float* __restrict__ rgb_out, uint8_t* __restrict__ rgb8_out) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_pixels) return;
+  float s[3] = {0.0f, 0.0f, 0.0f};
+  for (uint32_t k = 0; k < aa; ++k)
+    for (int c = 0; c < 3; ++c) s[c] += sample_rgb[(static_cast<size_t>(i) * aa + k) * 3 + c];
+  float inv = 1.0f / static_cast<float>(aa);
+  for (int c = 0; c < 3; ++c) {
+    float v = s[c] * inv;
+    if (rgb_out) rgb_out[3 * static_cast<size_t>(i) + c] = v;
+    if (rgb8_out) {
+      float x = fmaxf(v, 0.0f);
+      float t = x / (1.0f + x);
+      float mapped = fminf(powf(t, 1.0f / 2.2f), 1.0f);
+      rgb8_out[3 * static_cast<size_t>(i) + c] = static_cast<uint8_t>(mapped * 255.0f);
+    }
+  }
+}
+
 // Dependent-FMA chains, 8 per thread, for the FP32 roofline denominator.
 __global__ void fma_peak_kernel(float* out, int iters, float a, float b) {
   float x0 = threadIdx.x * 1e-3f, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6,
@@ -807,7 +1069,8 @@ struct ft_scene {
   float* d_t = nullptr;
   uint8_t* d_mask = nullptr;
   uint32_t* d_mat = nullptr;
-  float* d_normal = nullptr;
+  float* d_normal = nullptr;  // also the per-sample radiance of traces
+  float* d_rgbf = nullptr;
   uint8_t* d_rgb = nullptr;
   size_t cap_items = 0, cap_pixels = 0;
   unsigned long long* d_stats = nullptr;
@@ -838,6 +1101,11 @@ ft_status upload_scene(ft_scene* sc) {
       {im.instrs.data(), im.instrs.size() * sizeof(ft_instr), 0},
       {im.ur_cell_offsets.data(), im.ur_cell_offsets.size() * sizeof(uint32_t), 0},
       {im.ur_cell_prims.data(), im.ur_cell_prims.size() * sizeof(int32_t), 0},
+      {im.materials.data(), im.materials.size() * sizeof(ft_material), 0},
+      {im.lights.data(), im.lights.size() * sizeof(ft_light), 0},
+      {im.node_op_begin.data(), im.node_op_begin.size() * sizeof(int32_t), 0},
+      {im.node_op_end.data(), im.node_op_end.size() * sizeof(int32_t), 0},
+      {im.ur_inner_blend.data(), im.ur_inner_blend.size() * sizeof(int32_t), 0},
   };
   size_t total = 0;
   for (Part& p : parts) {
@@ -865,6 +1133,14 @@ ft_status upload_scene(ft_scene* sc) {
   d.instrs = reinterpret_cast<const ft_instr*>(base + parts[10].off);
   d.ur_cell_offsets = reinterpret_cast<const uint32_t*>(base + parts[11].off);
   d.ur_cell_prims = reinterpret_cast<const int32_t*>(base + parts[12].off);
+  d.materials = reinterpret_cast<const ft_material*>(base + parts[13].off);
+  d.lights = reinterpret_cast<const ft_light*>(base + parts[14].off);
+  d.node_op_begin = reinterpret_cast<const int32_t*>(base + parts[15].off);
+  d.node_op_end = reinterpret_cast<const int32_t*>(base + parts[16].off);
+  d.ur_inner_blend = reinterpret_cast<const int32_t*>(base + parts[17].off);
+  d.n_materials = static_cast<int32_t>(im.materials.size());
+  d.n_lights = static_cast<int32_t>(im.lights.size());
+  d.env_program = im.environment_program;
   d.bvh_root = im.bvh_root;
   std::memcpy(d.smin, im.scene_min, sizeof(d.smin));
   std::memcpy(d.smax, im.scene_max, sizeof(d.smax));
@@ -897,9 +1173,12 @@ ft_status ensure_buffers(ft_scene* sc, size_t items, size_t pixels) {
   }
   if (pixels > sc->cap_pixels) {
     cudaFree(sc->d_rgb);
+    cudaFree(sc->d_rgbf);
     sc->d_rgb = nullptr;
+    sc->d_rgbf = nullptr;
     sc->cap_pixels = 0;
     FT_CUDA_TRY(cudaMalloc(&sc->d_rgb, pixels * 3), "cudaMalloc(rgb)");
+    FT_CUDA_TRY(cudaMalloc(&sc->d_rgbf, pixels * 3 * sizeof(float)), "cudaMalloc(rgb linear)");
     sc->cap_pixels = pixels;
   }
   return FT_OK;
@@ -1033,6 +1312,7 @@ void ft_scene_destroy(ft_scene* sc) {
   cudaFree(sc->d_mask);
   cudaFree(sc->d_mat);
   cudaFree(sc->d_normal);
+  cudaFree(sc->d_rgbf);
   cudaFree(sc->d_rgb);
   cudaFree(sc->d_stats);
   cudaSetDevice(prev);
@@ -1109,6 +1389,41 @@ ft_status ft_render_depth_preview_noalloc(ft_scene* sc, const ft_render_options*
   uint32_t np = static_cast<uint32_t>(pixels);
   depth_rgb8_kernel<<<(np + 255) / 256, 256, 0, st>>>(t, mask, np, aa, options->max_dist, rgb8_out);
   FT_CUDA_TRY(cudaGetLastError(), "depth_rgb8_kernel launch");
+  ftcommon::clear_last_error();
+  return FT_OK;
+}
+
+ft_status ft_render_trace(ft_scene* sc, const ft_render_options* options, ft_accel_mode accel, uint32_t aa_samples,
+                          uint32_t max_depth, float* rgb_out, uint8_t* rgb8_out, uint32_t flags, void* stream) {
+  if (!sc) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "scene must be non-null");
+  if (accel < FT_ACCEL_NAIVE || accel > FT_ACCEL_BRICKS) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "unknown accel mode");
+  uint32_t aa = std::max(aa_samples, 1u);
+  if (ft_status s = check_options(options, aa)) return s;
+  uint32_t depth = std::max(max_depth, 1u);  // RaySettings::max_depth.max(1)
+  if (depth > 10) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "max_depth must be <= 10");
+  std::lock_guard<std::mutex> lock(sc->mu);
+  FT_CUDA_TRY(cudaSetDevice(sc->device), "cudaSetDevice");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const bool dev_ptrs = (flags & FT_FLAG_DEVICE_POINTERS) != 0;
+  size_t pixels = static_cast<size_t>(options->width) * options->height;
+  size_t items = pixels * aa;
+  if (ft_status s = ensure_buffers(sc, items, pixels)) return s;
+  RayParams P = make_params(sc, *options, aa);
+  uint64_t blocks = (P.n_items + 127) / 128;
+  if (blocks > 0x7fffffffull) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "image too large");
+  trace_kernel<false><<<static_cast<unsigned>(blocks), 128, 0, st>>>(sc->dev, P, depth, sc->d_normal, nullptr);
+  FT_CUDA_TRY(cudaGetLastError(), "trace_kernel launch");
+  float* rgbf = rgb_out ? (dev_ptrs ? rgb_out : sc->d_rgbf) : nullptr;
+  uint8_t* rgb8 = rgb8_out ? (dev_ptrs ? rgb8_out : sc->d_rgb) : nullptr;
+  uint32_t np = static_cast<uint32_t>(pixels);
+  trace_pixels_kernel<<<(np + 255) / 256, 256, 0, st>>>(sc->d_normal, np, aa, rgbf, rgb8);
+  FT_CUDA_TRY(cudaGetLastError(), "trace_pixels_kernel launch");
+  if (!dev_ptrs) {
+    if (rgb_out) FT_CUDA_TRY(cudaMemcpyAsync(rgb_out, rgbf, pixels * 3 * sizeof(float), cudaMemcpyDeviceToHost, st),
+                             "copy rgb");
+    if (rgb8_out) FT_CUDA_TRY(cudaMemcpyAsync(rgb8_out, rgb8, pixels * 3, cudaMemcpyDeviceToHost, st), "copy rgb8");
+  }
+  FT_CUDA_TRY(cudaStreamSynchronize(st), "trace");
   ftcommon::clear_last_error();
   return FT_OK;
 }

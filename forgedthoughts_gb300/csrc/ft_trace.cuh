@@ -1,0 +1,787 @@
+// Whitted ray tracing on sm_103a (included by ft_render.cu, inside its
+// anonymous namespace, after the distance evaluators).
+//
+// Restates trace_ray_recursive / trace_hit_with_material
+// (crates/forgedthoughts/src/renderer/ray.rs:3-222) as a stack-based bounce
+// loop: each stacked ray carries the product of the weights and medium
+// attenuations of its ancestors, so the recursion's nested sums become one
+// accumulation per sample.  Shading at a hit follows build_bsdf_context
+// (R:4397-4449): the geometric normal is the tree-resolved, smoothstep-blended
+// normal (R:4462-4570), the material is the blended material of the tree
+// (R:6926-7162, R:7602-7683) and a smooth boolean at the root splits the hit
+// into two material traces mixed by its blend weight (ray.rs:31-35).
+//
+// Blend weights that are exactly 0 or 1 contribute exactly nothing, which lets
+// the union_round path resolve normals and materials from the primitives near
+// the hit only.  Whether a subtree's material becomes a Blend depends only on
+// whether its primitives mix material models, a static per-node flag.
+
+constexpr int kTraceStack = 32;
+constexpr int kGather = 32;
+constexpr float kNormalEps = 1.0e-4f;  // resolve_surface_normal_at_hit epsilon (R:4411)
+
+struct DParams {  // MaterialParams (materials/mod.rs:66-86)
+  F3 color;
+  float roughness, metallic, specular, specular_weight;
+  F3 spec_color;
+  float ior, clearcoat, clearcoat_roughness, transmission;
+  int thin;
+  F3 emission_color;
+  float emission_strength;
+};
+
+struct DMat {  // Material incl. Blend (materials/mod.rs:214-230)
+  int kind;  // ft_material_kind, or kBlendKind
+  int a_model, b_model;
+  float t;
+  DParams a, b;
+};
+constexpr int kBlendKind = 4;
+
+__device__ __forceinline__ F3 mul3(F3 a, F3 b) { return f3(a.x * b.x, a.y * b.y, a.z * b.z); }
+__device__ __forceinline__ float clamp01(float x) { return ftd::rclamp(x, 0.0f, 1.0f); }
+// lerp_spectrum (R:5205-5213)
+__device__ __forceinline__ F3 lerp_sp(F3 a, F3 b, float t) {
+  float tt = clamp01(t);
+  return f3(a.x * (1.0f - tt) + b.x * tt, a.y * (1.0f - tt) + b.y * tt, a.z * (1.0f - tt) + b.z * tt);
+}
+
+__device__ DParams params_of(const ft_material& m) {
+  DParams p;
+  p.color = f3(m.color[0], m.color[1], m.color[2]);
+  p.roughness = m.roughness;
+  p.metallic = m.metallic;
+  p.specular = m.specular;
+  p.specular_weight = m.specular_weight;
+  p.spec_color = f3(m.specular_color[0], m.specular_color[1], m.specular_color[2]);
+  p.ior = m.ior;
+  p.clearcoat = m.clearcoat;
+  p.clearcoat_roughness = m.clearcoat_roughness;
+  p.transmission = m.transmission;
+  p.thin = m.thin_walled;
+  p.emission_color = f3(m.emission_color[0], m.emission_color[1], m.emission_color[2]);
+  p.emission_strength = m.emission_strength;
+  return p;
+}
+
+// material_for_id (R:6895-6900)
+__device__ DMat mat_of_id(const DevScene& S, uint32_t id) {
+  const ft_material& fm = S.materials[id < static_cast<uint32_t>(S.n_materials) ? id : 0u];
+  DMat m;
+  m.kind = fm.kind;
+  m.a_model = m.b_model = fm.kind;
+  m.t = 0.0f;
+  m.a = params_of(fm);
+  m.b = m.a;
+  return m;
+}
+
+__device__ __forceinline__ int dom_model(const DMat& m) {
+  if (m.kind != kBlendKind) return m.kind;
+  return m.t < 0.5f ? m.a_model : m.b_model;
+}
+__device__ __forceinline__ const DParams& dom_params(const DMat& m) {
+  if (m.kind != kBlendKind) return m.a;
+  return m.t < 0.5f ? m.a : m.b;
+}
+
+// blend_params (R:7602-7627)
+__device__ DParams blend_params(DParams a, const DParams& b, float t) {
+  a.color = lerp_sp(a.color, b.color, t);
+  a.roughness = a.roughness + (b.roughness - a.roughness) * t;
+  a.metallic = a.metallic + (b.metallic - a.metallic) * t;
+  a.specular = a.specular + (b.specular - a.specular) * t;
+  a.specular_weight = a.specular_weight + (b.specular_weight - a.specular_weight) * t;
+  a.spec_color = lerp_sp(a.spec_color, b.spec_color, t);
+  a.ior = a.ior + (b.ior - a.ior) * t;
+  a.clearcoat = a.clearcoat + (b.clearcoat - a.clearcoat) * t;
+  a.clearcoat_roughness = a.clearcoat_roughness + (b.clearcoat_roughness - a.clearcoat_roughness) * t;
+  a.transmission = a.transmission + (b.transmission - a.transmission) * t;
+  a.thin = t < 0.5f ? a.thin : b.thin;
+  a.emission_color = lerp_sp(a.emission_color, b.emission_color, t);
+  a.emission_strength = a.emission_strength + (b.emission_strength - a.emission_strength) * t;
+  return a;
+}
+
+// blend_materials (R:7629-7651)
+__device__ DMat blend_materials(const DMat& a, const DMat& b, float t) {
+  DMat m;
+  if (a.kind != kBlendKind && a.kind == b.kind) {
+    m.kind = a.kind;
+    m.a_model = m.b_model = a.kind;
+    m.t = 0.0f;
+    m.a = blend_params(a.a, b.a, t);
+    m.b = m.a;
+    return m;
+  }
+  m.kind = kBlendKind;
+  m.a_model = dom_model(a);
+  m.a = dom_params(a);
+  m.b_model = dom_model(b);
+  m.b = dom_params(b);
+  m.t = clamp01(t);
+  return m;
+}
+
+// The material of a node whose other child has blend weight exactly 0 (near
+// child taken with t = 0 when it is the lhs, t = 1 when it is the rhs): equal
+// to blend_materials with any finite far material in every later use.
+__device__ DMat blend_with_far(const DMat& near_m, bool near_is_lhs, bool node_mixes_models) {
+  if (!node_mixes_models) return near_m;
+  DMat m;
+  m.kind = kBlendKind;
+  m.a_model = m.b_model = dom_model(near_m);
+  m.a = dom_params(near_m);
+  m.b = m.a;
+  m.t = near_is_lhs ? 0.0f : 1.0f;
+  return m;
+}
+
+__device__ __forceinline__ F3 emission_of(const DParams& p) { return p.emission_color * fmaxf(p.emission_strength, 0.0f); }
+// Material::emission (materials/mod.rs:284-296)
+__device__ F3 mat_emission(const DMat& m) {
+  if (m.kind != kBlendKind) return emission_of(m.a);
+  return lerp_sp(emission_of(m.a), emission_of(m.b), m.t);
+}
+
+constexpr float kPi = 3.14159265358979323846f;
+
+// metal.rs:7-20, 84-102
+__device__ float ggx_d(float ndoth, float alpha) {
+  float a2 = alpha * alpha, n2 = ndoth * ndoth;
+  float denom = fmaxf(n2 * (a2 - 1.0f) + 1.0f, 1.0e-5f);
+  return a2 / (kPi * denom * denom);
+}
+__device__ float smith_g1(float ndotx, float alpha) {
+  float k = (alpha * alpha) * 0.5f;
+  return ndotx / fmaxf(ndotx * (1.0f - k) + k, 1.0e-5f);
+}
+__device__ F3 metal_eval(F3 color, float roughness, F3 n, F3 wi, F3 wo) {
+  float ndotl = fmaxf(ftd::dot3(n, wi), 0.0f), ndotv = fmaxf(ftd::dot3(n, wo), 0.0f);
+  if (ndotl <= 0.0f || ndotv <= 0.0f) return f3(0.0f, 0.0f, 0.0f);
+  F3 h = ftd::normalize3(wi + wo);
+  float ndoth = fmaxf(ftd::dot3(n, h), 0.0f), vdoth = fmaxf(ftd::dot3(wo, h), 0.0f);
+  float rr = ftd::rclamp(roughness, 0.02f, 1.0f);
+  float alpha = rr * rr;
+  float d = ggx_d(ndoth, alpha);
+  float g = smith_g1(ndotl, alpha) * smith_g1(ndotv, alpha);
+  float x = 1.0f - clamp01(vdoth);
+  float m5 = x * x * x * x * x;
+  F3 fres = color + f3(m5, m5, m5) + color * (-m5);
+  return fres * ((d * g) / fmaxf(4.0f * ndotl * ndotv, 1.0e-5f));
+}
+__device__ float f0_from_ior(float ior) {
+  float i = fmaxf(ior, 1.0e-3f);
+  float r = (i - 1.0f) / (i + 1.0f);
+  return r * r;
+}
+// standard.rs:6-43, 170-183
+__device__ F3 standard_eval(const DParams& m, F3 n, F3 wi, F3 wo) {
+  float ndotl = fmaxf(ftd::dot3(n, wi), 0.0f), ndotv = fmaxf(ftd::dot3(n, wo), 0.0f);
+  if (ndotl <= 0.0f || ndotv <= 0.0f) return f3(0.0f, 0.0f, 0.0f);
+  float metallic = clamp01(m.metallic), transmission = clamp01(m.transmission), clearcoat = clamp01(m.clearcoat);
+  float cx = clamp01(1.0f - clamp01(ndotv));
+  float x2 = cx * cx;
+  float sw = x2 * x2 * cx;
+  float coat = ftd::rclamp(clearcoat * (0.2f + 0.8f * sw) * 0.65f, 0.0f, 0.95f);
+  float base_kd = clamp01((1.0f - metallic) * (1.0f - transmission)) * (1.0f - coat);
+  F3 diffuse = m.color * (base_kd / kPi);
+  float f0d = clamp01(f0_from_ior(m.ior));
+  F3 base_f0 = mul3(f3(f0d, f0d, f0d) * (clamp01(m.specular) * clamp01(m.specular_weight)), m.spec_color);
+  F3 spec_f0 = base_f0 * (1.0f - metallic) + m.color * metallic;
+  F3 specular = metal_eval(spec_f0, m.roughness, n, wi, wo) * (1.0f - coat * 0.85f);
+  F3 cc = f3(0.0f, 0.0f, 0.0f);
+  if (clearcoat > 1.0e-5f)
+    cc = metal_eval(f3(1.0f, 1.0f, 1.0f), ftd::rclamp(m.clearcoat_roughness, 0.02f, 1.0f), n, wi, wo) *
+         (clearcoat * 0.18f);
+  return diffuse + specular + cc;
+}
+__device__ F3 model_eval(int model, const DParams& p, F3 n, F3 wi, F3 wo) {
+  switch (model) {
+    case FT_MAT_STANDARD: return standard_eval(p, n, wi, wo);
+    case FT_MAT_LAMBERT:
+      return ftd::dot3(n, wi) <= 0.0f ? f3(0.0f, 0.0f, 0.0f) : p.color * (1.0f / kPi);  // lambert.rs:7-13
+    case FT_MAT_METAL: return metal_eval(p.color, p.roughness, n, wi, wo);
+    default: return f3(0.0f, 0.0f, 0.0f);  // dielectric.rs:5-7
+  }
+}
+// Material::eval (materials/mod.rs:298-310)
+__device__ F3 mat_eval(const DMat& m, F3 n, F3 wi, F3 wo) {
+  if (m.kind != kBlendKind) return model_eval(m.kind, m.a, n, wi, wo);
+  return lerp_sp(model_eval(m.a_model, m.a, n, wi, wo), model_eval(m.b_model, m.b, n, wi, wo), m.t);
+}
+
+// smoothstepf (R:7538-7541) of the blend weight (R:4540-4545, R:7105-7110)
+__device__ __forceinline__ float blend_weight(float l, float r, float radius, bool diff) {
+  float k = fmaxf(fabsf(radius), 1.0e-6f);
+  float x = diff ? 0.5f + 0.5f * (((-r) - l) / k) : 0.5f + 0.5f * ((l - r) / k);
+  float t = clamp01(x / fmaxf(1.0f, 1.0e-6f));
+  return t * t * (3.0f - 2.0f * t);
+}
+
+__device__ bool blend_kind(int kind, bool* diff) {
+  switch (kind) {
+    case FT_NODE_UNION_ROUND: case FT_NODE_UNION_CHAMFER: case FT_NODE_UNION_SOFT: case FT_NODE_INTERSECT_ROUND:
+    case FT_NODE_INTERSECT_CHAMFER: case FT_NODE_UNION_COLUMNS: case FT_NODE_UNION_STAIRS:
+    case FT_NODE_INTERSECT_COLUMNS: case FT_NODE_INTERSECT_STAIRS:
+      *diff = false;
+      return true;
+    case FT_NODE_DIFF_ROUND: case FT_NODE_DIFF_CHAMFER: case FT_NODE_DIFF_COLUMNS: case FT_NODE_DIFF_STAIRS:
+    case FT_NODE_PIPE: case FT_NODE_ENGRAVE: case FT_NODE_GROOVE: case FT_NODE_TONGUE:
+      *diff = true;
+      return true;
+    default: return false;
+  }
+}
+__device__ __forceinline__ float blend_radius(const DevNode& n) {
+  return (n.kind == FT_NODE_GROOVE || n.kind == FT_NODE_TONGUE) ? fmaxf(n.f[0], n.f[1]) : n.f[0];
+}
+
+// blend_surface_normals' combination (R:4529-4552)
+__device__ F3 blend_normals(F3 left, F3 right, float t, bool diff) {
+  if (diff) right = right * -1.0f;
+  F3 m = left * (1.0f - t) + right * t;
+  if (ftd::len3(m) > 1.0e-6f) return ftd::normalize3(m);
+  return t < 0.5f ? left : right;
+}
+
+// estimate_node_normal (R:4554-4570) of one primitive.
+__device__ F3 prim_normal(const DevNode& n, F3 p) {
+  const float e = kNormalEps;
+  F3 k1 = f3(1.0f, -1.0f, -1.0f), k2 = f3(-1.0f, -1.0f, 1.0f), k3 = f3(-1.0f, 1.0f, -1.0f), k4 = f3(1.0f, 1.0f, 1.0f);
+  F3 nn = k1 * ftd::prim_distance(n, p + k1 * e) + k2 * ftd::prim_distance(n, p + k2 * e) +
+          k3 * ftd::prim_distance(n, p + k3 * e) + k4 * ftd::prim_distance(n, p + k4 * e);
+  return ftd::len3(nn) > 1.0e-6f ? ftd::normalize3(nn) : f3(0.0f, 1.0f, 0.0f);
+}
+
+// Result of resolving a hit against the tree: geometric normal (not yet
+// oriented to the front face), material, and the optional root split.
+struct Resolved {
+  F3 normal;
+  DMat m;      // material (or the split's left material)
+  DMat mb;     // split's right material
+  float t;     // split weight
+  bool split;
+  bool ok;
+};
+
+// ---------------------------------------------------------------- generic leaves
+struct GEntry {
+  float d;
+  F3 n;
+  DMat m;
+};
+
+// Post-order over a generic leaf's node tree: each node's value at p, its
+// resolved normal and material (R:4462-4552, R:6945-7113).  Subtree values of
+// modifiers come from their postfix op range.
+template <bool kStats>
+__device__ __noinline__ void resolve_generic(const DevScene& S, int root, F3 p, Resolved* out, Ctx<kStats>& cx) {
+  GEntry st[8];
+  int sp = 0;
+  int node_stack[24];
+  unsigned char stage[24];
+  int top = 0;
+  node_stack[0] = root;
+  stage[0] = 0;
+  out->ok = false;
+  out->split = false;
+  while (top >= 0) {
+    int ni = node_stack[top];
+    const DevNode& n = S.nodes[ni];
+    bool is_prim = n.kind <= FT_NODE_EXTRUDE_POLYGON;
+    bool unary = n.kind == FT_NODE_DOMAIN || n.kind == FT_NODE_DISTANCE_POST || n.kind == FT_NODE_NOISE ||
+                 n.kind == FT_NODE_SLICE || n.kind == FT_NODE_SMOOTH;
+    int nchild = is_prim ? 0 : (unary ? 1 : 2);
+    if (stage[top] < nchild) {
+      int c = stage[top] == 0 ? n.a : n.b;
+      ++stage[top];
+      if (top + 1 >= 24 || sp + 2 > 8) return;  // deeper than supported: leave out->ok false
+      ++top;
+      node_stack[top] = c;
+      stage[top] = 0;
+      continue;
+    }
+    GEntry e;
+    if (is_prim) {
+      e.d = ftd::prim_distance(n, p);
+      e.n = prim_normal(n, p);
+      e.m = mat_of_id(S, n.material_id);
+    } else if (n.kind == FT_NODE_DOMAIN || n.kind == FT_NODE_DISTANCE_POST || n.kind == FT_NODE_NOISE) {
+      GEntry base = st[--sp];
+      int b = S.node_op_begin[ni], c = S.node_op_end[ni] - S.node_op_begin[ni];
+      const float ee = kNormalEps;
+      F3 k1 = f3(1.0f, -1.0f, -1.0f), k2 = f3(-1.0f, -1.0f, 1.0f), k3 = f3(-1.0f, 1.0f, -1.0f),
+         k4 = f3(1.0f, 1.0f, 1.0f);
+      e.d = eval_generic(S, b, c, p, cx).d;
+      F3 nn = k1 * eval_generic(S, b, c, p + k1 * ee, cx).d + k2 * eval_generic(S, b, c, p + k2 * ee, cx).d +
+              k3 * eval_generic(S, b, c, p + k3 * ee, cx).d + k4 * eval_generic(S, b, c, p + k4 * ee, cx).d;
+      e.n = ftd::len3(nn) > 1.0e-6f ? ftd::normalize3(nn) : f3(0.0f, 1.0f, 0.0f);
+      e.m = base.m;  // modifiers resolve the base's material (R:6990-6993)
+    } else if (n.kind == FT_NODE_SLICE || n.kind == FT_NODE_SMOOTH) {
+      e = st[--sp];
+      if (n.kind == FT_NODE_SMOOTH) {
+        e.d -= n.f[0] * 0.1f;
+      } else {
+        float coord = n.ival == 0 ? p.x : (n.ival == 1 ? p.y : p.z);
+        e.d = ftd::rmax(e.d, ftd::rmax(n.f[0] - coord, coord - n.f[1]));
+      }
+    } else {
+      GEntry r = st[--sp];
+      GEntry l = st[--sp];
+      Info li{l.d, 0u, 0u}, ri{r.d, 0u, 0u};
+      float d = ftd::combine(n.kind, n.f[0], n.f[1], li, ri).d;
+      bool diff;
+      if (n.kind == FT_NODE_UNION) {
+        e = l.d <= r.d ? l : r;
+      } else if (n.kind == FT_NODE_INTERSECT) {
+        e = l.d >= r.d ? l : r;
+      } else if (n.kind == FT_NODE_SUBTRACT) {
+        if (l.d >= -r.d) {
+          e = l;
+        } else {
+          e = r;
+          e.n = r.n * -1.0f;
+        }
+      } else if (blend_kind(n.kind, &diff)) {
+        float t = blend_weight(l.d, r.d, blend_radius(n), diff);
+        e.n = blend_normals(l.n, r.n, t, diff);
+        if (top == 0) {  // smooth boolean at the leaf root: material split
+          out->m = l.m;
+          out->mb = r.m;
+          out->t = t;
+          out->split = true;
+        }
+        e.m = blend_materials(l.m, r.m, t);
+      } else {
+        e = l;
+      }
+      e.d = d;
+    }
+    st[sp++] = e;
+    --top;
+  }
+  out->normal = st[0].n;
+  if (!out->split) out->m = st[0].m;
+  out->ok = true;
+}
+
+// ---------------------------------------------------------------- union_round trees
+// Gather the primitives within `reach` of p (exact distances) through the
+// tree's BVH.  Returns false when more than kGather qualify.
+__device__ bool ur_gather(const DevScene& S, const DevUrTree& t, F3 p, float reach, int* pos, float* dist, int* n) {
+  int stack[48];
+  int sp = 0;
+  *n = 0;
+  stack[sp++] = t.bvh_root;
+  while (sp > 0) {
+    const DevUrBvh& bn = S.ur_bvh[stack[--sp]];
+    if (node_lb(p, bn.bmin, bn.bmax) >= reach) continue;
+    if (bn.prim_count > 0) {
+      for (int k = 0; k < bn.prim_count; ++k) {
+        int ps = S.ur_bvh_prims[bn.prim_begin + k];
+        const DevNode& pn = S.nodes[S.ur_prims[t.prim_first + ps]];
+        if (node_lb(p, pn.bmin, pn.bmax) >= reach) continue;
+        float d = ftd::prim_distance(pn, p);
+        if (d < reach) {
+          if (*n >= kGather) return false;
+          pos[*n] = ps;
+          dist[*n] = d;
+          ++*n;
+        }
+      }
+      continue;
+    }
+    if (sp + 2 > 48) return false;
+    stack[sp++] = bn.left;
+    stack[sp++] = bn.right;
+  }
+  return true;
+}
+
+// Exact value of the union_round subtree `c` (inner index, or -(pos + 1) for
+// a primitive) at p from the gathered primitives; kInf when it holds none
+// (its true value is then >= reach).  Primitives outside the gather are >= the
+// reach, which keeps every union_round on the fold's path exact.
+__device__ float ur_subtree_value(const DevScene& S, const DevUrTree& t, int c, const int* gpos, const float* gdist,
+                                  int ng) {
+  auto prim_value = [&](int ps) {
+    for (int k = 0; k < ng; ++k)
+      if (gpos[k] == ps) return gdist[k];
+    return kInf;
+  };
+  if (c < 0) return prim_value(-c - 1);
+  auto has = [&](int in) {
+    const DevUrInner& u = S.ur_inner[in];
+    for (int k = 0; k < ng; ++k)
+      if (gpos[k] >= u.lo && gpos[k] < u.hi) return true;
+    return false;
+  };
+  if (!has(c)) return kInf;
+  struct VF {
+    int inner, stage;
+    float v[2];
+  };
+  VF fr[24];
+  int fp = 0;
+  fr[0].inner = c;
+  fr[0].stage = 0;
+  for (;;) {
+    VF& F = fr[fp];
+    if (F.stage < 2) {
+      int ch = S.ur_inner[F.inner].child[F.stage];
+      if (ch < 0) {
+        F.v[F.stage++] = prim_value(-ch - 1);
+        continue;
+      }
+      if (!has(ch)) {
+        F.v[F.stage++] = kInf;
+        continue;
+      }
+      if (fp + 1 >= 24) return kInf;  // deeper than supported; the caller widens and falls back
+      ++F.stage;
+      ++fp;
+      fr[fp].inner = ch;
+      fr[fp].stage = 0;
+      continue;
+    }
+    float v = (F.v[0] == kInf && F.v[1] == kInf)
+                  ? kInf
+                  : ftd::combine(FT_NODE_UNION_ROUND, t.r, 0.0f, Info{F.v[0], 0u, 0u}, Info{F.v[1], 0u, 0u}).d;
+    if (fp == 0) return v;
+    --fp;
+    fr[fp].v[fr[fp].stage - 1] = v;
+  }
+}
+
+struct NEntry {
+  F3 n;
+  DMat m;
+};
+
+// Top-down resolution over the nodes with nonzero blend weight.  Each visited
+// node gets both child values from exact restricted folds, hence its exact
+// weight t; a child with weight exactly 0 is skipped.  A child without
+// gathered primitives is provably weightless when reach >= (other value) + r;
+// otherwise *need receives the reach required.
+__device__ __noinline__ bool resolve_urtree_reach(const DevScene& S, const DevUrTree& t, F3 p, float reach,
+                                                  Resolved* out, float* need) {
+  int gpos[kGather];
+  float gdist[kGather];
+  int ng = 0;
+  if (!ur_gather(S, t, p, reach, gpos, gdist, &ng)) {
+    *need = -1.0f;
+    return false;
+  }
+  struct Frame {
+    int inner, stage;
+    float tw;
+    bool useL, useR;
+    NEntry slot[2];
+  };
+  Frame fr[20];
+  int fp = 0;
+  const float r = t.r;
+  // Set up a frame: child values, exact weight, which children carry weight.
+  auto open = [&](int fi, int inner) -> bool {
+    Frame& F = fr[fi];
+    F.inner = inner;
+    F.stage = 0;
+    const DevUrInner& u = S.ur_inner[inner];
+    float vL = ur_subtree_value(S, t, u.child[0], gpos, gdist, ng);
+    float vR = ur_subtree_value(S, t, u.child[1], gpos, gdist, ng);
+    if (vL == kInf && vR == kInf) {
+      *need = -1.0f;
+      return false;
+    }
+    if (vL == kInf || vR == kInf) {
+      float vn = vL == kInf ? vR : vL;
+      if (reach < vn + r) {
+        *need = vn + r;
+        return false;
+      }
+    }
+    F.tw = blend_weight(vL, vR, r, false);
+    F.useL = F.tw != 1.0f;
+    F.useR = F.tw != 0.0f;
+    return true;
+  };
+  if (!open(0, t.inner_root)) return false;
+  for (;;) {
+    Frame& F = fr[fp];
+    if (F.stage < 2) {
+      bool use = F.stage == 0 ? F.useL : F.useR;
+      int c = S.ur_inner[F.inner].child[F.stage];
+      if (!use) {
+        ++F.stage;
+        continue;
+      }
+      if (c < 0) {
+        const DevNode& pn = S.nodes[S.ur_prims[t.prim_first + (-c - 1)]];
+        F.slot[F.stage].n = prim_normal(pn, p);
+        F.slot[F.stage].m = mat_of_id(S, pn.material_id);
+        ++F.stage;
+        continue;
+      }
+      if (fp + 1 >= 20) {
+        *need = -1.0f;
+        return false;
+      }
+      ++F.stage;
+      ++fp;
+      if (!open(fp, c)) return false;
+      continue;
+    }
+    NEntry res;
+    bool mixes = S.ur_inner_blend[F.inner] != 0;
+    if (F.useL && F.useR) {
+      res.n = blend_normals(F.slot[0].n, F.slot[1].n, F.tw, false);
+      res.m = blend_materials(F.slot[0].m, F.slot[1].m, F.tw);
+    } else {
+      const NEntry& e = F.useL ? F.slot[0] : F.slot[1];
+      res.n = blend_normals(e.n, e.n, F.tw, false);
+      res.m = blend_with_far(e.m, F.useL, mixes);
+    }
+    if (fp == 0) {
+      out->normal = res.n;
+      out->t = F.tw;
+      out->split = true;
+      out->m = F.useL ? F.slot[0].m : F.slot[1].m;
+      out->mb = F.useR ? F.slot[1].m : F.slot[0].m;
+      out->ok = true;
+      return true;
+    }
+    --fp;
+    fr[fp].slot[fr[fp].stage - 1] = res;
+  }
+}
+
+__device__ void resolve_urtree(const DevScene& S, const DevUrTree& t, F3 p, Resolved* out) {
+  float reach = 3.0f * t.r;
+  out->ok = false;
+  for (int attempt = 0; attempt < 6; ++attempt) {
+    float need = 0.0f;
+    if (resolve_urtree_reach(S, t, p, reach, out, &need)) return;
+    if (need < 0.0f) return;  // capacity exceeded
+    reach = fmaxf(1.5f * reach, need * 1.0001f + 1.0e-6f);
+  }
+}
+
+// Normal and material at a hit on leaf `li`.
+template <bool kStats>
+__device__ void resolve_hit(const DevScene& S, int li, F3 p, Resolved* out, Ctx<kStats>& cx) {
+  const DevLeaf& lf = S.leaves[li];
+  out->split = false;
+  out->ok = false;
+  if (lf.kind == ftgpu::kLeafPrim) {
+    const DevNode& n = S.nodes[lf.node];
+    out->normal = prim_normal(n, p);
+    out->m = mat_of_id(S, n.material_id);
+    out->ok = true;
+    return;
+  }
+  if (lf.kind == ftgpu::kLeafUrTree) {
+    resolve_urtree(S, S.urtrees[lf.first], p, out);
+    if (out->ok) return;
+  }
+  resolve_generic(S, lf.node, p, out, cx);
+}
+
+// ---------------------------------------------------------------- lights and shadows
+// Accelerator::lower_bound over the leaf BVH (bvh_lower_bound, R:788-822):
+// the nearest leaf box.
+__device__ float scene_lower_bound(const DevScene& S, F3 p) {
+  float best = kInf;
+  int stack[64];
+  float slb[64];
+  int sp = 0;
+  stack[0] = S.bvh_root;
+  slb[0] = node_lb(p, S.bvh[S.bvh_root].bmin, S.bvh[S.bvh_root].bmax);
+  sp = 1;
+  while (sp > 0) {
+    --sp;
+    if (slb[sp] > best) continue;
+    const DevBvhNode& n = S.bvh[stack[sp]];
+    if (n.leaf >= 0) {
+      best = fminf(best, slb[sp]);
+      continue;
+    }
+    if (sp + 2 > 64) break;
+    float ll = node_lb(p, S.bvh[n.lhs].bmin, S.bvh[n.lhs].bmax), rl = node_lb(p, S.bvh[n.rhs].bmin, S.bvh[n.rhs].bmax);
+    if (ll <= rl) {
+      stack[sp] = n.rhs; slb[sp] = rl; ++sp;
+      stack[sp] = n.lhs; slb[sp] = ll; ++sp;
+    } else {
+      stack[sp] = n.lhs; slb[sp] = ll; ++sp;
+      stack[sp] = n.rhs; slb[sp] = rl; ++sp;
+    }
+  }
+  return best;
+}
+
+// shadow_visibility (R:4706-4733)
+template <bool kStats>
+__device__ float shadow_visibility(const DevScene& S, F3 o, F3 d, float max_t, float eps, Ctx<kStats>& cx) {
+  float t = eps * 2.0f;
+  float vis = 1.0f;
+  for (int i = 0; i < 80; ++i) {
+    if (t >= max_t) return clamp01(vis);
+    F3 p = o + d * t;
+    float lower = fabsf(scene_lower_bound(S, p));
+    float h = lower > fmaxf(eps * 8.0f, 0.02f) ? lower : fabsf(scene_distance(S, p, cx).d);
+    if (h < eps * 4.0f) return 0.0f;
+    vis = fminf(vis, clamp01(10.0f * h / t));
+    t += fmaxf(h, eps * 2.0f);
+  }
+  return clamp01(vis);
+}
+
+// Light::sample_li_indexed (render_api.rs:172-259)
+__device__ void sample_light(const ft_light& L, F3 p, uint32_t idx, uint32_t count, F3* wi, F3* rad, float* dist) {
+  F3 inten = f3(L.intensity[0], L.intensity[1], L.intensity[2]);
+  if (L.kind == FT_LIGHT_ENV) {
+    *wi = f3(0.0f, 1.0f, 0.0f);
+    *rad = inten;
+    *dist = kInf;
+    return;
+  }
+  F3 lp = f3(L.position[0], L.position[1], L.position[2]);
+  F3 target = lp;
+  if (L.kind == FT_LIGHT_SPHERE && L.radius > 1.0e-5f) {
+    F3 nrm = ftd::normalize3(p - lp);
+    F3 up = fabsf(nrm.y) < 0.99f ? f3(0.0f, 1.0f, 0.0f) : f3(1.0f, 0.0f, 0.0f);
+    auto cross3 = [](F3 a, F3 b) { return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); };
+    F3 tangent = ftd::normalize3(cross3(nrm, up));
+    F3 bit = ftd::normalize3(cross3(tangent, nrm));
+    uint32_t nsm = count > 0 ? count : 1u;
+    float u = (static_cast<float>(idx) + 0.5f) / static_cast<float>(nsm);  // hammersley_2d (render_api.rs:262-272)
+    uint32_t bits = (idx >> 16) | (idx << 16);
+    bits = ((bits & 0x55555555u) << 1) | ((bits & 0xAAAAAAAAu) >> 1);
+    bits = ((bits & 0x33333333u) << 2) | ((bits & 0xCCCCCCCCu) >> 2);
+    bits = ((bits & 0x0F0F0F0Fu) << 4) | ((bits & 0xF0F0F0F0u) >> 4);
+    bits = ((bits & 0x00FF00FFu) << 8) | ((bits & 0xFF00FF00u) >> 8);
+    float v = static_cast<float>(bits) * 2.3283064e-10f;
+    float sx = 2.0f * u - 1.0f, sy = 2.0f * v - 1.0f;  // concentric_disk_sample (render_api.rs:274-289)
+    float dx = 0.0f, dy = 0.0f;
+    if (!(fabsf(sx) <= 1.1920929e-7f && fabsf(sy) <= 1.1920929e-7f)) {
+      float rr, th;
+      if (fabsf(sx) > fabsf(sy)) {
+        rr = sx;
+        th = 0.78539816339744830962f * (sy / sx);
+      } else {
+        rr = sy;
+        th = 1.57079632679489661923f - 0.78539816339744830962f * (sx / sy);
+      }
+      dx = rr * cosf(th);
+      dy = rr * sinf(th);
+    }
+    target = lp + tangent * (dx * L.radius) + bit * (dy * L.radius);
+  }
+  F3 to = target - p;
+  float dd = fmaxf(ftd::len3(to), 1.0e-4f);
+  *wi = to * (1.0f / dd);
+  *rad = inten * (1.0f / (dd * dd));
+  *dist = dd;
+}
+
+// offset_ray_origin (R:5067-5078)
+__device__ F3 offset_origin(F3 pos, F3 gn, F3 dir, float eps) {
+  F3 n = ftd::len3(gn) > 1.0e-8f ? ftd::normalize3(gn) : ftd::normalize3(dir);
+  float sign = ftd::dot3(dir, n) >= 0.0f ? 1.0f : -1.0f;
+  F3 no = n * (sign * fmaxf(eps * 16.0f, 2.0e-4f));
+  float step = fmaxf(eps * 8.0f, 1.0e-4f);
+  return pos + no + ftd::normalize3(dir) * step;
+}
+
+// shade_color (R:4217-4276)
+template <bool kStats>
+__device__ F3 shade_color(const DevScene& S, const DMat& mat, F3 pos, F3 gn, F3 n_shade, F3 wo, float eps,
+                          float max_dist, Ctx<kStats>& cx) {
+  if (S.n_lights == 0) return f3(1.0f, 1.0f, 1.0f);
+  F3 n = ftd::normalize3(n_shade);
+  F3 color = f3(0.0f, 0.0f, 0.0f);
+  for (int li = 0; li < S.n_lights; ++li) {
+    const ft_light& L = S.lights[li];
+    uint32_t samples = L.kind == FT_LIGHT_SPHERE ? (L.samples > 0 ? L.samples : 1u) : 1u;
+    float inv = 1.0f / static_cast<float>(samples);
+    for (uint32_t s = 0; s < samples; ++s) {
+      F3 wi, rad;
+      float dist;
+      sample_light(L, pos, s, samples, &wi, &rad, &dist);
+      wi = ftd::normalize3(wi);
+      float ndotl = n.x * wi.x + n.y * wi.y + n.z * wi.z;
+      if (ndotl <= 0.0f) continue;
+      F3 so = offset_origin(pos, gn, wi, eps);
+      float max_t = isfinite(dist) ? fmaxf(dist - eps * 8.0f, 0.0f) : max_dist;
+      if (max_t <= 0.0f) continue;
+      float vis = shadow_visibility(S, so, wi, max_t, eps, cx);
+      if (vis <= 0.0f) continue;
+      F3 f = mat_eval(mat, n_shade, wi, wo);
+      color = color + mul3(f, rad) * (ndotl * vis * inv);
+    }
+  }
+  return color;
+}
+
+// fresnel_dielectric_scalar (R:5188-5204)
+__device__ float fresnel_dielectric(float ci, float eta_i, float eta_t) {
+  float ei = fmaxf(eta_i, 1.0e-4f), et = fmaxf(eta_t, 1.0e-4f);
+  if (fabsf(ei - et) < 1.0e-6f) return 0.0f;
+  ci = clamp01(ci);
+  float eta = ei / et;
+  float sin2 = eta * eta * (1.0f - ci * ci);
+  if (sin2 >= 1.0f) return 1.0f;
+  float ct = sqrtf(1.0f - sin2);
+  float rs = ((ei * ci) - (et * ct)) / fmaxf((ei * ci) + (et * ct), 1.0e-6f);
+  float rp = ((et * ci) - (ei * ct)) / fmaxf((et * ci) + (ei * ct), 1.0e-6f);
+  return 0.5f * (rs * rs + rp * rp);
+}
+
+// refract (R:5080-5095)
+__device__ bool refract_dir(F3 inc, F3 nrm, float eta, F3* out) {
+  F3 i = ftd::normalize3(inc);
+  F3 n = ftd::normalize3(nrm);
+  float cosi = ftd::rclamp(ftd::dot3(i, n), -1.0f, 1.0f);
+  if (cosi > 0.0f) n = n * -1.0f;
+  else cosi = -cosi;
+  float sin2 = eta * eta * (1.0f - cosi * cosi);
+  if (sin2 > 1.0f) return false;
+  float cost = sqrtf(1.0f - sin2);
+  *out = ftd::normalize3(i * eta + n * (eta * cosi - cost));
+  return true;
+}
+
+struct MediumD {
+  float ior;
+  F3 absorption;
+  float density;
+};
+__device__ __forceinline__ MediumD air() { return MediumD{1.0f, f3(1.0f, 1.0f, 1.0f), 0.0f}; }
+
+// medium_transmittance (R:5109-5119)
+__device__ F3 transmittance(const MediumD& m, float dist) {
+  if (m.density <= 0.0f || dist <= 0.0f) return f3(1.0f, 1.0f, 1.0f);
+  float e = m.density * fmaxf(dist, 0.0f);
+  return f3(powf(clamp01(m.absorption.x), e), powf(clamp01(m.absorption.y), e), powf(clamp01(m.absorption.z), e));
+}
+
+// transition_medium (R:5147-5175) for materials without an explicit medium
+__device__ MediumD transition(const DMat& m, bool front, MediumD cur) {
+  int model = dom_model(m);
+  const DParams& p = dom_params(m);
+  bool transmissive = model == FT_MAT_DIELECTRIC || (model == FT_MAT_STANDARD && p.transmission > 0.01f);
+  if (!transmissive) return cur;
+  if (front) return MediumD{ftd::rclamp(p.ior, 1.0f, 3.0f), f3(1.0f, 1.0f, 1.0f), 0.0f};
+  return air();
+}
+
+struct RayJob {
+  F3 o, d, w;  // origin, direction, throughput
+  MediumD med;
+  int depth;
+};
+
+struct TraceParams {
+  RayParams P;
+  uint32_t max_depth;
+};

@@ -66,6 +66,25 @@ class Builder {
     img_->has_camera = d_.has_camera;
     img_->programs.assign(d_.programs, d_.programs + d_.n_programs);
     img_->instrs.assign(d_.instrs, d_.instrs + d_.n_instrs);
+    img_->materials.assign(d_.materials, d_.materials + d_.n_materials);
+    img_->lights.assign(d_.lights, d_.lights + d_.n_lights);
+    img_->environment_program = d_.environment_program;
+    if (img_->materials.empty()) {  // default_material (R:7937-7953)
+      ft_material m;
+      std::memset(&m, 0, sizeof(m));
+      m.kind = FT_MAT_STANDARD;
+      m.color_program = -1;
+      m.color[0] = m.color[1] = m.color[2] = 0.8f;
+      m.roughness = 0.5f;
+      m.ior = 1.5f;
+      m.specular = 0.5f;
+      m.specular_weight = 1.0f;
+      m.specular_color[0] = m.specular_color[1] = m.specular_color[2] = 1.0f;
+      m.clearcoat_roughness = 0.1f;
+      img_->materials.push_back(m);
+    }
+    img_->node_op_begin.assign(d_.n_nodes, -1);
+    img_->node_op_end.assign(d_.n_nodes, -1);
 
     collect_leaves(d_.root);
     std::vector<size_t> idx(img_->leaves.size());
@@ -126,6 +145,24 @@ class Builder {
           return fail("distance_post hook must map (f32, vec3) -> f32");
       }
       if (n.kind == FT_NODE_SLICE && (n.ival < 0 || n.ival > 2)) return fail("slice axis out of range");
+    }
+    if (d_.environment_program >= 0) {
+      if (static_cast<uint32_t>(d_.environment_program) >= d_.n_programs)
+        return fail("environment program index out of range");
+      const ft_program& p = d_.programs[d_.environment_program];
+      if (p.n_params != 1 || p.param_is_vec3 != 1u || !p.result_is_vec3)
+        return fail("environment color program must map vec3 -> vec3");
+    }
+    if (d_.n_lights && !d_.lights) return fail("lights pointer is null");
+    if (d_.n_materials && !d_.materials) return fail("materials pointer is null");
+    for (uint32_t i = 0; i < d_.n_lights; ++i) {
+      if (d_.lights[i].kind < FT_LIGHT_POINT || d_.lights[i].kind > FT_LIGHT_SPHERE)
+        return fail("light " + std::to_string(i) + " has an unknown kind");
+      if (d_.lights[i].samples > 4096) return fail("light " + std::to_string(i) + " has too many samples");
+    }
+    for (uint32_t i = 0; i < d_.n_materials; ++i) {
+      if (d_.materials[i].kind < FT_MAT_STANDARD || d_.materials[i].kind > FT_MAT_DIELECTRIC)
+        return fail("material " + std::to_string(i) + " has an unknown kind");
     }
     // The node graph must be a DAG reachable from the root (no cycles).
     std::vector<char> state(d_.n_nodes, 0);
@@ -273,7 +310,17 @@ class Builder {
   }
 
   // Postfix program over a leaf's node tree; tracks stack depths.
+  // Postfix ops of every subtree are contiguous: record each node's range so a
+  // shading pass can re-evaluate any subtree at arbitrary points.
   bool emit_generic(int i, int vdepth, int pdepth, int* vmax, int* pmax) {
+    int32_t begin = static_cast<int32_t>(img_->gops.size());
+    bool ok = emit_generic_ops(i, vdepth, pdepth, vmax, pmax);
+    img_->node_op_begin[i] = begin;
+    img_->node_op_end[i] = static_cast<int32_t>(img_->gops.size());
+    return ok;
+  }
+
+  bool emit_generic_ops(int i, int vdepth, int pdepth, int* vmax, int* pmax) {
     const ft_node& n = d_.nodes[i];
     auto op = [&](uint32_t code) { img_->gops.push_back((code << kGOpShift) | static_cast<uint32_t>(i)); };
     *pmax = std::max(*pmax, pdepth);
@@ -401,6 +448,12 @@ class Builder {
     img_->ur_bvh[self].left = l;
     img_->ur_bvh[self].right = r;
     return self;
+  }
+
+  // material_for_id (R:6895-6900): out-of-range ids fall back to material 0.
+  int material_kind(uint32_t id) const {
+    if (img_->materials.empty()) return FT_MAT_STANDARD;
+    return img_->materials[id < img_->materials.size() ? id : 0].kind;
   }
 
   // Radius of a ball around the primitive's centre that lies inside the solid
@@ -543,6 +596,19 @@ class Builder {
     };
     t.inner_root = walk(leaf.node);
     t.n_prims = static_cast<int32_t>(img_->ur_prims.size()) - t.prim_first;
+    // Static material-model mixing of each inner node's primitives.
+    img_->ur_inner_blend.resize(img_->ur_inner.size(), 0);
+    for (size_t in = static_cast<size_t>(t.inner_root); in < img_->ur_inner.size(); ++in) {
+      const HostUrInner& u = img_->ur_inner[in];
+      int model = -1;
+      int32_t mixed = 0;
+      for (int k = u.lo; k < u.hi; ++k) {
+        int mk = material_kind(img_->nodes[img_->ur_prims[t.prim_first + k]].material_id);
+        if (model < 0) model = mk;
+        else if (mk != model) mixed = 1;
+      }
+      img_->ur_inner_blend[in] = mixed;
+    }
     std::vector<int32_t> pos(t.n_prims);
     std::iota(pos.begin(), pos.end(), 0);
     t.bvh_root = build_ur_bvh(pos, 0, pos.size(), t.prim_first);

@@ -105,6 +105,13 @@ struct SceneImage {
   std::vector<HostUrInner> ur_inner;
   std::vector<uint32_t> ur_cell_offsets;  // per grid cell: begin into ur_cell_prims
   std::vector<int32_t> ur_cell_prims;     // in-order primitive positions
+  // per ur_inner node: 1 when its primitives use more than one material model
+  // (blend_materials then yields a Blend whatever the weights)
+  std::vector<int32_t> ur_inner_blend;
+  std::vector<int32_t> node_op_begin, node_op_end;  // postfix op range of each node's subtree
+  std::vector<ft_material> materials;
+  std::vector<ft_light> lights;
+  int32_t environment_program = -1;
   std::vector<ft_program> programs;
   std::vector<ft_instr> instrs;
   float scene_min[3], scene_max[3];

@@ -335,6 +335,17 @@ ft_status ft_render_depth(ft_scene* scene, const ft_render_options* options,
                           uint32_t* material_out, float* normal_out,
                           uint8_t* rgb8_out, uint32_t flags, void* stream);
 
+/* Whitted trace: `render_ray_progressive_with_accel` (R:1201-1236) /
+ * `trace_ray_recursive` (crates/forgedthoughts/src/renderer/ray.rs:3-222)
+ * without the tile callback.  max_depth is RaySettings::max_depth (1..10).
+ * Outputs (each nullable):
+ *   rgb_out   width*height*3 floats, linear radiance averaged over AA samples
+ *   rgb8_out  width*height*3 bytes, Reinhard + gamma 2.2 (R:5229-5239)
+ * Other arguments as ft_render_depth. */
+ft_status ft_render_trace(ft_scene* scene, const ft_render_options* options,
+                          ft_accel_mode accel, uint32_t aa_samples, uint32_t max_depth,
+                          float* rgb_out, uint8_t* rgb8_out, uint32_t flags, void* stream);
+
 /* Kernel statistics of the last render on this scene: number of distance
  * evaluations, primitive evaluations and culling-box tests, summed over all
  * rays (used for the FP32 roofline). */
