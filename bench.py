@@ -1,17 +1,25 @@
 #!/usr/bin/env python3
-"""Benchmark of the GB300 depth march.
+"""Benchmark of the GB300 sphere-tracing path.
 
-Workload (default): 1920x1080 frame, 2x2 deterministic AA grid (8,294,400
-primary samples per step), a 512-primitive balanced union_round(0.1) tree over
-a ground box, march with max 256 steps / eps 1e-4 / max dist 100 / step scale
-0.7, Bricks accelerator semantics.  A step is one full frame: refined hit
-distance, hit mask, material id, estimate_normal and the gray depth preview.
+Workload (default, ``--mode trace``): the 512-primitive union_round field
+(balanced union_round(0.1) tree of spheres and rotated boxes over a ground box,
+Lambert / Metal / Dielectric materials, one point light, an environment light
+and a sky environment), rendered as a Whitted trace at 1920x1080 with a 2x2
+deterministic AA grid (8,294,400 primary samples per step), max bounce depth 6,
+Bricks accelerator semantics, march max 256 steps / eps 1e-4 / max dist 100 /
+step scale 0.7.  A step is one full frame: every bounce, shadow ray, blended
+normal and material, the per-pixel AA average (linear RGB) and the Reinhard
+RGB8 image.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+``--mode depth`` times the plain depth march of the same scene (refined hit
+distance, hit mask, material id, estimate_normal and the gray preview).  The
+trace line carries the depth march as a secondary figure.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--mode trace|depth]
 
 Prints one JSON line.  ``--impl reference`` times the CPU restatement of the
-reference's depth path (the oracle) on the host cores over a row sample of the
-same workload.
+reference's path (the oracle) on the host cores over a row sample of the same
+workload.
 """
 from __future__ import annotations
 
@@ -42,6 +50,8 @@ FLOP_BOX = 15.0
 FLOP_PRIM = 34.0
 # march step bookkeeping: point (6), |d| test, step (4)
 FLOP_STEP = 12.0
+
+L2_FLUSH_BYTES = 256 << 20  # > 129 MB L2
 
 
 def _env_int(name: str, default: int) -> int:
@@ -109,83 +119,248 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(w, budget_s: float = 12.0) -> dict:
+def _oracle_rows(st, w, mode: str, threads: int, rows):
+    import oracle
+
+    if mode == "trace":
+        oracle.render_trace(st, w.options, int(w.accel), w.aa, w.max_depth, 32, threads, rows=rows)
+    else:
+        oracle.render_depth(st, w.options, int(w.accel), w.aa, 32, threads, rows=rows)
+
+
+def _row_sample(st, w, mode: str, threads: int, budget_s: float):
+    """Rows (begin, end, step) sized so one oracle pass takes about budget_s."""
+    h = w.options.height
+    t0 = time.perf_counter()
+    _oracle_rows(st, w, mode, threads, (h // 2, h // 2 + 1, 1))
+    per_row = max(time.perf_counter() - t0, 1e-3)
+    n_rows = int(min(max(budget_s / per_row, 1), h))
+    step = max(h // n_rows, 1)
+    # rows centred in their bands (a one-row sample is the middle row, not the sky)
+    return (step // 2, h, step), len(range(step // 2, h, step))
+
+
+def _sample_text(w, mode: str, rows: int, step: int) -> str:
+    what = (f"Whitted trace depth {w.max_depth}" if mode == "trace" else "depth march")
+    return (f"{rows} of {w.options.height} rows (every {step}th) x {w.options.width} px x {w.aa} AA samples, "
+            f"f32 C++ restatement of the reference {what}, {w.accel.name} accel")
+
+
+def cpu_baseline(w, mode: str, budget_s: float = 12.0) -> dict:
     """Oracle (f32 restatement of the reference CPU path) on a row sample."""
     import forgedthoughts_gb300 as ft
-    import oracle
 
     st = ft.parse_and_eval(w.source)
     threads = os.cpu_count() or 1
-    h = w.options.height
+    rows, n = _row_sample(st, w, mode, threads, budget_s)
     t0 = time.perf_counter()
-    oracle.render_depth(st, w.options, int(w.accel), w.aa, 32, threads, rows=(h // 2, h // 2 + 1, 1))
-    per_row = max(time.perf_counter() - t0, 1e-3)
-    n_rows = int(min(max(budget_s / per_row, 2), h))
-    step = max(h // n_rows, 1)
-    t0 = time.perf_counter()
-    oracle.render_depth(st, w.options, int(w.accel), w.aa, 32, threads, rows=(0, h, step))
+    _oracle_rows(st, w, mode, threads, rows)
     dt = time.perf_counter() - t0
-    rows = len(range(0, h, step))
-    rays = rows * w.options.width * w.aa
+    rays = n * w.options.width * w.aa
     return {"value": rays / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{rows} of {h} rows (every {step}th) x {w.options.width} px x {w.aa} AA samples, "
-                      f"f32 C++ restatement of the reference depth path, {w.accel.name} accel, {dt:.1f} s"}
+            "sample": _sample_text(w, mode, n, rows[2]) + f", {dt:.1f} s"}
 
 
 def run_reference(args, w) -> None:
     """`--impl reference`: the reference algorithm on the host cores."""
     import forgedthoughts_gb300 as ft
-    import oracle
 
     rank = _env_int("RANK", 0)
     if rank != 0:
         return
     st = ft.parse_and_eval(w.source)
     threads = os.cpu_count() or 1
-    h = w.options.height
     # bounded sample per step: a fixed set of rows spread over the frame
-    t0 = time.perf_counter()
-    oracle.render_depth(st, w.options, int(w.accel), w.aa, 32, threads, rows=(h // 2, h // 2 + 1, 1))
-    per_row = max(time.perf_counter() - t0, 1e-3)
     budget = 60.0 / max(args.steps + args.warmup, 1)
-    n_rows = int(min(max(budget / per_row, 1), h))
-    step = max(h // n_rows, 1)
-    rows = len(range(0, h, step))
+    rows, n = _row_sample(st, w, args.mode, threads, budget)
     for _ in range(args.warmup):
-        oracle.render_depth(st, w.options, int(w.accel), w.aa, 32, threads, rows=(0, h, step))
+        _oracle_rows(st, w, args.mode, threads, rows)
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        oracle.render_depth(st, w.options, int(w.accel), w.aa, 32, threads, rows=(0, h, step))
+        _oracle_rows(st, w, args.mode, threads, rows)
         times.append(time.perf_counter() - t0)
-    rays = rows * w.options.width * w.aa
+    rays = n * w.options.width * w.aa
     total = sum(times)
     value = rays * len(times) / total / 1e6
-    sample = (f"{rows} of {h} rows (every {step}th) x {w.options.width} px x {w.aa} AA samples per step, "
-              f"f32 C++ restatement of the reference depth path, {w.accel.name} accel")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total / len(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": w.name, "width": w.options.width, "height": w.options.height, "aa": w.aa,
-                       "accel": w.accel.name, "sample_rows": rows},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "config": _config(w, args.mode, 1) | {"sample_rows": n},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": _sample_text(w, args.mode, n, rows[2]) + " per step"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def _config(w, mode: str, world: int) -> dict:
+    cfg = {"workload": w.name, "mode": mode, "width": w.options.width, "height": w.options.height, "aa": w.aa,
+           "primary_samples_per_step": w.options.width * w.options.height * w.aa, "accel": w.accel.name,
+           "variant": "plain_fp32", "l2": "flushed between steps (256 MiB write)",
+           "parallelism": f"replicas x{world}"}
+    if mode == "trace":
+        cfg["max_depth"] = w.max_depth
+        cfg["outputs"] = "linear rgb f32 + rgb8 (device)"
+    else:
+        cfg["outputs"] = "t, mask, material, normal, rgb8 (device)"
+    return cfg
+
+
+class Renderer:
+    """One render step through the C ABI with device outputs."""
+
+    def __init__(self, lib, scene, w, mode: str, dev, stream):
+        import torch
+
+        from forgedthoughts_gb300 import _native
+
+        self.lib, self.scene, self.w, self.mode = lib, scene, w, mode
+        self.native = _native
+        self.opts = w.options.to_c()
+        self.pixels = w.options.width * w.options.height
+        self.items = self.pixels * w.aa
+        self.sptr = ctypes.c_void_p(stream.cuda_stream)
+        e = lambda n, dt: torch.empty(n, dtype=dt, device=dev)  # noqa: E731
+        if mode == "trace":
+            self.rgbf = e(self.pixels * 3, torch.float32)
+            self.rgb8 = e(self.pixels * 3, torch.uint8)
+        else:
+            self.t = e(self.items, torch.float32)
+            self.m = e(self.items, torch.uint8)
+            self.mat = e(self.items, torch.int32)
+            self.n = e(self.items * 3, torch.float32)
+            self.rgb8 = e(self.pixels * 3, torch.uint8)
+
+    def __call__(self, full_outputs: bool = True):
+        p = lambda x: ctypes.c_void_p(x.data_ptr())  # noqa: E731
+        w = self.w
+        if self.mode == "trace":
+            rc = self.lib.ft_render_trace(self.scene.handle, ctypes.byref(self.opts), int(w.accel), w.aa, w.max_depth,
+                                          p(self.rgbf) if full_outputs else None,
+                                          p(self.rgb8) if full_outputs else None,
+                                          self.native.FT_FLAG_DEVICE_POINTERS, self.sptr)
+        else:
+            rc = self.lib.ft_render_depth(self.scene.handle, ctypes.byref(self.opts), int(w.accel), w.aa, p(self.t),
+                                          p(self.m), p(self.mat), p(self.n), p(self.rgb8) if full_outputs else None,
+                                          self.native.FT_FLAG_DEVICE_POINTERS, self.sptr)
+        if rc != 0:
+            raise RuntimeError(self.native.last_error())
+
+    def stats(self):
+        s = self.native.RenderStatsC()
+        w = self.w
+        if self.mode == "trace":
+            rc = self.lib.ft_render_trace_stats(self.scene.handle, ctypes.byref(self.opts), int(w.accel), w.aa,
+                                                w.max_depth, ctypes.byref(s))
+        else:
+            rc = self.lib.ft_render_depth_stats(self.scene.handle, ctypes.byref(self.opts), int(w.accel), w.aa,
+                                                ctypes.byref(s))
+        if rc != 0:
+            raise RuntimeError(self.native.last_error())
+        return s
+
+
+def _time_steps(fn, steps: int, stream, flush) -> list[float]:
+    import torch
+
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    stops = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    for k in range(steps):
+        flush.fill_(k & 0xFF)  # evict L2 between steps (outside the timed events)
+        starts[k].record(stream)
+        fn()
+        stops[k].record(stream)
+    torch.cuda.synchronize()
+    return [a.elapsed_time(b) for a, b in zip(starts, stops)]
+
+
+def _kernel_roofline(r: Renderer, kernel_ms: float, peak: float, kernel: str) -> dict:
+    s = r.stats()
+    flops = s.box_tests * FLOP_BOX + s.primitive_evals * FLOP_PRIM + s.march_steps * FLOP_STEP
+    achieved = flops / (kernel_ms * 1e-3) / 1e12
+    return {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak if peak else None, "kernel": kernel, "kernel_ms": kernel_ms,
+            "flop_per_launch": flops,
+            "peak_source": "measured dependent-FMA kernel (ft_measure_fp32_peak), of measured",
+            "counts": {"distance_evals": s.distance_evals, "primitive_evals": s.primitive_evals,
+                       "box_tests": s.box_tests, "march_steps": s.march_steps}}
+
+
+def _traffic(kernel: str, w) -> int | None:
+    """Per-launch DRAM bytes of the dominant kernel from a committed ncu summary."""
+    prof = ROOT / "profiles" / f"{kernel}_traffic.txt"
+    if not prof.exists() or not w.name.startswith("union_round512"):
+        return None
+    full = w.options.width * w.options.height * w.aa
+    for ln in prof.read_text().splitlines():
+        if ln.startswith(f"bytes_per_full_launch[{full}]:"):
+            return int(ln.split(":", 1)[1])
+    return None
+
+
+def _e2e(lib, st, w, mode: str, steps: int):
+    """The same render through the public C ABI with host buffers: scene upload
+    (host -> device), render, outputs copied back to pinned host memory."""
+    import torch
+
+    from forgedthoughts_gb300 import _native
+
+    opts = w.options.to_c()
+    pixels = w.options.width * w.options.height
+    items = pixels * w.aa
+    pin = lambda n, dt: torch.empty(n, dtype=dt, pin_memory=True)  # noqa: E731
+    p = lambda x: ctypes.c_void_p(x.data_ptr())  # noqa: E731
+    if mode == "trace":
+        h_rgbf, h_rgb = pin(pixels * 3, torch.float32), pin(pixels * 3, torch.uint8)
+        d2h = pixels * 3 * 4 + pixels * 3
+    else:
+        h_t, h_m, h_mat = pin(items, torch.float32), pin(items, torch.uint8), pin(items, torch.int32)
+        h_n, h_rgb = pin(items * 3, torch.float32), pin(pixels * 3, torch.uint8)
+        d2h = items * (4 + 1 + 4 + 12) + pixels * 3
+    times, h2d = [], 0
+    for k in range(steps + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        handle = ctypes.c_void_p()
+        if lib.ft_scene_create(st.desc_ptr, ctypes.byref(handle)) != 0:
+            raise RuntimeError(_native.last_error())
+        if mode == "trace":
+            rc = lib.ft_render_trace(handle, ctypes.byref(opts), int(w.accel), w.aa, w.max_depth, p(h_rgbf), p(h_rgb),
+                                     0, None)
+        else:
+            rc = lib.ft_render_depth(handle, ctypes.byref(opts), int(w.accel), w.aa, p(h_t), p(h_m), p(h_mat), p(h_n),
+                                     p(h_rgb), 0, None)
+        nbytes = ctypes.c_uint64(0)
+        lib.ft_scene_device_bytes(handle, ctypes.byref(nbytes))
+        lib.ft_scene_destroy(handle)
+        if rc != 0:
+            raise RuntimeError(_native.last_error())
+        if k > 0:  # first call pays one-time CUDA module and allocator set-up
+            times.append(time.perf_counter() - t0)
+        h2d = int(nbytes.value) + ctypes.sizeof(opts)
+    value = items / statistics.mean(times) / 1e6 if times else None
+    return {"value": value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+            "includes": "scene upload + accelerator build + render + output copy to pinned host"}
 
 
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--steps", type=int, default=0, help="timed steps (default 10 trace / 30 depth)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--mode", choices=["trace", "depth"], default="trace")
     ap.add_argument("--workload", default="union_round")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true")
     ap.add_argument("--width", type=int, default=0, help="override the workload's width (profiling runs)")
     ap.add_argument("--height", type=int, default=0)
     ap.add_argument("--aa", type=int, default=0)
+    ap.add_argument("--max-depth", type=int, default=0)
     args = ap.parse_args()
+    if args.steps <= 0:
+        args.steps = 10 if args.mode == "trace" else 30
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
 
     from forgedthoughts_gb300.build import build_all
@@ -198,11 +373,14 @@ def main() -> None:
         w.options.height = args.height
     if args.aa:
         w.aa = args.aa
+    if args.max_depth:
+        w.max_depth = args.max_depth
+    if args.mode == "trace" and w.max_depth <= 0:
+        w.max_depth = 6
     if args.impl == "reference":
         run_reference(args, w)
         return
 
-    import numpy as np
     import torch
 
     import forgedthoughts_gb300 as ft
@@ -219,49 +397,24 @@ def main() -> None:
     lib = _native.lib()
     st = ft.parse_and_eval(w.source)
     scene = st.gpu()
-    opts = w.options.to_c()
-    aa = w.aa
-    pixels = w.options.width * w.options.height
-    items = pixels * aa
     dev = torch.device("cuda", local)
-    t_buf = torch.empty(items, dtype=torch.float32, device=dev)
-    m_buf = torch.empty(items, dtype=torch.uint8, device=dev)
-    mat_buf = torch.empty(items, dtype=torch.int32, device=dev)
-    n_buf = torch.empty(items * 3, dtype=torch.float32, device=dev)
-    rgb_buf = torch.empty(pixels * 3, dtype=torch.uint8, device=dev)
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # > 129 MB L2
     stream = torch.cuda.current_stream()
-    sptr = ctypes.c_void_p(stream.cuda_stream)
-
-    def render(with_rgb: bool = True):
-        rc = lib.ft_render_depth(scene.handle, ctypes.byref(opts), int(w.accel), aa, ctypes.c_void_p(t_buf.data_ptr()),
-                                 ctypes.c_void_p(m_buf.data_ptr()), ctypes.c_void_p(mat_buf.data_ptr()),
-                                 ctypes.c_void_p(n_buf.data_ptr()),
-                                 ctypes.c_void_p(rgb_buf.data_ptr()) if with_rgb else None,
-                                 _native.FT_FLAG_DEVICE_POINTERS, sptr)
-        if rc != 0:
-            raise RuntimeError(_native.last_error())
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    r = Renderer(lib, scene, w, args.mode, dev, stream)
+    items = r.items
 
     clocks = ClockSampler(local)
     clocks.start()
     for _ in range(args.warmup):
-        render()
+        r()
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    stops = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    for k in range(args.steps):
-        flush.fill_(k & 0xFF)  # evict L2 between steps (outside the timed events)
-        starts[k].record(stream)
-        render()
-        stops[k].record(stream)
-    torch.cuda.synchronize()
+    step_ms = _time_steps(r, args.steps, stream, flush)
     if dist:
         dist.barrier()
     clk = clocks.stop()
-    step_ms = [a.elapsed_time(b) for a, b in zip(starts, stops)]
     total_ms = sum(step_ms)
     if dist:
         tt = torch.tensor([total_ms], device=dev)
@@ -270,88 +423,46 @@ def main() -> None:
     ms_per_step = total_ms / args.steps
     value = items * args.steps * world / (total_ms * 1e-3) / 1e6
 
-    # Dominant kernel alone (march_depth_kernel): same stream, CUDA events.
-    k_starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    k_stops = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    for k in range(args.steps):
-        flush.fill_(k & 0xFF)
-        k_starts[k].record(stream)
-        render(with_rgb=False)
-        k_stops[k].record(stream)
-    torch.cuda.synchronize()
-    march_ms = statistics.mean(a.elapsed_time(b) for a, b in zip(k_starts, k_stops))
-
-    stats = _native.RenderStatsC()
-    if lib.ft_render_depth_stats(scene.handle, ctypes.byref(opts), int(w.accel), aa, ctypes.byref(stats)) != 0:
-        raise RuntimeError(_native.last_error())
-    flops = (stats.box_tests * FLOP_BOX + stats.primitive_evals * FLOP_PRIM + stats.march_steps * FLOP_STEP)
     peak = ctypes.c_double(0.0)
     if lib.ft_measure_fp32_peak(ctypes.byref(peak)) != 0:
         raise RuntimeError(_native.last_error())
-    achieved = flops / (march_ms * 1e-3) / 1e12
 
-    # End to end through the public API with host buffers: scene upload
-    # (host -> device), render, every output copied to pinned host memory.
-    pin = lambda n, dt: torch.empty(n, dtype=dt, pin_memory=True)  # noqa: E731
-    h_t, h_m, h_mat = pin(items, torch.float32), pin(items, torch.uint8), pin(items, torch.int32)
-    h_n, h_rgb = pin(items * 3, torch.float32), pin(pixels * 3, torch.uint8)
-    e2e_times = []
-    h2d = 0
-    for k in range(0 if args.no_e2e else args.steps + 1):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        handle = ctypes.c_void_p()
-        if lib.ft_scene_create(st.desc_ptr, ctypes.byref(handle)) != 0:
-            raise RuntimeError(_native.last_error())
-        rc = lib.ft_render_depth(handle, ctypes.byref(opts), int(w.accel), aa, ctypes.c_void_p(h_t.data_ptr()),
-                                 ctypes.c_void_p(h_m.data_ptr()), ctypes.c_void_p(h_mat.data_ptr()),
-                                 ctypes.c_void_p(h_n.data_ptr()), ctypes.c_void_p(h_rgb.data_ptr()), 0, None)
-        nbytes = ctypes.c_uint64(0)
-        lib.ft_scene_device_bytes(handle, ctypes.byref(nbytes))
-        lib.ft_scene_destroy(handle)
-        if rc != 0:
-            raise RuntimeError(_native.last_error())
-        if k > 0:  # first call allocates the per-scene output buffers
-            e2e_times.append(time.perf_counter() - t0)
-        h2d = int(nbytes.value) + ctypes.sizeof(opts)
-    d2h = items * (4 + 1 + 4 + 12) + pixels * 3
-    e2e_value = items / statistics.mean(e2e_times) / 1e6 if e2e_times else None
-
-    # Traffic of the dominant kernel from an ncu capture (small case scaled
-    # to a full launch), committed under profiles/.
-    traffic = None
-    prof = ROOT / "profiles" / "march_depth_traffic.txt"
-    if prof.exists() and w.name.startswith("union_round512") and items == 8294400:
-        for ln in prof.read_text().splitlines():
-            if ln.startswith("bytes_per_full_launch:"):
-                traffic = int(ln.split(":", 1)[1])
+    # Dominant kernel: the same launch without the output conversion pass.
+    kernel = "trace_kernel" if args.mode == "trace" else "march_depth_persistent"
+    kernel_ms = statistics.mean(_time_steps(lambda: r(full_outputs=False), max(args.steps // 2, 3), stream, flush))
+    roofline = _kernel_roofline(r, kernel_ms, peak.value, kernel)
+    roofline["traffic"] = _traffic(kernel, w)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": w.name, "width": w.options.width, "height": w.options.height, "aa": aa,
-                   "primary_samples_per_step": items, "primitives": 512, "accel": w.accel.name,
-                   "variant": "plain_fp32", "outputs": "t, mask, material, normal, rgb8 (device)",
-                   "l2": "flushed between steps (256 MiB write)", "parallelism": f"replicas x{world}"},
-        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak.value, "unit": "TFLOP/s",
-                     "frac": achieved / peak.value if peak.value else None, "traffic": traffic,
-                     "kernel": "march_depth_kernel", "kernel_ms": march_ms, "flop_per_launch": flops,
-                     "peak_source": "measured dependent-FMA kernel (ft_measure_fp32_peak)",
-                     "counts": {"distance_evals": stats.distance_evals, "primitive_evals": stats.primitive_evals,
-                                "box_tests": stats.box_tests, "march_steps": stats.march_steps}},
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator, no dataset)",
+        "config": _config(w, args.mode, world),
+        "roofline": roofline,
+        "e2e": None if args.no_e2e else _e2e(lib, st, w, args.mode, min(args.steps, 5)),
         "clocks": clk,
         "gpu_launches": 2 * args.steps,
     }
+    if args.mode == "trace" and not args.no_secondary:
+        # The plain depth march of the same frame: the north-star's plain FP32 form.
+        d = Renderer(lib, scene, w, "depth", dev, stream)
+        for _ in range(3):
+            d()
+        torch.cuda.synchronize()
+        d_ms = _time_steps(d, 20, stream, flush)
+        dk_ms = statistics.mean(_time_steps(lambda: d(full_outputs=False), 10, stream, flush))
+        dl = _kernel_roofline(d, dk_ms, peak.value, "march_depth_persistent")
+        dl["traffic"] = _traffic("march_depth_persistent", w)
+        line["depth_march"] = {"value": d.items * len(d_ms) / (sum(d_ms) * 1e-3) / 1e6, "unit": UNIT,
+                               "ms_per_step": statistics.mean(d_ms), "roofline": dl,
+                               "gpu_launches_per_step": 2}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(w)
+        line["cpu_baseline"] = cpu_baseline(w, args.mode)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
     st.close()
-    del np
 
 
 if __name__ == "__main__":

@@ -119,6 +119,8 @@ SIGNATURES = {
     "ft_render_depth_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RenderOptionsC), ctypes.c_int,
                                              ctypes.c_uint32, ctypes.POINTER(RenderStatsC)]),
     "ft_measure_fp32_peak": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double)]),
+    "ft_render_trace_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RenderOptionsC), ctypes.c_int,
+                                             ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(RenderStatsC)]),
     "ft_render_depth_preview_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RenderOptionsC), ctypes.c_int,
                                                        ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p]),
 }

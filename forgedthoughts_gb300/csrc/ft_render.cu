@@ -1428,6 +1428,35 @@ ft_status ft_render_trace(ft_scene* sc, const ft_render_options* options, ft_acc
   return FT_OK;
 }
 
+ft_status ft_render_trace_stats(ft_scene* sc, const ft_render_options* options, ft_accel_mode accel,
+                                uint32_t aa_samples, uint32_t max_depth, ft_render_stats* stats) {
+  if (!sc || !stats) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "scene and stats must be non-null");
+  if (accel < FT_ACCEL_NAIVE || accel > FT_ACCEL_BRICKS) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "unknown accel mode");
+  uint32_t aa = std::max(aa_samples, 1u);
+  if (ft_status s = check_options(options, aa)) return s;
+  uint32_t depth = std::max(max_depth, 1u);
+  if (depth > 10) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "max_depth must be <= 10");
+  std::lock_guard<std::mutex> lock(sc->mu);
+  FT_CUDA_TRY(cudaSetDevice(sc->device), "cudaSetDevice");
+  size_t pixels = static_cast<size_t>(options->width) * options->height;
+  if (ft_status s = ensure_buffers(sc, pixels * aa, pixels)) return s;
+  RayParams P = make_params(sc, *options, aa);
+  uint64_t blocks = (P.n_items + 127) / 128;
+  FT_CUDA_TRY(cudaMemset(sc->d_stats, 0, 16 * sizeof(unsigned long long)), "cudaMemset(stats)");
+  trace_kernel<true><<<static_cast<unsigned>(blocks), 128>>>(sc->dev, P, depth, sc->d_normal, sc->d_stats);
+  FT_CUDA_TRY(cudaGetLastError(), "trace_kernel launch");
+  unsigned long long h[8] = {0};
+  FT_CUDA_TRY(cudaMemcpy(h, sc->d_stats, sizeof(h), cudaMemcpyDeviceToHost), "copy stats");
+  stats->rays = pixels * aa;
+  stats->distance_evals = h[0];
+  stats->primitive_evals = h[1];
+  stats->box_tests = h[2];
+  stats->hook_instrs = h[3];
+  stats->march_steps = h[4];
+  ftcommon::clear_last_error();
+  return FT_OK;
+}
+
 ft_status ft_render_depth_stats(ft_scene* sc, const ft_render_options* options, ft_accel_mode accel,
                                 uint32_t aa_samples, ft_render_stats* stats) {
   if (!sc || !stats) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "scene and stats must be non-null");

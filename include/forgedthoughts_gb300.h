@@ -388,6 +388,11 @@ ft_status ft_render_depth_stats(ft_scene* scene, const ft_render_options* option
                                 ft_accel_mode accel, uint32_t aa_samples,
                                 ft_render_stats* stats);
 
+/* The same counters for a Whitted trace (ft_render_trace); output discarded. */
+ft_status ft_render_trace_stats(ft_scene* scene, const ft_render_options* options,
+                                ft_accel_mode accel, uint32_t aa_samples, uint32_t max_depth,
+                                ft_render_stats* stats);
+
 /* Measured FP32 FMA throughput of the current device in TFLOP/s (a short
  * dependent-FMA kernel), used as the roofline denominator of the march. */
 ft_status ft_measure_fp32_peak(double* tflops);

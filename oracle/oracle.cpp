@@ -898,6 +898,10 @@ Opts resolve(const ft_render_options* o) {
   return Opts{o->width, o->height, o->max_steps, o->max_dist, o->epsilon, o->step_scale, o->camera_z, o->fov_y_degrees};
 }
 
+// Pixels per work item of the host thread pool (a row segment, so that a
+// sample of a few rows still spreads over every core).
+constexpr uint32_t kSegment = 32;
+
 template <class R>
 int render_depth(const ft_scene_desc* desc, const ft_render_options* options, int accel, uint32_t aa, int threads,
                  uint32_t row_begin, uint32_t row_end, uint32_t row_step, float* t_out, uint8_t* mask_out,
@@ -915,15 +919,17 @@ int render_depth(const ft_scene_desc* desc, const ft_render_options* options, in
   row_end = std::min(row_end, op.height);
   std::vector<uint32_t> rows;
   for (uint32_t y = row_begin; y < row_end; y += row_step) rows.push_back(y);
+  const size_t segs = (op.width + kSegment - 1) / kSegment;  // work item: one row segment
   std::atomic<size_t> next{0};
   std::atomic<uint64_t> total{0};
   auto worker = [&]() {
     uint64_t evals = 0;
     for (;;) {
       size_t k = next.fetch_add(1);
-      if (k >= rows.size()) break;
-      uint32_t y = rows[k];
-      for (uint32_t x = 0; x < op.width; ++x) {
+      if (k >= rows.size() * segs) break;
+      uint32_t y = rows[k / segs];
+      uint32_t x0 = static_cast<uint32_t>(k % segs) * kSegment, x1 = std::min(x0 + kSegment, op.width);
+      for (uint32_t x = x0; x < x1; ++x) {
         float sum = 0.0f;
         for (uint32_t s = 0; s < aa; ++s) {
           float px = ((static_cast<float>(x) + offs[s].first) / static_cast<float>(op.width)) * 2.0f - 1.0f;
@@ -1675,15 +1681,17 @@ int render_trace(const ft_scene_desc* desc, const ft_render_options* options, in
   row_end = std::min(row_end, op.height);
   std::vector<uint32_t> rows;
   for (uint32_t y = row_begin; y < row_end; y += row_step) rows.push_back(y);
+  const size_t segs = (op.width + kSegment - 1) / kSegment;  // work item: one row segment
   std::atomic<size_t> next{0};
   std::atomic<uint64_t> total{0};
   auto worker = [&]() {
     uint64_t evals = 0;
     for (;;) {
       size_t k = next.fetch_add(1);
-      if (k >= rows.size()) break;
-      uint32_t y = rows[k];
-      for (uint32_t x = 0; x < op.width; ++x) {
+      if (k >= rows.size() * segs) break;
+      uint32_t y = rows[k / segs];
+      uint32_t x0 = static_cast<uint32_t>(k % segs) * kSegment, x1 = std::min(x0 + kSegment, op.width);
+      for (uint32_t x = x0; x < x1; ++x) {
         Sp<float> sum = sp(0.0f, 0.0f, 0.0f);
         for (uint32_t s = 0; s < aa; ++s) {
           float px = ((static_cast<float>(x) + offs[s].first) / static_cast<float>(op.width)) * 2.0f - 1.0f;
