@@ -209,12 +209,13 @@ def _config(w, mode: str, world: int) -> dict:
 class Renderer:
     """One render step through the C ABI with device outputs."""
 
-    def __init__(self, lib, scene, w, mode: str, dev, stream):
+    def __init__(self, lib, scene, w, mode: str, dev, stream, extra_flags: int = 0):
         import torch
 
         from forgedthoughts_gb300 import _native
 
         self.lib, self.scene, self.w, self.mode = lib, scene, w, mode
+        self.extra_flags = extra_flags
         self.native = _native
         self.opts = w.options.to_c()
         self.pixels = w.options.width * w.options.height
@@ -242,7 +243,7 @@ class Renderer:
         else:
             rc = self.lib.ft_render_depth(self.scene.handle, ctypes.byref(self.opts), int(w.accel), w.aa, p(self.t),
                                           p(self.m), p(self.mat), p(self.n), p(self.rgb8) if full_outputs else None,
-                                          self.native.FT_FLAG_DEVICE_POINTERS, self.sptr)
+                                          self.native.FT_FLAG_DEVICE_POINTERS | self.extra_flags, self.sptr)
         if rc != 0:
             raise RuntimeError(self.native.last_error())
 
@@ -254,7 +255,7 @@ class Renderer:
                                                 w.max_depth, ctypes.byref(s))
         else:
             rc = self.lib.ft_render_depth_stats(self.scene.handle, ctypes.byref(self.opts), int(w.accel), w.aa,
-                                                ctypes.byref(s))
+                                                self.extra_flags, ctypes.byref(s))
         if rc != 0:
             raise RuntimeError(self.native.last_error())
         return s
@@ -284,6 +285,56 @@ def _kernel_roofline(r: Renderer, kernel_ms: float, peak: float, kernel: str) ->
             "peak_source": "measured dependent-FMA kernel (ft_measure_fp32_peak), of measured",
             "counts": {"distance_evals": s.distance_evals, "primitive_evals": s.primitive_evals,
                        "box_tests": s.box_tests, "march_steps": s.march_steps}}
+
+
+def _depth_figures(lib, scene, w, dev, stream, flush, peak: float, flags: int) -> dict:
+    import torch
+
+    d = Renderer(lib, scene, w, "depth", dev, stream, flags)
+    for _ in range(3):
+        d()
+    torch.cuda.synchronize()
+    d_ms = _time_steps(d, 20, stream, flush)
+    dk_ms = statistics.mean(_time_steps(lambda: d(full_outputs=False), 10, stream, flush))
+    dl = _kernel_roofline(d, dk_ms, peak, "march_depth_persistent")
+    dl["traffic"] = _traffic("march_depth_persistent" + ("_fp16_bricks" if flags else ""), w)
+    s = d.stats()
+    dl["counts"]["far_steps"] = s.far_steps
+    dl["counts"]["brick_fetches"] = s.brick_fetches
+    return {"value": d.items * len(d_ms) / (sum(d_ms) * 1e-3) / 1e6, "unit": UNIT,
+            "ms_per_step": statistics.mean(d_ms), "roofline": dl, "gpu_launches_per_step": 2}
+
+
+def _brick_figures(lib, scene, w, dev, stream, flush, peak: float) -> dict:
+    """Build the FP16 brick cache, time the precision-form depth march, and
+    compare its frame with the plain march's (mask agreement, depth error)."""
+    import numpy as np
+    import torch
+
+    from forgedthoughts_gb300 import _native
+
+    info = _native.BrickInfoC()
+    o = _native.BrickOptionsC(0.02, 0.0, 0.0, 0)
+    if lib.ft_scene_build_bricks(scene.handle, ctypes.byref(o), ctypes.byref(info)) != 0:
+        raise RuntimeError(_native.last_error())
+    out = _depth_figures(lib, scene, w, dev, stream, flush, peak, _native.FT_FLAG_FP16_BRICKS)
+    a = Renderer(lib, scene, w, "depth", dev, stream, 0)
+    b = Renderer(lib, scene, w, "depth", dev, stream, _native.FT_FLAG_FP16_BRICKS)
+    a()
+    b()
+    torch.cuda.synchronize()
+    ma, mb = a.m.cpu().numpy(), b.m.cpu().numpy()
+    ta, tb = a.t.cpu().numpy().astype(np.float64), b.t.cpu().numpy().astype(np.float64)
+    both = (ma == 1) & (mb == 1)
+    err = np.abs(ta[both] - tb[both]) if both.any() else np.zeros(1)
+    out["vs_plain_fp32"] = {"mask_agreement": float((ma == mb).mean()),
+                            "depth_err_max": float(err.max()), "depth_err_q999": float(np.quantile(err, 0.999)),
+                            "depth_within_1e-4": float((err <= 1e-4).mean())}
+    out["bricks"] = {"voxel_size": 0.02, "brick_voxels": 8, "storage": "fp16 9^3 texels, trilinear texture fetch",
+                     "near_bricks": info.near_bricks, "cells": list(info.bricks), "exact_leaves": info.exact_leaves,
+                     "band": info.band, "max_lipschitz": info.max_lipschitz, "device_bytes": info.device_bytes,
+                     "build_ms": info.build_ms}
+    return out
 
 
 def _traffic(kernel: str, w) -> int | None:
@@ -443,19 +494,18 @@ def main() -> None:
         "clocks": clk,
         "gpu_launches": 2 * args.steps,
     }
-    if args.mode == "trace" and not args.no_secondary:
-        # The plain depth march of the same frame: the north-star's plain FP32 form.
-        d = Renderer(lib, scene, w, "depth", dev, stream)
-        for _ in range(3):
-            d()
-        torch.cuda.synchronize()
-        d_ms = _time_steps(d, 20, stream, flush)
-        dk_ms = statistics.mean(_time_steps(lambda: d(full_outputs=False), 10, stream, flush))
-        dl = _kernel_roofline(d, dk_ms, peak.value, "march_depth_persistent")
-        dl["traffic"] = _traffic("march_depth_persistent", w)
-        line["depth_march"] = {"value": d.items * len(d_ms) / (sum(d_ms) * 1e-3) / 1e6, "unit": UNIT,
-                               "ms_per_step": statistics.mean(d_ms), "roofline": dl,
-                               "gpu_launches_per_step": 2}
+    if not args.no_secondary:
+        plain = None
+        if args.mode == "trace":
+            # The plain depth march of the same frame: the plain FP32 form.
+            plain = _depth_figures(lib, scene, w, dev, stream, flush, peak.value, 0)
+            line["depth_march"] = plain
+        else:
+            plain = {"value": value}
+        # The FP16 brick precision form of the same depth march.
+        fp16 = _brick_figures(lib, scene, w, dev, stream, flush, peak.value)
+        fp16["speedup_vs_plain_fp32"] = fp16["value"] / plain["value"]
+        line["depth_march_fp16_bricks"] = fp16
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(w, args.mode)
     if rank == 0:

@@ -200,6 +200,24 @@ class GpuScene:
     def handle(self) -> ctypes.c_void_p:
         return self._h
 
+    def build_bricks(self, voxel_size: float = 0.02, band: float = 0.0, safety: float = 0.0,
+                     max_lattice_points: int = 0, far_steps_per_pass: int = 0) -> "BrickInfo":
+        """Build the FP16 brick distance cache (``ft_scene_build_bricks``)."""
+        o = _native.BrickOptionsC(voxel_size, band, safety, max_lattice_points, far_steps_per_pass, 0)
+        info = _native.BrickInfoC()
+        _check(_native.lib().ft_scene_build_bricks(self._h, ctypes.byref(o), ctypes.byref(info)))
+        return BrickInfo(tuple(info.region_min), tuple(info.region_max), tuple(info.bricks), info.near_bricks,
+                         info.exact_leaves, info.max_lipschitz, info.band, info.device_bytes, info.build_ms)
+
+    def brick_bounds(self, points: np.ndarray) -> tuple:
+        """(far-field bound, exact distance) at ``points`` (N, 3)."""
+        pts = np.ascontiguousarray(points, np.float32).reshape(-1, 3)
+        n = pts.shape[0]
+        bound = np.empty(n, np.float32)
+        exact = np.empty(n, np.float32)
+        _check(_native.lib().ft_scene_brick_bounds(self._h, _ptr(pts), n, _ptr(bound), _ptr(exact)))
+        return bound, exact
+
     def close(self) -> None:
         if self._h:
             _native.lib().ft_scene_destroy(self._h)
@@ -210,6 +228,21 @@ class GpuScene:
             self.close()
         except Exception:
             pass
+
+
+@dataclasses.dataclass
+class BrickInfo:
+    """``ft_brick_info``: the FP16 brick cache of a scene."""
+
+    region_min: tuple
+    region_max: tuple
+    bricks: tuple
+    near_bricks: int
+    exact_leaves: int
+    max_lipschitz: float
+    band: float
+    device_bytes: int
+    build_ms: float
 
 
 @dataclasses.dataclass
@@ -230,8 +263,10 @@ def _ptr(a: Optional[np.ndarray]):
 
 def render_depth(state: SceneState, options: RenderOptions, accel: AccelMode = AccelMode.Bvh, aa_samples: int = 1,
                  *, want_t: bool = True, want_mask: bool = True, want_material: bool = False,
-                 want_normal: bool = False, want_rgb8: bool = True) -> DepthImage:
-    """Depth preview of ``state`` on the GPU (host output buffers)."""
+                 want_normal: bool = False, want_rgb8: bool = True, fp16_bricks: bool = False) -> DepthImage:
+    """Depth preview of ``state`` on the GPU (host output buffers).  With
+    ``fp16_bricks`` the march uses the scene's FP16 brick cache
+    (``state.gpu().build_bricks()`` must have run)."""
     aa = max(int(aa_samples), 1)
     h, w = int(options.height), int(options.width)
     t = np.empty((h, w, aa), np.float32) if want_t else None
@@ -241,7 +276,8 @@ def render_depth(state: SceneState, options: RenderOptions, accel: AccelMode = A
     rgb = np.empty((h, w, 3), np.uint8) if want_rgb8 else None
     opts = options.to_c()
     _check(_native.lib().ft_render_depth(state.gpu().handle, ctypes.byref(opts), int(accel), aa, _ptr(t), _ptr(mask),
-                                         _ptr(mat), _ptr(nrm), _ptr(rgb), 0, None))
+                                         _ptr(mat), _ptr(nrm), _ptr(rgb),
+                                         _native.FT_FLAG_FP16_BRICKS if fp16_bricks else 0, None))
     return DepthImage(w, h, aa, t, mask, mat, nrm, rgb)
 
 
@@ -393,3 +429,187 @@ def read_png(path) -> np.ndarray:
     if ch == 1:
         img = np.repeat(img, 3, axis=2)
     return img[:, :, :3]
+
+
+class Batch:
+    """Many renders in one CUDA-graph launch (``ft_batch``).
+
+    ``items`` are ``(SceneState, RenderOptions, aa_samples, max_depth)``
+    tuples; ``max_depth`` 0 renders the depth preview, 1..10 a Whitted trace.
+    The scenes must stay alive while the batch exists.
+    """
+
+    def __init__(self, items, fp16_bricks: bool = False):
+        lib = _native.lib()
+        arr = (_native.BatchItemC * len(items))()
+        self._states = []
+        self._items = []
+        for k, (state, options, aa, max_depth) in enumerate(items):
+            arr[k].scene = state.gpu().handle.value
+            arr[k].options = options.to_c()
+            arr[k].aa_samples = max(int(aa), 1)
+            arr[k].max_depth = int(max_depth)
+            self._states.append(state)
+            self._items.append((int(options.width), int(options.height), max(int(aa), 1), int(max_depth)))
+        h = ctypes.c_void_p()
+        _check(lib.ft_batch_create(arr, len(items), _native.FT_BATCH_FP16_BRICKS if fp16_bricks else 0,
+                                   ctypes.byref(h)))
+        self._h = h
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._h
+
+    def samples(self) -> int:
+        n = ctypes.c_uint64()
+        _check(_native.lib().ft_batch_samples(self._h, ctypes.byref(n)))
+        return int(n.value)
+
+    def set_tuning(self, tile_w: int, tile_h: int, refill: int) -> None:
+        t = _native.BatchTuningC(tile_w, tile_h, refill, 0.0)
+        _check(_native.lib().ft_batch_set_tuning(self._h, ctypes.byref(t)))
+
+    def autotune(self) -> dict:
+        t = _native.BatchTuningC()
+        _check(_native.lib().ft_batch_autotune(self._h, ctypes.byref(t)))
+        return {"tile_w": t.tile_w, "tile_h": t.tile_h, "refill": t.refill, "ms": t.ms}
+
+    def launch(self, stream=None) -> None:
+        _check(_native.lib().ft_batch_launch(self._h, stream))
+
+    def read(self, item: int) -> dict:
+        """Outputs of one item (synchronises): depth items give t, mask, rgb
+        (preview value), rgb8; traces give rgb (linear radiance) and rgb8."""
+        if not 0 <= item < len(self._items):
+            raise RenderError(f"batch item {item} out of range")
+        w, h, aa, depth = self._items[item]
+        t = np.empty((h, w, aa), np.float32) if depth == 0 else None
+        mask = np.empty((h, w, aa), np.uint8) if depth == 0 else None
+        rgb = np.empty((h, w, 3), np.float32)
+        rgb8 = np.empty((h, w, 3), np.uint8)
+        _check(_native.lib().ft_batch_read(self._h, item, _ptr(t), _ptr(mask), _ptr(rgb), _ptr(rgb8)))
+        return {"t": t, "mask": mask, "rgb": rgb, "rgb8": rgb8}
+
+    def close(self) -> None:
+        if self._h:
+            _native.lib().ft_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ------------------------------------------------------------ differentiation
+
+def views_c(views) -> ctypes.Array:
+    """``ft_view`` array from (origin, target, fov_y_degrees) triples."""
+    arr = (_native.ViewC * len(views))()
+    for k, v in enumerate(views):
+        if isinstance(v, _native.ViewC):
+            arr[k] = v
+        else:
+            o, t, f = v
+            arr[k] = _native.ViewC((ctypes.c_float * 3)(*o), (ctypes.c_float * 3)(*t), float(f))
+    return arr
+
+
+def ring_views(n: int, radius: float = 5.0, height: float = 1.5, fov: float = 45.0, target=(0.0, 0.0, 0.0)):
+    """n cameras evenly spaced on a horizontal ring, looking at ``target``."""
+    out = []
+    for k in range(n):
+        a = 2.0 * np.pi * k / n
+        out.append(((radius * np.sin(a), height, -radius * np.cos(a)), tuple(target), fov))
+    return out
+
+
+class ParamScene:
+    """A scene whose union_round tree(s) carry differentiable parameters:
+    per sphere / box primitive (cx, cy, cz, rot_y, s0, s1, s2) and each
+    tree's blend radius (``ft_scene_param_layout``)."""
+
+    def __init__(self, source: str):
+        self.state = SceneState(source)
+        lib = _native.lib()
+        n = ctypes.c_uint32()
+        _check(lib.ft_scene_param_layout(self.state.desc_ptr, 0, None, ctypes.byref(n)))
+        self.layout = (_native.ParamC * n.value)()
+        _check(lib.ft_scene_param_layout(self.state.desc_ptr, n.value, self.layout, ctypes.byref(n)))
+
+    @property
+    def n_params(self) -> int:
+        return len(self.layout)
+
+    def names(self) -> list:
+        return [f"node{p.node}.{_native.FT_PARAM_FIELDS[p.field]}" for p in self.layout]
+
+    def get_params(self) -> np.ndarray:
+        v = np.empty(self.n_params, np.float32)
+        _check(_native.lib().ft_scene_desc_get_params(self.state.desc_ptr, self.layout, self.n_params, _ptr(v)))
+        return v
+
+    def set_params(self, values) -> None:
+        v = np.ascontiguousarray(values, np.float32).reshape(-1)
+        if v.size != self.n_params:
+            raise ValueError(f"expected {self.n_params} parameters")
+        _check(_native.lib().ft_scene_desc_set_params(self.state.desc_ptr, self.layout, self.n_params, _ptr(v)))
+        if self.state._gpu is not None:  # the GPU copy is rebuilt on next use
+            self.state._gpu.close()
+            self.state._gpu = None
+
+    def render(self, views, options: RenderOptions, tau: float = 0.05):
+        """(t, mask, sil), each (n_views, H, W): ``ft_render_views``."""
+        varr = views_c(views)
+        n, h, w = len(views), int(options.height), int(options.width)
+        t = np.empty((n, h, w), np.float32)
+        mask = np.empty((n, h, w), np.uint8)
+        sil = np.empty((n, h, w), np.float32)
+        opts = options.to_c()
+        _check(_native.lib().ft_render_views(self.state.gpu().handle, varr, n, ctypes.byref(opts), float(tau),
+                                             _ptr(t), _ptr(mask), _ptr(sil), 0, None))
+        return t, mask, sil
+
+    def backward(self, views, options: RenderOptions, dl_dt=None, dl_dsil=None, tau: float = 0.05) -> np.ndarray:
+        """dL/dparams (float64) for upstream gradients of the depth and
+        silhouette images: ``ft_render_backward``."""
+        varr = views_c(views)
+        a = None if dl_dt is None else np.ascontiguousarray(dl_dt, np.float32)
+        b = None if dl_dsil is None else np.ascontiguousarray(dl_dsil, np.float32)
+        g = np.zeros(self.n_params, np.float64)
+        opts = options.to_c()
+        _check(_native.lib().ft_render_backward(self.state.gpu().handle, varr, len(views), ctypes.byref(opts),
+                                                float(tau), self.layout, self.n_params, _ptr(a), _ptr(b), _ptr(g), 0,
+                                                None))
+        return g
+
+
+def render_function():
+    """A ``torch.autograd.Function`` over ParamScene: forward renders depth and
+    silhouette for a parameter tensor, backward is the adjoint march
+    (``render_backward``).  Built lazily so importing the package does not
+    import torch."""
+    import torch
+
+    class RenderViews(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, params, scene: ParamScene, views, options: RenderOptions, tau: float):
+            scene.set_params(params.detach().cpu().numpy())
+            t, mask, sil = scene.render(views, options, tau)
+            ctx.scene, ctx.views, ctx.options, ctx.tau = scene, views, options, tau
+            ctx.device, ctx.dtype = params.device, params.dtype
+            out_t = torch.from_numpy(t).to(params.device)
+            out_mask = torch.from_numpy(mask).to(params.device)
+            out_sil = torch.from_numpy(sil).to(params.device)
+            ctx.mark_non_differentiable(out_mask)
+            return out_t, out_mask, out_sil
+
+        @staticmethod
+        def backward(ctx, grad_t, grad_mask, grad_sil):
+            gt = None if grad_t is None else grad_t.detach().float().cpu().numpy()
+            gs = None if grad_sil is None else grad_sil.detach().float().cpu().numpy()
+            g = ctx.scene.backward(ctx.views, ctx.options, gt, gs, ctx.tau)
+            return torch.from_numpy(g).to(ctx.device, ctx.dtype), None, None, None, None
+
+    return RenderViews

@@ -26,6 +26,7 @@ FT_ERR_UNSUPPORTED = 10
 FT_ERR_NO_DEVICE = 11
 
 FT_FLAG_DEVICE_POINTERS = 1
+FT_FLAG_FP16_BRICKS = 2
 FT_ABI_VERSION = 1
 FT_MAX_PROGRAM_REGS = 64
 
@@ -97,8 +98,45 @@ class BuildInfoC(ctypes.Structure):
 
 class RenderStatsC(ctypes.Structure):
     _fields_ = [("rays", ctypes.c_uint64), ("distance_evals", ctypes.c_uint64), ("primitive_evals", ctypes.c_uint64),
-                ("box_tests", ctypes.c_uint64), ("hook_instrs", ctypes.c_uint64), ("march_steps", ctypes.c_uint64)]
+                ("box_tests", ctypes.c_uint64), ("hook_instrs", ctypes.c_uint64), ("march_steps", ctypes.c_uint64),
+                ("far_steps", ctypes.c_uint64), ("brick_fetches", ctypes.c_uint64)]
 
+
+class BrickOptionsC(ctypes.Structure):
+    _fields_ = [("voxel_size", ctypes.c_float), ("band", ctypes.c_float), ("safety", ctypes.c_float),
+                ("max_lattice_points", ctypes.c_uint32), ("far_steps_per_pass", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32)]
+
+
+class BrickInfoC(ctypes.Structure):
+    _fields_ = [("region_min", ctypes.c_float * 3), ("region_max", ctypes.c_float * 3),
+                ("bricks", ctypes.c_uint32 * 3), ("near_bricks", ctypes.c_uint32), ("exact_leaves", ctypes.c_uint32),
+                ("max_lipschitz", ctypes.c_float), ("band", ctypes.c_float), ("device_bytes", ctypes.c_uint64),
+                ("build_ms", ctypes.c_double)]
+
+
+class BatchItemC(ctypes.Structure):
+    _fields_ = [("scene", ctypes.c_void_p), ("options", RenderOptionsC), ("aa_samples", ctypes.c_uint32),
+                ("max_depth", ctypes.c_uint32)]
+
+
+class BatchTuningC(ctypes.Structure):
+    _fields_ = [("tile_w", ctypes.c_uint32), ("tile_h", ctypes.c_uint32), ("refill", ctypes.c_uint32),
+                ("ms", ctypes.c_float)]
+
+
+FT_BATCH_FP16_BRICKS = 1
+
+
+class ViewC(ctypes.Structure):
+    _fields_ = [("origin", ctypes.c_float * 3), ("target", ctypes.c_float * 3), ("fov_y_degrees", ctypes.c_float)]
+
+
+class ParamC(ctypes.Structure):
+    _fields_ = [("node", ctypes.c_int32), ("field", ctypes.c_int32)]
+
+
+FT_PARAM_FIELDS = ("cx", "cy", "cz", "rot_y", "s0", "s1", "s2", "radius")
 
 # Every symbol include/forgedthoughts_gb300.h declares, with its signature.
 SIGNATURES = {
@@ -117,10 +155,36 @@ SIGNATURES = {
                                        ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
                                        ctypes.c_void_p]),
     "ft_render_depth_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RenderOptionsC), ctypes.c_int,
-                                             ctypes.c_uint32, ctypes.POINTER(RenderStatsC)]),
+                                             ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(RenderStatsC)]),
+    "ft_scene_build_bricks": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BrickOptionsC),
+                                             ctypes.POINTER(BrickInfoC)]),
+    "ft_scene_brick_bounds": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p,
+                                             ctypes.c_void_p]),
     "ft_measure_fp32_peak": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double)]),
     "ft_render_trace_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RenderOptionsC), ctypes.c_int,
                                              ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(RenderStatsC)]),
+    "ft_batch_create": (ctypes.c_int, [ctypes.POINTER(BatchItemC), ctypes.c_uint32, ctypes.c_uint32,
+                                       ctypes.POINTER(ctypes.c_void_p)]),
+    "ft_batch_set_tuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BatchTuningC)]),
+    "ft_batch_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BatchTuningC)]),
+    "ft_batch_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "ft_batch_read": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p,
+                                     ctypes.c_void_p, ctypes.c_void_p]),
+    "ft_batch_samples": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]),
+    "ft_batch_destroy": (None, [ctypes.c_void_p]),
+    "ft_scene_param_layout": (ctypes.c_int, [ctypes.POINTER(SceneDescC), ctypes.c_uint32, ctypes.POINTER(ParamC),
+                                             ctypes.POINTER(ctypes.c_uint32)]),
+    "ft_scene_desc_get_params": (ctypes.c_int, [ctypes.POINTER(SceneDescC), ctypes.POINTER(ParamC), ctypes.c_uint32,
+                                                ctypes.c_void_p]),
+    "ft_scene_desc_set_params": (ctypes.c_int, [ctypes.POINTER(SceneDescC), ctypes.POINTER(ParamC), ctypes.c_uint32,
+                                                ctypes.c_void_p]),
+    "ft_render_views": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ViewC), ctypes.c_uint32,
+                                       ctypes.POINTER(RenderOptionsC), ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p,
+                                       ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p]),
+    "ft_render_backward": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ViewC), ctypes.c_uint32,
+                                          ctypes.POINTER(RenderOptionsC), ctypes.c_float, ctypes.POINTER(ParamC),
+                                          ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_uint32, ctypes.c_void_p]),
     "ft_render_depth_preview_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RenderOptionsC), ctypes.c_int,
                                                        ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p]),
 }

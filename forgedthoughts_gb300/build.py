@@ -37,7 +37,7 @@ CXXFLAGS = ["-std=c++17", "-O2", "-fPIC", "-Wall", "-Wextra", "-Wno-unused-param
 CPP_SOURCES = ["frontend_parse.cpp", "frontend_eval.cpp", "frontend_lower.cpp", "frontend_api.cpp",
                "scene_build.cpp"]
 CU_SOURCES = ["ft_render.cu"]
-HEADERS = ["frontend.h", "common.h", "scene_build.h", "ft_device.cuh", "ft_trace.cuh"]
+HEADERS = ["frontend.h", "common.h", "scene_build.h", "ft_device.cuh", "ft_trace.cuh", "ft_bricks.cuh", "ft_diff.cuh"]
 
 
 def _nvcc() -> str:

@@ -1,0 +1,222 @@
+// FP16 brick distance cache: the precision form of the depth march.
+//
+// There is no counterpart in the reference (its `Bricks` accelerator,
+// R:824-1022, is a grid of leaf lists).  The distance field of the scene
+// without its few very large leaves is sampled on a lattice of spacing h over
+// a region around the other leaves.  The region is cut into bricks of 8^3
+// voxels; each brick gets an interpolation error bound
+//
+//     delta_b = safety * max(L_b, 1) * h * sqrt(3),
+//
+// where L_b is the largest finite difference |dF| / h between neighbouring
+// lattice points of the brick.  Every lattice point is stored as one FP16
+// texel of a 3D texture holding
+//
+//     round_down_fp16( F(point) - max delta_b over the bricks sharing it ).
+//
+// For a field that is L_b-Lipschitz inside the brick, every corner of the
+// voxel holding p then stores a value <= F(p), and so does any convex
+// combination of them: the hardware trilinear fetch (its 8-bit fixed-point
+// weights still sum to one) is a lower bound of F(p), one fetch per step with
+// no table indirection.  All bricks are stored (2 bytes per lattice point):
+// far from surfaces the bound is F - delta too, so far-field steps stay at
+// least as long as the plain march's 0.7 |F| once |F| exceeds about 3 delta.
+//
+// Included by ft_render.cu after the exact evaluators, inside its anonymous
+// namespace.
+#pragma once
+
+constexpr int kBrickVox = 8;   // voxels per brick edge
+constexpr int kMaxExactLeaves = 4;
+
+struct DevBricks {
+  float rmin[3];             // lattice point (0, 0, 0)
+  float rmax[3];             // last lattice point
+  float inv_h;               // 1 / voxel size
+  float last[3];             // lattice points per axis - 1
+  cudaTextureObject_t atlas; // FP16 texels, linear filtering, unnormalised coordinates
+  float band, band_exit;
+  int32_t far_batch;         // far-field steps per pass of the warp
+  int32_t n_exact;
+  int32_t exact_leaf[kMaxExactLeaves];
+};
+
+// Leaf-BVH walk of the scene minus the exact leaves (bvh_distance_info,
+// R:743-786, with those leaves left out): the field the cache samples.
+template <bool kStats>
+__device__ Info scene_distance_skip(const DevScene& S, F3 p, const DevBricks& B, Ctx<kStats>& cx) {
+  float best = kInf;
+  Info cur{kInf, 0u, 0u};
+  int stack[64];
+  float stack_lb[64];
+  int sp = 0;
+  stack[sp] = S.bvh_root;
+  stack_lb[sp] = node_lb(p, S.bvh[S.bvh_root].bmin, S.bvh[S.bvh_root].bmax);
+  ++sp;
+  while (sp > 0) {
+    --sp;
+    int ni = stack[sp];
+    if (stack_lb[sp] > best) continue;
+    const DevBvhNode& n = S.bvh[ni];
+    if (n.leaf >= 0) {
+      bool skip = false;
+      for (int i = 0; i < B.n_exact; ++i) skip |= (B.exact_leaf[i] == n.leaf);
+      if (skip) continue;
+      Info in = eval_leaf(S, S.leaves[n.leaf], p, best, cx);
+      if (in.d < best) {
+        best = in.d;
+        cur = in;
+      }
+      continue;
+    }
+    float ll = node_lb(p, S.bvh[n.lhs].bmin, S.bvh[n.lhs].bmax), rl = node_lb(p, S.bvh[n.rhs].bmin, S.bvh[n.rhs].bmax);
+    if (sp + 2 > 64) break;
+    if (ll <= rl) {
+      stack[sp] = n.rhs; stack_lb[sp] = rl; ++sp;
+      stack[sp] = n.lhs; stack_lb[sp] = ll; ++sp;
+    } else {
+      stack[sp] = n.lhs; stack_lb[sp] = ll; ++sp;
+      stack[sp] = n.rhs; stack_lb[sp] = rl; ++sp;
+    }
+  }
+  return cur;
+}
+
+// Far-field lower bound of the scene distance at p: the cached field (one
+// texture fetch) and the exact leaves.  Returns false outside the brick
+// region, where the march is exact (a distance-to-region bound would give
+// tiny steps to rays passing close to the region's box, and the exact field
+// outside it is cheap: the cached leaves are culled by their boxes).
+template <bool kStats>
+__device__ __forceinline__ bool far_bound(const DevScene& S, const DevBricks& B, F3 p, float* out, Ctx<kStats>& cx) {
+  float gx = (p.x - B.rmin[0]) * B.inv_h, gy = (p.y - B.rmin[1]) * B.inv_h, gz = (p.z - B.rmin[2]) * B.inv_h;
+  if (!(gx >= 0.0f && gy >= 0.0f && gz >= 0.0f && gx <= B.last[0] && gy <= B.last[1] && gz <= B.last[2]))
+    return false;
+  cx.fetch();
+  // texel centres sit at integer + 0.5 in unnormalised coordinates
+  float v = tex3D<float>(B.atlas, gx + 0.5f, gy + 0.5f, gz + 0.5f);
+  for (int i = 0; i < B.n_exact; ++i) v = fminf(v, eval_leaf(S, S.leaves[B.exact_leaf[i]], p, kInf, cx).d);
+  *out = v;
+  return true;
+}
+
+// ------------------------------------------------------------------ build
+
+struct BrickBuild {
+  float rmin[3];
+  float h;
+  int32_t dims[3];
+  uint32_t nx, ny, nz;  // lattice points per axis (dims * 8 + 1)
+};
+
+// Sample the cached field at every lattice point.
+__global__ void __launch_bounds__(128) brick_lattice_kernel(DevScene S, DevBricks B, BrickBuild G,
+                                                            float* __restrict__ lattice) {
+  Ctx<false> cx;
+  cx.c = Counters{};
+  const uint64_t n = (uint64_t)G.nx * G.ny * G.nz;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t x = (uint32_t)(i % G.nx);
+    uint64_t r = i / G.nx;
+    uint32_t y = (uint32_t)(r % G.ny);
+    uint32_t z = (uint32_t)(r / G.ny);
+    F3 p = f3(G.rmin[0] + G.h * (float)x, G.rmin[1] + G.h * (float)y, G.rmin[2] + G.h * (float)z);
+    lattice[i] = scene_distance_skip(S, p, B, cx).d;
+  }
+}
+
+__device__ __forceinline__ size_t lattice_index(const BrickBuild& G, uint32_t x, uint32_t y, uint32_t z) {
+  return (size_t)x + (size_t)G.nx * ((size_t)y + (size_t)G.ny * z);
+}
+
+// One warp per brick: its Lipschitz estimate and error bound, and whether a
+// surface passes within `near` of it (for the build summary).
+__global__ void __launch_bounds__(128) brick_bound_kernel(BrickBuild G, const float* __restrict__ lattice,
+                                                          float safety, float near, float* __restrict__ delta,
+                                                          unsigned int* __restrict__ near_count,
+                                                          unsigned int* __restrict__ max_lip_bits) {
+  constexpr uint32_t kPts = kBrickVox + 1;
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint64_t n_cells = (uint64_t)G.dims[0] * G.dims[1] * G.dims[2];
+  const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x / 32);
+  for (uint64_t cell = (uint64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32; cell < n_cells; cell += warps) {
+    uint32_t cx = (uint32_t)(cell % G.dims[0]);
+    uint64_t r = cell / G.dims[0];
+    uint32_t cy = (uint32_t)(r % G.dims[1]);
+    uint32_t cz = (uint32_t)(r / G.dims[1]);
+    float vmin = kInf, dmax = 0.0f;
+    for (uint32_t k = lane; k < kPts * kPts * kPts; k += 32) {
+      uint32_t lx = k % kPts, ly = (k / kPts) % kPts, lz = k / (kPts * kPts);
+      uint32_t x = cx * kBrickVox + lx, y = cy * kBrickVox + ly, z = cz * kBrickVox + lz;
+      float v = lattice[lattice_index(G, x, y, z)];
+      vmin = fminf(vmin, v);
+      // Pairs with both samples inside a solid are left out: the far field is
+      // only used at points with a positive bound, and the reference's leaf
+      // culling makes the field jump inside overlapping solids.
+      float w;
+      if (lx + 1 < kPts) {
+        w = lattice[lattice_index(G, x + 1, y, z)];
+        if (v >= 0.0f || w >= 0.0f) dmax = fmaxf(dmax, fabsf(w - v));
+      }
+      if (ly + 1 < kPts) {
+        w = lattice[lattice_index(G, x, y + 1, z)];
+        if (v >= 0.0f || w >= 0.0f) dmax = fmaxf(dmax, fabsf(w - v));
+      }
+      if (lz + 1 < kPts) {
+        w = lattice[lattice_index(G, x, y, z + 1)];
+        if (v >= 0.0f || w >= 0.0f) dmax = fmaxf(dmax, fabsf(w - v));
+      }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+      vmin = fminf(vmin, __shfl_xor_sync(0xffffffffu, vmin, off));
+      dmax = fmaxf(dmax, __shfl_xor_sync(0xffffffffu, dmax, off));
+    }
+    if (lane == 0) {
+      float lip = fmaxf(dmax / G.h, 1.0f);
+      float del = safety * lip * G.h * 1.7320508f;
+      delta[cell] = del;
+      if (vmin - del < near) atomicAdd(near_count, 1u);
+      atomicMax(max_lip_bits, __float_as_uint(lip));  // positive floats order like their bits
+    }
+  }
+}
+
+// One texel per lattice point: the sample lowered by the largest bound of the
+// (up to eight) bricks sharing the point, rounded down to FP16.
+__global__ void __launch_bounds__(256) brick_texel_kernel(BrickBuild G, const float* __restrict__ lattice,
+                                                          const float* __restrict__ delta, cudaSurfaceObject_t atlas) {
+  const uint64_t n = (uint64_t)G.nx * G.ny * G.nz;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t x = (uint32_t)(i % G.nx);
+    uint64_t r = i / G.nx;
+    uint32_t y = (uint32_t)(r % G.ny);
+    uint32_t z = (uint32_t)(r / G.ny);
+    // bricks along each axis that contain this lattice coordinate
+    int bx1 = min((int)(x / kBrickVox), G.dims[0] - 1), bx0 = (x % kBrickVox == 0 && x > 0) ? bx1 - 1 : bx1;
+    int by1 = min((int)(y / kBrickVox), G.dims[1] - 1), by0 = (y % kBrickVox == 0 && y > 0) ? by1 - 1 : by1;
+    int bz1 = min((int)(z / kBrickVox), G.dims[2] - 1), bz0 = (z % kBrickVox == 0 && z > 0) ? bz1 - 1 : bz1;
+    if (x == G.nx - 1) bx0 = bx1;
+    if (y == G.ny - 1) by0 = by1;
+    if (z == G.nz - 1) bz0 = bz1;
+    float del = 0.0f;
+    for (int bz = bz0; bz <= bz1; ++bz)
+      for (int by = by0; by <= by1; ++by)
+        for (int bx = bx0; bx <= bx1; ++bx)
+          del = fmaxf(del, delta[(size_t)bx + (size_t)G.dims[0] * ((size_t)by + (size_t)G.dims[1] * bz)]);
+    __half hv = __float2half_rd(lattice[i] - del);
+    surf3Dwrite(__half_as_ushort(hv), atlas, (int)(x * sizeof(unsigned short)), (int)y, (int)z);
+  }
+}
+
+// Validation: the far-field bound and the exact distance at given points.
+__global__ void brick_query_kernel(DevScene S, DevBricks B, const float* __restrict__ pts, uint32_t n,
+                                   float* __restrict__ bound, float* __restrict__ exact) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  Ctx<false> cx;
+  cx.c = Counters{};
+  F3 p = f3(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]);
+  float b;
+  bound[i] = far_bound(S, B, p, &b, cx) ? b : __int_as_float(0x7fc00000);  // NaN: no bound here
+  exact[i] = scene_distance(S, p, cx).d;
+}

@@ -7,12 +7,15 @@
 // the reference's order (R:743-786) visits leaves in the same sequence.
 #include "scene_build.h"
 
+#include "common.h"
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <functional>
 #include <limits>
 #include <numeric>
+#include <string>
 #include <atomic>
 #include <thread>
 
@@ -647,7 +650,7 @@ bool build_scene_image(const ft_scene_desc& desc, SceneImage* out, std::string* 
 
 // parse_camera (R:6263-6286) + PinholeCamera::generate_ray basis
 // (crates/forgedthoughts/src/render_api.rs:132-144), all in f32.
-CameraBasis resolve_camera(const SceneImage& img, const ft_render_options& opt) {
+CameraBasis camera_basis(const float org[3], const float tgt[3], float fov) {
   auto normalize = [](float v[3]) {
     float l = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
     if (l <= std::numeric_limits<float>::epsilon()) return;
@@ -662,15 +665,7 @@ CameraBasis resolve_camera(const SceneImage& img, const ft_render_options& opt) 
     o[2] = a[0] * b[1] - a[1] * b[0];
   };
   CameraBasis cb;
-  float org[3] = {img.scene_center[0], img.scene_center[1], img.scene_center[2] + opt.camera_z};
-  float tgt[3] = {img.scene_center[0], img.scene_center[1], img.scene_center[2]};
-  float fov = opt.fov_y_degrees;
-  if (img.has_camera) {
-    if (!std::isnan(img.camera.origin[0])) std::memcpy(org, img.camera.origin, sizeof(org));
-    if (!std::isnan(img.camera.target[0])) std::memcpy(tgt, img.camera.target, sizeof(tgt));
-    if (!std::isnan(img.camera.fov_y_degrees)) fov = img.camera.fov_y_degrees;
-  }
-  std::memcpy(cb.origin, org, sizeof(org));
+  std::memcpy(cb.origin, org, sizeof(cb.origin));
   float up0[3] = {0.0f, 1.0f, 0.0f};
   float f[3] = {tgt[0] - org[0], tgt[1] - org[1], tgt[2] - org[2]};
   normalize(f);
@@ -687,4 +682,150 @@ CameraBasis resolve_camera(const SceneImage& img, const ft_render_options& opt) 
   return cb;
 }
 
+CameraBasis resolve_camera(const SceneImage& img, const ft_render_options& opt) {
+  float org[3] = {img.scene_center[0], img.scene_center[1], img.scene_center[2] + opt.camera_z};
+  float tgt[3] = {img.scene_center[0], img.scene_center[1], img.scene_center[2]};
+  float fov = opt.fov_y_degrees;
+  if (img.has_camera) {
+    if (!std::isnan(img.camera.origin[0])) std::memcpy(org, img.camera.origin, sizeof(org));
+    if (!std::isnan(img.camera.target[0])) std::memcpy(tgt, img.camera.target, sizeof(tgt));
+    if (!std::isnan(img.camera.fov_y_degrees)) fov = img.camera.fov_y_degrees;
+  }
+  return camera_basis(org, tgt, fov);
+}
+
 }  // namespace ftgpu
+
+// ------------------------------------------------------------ parameters
+namespace {
+
+bool param_prim(const ft_node& n) { return n.kind == FT_NODE_SPHERE || n.kind == FT_NODE_BOX; }
+
+// union_round trees reachable from the root, each as (root node, in-order
+// primitives); false with `error` when a tree holds something the adjoint
+// does not differentiate.
+bool param_trees(const ft_scene_desc& d, std::vector<std::pair<int, std::vector<int>>>* trees, std::string* error) {
+  std::vector<std::pair<int, int>> stack{{d.root, -1}};  // (node, parent kind)
+  std::vector<char> seen(d.n_nodes, 0);
+  while (!stack.empty()) {
+    auto [i, parent_kind] = stack.back();
+    stack.pop_back();
+    if (i < 0 || static_cast<uint32_t>(i) >= d.n_nodes || seen[i]) continue;
+    seen[i] = 1;
+    const ft_node& n = d.nodes[i];
+    if (n.kind == FT_NODE_UNION_ROUND && parent_kind != FT_NODE_UNION_ROUND) {
+      std::vector<int> prims;
+      std::vector<int> walk{i};
+      // in-order: left subtree first
+      std::function<bool(int)> rec = [&](int k) -> bool {
+        if (k < 0 || static_cast<uint32_t>(k) >= d.n_nodes) return false;
+        const ft_node& m = d.nodes[k];
+        if (m.kind == FT_NODE_UNION_ROUND) return rec(m.a) && rec(m.b);
+        if (!param_prim(m)) {
+          *error = "union_round tree holds a node kind the adjoint does not differentiate";
+          return false;
+        }
+        bool shell = m.kind == FT_NODE_SPHERE ? m.f[1] != 0.0f : (m.f[3] != 0.0f || m.f[4] != 0.0f);
+        if (shell || m.rot_deg[0] != 0.0f || m.rot_deg[2] != 0.0f) {
+          *error = "differentiable primitives need no x / z rotation, rounding or shell";
+          return false;
+        }
+        prims.push_back(k);
+        return true;
+      };
+      if (!rec(i)) {
+        if (error->empty()) *error = "malformed union_round tree";
+        return false;
+      }
+      trees->emplace_back(i, std::move(prims));
+      continue;
+    }
+    if (n.kind >= FT_NODE_UNION && n.kind != FT_NODE_SLICE && n.kind != FT_NODE_SMOOTH) {
+      stack.push_back({n.b, n.kind});
+      stack.push_back({n.a, n.kind});
+    }
+  }
+  return true;
+}
+
+float* param_field(ft_node& n, int field) {
+  switch (field) {
+    case FT_PARAM_CX: return &n.center[0];
+    case FT_PARAM_CY: return &n.center[1];
+    case FT_PARAM_CZ: return &n.center[2];
+    case FT_PARAM_ROT_Y: return &n.rot_deg[1];
+    case FT_PARAM_S0: return &n.f[0];
+    case FT_PARAM_S1: return &n.f[1];
+    case FT_PARAM_S2: return &n.f[2];
+    case FT_PARAM_RADIUS: return &n.f[0];
+    default: return nullptr;
+  }
+}
+
+bool check_param(const ft_scene_desc& d, const ft_param& p) {
+  if (p.node < 0 || static_cast<uint32_t>(p.node) >= d.n_nodes || p.field < 0 || p.field > FT_PARAM_RADIUS) return false;
+  const ft_node& n = d.nodes[p.node];
+  return p.field == FT_PARAM_RADIUS ? n.kind == FT_NODE_UNION_ROUND : param_prim(n);
+}
+
+}  // namespace
+
+extern "C" {
+
+ft_status ft_scene_param_layout(const ft_scene_desc* desc, uint32_t capacity, ft_param* params, uint32_t* count) {
+  if (!desc || !count || (capacity && !params))
+    return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "desc, count and params must be non-null");
+  if (desc->root < 0 || static_cast<uint32_t>(desc->root) >= desc->n_nodes || !desc->nodes)
+    return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "invalid scene description");
+  std::vector<std::pair<int, std::vector<int>>> trees;
+  std::string err;
+  if (!param_trees(*desc, &trees, &err)) return ftcommon::fail(FT_ERR_UNSUPPORTED, err);
+  std::vector<ft_param> out;
+  for (const auto& tr : trees) {
+    for (int prim : tr.second)
+      for (int f = FT_PARAM_CX; f <= FT_PARAM_S2; ++f) out.push_back(ft_param{prim, f});
+    out.push_back(ft_param{tr.first, FT_PARAM_RADIUS});
+  }
+  *count = static_cast<uint32_t>(out.size());
+  for (uint32_t i = 0; i < std::min<uint32_t>(capacity, *count); ++i) params[i] = out[i];
+  ftcommon::clear_last_error();
+  return FT_OK;
+}
+
+ft_status ft_scene_desc_get_params(const ft_scene_desc* desc, const ft_param* params, uint32_t n, float* values) {
+  if (!desc || (n && (!params || !values))) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "null argument");
+  for (uint32_t i = 0; i < n; ++i) {
+    if (!check_param(*desc, params[i]))
+      return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "parameter " + std::to_string(i) + " is not differentiable");
+    values[i] = *param_field(const_cast<ft_node&>(desc->nodes[params[i].node]), params[i].field);
+  }
+  return FT_OK;
+}
+
+ft_status ft_scene_desc_set_params(ft_scene_desc* desc, const ft_param* params, uint32_t n, const float* values) {
+  if (!desc || (n && (!params || !values))) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "null argument");
+  for (uint32_t i = 0; i < n; ++i)
+    if (!check_param(*desc, params[i]) || !std::isfinite(values[i]))
+      return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "parameter " + std::to_string(i) + " is invalid");
+  for (uint32_t i = 0; i < n; ++i) {
+    if (params[i].field == FT_PARAM_RADIUS) {
+      std::vector<int> stack{params[i].node};
+      while (!stack.empty()) {
+        int k = stack.back();
+        stack.pop_back();
+        if (k < 0 || static_cast<uint32_t>(k) >= desc->n_nodes) continue;
+        // descriptions are library- or caller-owned writable arrays behind a const view
+        ft_node& m = const_cast<ft_node&>(desc->nodes[k]);
+        if (m.kind != FT_NODE_UNION_ROUND) continue;
+        m.f[0] = values[i];
+        stack.push_back(m.a);
+        stack.push_back(m.b);
+      }
+    } else {
+      *param_field(const_cast<ft_node&>(desc->nodes[params[i].node]), params[i].field) = values[i];
+    }
+  }
+  return FT_OK;
+}
+
+}  // extern "C"

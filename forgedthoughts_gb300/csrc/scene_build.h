@@ -130,5 +130,7 @@ struct CameraBasis {
   float tan_fov;
 };
 CameraBasis resolve_camera(const SceneImage& img, const ft_render_options& opt);
+// Basis of a camera at `org` looking at `tgt` (up (0, 1, 0)).
+CameraBasis camera_basis(const float org[3], const float tgt[3], float fov);
 
 }  // namespace ftgpu

@@ -148,3 +148,78 @@ def twisted_shells(n: int = 4096, seed: int = 0, width: int = 1920, height: int 
     lines.append("let scene = ground + " + " + ".join(names) + ";")
     return Workload(f"twisted_shells{n}_{width}x{height}", "\n".join(lines) + "\n", _march_options(width, height),
                     AccelMode.Bvh, 1, 2)
+
+
+def batch_scenes(n: int = 256, first_seed: int = 0) -> list:
+    """Independent scenes of uneven size for the batched launch.
+
+    Scene i uses seed first_seed + i: primitive count round(exp(U[ln 8,
+    ln 2048])) spheres drawn as in spheres_on_ground (radius U[0.2, 0.6],
+    centre U([-2, 2] x [0.2, 1.5] x [-2, 2])) over the ground box; resolution
+    uniform from {64^2, 128^2, 256^2, 512^2}; camera on the ring of radius 5 at
+    height 1 around the origin at azimuth U[0, 2 pi), looking at the origin,
+    fov 45; depth-only (p 0.5) or a Whitted trace of max depth 2.  One
+    sample per pixel, Bvh accelerator.
+    """
+    out = []
+    for i in range(n):
+        rng = np.random.default_rng(first_seed + i)
+        count = int(round(np.exp(rng.uniform(np.log(8), np.log(2048)))))
+        res = int(rng.choice([64, 128, 256, 512]))
+        az = rng.uniform(0, 2 * np.pi)
+        trace = bool(rng.uniform() < 0.5)
+        eye = (5.0 * np.sin(az), 1.0, -5.0 * np.cos(az))
+        lines = [f"let camera = Camera {{ origin: {v3(*eye)}, target: {v3(0, 0, 0)}, fov_y: 45.0 }};", GROUND]
+        names = []
+        for j in range(count):
+            r = rng.uniform(0.2, 0.6)
+            c = (rng.uniform(-2, 2), rng.uniform(0.2, 1.5), rng.uniform(-2, 2))
+            lines.append(f"let s{j} = Sphere {{ radius: {num(r)}, pos: {v3(*c)} }};")
+            names.append(f"s{j}")
+        lines.append("let scene = ground + " + " + ".join(names) + ";")
+        out.append(Workload(f"batch{i}_spheres{count}_{res}x{res}_{'trace2' if trace else 'depth'}",
+                            "\n".join(lines) + "\n", _march_options(res, res), AccelMode.Bvh, 1,
+                            2 if trace else 0))
+    return out
+
+
+def shape_fit(n: int = 64, seed: int = 7, k: float = 0.15) -> str:
+    """Inverse shape fitting scene: n primitives (even i sphere, odd i box) in a
+    balanced pairwise union_round(k) tree, no ground.
+
+    Centre U([-1.2, 1.2] x [-0.6, 0.8] x [-1.2, 1.2]); sphere radius
+    U[0.15, 0.35]; box half size U[0.1, 0.3]^3; rot.y U[0, 360) degrees.  The
+    parameter layout is 7 per primitive plus the shared radius (449 for 64).
+    """
+    rng = np.random.default_rng(seed)
+    lines = []
+    prims = []
+    for i in range(n):
+        c = (rng.uniform(-1.2, 1.2), rng.uniform(-0.6, 0.8), rng.uniform(-1.2, 1.2))
+        if i % 2 == 0:
+            size = f"radius: {num(rng.uniform(0.15, 0.35))}"
+            kind = "Sphere"
+        else:
+            h = rng.uniform(0.1, 0.3, 3)
+            size = f"size: {v3(2 * h[0], 2 * h[1], 2 * h[2])}"
+            kind = "Box"
+        rot = rng.uniform(0, 360)
+        lines.append(f"let p{i} = {kind} {{ {size}, pos: {v3(*c)}, rot: {v3(0, rot, 0)} }};")
+        prims.append(f"p{i}")
+    level = 0
+    while len(prims) > 1:
+        nxt = []
+        for j in range(0, len(prims) - 1, 2):
+            name = f"u{level}_{j // 2}"
+            lines.append(f"let {name} = {prims[j]}.union_round({prims[j + 1]}, {num(k)});")
+            nxt.append(name)
+        if len(prims) % 2:
+            nxt.append(prims[-1])
+        prims = nxt
+        level += 1
+    lines.append(f"let scene = {prims[0]};")
+    return "\n".join(lines) + "\n"
+
+
+def shape_fit_options(size: int = 256) -> RenderOptions:
+    return _march_options(size, size)

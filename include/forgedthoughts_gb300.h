@@ -269,6 +269,8 @@ typedef struct ft_scene ft_scene;
 
 /* Render-call flags. */
 #define FT_FLAG_DEVICE_POINTERS 1u  /* output pointers are device memory */
+#define FT_FLAG_FP16_BRICKS 2u      /* depth march through the FP16 brick cache
+                                       (ft_scene_build_bricks must have run) */
 
 /* ---------------------------------------------------------------------------
  * Entry points.
@@ -355,7 +357,9 @@ typedef struct ft_render_stats {
   uint64_t primitive_evals;
   uint64_t box_tests;
   uint64_t hook_instrs;
-  uint64_t march_steps;
+  uint64_t march_steps;     /* exact (FP32) march steps */
+  uint64_t far_steps;       /* far-field steps on the FP16 brick bound */
+  uint64_t brick_fetches;   /* trilinear FP16 texture fetches */
 } ft_render_stats;
 
 /* Depth preview for callers that cannot allocate device memory.
@@ -384,14 +388,185 @@ ft_status ft_render_depth_preview_noalloc(ft_scene* scene, const ft_render_optio
                                           ft_accel_mode accel, uint32_t aa_samples,
                                           uint8_t* rgb8_out, void* stream);
 
+/* Counters of one depth march with `flags` (FT_FLAG_FP16_BRICKS selects the
+ * precision form); the outputs are discarded. */
 ft_status ft_render_depth_stats(ft_scene* scene, const ft_render_options* options,
-                                ft_accel_mode accel, uint32_t aa_samples,
+                                ft_accel_mode accel, uint32_t aa_samples, uint32_t flags,
                                 ft_render_stats* stats);
 
 /* The same counters for a Whitted trace (ft_render_trace); output discarded. */
 ft_status ft_render_trace_stats(ft_scene* scene, const ft_render_options* options,
                                 ft_accel_mode accel, uint32_t aa_samples, uint32_t max_depth,
                                 ft_render_stats* stats);
+
+/* FP16 brick distance cache: the precision form of the depth march.
+ *
+ * No counterpart in the reference, whose `Bricks` accelerator is a grid of
+ * leaf lists (R:824-1022).  The scene's distance field without its few very
+ * large leaves (a ground box) is sampled on a lattice of `voxel_size` over the
+ * region around the other leaves, cut into bricks of 8^3 voxels.  Each brick
+ * gets an interpolation error bound (its Lipschitz estimate x voxel diagonal
+ * x `safety`); every lattice point is stored as one FP16 texel of a 3D
+ * texture holding the sample minus the largest bound of the bricks sharing
+ * it, rounded down, so a hardware trilinear fetch is a lower bound of the
+ * distance.
+ *
+ * ft_render_depth with FT_FLAG_FP16_BRICKS marches on that bound (large
+ * leaves evaluated exactly; exact march outside the region) while it is at
+ * least `band`, stepping by the
+ * bound minus band/2, then continues with the exact FP32 march of the plain
+ * method (same step rule), returning to the far field when the exact distance
+ * exceeds band_exit.  At the hit, secant steps on the exact distance between
+ * the last two exact points find the eps-shell crossing (each verified by an
+ * exact evaluation); the normal is the plain method's six-tap estimate.
+ * Build once per scene; rebuilding replaces the cache.  Synchronous on the
+ * legacy default stream. */
+typedef struct ft_brick_options {
+  float voxel_size;             /* lattice spacing; 0 = 0.02 */
+  float band;                   /* far-field threshold; 0 = 4 voxels */
+  float safety;                 /* factor on the error bound; 0 = 1.25 */
+  uint32_t max_lattice_points;  /* refuse larger lattices; 0 = 2^29 */
+  uint32_t far_steps_per_pass;  /* far-field steps a lane takes per pass of its warp; 0 = 4 */
+  uint32_t reserved;
+} ft_brick_options;
+
+typedef struct ft_brick_info {
+  float region_min[3];
+  float region_max[3];
+  uint32_t bricks[3];         /* bricks per axis */
+  uint32_t near_bricks;       /* bricks with a surface within band + half a brick */
+  uint32_t exact_leaves;      /* large leaves evaluated exactly */
+  float max_lipschitz;        /* largest per-brick Lipschitz estimate */
+  float band;                 /* effective far-field threshold */
+  uint64_t device_bytes;      /* FP16 texture */
+  double build_ms;
+} ft_brick_info;
+
+ft_status ft_scene_build_bricks(ft_scene* scene, const ft_brick_options* options, ft_brick_info* info);
+
+/* Far-field bound and exact scene distance at `n` points (host arrays of
+ * n*3 / n floats): bound_out[i] is the brick cache's lower bound (NaN outside
+ * the brick region), exact_out[i] the exact FP32 distance of the plain march.
+ * For validating the cache. */
+ft_status ft_scene_brick_bounds(ft_scene* scene, const float* points, uint32_t n, float* bound_out,
+                                float* exact_out);
+
+/* ---------------------------------------------------------------------------
+ * Batched form: many independent renders (scenes, views, resolutions, depth
+ * previews and Whitted traces mixed) in one CUDA-graph launch.  No
+ * counterpart in the reference, which renders one scene per call.
+ *
+ * The depth items run in one persistent march kernel whose warps take rays of
+ * any item from a global counter (a lane keeps its item's scene, parameters
+ * and brick cache), the trace items in one persistent trace kernel, and one
+ * pixel kernel writes every item's image; the three are captured once into a
+ * CUDA graph.  Work items are tiles of tile_w x tile_h pixels (x AA
+ * samples); a warp of the depth march refills its idle lanes when at least
+ * `refill` of them are idle.  ft_batch_autotune times the candidate tiles
+ * (8x8, 16x8, 32x8) and refill thresholds (4, 8, 16) on this batch and keeps
+ * the fastest.
+ * ------------------------------------------------------------------------- */
+typedef struct ft_batch ft_batch;
+
+typedef struct ft_batch_item {
+  ft_scene* scene;             /* must outlive the batch */
+  ft_render_options options;   /* resolution and march parameters */
+  uint32_t aa_samples;
+  uint32_t max_depth;          /* 0: depth preview; 1..10: Whitted trace depth */
+} ft_batch_item;
+
+typedef struct ft_batch_tuning {
+  uint32_t tile_w, tile_h;     /* pixels per work tile (1..64 each) */
+  uint32_t refill;             /* 1..32 */
+  float ms;                    /* batch time measured by ft_batch_autotune */
+} ft_batch_tuning;
+
+#define FT_BATCH_FP16_BRICKS 1u  /* depth items march through their scenes' brick caches */
+
+ft_status ft_batch_create(const ft_batch_item* items, uint32_t n_items, uint32_t flags, ft_batch** out);
+ft_status ft_batch_set_tuning(ft_batch* batch, const ft_batch_tuning* tuning);
+ft_status ft_batch_autotune(ft_batch* batch, ft_batch_tuning* best);
+/* Enqueue the whole batch (one graph launch) on `stream`; returns without
+ * waiting.  Calls on one batch must not overlap on the GPU. */
+ft_status ft_batch_launch(ft_batch* batch, void* stream);
+/* Host copies of one item's outputs after the launch has completed (the call
+ * synchronises the device): t_out / mask_out (w*h*aa, depth items only),
+ * rgb_out (w*h*3 floats: preview value or averaged radiance), rgb8_out
+ * (w*h*3: the gray preview or the Reinhard image).  Each nullable. */
+ft_status ft_batch_read(ft_batch* batch, uint32_t item, float* t_out, uint8_t* mask_out, float* rgb_out,
+                        uint8_t* rgb8_out);
+ft_status ft_batch_samples(const ft_batch* batch, uint64_t* primary_samples);
+void ft_batch_destroy(ft_batch* batch);
+
+/* ---------------------------------------------------------------------------
+ * Differentiation form: multi-view depth + soft silhouette of a scene whose
+ * union_round tree carries the parameters, and the adjoint of that render.
+ * No counterpart in the reference (it has no gradients).
+ *
+ * Forward, per ray of each view (the reference camera, R:6263-6286, one
+ * sample per pixel at the pixel centre):
+ *   - the plain march (step rule, eps hit, ten bisections, R:4091-4200);
+ *   - on a hit, depth t* = the zero of f(o + t d) found by three secant
+ *     steps from the bisection bracket (the eps-shell crossing moved onto the
+ *     surface, so depth is a smooth function of the parameters), mask 1,
+ *     silhouette 1;
+ *   - on a miss, m* = the local minimum of f(o + t d) next to the smallest
+ *     march sample (bracket continued past either end of the samples while
+ *     f falls, then 40 golden-section steps); silhouette =
+ *     exp(-max(m*, 0) / tau), depth 0, mask 0.
+ * Backward (ft_render_backward) re-marches every ray (no per-step state is
+ * stored) and, by implicit differentiation,
+ *   d depth / d theta = -(df / d theta) / (grad_p f . d)   at the hit point,
+ *   d sil / d theta = -(sil / tau) df / d theta           at the miss minimum,
+ * with df / d theta from the primitives' and union_round blends' analytic
+ * derivatives; dL / d theta = sum over rays of dL_dt d depth / d theta +
+ * dL_dsil d sil / d theta, reduced across pixels in FP64.
+ * ------------------------------------------------------------------------- */
+typedef struct ft_view {
+  float origin[3];
+  float target[3];
+  float fov_y_degrees;
+} ft_view;
+
+typedef enum ft_param_field {
+  FT_PARAM_CX = 0,     /* primitive centre */
+  FT_PARAM_CY = 1,
+  FT_PARAM_CZ = 2,
+  FT_PARAM_ROT_Y = 3,  /* rotation about y, degrees */
+  FT_PARAM_S0 = 4,     /* sphere radius, box half size x */
+  FT_PARAM_S1 = 5,     /* box half size y (inert for spheres) */
+  FT_PARAM_S2 = 6,     /* box half size z (inert for spheres) */
+  FT_PARAM_RADIUS = 7  /* union_round blend radius of a whole tree (node = any of its union_round nodes) */
+} ft_param_field;
+
+typedef struct ft_param {
+  int32_t node;   /* ft_node index */
+  int32_t field;  /* ft_param_field */
+} ft_param;
+
+/* The differentiable parameters of `desc`: for each sphere / box primitive
+ * under a union_round tree (in node order) its seven fields, then each tree's
+ * radius.  Such primitives must have no x / z rotation, rounding or shell.
+ * Writes min(capacity, count) entries and the count. */
+ft_status ft_scene_param_layout(const ft_scene_desc* desc, uint32_t capacity, ft_param* params, uint32_t* count);
+/* Read / write parameter values in a description (radius writes every
+ * union_round node of the tree); rebuild the GPU scene after writing. */
+ft_status ft_scene_desc_get_params(const ft_scene_desc* desc, const ft_param* params, uint32_t n, float* values);
+ft_status ft_scene_desc_set_params(ft_scene_desc* desc, const ft_param* params, uint32_t n, const float* values);
+
+/* Forward: per view `width*height` samples (options give resolution and
+ * march parameters); outputs (each nullable, view-major): t_out floats,
+ * mask_out bytes, sil_out floats.  Host pointers unless
+ * FT_FLAG_DEVICE_POINTERS. */
+ft_status ft_render_views(ft_scene* scene, const ft_view* views, uint32_t n_views,
+                          const ft_render_options* options, float tau, float* t_out, uint8_t* mask_out,
+                          float* sil_out, uint32_t flags, void* stream);
+/* Adjoint: dL_dt and dL_dsil (n_views*width*height floats each, nullable =
+ * zero) to dL_dparams (n_params doubles, overwritten). */
+ft_status ft_render_backward(ft_scene* scene, const ft_view* views, uint32_t n_views,
+                             const ft_render_options* options, float tau, const ft_param* params,
+                             uint32_t n_params, const float* dL_dt, const float* dL_dsil, double* dL_dparams,
+                             uint32_t flags, void* stream);
 
 /* Measured FP32 FMA throughput of the current device in TFLOP/s (a short
  * dependent-FMA kernel), used as the roofline denominator of the march. */

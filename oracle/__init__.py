@@ -36,6 +36,12 @@ def lib() -> ctypes.CDLL:
         h.oracle_render_trace.argtypes = [vp, vp, ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int,
                                           ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, vp, vp,
                                           ctypes.POINTER(ctypes.c_uint64)]
+        h.oracle_render_views.restype = ctypes.c_int
+        h.oracle_render_views.argtypes = [vp, vp, ctypes.c_uint32, vp, ctypes.c_float, ctypes.c_int, ctypes.c_int,
+                                          vp, vp, vp]
+        h.oracle_render_backward.restype = ctypes.c_int
+        h.oracle_render_backward.argtypes = [vp, vp, ctypes.c_uint32, vp, ctypes.c_float, vp, ctypes.c_uint32, vp,
+                                             vp, ctypes.c_int, ctypes.c_int, vp]
         h.oracle_last_error.restype = ctypes.c_char_p
         _lib = h
     return _lib
@@ -114,3 +120,51 @@ def eval_program(state, program: int, args: np.ndarray, precision: int = 32) -> 
     out = np.zeros((n, 3), np.float64)
     _check(lib().oracle_eval_program(_vp(state.desc_ptr), int(program), int(precision), _arr(a), n, _arr(out)))
     return out
+
+
+def _views_c(views):
+    from forgedthoughts_gb300 import _native
+
+    arr = (_native.ViewC * len(views))()
+    for k, v in enumerate(views):
+        arr[k] = v if isinstance(v, _native.ViewC) else _native.ViewC(*v)
+    return arr
+
+
+def render_views(state, views, options, tau: float = 0.05, precision: int = 64, threads: int = 0):
+    """Multi-view depth / mask / soft silhouette (the definitions of
+    ft_render_views).  ``views``: (origin, target, fov) triples or ViewC.
+    Returns (t, mask, sil), each (n_views, H, W)."""
+    from forgedthoughts_gb300 import _native
+
+    varr = _views_c(views)
+    n = len(views)
+    h, w = int(options.height), int(options.width)
+    t = np.zeros((n, h, w), np.float64)
+    mask = np.zeros((n, h, w), np.uint8)
+    sil = np.zeros((n, h, w), np.float64)
+    opts = options.to_c() if hasattr(options, "to_c") else options
+    assert isinstance(opts, _native.RenderOptionsC)
+    _check(lib().oracle_render_views(_vp(state.desc_ptr), ctypes.cast(varr, ctypes.c_void_p), n,
+                                     ctypes.cast(ctypes.pointer(opts), ctypes.c_void_p), float(tau), int(precision),
+                                     int(threads), _arr(t), _arr(mask), _arr(sil)))
+    return t, mask, sil
+
+
+def render_backward(state, views, options, params, dl_dt=None, dl_dsil=None, tau: float = 0.05,
+                    precision: int = 64, threads: int = 0) -> np.ndarray:
+    """The adjoint of render_views: dL/dparams (float64) for the upstream
+    gradients dl_dt / dl_dsil (each (n_views, H, W) or None)."""
+    from forgedthoughts_gb300 import _native
+
+    varr = _views_c(views)
+    parr = params if isinstance(params, ctypes.Array) else (_native.ParamC * len(params))(*params)
+    opts = options.to_c() if hasattr(options, "to_c") else options
+    a = None if dl_dt is None else np.ascontiguousarray(dl_dt, np.float32)
+    b = None if dl_dsil is None else np.ascontiguousarray(dl_dsil, np.float32)
+    g = np.zeros(len(parr), np.float64)
+    _check(lib().oracle_render_backward(_vp(state.desc_ptr), ctypes.cast(varr, ctypes.c_void_p), len(views),
+                                        ctypes.cast(ctypes.pointer(opts), ctypes.c_void_p), float(tau),
+                                        ctypes.cast(parr, ctypes.c_void_p), len(parr), _arr(a), _arr(b),
+                                        int(precision), int(threads), _arr(g)))
+    return g

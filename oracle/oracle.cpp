@@ -1724,6 +1724,332 @@ int render_trace(const ft_scene_desc* desc, const ft_render_options* options, in
   return 0;
 }
 
+// ============================================================ differentiation
+// Multi-view depth + soft silhouette and its adjoint: the definitions of
+// ft_render_views / ft_render_backward (include/forgedthoughts_gb300.h),
+// restated on the CPU so the GPU adjoint has an FP64 reference and finite
+// differences have an FP64 forward.
+
+// Parameter slot of every (node, field) pair; a tree's radius slot is shared
+// by all union_round nodes below the node named in the layout.
+struct ParamSlots {
+  std::vector<int32_t> slot;  // node * 8 + field -> parameter index, -1 if none
+  ParamSlots(const ft_scene_desc& d, const ft_param* ps, uint32_t n) : slot(static_cast<size_t>(d.n_nodes) * 8, -1) {
+    for (uint32_t i = 0; i < n; ++i) {
+      if (ps[i].node < 0 || static_cast<uint32_t>(ps[i].node) >= d.n_nodes || ps[i].field < 0 || ps[i].field > 7)
+        continue;
+      if (ps[i].field == FT_PARAM_RADIUS) {
+        std::vector<int> stack{ps[i].node};
+        while (!stack.empty()) {
+          int k = stack.back();
+          stack.pop_back();
+          const ft_node& nd = d.nodes[k];
+          if (nd.kind != FT_NODE_UNION_ROUND) continue;
+          slot[static_cast<size_t>(k) * 8 + FT_PARAM_RADIUS] = static_cast<int32_t>(i);
+          stack.push_back(nd.a);
+          stack.push_back(nd.b);
+        }
+      } else {
+        slot[static_cast<size_t>(ps[i].node) * 8 + ps[i].field] = static_cast<int32_t>(i);
+      }
+    }
+  }
+  int at(int node, int field) const { return slot[static_cast<size_t>(node) * 8 + field]; }
+};
+
+// adj * d(value of subtree idx at p) / d(parameters, p), accumulated.
+template <class R>
+struct Backprop {
+  const Scene<R>& sc;
+  const ParamSlots& ps;
+  std::vector<R>& g;
+  V<R> gp = mk(R(0), R(0), R(0));
+  bool unsupported = false;
+
+  R value(int idx, V<R> p) const { return sc.info(idx, p).d; }
+
+  void add(int node, int field, R v) {
+    int k = ps.at(node, field);
+    if (k >= 0) g[k] += v;
+  }
+
+  void run(int idx, V<R> p, R adj) {
+    const ft_node& n = sc.node(idx);
+    switch (n.kind) {
+      case FT_NODE_SPHERE:
+      case FT_NODE_BOX: {
+        // q = rotate_y(p - c, -rot_y) (x / z rotations are zero for parameter primitives)
+        V<R> dpc = p - sc.center(n);
+        R a = to_radians(-R(n.rot_deg[1])), s = std::sin(a), c = std::cos(a);
+        V<R> q = mk(c * dpc.x + s * dpc.z, dpc.y, -s * dpc.x + c * dpc.z);
+        V<R> dq;  // d value / d q
+        if (n.kind == FT_NODE_SPHERE) {
+          R l = len(q);
+          dq = l > R(0) ? q * (R(1) / l) : mk(R(0), R(0), R(0));
+          add(idx, FT_PARAM_S0, -adj);
+        } else {
+          R h[3] = {R(n.f[0]), R(n.f[1]), R(n.f[2])};
+          R qv[3] = {q.x, q.y, q.z};
+          R qa[3], o[3];
+          for (int i = 0; i < 3; ++i) {
+            qa[i] = std::fabs(qv[i]) - h[i];
+            o[i] = rmax(qa[i], R(0));
+          }
+          R outside = std::sqrt(o[0] * o[0] + o[1] * o[1] + o[2] * o[2]);
+          R dqa[3] = {R(0), R(0), R(0)};
+          if (outside > R(0)) {
+            for (int i = 0; i < 3; ++i) dqa[i] = o[i] / outside;
+          } else {
+            int m = 0;
+            for (int i = 1; i < 3; ++i)
+              if (qa[i] > qa[m]) m = i;
+            dqa[m] = R(1);
+          }
+          R sg[3];
+          for (int i = 0; i < 3; ++i) sg[i] = qv[i] < R(0) ? R(-1) : R(1);
+          dq = mk(dqa[0] * sg[0], dqa[1] * sg[1], dqa[2] * sg[2]);
+          add(idx, FT_PARAM_S0, -adj * dqa[0]);
+          add(idx, FT_PARAM_S1, -adj * dqa[1]);
+          add(idx, FT_PARAM_S2, -adj * dqa[2]);
+        }
+        // d q / d p = rotation; d value / d p = R^T dq
+        V<R> dp = mk(c * dq.x - s * dq.z, dq.y, s * dq.x + c * dq.z);
+        gp = gp + dp * adj;
+        add(idx, FT_PARAM_CX, -adj * dp.x);
+        add(idx, FT_PARAM_CY, -adj * dp.y);
+        add(idx, FT_PARAM_CZ, -adj * dp.z);
+        // d q / d rot_y = (q.z, 0, -q.x) * d a / d rot_y, d a / d rot_y = -pi / 180
+        add(idx, FT_PARAM_ROT_Y, adj * (dq.x * q.z - dq.z * q.x) * (-pi<R>() / R(180)));
+        return;
+      }
+      case FT_NODE_UNION_ROUND: {
+        R a = value(n.a, p), b = value(n.b, p);
+        R r0 = R(n.f[0]);
+        R r = rmax(std::fabs(r0), R(1.0e-6));
+        R ux = rmax(r - a, R(0)), uy = rmax(r - b, R(0));
+        R l = std::sqrt(ux * ux + uy * uy);
+        R pa, pb, pr;
+        if (l > R(0)) {
+          pa = ux / l;
+          pb = uy / l;
+          pr = R(1) - (ux + uy) / l;
+        } else {
+          pa = a < b ? R(1) : R(0);
+          pb = a < b ? R(0) : R(1);
+          pr = R(0);
+        }
+        if (std::fabs(r0) > R(1.0e-6)) add(idx, FT_PARAM_RADIUS, adj * pr * (r0 < R(0) ? R(-1) : R(1)));
+        if (pa != R(0)) run(n.a, p, adj * pa);
+        if (pb != R(0)) run(n.b, p, adj * pb);
+        return;
+      }
+      case FT_NODE_UNION: {
+        // the culled min of the Union arm: the gradient follows the winner
+        Info<R> l = sc.info(n.a, p), rr = sc.info(n.b, p);
+        run(l.d <= rr.d ? n.a : n.b, p, adj);
+        return;
+      }
+      default:
+        unsupported = true;
+        return;
+    }
+  }
+};
+
+constexpr int kGoldenSteps = 40;  // golden-section steps of the silhouette minimum
+
+template <class R>
+struct ViewRay {
+  bool hit = false;
+  R t = R(0);      // depth (zero of f) on a hit
+  R sil = R(0);
+  R tm = R(0);     // position of the refined minimum on a miss
+  R m = R(0);      // refined minimum value
+};
+
+template <class R>
+struct ViewCamera {
+  V<R> origin, forward, right, up;
+  R tan_fov;
+  explicit ViewCamera(const ft_view& v) {
+    origin = mk(R(v.origin[0]), R(v.origin[1]), R(v.origin[2]));
+    V<R> tgt = mk(R(v.target[0]), R(v.target[1]), R(v.target[2]));
+    forward = normalize(tgt - origin);
+    right = normalize(cross(forward, mk(R(0), R(1), R(0))));
+    up = normalize(cross(right, forward));
+    tan_fov = std::tan(R(0.5) * to_radians(R(v.fov_y_degrees)));
+  }
+  V<R> dir(uint32_t x, uint32_t y, const Opts& op) const {
+    float aspect = static_cast<float>(op.width) / static_cast<float>(op.height);
+    float px = ((static_cast<float>(x) + 0.5f) / static_cast<float>(op.width)) * 2.0f - 1.0f;
+    float py = 1.0f - ((static_cast<float>(y) + 0.5f) / static_cast<float>(op.height)) * 2.0f;
+    V<R> d = normalize(forward + right * (R(px * aspect) * tan_fov) + up * (R(py) * tan_fov));
+    return normalize(d);
+  }
+};
+
+template <class R>
+ViewRay<R> view_ray(const Accel<R>& acc, V<R> o, V<R> d, const Opts& op, R tau) {
+  ViewRay<R> out;
+  R t0, t1;
+  if (!ray_aabb(o, d, acc.scene_bounds, &t0, &t1)) return out;  // sil 0: nothing along the ray
+  R max_t = rmin(R(op.max_dist), t1);
+  R traveled = rmax(t0, R(0)), prev = traveled;
+  R eps = R(op.epsilon);
+  R best = std::numeric_limits<R>::infinity(), tb_prev = traveled, tb = traveled, tb_next = traveled;
+  bool need_next = false;
+  auto f = [&](R t) { return acc.distance(o + d * t); };
+  for (uint32_t s = 0; s < op.max_steps; ++s) {
+    if (traveled > max_t) break;
+    R dv = f(traveled);
+    if (need_next) {
+      tb_next = traveled;
+      need_next = false;
+    }
+    if (dv < best) {
+      best = dv;
+      tb_prev = prev;
+      tb = traveled;
+      tb_next = traveled;
+      need_next = true;
+    }
+    if (std::fabs(dv) < eps) {
+      R lo = prev, hi = traveled;
+      for (int k = 0; k < 10; ++k) {
+        R mid = R(0.5) * (lo + hi);
+        if (std::fabs(f(mid)) < eps) hi = mid;
+        else lo = mid;
+      }
+      // secant steps from the bisection bracket onto the zero of f
+      R fa = f(lo), fb = f(hi);
+      for (int k = 0; k < 3; ++k) {
+        if (fb == fa) break;
+        R tn = hi - fb * (hi - lo) / (fb - fa);
+        lo = hi;
+        fa = fb;
+        hi = tn;
+        fb = f(hi);
+      }
+      out.hit = true;
+      out.t = hi;
+      out.sil = R(1);
+      return out;
+    }
+    prev = traveled;
+    traveled += rmax(std::fabs(dv) * rclamp(R(op.step_scale), R(0.05), R(1)), rmax(eps * R(0.5), R(1.0e-5)));
+  }
+  if (!(best < std::numeric_limits<R>::infinity())) return out;
+  // Bracket a local minimum around the smallest sample: continue the descent
+  // past the end of the march while f keeps falling, then golden-section
+  // search on the triple (a, x, b) with f(x) <= f(a), f(b).
+  auto step_of = [&](R fv) {
+    return rmax(std::fabs(fv) * rclamp(R(op.step_scale), R(0.05), R(1)), rmax(eps * R(0.5), R(1.0e-5)));
+  };
+  // (the samples start at the scene box, so the descent may also continue
+  // towards the camera when the first sample is the smallest)
+  R a = tb_prev, x = tb, fx = best;
+  R b = need_next ? x + step_of(fx) : tb_next;
+  R fb = f(b);
+  for (int k = 0; k < 64 && fb < fx && b < R(op.max_dist); ++k) {
+    a = x;
+    x = b;
+    fx = fb;
+    b = x + step_of(fx);
+    fb = f(b);
+  }
+  if (!(a < x)) a = rmax(x - step_of(fx), R(0));
+  R fa = f(a);
+  for (int k = 0; k < 64 && fa < fx && a > R(0); ++k) {
+    b = x;
+    x = a;
+    fx = fa;
+    a = rmax(x - step_of(fx), R(0));
+    fa = f(a);
+  }
+  for (int k = 0; k < kGoldenSteps; ++k) {
+    R u = (b - x > x - a) ? x + R(0.3819660112501051) * (b - x) : x - R(0.3819660112501051) * (x - a);
+    R fu = f(u);
+    if (fu < fx) {
+      if (u > x) a = x;
+      else b = x;
+      x = u;
+      fx = fu;
+    } else {
+      if (u > x) b = u;
+      else a = u;
+    }
+  }
+  out.tm = x;
+  out.m = fx;
+  out.sil = std::exp(-rmax(out.m, R(0)) / tau);
+  return out;
+}
+
+template <class R>
+int render_views(const ft_scene_desc* desc, const ft_view* views, uint32_t n_views, const ft_render_options* options,
+                 R tau, int threads, double* t_out, uint8_t* mask_out, double* sil_out, const ft_param* params,
+                 uint32_t n_params, const float* dl_dt, const float* dl_dsil, double* grad_out) {
+  Opts op = resolve(options);
+  Scene<R> scene(*desc);
+  Accel<R> acc(scene, FT_ACCEL_BVH);
+  ParamSlots slots(*desc, params, n_params);
+  if (threads <= 0) threads = static_cast<int>(std::max(1u, std::thread::hardware_concurrency()));
+  const uint64_t per_view = static_cast<uint64_t>(op.width) * op.height;
+  const uint64_t rows = static_cast<uint64_t>(n_views) * op.height;
+  std::atomic<uint64_t> next{0};
+  std::atomic<bool> bad{false};
+  std::vector<std::vector<R>> partial(threads, std::vector<R>(n_params, R(0)));
+  auto worker = [&](int w) {
+    std::vector<R>& g = partial[w];
+    for (;;) {
+      uint64_t row = next.fetch_add(1);
+      if (row >= rows) break;
+      uint32_t v = static_cast<uint32_t>(row / op.height), y = static_cast<uint32_t>(row % op.height);
+      ViewCamera<R> cam(views[v]);
+      for (uint32_t x = 0; x < op.width; ++x) {
+        size_t i = v * per_view + static_cast<size_t>(y) * op.width + x;
+        V<R> d = cam.dir(x, y, op);
+        ViewRay<R> r = view_ray(acc, cam.origin, d, op, tau);
+        if (t_out) t_out[i] = r.hit ? static_cast<double>(r.t) : 0.0;
+        if (mask_out) mask_out[i] = r.hit ? 1 : 0;
+        if (sil_out) sil_out[i] = static_cast<double>(r.sil);
+        if (!grad_out) continue;
+        R wt = dl_dt ? R(dl_dt[i]) : R(0), ws = dl_dsil ? R(dl_dsil[i]) : R(0);
+        std::vector<R> gl(n_params, R(0));
+        if (r.hit && wt != R(0)) {
+          Backprop<R> bp{scene, slots, gl};
+          bp.run(desc->root, cam.origin + d * r.t, R(1));
+          if (bp.unsupported) bad = true;
+          R den = dot(bp.gp, d);
+          if (std::fabs(den) > R(1.0e-8))
+            for (uint32_t k = 0; k < n_params; ++k) g[k] += wt * (-gl[k] / den);
+        } else if (!r.hit && ws != R(0) && r.m > R(0) && r.sil > R(0)) {
+          Backprop<R> bp{scene, slots, gl};
+          bp.run(desc->root, cam.origin + d * r.tm, R(1));
+          if (bp.unsupported) bad = true;
+          for (uint32_t k = 0; k < n_params; ++k) g[k] += ws * (-(r.sil / tau) * gl[k]);
+        }
+      }
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int i = 1; i < threads; ++i) pool.emplace_back(worker, i);
+  worker(0);
+  for (auto& t : pool) t.join();
+  if (grad_out) {
+    for (uint32_t k = 0; k < n_params; ++k) {
+      double s = 0.0;
+      for (int w = 0; w < threads; ++w) s += static_cast<double>(partial[w][k]);
+      grad_out[k] = s;
+    }
+  }
+  if (bad) {
+    g_error = "scene has node kinds the adjoint does not differentiate";
+    return FT_ERR_UNSUPPORTED;
+  }
+  return 0;
+}
+
 int check_desc(const ft_scene_desc* d) {
   if (!d || d->abi_version != FT_ABI_VERSION || d->root < 0 || static_cast<uint32_t>(d->root) >= d->n_nodes) {
     g_error = "invalid scene description";
@@ -1818,4 +2144,36 @@ extern "C" int oracle_render_trace(const ft_scene_desc* desc, const ft_render_op
                                 rgb_out, rgb8_out, evals_out);
   return render_trace<float>(desc, options, accel, aa_samples, max_depth, threads, row_begin, row_end, row_step,
                              rgb_out, rgb8_out, evals_out);
+}
+
+extern "C" int oracle_render_views(const ft_scene_desc* desc, const ft_view* views, uint32_t n_views,
+                                   const ft_render_options* options, float tau, int precision, int threads,
+                                   double* t_out, uint8_t* mask_out, double* sil_out) {
+  if (int e = check_desc(desc)) return e;
+  if (!options || options->width == 0 || options->height == 0 || !views || !(tau > 0.0f)) {
+    g_error = "invalid view render arguments";
+    return FT_ERR_INVALID_ARGUMENT;
+  }
+  if (precision == 64)
+    return render_views<double>(desc, views, n_views, options, double(tau), threads, t_out, mask_out, sil_out,
+                                nullptr, 0, nullptr, nullptr, nullptr);
+  return render_views<float>(desc, views, n_views, options, tau, threads, t_out, mask_out, sil_out, nullptr, 0,
+                             nullptr, nullptr, nullptr);
+}
+
+extern "C" int oracle_render_backward(const ft_scene_desc* desc, const ft_view* views, uint32_t n_views,
+                                      const ft_render_options* options, float tau, const ft_param* params,
+                                      uint32_t n_params, const float* dl_dt, const float* dl_dsil, int precision,
+                                      int threads, double* grad_out) {
+  if (int e = check_desc(desc)) return e;
+  if (!options || options->width == 0 || options->height == 0 || !views || !(tau > 0.0f) || !grad_out ||
+      (n_params && !params)) {
+    g_error = "invalid backward arguments";
+    return FT_ERR_INVALID_ARGUMENT;
+  }
+  if (precision == 64)
+    return render_views<double>(desc, views, n_views, options, double(tau), threads, nullptr, nullptr, nullptr,
+                                params, n_params, dl_dt, dl_dsil, grad_out);
+  return render_views<float>(desc, views, n_views, options, tau, threads, nullptr, nullptr, nullptr, params, n_params,
+                             dl_dt, dl_dsil, grad_out);
 }

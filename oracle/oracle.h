@@ -53,6 +53,21 @@ int oracle_distance(const ft_scene_desc* desc, int accel, int precision,
 int oracle_eval_program(const ft_scene_desc* desc, int program, int precision,
                         const float* args, size_t n, double* out);
 
+/* Multi-view depth / mask / soft silhouette (the definitions of
+ * ft_render_views), Bvh accelerator, outputs view-major and nullable; depth
+ * and silhouette as doubles so finite differences of the FP64 march keep
+ * its precision. */
+int oracle_render_views(const ft_scene_desc* desc, const ft_view* views, uint32_t n_views,
+                        const ft_render_options* options, float tau, int precision, int threads,
+                        double* t_out, uint8_t* mask_out, double* sil_out);
+
+/* The adjoint of oracle_render_views (the definitions of ft_render_backward):
+ * grad_out[k] = sum over rays of dl_dt dt/dparam_k + dl_dsil dsil/dparam_k. */
+int oracle_render_backward(const ft_scene_desc* desc, const ft_view* views, uint32_t n_views,
+                           const ft_render_options* options, float tau, const ft_param* params,
+                           uint32_t n_params, const float* dl_dt, const float* dl_dsil, int precision,
+                           int threads, double* grad_out);
+
 const char* oracle_last_error(void);
 
 #ifdef __cplusplus

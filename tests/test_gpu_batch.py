@@ -1,0 +1,81 @@
+"""Batched form: many scenes in one CUDA-graph launch must give exactly the
+single-scene results (each ray's computation is independent of its launch)."""
+import numpy as np
+import pytest
+
+import forgedthoughts_gb300 as ft
+from forgedthoughts_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def _small_batch(n=10):
+    out = []
+    for w in workloads.batch_scenes(n):
+        # keep the test quick: cap resolution and primitive count
+        side = min(w.options.width, 96)
+        w.options.width = w.options.height = side
+        out.append(w)
+    return out
+
+
+def _single(st, w, fp16=False):
+    if w.max_depth == 0:
+        img = ft.render_depth(st, w.options, w.accel, w.aa, fp16_bricks=fp16)
+        return img.t, img.mask, img.rgb8
+    lin, rgb8 = ft.render_trace(st, w.options, w.accel, w.aa, w.max_depth)
+    return lin, None, rgb8
+
+
+@pytest.mark.parametrize("fp16", [False, True])
+def test_batch_matches_single_renders(fp16):
+    ws = _small_batch()
+    states = [ft.parse_and_eval(w.source) for w in ws]
+    if fp16:
+        for st, w in zip(states, ws):
+            if w.max_depth == 0:
+                st.gpu().build_bricks()
+    b = ft.Batch([(st, w.options, w.aa, w.max_depth) for st, w in zip(states, ws)], fp16_bricks=fp16)
+    assert b.samples() == sum(w.options.width * w.options.height * w.aa for w in ws)
+    for tuning in [(8, 8, 8), (32, 8, 4), (16, 8, 16), (5, 3, 1)]:
+        b.set_tuning(*tuning)
+        b.launch()
+        for k, (st, w) in enumerate(zip(states, ws)):
+            got = b.read(k)
+            a, m, rgb8 = _single(st, w, fp16)
+            if w.max_depth == 0:
+                assert np.array_equal(got["t"], a), (k, tuning)
+                assert np.array_equal(got["mask"], m), (k, tuning)
+            else:
+                assert np.array_equal(got["rgb"], a), (k, tuning)
+            assert np.array_equal(got["rgb8"], rgb8), (k, tuning)
+    best = b.autotune()
+    assert best["tile_w"] in (8, 16, 32) and best["tile_h"] == 8 and best["refill"] in (4, 8, 16)
+    assert best["ms"] > 0
+    b.launch()
+    st, w = states[0], ws[0]
+    a, m, rgb8 = _single(st, w, fp16)
+    assert np.array_equal(b.read(0)["rgb8"], rgb8)
+    b.close()
+
+
+def test_batch_errors():
+    ws = _small_batch(2)
+    states = [ft.parse_and_eval(w.source) for w in ws]
+    with pytest.raises(ft.RenderError):
+        ft.Batch([])
+    depth_items = [(st, w.options, 1, 0) for st, w in zip(states, ws)]
+    with pytest.raises(ft.RenderError, match="ft_scene_build_bricks"):
+        ft.Batch(depth_items, fp16_bricks=True)
+    b = ft.Batch(depth_items)
+    with pytest.raises(ft.RenderError):
+        b.set_tuning(0, 8, 8)
+    with pytest.raises(ft.RenderError):
+        b.set_tuning(8, 8, 33)
+    with pytest.raises(ft.RenderError):
+        b.read(5)
+    bad = ft.RenderOptions(width=0, height=8)
+    with pytest.raises(ft.RenderError):
+        ft.Batch([(states[0], bad, 1, 0)])
+    with pytest.raises(ft.RenderError):
+        ft.Batch([(states[0], ws[0].options, 1, 11)])
