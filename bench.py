@@ -337,6 +337,189 @@ def _brick_figures(lib, scene, w, dev, stream, flush, peak: float) -> dict:
     return out
 
 
+def _cuda_ms(fn, reps: int) -> float:
+    """Median CUDA-event time of fn() on the current stream (fn synchronises)."""
+    import torch
+
+    s = torch.cuda.current_stream()
+    out = []
+    for _ in range(reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(s)
+        fn()
+        b.record(s)
+        torch.cuda.synchronize()
+        out.append(a.elapsed_time(b))
+    return float(statistics.median(out))
+
+
+def precision_form(reps: int = 2) -> dict:
+    """Hooked 4096-shell scene (domain rotate_y(p, p.y*18), distance_post
+    abs(d + sin(p.y*120)*0.004) - 0.03 on every sphere), 1920x1080 depth:
+    the plain FP32 march with the hook interpreter, the run-time compiled
+    (NVRTC) kernels, and the FP16 brick form on top of them."""
+    import numpy as np
+
+    import forgedthoughts_gb300 as ft
+    from forgedthoughts_gb300 import workloads
+
+    w = workloads.twisted_shells()
+    st = ft.parse_and_eval(w.source)
+    g = st.gpu()
+    items = w.options.width * w.options.height * w.aa
+    ft.render_depth(st, w.options, w.accel, 1)  # warm-up
+    plain_ms = _cuda_ms(lambda: ft.render_depth(st, w.options, w.accel, 1, want_rgb8=False), reps)
+    ref = ft.render_depth(st, w.options, w.accel, 1)
+    t0 = time.perf_counter()
+    jit = g.jit()
+    jit["wall_ms"] = 1000.0 * (time.perf_counter() - t0)
+    ft.render_depth(st, w.options, w.accel, 1)
+    jit_ms = _cuda_ms(lambda: ft.render_depth(st, w.options, w.accel, 1, want_rgb8=False), reps)
+    jimg = ft.render_depth(st, w.options, w.accel, 1)
+    info = g.build_bricks()
+    ft.render_depth(st, w.options, w.accel, 1, fp16_bricks=True)
+    b_ms = _cuda_ms(lambda: ft.render_depth(st, w.options, w.accel, 1, want_rgb8=False, fp16_bricks=True), reps)
+    bimg = ft.render_depth(st, w.options, w.accel, 1, fp16_bricks=True)
+
+    def agree(a, b):
+        both = (a.mask == 1) & (b.mask == 1)
+        err = np.abs(a.t[both].astype(np.float64) - b.t[both]) if both.any() else np.zeros(1)
+        return {"mask_agreement": float((a.mask == b.mask).mean()), "depth_err_q999": float(np.quantile(err, 0.999)),
+                "depth_within_1e-4": float((err <= 1e-4).mean())}
+
+    mr = lambda ms: items / (ms * 1e-3) / 1e6  # noqa: E731
+    return {"workload": w.name, "primary_samples": items, "unit": UNIT,
+            "plain_fp32_interpreter": {"value": mr(plain_ms), "ms": plain_ms},
+            "jit_nvrtc": {"value": mr(jit_ms), "ms": jit_ms, "speedup_vs_plain": plain_ms / jit_ms,
+                          "vs_plain": agree(ref, jimg), "compile": jit},
+            "jit_fp16_bricks": {"value": mr(b_ms), "ms": b_ms, "speedup_vs_plain": plain_ms / b_ms,
+                                "vs_plain": agree(ref, bimg),
+                                "bricks": {"build_ms": info.build_ms, "device_bytes": info.device_bytes,
+                                           "max_lipschitz": info.max_lipschitz, "near_bricks": info.near_bricks}}}
+
+
+def batched_form(reps: int = 3) -> dict:
+    """256 independent scenes (8..2048 spheres, 64^2..512^2, half depth
+    previews, half Whitted depth 2) in one CUDA-graph launch, autotuned, FP32
+    and FP16-brick; against the same renders launched one by one."""
+    import forgedthoughts_gb300 as ft
+    from forgedthoughts_gb300 import workloads
+
+    ws = workloads.batch_scenes()
+    t0 = time.perf_counter()
+    states = [ft.parse_and_eval(w.source) for w in ws]
+    for st in states:
+        st.gpu()
+    setup_ms = 1000.0 * (time.perf_counter() - t0)
+    items = [(st, w.options, w.aa, w.max_depth) for st, w in zip(states, ws)]
+
+    import torch
+
+    from forgedthoughts_gb300 import _native
+
+    lib = _native.lib()
+    big = max(w.options.width * w.options.height * w.aa for w in ws)
+    d_t = torch.empty(big, dtype=torch.float32, device="cuda")
+    d_m = torch.empty(big, dtype=torch.uint8, device="cuda")
+    d_rgb = torch.empty(big * 3, dtype=torch.float32, device="cuda")
+    d_rgb8 = torch.empty(big * 3, dtype=torch.uint8, device="cuda")
+    p = lambda x: ctypes.c_void_p(x.data_ptr())  # noqa: E731
+    copts = [w.options.to_c() for w in ws]
+
+    def one_by_one():
+        # the same renders through the C ABI, one call per scene, device outputs
+        for st, w, o in zip(states, ws, copts):
+            if w.max_depth == 0:
+                rc = lib.ft_render_depth(st.gpu().handle, ctypes.byref(o), int(w.accel), w.aa, p(d_t), p(d_m), None,
+                                         None, p(d_rgb8), _native.FT_FLAG_DEVICE_POINTERS, None)
+            else:
+                rc = lib.ft_render_trace(st.gpu().handle, ctypes.byref(o), int(w.accel), w.aa, w.max_depth, p(d_rgb),
+                                         p(d_rgb8), _native.FT_FLAG_DEVICE_POINTERS, None)
+            if rc != 0:
+                raise RuntimeError(_native.last_error())
+
+    one_by_one()
+    seq_ms = _cuda_ms(one_by_one, 1)
+    b32 = ft.Batch(items)
+    n = b32.samples()
+    tune32 = b32.autotune()
+    ms32 = _cuda_ms(lambda: (b32.launch(), __import__("torch").cuda.synchronize()), reps)
+    t0 = time.perf_counter()
+    for st, w in zip(states, ws):
+        if w.max_depth == 0:
+            st.gpu().build_bricks()
+    bricks_ms = 1000.0 * (time.perf_counter() - t0)
+    b16 = ft.Batch(items, fp16_bricks=True)
+    tune16 = b16.autotune()
+    ms16 = _cuda_ms(lambda: (b16.launch(), __import__("torch").cuda.synchronize()), reps)
+    mr = lambda ms: n / (ms * 1e-3) / 1e6  # noqa: E731
+    return {"scenes": len(ws), "primary_samples": n, "unit": UNIT, "host_setup_ms": setup_ms,
+            "one_by_one": {"value": mr(seq_ms), "ms": seq_ms, "how": "one C-ABI call per scene, device outputs"},
+            "batched_fp32": {"value": mr(ms32), "ms": ms32, "tuning": tune32, "speedup_vs_one_by_one": seq_ms / ms32},
+            "batched_fp16_bricks": {"value": mr(ms16), "ms": ms16, "tuning": tune16,
+                                    "speedup_vs_one_by_one": seq_ms / ms16, "brick_build_ms": bricks_ms}}
+
+
+def differentiation_form(adam_steps: int = 200, reps: int = 3) -> dict:
+    """Inverse shape fitting: 64 primitives (32 spheres, 32 boxes) in a
+    union_round(0.15) tree, 449 parameters, 64 views at 256^2 on a ring of
+    radius 5 at height 1.5; loss = L2(depth on pixels both renders hit) +
+    L2(soft silhouette).  Times the forward + adjoint march (gradient
+    evaluations per second) and runs Adam from the seed-7 init towards the
+    target (init + N(0, 0.05))."""
+    import numpy as np
+
+    import forgedthoughts_gb300 as ft
+    from forgedthoughts_gb300 import workloads
+
+    src = workloads.shape_fit()
+    ps = ft.ParamScene(src)
+    opts = workloads.shape_fit_options(256)
+    views = ft.ring_views(64)
+    theta0 = ps.get_params()
+    rng = np.random.default_rng(7)
+    target_params = (theta0 + rng.normal(0.0, 0.05, size=theta0.shape)).astype(np.float32)
+    ps.set_params(target_params)
+    tt, tm, ts = ps.render(views, opts)
+    ps.set_params(theta0)
+
+    def loss_and_grad(theta):
+        ps.set_params(theta)
+        t, m, s = ps.render(views, opts)
+        both = (m == 1) & (tm == 1)
+        dt = np.where(both, 2.0 * (t - tt), 0.0).astype(np.float32)
+        ds = (2.0 * (s - ts)).astype(np.float32)
+        loss = float(np.sum(np.where(both, (t - tt) ** 2, 0.0)) + np.sum((s - ts) ** 2))
+        return loss, ps.backward(views, opts, dt, ds)
+
+    loss_and_grad(theta0)
+    rays = len(views) * opts.width * opts.height
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        loss_and_grad(theta0)
+    step_s = (time.perf_counter() - t0) / reps
+    # Adam
+    theta = theta0.astype(np.float64).copy()
+    mom, vel = np.zeros_like(theta), np.zeros_like(theta)
+    lr, b1, b2, eps = 0.01, 0.9, 0.999, 1e-8
+    losses = []
+    for k in range(1, adam_steps + 1):
+        loss, g = loss_and_grad(theta.astype(np.float32))
+        losses.append(loss)
+        mom = b1 * mom + (1 - b1) * g
+        vel = b2 * vel + (1 - b2) * g * g
+        theta -= lr * (mom / (1 - b1 ** k)) / (np.sqrt(vel / (1 - b2 ** k)) + eps)
+    final, _ = loss_and_grad(theta.astype(np.float32))
+    err0 = float(np.sqrt(np.mean((theta0 - target_params) ** 2)))
+    err1 = float(np.sqrt(np.mean((theta - target_params) ** 2)))
+    return {"params": ps.n_params, "views": len(views), "rays_per_pass": rays,
+            "forward_backward_s": step_s, "gradient_evaluations_per_s": 1.0 / step_s,
+            "grads_per_s": rays * ps.n_params / step_s,
+            "grads_per_s_definition": "rays x parameters per second of forward + adjoint march",
+            "adam": {"steps": adam_steps, "lr": lr, "loss_first": losses[0], "loss_last": final,
+                     "param_rmse_to_target_init": err0, "param_rmse_to_target_final": err1}}
+
+
 def _traffic(kernel: str, w) -> int | None:
     """Per-launch DRAM bytes of the dominant kernel from a committed ncu summary."""
     prof = ROOT / "profiles" / f"{kernel}_traffic.txt"
@@ -405,6 +588,8 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-secondary", action="store_true")
+    ap.add_argument("--no-forms", action="store_true", help="skip the precision, batched and differentiation forms")
+    ap.add_argument("--adam-steps", type=int, default=200)
     ap.add_argument("--width", type=int, default=0, help="override the workload's width (profiling runs)")
     ap.add_argument("--height", type=int, default=0)
     ap.add_argument("--aa", type=int, default=0)
@@ -506,6 +691,11 @@ def main() -> None:
         fp16 = _brick_figures(lib, scene, w, dev, stream, flush, peak.value)
         fp16["speedup_vs_plain_fp32"] = fp16["value"] / plain["value"]
         line["depth_march_fp16_bricks"] = fp16
+    if rank == 0 and not args.no_forms:
+        # the north-star's three chosen forms beside the plain method
+        line["forms"] = {"precision_fp16_bricks_and_jit": precision_form(),
+                         "batched": batched_form(),
+                         "differentiation": differentiation_form(args.adam_steps)}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(w, args.mode)
     if rank == 0:

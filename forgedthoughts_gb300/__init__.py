@@ -90,12 +90,16 @@ class EvalError(RenderError):
     status = _native.FT_ERR_EVAL
 
 
+class JitError(RenderError):
+    status = _native.FT_ERR_JIT
+
+
 class CudaError(RenderError):
     status = _native.FT_ERR_CUDA
 
 
 _ERRORS = {cls.status: cls for cls in (MissingSceneRoot, UnsupportedObjectType, ExpectedObject, ParseError,
-                                       EvalError, CudaError)}
+                                       EvalError, CudaError, JitError)}
 
 
 def _check(status: int) -> None:
@@ -199,6 +203,15 @@ class GpuScene:
     @property
     def handle(self) -> ctypes.c_void_p:
         return self._h
+
+    def jit(self) -> dict:
+        """Compile the scene's hook programs with the march and trace kernels
+        at run time (NVRTC, ``ft_scene_jit``); later renders of this scene use
+        the compiled kernels."""
+        info = _native.JitInfoC()
+        _check(_native.lib().ft_scene_jit(self._h, ctypes.byref(info)))
+        return {"programs": info.programs, "cached": bool(info.cached), "source_bytes": info.source_bytes,
+                "cubin_bytes": info.cubin_bytes, "compile_ms": info.compile_ms, "load_ms": info.load_ms}
 
     def build_bricks(self, voxel_size: float = 0.02, band: float = 0.0, safety: float = 0.0,
                      max_lattice_points: int = 0, far_steps_per_pass: int = 0) -> "BrickInfo":

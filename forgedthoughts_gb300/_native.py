@@ -24,6 +24,7 @@ FT_ERR_TIMEOUT = 8
 FT_ERR_OUT_OF_MEMORY = 9
 FT_ERR_UNSUPPORTED = 10
 FT_ERR_NO_DEVICE = 11
+FT_ERR_JIT = 12
 
 FT_FLAG_DEVICE_POINTERS = 1
 FT_FLAG_FP16_BRICKS = 2
@@ -128,6 +129,11 @@ class BatchTuningC(ctypes.Structure):
 FT_BATCH_FP16_BRICKS = 1
 
 
+class JitInfoC(ctypes.Structure):
+    _fields_ = [("programs", ctypes.c_uint32), ("cached", ctypes.c_uint32), ("source_bytes", ctypes.c_uint64),
+                ("cubin_bytes", ctypes.c_uint64), ("compile_ms", ctypes.c_double), ("load_ms", ctypes.c_double)]
+
+
 class ViewC(ctypes.Structure):
     _fields_ = [("origin", ctypes.c_float * 3), ("target", ctypes.c_float * 3), ("fov_y_degrees", ctypes.c_float)]
 
@@ -185,6 +191,7 @@ SIGNATURES = {
                                           ctypes.POINTER(RenderOptionsC), ctypes.c_float, ctypes.POINTER(ParamC),
                                           ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                           ctypes.c_uint32, ctypes.c_void_p]),
+    "ft_scene_jit": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(JitInfoC)]),
     "ft_render_depth_preview_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RenderOptionsC), ctypes.c_int,
                                                        ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p]),
 }

@@ -35,9 +35,51 @@ GENCODE = "arch=compute_103a,code=sm_103a"
 CXXFLAGS = ["-std=c++17", "-O2", "-fPIC", "-Wall", "-Wextra", "-Wno-unused-parameter"]
 
 CPP_SOURCES = ["frontend_parse.cpp", "frontend_eval.cpp", "frontend_lower.cpp", "frontend_api.cpp",
-               "scene_build.cpp"]
+               "scene_build.cpp", "jit_codegen.cpp"]
 CU_SOURCES = ["ft_render.cu"]
-HEADERS = ["frontend.h", "common.h", "scene_build.h", "ft_device.cuh", "ft_trace.cuh", "ft_bricks.cuh", "ft_diff.cuh"]
+HEADERS = ["frontend.h", "common.h", "scene_build.h", "ft_device.cuh", "ft_trace.cuh", "ft_bricks.cuh", "ft_diff.cuh",
+           "ft_kernels.cuh", "ft_layout.h", "jit.h"]
+# Device headers embedded for run-time compilation (NVRTC) of scene kernels.
+JIT_HEADERS = ["ft_kernels.cuh", "ft_device.cuh", "ft_layout.h", "ft_bricks.cuh", "ft_trace.cuh", "ft_diff.cuh"]
+
+# Minimal C headers for the run-time compile unit (NVRTC ships no C library).
+_JIT_SHIMS = {
+    "stdint.h": (
+        "#pragma once\n"
+        "typedef signed char int8_t; typedef short int16_t; typedef int int32_t; typedef long long int64_t;\n"
+        "typedef unsigned char uint8_t; typedef unsigned short uint16_t; typedef unsigned int uint32_t;\n"
+        "typedef unsigned long long uint64_t;\n"),
+    "stddef.h": "#pragma once\n",  # size_t and ptrdiff_t are built into the run-time compiler
+    "cstdint": (
+        "#pragma once\n#include <stdint.h>\nnamespace std { using ::int8_t; using ::int16_t; using ::int32_t;\n"
+        "using ::int64_t; using ::uint8_t; using ::uint16_t; using ::uint32_t; using ::uint64_t; }\n"),
+}
+
+
+def _c_string(text: str) -> str:
+    # raw string literal chunks (MSVC-style limits do not apply; keep lines short anyway)
+    parts = []
+    for i in range(0, len(text), 16000):
+        parts.append('R"FTJIT(' + text[i:i + 16000] + ')FTJIT"')
+    return "\n".join(parts)
+
+
+def _write_jit_headers(path: Path) -> None:
+    entries = [(name, (CSRC / name).read_text()) for name in JIT_HEADERS]
+    entries.append(("forgedthoughts_gb300.h", (INCLUDE / "forgedthoughts_gb300.h").read_text()))
+    entries += list(_JIT_SHIMS.items())
+    out = ["// Generated by forgedthoughts_gb300/build.py: device headers for run-time compilation.",
+           '#include "jit.h"', "namespace ftgpu {", "namespace {",
+           "const char* const kNames[] = {" + ", ".join('"%s"' % n for n, _ in entries) + "};",
+           "const char* const kTexts[] = {"]
+    for _, text in entries:
+        out.append(_c_string(text) + ",")
+    out += ["};", "}  // namespace",
+            "int jit_header_count() { return %d; }" % len(entries),
+            "const char* jit_header_name(int i) { return kNames[i]; }",
+            "const char* jit_header_text(int i) { return kTexts[i]; }",
+            "}  // namespace ftgpu", ""]
+    path.write_text("\n".join(out))
 
 
 def _nvcc() -> str:
@@ -79,10 +121,12 @@ def build_library(force: bool = False) -> Path:
     nvcc = _nvcc()
     jobs = []
     objs = []
-    for src in CPP_SOURCES:
-        obj = BUILD / (src + ".o")
+    gen = BUILD / "ft_jit_headers.cpp"
+    _write_jit_headers(gen)
+    for src in [CSRC / s for s in CPP_SOURCES] + [gen]:
+        obj = BUILD / (src.name + ".o")
         objs.append(obj)
-        jobs.append(["g++", *CXXFLAGS, "-I", str(INCLUDE), "-I", str(CSRC), "-c", str(CSRC / src), "-o", str(obj)])
+        jobs.append(["g++", *CXXFLAGS, "-I", str(INCLUDE), "-I", str(CSRC), "-c", str(src), "-o", str(obj)])
     for src in CU_SOURCES:
         obj = BUILD / (src + ".o")
         objs.append(obj)
@@ -92,7 +136,7 @@ def build_library(force: bool = False) -> Path:
         list(ex.map(_run, jobs))
     tmp = BUILD / (LIB_NAME + ".tmp")
     _run([nvcc, "-shared", "-gencode", GENCODE, "-cudart", "static", "-o", str(tmp), *map(str, objs),
-          "-Xlinker", "--no-undefined", "-lpthread", "-ldl", "-lrt"])
+          "-Xlinker", "--no-undefined", "-lnvrtc", "-lpthread", "-ldl", "-lrt"])
     os.replace(tmp, out)
     stamp.write_text(digest)
     return out

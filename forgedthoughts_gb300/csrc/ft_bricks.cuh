@@ -28,6 +28,7 @@
 
 constexpr int kBrickVox = 8;   // voxels per brick edge
 constexpr int kMaxExactLeaves = 4;
+constexpr float kTrustLipschitz = 4.0f;  // larger per-brick estimates: exact marching only
 
 struct DevBricks {
   float rmin[3];             // lattice point (0, 0, 0)
@@ -100,6 +101,7 @@ __device__ __forceinline__ bool far_bound(const DevScene& S, const DevBricks& B,
   return true;
 }
 
+#ifndef FT_JIT  // build and query kernels: precompiled only
 // ------------------------------------------------------------------ build
 
 struct BrickBuild {
@@ -132,7 +134,8 @@ __device__ __forceinline__ size_t lattice_index(const BrickBuild& G, uint32_t x,
 // One warp per brick: its Lipschitz estimate and error bound, and whether a
 // surface passes within `near` of it (for the build summary).
 __global__ void __launch_bounds__(128) brick_bound_kernel(BrickBuild G, const float* __restrict__ lattice,
-                                                          float safety, float near, float* __restrict__ delta,
+                                                          float safety, float near, const float* __restrict__ untrusted,
+                                                          float* __restrict__ delta,
                                                           unsigned int* __restrict__ near_count,
                                                           unsigned int* __restrict__ max_lip_bits) {
   constexpr uint32_t kPts = kBrickVox + 1;
@@ -173,7 +176,15 @@ __global__ void __launch_bounds__(128) brick_bound_kernel(BrickBuild G, const fl
     }
     if (lane == 0) {
       float lip = fmaxf(dmax / G.h, 1.0f);
-      float del = safety * lip * G.h * 1.7320508f;
+      // A brick whose samples jump (the field is not Lipschitz there, e.g.
+      // where leaf culling switches), or that a hooked leaf can reach (hooks
+      // move surfaces off their boxes), gets no usable bound: the march is
+      // exact inside it.  (A large finite bound keeps trilinear mixes finite.)
+      const float bs = G.h * kBrickVox;
+      float lo[3] = {G.rmin[0] + bs * cx, G.rmin[1] + bs * cy, G.rmin[2] + bs * cz};
+      bool hooked = untrusted[0] <= untrusted[3];
+      for (int a = 0; a < 3; ++a) hooked &= lo[a] <= untrusted[3 + a] && lo[a] + bs >= untrusted[a];
+      float del = (lip > kTrustLipschitz || hooked) ? 1.0e4f : safety * lip * G.h * 1.7320508f;
       delta[cell] = del;
       if (vmin - del < near) atomicAdd(near_count, 1u);
       atomicMax(max_lip_bits, __float_as_uint(lip));  // positive floats order like their bits
@@ -220,3 +231,4 @@ __global__ void brick_query_kernel(DevScene S, DevBricks B, const float* __restr
   bound[i] = far_bound(S, B, p, &b, cx) ? b : __int_as_float(0x7fc00000);  // NaN: no bound here
   exact[i] = scene_distance(S, p, cx).d;
 }
+#endif  // FT_JIT

@@ -12,7 +12,8 @@
 //   backward: the march is recomputed (nothing per step is stored); at the
 //   hit point  d depth / d theta = -(df/dtheta) / (grad_p f . d), at the
 //   miss minimum  d sil / d theta = -(sil / tau) df/dtheta  (its position
-//   is stationary along the ray); df/dtheta comes from a full fold of the
+//   is stationary along the ray, and is polished by secant steps on
+//   grad_p f . d = 0 before the derivative is taken); df/dtheta comes from a full fold of the
 //   winning union_round tree with reverse-mode derivatives of op_union_round
 //   and of the sphere / box distances.  Per-parameter sums across pixels are
 //   FP64: shared-memory accumulators per block, one global atomic per block
@@ -24,6 +25,7 @@
 constexpr int kMaxDiffPrims = 512;  // union_round trees the adjoint folds (primitives)
 constexpr int kGoldenSteps = 40;
 constexpr int kSecantSteps = 3;
+constexpr int kMinPolishSteps = 4;  // secant steps on df/dt at the silhouette minimum (backward)
 
 struct DiffTables {
   const int32_t* slot;         // node * 8 + field -> parameter index, -1 if none
@@ -339,8 +341,30 @@ __global__ void __launch_bounds__(128) views_backward_kernel(DevScene S, const R
       GradSink sink{acc, &T, -wt / den, f3(0.0f, 0.0f, 0.0f)};
       scene_backprop(S, p, vals, adjs, T, sink, cx);
     } else if (!r.hit && ws != 0.0f && r.m > 0.0f && r.sil > 0.0f) {
+      // The minimum is flat along the ray, so its FP32 position is only known
+      // to ~1e-3: polish it with secant steps on df/dt = grad_p f . d = 0.
+      float tm = r.tm;
+      bool ok = true;
+      auto slope = [&](float tt) {
+        GradSink probe{acc, &T, 0.0f, f3(0.0f, 0.0f, 0.0f)};
+        ok &= scene_backprop(S, o + d * tt, vals, adjs, T, probe, cx);
+        return ftd::dot3(probe.gp, d);
+      };
+      const float dt0 = 1.0e-3f * fmaxf(1.0f, tm);
+      const float g0 = slope(tm);
+      float ta = tm - dt0, tb = tm + dt0;
+      float ga = slope(ta), gb = slope(tb);
+      for (int k = 0; k < kMinPolishSteps && ok && gb != ga; ++k) {
+        float tn = tb - gb * (tb - ta) / (gb - ga);
+        tn = fminf(fmaxf(tn, tm - 4.0f * dt0), tm + 4.0f * dt0);
+        ta = tb;
+        ga = gb;
+        tb = tn;
+        gb = slope(tb);
+      }
+      if (ok && fabsf(gb) < fabsf(g0)) tm = tb;
       GradSink sink{acc, &T, -ws * r.sil / tau, f3(0.0f, 0.0f, 0.0f)};
-      if (!scene_backprop(S, o + d * r.tm, vals, adjs, T, sink, cx)) atomicOr(unsupported, 1);
+      if (!ok || !scene_backprop(S, o + d * tm, vals, adjs, T, sink, cx)) atomicOr(unsupported, 1);
     }
   }
   if (shared_acc) {

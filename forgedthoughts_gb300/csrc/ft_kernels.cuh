@@ -1,0 +1,1279 @@
+// Device code of the renderer: the device scene image, the exact scene
+// evaluators (leaf BVH, union_round trees, generic leaves), the persistent
+// depth march, the Whitted trace, the FP16 brick cache, the batched launch and
+// the adjoint march.  Compiled by nvcc into the library and, with FT_JIT
+// defined, by NVRTC at run time together with a scene's hook programs lowered
+// to CUDA (ft_scene_jit); it therefore includes no host headers.
+#pragma once
+
+#ifndef FT_JIT
+#include <cuda_fp16.h>
+#endif
+
+#include "ft_device.cuh"
+#include "ft_layout.h"
+
+using ftd::DevNode;
+using ftd::F3;
+using ftd::f3;
+using ftd::Info;
+
+namespace {
+
+#ifdef FT_JIT
+// (the run-time compiler has no constant-expression infinity builtin)
+#define kInf (__int_as_float(0x7f800000))
+#else
+constexpr float kInf = __builtin_huge_valf();
+#endif
+
+struct DevLeaf {
+  float bmin[3], bmax[3];
+  int32_t kind, node, first, count;
+};
+struct DevBvhNode {
+  float bmin[3], bmax[3];
+  int32_t lhs, rhs, leaf, pad;
+};
+struct DevUrTree {
+  float r;
+  int32_t n_prims, prim_first, bvh_root, inner_root, depth, fallback_first, fallback_count;
+  float gmin[3];
+  float cell, inv_cell;
+  int32_t dims[3];
+  int32_t cell_first, pad;
+};
+struct DevUrBvh {
+  float bmin[3], bmax[3];
+  int32_t left, right, prim_begin, prim_count;
+};
+struct DevUrInner {
+  int32_t child[2];
+  int32_t lo, hi;
+};
+
+struct DevScene {
+  const DevNode* __restrict__ nodes;
+  const DevLeaf* __restrict__ leaves;
+  const DevBvhNode* __restrict__ bvh;
+  const uint32_t* __restrict__ gops;
+  const DevUrTree* __restrict__ urtrees;
+  const DevUrBvh* __restrict__ ur_bvh;
+  const int32_t* __restrict__ ur_bvh_prims;
+  const int32_t* __restrict__ ur_prims;
+  const DevUrInner* __restrict__ ur_inner;
+  const uint32_t* __restrict__ ur_cell_offsets;
+  const int32_t* __restrict__ ur_cell_prims;
+  const ft_program* __restrict__ programs;
+  const ft_instr* __restrict__ instrs;
+  const ft_material* __restrict__ materials;
+  const ft_light* __restrict__ lights;
+  const int32_t* __restrict__ node_op_begin;
+  const int32_t* __restrict__ node_op_end;
+  const int32_t* __restrict__ ur_inner_blend;
+  int32_t n_materials, n_lights, env_program;
+  int32_t bvh_root;
+  float smin[3], smax[3];
+};
+
+#ifdef FT_JIT
+// The scene's hook programs lowered to CUDA (generated by ft_scene_jit and
+// defined after this header in the same translation unit).
+__device__ F3 ft_jit_program(int index, const F3* args);
+#endif
+
+// Hook program `index` of the scene: native code in a run-time compiled
+// module, the register interpreter otherwise.
+__device__ __forceinline__ F3 scene_program(const DevScene& S, int index, const F3* args,
+                                            unsigned long long* instr_count) {
+#ifdef FT_JIT
+  return ft_jit_program(index, args);
+#else
+  return ftd::run_program(S.programs[index], S.instrs, args, instr_count);
+#endif
+}
+
+struct RayParams {
+  float origin[3], fwd[3], right[3], up[3];
+  float tan_fov, aspect;
+  uint32_t width, height, aa, grid, max_steps;
+  float max_dist, eps, step_scale;
+  uint32_t tiles_x;
+  uint32_t tile_w, tile_h;  // pixels per work tile (rays of a tile are consecutive work items)
+  uint32_t refill;          // idle lanes that make a warp of the persistent march refill
+  uint64_t n_items;
+};
+
+
+// Per-thread work counters (only compiled into the statistics variant).
+struct Counters {
+  unsigned long long evals, prims, boxes, hook_instrs, steps, far_steps, fetches;
+};
+constexpr int kNumCounters = 7;
+
+template <bool kStats>
+struct Ctx {
+  Counters c;
+  __device__ void eval() {
+    if (kStats) ++c.evals;
+  }
+  __device__ void prim() {
+    if (kStats) ++c.prims;
+  }
+  __device__ void box() {
+    if (kStats) ++c.boxes;
+  }
+  __device__ void step() {
+    if (kStats) ++c.steps;
+  }
+  __device__ void far_step() {
+    if (kStats) ++c.far_steps;
+  }
+  __device__ void fetch() {
+    if (kStats) ++c.fetches;
+  }
+  __device__ unsigned long long* hooks() { return kStats ? &c.hook_instrs : nullptr; }
+};
+
+__device__ __forceinline__ float node_lb(F3 p, const float* mn, const float* mx) { return ftd::aabb_lb(p, mn, mx); }
+
+// Generic leaf: postfix program over the leaf's node tree (exact).
+template <bool kStats>
+__device__ __noinline__ Info eval_generic(const DevScene& S, int first, int count, F3 p, Ctx<kStats>& cx) {
+  Info vs[ftgpu::kMaxGenericValueStack];
+  F3 ps[ftgpu::kMaxGenericPointStack];
+  int vsp = 0, psp = 0;
+  ps[0] = p;
+  for (int k = 0; k < count; ++k) {
+    uint32_t w = S.gops[first + k];
+    uint32_t op = w >> ftgpu::kGOpShift;
+    const DevNode& n = S.nodes[w & ftgpu::kGNodeMask];
+    switch (op) {
+      case ftgpu::kGPrim:
+        cx.prim();
+        vs[vsp++] = Info{ftd::prim_distance(n, ps[psp]), n.object_id, n.material_id};
+        break;
+      case ftgpu::kGDomainPush: {
+        F3 q = ftd::to_local(ps[psp], n);
+        ps[psp + 1] = scene_program(S, n.program, &q, cx.hooks());
+        ++psp;
+        break;
+      }
+      case ftgpu::kGLocalPush:
+        ps[psp + 1] = ftd::to_local(ps[psp], n);
+        ++psp;
+        break;
+      case ftgpu::kGPostPop: {
+        float d = vs[vsp - 1].d;
+        F3 args[2] = {f3(d, d, d), ps[psp]};
+        vs[vsp - 1].d = scene_program(S, n.program, args, cx.hooks()).x;
+        --psp;
+        break;
+      }
+      case ftgpu::kGNoisePop:
+        vs[vsp - 1].d = ftd::apply_noise(ps[psp], vs[vsp - 1].d, n.ival, n.f[0], n.f[1]);
+        --psp;
+        break;
+      case ftgpu::kGPop: --psp; break;
+      case ftgpu::kGBinary: {
+        Info r = vs[--vsp];
+        Info l = vs[--vsp];
+        vs[vsp++] = ftd::combine(n.kind, n.f[0], n.f[1], l, r);
+        break;
+      }
+      case ftgpu::kGSlice: {
+        F3 q = ps[psp];
+        float coord = n.ival == 0 ? q.x : (n.ival == 1 ? q.y : q.z);
+        float slab = ftd::rmax(n.f[0] - coord, coord - n.f[1]);
+        vs[vsp - 1].d = ftd::rmax(vs[vsp - 1].d, slab);
+        break;
+      }
+      case ftgpu::kGSmooth: vs[vsp - 1].d -= n.f[0] * 0.1f; break;
+    }
+  }
+  return vs[0];
+}
+
+// union_round tree of primitives with a single radius r.
+//
+// For every primitive with exact distance >= r each union_round it feeds is
+// in its min(a, b) regime (op_union_round, R:6024-6029), so the tree value
+// only depends on the set N of primitives closer than r:
+//   * N empty: the value is the minimum primitive distance, exactly;
+//   * otherwise: evaluate the tree restricted to subtrees containing an
+//     N-primitive, treating every other subtree as +inf, which reproduces
+//     op_union_round(a, b, r) bit for bit for any b >= r.
+// N is gathered through a BVH over the tree's primitives with pruning bound
+// max(r, min(best so far, cutoff)); primitive AABBs bound their distances from
+// below, so no primitive that can change the result is skipped.
+__device__ __noinline__ Info ur_fold(const DevScene& S, const DevUrTree& t, const int* near_pos,
+                                     const Info* near_info, int nn);
+
+template <bool kStats>
+__device__ __forceinline__ Info eval_urtree(const DevScene& S, const DevUrTree& t, F3 p, float cutoff,
+                                            Ctx<kStats>& cx) {
+  const float r = t.r;
+  int near_pos[ftgpu::kUrNear];
+  Info near_info[ftgpu::kUrNear];
+  int nn = 0;
+  bool overflow = false;
+  Info best{kInf, 0u, 0u};
+  // Test one primitive against the running bound; evaluate it if it can
+  // matter and record it in the near set when closer than r.
+  auto consider = [&](int pos) {
+    const DevNode& pn = S.nodes[S.ur_prims[t.prim_first + pos]];
+    cx.box();
+    float lim = ftd::rmax(r, fminf(best.d, cutoff));
+    if (node_lb(p, pn.bmin, pn.bmax) >= lim) return;
+    cx.prim();
+    float d = ftd::prim_distance(pn, p);
+    if (d < best.d) best = Info{d, pn.object_id, pn.material_id};
+    if (d < r) {
+      if (nn < ftgpu::kUrNear) {
+        near_pos[nn] = pos;
+        near_info[nn] = Info{d, pn.object_id, pn.material_id};
+        ++nn;
+      } else {
+        overflow = true;
+      }
+    }
+  };
+  int stack[48];
+  int sp = 0;
+  // Inside the candidate grid one cell list replaces the BVH walk.
+  float gx = (p.x - t.gmin[0]) * t.inv_cell, gy = (p.y - t.gmin[1]) * t.inv_cell, gz = (p.z - t.gmin[2]) * t.inv_cell;
+  if (t.dims[0] > 0 && gx >= 0.0f && gy >= 0.0f && gz >= 0.0f && gx < (float)t.dims[0] && gy < (float)t.dims[1] &&
+      gz < (float)t.dims[2]) {
+    int ix = min((int)gx, t.dims[0] - 1), iy = min((int)gy, t.dims[1] - 1), iz = min((int)gz, t.dims[2] - 1);
+    int cell = t.cell_first + ix + t.dims[0] * (iy + t.dims[1] * iz);
+    uint32_t beg = S.ur_cell_offsets[cell], end = S.ur_cell_offsets[cell + 1];
+    for (uint32_t k = beg; k < end; ++k) consider(S.ur_cell_prims[k]);
+  } else {
+    stack[sp++] = t.bvh_root;
+  }
+  while (sp > 0) {
+    const DevUrBvh& bn = S.ur_bvh[stack[--sp]];
+    cx.box();
+    float bound = ftd::rmax(r, fminf(best.d, cutoff));
+    if (node_lb(p, bn.bmin, bn.bmax) >= bound) continue;
+    if (bn.prim_count > 0) {
+      for (int k = 0; k < bn.prim_count; ++k) consider(S.ur_bvh_prims[bn.prim_begin + k]);
+      continue;
+    }
+    const DevUrBvh& L = S.ur_bvh[bn.left];
+    const DevUrBvh& R = S.ur_bvh[bn.right];
+    float ll = node_lb(p, L.bmin, L.bmax), rl = node_lb(p, R.bmin, R.bmax);
+    if (sp + 2 > 48) {
+      overflow = true;
+      break;
+    }
+    if (ll <= rl) {
+      stack[sp++] = bn.right;
+      stack[sp++] = bn.left;
+    } else {
+      stack[sp++] = bn.left;
+      stack[sp++] = bn.right;
+    }
+  }
+  if (overflow) return eval_generic(S, t.fallback_first, t.fallback_count, p, cx);
+  if (nn == 0) return best;
+  return ur_fold(S, t, near_pos, near_info, nn);
+}
+
+// Restricted union_round fold over the subtrees holding near primitives
+// (out of line: only points within r of a primitive take it).
+__device__ __noinline__ Info ur_fold(const DevScene& S, const DevUrTree& t, const int* near_pos,
+                                     const Info* near_info, int nn) {
+  const float r = t.r;
+  // Frames hold partially combined inner nodes.
+  struct Frame {
+    int inner, stage;
+    Info slot[2];
+  };
+  Frame fr[ftgpu::kMaxUrDepth + 1];
+  int fp = 0;
+  fr[0].inner = t.inner_root;
+  fr[0].stage = 0;
+  for (;;) {
+    Frame& F = fr[fp];
+    if (F.stage < 2) {
+      const DevUrInner& in = S.ur_inner[F.inner];
+      int c = in.child[F.stage];
+      if (c < 0) {
+        int pos = -c - 1;
+        Info v{kInf, 0u, 0u};
+        for (int k = 0; k < nn; ++k)
+          if (near_pos[k] == pos) v = near_info[k];
+        F.slot[F.stage++] = v;
+        continue;
+      }
+      const DevUrInner& ci = S.ur_inner[c];
+      bool has = false;
+      for (int k = 0; k < nn; ++k) has |= (near_pos[k] >= ci.lo && near_pos[k] < ci.hi);
+      if (!has) {
+        F.slot[F.stage++] = Info{kInf, 0u, 0u};
+        continue;
+      }
+      ++F.stage;
+      ++fp;
+      fr[fp].inner = c;
+      fr[fp].stage = 0;
+      continue;
+    }
+    Info res = ftd::combine(FT_NODE_UNION_ROUND, r, 0.0f, F.slot[0], F.slot[1]);
+    if (fp == 0) return res;
+    --fp;
+    fr[fp].slot[fr[fp].stage - 1] = res;
+  }
+}
+
+template <bool kStats>
+__device__ __forceinline__ Info eval_leaf(const DevScene& S, const DevLeaf& lf, F3 p, float cutoff, Ctx<kStats>& cx) {
+  if (lf.kind == ftgpu::kLeafPrim) {
+    const DevNode& n = S.nodes[lf.node];
+    cx.prim();
+    return Info{ftd::prim_distance(n, p), n.object_id, n.material_id};
+  }
+  if (lf.kind == ftgpu::kLeafUrTree) return eval_urtree(S, S.urtrees[lf.first], p, cutoff, cx);
+  return eval_generic(S, lf.first, lf.count, p, cx);
+}
+
+// Accelerator::distance_info over the leaf BVH (bvh_distance_info,
+// R:743-786): nearest-first, a node is skipped when its box bound exceeds the
+// best distance so far, a later leaf replaces the result only when strictly
+// closer.
+template <bool kStats>
+__device__ __noinline__ Info scene_distance_bvh(const DevScene& S, F3 p, Ctx<kStats>& cx) {
+  float best = kInf;
+  Info cur{kInf, 0u, 0u};
+  int stack[64];
+  float stack_lb[64];
+  int sp = 0;
+  stack[sp] = S.bvh_root;
+  stack_lb[sp] = node_lb(p, S.bvh[S.bvh_root].bmin, S.bvh[S.bvh_root].bmax);
+  ++sp;
+  cx.box();
+  while (sp > 0) {
+    --sp;
+    int ni = stack[sp];
+    if (stack_lb[sp] > best) continue;
+    const DevBvhNode& n = S.bvh[ni];
+    if (n.leaf >= 0) {
+      Info in = eval_leaf(S, S.leaves[n.leaf], p, best, cx);
+      if (in.d < best) {
+        best = in.d;
+        cur = in;
+      }
+      continue;
+    }
+    const DevBvhNode& L = S.bvh[n.lhs];
+    const DevBvhNode& R = S.bvh[n.rhs];
+    float ll = node_lb(p, L.bmin, L.bmax), rl = node_lb(p, R.bmin, R.bmax);
+    cx.box();
+    cx.box();
+    if (sp + 2 > 64) break;  // depth is bounded by the median-split build
+    if (ll <= rl) {
+      stack[sp] = n.rhs; stack_lb[sp] = rl; ++sp;
+      stack[sp] = n.lhs; stack_lb[sp] = ll; ++sp;
+    } else {
+      stack[sp] = n.lhs; stack_lb[sp] = ll; ++sp;
+      stack[sp] = n.rhs; stack_lb[sp] = rl; ++sp;
+    }
+  }
+  return cur;
+}
+
+// Same traversal, with the one- and two-leaf BVHs (a single object, or a
+// ground plus one composite object) walked without a stack.
+template <bool kStats>
+__device__ __forceinline__ Info scene_distance_inl(const DevScene& S, F3 p, Ctx<kStats>& cx) {
+  cx.eval();
+  const DevBvhNode& root = S.bvh[S.bvh_root];
+  if (root.leaf >= 0) return eval_leaf(S, S.leaves[root.leaf], p, kInf, cx);
+  const DevBvhNode& L = S.bvh[root.lhs];
+  const DevBvhNode& R = S.bvh[root.rhs];
+  if (L.leaf < 0 || R.leaf < 0) return scene_distance_bvh(S, p, cx);
+  cx.box();
+  cx.box();
+  float ll = node_lb(p, L.bmin, L.bmax), rl = node_lb(p, R.bmin, R.bmax);
+  const bool lfirst = ll <= rl;
+  const DevLeaf& first = S.leaves[lfirst ? L.leaf : R.leaf];
+  const DevLeaf& second = S.leaves[lfirst ? R.leaf : L.leaf];
+  Info cur = eval_leaf(S, first, p, kInf, cx);
+  if ((lfirst ? rl : ll) <= cur.d) {
+    Info in = eval_leaf(S, second, p, cur.d, cx);
+    if (in.d < cur.d) cur = in;
+  }
+  return cur;
+}
+
+template <bool kStats>
+__device__ __noinline__ Info scene_distance(const DevScene& S, F3 p, Ctx<kStats>& cx) {
+  return scene_distance_inl(S, p, cx);
+}
+
+template <bool kStats>
+__device__ __forceinline__ float scene_d(const DevScene& S, F3 p, Ctx<kStats>& cx) {
+  return scene_distance(S, p, cx).d;
+}
+
+// The same leaf-BVH walk reporting the winning hard-union leaf: the leaf whose
+// subtree the reference's Union walks descend into when resolving a hit's
+// normal and material (R:4471-4478, R:6995-7002).
+template <bool kStats>
+__device__ __noinline__ Info scene_distance_leaf(const DevScene& S, F3 p, int* leaf, Ctx<kStats>& cx) {
+  cx.eval();
+  float best = kInf;
+  Info cur{kInf, 0u, 0u};
+  *leaf = 0;
+  int stack[64];
+  float stack_lb[64];
+  int sp = 0;
+  stack[sp] = S.bvh_root;
+  stack_lb[sp] = node_lb(p, S.bvh[S.bvh_root].bmin, S.bvh[S.bvh_root].bmax);
+  ++sp;
+  while (sp > 0) {
+    --sp;
+    int ni = stack[sp];
+    if (stack_lb[sp] > best) continue;
+    const DevBvhNode& n = S.bvh[ni];
+    if (n.leaf >= 0) {
+      Info in = eval_leaf(S, S.leaves[n.leaf], p, best, cx);
+      if (in.d < best) {
+        best = in.d;
+        cur = in;
+        *leaf = n.leaf;
+      }
+      continue;
+    }
+    float ll = node_lb(p, S.bvh[n.lhs].bmin, S.bvh[n.lhs].bmax), rl = node_lb(p, S.bvh[n.rhs].bmin, S.bvh[n.rhs].bmax);
+    if (sp + 2 > 64) break;
+    if (ll <= rl) {
+      stack[sp] = n.rhs; stack_lb[sp] = rl; ++sp;
+      stack[sp] = n.lhs; stack_lb[sp] = ll; ++sp;
+    } else {
+      stack[sp] = n.lhs; stack_lb[sp] = ll; ++sp;
+      stack[sp] = n.rhs; stack_lb[sp] = rl; ++sp;
+    }
+  }
+  return cur;
+}
+
+// ray_aabb_intersection (R:4141-4173)
+__device__ bool ray_aabb(F3 o, F3 d, const float* mn, const float* mx, float* t0o, float* t1o) {
+  float tmin = -kInf, tmax = kInf;
+  float os[3] = {o.x, o.y, o.z}, ds[3] = {d.x, d.y, d.z};
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    if (fabsf(ds[k]) <= 1.0e-8f) {
+      if (os[k] < mn[k] || os[k] > mx[k]) return false;
+      continue;
+    }
+    float inv = 1.0f / ds[k];
+    float t0 = (mn[k] - os[k]) * inv, t1 = (mx[k] - os[k]) * inv;
+    if (t0 > t1) {
+      float tt = t0;
+      t0 = t1;
+      t1 = tt;
+    }
+    tmin = fmaxf(tmin, t0);
+    tmax = fminf(tmax, t1);
+    if (tmax < tmin) return false;
+  }
+  *t0o = tmin;
+  *t1o = tmax;
+  return true;
+}
+
+struct HitOut {
+  float t;
+  uint32_t mat;
+  bool hit;
+  F3 normal;
+};
+
+template <bool kStats>
+__device__ HitOut march(const DevScene& S, const RayParams& P, F3 o, F3 d, bool want_normal, Ctx<kStats>& cx) {
+  HitOut h{0.0f, 0u, false, f3(0.0f, 0.0f, 0.0f)};
+  float t0, t1;
+  if (!ray_aabb(o, d, S.smin, S.smax, &t0, &t1)) return h;
+  float max_t = fminf(P.max_dist, t1);
+  float traveled = fmaxf(0.0f, fmaxf(t0, 0.0f));
+  float prev = traveled;
+  const float eps = P.eps;
+  const float scale = ftd::rclamp(P.step_scale, 0.05f, 1.0f);
+  const float min_step = fmaxf(eps * 0.5f, 1.0e-5f);
+  for (uint32_t s = 0; s < P.max_steps; ++s) {
+    if (traveled > max_t) return h;
+    cx.step();
+    Info info = scene_distance(S, o + d * traveled, cx);
+    if (fabsf(info.d) < eps) {
+      float lo = prev, hi = traveled;
+      for (int k = 0; k < 10; ++k) {
+        float mid = 0.5f * (lo + hi);
+        float dm = fabsf(scene_d(S, o + d * mid, cx));
+        if (dm < eps) hi = mid;
+        else lo = mid;
+      }
+      F3 pos = o + d * hi;
+      if (want_normal) {
+        // estimate_normal (R:4202-4215)
+        float e = fmaxf(eps * 4.0f, 1.0e-5f);
+        float dx = scene_d(S, f3(pos.x + e, pos.y, pos.z), cx) - scene_d(S, f3(pos.x - e, pos.y, pos.z), cx);
+        float dy = scene_d(S, f3(pos.x, pos.y + e, pos.z), cx) - scene_d(S, f3(pos.x, pos.y - e, pos.z), cx);
+        float dz = scene_d(S, f3(pos.x, pos.y, pos.z + e), cx) - scene_d(S, f3(pos.x, pos.y, pos.z - e), cx);
+        F3 nn = f3(dx, dy, dz);
+        h.normal = ftd::len3(nn) > 1.0e-8f ? ftd::normalize3(nn) : f3(0.0f, 1.0f, 0.0f);
+      }
+      Info fin = scene_distance(S, pos, cx);
+      h.t = hi;
+      h.mat = fin.mat;
+      h.hit = true;
+      return h;
+    }
+    prev = traveled;
+    traveled += fmaxf(fabsf(info.d) * scale, min_step);
+  }
+  return h;
+}
+
+__device__ __forceinline__ void item_coords(const RayParams& P, uint64_t i, uint32_t* px, uint32_t* py, uint32_t* s) {
+  uint32_t per_tile = P.tile_w * P.tile_h * P.aa;
+  uint64_t tile = i / per_tile;
+  uint32_t k = static_cast<uint32_t>(i - tile * per_tile);
+  *s = k % P.aa;
+  uint32_t j = k / P.aa;
+  *px = static_cast<uint32_t>(tile % P.tiles_x) * P.tile_w + j % P.tile_w;
+  *py = static_cast<uint32_t>(tile / P.tiles_x) * P.tile_h + j / P.tile_w;
+}
+
+#include "ft_bricks.cuh"
+
+// Many renders in one launch: per-item scene, parameters and brick cache, and
+// the prefix sums that map a global work item to (item, local work item) and
+// an item's outputs into the concatenated output arrays.
+struct BatchView {
+  const DevScene* scenes;
+  const RayParams* params;
+  const DevBricks* bricks;
+  const uint64_t* ray_first;  // n_items + 1 entries
+  const uint64_t* out_first;  // first output sample of each item
+  uint32_t n_items;
+  uint64_t n_rays;
+};
+
+// Item holding global work item `g` (ray_first is sorted; ray_first[0] = 0).
+__device__ __forceinline__ uint32_t batch_item(const BatchView& V, uint64_t g) {
+  uint32_t lo = 0, hi = V.n_items;  // ray_first[lo] <= g < ray_first[hi]
+  while (hi - lo > 1) {
+    uint32_t mid = (lo + hi) >> 1;
+    if (__ldg(&V.ray_first[mid]) <= g) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+template <bool kStats>
+__global__ void __launch_bounds__(128) march_depth_kernel(DevScene S, RayParams P, float* __restrict__ t_out,
+                                                          uint8_t* __restrict__ mask_out,
+                                                          uint32_t* __restrict__ mat_out,
+                                                          float* __restrict__ normal_out,
+                                                          unsigned long long* __restrict__ stats) {
+  uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  Ctx<kStats> cx;
+  cx.c = Counters{};
+  bool active = i < P.n_items;
+  uint32_t px = 0, py = 0, s = 0;
+  if (active) {
+    item_coords(P, i, &px, &py, &s);
+    active = px < P.width && py < P.height;
+  }
+  if (active) {
+    // pixel_sample_offsets (R:4838-4854) and the NDC map of render_depth_tile.
+    float sx = (static_cast<float>(s % P.grid) + 0.5f) / static_cast<float>(P.grid);
+    float sy = (static_cast<float>(s / P.grid) + 0.5f) / static_cast<float>(P.grid);
+    float ndc_x = ((static_cast<float>(px) + sx) / static_cast<float>(P.width)) * 2.0f - 1.0f;
+    float ndc_y = 1.0f - ((static_cast<float>(py) + sy) / static_cast<float>(P.height)) * 2.0f;
+    ndc_x *= P.aspect;
+    F3 fwd = f3(P.fwd[0], P.fwd[1], P.fwd[2]), rt = f3(P.right[0], P.right[1], P.right[2]);
+    F3 up = f3(P.up[0], P.up[1], P.up[2]);
+    F3 dir = ftd::normalize3(fwd + rt * (ndc_x * P.tan_fov) + up * (ndc_y * P.tan_fov));
+    dir = ftd::normalize3(dir);
+    F3 o = f3(P.origin[0], P.origin[1], P.origin[2]);
+    HitOut h = march(S, P, o, dir, normal_out != nullptr, cx);
+    size_t idx = (static_cast<size_t>(py) * P.width + px) * P.aa + s;
+    t_out[idx] = h.hit ? h.t : 0.0f;
+    mask_out[idx] = h.hit ? 1 : 0;
+    if (mat_out) mat_out[idx] = h.hit ? h.mat : 0u;
+    if (normal_out) {
+      normal_out[3 * idx] = h.normal.x;
+      normal_out[3 * idx + 1] = h.normal.y;
+      normal_out[3 * idx + 2] = h.normal.z;
+    }
+  }
+  if (kStats) {
+    unsigned long long v[5] = {cx.c.evals, cx.c.prims, cx.c.boxes, cx.c.hook_instrs, cx.c.steps};
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      unsigned long long x = v[k];
+      for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+      if ((threadIdx.x & 31) == 0 && x) atomicAdd(&stats[k], x);
+    }
+  }
+}
+
+// Primary ray of work item i (pixel_sample_offsets R:4838-4854, NDC map of
+// render_depth_tile R:3951-3955, generate_ray render_api.rs:132-144 and the
+// second normalisation of the tile loop).
+__device__ __forceinline__ bool item_ray(const RayParams& P, uint64_t i, F3* dir, size_t* out_idx) {
+  uint32_t px, py, s;
+  item_coords(P, i, &px, &py, &s);
+  if (px >= P.width || py >= P.height) return false;
+  float sx = (static_cast<float>(s % P.grid) + 0.5f) / static_cast<float>(P.grid);
+  float sy = (static_cast<float>(s / P.grid) + 0.5f) / static_cast<float>(P.grid);
+  float ndc_x = ((static_cast<float>(px) + sx) / static_cast<float>(P.width)) * 2.0f - 1.0f;
+  float ndc_y = 1.0f - ((static_cast<float>(py) + sy) / static_cast<float>(P.height)) * 2.0f;
+  ndc_x *= P.aspect;
+  F3 fwd = f3(P.fwd[0], P.fwd[1], P.fwd[2]), rt = f3(P.right[0], P.right[1], P.right[2]);
+  F3 up = f3(P.up[0], P.up[1], P.up[2]);
+  F3 d = ftd::normalize3(fwd + rt * (ndc_x * P.tan_fov) + up * (ndc_y * P.tan_fov));
+  *dir = ftd::normalize3(d);
+  *out_idx = (static_cast<size_t>(py) * P.width + px) * P.aa + s;
+  return true;
+}
+
+// Persistent march with per-lane state machines.
+//
+// Every loop iteration performs exactly one scene distance evaluation per
+// live lane, whatever the lane is doing: a march step (R:4100-4137), one of
+// the ten bisection steps (refine_hit_distance, R:4180-4200), one of the six
+// estimate_normal taps (R:4202-4215) or the final material lookup.  Lanes
+// whose ray finished pick up the next work item from a global counter once a
+// quarter of the warp is idle, so divergent march lengths do not leave lanes
+// idle for the rest of the warp's life.  The sequence of evaluation points of
+// each ray is exactly the reference's.
+//
+// With kBricks (the FP16 precision form) a ray starts in the far-field phase:
+// up to far_batch steps per iteration on the brick lower bound b (one texture
+// fetch each), stepping by b - band/2 so the exact distance stays above band/2,
+// until b < band or the ray leaves the brick region (each far-field step counts
+// as one step against max_steps).  It then continues from that point with the
+// plain method's exact FP32 march (same step rule), and goes back to the far
+// field whenever an exact step finds
+// |d| > band_exit.  At the hit the eps-shell crossing between the last two
+// exact points is found by secant steps on the exact distance (each verified
+// by an exact evaluation) instead of ten bisections, and the material comes
+// from the accepted point's evaluation; the normal is the plain method's.
+enum Phase : int { kMarch = 0, kRefine = 1, kNormal = 2, kFinal = 3, kFar = 4, kSecant = 5 };
+
+//
+// With kBatch the launch serves many renders: each lane carries the index of
+// the item its ray belongs to and reads that item's scene, parameters and
+// brick cache from the batch tables (otherwise they are the kernel's own
+// parameters); outputs are the concatenated arrays of all items.
+template <bool kStats, bool kBricks, bool kBatch>
+__global__ void __launch_bounds__(128) march_depth_persistent(DevScene S0, RayParams P0, DevBricks B0, BatchView V,
+                                                              float* __restrict__ t_out,
+                                                              uint8_t* __restrict__ mask_out,
+                                                              uint32_t* __restrict__ mat_out,
+                                                              float* __restrict__ normal_out,
+                                                              unsigned long long* __restrict__ stats,
+                                                              unsigned long long* __restrict__ next_item) {
+  const unsigned lane = threadIdx.x & 31u;
+  const bool want_normal = normal_out != nullptr;
+  const uint64_t n_work = kBatch ? V.n_rays : P0.n_items;
+  const unsigned refill = kBatch ? V.params[0].refill : P0.refill;
+  Ctx<kStats> cx;
+  cx.c = Counters{};
+
+  bool live = false;
+  bool queue_done = false;
+  size_t idx = 0;
+  uint32_t item_of_lane = 0;
+  // per-ray constants (per item with kBatch)
+  F3 o = f3(P0.origin[0], P0.origin[1], P0.origin[2]);
+  float eps = P0.eps;
+  float scale = ftd::rclamp(P0.step_scale, 0.05f, 1.0f);
+  float min_step = fmaxf(eps * 0.5f, 1.0e-5f);
+  float ne = fmaxf(eps * 4.0f, 1.0e-5f);
+  F3 d = f3(0.0f, 0.0f, 0.0f), pos = f3(0.0f, 0.0f, 0.0f);
+  float traveled = 0.0f, prev = 0.0f, max_t = 0.0f, lo = 0.0f, hi = 0.0f;
+  float nx = 0.0f, ny = 0.0f, nz = 0.0f;  // estimate_normal differences
+  uint32_t steps = 0;
+  int phase = kMarch, k = 0;
+  // precision form: exact distance at `prev` (< 0: unknown), secant bracket
+  // values, material of the accepted hit point
+  float dprev = -1.0f, dlo = 0.0f, dhi = 0.0f;
+  uint32_t hit_mat = 0u;
+  bool mat_known = false;
+  auto write_miss = [&]() {
+    live = false;
+    t_out[idx] = 0.0f;
+    mask_out[idx] = 0;
+    if (mat_out) mat_out[idx] = 0u;
+    if (normal_out) {
+      normal_out[3 * idx] = 0.0f;
+      normal_out[3 * idx + 1] = 0.0f;
+      normal_out[3 * idx + 2] = 0.0f;
+    }
+  };
+  auto write_hit = [&](uint32_t mat) {
+    live = false;
+    t_out[idx] = hi;
+    mask_out[idx] = 1;
+    if (mat_out) mat_out[idx] = mat;
+    if (normal_out) {
+      F3 nn = f3(nx, ny, nz);
+      F3 nr = ftd::len3(nn) > 1.0e-8f ? ftd::normalize3(nn) : f3(0.0f, 1.0f, 0.0f);
+      normal_out[3 * idx] = nr.x;
+      normal_out[3 * idx + 1] = nr.y;
+      normal_out[3 * idx + 2] = nr.z;
+    }
+  };
+
+  for (;;) {
+    // Refill idle lanes when enough of the warp is idle (or all of it).
+    unsigned idle = __ballot_sync(0xffffffffu, !live);
+    if (!queue_done && (__popc(idle) >= refill || idle == 0xffffffffu)) {
+      unsigned n = __popc(idle);
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(next_item, static_cast<unsigned long long>(n));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (base >= n_work) queue_done = true;
+      if (!live) {
+        unsigned rank = __popc(idle & ((1u << lane) - 1u));
+        uint64_t item = base + rank;
+        bool got = false;
+        if (item < n_work) {
+          if (kBatch) {
+            item_of_lane = batch_item(V, item);
+            const RayParams& Pi = V.params[item_of_lane];
+            got = item_ray(Pi, item - V.ray_first[item_of_lane], &d, &idx);
+            idx += V.out_first[item_of_lane];
+            o = f3(Pi.origin[0], Pi.origin[1], Pi.origin[2]);
+            eps = Pi.eps;
+            scale = ftd::rclamp(Pi.step_scale, 0.05f, 1.0f);
+            min_step = fmaxf(eps * 0.5f, 1.0e-5f);
+            ne = fmaxf(eps * 4.0f, 1.0e-5f);
+          } else {
+            got = item_ray(P0, item, &d, &idx);
+          }
+        }
+        const DevScene& S = kBatch ? V.scenes[item_of_lane] : S0;
+        const RayParams& P = kBatch ? V.params[item_of_lane] : P0;
+        if (got) {
+          float t0, t1;
+          bool inside = ray_aabb(o, d, S.smin, S.smax, &t0, &t1);
+          traveled = fmaxf(0.0f, fmaxf(t0, 0.0f));
+          max_t = fminf(P.max_dist, t1);
+          if (inside && P.max_steps > 0 && !(traveled > max_t)) {
+            live = true;
+            prev = traveled;
+            steps = 0;
+            phase = kBricks ? kFar : kMarch;
+            dprev = -1.0f;
+            mat_known = false;
+          } else {
+            write_miss();
+          }
+        }
+      }
+    }
+    if (__ballot_sync(0xffffffffu, live) == 0u) {
+      if (queue_done) break;
+      continue;
+    }
+    if (!live) continue;
+    const DevScene& S = kBatch ? V.scenes[item_of_lane] : S0;
+    const RayParams& P = kBatch ? V.params[item_of_lane] : P0;
+    const DevBricks& B = kBatch ? V.bricks[item_of_lane] : B0;
+
+    if (kBricks && phase == kFar) {
+      bool exact = false, missed = false;
+      for (int f = 0; f < B.far_batch; ++f) {
+        float b;
+        if (!far_bound(S, B, o + d * traveled, &b, cx) || b < B.band) {
+          exact = true;
+          break;
+        }
+        traveled += b - 0.5f * B.band;
+        cx.far_step();
+        ++steps;  // a far-field step is one step of the march
+        if (steps >= P.max_steps || traveled > max_t) {
+          missed = true;
+          break;
+        }
+      }
+      if (missed) {
+        write_miss();
+        continue;
+      }
+      if (!exact) continue;
+      phase = kMarch;  // exact evaluation at `traveled` in this iteration
+      prev = traveled;
+      dprev = -1.0f;
+    }
+
+    // The point this lane evaluates in this iteration.
+    F3 q;
+    float mid = 0.0f;
+    if (phase == kMarch) {
+      q = o + d * traveled;
+      cx.step();
+    } else if (phase == kRefine) {
+      mid = 0.5f * (lo + hi);
+      q = o + d * mid;
+    } else if (kBricks && phase == kSecant) {
+      // crossing of d = eps on the line through (lo, dlo) and (hi, dhi)
+      mid = lo + (dlo - eps) / (dlo - dhi) * (hi - lo);
+      mid = fminf(fmaxf(mid, lo), hi);
+      q = o + d * mid;
+    } else if (phase == kNormal) {
+      float sgn = (k & 1) ? -ne : ne;
+      q = pos;
+      if (k < 2) q.x += sgn;
+      else if (k < 4) q.y += sgn;
+      else q.z += sgn;
+    } else {
+      q = pos;
+    }
+    Info info = scene_distance_inl(S, q, cx);
+
+    if (phase == kMarch) {
+      if (fabsf(info.d) < eps) {
+        lo = prev;
+        hi = traveled;
+        k = 0;
+        if (kBricks && dprev >= eps) {
+          phase = kSecant;
+          dlo = dprev;
+          dhi = info.d;
+          hit_mat = info.mat;
+        } else {
+          phase = kRefine;
+        }
+      } else {
+        prev = traveled;
+        if (kBricks) dprev = info.d;
+        traveled += fmaxf(fabsf(info.d) * scale, min_step);
+        ++steps;
+        if (kBricks && fabsf(info.d) > B.band_exit) phase = kFar;
+        if (steps >= P.max_steps || traveled > max_t) write_miss();
+      }
+    } else if (kBricks && phase == kSecant) {
+      bool accept = true;
+      if (fabsf(info.d) < eps) {
+        hi = mid;
+        hit_mat = info.mat;
+      } else if (info.d > 0.0f && ++k < 3) {
+        lo = mid;
+        dlo = info.d;
+        accept = false;
+      }
+      if (accept) {
+        pos = o + d * hi;
+        mat_known = true;
+        k = 0;
+        if (want_normal) phase = kNormal;
+        else write_hit(hit_mat);
+      }
+    } else if (phase == kRefine) {
+      if (fabsf(info.d) < eps) hi = mid;
+      else lo = mid;
+      if (++k == 10) {
+        pos = o + d * hi;
+        phase = want_normal ? kNormal : kFinal;
+        k = 0;
+      }
+    } else if (phase == kNormal) {
+      // dx = d(p + e x) - d(p - e x), one subtraction as in the reference
+      if (k == 0) nx = info.d;
+      else if (k == 1) nx = nx - info.d;
+      else if (k == 2) ny = info.d;
+      else if (k == 3) ny = ny - info.d;
+      else if (k == 4) nz = info.d;
+      else nz = nz - info.d;
+      if (++k == 6) {
+        if (kBricks && mat_known) write_hit(hit_mat);
+        else phase = kFinal;
+      }
+    } else {
+      write_hit(info.mat);
+    }
+  }
+  if (kStats) {
+    unsigned long long v[kNumCounters] = {cx.c.evals, cx.c.prims,     cx.c.boxes,  cx.c.hook_instrs,
+                                          cx.c.steps, cx.c.far_steps, cx.c.fetches};
+#pragma unroll
+    for (int j = 0; j < kNumCounters; ++j) {
+      unsigned long long x = v[j];
+      for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+      if (lane == 0 && x) atomicAdd(&stats[j], x);
+    }
+  }
+}
+
+#ifndef FT_JIT
+// Depth preview pixels (render_depth_tile R:3931-3971, depth_preview_value
+// R:5215-5219, spectrum_to_rgb8 R:5221-5227).
+__device__ __forceinline__ float depth_pixel_value(const float* __restrict__ t, const uint8_t* __restrict__ mask,
+                                                   size_t first, uint32_t aa, float max_dist) {
+  float sum = 0.0f;
+  float md = fmaxf(max_dist, 1.0e-6f);
+  for (uint32_t s = 0; s < aa; ++s) {
+    size_t k = first + s;
+    float depth = 0.0f;
+    if (mask[k]) {
+      float d = ftd::rclamp(t[k] / md, 0.0f, 1.0f);
+      float shaped = 1.0f - d;
+      depth = shaped * shaped;
+    }
+    sum += depth;
+  }
+  return sum * (1.0f / static_cast<float>(aa));
+}
+
+// spectrum_to_rgb8 (R:5221-5227): gamma 2.2, clamped, truncated
+__device__ __forceinline__ uint8_t gamma_u8(float v) {
+  float mapped = fminf(powf(fmaxf(v, 0.0f), 1.0f / 2.2f), 1.0f);
+  return static_cast<uint8_t>(mapped * 255.0f);
+}
+
+// spectrum_to_rgb8_reinhard (R:5229-5239)
+__device__ __forceinline__ uint8_t reinhard_u8(float v) {
+  float x = fmaxf(v, 0.0f);
+  float t = x / (1.0f + x);
+  float mapped = fminf(powf(t, 1.0f / 2.2f), 1.0f);
+  return static_cast<uint8_t>(mapped * 255.0f);
+}
+
+__global__ void depth_rgb8_kernel(const float* __restrict__ t, const uint8_t* __restrict__ mask, uint32_t n_pixels,
+                                  uint32_t aa, float max_dist, uint8_t* __restrict__ rgb) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_pixels) return;
+  uint8_t g = gamma_u8(depth_pixel_value(t, mask, static_cast<size_t>(i) * aa, aa, max_dist));
+  rgb[3 * static_cast<size_t>(i)] = g;
+  rgb[3 * static_cast<size_t>(i) + 1] = g;
+  rgb[3 * static_cast<size_t>(i) + 2] = g;
+}
+
+#endif  // FT_JIT
+
+#include "ft_trace.cuh"
+
+struct TraceHit {
+  float t;
+  F3 pos, normal;
+  uint32_t mat;
+  int leaf;
+};
+
+// raymarch_hit (R:4091-4139) from min_t, with the six-tap normal and the
+// winning leaf of the final evaluation.
+template <bool kStats>
+__device__ bool march_hit(const DevScene& S, const RayParams& P, F3 o, F3 d, float min_t, TraceHit* h,
+                          Ctx<kStats>& cx) {
+  float t0, t1;
+  if (!ray_aabb(o, d, S.smin, S.smax, &t0, &t1)) return false;
+  float max_t = fminf(P.max_dist, t1);
+  float traveled = fmaxf(min_t, fmaxf(t0, 0.0f));
+  float prev = traveled;
+  const float eps = P.eps;
+  const float scale = ftd::rclamp(P.step_scale, 0.05f, 1.0f);
+  const float min_step = fmaxf(eps * 0.5f, 1.0e-5f);
+  for (uint32_t s = 0; s < P.max_steps; ++s) {
+    if (traveled > max_t) return false;
+    cx.step();
+    Info info = scene_distance(S, o + d * traveled, cx);
+    if (fabsf(info.d) < eps) {
+      float lo = prev, hi = traveled;
+      for (int k = 0; k < 10; ++k) {
+        float mid = 0.5f * (lo + hi);
+        if (fabsf(scene_d(S, o + d * mid, cx)) < eps) hi = mid;
+        else lo = mid;
+      }
+      F3 pos = o + d * hi;
+      float e = fmaxf(eps * 4.0f, 1.0e-5f);
+      float dx = scene_d(S, f3(pos.x + e, pos.y, pos.z), cx) - scene_d(S, f3(pos.x - e, pos.y, pos.z), cx);
+      float dy = scene_d(S, f3(pos.x, pos.y + e, pos.z), cx) - scene_d(S, f3(pos.x, pos.y - e, pos.z), cx);
+      float dz = scene_d(S, f3(pos.x, pos.y, pos.z + e), cx) - scene_d(S, f3(pos.x, pos.y, pos.z - e), cx);
+      F3 nn = f3(dx, dy, dz);
+      h->normal = ftd::len3(nn) > 1.0e-8f ? ftd::normalize3(nn) : f3(0.0f, 1.0f, 0.0f);
+      Info fin = scene_distance_leaf(S, pos, &h->leaf, cx);
+      h->t = hi;
+      h->pos = pos;
+      h->mat = fin.mat;
+      return true;
+    }
+    prev = traveled;
+    traveled += fmaxf(fabsf(info.d) * scale, min_step);
+  }
+  return false;
+}
+
+// environment_color (R:4328-4333), falling back to the sum of EnvLight
+// radiances (env_radiance, R:4318-4326).
+__device__ F3 environment(const DevScene& S, F3 dir) {
+  if (S.env_program >= 0) return scene_program(S, S.env_program, &dir, nullptr);
+  F3 s = f3(0.0f, 0.0f, 0.0f);
+  for (int i = 0; i < S.n_lights; ++i)
+    if (S.lights[i].kind == FT_LIGHT_ENV) s = s + f3(S.lights[i].intensity[0], S.lights[i].intensity[1], S.lights[i].intensity[2]);
+  return s;
+}
+
+// The full Whitted tree of one primary sample (trace_ray_recursive,
+// ray.rs:3-222), as a stack of ray jobs carrying their throughput weights.
+template <bool kStats>
+__device__ __forceinline__ F3 trace_sample(const DevScene& S, const RayParams& P, uint32_t max_depth, F3 dir,
+                                           Ctx<kStats>& cx) {
+  F3 acc = f3(0.0f, 0.0f, 0.0f);
+  {
+    const float eps = P.eps;
+    RayJob stack[kTraceStack];
+    int sp = 0;
+    stack[sp++] = RayJob{f3(P.origin[0], P.origin[1], P.origin[2]), dir, f3(1.0f, 1.0f, 1.0f), air(), 0};
+    while (sp > 0) {
+      RayJob J = stack[--sp];
+      if (static_cast<uint32_t>(J.depth) >= max_depth) continue;
+      float min_t = J.depth == 0 ? 0.0f : eps * 2.0f;  // secondary_min_t (R:4175-4178)
+      TraceHit h;
+      if (!march_hit(S, P, J.o, J.d, min_t, &h, cx)) {
+        acc = acc + mul3(J.w, mul3(environment(S, J.d), transmittance(J.med, P.max_dist)));
+        continue;
+      }
+      Resolved rs;
+      resolve_hit(S, h.leaf, h.pos, &rs, cx);
+      bool front = ftd::dot3(h.normal, J.d) < 0.0f;
+      F3 normal = front ? ftd::normalize3(h.normal) : ftd::normalize3(h.normal * -1.0f);
+      F3 shading_n = normal;
+      if (rs.ok) shading_n = ftd::normalize3(front ? rs.normal : rs.normal * -1.0f);
+      DMat mats[2];
+      float ws[2];
+      int nm = 0;
+      if (rs.ok && rs.split) {
+        float tt = clamp01(rs.t);  // lerp_spectrum(a, b, t): a (1 - t) + b t
+        if (tt != 1.0f) { mats[nm] = rs.m; ws[nm++] = 1.0f - tt; }
+        if (tt != 0.0f) { mats[nm] = rs.mb; ws[nm++] = tt; }
+      } else {
+        mats[0] = rs.ok ? rs.m : mat_of_id(S, h.mat);
+        ws[0] = 1.0f;
+        nm = 1;
+      }
+      F3 att = transmittance(J.med, h.t);
+      F3 wo = ftd::normalize3(J.d * -1.0f);
+      for (int mi = 0; mi < nm; ++mi) {
+        const DMat& mat = mats[mi];
+        F3 W = mul3(J.w * ws[mi], att);
+        // trace_hit_with_material (ray.rs:41-222)
+        const DParams& Pm = dom_params(mat);
+        float rough = clamp01(Pm.roughness);
+        int model = dom_model(mat);
+        float transmission, ior, metallic, clearcoat, specular_strength;
+        bool thin;
+        F3 spec_color, base_color;
+        if (model == FT_MAT_STANDARD) {
+          transmission = clamp01(Pm.transmission); ior = ftd::rclamp(Pm.ior, 1.0f, 3.0f); thin = Pm.thin != 0;
+          spec_color = Pm.spec_color; base_color = Pm.color; metallic = clamp01(Pm.metallic);
+          clearcoat = clamp01(Pm.clearcoat); specular_strength = clamp01(Pm.specular * Pm.specular_weight);
+        } else if (model == FT_MAT_LAMBERT) {
+          transmission = 0.0f; ior = 1.0f; thin = false; spec_color = f3(0.0f, 0.0f, 0.0f); base_color = Pm.color;
+          metallic = 0.0f; clearcoat = 0.0f; specular_strength = 0.0f;
+        } else if (model == FT_MAT_METAL) {
+          transmission = 0.0f; ior = 1.0f; thin = false; spec_color = Pm.color; base_color = Pm.color;
+          metallic = 1.0f; clearcoat = 0.0f; specular_strength = 1.0f;
+        } else {
+          transmission = 1.0f; ior = ftd::rclamp(Pm.ior, 1.0f, 3.0f); thin = Pm.thin != 0;
+          spec_color = f3(1.0f, 1.0f, 1.0f); base_color = Pm.color; metallic = 0.0f; clearcoat = 0.0f;
+          specular_strength = 1.0f;
+        }
+        float eta_i, eta_t, next_ior;
+        if (thin) { eta_i = 1.0f; eta_t = 1.0f; next_ior = J.med.ior; }
+        else if (front) { eta_i = J.med.ior; eta_t = ior; next_ior = ior; }
+        else { eta_i = J.med.ior; eta_t = 1.0f; next_ior = 1.0f; }
+        float cosv = fabsf(ftd::dot3(normal, wo));
+        float fresnel;
+        if (transmission > 1.0e-4f) {
+          fresnel = fresnel_dielectric(cosv, eta_i, eta_t);
+        } else {
+          float f0 = clamp01(f0_from_ior(ior));
+          float x = 1.0f - clamp01(cosv);
+          float m5 = x * x * x * x * x;
+          fresnel = clamp01(f0 + (1.0f - f0) * m5);
+        }
+        float reflect_w;
+        if (transmission > 1.0e-4f) {
+          reflect_w = clamp01(fresnel);
+        } else {
+          float base = metallic > 0.5f ? 1.0f : clamp01(specular_strength);
+          reflect_w = clamp01(base * fresnel + metallic * 0.8f + clearcoat * 0.2f);
+        }
+        float local_w = clamp01((1.0f - transmission) * (1.0f - reflect_w));
+        F3 local = shade_color(S, mat, h.pos, normal, shading_n, wo, eps, P.max_dist, cx) * local_w;
+        acc = acc + mul3(W, local + mat_emission(mat));
+        if (reflect_w > 1.0e-4f && sp < kTraceStack) {
+          F3 rd = ftd::normalize3(J.d - normal * (2.0f * ftd::dot3(J.d, normal)));
+          F3 ro = offset_origin(h.pos, normal, rd, eps * (1.0f + rough * 6.0f));
+          F3 tint = lerp_sp(spec_color, base_color, clamp01(metallic));
+          stack[sp++] = RayJob{ro, rd, mul3(W, tint * reflect_w), J.med, J.depth + 1};
+        }
+        if (transmission > 1.0e-4f && sp < kTraceStack) {
+          MediumD next = thin ? J.med : transition(mat, front, J.med);
+          next.ior = ftd::rclamp(next_ior, 1.0f, 3.0f);
+          F3 td;
+          if (refract_dir(J.d, normal, eta_i / eta_t, &td)) {
+            F3 to = offset_origin(h.pos, normal, td, eps * (8.0f + rough * 12.0f));
+            float tt = clamp01(transmission);
+            F3 tint = f3(1.0f - (1.0f - clamp01(base_color.x)) * tt, 1.0f - (1.0f - clamp01(base_color.y)) * tt,
+                         1.0f - (1.0f - clamp01(base_color.z)) * tt);
+            stack[sp++] = RayJob{to, ftd::normalize3(td), mul3(W, tint * (transmission * (1.0f - fresnel))), next,
+                                 J.depth + 1};
+          }
+        }
+      }
+    }
+  }
+  return acc;
+}
+
+template <bool kStats>
+__device__ __forceinline__ void flush_counters(const Ctx<kStats>& cx, unsigned long long* stats) {
+  if (kStats) {
+    unsigned long long v[5] = {cx.c.evals, cx.c.prims, cx.c.boxes, cx.c.hook_instrs, cx.c.steps};
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      unsigned long long x = v[k];
+      for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+      if ((threadIdx.x & 31) == 0 && x) atomicAdd(&stats[k], x);
+    }
+  }
+}
+
+// One thread per (pixel, AA sample).
+template <bool kStats>
+__global__ void __launch_bounds__(128) trace_kernel(DevScene S, RayParams P, uint32_t max_depth,
+                                                    float* __restrict__ sample_rgb,
+                                                    unsigned long long* __restrict__ stats) {
+  uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  Ctx<kStats> cx;
+  cx.c = Counters{};
+  F3 dir;
+  size_t idx = 0;
+  if (i < P.n_items && item_ray(P, i, &dir, &idx)) {
+    F3 acc = trace_sample(S, P, max_depth, dir, cx);
+    sample_rgb[3 * idx] = acc.x;
+    sample_rgb[3 * idx + 1] = acc.y;
+    sample_rgb[3 * idx + 2] = acc.z;
+  }
+  flush_counters(cx, stats);
+}
+
+#ifndef FT_JIT  // batch, pixel, adjoint and measurement kernels: precompiled only
+// Batched traces: a persistent grid whose warps take 32 work items at a time
+// from a global counter; each item's scene and parameters come from the batch
+// tables and its samples land in the concatenated sample array.
+__global__ void __launch_bounds__(128) trace_batch_kernel(BatchView V, const uint32_t* __restrict__ max_depth,
+                                                          float* __restrict__ sample_rgb,
+                                                          unsigned long long* __restrict__ next_item) {
+  const unsigned lane = threadIdx.x & 31u;
+  Ctx<false> cx;
+  cx.c = Counters{};
+  for (;;) {
+    unsigned long long base = 0;
+    if (lane == 0) base = atomicAdd(next_item, 32ull);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= V.n_rays) break;
+    uint64_t g = base + lane;
+    if (g >= V.n_rays) continue;
+    uint32_t it = batch_item(V, g);
+    const RayParams& P = V.params[it];
+    F3 dir;
+    size_t idx = 0;
+    if (!item_ray(P, g - V.ray_first[it], &dir, &idx)) continue;
+    F3 acc = trace_sample(V.scenes[it], P, max_depth[it], dir, cx);
+    idx += V.out_first[it];
+    sample_rgb[3 * idx] = acc.x;
+    sample_rgb[3 * idx + 1] = acc.y;
+    sample_rgb[3 * idx + 2] = acc.z;
+  }
+}
+
+// AA average per pixel and spectrum_to_rgb8_reinhard (R:3908-3921, R:5229-5239).
+__global__ void trace_pixels_kernel(const float* __restrict__ sample_rgb, uint32_t n_pixels, uint32_t aa,
+                                    float* __restrict__ rgb_out, uint8_t* __restrict__ rgb8_out) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_pixels) return;
+  float s[3] = {0.0f, 0.0f, 0.0f};
+  for (uint32_t k = 0; k < aa; ++k)
+    for (int c = 0; c < 3; ++c) s[c] += sample_rgb[(static_cast<size_t>(i) * aa + k) * 3 + c];
+  float inv = 1.0f / static_cast<float>(aa);
+  for (int c = 0; c < 3; ++c) {
+    float v = s[c] * inv;
+    if (rgb_out) rgb_out[3 * static_cast<size_t>(i) + c] = v;
+    if (rgb8_out) rgb8_out[3 * static_cast<size_t>(i) + c] = reinhard_u8(v);
+  }
+}
+
+// Pixels of a batch: each item's depth preview or AA-averaged trace in the
+// concatenated image arrays (rgb holds the linear value: the preview value of
+// depth items, the averaged radiance of traces).
+struct BatchPixItem {
+  uint64_t pix_first;  // first pixel of the item in the image arrays
+  uint64_t out_first;  // first sample in the depth (t, mask) or trace sample arrays
+  uint32_t aa, kind;   // kind 0: depth preview, 1: trace
+  float max_dist;
+  uint32_t pad;
+};
+
+__global__ void batch_pixels_kernel(const BatchPixItem* __restrict__ items, uint32_t n_items, uint64_t n_pixels,
+                                    const float* __restrict__ t, const uint8_t* __restrict__ mask,
+                                    const float* __restrict__ sample_rgb, float* __restrict__ rgb_out,
+                                    uint8_t* __restrict__ rgb8_out) {
+  for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n_pixels;
+       g += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t lo = 0, hi = n_items;
+    while (hi - lo > 1) {
+      uint32_t mid = (lo + hi) >> 1;
+      if (items[mid].pix_first <= g) lo = mid;
+      else hi = mid;
+    }
+    const BatchPixItem& it = items[lo];
+    uint64_t local = g - it.pix_first;
+    size_t first = it.out_first + local * it.aa;
+    if (it.kind == 0) {
+      float v = depth_pixel_value(t, mask, first, it.aa, it.max_dist);
+      uint8_t c8 = gamma_u8(v);
+      for (int c = 0; c < 3; ++c) {
+        rgb_out[3 * g + c] = v;
+        rgb8_out[3 * g + c] = c8;
+      }
+    } else {
+      float s[3] = {0.0f, 0.0f, 0.0f};
+      for (uint32_t k = 0; k < it.aa; ++k)
+        for (int c = 0; c < 3; ++c) s[c] += sample_rgb[(first + k) * 3 + c];
+      float inv = 1.0f / static_cast<float>(it.aa);
+      for (int c = 0; c < 3; ++c) {
+        float v = s[c] * inv;
+        rgb_out[3 * g + c] = v;
+        rgb8_out[3 * g + c] = reinhard_u8(v);
+      }
+    }
+  }
+}
+
+#include "ft_diff.cuh"
+
+// Dependent-FMA chains, 8 per thread, for the FP32 roofline denominator.
+__global__ void fma_peak_kernel(float* out, int iters, float a, float b) {
+  float x0 = threadIdx.x * 1e-3f, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6,
+        x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fmaf(x0, a, b); x1 = fmaf(x1, a, b); x2 = fmaf(x2, a, b); x3 = fmaf(x3, a, b);
+    x4 = fmaf(x4, a, b); x5 = fmaf(x5, a, b); x6 = fmaf(x6, a, b); x7 = fmaf(x7, a, b);
+  }
+  float s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+  if (s == 12345.678f) out[0] = s;
+}
+
+#endif  // FT_JIT
+
+}  // namespace

@@ -43,7 +43,8 @@ typedef enum ft_status {
   FT_ERR_TIMEOUT = 8,
   FT_ERR_OUT_OF_MEMORY = 9,
   FT_ERR_UNSUPPORTED = 10,
-  FT_ERR_NO_DEVICE = 11
+  FT_ERR_NO_DEVICE = 11,
+  FT_ERR_JIT = 12           /* run-time compilation (NVRTC) or module load failed */
 } ft_status;
 
 /* `enum AccelMode` (R:58-63). */
@@ -409,7 +410,11 @@ ft_status ft_render_trace_stats(ft_scene* scene, const ft_render_options* option
  * x `safety`); every lattice point is stored as one FP16 texel of a 3D
  * texture holding the sample minus the largest bound of the bricks sharing
  * it, rounded down, so a hardware trilinear fetch is a lower bound of the
- * distance.
+ * distance.  Bricks whose Lipschitz estimate exceeds 4 (the field jumps there,
+ * e.g. where the reference's leaf culling switches), and bricks a hooked or
+ * modified leaf can reach (hooks move surfaces off their boxes; a domain +
+ * distance_post pair applies its transform twice), store no bound: the march
+ * is exact inside them.
  *
  * ft_render_depth with FT_FLAG_FP16_BRICKS marches on that bound (large
  * leaves evaluated exactly; exact march outside the region) while it is at
@@ -423,7 +428,7 @@ ft_status ft_render_trace_stats(ft_scene* scene, const ft_render_options* option
  * legacy default stream. */
 typedef struct ft_brick_options {
   float voxel_size;             /* lattice spacing; 0 = 0.02 */
-  float band;                   /* far-field threshold; 0 = 4 voxels */
+  float band;                   /* far-field threshold; 0 = 10 voxels */
   float safety;                 /* factor on the error bound; 0 = 1.25 */
   uint32_t max_lattice_points;  /* refuse larger lattices; 0 = 2^29 */
   uint32_t far_steps_per_pass;  /* far-field steps a lane takes per pass of its warp; 0 = 4 */
@@ -567,6 +572,30 @@ ft_status ft_render_backward(ft_scene* scene, const ft_view* views, uint32_t n_v
                              const ft_render_options* options, float tau, const ft_param* params,
                              uint32_t n_params, const float* dL_dt, const float* dL_dsil, double* dL_dparams,
                              uint32_t flags, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Scene JIT: the role of the reference's Cranelift JIT (J:607-747,
+ * J:2931-3016).  The scene's hook programs (domain, distance_post, the
+ * environment colour) are lowered to CUDA C++, one straight-line function per
+ * program with its registers as locals, and compiled together with the march
+ * and trace kernels for sm_103a by NVRTC; the module is loaded with the CUDA
+ * runtime's library API.  Afterwards ft_render_depth (plain and FP16-brick)
+ * and ft_render_trace of this scene launch the compiled kernels instead of
+ * the precompiled ones with the hook interpreter; statistics, batch,
+ * no-allocation and adjoint entry points keep the precompiled kernels.
+ * Results equal the interpreter's up to FMA contraction differences.
+ * Modules are cached per process by source, so scenes with the same hook
+ * programs compile once.  Synchronous. */
+typedef struct ft_jit_info {
+  uint32_t programs;      /* hook programs lowered */
+  uint32_t cached;        /* 1 when the module came from the process cache */
+  uint64_t source_bytes;  /* generated CUDA source */
+  uint64_t cubin_bytes;
+  double compile_ms;      /* NVRTC compile (0 when cached) */
+  double load_ms;         /* module load and kernel lookup */
+} ft_jit_info;
+
+ft_status ft_scene_jit(ft_scene* scene, ft_jit_info* info);
 
 /* Measured FP32 FMA throughput of the current device in TFLOP/s (a short
  * dependent-FMA kernel), used as the roofline denominator of the march. */

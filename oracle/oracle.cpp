@@ -2024,8 +2024,28 @@ int render_views(const ft_scene_desc* desc, const ft_view* views, uint32_t n_vie
           if (std::fabs(den) > R(1.0e-8))
             for (uint32_t k = 0; k < n_params; ++k) g[k] += wt * (-gl[k] / den);
         } else if (!r.hit && ws != R(0) && r.m > R(0) && r.sil > R(0)) {
+          // polish the minimum's position: secant steps on grad_p f . d = 0
+          auto slope = [&](R tt) {
+            std::vector<R> scratch(n_params, R(0));
+            Backprop<R> probe{scene, slots, scratch};
+            probe.run(desc->root, cam.origin + d * tt, R(1));
+            return dot(probe.gp, d);
+          };
+          R tm = r.tm;
+          const R dt0 = R(1.0e-3) * rmax(R(1), tm);
+          const R g0 = slope(tm);
+          R ta = tm - dt0, tb = tm + dt0, ga = slope(ta), gb = slope(tb);
+          for (int k = 0; k < 4 && gb != ga; ++k) {
+            R tn = tb - gb * (tb - ta) / (gb - ga);
+            tn = rmin(rmax(tn, tm - R(4) * dt0), tm + R(4) * dt0);
+            ta = tb;
+            ga = gb;
+            tb = tn;
+            gb = slope(tb);
+          }
+          if (std::fabs(gb) < std::fabs(g0)) tm = tb;
           Backprop<R> bp{scene, slots, gl};
-          bp.run(desc->root, cam.origin + d * r.tm, R(1));
+          bp.run(desc->root, cam.origin + d * tm, R(1));
           if (bp.unsupported) bad = true;
           for (uint32_t k = 0; k < n_params; ++k) g[k] += ws * (-(r.sil / tau) * gl[k]);
         }
