@@ -664,7 +664,9 @@ def main() -> None:
         raise RuntimeError(_native.last_error())
 
     # Dominant kernel: the same launch without the output conversion pass.
-    kernel = "trace_kernel" if args.mode == "trace" else "march_depth_persistent"
+    # (the trace's kernel time is the whole wavefront: wf_march, wf_shade and
+    # wf_shadow per bounce level; its FLOP count is the statistics pass's)
+    kernel = "wavefront_trace" if args.mode == "trace" else "march_depth_persistent"
     kernel_ms = statistics.mean(_time_steps(lambda: r(full_outputs=False), max(args.steps // 2, 3), stream, flush))
     roofline = _kernel_roofline(r, kernel_ms, peak.value, kernel)
     roofline["traffic"] = _traffic(kernel, w)

@@ -1021,119 +1021,176 @@ __device__ F3 environment(const DevScene& S, F3 dir) {
   return s;
 }
 
+// Shading of one hit (trace_hit_with_material, ray.rs:41-222, for each
+// material of the hit, ray.rs:31-35): the radiance it adds, its light samples
+// and its secondary rays, reported to `sink`:
+//   sink.emit(rgb)                          radiance added at this hit,
+//   sink.light(contrib, origin, dir, max_t) a light sample whose contribution
+//                                           is contrib x shadow_visibility,
+//   sink.push(job)                          a reflected or refracted ray.
+// shade_color (R:4217-4276) is distributed over the light samples:
+// W (sum_s f rad ndotl vis inv) local_w = sum_s W f rad ndotl inv local_w vis.
+template <bool kStats, class Sink>
+__device__ __forceinline__ void shade_hit(const DevScene& S, const RayParams& P, const RayJob& J, const TraceHit& h,
+                                          Sink& sink, Ctx<kStats>& cx) {
+  const float eps = P.eps;
+  Resolved rs;
+  resolve_hit(S, h.leaf, h.pos, &rs, cx);
+  bool front = ftd::dot3(h.normal, J.d) < 0.0f;
+  F3 normal = front ? ftd::normalize3(h.normal) : ftd::normalize3(h.normal * -1.0f);
+  F3 shading_n = normal;
+  if (rs.ok) shading_n = ftd::normalize3(front ? rs.normal : rs.normal * -1.0f);
+  DMat mats[2];
+  float ws[2];
+  int nm = 0;
+  if (rs.ok && rs.split) {
+    float tt = clamp01(rs.t);  // lerp_spectrum(a, b, t): a (1 - t) + b t
+    if (tt != 1.0f) { mats[nm] = rs.m; ws[nm++] = 1.0f - tt; }
+    if (tt != 0.0f) { mats[nm] = rs.mb; ws[nm++] = tt; }
+  } else {
+    mats[0] = rs.ok ? rs.m : mat_of_id(S, h.mat);
+    ws[0] = 1.0f;
+    nm = 1;
+  }
+  F3 att = transmittance(J.med, h.t);
+  F3 wo = ftd::normalize3(J.d * -1.0f);
+  for (int mi = 0; mi < nm; ++mi) {
+    const DMat& mat = mats[mi];
+    F3 W = mul3(J.w * ws[mi], att);
+    const DParams& Pm = dom_params(mat);
+    float rough = clamp01(Pm.roughness);
+    int model = dom_model(mat);
+    float transmission, ior, metallic, clearcoat, specular_strength;
+    bool thin;
+    F3 spec_color, base_color;
+    if (model == FT_MAT_STANDARD) {
+      transmission = clamp01(Pm.transmission); ior = ftd::rclamp(Pm.ior, 1.0f, 3.0f); thin = Pm.thin != 0;
+      spec_color = Pm.spec_color; base_color = Pm.color; metallic = clamp01(Pm.metallic);
+      clearcoat = clamp01(Pm.clearcoat); specular_strength = clamp01(Pm.specular * Pm.specular_weight);
+    } else if (model == FT_MAT_LAMBERT) {
+      transmission = 0.0f; ior = 1.0f; thin = false; spec_color = f3(0.0f, 0.0f, 0.0f); base_color = Pm.color;
+      metallic = 0.0f; clearcoat = 0.0f; specular_strength = 0.0f;
+    } else if (model == FT_MAT_METAL) {
+      transmission = 0.0f; ior = 1.0f; thin = false; spec_color = Pm.color; base_color = Pm.color;
+      metallic = 1.0f; clearcoat = 0.0f; specular_strength = 1.0f;
+    } else {
+      transmission = 1.0f; ior = ftd::rclamp(Pm.ior, 1.0f, 3.0f); thin = Pm.thin != 0;
+      spec_color = f3(1.0f, 1.0f, 1.0f); base_color = Pm.color; metallic = 0.0f; clearcoat = 0.0f;
+      specular_strength = 1.0f;
+    }
+    float eta_i, eta_t, next_ior;
+    if (thin) { eta_i = 1.0f; eta_t = 1.0f; next_ior = J.med.ior; }
+    else if (front) { eta_i = J.med.ior; eta_t = ior; next_ior = ior; }
+    else { eta_i = J.med.ior; eta_t = 1.0f; next_ior = 1.0f; }
+    float cosv = fabsf(ftd::dot3(normal, wo));
+    float fresnel;
+    if (transmission > 1.0e-4f) {
+      fresnel = fresnel_dielectric(cosv, eta_i, eta_t);
+    } else {
+      float f0 = clamp01(f0_from_ior(ior));
+      float x = 1.0f - clamp01(cosv);
+      float m5 = x * x * x * x * x;
+      fresnel = clamp01(f0 + (1.0f - f0) * m5);
+    }
+    float reflect_w;
+    if (transmission > 1.0e-4f) {
+      reflect_w = clamp01(fresnel);
+    } else {
+      float base = metallic > 0.5f ? 1.0f : clamp01(specular_strength);
+      reflect_w = clamp01(base * fresnel + metallic * 0.8f + clearcoat * 0.2f);
+    }
+    float local_w = clamp01((1.0f - transmission) * (1.0f - reflect_w));
+    // shade_color (R:4217-4276), light by light
+    if (S.n_lights == 0) {
+      sink.emit(W * local_w);
+    } else {
+      F3 n = ftd::normalize3(shading_n);
+      for (int li = 0; li < S.n_lights; ++li) {
+        const ft_light& L = S.lights[li];
+        uint32_t samples = L.kind == FT_LIGHT_SPHERE ? (L.samples > 0 ? L.samples : 1u) : 1u;
+        float inv = 1.0f / static_cast<float>(samples);
+        for (uint32_t smp = 0; smp < samples; ++smp) {
+          F3 wi, rad;
+          float dist;
+          sample_light(L, h.pos, smp, samples, &wi, &rad, &dist);
+          wi = ftd::normalize3(wi);
+          float ndotl = n.x * wi.x + n.y * wi.y + n.z * wi.z;
+          if (ndotl <= 0.0f) continue;
+          F3 so = offset_origin(h.pos, normal, wi, eps);
+          float max_t = isfinite(dist) ? fmaxf(dist - eps * 8.0f, 0.0f) : P.max_dist;
+          if (max_t <= 0.0f) continue;
+          F3 f = mat_eval(mat, shading_n, wi, wo);
+          sink.light(mul3(W, mul3(f, rad) * (ndotl * inv * local_w)), so, wi, max_t);
+        }
+      }
+    }
+    sink.emit(mul3(W, mat_emission(mat)));
+    if (reflect_w > 1.0e-4f) {
+      F3 rd = ftd::normalize3(J.d - normal * (2.0f * ftd::dot3(J.d, normal)));
+      F3 ro = offset_origin(h.pos, normal, rd, eps * (1.0f + rough * 6.0f));
+      F3 tint = lerp_sp(spec_color, base_color, clamp01(metallic));
+      sink.push(RayJob{ro, rd, mul3(W, tint * reflect_w), J.med, J.depth + 1});
+    }
+    if (transmission > 1.0e-4f) {
+      MediumD next = thin ? J.med : transition(mat, front, J.med);
+      next.ior = ftd::rclamp(next_ior, 1.0f, 3.0f);
+      F3 td;
+      if (refract_dir(J.d, normal, eta_i / eta_t, &td)) {
+        F3 to = offset_origin(h.pos, normal, td, eps * (8.0f + rough * 12.0f));
+        float tt = clamp01(transmission);
+        F3 tint = f3(1.0f - (1.0f - clamp01(base_color.x)) * tt, 1.0f - (1.0f - clamp01(base_color.y)) * tt,
+                     1.0f - (1.0f - clamp01(base_color.z)) * tt);
+        sink.push(RayJob{to, ftd::normalize3(td), mul3(W, tint * (transmission * (1.0f - fresnel))), next,
+                         J.depth + 1});
+      }
+    }
+  }
+}
+
+// Sink of the per-sample integrator: shadow rays are marched at once and the
+// secondary rays go to the sample's own job stack.
+template <bool kStats>
+struct StackSink {
+  const DevScene& S;
+  float eps;
+  F3 acc;
+  RayJob* stack;
+  int sp;
+  Ctx<kStats>& cx;
+  __device__ void emit(F3 v) { acc = acc + v; }
+  __device__ void light(F3 contrib, F3 o, F3 d, float max_t) {
+    float vis = shadow_visibility(S, o, d, max_t, eps, cx);
+    if (vis > 0.0f) acc = acc + contrib * vis;
+  }
+  __device__ void push(const RayJob& j) {
+    if (sp < kTraceStack) stack[sp++] = j;
+  }
+};
+
 // The full Whitted tree of one primary sample (trace_ray_recursive,
 // ray.rs:3-222), as a stack of ray jobs carrying their throughput weights.
 template <bool kStats>
 __device__ __forceinline__ F3 trace_sample(const DevScene& S, const RayParams& P, uint32_t max_depth, F3 dir,
                                            Ctx<kStats>& cx) {
-  F3 acc = f3(0.0f, 0.0f, 0.0f);
-  {
-    const float eps = P.eps;
-    RayJob stack[kTraceStack];
-    int sp = 0;
-    stack[sp++] = RayJob{f3(P.origin[0], P.origin[1], P.origin[2]), dir, f3(1.0f, 1.0f, 1.0f), air(), 0};
-    while (sp > 0) {
-      RayJob J = stack[--sp];
-      if (static_cast<uint32_t>(J.depth) >= max_depth) continue;
-      float min_t = J.depth == 0 ? 0.0f : eps * 2.0f;  // secondary_min_t (R:4175-4178)
-      TraceHit h;
-      if (!march_hit(S, P, J.o, J.d, min_t, &h, cx)) {
-        acc = acc + mul3(J.w, mul3(environment(S, J.d), transmittance(J.med, P.max_dist)));
-        continue;
-      }
-      Resolved rs;
-      resolve_hit(S, h.leaf, h.pos, &rs, cx);
-      bool front = ftd::dot3(h.normal, J.d) < 0.0f;
-      F3 normal = front ? ftd::normalize3(h.normal) : ftd::normalize3(h.normal * -1.0f);
-      F3 shading_n = normal;
-      if (rs.ok) shading_n = ftd::normalize3(front ? rs.normal : rs.normal * -1.0f);
-      DMat mats[2];
-      float ws[2];
-      int nm = 0;
-      if (rs.ok && rs.split) {
-        float tt = clamp01(rs.t);  // lerp_spectrum(a, b, t): a (1 - t) + b t
-        if (tt != 1.0f) { mats[nm] = rs.m; ws[nm++] = 1.0f - tt; }
-        if (tt != 0.0f) { mats[nm] = rs.mb; ws[nm++] = tt; }
-      } else {
-        mats[0] = rs.ok ? rs.m : mat_of_id(S, h.mat);
-        ws[0] = 1.0f;
-        nm = 1;
-      }
-      F3 att = transmittance(J.med, h.t);
-      F3 wo = ftd::normalize3(J.d * -1.0f);
-      for (int mi = 0; mi < nm; ++mi) {
-        const DMat& mat = mats[mi];
-        F3 W = mul3(J.w * ws[mi], att);
-        // trace_hit_with_material (ray.rs:41-222)
-        const DParams& Pm = dom_params(mat);
-        float rough = clamp01(Pm.roughness);
-        int model = dom_model(mat);
-        float transmission, ior, metallic, clearcoat, specular_strength;
-        bool thin;
-        F3 spec_color, base_color;
-        if (model == FT_MAT_STANDARD) {
-          transmission = clamp01(Pm.transmission); ior = ftd::rclamp(Pm.ior, 1.0f, 3.0f); thin = Pm.thin != 0;
-          spec_color = Pm.spec_color; base_color = Pm.color; metallic = clamp01(Pm.metallic);
-          clearcoat = clamp01(Pm.clearcoat); specular_strength = clamp01(Pm.specular * Pm.specular_weight);
-        } else if (model == FT_MAT_LAMBERT) {
-          transmission = 0.0f; ior = 1.0f; thin = false; spec_color = f3(0.0f, 0.0f, 0.0f); base_color = Pm.color;
-          metallic = 0.0f; clearcoat = 0.0f; specular_strength = 0.0f;
-        } else if (model == FT_MAT_METAL) {
-          transmission = 0.0f; ior = 1.0f; thin = false; spec_color = Pm.color; base_color = Pm.color;
-          metallic = 1.0f; clearcoat = 0.0f; specular_strength = 1.0f;
-        } else {
-          transmission = 1.0f; ior = ftd::rclamp(Pm.ior, 1.0f, 3.0f); thin = Pm.thin != 0;
-          spec_color = f3(1.0f, 1.0f, 1.0f); base_color = Pm.color; metallic = 0.0f; clearcoat = 0.0f;
-          specular_strength = 1.0f;
-        }
-        float eta_i, eta_t, next_ior;
-        if (thin) { eta_i = 1.0f; eta_t = 1.0f; next_ior = J.med.ior; }
-        else if (front) { eta_i = J.med.ior; eta_t = ior; next_ior = ior; }
-        else { eta_i = J.med.ior; eta_t = 1.0f; next_ior = 1.0f; }
-        float cosv = fabsf(ftd::dot3(normal, wo));
-        float fresnel;
-        if (transmission > 1.0e-4f) {
-          fresnel = fresnel_dielectric(cosv, eta_i, eta_t);
-        } else {
-          float f0 = clamp01(f0_from_ior(ior));
-          float x = 1.0f - clamp01(cosv);
-          float m5 = x * x * x * x * x;
-          fresnel = clamp01(f0 + (1.0f - f0) * m5);
-        }
-        float reflect_w;
-        if (transmission > 1.0e-4f) {
-          reflect_w = clamp01(fresnel);
-        } else {
-          float base = metallic > 0.5f ? 1.0f : clamp01(specular_strength);
-          reflect_w = clamp01(base * fresnel + metallic * 0.8f + clearcoat * 0.2f);
-        }
-        float local_w = clamp01((1.0f - transmission) * (1.0f - reflect_w));
-        F3 local = shade_color(S, mat, h.pos, normal, shading_n, wo, eps, P.max_dist, cx) * local_w;
-        acc = acc + mul3(W, local + mat_emission(mat));
-        if (reflect_w > 1.0e-4f && sp < kTraceStack) {
-          F3 rd = ftd::normalize3(J.d - normal * (2.0f * ftd::dot3(J.d, normal)));
-          F3 ro = offset_origin(h.pos, normal, rd, eps * (1.0f + rough * 6.0f));
-          F3 tint = lerp_sp(spec_color, base_color, clamp01(metallic));
-          stack[sp++] = RayJob{ro, rd, mul3(W, tint * reflect_w), J.med, J.depth + 1};
-        }
-        if (transmission > 1.0e-4f && sp < kTraceStack) {
-          MediumD next = thin ? J.med : transition(mat, front, J.med);
-          next.ior = ftd::rclamp(next_ior, 1.0f, 3.0f);
-          F3 td;
-          if (refract_dir(J.d, normal, eta_i / eta_t, &td)) {
-            F3 to = offset_origin(h.pos, normal, td, eps * (8.0f + rough * 12.0f));
-            float tt = clamp01(transmission);
-            F3 tint = f3(1.0f - (1.0f - clamp01(base_color.x)) * tt, 1.0f - (1.0f - clamp01(base_color.y)) * tt,
-                         1.0f - (1.0f - clamp01(base_color.z)) * tt);
-            stack[sp++] = RayJob{to, ftd::normalize3(td), mul3(W, tint * (transmission * (1.0f - fresnel))), next,
-                                 J.depth + 1};
-          }
-        }
-      }
+  const float eps = P.eps;
+  RayJob stack[kTraceStack];
+  StackSink<kStats> sink{S, eps, f3(0.0f, 0.0f, 0.0f), stack, 0, cx};
+  stack[sink.sp++] = RayJob{f3(P.origin[0], P.origin[1], P.origin[2]), dir, f3(1.0f, 1.0f, 1.0f), air(), 0};
+  while (sink.sp > 0) {
+    RayJob J = stack[--sink.sp];
+    if (static_cast<uint32_t>(J.depth) >= max_depth) continue;
+    float min_t = J.depth == 0 ? 0.0f : eps * 2.0f;  // secondary_min_t (R:4175-4178)
+    TraceHit h;
+    if (!march_hit(S, P, J.o, J.d, min_t, &h, cx)) {
+      sink.emit(mul3(J.w, mul3(environment(S, J.d), transmittance(J.med, P.max_dist))));
+      continue;
     }
+    shade_hit(S, P, J, h, sink, cx);
   }
-  return acc;
+  return sink.acc;
 }
+
+#include "ft_wavefront.cuh"
 
 template <bool kStats>
 __device__ __forceinline__ void flush_counters(const Ctx<kStats>& cx, unsigned long long* stats) {

@@ -109,7 +109,16 @@ struct ft_scene {
   cudaLibrary_t jit_lib = nullptr;
   cudaKernel_t jit_depth[2] = {nullptr, nullptr};  // plain, FP16 bricks
   cudaKernel_t jit_trace = nullptr;
+  cudaKernel_t jit_wf[3] = {nullptr, nullptr, nullptr};  // march, shade, shadow
   int jit_blocks[2] = {1, 1};
+  // Wavefront trace queues (grown on demand, reused across calls)
+  WJob* wf_jobs[2] = {nullptr, nullptr};
+  uint64_t wf_jobs_cap[2] = {0, 0};
+  WHit* wf_hits = nullptr;
+  uint64_t wf_hits_cap = 0;
+  WShadow* wf_shadows = nullptr;
+  uint64_t wf_shadows_cap = 0;
+  unsigned long long* wf_counters = nullptr;  // job counts (2), shadow count, overflow flag
   std::mutex mu;
 };
 
@@ -488,6 +497,94 @@ ft_status check_tuning(const ft_batch_tuning& t) {
   return FT_OK;
 }
 
+
+template <class T>
+ft_status grow(T** buf, uint64_t* cap, uint64_t want, const char* what) {
+  if (want <= *cap) return FT_OK;
+  cudaFree(*buf);
+  *buf = nullptr;
+  *cap = 0;
+  uint64_t n = want + want / 4 + 1024;
+  FT_CUDA_TRY(cudaMalloc(buf, n * sizeof(T)), what);
+  *cap = n;
+  return FT_OK;
+}
+
+// Whitted trace of one frame as a wavefront: per bounce level one march, one
+// shade and one shadow kernel over queues (ft_wavefront.cuh).  Radiance per
+// sample lands in sc->d_normal.  Queue sizes are read back once per level to
+// size the next one; the capacities are exact upper bounds (a job pushes at
+// most two materials x two rays, and two materials x the light samples).
+ft_status trace_wavefront(ft_scene* sc, const RayParams& P, uint32_t max_depth, cudaStream_t st) {
+  const ftgpu::SceneImage& im = sc->img;
+  uint64_t light_samples = 0;
+  for (const ft_light& L : im.lights) light_samples += L.kind == FT_LIGHT_SPHERE ? std::max(L.samples, 1u) : 1u;
+  uint64_t n = P.n_items;  // work items, tile padding included
+  if (!sc->wf_counters) FT_CUDA_TRY(cudaMalloc(&sc->wf_counters, 4 * sizeof(unsigned long long)), "cudaMalloc(queues)");
+  if (ft_status s = grow(&sc->wf_jobs[0], &sc->wf_jobs_cap[0], n, "cudaMalloc(ray jobs)")) return s;
+  unsigned long long* c = sc->wf_counters;
+  float* radiance = sc->d_normal;
+  const size_t samples = static_cast<size_t>(P.width) * P.height * P.aa;
+  FT_CUDA_TRY(cudaMemsetAsync(radiance, 0, samples * 3 * sizeof(float), st), "cudaMemsetAsync(radiance)");
+  FT_CUDA_TRY(cudaMemsetAsync(c, 0, 4 * sizeof(unsigned long long), st), "cudaMemsetAsync(queues)");
+  unsigned long long first = n;
+  FT_CUDA_TRY(cudaMemcpyAsync(c, &first, sizeof(first), cudaMemcpyHostToDevice, st), "queue count");
+  wf_primary_kernel<<<static_cast<unsigned>((n + 127) / 128), 128, 0, st>>>(P, sc->wf_jobs[0]);
+  FT_CUDA_TRY(cudaGetLastError(), "wf_primary_kernel launch");
+  int sms = 0;
+  FT_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, sc->device), "sm count");
+  const void* k_march = sc->jit_wf[0] ? reinterpret_cast<const void*>(sc->jit_wf[0])
+                                      : reinterpret_cast<const void*>(wf_march_kernel);
+  const void* k_shade = sc->jit_wf[1] ? reinterpret_cast<const void*>(sc->jit_wf[1])
+                                      : reinterpret_cast<const void*>(wf_shade_kernel);
+  const void* k_shadow = sc->jit_wf[2] ? reinterpret_cast<const void*>(sc->jit_wf[2])
+                                       : reinterpret_cast<const void*>(wf_shadow_kernel);
+  DevScene S = sc->dev;
+  RayParams PP = P;
+  int cur = 0;
+  for (uint32_t level = 0; level < max_depth && n > 0; ++level) {
+    const int nxt = 1 - cur;
+    if (ft_status s = grow(&sc->wf_hits, &sc->wf_hits_cap, n, "cudaMalloc(hits)")) return s;
+    if (ft_status s = grow(&sc->wf_jobs[nxt], &sc->wf_jobs_cap[nxt], 4 * n, "cudaMalloc(ray jobs)")) return s;
+    if (ft_status s = grow(&sc->wf_shadows, &sc->wf_shadows_cap, std::max<uint64_t>(2 * n * light_samples, 1),
+                           "cudaMalloc(shadow jobs)"))
+      return s;
+    FT_CUDA_TRY(cudaMemsetAsync(c + nxt, 0, sizeof(unsigned long long), st), "cudaMemsetAsync(queues)");
+    FT_CUDA_TRY(cudaMemsetAsync(c + 2, 0, sizeof(unsigned long long), st), "cudaMemsetAsync(queues)");
+    unsigned grid = static_cast<unsigned>(std::max<uint64_t>(1, std::min<uint64_t>((n + 127) / 128,
+                                                                                  static_cast<uint64_t>(sms) * 16)));
+    const WJob* jobs = sc->wf_jobs[cur];
+    const unsigned long long* count = c + cur;
+    WHit* hits = sc->wf_hits;
+    void* margs[] = {&S, &PP, &jobs, &count, &hits, &radiance};
+    FT_CUDA_TRY(cudaLaunchKernel(k_march, dim3(grid), dim3(128), margs, 0, st), "wavefront march launch");
+    WQueues Q{radiance, sc->wf_jobs[nxt], c + nxt, sc->wf_jobs_cap[nxt], sc->wf_shadows, c + 2,
+              sc->wf_shadows_cap, reinterpret_cast<unsigned int*>(c + 3), max_depth};
+    const WHit* chits = hits;
+    void* sargs[] = {&S, &PP, &jobs, &count, &chits, &Q};
+    FT_CUDA_TRY(cudaLaunchKernel(k_shade, dim3(grid), dim3(128), sargs, 0, st), "wavefront shade launch");
+    unsigned long long h[2] = {0, 0};
+    FT_CUDA_TRY(cudaMemcpyAsync(&h[0], c + nxt, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st), "queue count");
+    FT_CUDA_TRY(cudaMemcpyAsync(&h[1], c + 2, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st), "queue count");
+    FT_CUDA_TRY(cudaStreamSynchronize(st), "wavefront level");
+    if (h[1] > 0) {
+      unsigned sgrid = static_cast<unsigned>(std::max<uint64_t>(1, std::min<uint64_t>((h[1] + 127) / 128,
+                                                                                     static_cast<uint64_t>(sms) * 16)));
+      const WShadow* shadows = sc->wf_shadows;
+      const unsigned long long* scount = c + 2;
+      void* hargs[] = {&S, &PP, &shadows, &scount, &radiance};
+      FT_CUDA_TRY(cudaLaunchKernel(k_shadow, dim3(sgrid), dim3(128), hargs, 0, st), "wavefront shadow launch");
+    }
+    n = h[0];
+    cur = nxt;
+  }
+  unsigned long long overflow = 0;
+  FT_CUDA_TRY(cudaMemcpyAsync(&overflow, c + 3, sizeof(overflow), cudaMemcpyDeviceToHost, st), "queue flags");
+  FT_CUDA_TRY(cudaStreamSynchronize(st), "wavefront");
+  if (overflow) return ftcommon::fail(FT_ERR_CUDA, "wavefront queue overflow");
+  return FT_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -570,6 +667,11 @@ void ft_scene_destroy(ft_scene* sc) {
   cudaFree(sc->d_stats);
   free_bricks(sc);
   if (sc->jit_lib) cudaLibraryUnload(sc->jit_lib);
+  cudaFree(sc->wf_jobs[0]);
+  cudaFree(sc->wf_jobs[1]);
+  cudaFree(sc->wf_hits);
+  cudaFree(sc->wf_shadows);
+  cudaFree(sc->wf_counters);
   cudaSetDevice(prev);
   delete sc;
 }
@@ -667,19 +769,7 @@ ft_status ft_render_trace(ft_scene* sc, const ft_render_options* options, ft_acc
   RayParams P = make_params(sc, *options, aa);
   uint64_t blocks = (P.n_items + 127) / 128;
   if (blocks > 0x7fffffffull) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "image too large");
-  if (sc->jit_trace) {
-    DevScene S = sc->dev;
-    uint32_t md = depth;
-    float* srgb = sc->d_normal;
-    unsigned long long* none = nullptr;
-    void* args[] = {&S, &P, &md, &srgb, &none};
-    FT_CUDA_TRY(cudaLaunchKernel(reinterpret_cast<const void*>(sc->jit_trace), dim3(static_cast<unsigned>(blocks)),
-                                 dim3(128), args, 0, st),
-                "launch of the compiled trace kernel");
-  } else {
-    trace_kernel<false><<<static_cast<unsigned>(blocks), 128, 0, st>>>(sc->dev, P, depth, sc->d_normal, nullptr);
-    FT_CUDA_TRY(cudaGetLastError(), "trace_kernel launch");
-  }
+  if (ft_status s = trace_wavefront(sc, P, depth, st)) return s;
   float* rgbf = rgb_out ? (dev_ptrs ? rgb_out : sc->d_rgbf) : nullptr;
   uint8_t* rgb8 = rgb8_out ? (dev_ptrs ? rgb8_out : sc->d_rgb) : nullptr;
   uint32_t np = static_cast<uint32_t>(pixels);
@@ -1305,11 +1395,12 @@ ft_status ft_scene_jit(ft_scene* sc, ft_jit_info* info) {
                                            im.instrs.data()) +
                     "}  // namespace\n";
   out.source_bytes = src.size();
-  static const char* const kExprs[3] = {"march_depth_persistent<false, false, false>",
-                                        "march_depth_persistent<false, true, false>", "trace_kernel<false>"};
+  static const char* const kExprs[6] = {"march_depth_persistent<false, false, false>",
+                                        "march_depth_persistent<false, true, false>", "trace_kernel<false>",
+                                        "wf_march_kernel", "wf_shade_kernel", "wf_shadow_kernel"};
   struct Module {
     std::vector<char> cubin;
-    std::string lowered[3];
+    std::string lowered[6];
   };
   static std::mutex cache_mu;
   static std::map<std::string, Module> cache;
@@ -1357,7 +1448,7 @@ ft_status ft_scene_jit(ft_scene* sc, ft_jit_info* info) {
     mod.cubin.resize(cubin_size);
     r = nvrtcGetCUBIN(prog, mod.cubin.data());
     if (r != NVRTC_SUCCESS) return ftcommon::fail(FT_ERR_JIT, "nvrtcGetCUBIN failed");
-    for (int k = 0; k < 3; ++k) {
+    for (int k = 0; k < 6; ++k) {
       const char* lowered = nullptr;
       r = nvrtcGetLoweredName(prog, kExprs[k], &lowered);
       if (r != NVRTC_SUCCESS || !lowered) return ftcommon::fail(FT_ERR_JIT, std::string("no kernel ") + kExprs[k]);
@@ -1370,8 +1461,8 @@ ft_status ft_scene_jit(ft_scene* sc, ft_jit_info* info) {
   cudaLibrary_t lib = nullptr;
   FT_CUDA_TRY(cudaLibraryLoadData(&lib, mod.cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0),
               "cudaLibraryLoadData(scene module)");
-  cudaKernel_t k[3] = {nullptr, nullptr, nullptr};
-  for (int i = 0; i < 3; ++i) {
+  cudaKernel_t k[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  for (int i = 0; i < 6; ++i) {
     cudaError_t e = cudaLibraryGetKernel(&k[i], lib, mod.lowered[i].c_str());
     if (e != cudaSuccess) {
       cudaLibraryUnload(lib);
@@ -1395,6 +1486,9 @@ ft_status ft_scene_jit(ft_scene* sc, ft_jit_info* info) {
   sc->jit_depth[0] = k[0];
   sc->jit_depth[1] = k[1];
   sc->jit_trace = k[2];
+  sc->jit_wf[0] = k[3];
+  sc->jit_wf[1] = k[4];
+  sc->jit_wf[2] = k[5];
   sc->jit_blocks[0] = blocks[0];
   sc->jit_blocks[1] = blocks[1];
   auto t2 = std::chrono::steady_clock::now();

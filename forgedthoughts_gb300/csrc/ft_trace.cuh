@@ -693,36 +693,6 @@ __device__ F3 offset_origin(F3 pos, F3 gn, F3 dir, float eps) {
   return pos + no + ftd::normalize3(dir) * step;
 }
 
-// shade_color (R:4217-4276)
-template <bool kStats>
-__device__ F3 shade_color(const DevScene& S, const DMat& mat, F3 pos, F3 gn, F3 n_shade, F3 wo, float eps,
-                          float max_dist, Ctx<kStats>& cx) {
-  if (S.n_lights == 0) return f3(1.0f, 1.0f, 1.0f);
-  F3 n = ftd::normalize3(n_shade);
-  F3 color = f3(0.0f, 0.0f, 0.0f);
-  for (int li = 0; li < S.n_lights; ++li) {
-    const ft_light& L = S.lights[li];
-    uint32_t samples = L.kind == FT_LIGHT_SPHERE ? (L.samples > 0 ? L.samples : 1u) : 1u;
-    float inv = 1.0f / static_cast<float>(samples);
-    for (uint32_t s = 0; s < samples; ++s) {
-      F3 wi, rad;
-      float dist;
-      sample_light(L, pos, s, samples, &wi, &rad, &dist);
-      wi = ftd::normalize3(wi);
-      float ndotl = n.x * wi.x + n.y * wi.y + n.z * wi.z;
-      if (ndotl <= 0.0f) continue;
-      F3 so = offset_origin(pos, gn, wi, eps);
-      float max_t = isfinite(dist) ? fmaxf(dist - eps * 8.0f, 0.0f) : max_dist;
-      if (max_t <= 0.0f) continue;
-      float vis = shadow_visibility(S, so, wi, max_t, eps, cx);
-      if (vis <= 0.0f) continue;
-      F3 f = mat_eval(mat, n_shade, wi, wo);
-      color = color + mul3(f, rad) * (ndotl * vis * inv);
-    }
-  }
-  return color;
-}
-
 // fresnel_dielectric_scalar (R:5188-5204)
 __device__ float fresnel_dielectric(float ci, float eta_i, float eta_t) {
   float ei = fmaxf(eta_i, 1.0e-4f), et = fmaxf(eta_t, 1.0e-4f);
