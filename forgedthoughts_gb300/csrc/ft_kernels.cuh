@@ -71,6 +71,9 @@ struct DevScene {
   const int32_t* __restrict__ node_op_begin;
   const int32_t* __restrict__ node_op_end;
   const int32_t* __restrict__ ur_inner_blend;
+  const float* __restrict__ ur_cell_gaps;   // per cell entry: box gap lower bound (ascending per cell)
+  const int32_t* __restrict__ ur_inner_up;  // parent link (parent << 1 | side), -1 at the root
+  const int32_t* __restrict__ ur_prim_up;   // per primitive position: parent link
   int32_t n_materials, n_lights, env_program;
   int32_t bvh_root;
   float smin[3], smax[3];
@@ -209,10 +212,58 @@ __device__ __noinline__ Info eval_generic(const DevScene& S, int first, int coun
 __device__ __noinline__ Info ur_fold(const DevScene& S, const DevUrTree& t, const int* near_pos,
                                      const Info* near_info, int nn);
 
+// Parent value of a node whose only child holding a near primitive is on
+// `side`: the other child is +inf (exact for any far subtree, see above).
+__device__ __forceinline__ Info ur_lift(Info v, int side, float r) {
+  const Info inf{kInf, 0u, 0u};
+  return side == 0 ? ftd::combine(FT_NODE_UNION_ROUND, r, 0.0f, v, inf)
+                   : ftd::combine(FT_NODE_UNION_ROUND, r, 0.0f, inf, v);
+}
+
+// The restricted fold for one or two near primitives, in registers: lift each
+// along its parent links to their lowest common ancestor, combine there, and
+// lift the result to the root.  The same operations in the same order as the
+// frame walk of ur_fold.
+__device__ __forceinline__ Info ur_fold_small(const DevScene& S, const DevUrTree& t, int p0, Info v0, int p1, Info v1,
+                                              int nn) {
+  const float r = t.r;
+  int link = S.ur_prim_up[t.prim_first + p0];
+  if (nn == 2) {
+    if (p1 < p0) {  // in-order: the smaller position is in the left subtree of the common ancestor
+      int tp = p0; p0 = p1; p1 = tp;
+      Info tv = v0; v0 = v1; v1 = tv;
+      link = S.ur_prim_up[t.prim_first + p0];
+    }
+    // lift p0 until its parent's range holds p1
+    for (int guard = 0; guard <= ftgpu::kMaxUrDepth; ++guard) {
+      const DevUrInner& in = S.ur_inner[link >> 1];
+      if (in.lo <= p1 && p1 < in.hi) break;
+      v0 = ur_lift(v0, link & 1, r);
+      link = S.ur_inner_up[link >> 1];
+    }
+    const int lca = link >> 1;
+    int l1 = S.ur_prim_up[t.prim_first + p1];
+    for (int guard = 0; guard <= ftgpu::kMaxUrDepth && (l1 >> 1) != lca; ++guard) {
+      v1 = ur_lift(v1, l1 & 1, r);
+      l1 = S.ur_inner_up[l1 >> 1];
+    }
+    v0 = ftd::combine(FT_NODE_UNION_ROUND, r, 0.0f, v0, v1);
+    link = S.ur_inner_up[lca];
+  }
+  for (int guard = 0; guard <= ftgpu::kMaxUrDepth && link >= 0; ++guard) {
+    v0 = ur_lift(v0, link & 1, r);
+    link = S.ur_inner_up[link >> 1];
+  }
+  return v0;
+}
+
 template <bool kStats>
 __device__ __forceinline__ Info eval_urtree(const DevScene& S, const DevUrTree& t, F3 p, float cutoff,
                                             Ctx<kStats>& cx) {
   const float r = t.r;
+  // near set: the first two entries in registers, the rest (rare) in arrays
+  int np0 = 0, np1 = 0;
+  Info ni0{kInf, 0u, 0u}, ni1{kInf, 0u, 0u};
   int near_pos[ftgpu::kUrNear];
   Info near_info[ftgpu::kUrNear];
   int nn = 0;
@@ -229,25 +280,36 @@ __device__ __forceinline__ Info eval_urtree(const DevScene& S, const DevUrTree& 
     float d = ftd::prim_distance(pn, p);
     if (d < best.d) best = Info{d, pn.object_id, pn.material_id};
     if (d < r) {
-      if (nn < ftgpu::kUrNear) {
-        near_pos[nn] = pos;
-        near_info[nn] = Info{d, pn.object_id, pn.material_id};
-        ++nn;
+      Info v{d, pn.object_id, pn.material_id};
+      if (nn == 0) {
+        np0 = pos; ni0 = v;
+      } else if (nn == 1) {
+        np1 = pos; ni1 = v;
+      } else if (nn < ftgpu::kUrNear) {
+        near_pos[nn] = pos; near_info[nn] = v;
       } else {
         overflow = true;
+        return;
       }
+      ++nn;
     }
   };
   int stack[48];
   int sp = 0;
-  // Inside the candidate grid one cell list replaces the BVH walk.
+  // Inside the candidate grid one cell list replaces the BVH walk.  The list
+  // is sorted by a lower bound of the box bound of its points, so the first
+  // entry at or above the running limit ends it: every later primitive
+  // would be skipped by that test.
   float gx = (p.x - t.gmin[0]) * t.inv_cell, gy = (p.y - t.gmin[1]) * t.inv_cell, gz = (p.z - t.gmin[2]) * t.inv_cell;
   if (t.dims[0] > 0 && gx >= 0.0f && gy >= 0.0f && gz >= 0.0f && gx < (float)t.dims[0] && gy < (float)t.dims[1] &&
       gz < (float)t.dims[2]) {
     int ix = min((int)gx, t.dims[0] - 1), iy = min((int)gy, t.dims[1] - 1), iz = min((int)gz, t.dims[2] - 1);
     int cell = t.cell_first + ix + t.dims[0] * (iy + t.dims[1] * iz);
     uint32_t beg = S.ur_cell_offsets[cell], end = S.ur_cell_offsets[cell + 1];
-    for (uint32_t k = beg; k < end; ++k) consider(S.ur_cell_prims[k]);
+    for (uint32_t k = beg; k < end; ++k) {
+      if (S.ur_cell_gaps[k] >= ftd::rmax(r, fminf(best.d, cutoff))) break;
+      consider(S.ur_cell_prims[k]);
+    }
   } else {
     stack[sp++] = t.bvh_root;
   }
@@ -277,6 +339,9 @@ __device__ __forceinline__ Info eval_urtree(const DevScene& S, const DevUrTree& 
   }
   if (overflow) return eval_generic(S, t.fallback_first, t.fallback_count, p, cx);
   if (nn == 0) return best;
+  if (nn <= 2) return ur_fold_small(S, t, np0, ni0, np1, ni1, nn);
+  near_pos[0] = np0; near_info[0] = ni0;
+  near_pos[1] = np1; near_info[1] = ni1;
   return ur_fold(S, t, near_pos, near_info, nn);
 }
 

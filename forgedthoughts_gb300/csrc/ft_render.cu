@@ -150,6 +150,9 @@ ft_status upload_scene(ft_scene* sc) {
       {im.node_op_begin.data(), im.node_op_begin.size() * sizeof(int32_t), 0},
       {im.node_op_end.data(), im.node_op_end.size() * sizeof(int32_t), 0},
       {im.ur_inner_blend.data(), im.ur_inner_blend.size() * sizeof(int32_t), 0},
+      {im.ur_cell_gaps.data(), im.ur_cell_gaps.size() * sizeof(float), 0},
+      {im.ur_inner_up.data(), im.ur_inner_up.size() * sizeof(int32_t), 0},
+      {im.ur_prim_up.data(), im.ur_prim_up.size() * sizeof(int32_t), 0},
   };
   size_t total = 0;
   for (Part& p : parts) {
@@ -182,6 +185,9 @@ ft_status upload_scene(ft_scene* sc) {
   d.node_op_begin = reinterpret_cast<const int32_t*>(base + parts[15].off);
   d.node_op_end = reinterpret_cast<const int32_t*>(base + parts[16].off);
   d.ur_inner_blend = reinterpret_cast<const int32_t*>(base + parts[17].off);
+  d.ur_cell_gaps = reinterpret_cast<const float*>(base + parts[18].off);
+  d.ur_inner_up = reinterpret_cast<const int32_t*>(base + parts[19].off);
+  d.ur_prim_up = reinterpret_cast<const int32_t*>(base + parts[20].off);
   d.n_materials = static_cast<int32_t>(im.materials.size());
   d.n_lights = static_cast<int32_t>(im.lights.size());
   d.env_program = im.environment_program;

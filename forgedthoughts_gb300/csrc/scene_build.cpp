@@ -519,11 +519,13 @@ class Builder {
     const int nz = dims[2];
     std::vector<std::vector<uint32_t>> slab_offsets(nz);
     std::vector<std::vector<int32_t>> slab_prims(nz);
+    std::vector<std::vector<float>> slab_gaps(nz);
     auto work = [&](int z) {
       std::vector<std::pair<double, int32_t>> cand;
       cand.reserve(64);
       auto& offs = slab_offsets[z];
       auto& prims = slab_prims[z];
+      auto& gaps = slab_gaps[z];
       for (int y = 0; y < dims[1]; ++y)
         for (int x = 0; x < dims[0]; ++x) {
           double mn[3], mx[3];
@@ -555,7 +557,12 @@ class Builder {
           }
           std::sort(cand.begin(), cand.end());
           offs.push_back(static_cast<uint32_t>(prims.size()));
-          for (const auto& c : cand) prims.push_back(c.second);
+          for (const auto& c : cand) {
+            prims.push_back(c.second);
+            // Points of the cell are at least pad inside the padded box, so
+            // the device's float box bound of any of them exceeds this value.
+            gaps.push_back(std::nextafter(static_cast<float>(std::sqrt(c.first) * (1.0 - 1e-6)), 0.0f));
+          }
         }
     };
     unsigned nthreads = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
@@ -570,6 +577,7 @@ class Builder {
       uint32_t base = static_cast<uint32_t>(img_->ur_cell_prims.size());
       for (uint32_t o : slab_offsets[z]) img_->ur_cell_offsets.push_back(base + o);
       img_->ur_cell_prims.insert(img_->ur_cell_prims.end(), slab_prims[z].begin(), slab_prims[z].end());
+      img_->ur_cell_gaps.insert(img_->ur_cell_gaps.end(), slab_gaps[z].begin(), slab_gaps[z].end());
     }
     img_->ur_cell_offsets.push_back(static_cast<uint32_t>(img_->ur_cell_prims.size()));
   }
@@ -599,6 +607,19 @@ class Builder {
     };
     t.inner_root = walk(leaf.node);
     t.n_prims = static_cast<int32_t>(img_->ur_prims.size()) - t.prim_first;
+    // Parent links (the device folds one or two near primitives up to the
+    // root along them).
+    img_->ur_inner_up.resize(img_->ur_inner.size(), -1);
+    img_->ur_prim_up.resize(img_->ur_prims.size(), -1);
+    if (t.inner_root >= 0) {
+      for (size_t in = static_cast<size_t>(t.inner_root); in < img_->ur_inner.size(); ++in)
+        for (int side = 0; side < 2; ++side) {
+          int32_t c = img_->ur_inner[in].child[side];
+          int32_t link = static_cast<int32_t>(in << 1) | side;
+          if (c >= 0) img_->ur_inner_up[c] = link;
+          else img_->ur_prim_up[t.prim_first + (-c - 1)] = link;
+        }
+    }
     // Static material-model mixing of each inner node's primitives.
     img_->ur_inner_blend.resize(img_->ur_inner.size(), 0);
     for (size_t in = static_cast<size_t>(t.inner_root); in < img_->ur_inner.size(); ++in) {

@@ -79,6 +79,13 @@ struct SceneImage {
   std::vector<HostUrInner> ur_inner;
   std::vector<uint32_t> ur_cell_offsets;  // per grid cell: begin into ur_cell_prims
   std::vector<int32_t> ur_cell_prims;     // in-order primitive positions
+  // per ur_cell_prims entry: a lower bound of the distance from any point of
+  // the cell to the primitive's box (the lists are sorted by it)
+  std::vector<float> ur_cell_gaps;
+  // parent links of the union_round trees, (parent ur_inner index << 1) |
+  // side, -1 at the root: per ur_inner node and per primitive position
+  std::vector<int32_t> ur_inner_up;
+  std::vector<int32_t> ur_prim_up;
   // per ur_inner node: 1 when its primitives use more than one material model
   // (blend_materials then yields a Blend whatever the weights)
   std::vector<int32_t> ur_inner_blend;
