@@ -52,6 +52,12 @@ FLOP_PRIM = 34.0
 FLOP_STEP = 12.0
 
 L2_FLUSH_BYTES = 256 << 20  # > 129 MB L2
+_T0 = time.perf_counter()
+
+
+def _log(what: str) -> None:
+    """Progress on stderr (the JSON line is the only stdout)."""
+    print(f"[bench {time.perf_counter() - _T0:8.1f}s] {what}", file=sys.stderr, flush=True)
 
 
 def _env_int(name: str, default: int) -> int:
@@ -246,6 +252,11 @@ class Renderer:
                                           self.native.FT_FLAG_DEVICE_POINTERS | self.extra_flags, self.sptr)
         if rc != 0:
             raise RuntimeError(self.native.last_error())
+        n = ctypes.c_uint32(0)
+        self.lib.ft_scene_last_launches(self.scene.handle, ctypes.byref(n))
+        self.launches += n.value
+
+    launches = 0  # kernels launched by the calls so far
 
     def stats(self):
         s = self.native.RenderStatsC()
@@ -370,9 +381,11 @@ def precision_form(reps: int = 2) -> dict:
     ft.render_depth(st, w.options, w.accel, 1)  # warm-up
     plain_ms = _cuda_ms(lambda: ft.render_depth(st, w.options, w.accel, 1, want_rgb8=False), reps)
     ref = ft.render_depth(st, w.options, w.accel, 1)
+    _log(f"  plain {plain_ms:.1f} ms; NVRTC compile")
     t0 = time.perf_counter()
     jit = g.jit()
     jit["wall_ms"] = 1000.0 * (time.perf_counter() - t0)
+    _log(f"  compiled in {jit['wall_ms']:.0f} ms")
     ft.render_depth(st, w.options, w.accel, 1)
     jit_ms = _cuda_ms(lambda: ft.render_depth(st, w.options, w.accel, 1, want_rgb8=False), reps)
     jimg = ft.render_depth(st, w.options, w.accel, 1)
@@ -411,6 +424,7 @@ def batched_form(reps: int = 3) -> dict:
     for st in states:
         st.gpu()
     setup_ms = 1000.0 * (time.perf_counter() - t0)
+    _log(f"  {len(ws)} scenes set up in {setup_ms:.0f} ms")
     items = [(st, w.options, w.aa, w.max_depth) for st, w in zip(states, ws)]
 
     import torch
@@ -440,6 +454,7 @@ def batched_form(reps: int = 3) -> dict:
 
     one_by_one()
     seq_ms = _cuda_ms(one_by_one, 1)
+    _log(f"  one by one {seq_ms:.1f} ms; autotune")
     b32 = ft.Batch(items)
     n = b32.samples()
     tune32 = b32.autotune()
@@ -503,7 +518,10 @@ def differentiation_form(adam_steps: int = 200, reps: int = 3) -> dict:
     mom, vel = np.zeros_like(theta), np.zeros_like(theta)
     lr, b1, b2, eps = 0.01, 0.9, 0.999, 1e-8
     losses = []
+    _log(f"  forward + adjoint {1000 * step_s:.1f} ms; Adam")
     for k in range(1, adam_steps + 1):
+        if k % 50 == 0:
+            _log(f"  Adam step {k}")
         loss, g = loss_and_grad(theta.astype(np.float32))
         losses.append(loss)
         mom = b1 * mom + (1 - b1) * g
@@ -640,6 +658,7 @@ def main() -> None:
     items = r.items
 
     clocks = ClockSampler(local)
+    _log(f"{args.mode}: {args.warmup} warm-up + {args.steps} timed steps")
     clocks.start()
     for _ in range(args.warmup):
         r()
@@ -647,7 +666,9 @@ def main() -> None:
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
+    r.launches = 0
     step_ms = _time_steps(r, args.steps, stream, flush)
+    timed_launches = r.launches
     if dist:
         dist.barrier()
     clk = clocks.stop()
@@ -671,6 +692,7 @@ def main() -> None:
     roofline = _kernel_roofline(r, kernel_ms, peak.value, kernel)
     roofline["traffic"] = _traffic(kernel, w)
 
+    _log("roofline done; end-to-end steps")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -679,8 +701,9 @@ def main() -> None:
         "roofline": roofline,
         "e2e": None if args.no_e2e else _e2e(lib, st, w, args.mode, min(args.steps, 5)),
         "clocks": clk,
-        "gpu_launches": 2 * args.steps,
+        "gpu_launches": timed_launches,
     }
+    _log("secondary figures")
     if not args.no_secondary:
         plain = None
         if args.mode == "trace":
@@ -695,11 +718,20 @@ def main() -> None:
         line["depth_march_fp16_bricks"] = fp16
     if rank == 0 and not args.no_forms:
         # the north-star's three chosen forms beside the plain method
-        line["forms"] = {"precision_fp16_bricks_and_jit": precision_form(),
-                         "batched": batched_form(),
-                         "differentiation": differentiation_form(args.adam_steps)}
+        forms = {}
+        for name, fn in (("precision_fp16_bricks_and_jit", precision_form), ("batched", batched_form),
+                         ("differentiation", lambda: differentiation_form(args.adam_steps))):
+            _log(name)
+            try:
+                forms[name] = fn()
+            except Exception as exc:  # a failing form is reported, the line still printed
+                forms[name] = {"error": f"{type(exc).__name__}: {exc}"}
+                _log(f"  {name} failed: {exc}")
+        line["forms"] = forms
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        _log("cpu baseline")
         line["cpu_baseline"] = cpu_baseline(w, args.mode)
+    _log("done")
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:

@@ -214,9 +214,11 @@ class GpuScene:
                 "cubin_bytes": info.cubin_bytes, "compile_ms": info.compile_ms, "load_ms": info.load_ms}
 
     def build_bricks(self, voxel_size: float = 0.02, band: float = 0.0, safety: float = 0.0,
-                     max_lattice_points: int = 0, far_steps_per_pass: int = 0) -> "BrickInfo":
+                     max_lattice_points: int = 0, far_steps_per_pass: int = 0,
+                     free_far_steps: bool = False) -> "BrickInfo":
         """Build the FP16 brick distance cache (``ft_scene_build_bricks``)."""
-        o = _native.BrickOptionsC(voxel_size, band, safety, max_lattice_points, far_steps_per_pass, 0)
+        o = _native.BrickOptionsC(voxel_size, band, safety, max_lattice_points, far_steps_per_pass,
+                                  _native.FT_BRICK_FREE_FAR_STEPS if free_far_steps else 0)
         info = _native.BrickInfoC()
         _check(_native.lib().ft_scene_build_bricks(self._h, ctypes.byref(o), ctypes.byref(info)))
         return BrickInfo(tuple(info.region_min), tuple(info.region_max), tuple(info.bricks), info.near_bricks,

@@ -28,6 +28,7 @@ FT_ERR_JIT = 12
 
 FT_FLAG_DEVICE_POINTERS = 1
 FT_FLAG_FP16_BRICKS = 2
+FT_BRICK_FREE_FAR_STEPS = 1
 FT_ABI_VERSION = 1
 FT_MAX_PROGRAM_REGS = 64
 
@@ -106,7 +107,7 @@ class RenderStatsC(ctypes.Structure):
 class BrickOptionsC(ctypes.Structure):
     _fields_ = [("voxel_size", ctypes.c_float), ("band", ctypes.c_float), ("safety", ctypes.c_float),
                 ("max_lattice_points", ctypes.c_uint32), ("far_steps_per_pass", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32)]
+                ("flags", ctypes.c_uint32)]
 
 
 class BrickInfoC(ctypes.Structure):
@@ -153,6 +154,7 @@ SIGNATURES = {
     "ft_scene_create": (ctypes.c_int, [ctypes.POINTER(SceneDescC), ctypes.POINTER(ctypes.c_void_p)]),
     "ft_scene_destroy": (None, [ctypes.c_void_p]),
     "ft_scene_device_bytes": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64)]),
+    "ft_scene_last_launches": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint32)]),
     "ft_scene_build_info": (ctypes.c_int, [ctypes.POINTER(SceneDescC), ctypes.POINTER(BuildInfoC)]),
     "ft_render_depth": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RenderOptionsC), ctypes.c_int,
                                        ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,

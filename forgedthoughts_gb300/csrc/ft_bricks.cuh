@@ -40,6 +40,13 @@ struct DevBricks {
   int32_t far_batch;         // far-field steps per pass of the warp
   int32_t n_exact;
   int32_t exact_leaf[kMaxExactLeaves];
+  int32_t free_far;          // FT_BRICK_FREE_FAR_STEPS: free far-field steps instead of the counted form
+  int32_t outside_ok;        // the cached leaves lie in the region box (no hooked or modified leaves)
+  float outside_margin;      // subtracted from the region-box distance (blend bulges)
+  int32_t plane_leaf;        // the only exact leaf when it is an axis-aligned box, else -1
+  uint32_t plane_obj;        // its object id
+  float plane_top;           // its top face: y = plane_top over [plane_lo, plane_hi] in x and z
+  float plane_lo[2], plane_hi[2];
 };
 
 // Leaf-BVH walk of the scene minus the exact leaves (bvh_distance_info,
@@ -54,7 +61,7 @@ __device__ Info scene_distance_skip(const DevScene& S, F3 p, const DevBricks& B,
   stack[sp] = S.bvh_root;
   stack_lb[sp] = node_lb(p, S.bvh[S.bvh_root].bmin, S.bvh[S.bvh_root].bmax);
   ++sp;
-  while (sp > 0) {
+  for (int walk = 0; sp > 0 && walk < ftgpu::kMaxWalk; ++walk) {  // a tree walk pops each node once
     --sp;
     int ni = stack[sp];
     if (stack_lb[sp] > best) continue;
@@ -99,6 +106,40 @@ __device__ __forceinline__ bool far_bound(const DevScene& S, const DevBricks& B,
   for (int i = 0; i < B.n_exact; ++i) v = fminf(v, eval_leaf(S, S.leaves[B.exact_leaf[i]], p, kInf, cx).d);
   *out = v;
   return true;
+}
+
+// Lower bound of the distance to the cached leaves (the scene without its
+// exact leaves) at p: the fetched bound inside the brick region; outside it
+// the distance to the region box less the margin where every cached leaf
+// lies inside that box, else -inf.
+template <bool kStats>
+__device__ __forceinline__ float cached_lb(const DevBricks& B, F3 p, Ctx<kStats>& cx) {
+  float gx = (p.x - B.rmin[0]) * B.inv_h, gy = (p.y - B.rmin[1]) * B.inv_h, gz = (p.z - B.rmin[2]) * B.inv_h;
+  if (gx >= 0.0f && gy >= 0.0f && gz >= 0.0f && gx <= B.last[0] && gy <= B.last[1] && gz <= B.last[2]) {
+    cx.fetch();
+    return tex3D<float>(B.atlas, gx + 0.5f, gy + 0.5f, gz + 0.5f);
+  }
+  if (!B.outside_ok) return -kInf;
+  return ftd::aabb_lb(p, B.rmin, B.rmax) - B.outside_margin;
+}
+
+// Whether the rest of a plain march from q (scene distance g, the plane
+// leaf's) is a descent onto the plane leaf's top face: the ray goes
+// down, q and the crossing lie over the face, and the cached leaves are
+// farther than the crossing along the ray (their distance shrinks by at most
+// the distance travelled, the plane's by sin(angle) times it, so the plane
+// stays the minimum at every sample).  Requires the minimum step to stay
+// below scale * eps, so every step above the shell is scale * height.
+__device__ __forceinline__ bool plane_jump(const DevBricks& B, F3 q, F3 d, float g, float cached, float eps,
+                                           float scale, float min_step) {
+  const float sdn = -d.y;
+  if (!(sdn > 0.0f) || !(g >= eps) || !(min_step < scale * eps) || !(scale * sdn < 1.0f)) return false;
+  if (!(q.y > B.plane_top)) return false;
+  const float along = g / sdn;
+  if (!(cached > along)) return false;
+  const float ex = q.x + d.x * along, ez = q.z + d.z * along;
+  return q.x > B.plane_lo[0] && q.x < B.plane_hi[0] && q.z > B.plane_lo[1] && q.z < B.plane_hi[1] &&
+         ex > B.plane_lo[0] && ex < B.plane_hi[0] && ez > B.plane_lo[1] && ez < B.plane_hi[1];
 }
 
 #ifndef FT_JIT  // build and query kernels: precompiled only

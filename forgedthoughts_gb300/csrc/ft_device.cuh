@@ -129,6 +129,13 @@ FT_DEV float prim_local(int kind, const float* f, int ival, F3 q) {
 
 FT_DEV float prim_distance(const DevNode& n, F3 p) { return prim_local(n.kind, n.f, n.ival, to_local(p, n)); }
 
+// Device-wide nanosecond timer (%globaltimer), for time limits of long loops.
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
 // point_aabb_lower_bound (R:5388-5411)
 FT_DEV float aabb_lb(F3 p, const float* mn, const float* mx) {
   float dx = p.x < mn[0] ? mn[0] - p.x : (p.x > mx[0] ? p.x - mx[0] : 0.0f);

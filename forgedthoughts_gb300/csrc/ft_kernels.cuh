@@ -313,7 +313,7 @@ __device__ __forceinline__ Info eval_urtree(const DevScene& S, const DevUrTree& 
   } else {
     stack[sp++] = t.bvh_root;
   }
-  while (sp > 0) {
+  for (int walk = 0; sp > 0 && walk < ftgpu::kMaxWalk; ++walk) {  // a tree walk pops each node once
     const DevUrBvh& bn = S.ur_bvh[stack[--sp]];
     cx.box();
     float bound = ftd::rmax(r, fminf(best.d, cutoff));
@@ -359,7 +359,7 @@ __device__ __noinline__ Info ur_fold(const DevScene& S, const DevUrTree& t, cons
   int fp = 0;
   fr[0].inner = t.inner_root;
   fr[0].stage = 0;
-  for (;;) {
+  for (int walk = 0; walk < ftgpu::kMaxWalk; ++walk) {  // each inner node is opened once
     Frame& F = fr[fp];
     if (F.stage < 2) {
       const DevUrInner& in = S.ur_inner[F.inner];
@@ -379,6 +379,7 @@ __device__ __noinline__ Info ur_fold(const DevScene& S, const DevUrTree& t, cons
         F.slot[F.stage++] = Info{kInf, 0u, 0u};
         continue;
       }
+      if (fp + 1 > ftgpu::kMaxUrDepth) break;  // deeper than the builder admits
       ++F.stage;
       ++fp;
       fr[fp].inner = c;
@@ -390,6 +391,7 @@ __device__ __noinline__ Info ur_fold(const DevScene& S, const DevUrTree& t, cons
     --fp;
     fr[fp].slot[fr[fp].stage - 1] = res;
   }
+  return Info{kInf, 0u, 0u};  // only a corrupted tree gets here
 }
 
 template <bool kStats>
@@ -418,7 +420,7 @@ __device__ __noinline__ Info scene_distance_bvh(const DevScene& S, F3 p, Ctx<kSt
   stack_lb[sp] = node_lb(p, S.bvh[S.bvh_root].bmin, S.bvh[S.bvh_root].bmax);
   ++sp;
   cx.box();
-  while (sp > 0) {
+  for (int walk = 0; sp > 0 && walk < ftgpu::kMaxWalk; ++walk) {  // a tree walk pops each node once
     --sp;
     int ni = stack[sp];
     if (stack_lb[sp] > best) continue;
@@ -497,7 +499,7 @@ __device__ __noinline__ Info scene_distance_leaf(const DevScene& S, F3 p, int* l
   stack[sp] = S.bvh_root;
   stack_lb[sp] = node_lb(p, S.bvh[S.bvh_root].bmin, S.bvh[S.bvh_root].bmax);
   ++sp;
-  while (sp > 0) {
+  for (int walk = 0; sp > 0 && walk < ftgpu::kMaxWalk; ++walk) {  // a tree walk pops each node once
     --sp;
     int ni = stack[sp];
     if (stack_lb[sp] > best) continue;
@@ -730,6 +732,7 @@ __device__ __forceinline__ bool item_ray(const RayParams& P, uint64_t i, F3* dir
 // by an exact evaluation) instead of ten bisections, and the material comes
 // from the accepted point's evaluation; the normal is the plain method's.
 enum Phase : int { kMarch = 0, kRefine = 1, kNormal = 2, kFinal = 3, kFar = 4, kSecant = 5 };
+constexpr unsigned long long kMarchWallNs = 20ull * 1000000000ull;  // per warp
 
 //
 // With kBatch the launch serves many renders: each lane carries the index of
@@ -755,6 +758,14 @@ __global__ void __launch_bounds__(128) march_depth_persistent(DevScene S0, RayPa
   bool queue_done = false;
   size_t idx = 0;
   uint32_t item_of_lane = 0;
+  // Self-checks: a ray takes at most max_steps + 17 iterations (one step per
+  // march or far-field iteration, then bisection or secant, normal taps and
+  // the final lookup), and a warp runs for at most kMarchWallNs.  A lane past
+  // either limit records it in next_item[1] (bit per phase; bit 8: time) and
+  // gives up, so a fault in the march ends the launch instead of hanging it.
+  uint32_t ray_iters = 0;
+  uint32_t loop_iters = 0;
+  const unsigned long long t_start = __shfl_sync(0xffffffffu, lane == 0 ? ftd::global_ns() : 0ull, 0);
   // per-ray constants (per item with kBatch)
   F3 o = f3(P0.origin[0], P0.origin[1], P0.origin[2]);
   float eps = P0.eps;
@@ -797,6 +808,14 @@ __global__ void __launch_bounds__(128) march_depth_persistent(DevScene S0, RayPa
   };
 
   for (;;) {
+    if ((++loop_iters & 1023u) == 0u) {
+      unsigned long long now = lane == 0 ? ftd::global_ns() : 0ull;
+      now = __shfl_sync(0xffffffffu, now, 0);
+      if (now - t_start > kMarchWallNs) {
+        if (lane == 0) atomicOr(&next_item[1], 1ull << 8);
+        break;
+      }
+    }
     // Refill idle lanes when enough of the warp is idle (or all of it).
     unsigned idle = __ballot_sync(0xffffffffu, !live);
     if (!queue_done && (__popc(idle) >= refill || idle == 0xffffffffu)) {
@@ -826,6 +845,8 @@ __global__ void __launch_bounds__(128) march_depth_persistent(DevScene S0, RayPa
         }
         const DevScene& S = kBatch ? V.scenes[item_of_lane] : S0;
         const RayParams& P = kBatch ? V.params[item_of_lane] : P0;
+        const DevBricks& B_of_lane = kBatch ? V.bricks[item_of_lane] : B0;
+        (void)B_of_lane;
         if (got) {
           float t0, t1;
           bool inside = ray_aabb(o, d, S.smin, S.smax, &t0, &t1);
@@ -833,9 +854,10 @@ __global__ void __launch_bounds__(128) march_depth_persistent(DevScene S0, RayPa
           max_t = fminf(P.max_dist, t1);
           if (inside && P.max_steps > 0 && !(traveled > max_t)) {
             live = true;
+            ray_iters = 0;
             prev = traveled;
             steps = 0;
-            phase = kBricks ? kFar : kMarch;
+            phase = kBricks && B_of_lane.free_far ? kFar : kMarch;
             dprev = -1.0f;
             mat_known = false;
           } else {
@@ -852,6 +874,11 @@ __global__ void __launch_bounds__(128) march_depth_persistent(DevScene S0, RayPa
     const DevScene& S = kBatch ? V.scenes[item_of_lane] : S0;
     const RayParams& P = kBatch ? V.params[item_of_lane] : P0;
     const DevBricks& B = kBatch ? V.bricks[item_of_lane] : B0;
+    if (++ray_iters > P.max_steps + 64u) {
+      atomicOr(&next_item[1], 1ull << (phase & 7));
+      write_miss();
+      continue;
+    }
 
     if (kBricks && phase == kFar) {
       bool exact = false, missed = false;
@@ -889,8 +916,10 @@ __global__ void __launch_bounds__(128) march_depth_persistent(DevScene S0, RayPa
       mid = 0.5f * (lo + hi);
       q = o + d * mid;
     } else if (kBricks && phase == kSecant) {
-      // crossing of d = eps on the line through (lo, dlo) and (hi, dhi)
-      mid = lo + (dlo - eps) / (dlo - dhi) * (hi - lo);
+      // crossing of d = eps on the line through (lo, dlo) and (hi, dhi),
+      // aimed 1/64 eps inside the shell so rounding keeps it there
+      const float target = eps * (1.0f - 1.0f / 64.0f);
+      mid = lo + (dlo - target) / (dlo - dhi) * (hi - lo);
       mid = fminf(fmaxf(mid, lo), hi);
       q = o + d * mid;
     } else if (phase == kNormal) {
@@ -914,15 +943,47 @@ __global__ void __launch_bounds__(128) march_depth_persistent(DevScene S0, RayPa
           dlo = dprev;
           dhi = info.d;
           hit_mat = info.mat;
+          mat_known = true;  // the march's own sample at hi
         } else {
           phase = kRefine;
         }
       } else {
+        // the nearest leaf is the ground and the ray descends: the cached
+        // bound decides whether the rest of the approach is a plane descent
+        if (kBricks && !B.free_far && B.plane_leaf >= 0 && info.obj == B.plane_obj && d.y < 0.0f &&
+            plane_jump(B, q, d, info.d, cached_lb(B, q, cx), eps, scale, min_step)) {
+          // The rest of the plain march descends on the plane: after n more
+          // steps it first samples inside the eps shell (heights shrink by
+          // 1 - scale*s per step).  Same outcome as the plain march: a miss
+          // when it would run out of steps or distance on the way.
+          const float sdn = -d.y;
+          const float g = info.d;
+          const double c = static_cast<double>(scale) * static_cast<double>(sdn);
+          const double x = log(static_cast<double>(eps) / static_cast<double>(g)) / log1p(-c);
+          const double n = floor(x) + 1.0;
+          const double tn = static_cast<double>(traveled) +
+                            (static_cast<double>(g) - static_cast<double>(g) * pow(1.0 - c, n)) / sdn;
+          cx.far_step();
+          if (!(n < 1.0e9) || static_cast<double>(steps) + n >= static_cast<double>(P.max_steps) ||
+              tn > static_cast<double>(max_t)) {
+            write_miss();
+            continue;
+          }
+          // bracket: here (distance g) and the plane crossing (distance 0)
+          lo = traveled;
+          dlo = g;
+          hi = traveled + g / sdn;
+          dhi = 0.0f;
+          k = 0;
+          phase = kSecant;
+          mat_known = false;  // hi is not a verified sample: the material comes from an evaluation
+          continue;
+        }
         prev = traveled;
         if (kBricks) dprev = info.d;
         traveled += fmaxf(fabsf(info.d) * scale, min_step);
         ++steps;
-        if (kBricks && fabsf(info.d) > B.band_exit) phase = kFar;
+        if (kBricks && B.free_far && fabsf(info.d) > B.band_exit) phase = kFar;
         if (steps >= P.max_steps || traveled > max_t) write_miss();
       }
     } else if (kBricks && phase == kSecant) {
@@ -930,6 +991,7 @@ __global__ void __launch_bounds__(128) march_depth_persistent(DevScene S0, RayPa
       if (fabsf(info.d) < eps) {
         hi = mid;
         hit_mat = info.mat;
+        mat_known = true;
       } else if (info.d > 0.0f && ++k < 3) {
         lo = mid;
         dlo = info.d;
@@ -937,10 +999,10 @@ __global__ void __launch_bounds__(128) march_depth_persistent(DevScene S0, RayPa
       }
       if (accept) {
         pos = o + d * hi;
-        mat_known = true;
         k = 0;
         if (want_normal) phase = kNormal;
-        else write_hit(hit_mat);
+        else if (mat_known) write_hit(hit_mat);
+        else phase = kFinal;
       }
     } else if (phase == kRefine) {
       if (fabsf(info.d) < eps) hi = mid;
@@ -1290,35 +1352,6 @@ __global__ void __launch_bounds__(128) trace_kernel(DevScene S, RayParams P, uin
 }
 
 #ifndef FT_JIT  // batch, pixel, adjoint and measurement kernels: precompiled only
-// Batched traces: a persistent grid whose warps take 32 work items at a time
-// from a global counter; each item's scene and parameters come from the batch
-// tables and its samples land in the concatenated sample array.
-__global__ void __launch_bounds__(128) trace_batch_kernel(BatchView V, const uint32_t* __restrict__ max_depth,
-                                                          float* __restrict__ sample_rgb,
-                                                          unsigned long long* __restrict__ next_item) {
-  const unsigned lane = threadIdx.x & 31u;
-  Ctx<false> cx;
-  cx.c = Counters{};
-  for (;;) {
-    unsigned long long base = 0;
-    if (lane == 0) base = atomicAdd(next_item, 32ull);
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (base >= V.n_rays) break;
-    uint64_t g = base + lane;
-    if (g >= V.n_rays) continue;
-    uint32_t it = batch_item(V, g);
-    const RayParams& P = V.params[it];
-    F3 dir;
-    size_t idx = 0;
-    if (!item_ray(P, g - V.ray_first[it], &dir, &idx)) continue;
-    F3 acc = trace_sample(V.scenes[it], P, max_depth[it], dir, cx);
-    idx += V.out_first[it];
-    sample_rgb[3 * idx] = acc.x;
-    sample_rgb[3 * idx + 1] = acc.y;
-    sample_rgb[3 * idx + 2] = acc.z;
-  }
-}
-
 // AA average per pixel and spectrum_to_rgb8_reinhard (R:3908-3921, R:5229-5239).
 __global__ void trace_pixels_kernel(const float* __restrict__ sample_rgb, uint32_t n_pixels, uint32_t aa,
                                     float* __restrict__ rgb_out, uint8_t* __restrict__ rgb8_out) {

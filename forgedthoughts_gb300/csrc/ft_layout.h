@@ -33,5 +33,9 @@ constexpr int kMaxGenericPointStack = 8;
 constexpr int kMaxUrDepth = 40;
 constexpr int kUrNear = 8;       // near-set capacity of the union_round tree path
 constexpr int kUrBvhLeafSize = 4;
+// Iteration cap of the device's stack walks over trees (BVHs, union_round
+// inner nodes): a valid tree pops each node once, so this only ends a walk
+// over a corrupted one.
+constexpr int kMaxWalk = 1 << 20;
 
 }  // namespace ftgpu

@@ -119,6 +119,7 @@ struct ft_scene {
   WShadow* wf_shadows = nullptr;
   uint64_t wf_shadows_cap = 0;
   unsigned long long* wf_counters = nullptr;  // job counts (2), shadow count, overflow flag
+  uint32_t last_launches = 0;  // kernels launched by the last ft_render_depth / ft_render_trace
   std::mutex mu;
 };
 
@@ -291,7 +292,7 @@ ft_status launch_depth(ft_scene* sc, const RayParams& P, cudaStream_t st, bool s
   if (stats)
     FT_CUDA_TRY(cudaMemsetAsync(sc->d_stats, 0, 16 * sizeof(unsigned long long), st), "cudaMemsetAsync(stats)");
   else
-    FT_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st), "cudaMemsetAsync(counter)");
+    FT_CUDA_TRY(cudaMemsetAsync(counter, 0, 2 * sizeof(unsigned long long), st), "cudaMemsetAsync(counter)");
   const DevBricks& B = sc->bricks;
   if (!stats && sc->jit_depth[bricks ? 1 : 0]) {
     // run-time compiled kernel: same signature as march_depth_persistent
@@ -425,6 +426,18 @@ struct ft_batch {
   cudaGraphExec_t exec = nullptr;
   ft_batch_tuning tuning{8, 8, 8, 0.0f};
   std::mutex mu;
+  // Wavefront queues of the trace items (sized per tuning: tiles pad the
+  // work items), their counters (job counts x2, shadow count, overflow
+  // flag), the bounce levels captured and the most light samples of a scene.
+  WJob* wf_jobs[2] = {nullptr, nullptr};
+  uint64_t wf_jobs_cap[2] = {0, 0};
+  WHit* wf_hits = nullptr;
+  uint64_t wf_hits_cap = 0;
+  WShadow* wf_shadows = nullptr;
+  uint64_t wf_shadows_cap = 0;
+  unsigned long long* wf_counters = nullptr;
+  uint32_t wf_levels = 0;
+  uint32_t wf_light_samples = 1;
 };
 
 namespace {
@@ -437,6 +450,28 @@ void free_part(BatchPart& p) {
   cudaFree(p.d_out_first);
   cudaFree(p.d_max_depth);
   p = BatchPart{};
+}
+
+template <class T>
+ft_status grow(T** buf, uint64_t* cap, uint64_t want, const char* what) {
+  if (want <= *cap) return FT_OK;
+  cudaFree(*buf);
+  *buf = nullptr;
+  *cap = 0;
+  uint64_t n = want + want / 4 + 1024;
+  FT_CUDA_TRY(cudaMalloc(buf, n * sizeof(T)), what);
+  *cap = n;
+  return FT_OK;
+}
+
+// Queue capacity of bounce level k of a batch wavefront over n work items: a
+// job pushes at most four (two materials x reflect / refract), so n * 4^k is
+// exact; it is capped at 16 n (Whitted queues shrink fast: diffuse hits push
+// nothing) and an overflow is reported when the results are read.
+uint64_t level_capacity(uint64_t n, uint32_t k) {
+  uint64_t f = 1;
+  for (uint32_t i = 0; i < k && f < 16; ++i) f *= 4;
+  return n * std::min<uint64_t>(f, 16);
 }
 
 // Per-item parameters and work prefix sums for the current tuning; uploads
@@ -462,6 +497,22 @@ ft_status batch_apply_tuning(ft_batch* b) {
                            cudaMemcpyHostToDevice),
                 "upload batch work offsets");
   }
+  if (!b->part[1].items.empty()) {
+    const uint64_t n = b->part[1].n_rays;
+    uint64_t want[2] = {0, 0}, hits = 0;
+    for (uint32_t k = 0; k < b->wf_levels; ++k) {
+      uint64_t c = level_capacity(n, k);
+      want[k & 1] = std::max(want[k & 1], c);
+      hits = std::max(hits, c);
+    }
+    for (int q = 0; q < 2; ++q)
+      if (ft_status s = grow(&b->wf_jobs[q], &b->wf_jobs_cap[q], std::max<uint64_t>(want[q], 1), "cudaMalloc(batch ray jobs)"))
+        return s;
+    if (ft_status s = grow(&b->wf_hits, &b->wf_hits_cap, hits, "cudaMalloc(batch hits)")) return s;
+    if (ft_status s = grow(&b->wf_shadows, &b->wf_shadows_cap, 2 * hits * b->wf_light_samples,
+                           "cudaMalloc(batch shadow jobs)"))
+      return s;
+  }
   if (b->exec) {
     cudaGraphExecDestroy(b->exec);
     b->exec = nullptr;
@@ -479,8 +530,28 @@ ft_status batch_apply_tuning(ft_batch* b) {
       march_depth_persistent<false, false, true><<<D.blocks, 128, 0, b->stream>>>(
           DevScene{}, RayParams{}, DevBricks{}, D.view(), b->d_t, b->d_mask, nullptr, nullptr, nullptr, b->d_counters);
   }
-  if (!T.items.empty())
-    trace_batch_kernel<<<T.blocks, 128, 0, b->stream>>>(T.view(), T.d_max_depth, b->d_srgb, b->d_counters + 1);
+  if (!T.items.empty()) {
+    // the Whitted items as a wavefront: one march, shade and shadow kernel
+    // per bounce level over every item's queue (counts stay on the device)
+    unsigned long long* c = b->wf_counters;
+    const BatchView V = T.view();
+    cudaMemsetAsync(b->d_srgb, 0, T.n_samples * 3 * sizeof(float), b->stream);
+    cudaMemsetAsync(c, 0, 4 * sizeof(unsigned long long), b->stream);
+    const unsigned grid = static_cast<unsigned>(T.blocks);
+    wf_primary_batch_kernel<<<grid, 128, 0, b->stream>>>(V, b->wf_jobs[0], c);
+    for (uint32_t level = 0; level < b->wf_levels; ++level) {
+      const int cur = static_cast<int>(level & 1), nxt = 1 - cur;
+      cudaMemsetAsync(c + nxt, 0, sizeof(unsigned long long), b->stream);
+      cudaMemsetAsync(c + 2, 0, sizeof(unsigned long long), b->stream);
+      wf_march_batch_kernel<<<grid, 128, 0, b->stream>>>(V, b->wf_jobs[cur], c + cur, b->wf_jobs_cap[cur],
+                                                         b->wf_hits, b->d_srgb);
+      WQueues Q{b->d_srgb, b->wf_jobs[nxt], c + nxt, b->wf_jobs_cap[nxt], b->wf_shadows, c + 2,
+                b->wf_shadows_cap, reinterpret_cast<unsigned int*>(c + 3), 0};
+      wf_shade_batch_kernel<<<grid, 128, 0, b->stream>>>(V, T.d_max_depth, b->wf_jobs[cur], c + cur,
+                                                         b->wf_jobs_cap[cur], b->wf_hits, Q);
+      wf_shadow_batch_kernel<<<grid, 128, 0, b->stream>>>(V, b->wf_shadows, c + 2, b->wf_shadows_cap, b->d_srgb);
+    }
+  }
   {
     uint64_t want = (b->n_pixels + 255) / 256;
     unsigned grid = static_cast<unsigned>(std::max<uint64_t>(1, std::min<uint64_t>(want, 152ull * 64)));
@@ -497,6 +568,32 @@ ft_status batch_apply_tuning(ft_batch* b) {
   return FT_OK;
 }
 
+// The persistent march's self-check slot (next to its work counter): bits of
+// the phases in which a ray exceeded its iteration limit, bit 8 when a warp
+// exceeded its time limit.
+ft_status march_check(unsigned long long flags) {
+  if (!flags) return FT_OK;
+  return ftcommon::fail(FT_ERR_TIMEOUT, "depth march gave up (self-check flags 0x" + [&] {
+    char buf[32];
+    std::snprintf(buf, sizeof(buf), "%llx", flags);
+    return std::string(buf);
+  }() + "): a ray exceeded max_steps + 64 iterations or a warp ran for over 20 s");
+}
+
+// After the batch's work has completed: fail if a Whitted queue overflowed or
+// the depth march gave up.
+ft_status batch_overflow(ft_batch* b) {
+  unsigned long long march = 0;
+  FT_CUDA_TRY(cudaMemcpy(&march, b->d_counters + 1, sizeof(march), cudaMemcpyDeviceToHost), "batch march flags");
+  if (ft_status s = march_check(march)) return s;
+  if (!b->wf_counters) return FT_OK;
+  unsigned long long flag = 0;
+  FT_CUDA_TRY(cudaMemcpy(&flag, b->wf_counters + 3, sizeof(flag), cudaMemcpyDeviceToHost), "batch queue flags");
+  if (flag) return ftcommon::fail(FT_ERR_CUDA, "batch Whitted queue overflow (more than 16 rays per primary sample "
+                                               "at one bounce level)");
+  return FT_OK;
+}
+
 ft_status check_tuning(const ft_batch_tuning& t) {
   if (t.tile_w < 1 || t.tile_w > 64 || t.tile_h < 1 || t.tile_h > 64 || t.refill < 1 || t.refill > 32)
     return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "tile sides must be 1..64 and refill 1..32");
@@ -504,24 +601,14 @@ ft_status check_tuning(const ft_batch_tuning& t) {
 }
 
 
-template <class T>
-ft_status grow(T** buf, uint64_t* cap, uint64_t want, const char* what) {
-  if (want <= *cap) return FT_OK;
-  cudaFree(*buf);
-  *buf = nullptr;
-  *cap = 0;
-  uint64_t n = want + want / 4 + 1024;
-  FT_CUDA_TRY(cudaMalloc(buf, n * sizeof(T)), what);
-  *cap = n;
-  return FT_OK;
-}
 
 // Whitted trace of one frame as a wavefront: per bounce level one march, one
 // shade and one shadow kernel over queues (ft_wavefront.cuh).  Radiance per
 // sample lands in sc->d_normal.  Queue sizes are read back once per level to
 // size the next one; the capacities are exact upper bounds (a job pushes at
 // most two materials x two rays, and two materials x the light samples).
-ft_status trace_wavefront(ft_scene* sc, const RayParams& P, uint32_t max_depth, cudaStream_t st) {
+ft_status trace_wavefront(ft_scene* sc, const RayParams& P, uint32_t max_depth, cudaStream_t st,
+                          uint32_t* launches) {
   const ftgpu::SceneImage& im = sc->img;
   uint64_t light_samples = 0;
   for (const ft_light& L : im.lights) light_samples += L.kind == FT_LIGHT_SPHERE ? std::max(L.samples, 1u) : 1u;
@@ -537,6 +624,7 @@ ft_status trace_wavefront(ft_scene* sc, const RayParams& P, uint32_t max_depth, 
   FT_CUDA_TRY(cudaMemcpyAsync(c, &first, sizeof(first), cudaMemcpyHostToDevice, st), "queue count");
   wf_primary_kernel<<<static_cast<unsigned>((n + 127) / 128), 128, 0, st>>>(P, sc->wf_jobs[0]);
   FT_CUDA_TRY(cudaGetLastError(), "wf_primary_kernel launch");
+  *launches = 1;
   int sms = 0;
   FT_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, sc->device), "sm count");
   const void* k_march = sc->jit_wf[0] ? reinterpret_cast<const void*>(sc->jit_wf[0])
@@ -562,13 +650,15 @@ ft_status trace_wavefront(ft_scene* sc, const RayParams& P, uint32_t max_depth, 
     const WJob* jobs = sc->wf_jobs[cur];
     const unsigned long long* count = c + cur;
     WHit* hits = sc->wf_hits;
-    void* margs[] = {&S, &PP, &jobs, &count, &hits, &radiance};
+    unsigned long long jcap = sc->wf_jobs_cap[cur];
+    void* margs[] = {&S, &PP, &jobs, &count, &jcap, &hits, &radiance};
     FT_CUDA_TRY(cudaLaunchKernel(k_march, dim3(grid), dim3(128), margs, 0, st), "wavefront march launch");
     WQueues Q{radiance, sc->wf_jobs[nxt], c + nxt, sc->wf_jobs_cap[nxt], sc->wf_shadows, c + 2,
               sc->wf_shadows_cap, reinterpret_cast<unsigned int*>(c + 3), max_depth};
     const WHit* chits = hits;
-    void* sargs[] = {&S, &PP, &jobs, &count, &chits, &Q};
+    void* sargs[] = {&S, &PP, &jobs, &count, &jcap, &chits, &Q};
     FT_CUDA_TRY(cudaLaunchKernel(k_shade, dim3(grid), dim3(128), sargs, 0, st), "wavefront shade launch");
+    *launches += 2;
     unsigned long long h[2] = {0, 0};
     FT_CUDA_TRY(cudaMemcpyAsync(&h[0], c + nxt, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st), "queue count");
     FT_CUDA_TRY(cudaMemcpyAsync(&h[1], c + 2, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st), "queue count");
@@ -578,10 +668,12 @@ ft_status trace_wavefront(ft_scene* sc, const RayParams& P, uint32_t max_depth, 
                                                                                      static_cast<uint64_t>(sms) * 16)));
       const WShadow* shadows = sc->wf_shadows;
       const unsigned long long* scount = c + 2;
-      void* hargs[] = {&S, &PP, &shadows, &scount, &radiance};
+      unsigned long long scap = sc->wf_shadows_cap;
+      void* hargs[] = {&S, &PP, &shadows, &scount, &scap, &radiance};
       FT_CUDA_TRY(cudaLaunchKernel(k_shadow, dim3(sgrid), dim3(128), hargs, 0, st), "wavefront shadow launch");
+      *launches += 1;
     }
-    n = h[0];
+    n = std::min<uint64_t>(h[0], sc->wf_jobs_cap[nxt]);  // an overflowed queue holds its capacity
     cur = nxt;
   }
   unsigned long long overflow = 0;
@@ -652,6 +744,12 @@ ft_status ft_scene_build_info(const ft_scene_desc* desc, ft_build_info* info) {
   return FT_OK;
 }
 
+ft_status ft_scene_last_launches(const ft_scene* sc, uint32_t* launches) {
+  if (!sc || !launches) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "scene and launches must be non-null");
+  *launches = sc->last_launches;
+  return FT_OK;
+}
+
 ft_status ft_scene_device_bytes(const ft_scene* sc, uint64_t* bytes) {
   if (!sc || !bytes) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "scene and bytes must be non-null");
   *bytes = sc->arena_bytes + sc->brick_bytes;
@@ -703,6 +801,7 @@ ft_status ft_render_depth(ft_scene* sc, const ft_render_options* options, ft_acc
   float* nrm = normal_out ? (dev_ptrs ? normal_out : sc->d_normal) : nullptr;
   const bool bricks = (flags & FT_FLAG_FP16_BRICKS) != 0;
   if (ft_status s = launch_depth(sc, P, st, false, bricks, t, mask, mat, nrm)) return s;
+  sc->last_launches = rgb8_out ? 2 : 1;
   if (rgb8_out) {
     uint8_t* rgb = dev_ptrs ? rgb8_out : sc->d_rgb;
     uint32_t np = static_cast<uint32_t>(pixels);
@@ -721,7 +820,11 @@ ft_status ft_render_depth(ft_scene* sc, const ft_render_options* options, ft_acc
       FT_CUDA_TRY(cudaMemcpyAsync(normal_out, nrm, items * 3 * sizeof(float), cudaMemcpyDeviceToHost, st),
                   "copy normal");
   }
+  unsigned long long march_flags = 0;
+  FT_CUDA_TRY(cudaMemcpyAsync(&march_flags, sc->d_stats + 9, sizeof(march_flags), cudaMemcpyDeviceToHost, st),
+              "march flags");
   FT_CUDA_TRY(cudaStreamSynchronize(st), "render");
+  if (ft_status s = march_check(march_flags)) return s;
   ftcommon::clear_last_error();
   return FT_OK;
 }
@@ -775,12 +878,14 @@ ft_status ft_render_trace(ft_scene* sc, const ft_render_options* options, ft_acc
   RayParams P = make_params(sc, *options, aa);
   uint64_t blocks = (P.n_items + 127) / 128;
   if (blocks > 0x7fffffffull) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "image too large");
-  if (ft_status s = trace_wavefront(sc, P, depth, st)) return s;
+  uint32_t launches = 0;
+  if (ft_status s = trace_wavefront(sc, P, depth, st, &launches)) return s;
   float* rgbf = rgb_out ? (dev_ptrs ? rgb_out : sc->d_rgbf) : nullptr;
   uint8_t* rgb8 = rgb8_out ? (dev_ptrs ? rgb8_out : sc->d_rgb) : nullptr;
   uint32_t np = static_cast<uint32_t>(pixels);
   trace_pixels_kernel<<<(np + 255) / 256, 256, 0, st>>>(sc->d_normal, np, aa, rgbf, rgb8);
   FT_CUDA_TRY(cudaGetLastError(), "trace_pixels_kernel launch");
+  sc->last_launches = launches + 1;
   if (!dev_ptrs) {
     if (rgb_out) FT_CUDA_TRY(cudaMemcpyAsync(rgb_out, rgbf, pixels * 3 * sizeof(float), cudaMemcpyDeviceToHost, st),
                              "copy rgb");
@@ -834,9 +939,10 @@ ft_status ft_render_depth_stats(ft_scene* sc, const ft_render_options* options, 
   RayParams P = make_params(sc, *options, aa);
   const bool bricks = (flags & FT_FLAG_FP16_BRICKS) != 0;
   if (ft_status s = launch_depth(sc, P, nullptr, true, bricks, sc->d_t, sc->d_mask, nullptr, sc->d_normal)) return s;
-  unsigned long long h[8] = {0};
+  unsigned long long h[10] = {0};
   FT_CUDA_TRY(cudaMemcpy(h, sc->d_stats, sizeof(h), cudaMemcpyDeviceToHost), "copy stats");
   std::memset(stats, 0, sizeof(*stats));
+  if (ft_status st = march_check(h[9])) return st;
   stats->rays = pixels * aa;
   stats->far_steps = h[5];
   stats->brick_fetches = h[6];
@@ -921,6 +1027,35 @@ ft_status ft_scene_build_bricks(ft_scene* sc, const ft_brick_options* options, f
   // bound of a 1-Lipschitz brick would hand over again
   B.band_exit = 2.0f * (band + safety * h * 1.7320508f);
   for (int a = 0; a < 3; ++a) B.rmax[a] = G.rmin[a] + bs * static_cast<float>(G.dims[a]);
+  B.free_far = (o.flags & FT_BRICK_FREE_FAR_STEPS) ? 1 : 0;
+  // Outside the region the cached leaves are at least the distance to its
+  // box away when each lies in its own box: primitives and union_round trees
+  // (a round blend can bulge out of its operands' boxes by 0.3 r, hence the
+  // margin), not hooked or modified leaves.
+  B.outside_ok = 1;
+  float r_max = 0.0f;
+  for (const ftgpu::HostUrTree& t : im.urtrees) r_max = std::max(r_max, t.r);
+  for (size_t j = 0; j < im.leaves.size(); ++j) {
+    if (std::find(exact.begin(), exact.end(), static_cast<int>(j)) != exact.end()) continue;
+    int kind = im.leaves[j].kind;
+    if (kind != ftgpu::kLeafPrim && kind != ftgpu::kLeafUrTree) B.outside_ok = 0;
+  }
+  B.outside_margin = std::max(band, r_max);
+  // A single exact leaf that is an axis-aligned box with sharp edges and no
+  // shell: its distance above the top face is the height over that face.
+  B.plane_leaf = -1;
+  if (exact.size() == 1 && im.leaves[exact[0]].kind == ftgpu::kLeafPrim) {
+    const ftgpu::HostNode& n = im.nodes[im.leaves[exact[0]].node];
+    if (n.kind == FT_NODE_BOX && !n.has_rot && n.f[3] == 0.0f && n.f[4] == 0.0f && n.program < 0) {
+      B.plane_leaf = exact[0];
+      B.plane_obj = n.object_id;
+      B.plane_top = n.c[1] + n.f[1];
+      B.plane_lo[0] = n.c[0] - n.f[0];
+      B.plane_hi[0] = n.c[0] + n.f[0];
+      B.plane_lo[1] = n.c[2] - n.f[2];
+      B.plane_hi[1] = n.c[2] + n.f[2];
+    }
+  }
 
   DeviceTemps tmp;
   float* lattice = nullptr;
@@ -1104,7 +1239,14 @@ ft_status ft_batch_create(const ft_batch_item* items, uint32_t n, uint32_t flags
         FT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, march_depth_persistent<false, false, true>,
                                                                   128, 0), "occupancy");
     } else {
-      FT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_batch_kernel, 128, 0), "occupancy");
+      per_sm = 16;  // grid-stride wavefront kernels
+      for (uint32_t it : part.items) {
+        b->wf_levels = std::max(b->wf_levels, std::max(b->items[it].max_depth, 1u));
+        uint32_t ls = 0;
+        for (const ft_light& L : b->items[it].scene->img.lights)
+          ls += L.kind == FT_LIGHT_SPHERE ? std::max(L.samples, 1u) : 1u;
+        b->wf_light_samples = std::max(b->wf_light_samples, ls);
+      }
     }
     part.blocks = std::max(1, sms * std::max(per_sm, 1));
   }
@@ -1118,6 +1260,9 @@ ft_status ft_batch_create(const ft_batch_item* items, uint32_t n, uint32_t flags
   FT_CUDA_TRY(cudaMalloc(&b->d_rgbf, pix_total * 3 * sizeof(float)), "cudaMalloc(batch rgb)");
   FT_CUDA_TRY(cudaMalloc(&b->d_rgb8, pix_total * 3), "cudaMalloc(batch rgb8)");
   FT_CUDA_TRY(cudaMalloc(&b->d_counters, 2 * sizeof(unsigned long long)), "cudaMalloc(batch counters)");
+  FT_CUDA_TRY(cudaMalloc(&b->wf_counters, 4 * sizeof(unsigned long long)), "cudaMalloc(batch queue counters)");
+  FT_CUDA_TRY(cudaMemset(b->wf_counters, 0, 4 * sizeof(unsigned long long)), "cudaMemset(batch queue counters)");
+  if (samples[1] >= kNoSample) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "too many Whitted samples in one batch");
   if (ft_status st = batch_apply_tuning(b)) return st;
   *out = guard.release();
   ftcommon::clear_last_error();
@@ -1147,11 +1292,13 @@ ft_status ft_batch_autotune(ft_batch* b, ft_batch_tuning* best) {
   FT_CUDA_TRY(cudaEventCreate(&e1), "cudaEventCreate");
   ft_batch_tuning top{8, 8, 8, 1e30f};
   ft_status status = FT_OK;
+  bool warm = false;
   for (const auto& tl : tiles) {
     for (uint32_t rf : refills) {
       b->tuning = ft_batch_tuning{tl[0], tl[1], rf, 0.0f};
       if ((status = batch_apply_tuning(b)) != FT_OK) break;
-      cudaGraphLaunch(b->exec, b->stream);  // warm-up
+      if (!warm) cudaGraphLaunch(b->exec, b->stream);  // one warm-up (first touch of the queues)
+      warm = true;
       cudaEventRecord(e0, b->stream);
       cudaGraphLaunch(b->exec, b->stream);
       cudaEventRecord(e1, b->stream);
@@ -1162,6 +1309,7 @@ ft_status ft_batch_autotune(ft_batch* b, ft_batch_tuning* best) {
         status = ftcommon::fail(FT_ERR_CUDA, cuda_msg(e, "batch autotune"));
         break;
       }
+      if ((status = batch_overflow(b)) != FT_OK) break;
       if (ms < top.ms) top = ft_batch_tuning{tl[0], tl[1], rf, ms};
     }
     if (status != FT_OK) break;
@@ -1192,6 +1340,7 @@ ft_status ft_batch_read(ft_batch* b, uint32_t item, float* t_out, uint8_t* mask_
   std::lock_guard<std::mutex> lock(b->mu);
   FT_CUDA_TRY(cudaSetDevice(b->device), "cudaSetDevice");
   FT_CUDA_TRY(cudaDeviceSynchronize(), "batch");
+  if (ft_status s = batch_overflow(b)) return s;
   const ft_batch_item& it = b->items[item];
   const BatchPixItem& pi = b->pix[item];
   uint64_t px = static_cast<uint64_t>(it.options.width) * it.options.height;
@@ -1231,6 +1380,11 @@ void ft_batch_destroy(ft_batch* b) {
   cudaFree(b->d_rgbf);
   cudaFree(b->d_rgb8);
   cudaFree(b->d_counters);
+  cudaFree(b->wf_jobs[0]);
+  cudaFree(b->wf_jobs[1]);
+  cudaFree(b->wf_hits);
+  cudaFree(b->wf_shadows);
+  cudaFree(b->wf_counters);
   if (b->stream) cudaStreamDestroy(b->stream);
   cudaSetDevice(prev);
   delete b;

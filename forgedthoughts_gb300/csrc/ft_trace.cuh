@@ -286,7 +286,7 @@ __device__ __noinline__ void resolve_generic(const DevScene& S, int root, F3 p, 
   stage[0] = 0;
   out->ok = false;
   out->split = false;
-  while (top >= 0) {
+  for (int walk = 0; top >= 0 && walk < ftgpu::kMaxWalk; ++walk) {  // each node is visited once
     int ni = node_stack[top];
     const DevNode& n = S.nodes[ni];
     bool is_prim = n.kind <= FT_NODE_EXTRUDE_POLYGON;
@@ -374,7 +374,7 @@ __device__ bool ur_gather(const DevScene& S, const DevUrTree& t, F3 p, float rea
   int sp = 0;
   *n = 0;
   stack[sp++] = t.bvh_root;
-  while (sp > 0) {
+  for (int walk = 0; sp > 0 && walk < ftgpu::kMaxWalk; ++walk) {  // a tree walk pops each node once
     const DevUrBvh& bn = S.ur_bvh[stack[--sp]];
     if (node_lb(p, bn.bmin, bn.bmax) >= reach) continue;
     if (bn.prim_count > 0) {
@@ -426,7 +426,7 @@ __device__ float ur_subtree_value(const DevScene& S, const DevUrTree& t, int c, 
   int fp = 0;
   fr[0].inner = c;
   fr[0].stage = 0;
-  for (;;) {
+  for (int walk = 0; walk < ftgpu::kMaxWalk; ++walk) {  // each inner node is opened once
     VF& F = fr[fp];
     if (F.stage < 2) {
       int ch = S.ur_inner[F.inner].child[F.stage];
@@ -452,6 +452,7 @@ __device__ float ur_subtree_value(const DevScene& S, const DevUrTree& t, int c, 
     --fp;
     fr[fp].v[fr[fp].stage - 1] = v;
   }
+  return kInf;  // only a corrupted tree gets here
 }
 
 struct NEntry {
@@ -507,7 +508,7 @@ __device__ __noinline__ bool resolve_urtree_reach(const DevScene& S, const DevUr
     return true;
   };
   if (!open(0, t.inner_root)) return false;
-  for (;;) {
+  for (int walk = 0; walk < ftgpu::kMaxWalk; ++walk) {  // each inner node is opened once
     Frame& F = fr[fp];
     if (F.stage < 2) {
       bool use = F.stage == 0 ? F.useL : F.useR;
@@ -554,6 +555,8 @@ __device__ __noinline__ bool resolve_urtree_reach(const DevScene& S, const DevUr
     --fp;
     fr[fp].slot[fr[fp].stage - 1] = res;
   }
+  *need = -1.0f;  // only a corrupted tree gets here
+  return false;
 }
 
 __device__ void resolve_urtree(const DevScene& S, const DevUrTree& t, F3 p, Resolved* out) {
@@ -598,7 +601,7 @@ __device__ float scene_lower_bound(const DevScene& S, F3 p) {
   stack[0] = S.bvh_root;
   slb[0] = node_lb(p, S.bvh[S.bvh_root].bmin, S.bvh[S.bvh_root].bmax);
   sp = 1;
-  while (sp > 0) {
+  for (int walk = 0; sp > 0 && walk < ftgpu::kMaxWalk; ++walk) {  // a tree walk pops each node once
     --sp;
     if (slb[sp] > best) continue;
     const DevBvhNode& n = S.bvh[stack[sp]];

@@ -318,6 +318,12 @@ ft_status ft_scene_build_info(const ft_scene_desc* desc, ft_build_info* info);
 /* Bytes of scene data the last ft_scene_create copied host -> device. */
 ft_status ft_scene_device_bytes(const ft_scene* scene, uint64_t* bytes);
 
+/* Kernels launched by the scene's last ft_render_depth or ft_render_trace
+ * call (the Whitted trace launches a data-dependent number: three per bounce
+ * level that still holds rays).  No counterpart in the reference
+ * (measurement). */
+ft_status ft_scene_last_launches(const ft_scene* scene, uint32_t* launches);
+
 /* Depth preview: `render_depth_png_with_accel` (R:1139-1156) /
  * `render_preview_progressive_with_accel` (R:1238-1277) without the PNG step.
  * One primary ray per (pixel, AA offset) with the reference's deterministic
@@ -416,24 +422,37 @@ ft_status ft_render_trace_stats(ft_scene* scene, const ft_render_options* option
  * distance_post pair applies its transform twice), store no bound: the march
  * is exact inside them.
  *
- * ft_render_depth with FT_FLAG_FP16_BRICKS marches on that bound (large
- * leaves evaluated exactly; exact march outside the region) while it is at
- * least `band`, stepping by the
- * bound minus band/2, then continues with the exact FP32 march of the plain
- * method (same step rule), returning to the far field when the exact distance
- * exceeds band_exit.  At the hit, secant steps on the exact distance between
- * the last two exact points find the eps-shell crossing (each verified by an
- * exact evaluation); the normal is the plain method's six-tap estimate.
- * Build once per scene; rebuilding replaces the cache.  Synchronous on the
- * legacy default stream. */
+ * ft_render_depth with FT_FLAG_FP16_BRICKS (default, counted form) takes the
+ * plain method's samples, so it ends on the same rays as the plain march,
+ * including those the plain march gives up on at its step limit.  When the
+ * only large leaf is an axis-aligned box (a ground), the nearest leaf at a
+ * sample is that box, the ray descends onto its top face, and the cached
+ * leaves are farther than the face along the ray (one fetch; outside the
+ * brick region the distance to the region's box less the largest blend
+ * radius, for scenes without hooked or modified leaves), the rest of the
+ * approach is the plain march towards a plane: its step count is computed in
+ * closed form, and the march jumps to the eps-shell crossing.
+ * With FT_BRICK_FREE_FAR_STEPS it instead marches on the bound while it is at
+ * least `band`, stepping by the bound minus band/2, then continues with the
+ * exact FP32 march of the plain method (same step rule), returning to the far
+ * field when the exact distance exceeds band_exit.  In both forms secant
+ * steps on the exact distance between the last two exact points find the
+ * eps-shell crossing at a hit (each verified by an exact evaluation), and the
+ * normal is the plain method's six-tap estimate.  Build once per scene;
+ * rebuilding replaces the cache.  Synchronous on the legacy default stream. */
 typedef struct ft_brick_options {
   float voxel_size;             /* lattice spacing; 0 = 0.02 */
   float band;                   /* far-field threshold; 0 = 10 voxels */
   float safety;                 /* factor on the error bound; 0 = 1.25 */
   uint32_t max_lattice_points;  /* refuse larger lattices; 0 = 2^29 */
   uint32_t far_steps_per_pass;  /* far-field steps a lane takes per pass of its warp; 0 = 4 */
-  uint32_t reserved;
+  uint32_t flags;               /* FT_BRICK_* */
 } ft_brick_options;
+
+/* March the far field with free steps (bound minus band/2, each counted as one
+ * step of the plain method) instead of the default counted form below; on
+ * rays the plain march gives up on (its step limit) the two can disagree. */
+#define FT_BRICK_FREE_FAR_STEPS 1u
 
 typedef struct ft_brick_info {
   float region_min[3];
@@ -463,13 +482,17 @@ ft_status ft_scene_brick_bounds(ft_scene* scene, const float* points, uint32_t n
  *
  * The depth items run in one persistent march kernel whose warps take rays of
  * any item from a global counter (a lane keeps its item's scene, parameters
- * and brick cache), the trace items in one persistent trace kernel, and one
- * pixel kernel writes every item's image; the three are captured once into a
- * CUDA graph.  Work items are tiles of tile_w x tile_h pixels (x AA
- * samples); a warp of the depth march refills its idle lanes when at least
- * `refill` of them are idle.  ft_batch_autotune times the candidate tiles
- * (8x8, 16x8, 32x8) and refill thresholds (4, 8, 16) on this batch and keeps
- * the fastest.
+ * and brick cache).  The trace items run as one wavefront over all of them:
+ * per bounce level (up to the largest max_depth) a march, a shade and a
+ * shadow kernel over shared queues whose counts stay on the device; a level
+ * may hold at most 16 rays per primary sample (ft_batch_read and
+ * ft_batch_autotune report an overflow).  One pixel kernel writes every
+ * item's image; everything is captured once into a CUDA graph.  Work items
+ * are tiles of tile_w x tile_h pixels (x AA samples); a warp of the depth
+ * march refills its idle lanes when at least `refill` of them are idle.
+ * ft_batch_autotune times the candidate tiles (8x8, 16x8, 32x8) and refill
+ * thresholds (4, 8, 16) on this batch, one launch each after one warm-up, and
+ * keeps the fastest.
  * ------------------------------------------------------------------------- */
 typedef struct ft_batch ft_batch;
 

@@ -153,3 +153,58 @@ def test_brick_stats_count_far_steps():
     assert s_fp16.far_steps > 0 and s_fp16.brick_fetches > 0
     # the precision form replaces most exact evaluations by far-field steps
     assert s_fp16.distance_evals < s_plain.distance_evals
+
+
+def _limited(max_steps):
+    import dataclasses
+
+    w = workloads.union_round_field(width=480, height=270, aa=1)
+    return w, dataclasses.replace(w.options, max_steps=max_steps)
+
+
+def test_counted_form_keeps_the_plain_step_limit():
+    """With a step limit of 96 the plain march gives up on the grazing ground
+    rays (a band below the horizon).  The counted brick form follows the plain
+    samples and counts the ground descent in closed form, so it gives up on
+    the same rays and agrees with the plain march and the FP64 oracle."""
+    w, opts = _limited(96)
+    st = ft.parse_and_eval(w.source)
+    st.gpu().build_bricks()
+    plain = ft.render_depth(st, opts, w.accel, 1)
+    full = ft.render_depth(st, w.options, w.accel, 1)
+    assert plain.mask.mean() < full.mask.mean() - 0.01  # the limit bites
+    fp16 = ft.render_depth(st, opts, w.accel, 1, fp16_bricks=True)
+    r = compare_depth(fp16.t, fp16.mask, plain.t, plain.mask)
+    assert r["mask_agreement"] >= MASK_AGREEMENT and r["depth_within_tol"] >= MASK_AGREEMENT, r
+    t64, m64, _, _, _ = oracle.render_depth(st, opts, int(w.accel), 1, 64)
+    r64 = compare_depth(fp16.t, fp16.mask, t64, m64)
+    p64 = compare_depth(plain.t, plain.mask, t64, m64)
+    assert r64["mask_agreement"] >= min(MASK_AGREEMENT, p64["mask_agreement"]), (r64, p64)
+    assert r64["depth_within_tol"] >= min(MASK_AGREEMENT, p64["depth_within_tol"]), (r64, p64)
+
+
+def test_counted_form_skips_most_evaluations():
+    """On the 512-primitive field the ground descents taken in closed form
+    (and secant hit refinement) leave far fewer evaluations than the plain
+    march, and the free far-field form keeps working beside it."""
+    import ctypes
+
+    from forgedthoughts_gb300 import _native
+
+    w = workloads.union_round_field(width=320, height=180, aa=1)
+    st = ft.parse_and_eval(w.source)
+    g = st.gpu()
+    g.build_bricks()
+    lib = _native.lib()
+    opts = w.options.to_c()
+    s_plain, s_fp16 = _native.RenderStatsC(), _native.RenderStatsC()
+    assert lib.ft_render_depth_stats(g.handle, ctypes.byref(opts), int(w.accel), 1, 0, ctypes.byref(s_plain)) == 0
+    assert lib.ft_render_depth_stats(g.handle, ctypes.byref(opts), int(w.accel), 1, _native.FT_FLAG_FP16_BRICKS,
+                                     ctypes.byref(s_fp16)) == 0
+    assert s_fp16.far_steps > 0  # ground descents taken in closed form
+    assert s_fp16.distance_evals < 0.75 * s_plain.distance_evals, (s_fp16.distance_evals, s_plain.distance_evals)
+    plain = ft.render_depth(st, w.options, w.accel, 1)
+    g.build_bricks(free_far_steps=True)
+    free = ft.render_depth(st, w.options, w.accel, 1, fp16_bricks=True)
+    r = compare_depth(free.t, free.mask, plain.t, plain.mask)
+    assert r["mask_agreement"] >= MASK_AGREEMENT and r["depth_within_tol"] >= MASK_AGREEMENT, r
