@@ -118,7 +118,9 @@ struct ft_scene {
   uint64_t wf_hits_cap = 0;
   WShadow* wf_shadows = nullptr;
   uint64_t wf_shadows_cap = 0;
-  unsigned long long* wf_counters = nullptr;  // job counts (2), shadow count, overflow flag
+  // job counts (2), shadow count, overflow flag, march and shadow work
+  // counters, self-check flags (kWfCounters)
+  unsigned long long* wf_counters = nullptr;
   uint32_t last_launches = 0;  // kernels launched by the last ft_render_depth / ft_render_trace
   std::mutex mu;
 };
@@ -438,6 +440,7 @@ struct ft_batch {
   unsigned long long* wf_counters = nullptr;
   uint32_t wf_levels = 0;
   uint32_t wf_light_samples = 1;
+  int sms = 1;
 };
 
 namespace {
@@ -536,20 +539,24 @@ ft_status batch_apply_tuning(ft_batch* b) {
     unsigned long long* c = b->wf_counters;
     const BatchView V = T.view();
     cudaMemsetAsync(b->d_srgb, 0, T.n_samples * 3 * sizeof(float), b->stream);
-    cudaMemsetAsync(c, 0, 4 * sizeof(unsigned long long), b->stream);
+    cudaMemsetAsync(c, 0, kWfCounters * sizeof(unsigned long long), b->stream);
     const unsigned grid = static_cast<unsigned>(T.blocks);
+    const unsigned mgrid = static_cast<unsigned>(b->sms * 6), sgrid = static_cast<unsigned>(b->sms * 8);
     wf_primary_batch_kernel<<<grid, 128, 0, b->stream>>>(V, b->wf_jobs[0], c);
     for (uint32_t level = 0; level < b->wf_levels; ++level) {
       const int cur = static_cast<int>(level & 1), nxt = 1 - cur;
       cudaMemsetAsync(c + nxt, 0, sizeof(unsigned long long), b->stream);
       cudaMemsetAsync(c + 2, 0, sizeof(unsigned long long), b->stream);
-      wf_march_batch_kernel<<<grid, 128, 0, b->stream>>>(V, b->wf_jobs[cur], c + cur, b->wf_jobs_cap[cur],
-                                                         b->wf_hits, b->d_srgb);
+      cudaMemsetAsync(c + 4, 0, 2 * sizeof(unsigned long long), b->stream);
+      wf_march_persistent<true><<<mgrid, 128, 0, b->stream>>>(DevScene{}, RayParams{}, V, b->wf_jobs[cur], c + cur,
+                                                              b->wf_jobs_cap[cur], b->wf_hits, b->d_srgb, c + 4,
+                                                              c + 6);
       WQueues Q{b->d_srgb, b->wf_jobs[nxt], c + nxt, b->wf_jobs_cap[nxt], b->wf_shadows, c + 2,
                 b->wf_shadows_cap, reinterpret_cast<unsigned int*>(c + 3), 0};
       wf_shade_batch_kernel<<<grid, 128, 0, b->stream>>>(V, T.d_max_depth, b->wf_jobs[cur], c + cur,
                                                          b->wf_jobs_cap[cur], b->wf_hits, Q);
-      wf_shadow_batch_kernel<<<grid, 128, 0, b->stream>>>(V, b->wf_shadows, c + 2, b->wf_shadows_cap, b->d_srgb);
+      wf_shadow_persistent<true><<<sgrid, 128, 0, b->stream>>>(DevScene{}, RayParams{}, V, b->wf_shadows, c + 2,
+                                                               b->wf_shadows_cap, b->d_srgb, c + 5, c + 6);
     }
   }
   {
@@ -573,7 +580,7 @@ ft_status batch_apply_tuning(ft_batch* b) {
 // exceeded its time limit.
 ft_status march_check(unsigned long long flags) {
   if (!flags) return FT_OK;
-  return ftcommon::fail(FT_ERR_TIMEOUT, "depth march gave up (self-check flags 0x" + [&] {
+  return ftcommon::fail(FT_ERR_TIMEOUT, "march gave up (self-check flags 0x" + [&] {
     char buf[32];
     std::snprintf(buf, sizeof(buf), "%llx", flags);
     return std::string(buf);
@@ -587,7 +594,9 @@ ft_status batch_overflow(ft_batch* b) {
   FT_CUDA_TRY(cudaMemcpy(&march, b->d_counters + 1, sizeof(march), cudaMemcpyDeviceToHost), "batch march flags");
   if (ft_status s = march_check(march)) return s;
   if (!b->wf_counters) return FT_OK;
-  unsigned long long flag = 0;
+  unsigned long long flag = 0, wf_march = 0;
+  FT_CUDA_TRY(cudaMemcpy(&wf_march, b->wf_counters + 6, sizeof(wf_march), cudaMemcpyDeviceToHost), "batch queue flags");
+  if (ft_status s = march_check(wf_march)) return s;
   FT_CUDA_TRY(cudaMemcpy(&flag, b->wf_counters + 3, sizeof(flag), cudaMemcpyDeviceToHost), "batch queue flags");
   if (flag) return ftcommon::fail(FT_ERR_CUDA, "batch Whitted queue overflow (more than 16 rays per primary sample "
                                                "at one bounce level)");
@@ -613,13 +622,14 @@ ft_status trace_wavefront(ft_scene* sc, const RayParams& P, uint32_t max_depth, 
   uint64_t light_samples = 0;
   for (const ft_light& L : im.lights) light_samples += L.kind == FT_LIGHT_SPHERE ? std::max(L.samples, 1u) : 1u;
   uint64_t n = P.n_items;  // work items, tile padding included
-  if (!sc->wf_counters) FT_CUDA_TRY(cudaMalloc(&sc->wf_counters, 4 * sizeof(unsigned long long)), "cudaMalloc(queues)");
+  if (!sc->wf_counters)
+    FT_CUDA_TRY(cudaMalloc(&sc->wf_counters, kWfCounters * sizeof(unsigned long long)), "cudaMalloc(queues)");
   if (ft_status s = grow(&sc->wf_jobs[0], &sc->wf_jobs_cap[0], n, "cudaMalloc(ray jobs)")) return s;
   unsigned long long* c = sc->wf_counters;
   float* radiance = sc->d_normal;
   const size_t samples = static_cast<size_t>(P.width) * P.height * P.aa;
   FT_CUDA_TRY(cudaMemsetAsync(radiance, 0, samples * 3 * sizeof(float), st), "cudaMemsetAsync(radiance)");
-  FT_CUDA_TRY(cudaMemsetAsync(c, 0, 4 * sizeof(unsigned long long), st), "cudaMemsetAsync(queues)");
+  FT_CUDA_TRY(cudaMemsetAsync(c, 0, kWfCounters * sizeof(unsigned long long), st), "cudaMemsetAsync(queues)");
   unsigned long long first = n;
   FT_CUDA_TRY(cudaMemcpyAsync(c, &first, sizeof(first), cudaMemcpyHostToDevice, st), "queue count");
   wf_primary_kernel<<<static_cast<unsigned>((n + 127) / 128), 128, 0, st>>>(P, sc->wf_jobs[0]);
@@ -628,13 +638,17 @@ ft_status trace_wavefront(ft_scene* sc, const RayParams& P, uint32_t max_depth, 
   int sms = 0;
   FT_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, sc->device), "sm count");
   const void* k_march = sc->jit_wf[0] ? reinterpret_cast<const void*>(sc->jit_wf[0])
-                                      : reinterpret_cast<const void*>(wf_march_kernel);
+                                      : reinterpret_cast<const void*>(wf_march_persistent<false>);
   const void* k_shade = sc->jit_wf[1] ? reinterpret_cast<const void*>(sc->jit_wf[1])
                                       : reinterpret_cast<const void*>(wf_shade_kernel);
   const void* k_shadow = sc->jit_wf[2] ? reinterpret_cast<const void*>(sc->jit_wf[2])
-                                       : reinterpret_cast<const void*>(wf_shadow_kernel);
+                                       : reinterpret_cast<const void*>(wf_shadow_persistent<false>);
   DevScene S = sc->dev;
   RayParams PP = P;
+  BatchView none{};
+  unsigned long long* march_next = c + 4;
+  unsigned long long* shadow_next = c + 5;
+  unsigned long long* flags = c + 6;
   int cur = 0;
   for (uint32_t level = 0; level < max_depth && n > 0; ++level) {
     const int nxt = 1 - cur;
@@ -651,8 +665,11 @@ ft_status trace_wavefront(ft_scene* sc, const RayParams& P, uint32_t max_depth, 
     const unsigned long long* count = c + cur;
     WHit* hits = sc->wf_hits;
     unsigned long long jcap = sc->wf_jobs_cap[cur];
-    void* margs[] = {&S, &PP, &jobs, &count, &jcap, &hits, &radiance};
-    FT_CUDA_TRY(cudaLaunchKernel(k_march, dim3(grid), dim3(128), margs, 0, st), "wavefront march launch");
+    FT_CUDA_TRY(cudaMemsetAsync(march_next, 0, sizeof(unsigned long long), st), "cudaMemsetAsync(queues)");
+    unsigned mgrid = static_cast<unsigned>(std::max<uint64_t>(1, std::min<uint64_t>((n + 127) / 128,
+                                                                                   static_cast<uint64_t>(sms) * 6)));
+    void* margs[] = {&S, &PP, &none, &jobs, &count, &jcap, &hits, &radiance, &march_next, &flags};
+    FT_CUDA_TRY(cudaLaunchKernel(k_march, dim3(mgrid), dim3(128), margs, 0, st), "wavefront march launch");
     WQueues Q{radiance, sc->wf_jobs[nxt], c + nxt, sc->wf_jobs_cap[nxt], sc->wf_shadows, c + 2,
               sc->wf_shadows_cap, reinterpret_cast<unsigned int*>(c + 3), max_depth};
     const WHit* chits = hits;
@@ -665,21 +682,23 @@ ft_status trace_wavefront(ft_scene* sc, const RayParams& P, uint32_t max_depth, 
     FT_CUDA_TRY(cudaStreamSynchronize(st), "wavefront level");
     if (h[1] > 0) {
       unsigned sgrid = static_cast<unsigned>(std::max<uint64_t>(1, std::min<uint64_t>((h[1] + 127) / 128,
-                                                                                     static_cast<uint64_t>(sms) * 16)));
+                                                                                     static_cast<uint64_t>(sms) * 8)));
       const WShadow* shadows = sc->wf_shadows;
       const unsigned long long* scount = c + 2;
       unsigned long long scap = sc->wf_shadows_cap;
-      void* hargs[] = {&S, &PP, &shadows, &scount, &scap, &radiance};
+      FT_CUDA_TRY(cudaMemsetAsync(shadow_next, 0, sizeof(unsigned long long), st), "cudaMemsetAsync(queues)");
+      void* hargs[] = {&S, &PP, &none, &shadows, &scount, &scap, &radiance, &shadow_next, &flags};
       FT_CUDA_TRY(cudaLaunchKernel(k_shadow, dim3(sgrid), dim3(128), hargs, 0, st), "wavefront shadow launch");
       *launches += 1;
     }
     n = std::min<uint64_t>(h[0], sc->wf_jobs_cap[nxt]);  // an overflowed queue holds its capacity
     cur = nxt;
   }
-  unsigned long long overflow = 0;
-  FT_CUDA_TRY(cudaMemcpyAsync(&overflow, c + 3, sizeof(overflow), cudaMemcpyDeviceToHost, st), "queue flags");
+  unsigned long long tail[4] = {0, 0, 0, 0};  // overflow flag, work counters, self-check flags
+  FT_CUDA_TRY(cudaMemcpyAsync(tail, c + 3, sizeof(tail), cudaMemcpyDeviceToHost, st), "queue flags");
   FT_CUDA_TRY(cudaStreamSynchronize(st), "wavefront");
-  if (overflow) return ftcommon::fail(FT_ERR_CUDA, "wavefront queue overflow");
+  if (tail[0]) return ftcommon::fail(FT_ERR_CUDA, "wavefront queue overflow");
+  if (ft_status s = march_check(tail[3])) return s;
   return FT_OK;
 }
 
@@ -1260,8 +1279,11 @@ ft_status ft_batch_create(const ft_batch_item* items, uint32_t n, uint32_t flags
   FT_CUDA_TRY(cudaMalloc(&b->d_rgbf, pix_total * 3 * sizeof(float)), "cudaMalloc(batch rgb)");
   FT_CUDA_TRY(cudaMalloc(&b->d_rgb8, pix_total * 3), "cudaMalloc(batch rgb8)");
   FT_CUDA_TRY(cudaMalloc(&b->d_counters, 2 * sizeof(unsigned long long)), "cudaMalloc(batch counters)");
-  FT_CUDA_TRY(cudaMalloc(&b->wf_counters, 4 * sizeof(unsigned long long)), "cudaMalloc(batch queue counters)");
-  FT_CUDA_TRY(cudaMemset(b->wf_counters, 0, 4 * sizeof(unsigned long long)), "cudaMemset(batch queue counters)");
+  FT_CUDA_TRY(cudaMalloc(&b->wf_counters, kWfCounters * sizeof(unsigned long long)),
+              "cudaMalloc(batch queue counters)");
+  FT_CUDA_TRY(cudaMemset(b->wf_counters, 0, kWfCounters * sizeof(unsigned long long)),
+              "cudaMemset(batch queue counters)");
+  b->sms = sms;
   if (samples[1] >= kNoSample) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "too many Whitted samples in one batch");
   if (ft_status st = batch_apply_tuning(b)) return st;
   *out = guard.release();
@@ -1557,7 +1579,8 @@ ft_status ft_scene_jit(ft_scene* sc, ft_jit_info* info) {
   out.source_bytes = src.size();
   static const char* const kExprs[6] = {"march_depth_persistent<false, false, false>",
                                         "march_depth_persistent<false, true, false>", "trace_kernel<false>",
-                                        "wf_march_kernel", "wf_shade_kernel", "wf_shadow_kernel"};
+                                        "wf_march_persistent<false>", "wf_shade_kernel",
+                                        "wf_shadow_persistent<false>"};
   struct Module {
     std::vector<char> cubin;
     std::string lowered[6];

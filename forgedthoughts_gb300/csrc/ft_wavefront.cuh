@@ -19,6 +19,10 @@
 #pragma once
 
 constexpr uint32_t kNoSample = 0xffffffffu;
+// Queue counters of a wavefront: job counts of the two levels in flight, the
+// shadow count, the overflow flag, the march and shadow kernels' work
+// counters and the self-check flags.
+constexpr int kWfCounters = 8;
 
 struct WJob {
   float o[3], d[3], w[3];
@@ -123,26 +127,6 @@ __global__ void __launch_bounds__(128) wf_primary_kernel(RayParams P, WJob* __re
   jobs[i] = j;
 }
 
-// One queued ray: march it; a miss adds the environment, a hit is recorded.
-__device__ __forceinline__ void wf_march_job(const DevScene& S, const RayParams& P, const WJob& wj, WHit* out,
-                                             float* radiance, Ctx<false>& cx) {
-  WHit h_out{};
-  RayJob J = job_of(wj);
-  float min_t = J.depth == 0 ? 0.0f : P.eps * 2.0f;  // secondary_min_t (R:4175-4178)
-  TraceHit h;
-  if (!march_hit(S, P, J.o, J.d, min_t, &h, cx)) {
-    add_radiance(radiance, wj.sample, mul3(J.w, mul3(environment(S, J.d), transmittance(J.med, P.max_dist))));
-    h_out.leaf = -1;
-  } else {
-    h_out.t = h.t;
-    h_out.pos[0] = h.pos.x; h_out.pos[1] = h.pos.y; h_out.pos[2] = h.pos.z;
-    h_out.normal[0] = h.normal.x; h_out.normal[1] = h.normal.y; h_out.normal[2] = h.normal.z;
-    h_out.mat = h.mat;
-    h_out.leaf = h.leaf;
-  }
-  *out = h_out;
-}
-
 // One recorded hit: shade it into the queues.
 __device__ __forceinline__ void wf_shade_job(const DevScene& S, const RayParams& P, const WJob& wj, const WHit& wh,
                                              const WQueues& Q, Ctx<false>& cx) {
@@ -157,32 +141,9 @@ __device__ __forceinline__ void wf_shade_job(const DevScene& S, const RayParams&
   shade_hit(S, P, J, h, sink, cx);
 }
 
-// One shadow job: its visibility times its contribution.
-__device__ __forceinline__ void wf_shadow_job(const DevScene& S, const RayParams& P, const WShadow& sj,
-                                              float* radiance, Ctx<false>& cx) {
-  float vis = shadow_visibility(S, f3(sj.o[0], sj.o[1], sj.o[2]), f3(sj.d[0], sj.d[1], sj.d[2]), sj.max_t, P.eps, cx);
-  if (vis > 0.0f) add_radiance(radiance, sj.sample, f3(sj.contrib[0], sj.contrib[1], sj.contrib[2]) * vis);
-}
-
 #define FT_GRID_STRIDE(i, n)                                                                             \
   for (unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x; \
        i < (n); i += static_cast<unsigned long long>(gridDim.x) * blockDim.x)
-
-__global__ void __launch_bounds__(128) wf_march_kernel(DevScene S, RayParams P, const WJob* __restrict__ jobs,
-                                                       const unsigned long long* __restrict__ count,
-                                                       unsigned long long cap, WHit* __restrict__ hits,
-                                                       float* __restrict__ radiance) {
-  Ctx<false> cx;
-  cx.c = Counters{};
-  const unsigned long long n = min(*count, cap);  // a queue that overflowed holds cap jobs
-  FT_GRID_STRIDE(i, n) {
-    if (jobs[i].sample == kNoSample) {
-      hits[i].leaf = -2;
-      continue;
-    }
-    wf_march_job(S, P, jobs[i], &hits[i], radiance, cx);
-  }
-}
 
 __global__ void __launch_bounds__(128) wf_shade_kernel(DevScene S, RayParams P, const WJob* __restrict__ jobs,
                                                        const unsigned long long* __restrict__ count,
@@ -197,22 +158,9 @@ __global__ void __launch_bounds__(128) wf_shade_kernel(DevScene S, RayParams P, 
   }
 }
 
-__global__ void __launch_bounds__(128) wf_shadow_kernel(DevScene S, RayParams P, const WShadow* __restrict__ shadows,
-                                                        const unsigned long long* __restrict__ count,
-                                                        unsigned long long cap, float* __restrict__ radiance) {
-  Ctx<false> cx;
-  cx.c = Counters{};
-  const unsigned long long n = min(*count, cap);
-  FT_GRID_STRIDE(i, n) wf_shadow_job(S, P, shadows[i], radiance, cx);
-}
 
-#ifndef FT_JIT
-// ---------------------------------------------------------------- batches
-// The same kernels over the queues of many renders at once (ft_batch): every
-// job carries its global sample index, and the render it belongs to is the
-// last whose first sample is not above it.  The counts stay on the device, so
-// a batch captures its levels into one CUDA graph.
-
+// Render of a queued job in a batch: the last whose first sample is not
+// above the job's sample.
 __device__ __forceinline__ uint32_t sample_item(const BatchView& V, uint64_t sample) {
   uint32_t lo = 0, hi = V.n_items;  // out_first[lo] <= sample < out_first[hi]
   while (hi - lo > 1) {
@@ -222,6 +170,263 @@ __device__ __forceinline__ uint32_t sample_item(const BatchView& V, uint64_t sam
   }
   return lo;
 }
+
+// Queue kernels with warp refill.  A grid-stride loop gives each lane one
+// job to the end, so a warp waits for its longest march (the shadow kernel
+// kept 8 of 32 lanes busy).  Here every lane runs one distance evaluation per
+// iteration of a small state machine and takes the next job of the queue
+// (one atomic per warp) once at least kWfRefill lanes are idle.  With kBatch
+// each job's render (scene, parameters) is looked up from its sample index.
+// Self-checks as in march_depth_persistent: a job may take at most
+// max_steps + 64 iterations, a warp at most kMarchWallNs; a lane past either
+// limit sets a bit in *flags and gives up.
+constexpr unsigned kWfRefill = 8;
+
+#define FT_WF_REFILL_TOP(live, queue_done, n_jobs, next_job, base_out, took)                       \
+  if ((++loop_iters & 1023u) == 0u) {                                                            \
+    unsigned long long now_ = lane == 0 ? ftd::global_ns() : 0ull;                               \
+    now_ = __shfl_sync(0xffffffffu, now_, 0);                                                    \
+    if (now_ - t_start > kMarchWallNs) {                                                         \
+      if (lane == 0) atomicOr(flags, 1ull << 8);                                                 \
+      break;                                                                                     \
+    }                                                                                            \
+  }                                                                                              \
+  bool took = false;                                                                             \
+  unsigned long long base_out = 0;                                                               \
+  {                                                                                              \
+    unsigned idle_ = __ballot_sync(0xffffffffu, !(live));                                        \
+    if (!(queue_done) && (__popc(idle_) >= kWfRefill || idle_ == 0xffffffffu)) {                 \
+      unsigned want_ = __popc(idle_);                                                            \
+      unsigned long long b_ = 0;                                                                 \
+      if (lane == 0) b_ = atomicAdd(next_job, static_cast<unsigned long long>(want_));           \
+      b_ = __shfl_sync(0xffffffffu, b_, 0);                                                      \
+      if (b_ >= (n_jobs)) queue_done = true;                                                     \
+      if (!(live)) {                                                                             \
+        base_out = b_ + __popc(idle_ & ((1u << lane) - 1u));                                     \
+        took = base_out < (n_jobs);                                                              \
+      }                                                                                          \
+    }                                                                                            \
+  }
+
+enum WfPhase : int { kWfMarch = 0, kWfRefine = 1, kWfNormal = 2, kWfFinal = 3 };
+
+// raymarch_hit (R:4091-4139) of every queued ray: march from the ray's
+// secondary_min_t (R:4175-4178), ten bisections, the six-tap normal and the
+// hit leaf's lookup (march_hit, one evaluation per iteration); a miss adds
+// the environment seen through the ray's medium.
+template <bool kBatch>
+__global__ void __launch_bounds__(128, 6) wf_march_persistent(DevScene S0, RayParams P0, BatchView V,
+                                                              const WJob* __restrict__ jobs,
+                                                              const unsigned long long* __restrict__ count,
+                                                              unsigned long long cap, WHit* __restrict__ hits,
+                                                              float* __restrict__ radiance,
+                                                              unsigned long long* __restrict__ next_job,
+                                                              unsigned long long* __restrict__ flags) {
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned long long n_jobs = min(*count, cap);
+  Ctx<false> cx;
+  cx.c = Counters{};
+  const unsigned long long t_start = __shfl_sync(0xffffffffu, lane == 0 ? ftd::global_ns() : 0ull, 0);
+  uint32_t loop_iters = 0;
+  bool live = false, queue_done = false;
+  unsigned long long job = 0;
+  uint32_t item = 0, steps = 0, ray_iters = 0;
+  int phase = kWfMarch, k = 0;
+  F3 o = f3(0.0f, 0.0f, 0.0f), d = o, pos = o;
+  float traveled = 0.0f, prev = 0.0f, max_t = 0.0f, lo = 0.0f, hi = 0.0f, nx = 0.0f, ny = 0.0f, nz = 0.0f;
+  auto miss = [&](const DevScene& S, const RayParams& P) {
+    const WJob& wj = jobs[job];
+    RayJob J = job_of(wj);
+    add_radiance(radiance, wj.sample, mul3(J.w, mul3(environment(S, J.d), transmittance(J.med, P.max_dist))));
+    hits[job].leaf = -1;
+    live = false;
+  };
+  for (;;) {
+    FT_WF_REFILL_TOP(live, queue_done, n_jobs, next_job, mine, took)
+    if (took) {
+      job = mine;
+      const WJob& wj = jobs[job];
+      if (wj.sample == kNoSample) {
+        hits[job].leaf = -2;
+      } else {
+        item = kBatch ? sample_item(V, wj.sample) : 0u;
+        const DevScene& S = kBatch ? V.scenes[item] : S0;
+        const RayParams& P = kBatch ? V.params[item] : P0;
+        o = f3(wj.o[0], wj.o[1], wj.o[2]);
+        d = f3(wj.d[0], wj.d[1], wj.d[2]);
+        float t0, t1;
+        if (!ray_aabb(o, d, S.smin, S.smax, &t0, &t1)) {
+          miss(S, P);
+        } else {
+          const float min_t = wj.depth == 0 ? 0.0f : P.eps * 2.0f;  // secondary_min_t (R:4175-4178)
+          max_t = fminf(P.max_dist, t1);
+          traveled = fmaxf(min_t, fmaxf(t0, 0.0f));
+          prev = traveled;
+          steps = 0;
+          ray_iters = 0;
+          phase = kWfMarch;
+          live = true;
+        }
+      }
+    }
+    if (__ballot_sync(0xffffffffu, live) == 0u) {
+      if (queue_done) break;
+      continue;
+    }
+    if (!live) continue;
+    const DevScene& S = kBatch ? V.scenes[item] : S0;
+    const RayParams& P = kBatch ? V.params[item] : P0;
+    const float eps = P.eps;
+    if (++ray_iters > P.max_steps + 64u) {
+      atomicOr(flags, 1ull << (phase & 7));
+      miss(S, P);
+      continue;
+    }
+    if (phase == kWfMarch && (steps >= P.max_steps || traveled > max_t)) {
+      miss(S, P);
+      continue;
+    }
+    const float ne = fmaxf(eps * 4.0f, 1.0e-5f);
+    F3 q;
+    float mid = 0.0f;
+    if (phase == kWfMarch) {
+      q = o + d * traveled;
+      cx.step();
+    } else if (phase == kWfRefine) {
+      mid = 0.5f * (lo + hi);
+      q = o + d * mid;
+    } else if (phase == kWfNormal) {
+      float sgn = (k & 1) ? -ne : ne;
+      q = pos;
+      if (k < 2) q.x += sgn;
+      else if (k < 4) q.y += sgn;
+      else q.z += sgn;
+    } else {
+      q = pos;
+    }
+    if (phase == kWfFinal) {
+      WHit h{};
+      Info fin = scene_distance_leaf(S, pos, &h.leaf, cx);
+      F3 nn = f3(nx, ny, nz);
+      F3 nr = ftd::len3(nn) > 1.0e-8f ? ftd::normalize3(nn) : f3(0.0f, 1.0f, 0.0f);
+      h.t = hi;
+      h.pos[0] = pos.x; h.pos[1] = pos.y; h.pos[2] = pos.z;
+      h.normal[0] = nr.x; h.normal[1] = nr.y; h.normal[2] = nr.z;
+      h.mat = fin.mat;
+      hits[job] = h;
+      live = false;
+      continue;
+    }
+    const float dq = scene_distance_inl(S, q, cx).d;
+    if (phase == kWfMarch) {
+      if (fabsf(dq) < eps) {
+        lo = prev;
+        hi = traveled;
+        k = 0;
+        phase = kWfRefine;
+      } else {
+        prev = traveled;
+        traveled += fmaxf(fabsf(dq) * ftd::rclamp(P.step_scale, 0.05f, 1.0f), fmaxf(eps * 0.5f, 1.0e-5f));
+        ++steps;
+      }
+    } else if (phase == kWfRefine) {
+      if (fabsf(dq) < eps) hi = mid;
+      else lo = mid;
+      if (++k == 10) {
+        pos = o + d * hi;
+        k = 0;
+        phase = kWfNormal;
+      }
+    } else {
+      // dx = d(p + e x) - d(p - e x), one subtraction as march_hit
+      if (k == 0) nx = dq;
+      else if (k == 1) nx = nx - dq;
+      else if (k == 2) ny = dq;
+      else if (k == 3) ny = ny - dq;
+      else if (k == 4) nz = dq;
+      else nz = nz - dq;
+      if (++k == 6) phase = kWfFinal;
+    }
+  }
+}
+
+// shadow_visibility (R:4706-4733) of every queued shadow job, one step per
+// iteration; the radiance gets contribution x visibility.
+template <bool kBatch>
+__global__ void __launch_bounds__(128, 8) wf_shadow_persistent(DevScene S0, RayParams P0, BatchView V,
+                                                               const WShadow* __restrict__ shadows,
+                                                               const unsigned long long* __restrict__ count,
+                                                               unsigned long long cap, float* __restrict__ radiance,
+                                                               unsigned long long* __restrict__ next_job,
+                                                               unsigned long long* __restrict__ flags) {
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned long long n_jobs = min(*count, cap);
+  Ctx<false> cx;
+  cx.c = Counters{};
+  const unsigned long long t_start = __shfl_sync(0xffffffffu, lane == 0 ? ftd::global_ns() : 0ull, 0);
+  uint32_t loop_iters = 0;
+  bool live = false, queue_done = false;
+  unsigned long long job = 0;
+  uint32_t item = 0;
+  int it = 0;
+  F3 o = f3(0.0f, 0.0f, 0.0f), d = o;
+  float t = 0.0f, max_t = 0.0f, vis = 1.0f;
+  auto finish = [&](float v) {
+    if (v > 0.0f) {
+      const WShadow& sj = shadows[job];
+      add_radiance(radiance, sj.sample, f3(sj.contrib[0], sj.contrib[1], sj.contrib[2]) * v);
+    }
+    live = false;
+  };
+  for (;;) {
+    FT_WF_REFILL_TOP(live, queue_done, n_jobs, next_job, mine, took)
+    if (took) {
+      job = mine;
+      const WShadow& sj = shadows[job];
+      item = kBatch ? sample_item(V, sj.sample) : 0u;
+      const RayParams& P = kBatch ? V.params[item] : P0;
+      o = f3(sj.o[0], sj.o[1], sj.o[2]);
+      d = f3(sj.d[0], sj.d[1], sj.d[2]);
+      max_t = sj.max_t;
+      t = P.eps * 2.0f;
+      vis = 1.0f;
+      it = 0;
+      live = true;
+    }
+    if (__ballot_sync(0xffffffffu, live) == 0u) {
+      if (queue_done) break;
+      continue;
+    }
+    if (!live) continue;
+    const DevScene& S = kBatch ? V.scenes[item] : S0;
+    const RayParams& P = kBatch ? V.params[item] : P0;
+    const float eps = P.eps;
+    if (it >= 80 || t >= max_t) {
+      finish(clamp01(vis));
+      continue;
+    }
+    F3 p = o + d * t;
+    float lower = fabsf(scene_lower_bound(S, p));
+    float h = lower > fmaxf(eps * 8.0f, 0.02f) ? lower : fabsf(scene_distance_inl(S, p, cx).d);
+    if (h < eps * 4.0f) {
+      finish(0.0f);
+      continue;
+    }
+    vis = fminf(vis, clamp01(10.0f * h / t));
+    t += fmaxf(h, eps * 2.0f);
+    ++it;
+  }
+}
+
+#undef FT_WF_REFILL_TOP
+
+#ifndef FT_JIT
+// ---------------------------------------------------------------- batches
+// The same kernels over the queues of many renders at once (ft_batch): every
+// job carries its global sample index, and the render it belongs to is the
+// last whose first sample is not above it.  The counts stay on the device, so
+// a batch captures its levels into one CUDA graph.
+
 
 // Primary jobs of every render; the level-0 count is the work-item total.
 __global__ void __launch_bounds__(128) wf_primary_batch_kernel(BatchView V, WJob* __restrict__ jobs,
@@ -250,23 +455,6 @@ __global__ void __launch_bounds__(128) wf_primary_batch_kernel(BatchView V, WJob
   }
 }
 
-__global__ void __launch_bounds__(128) wf_march_batch_kernel(BatchView V, const WJob* __restrict__ jobs,
-                                                             const unsigned long long* __restrict__ count,
-                                                             unsigned long long cap, WHit* __restrict__ hits,
-                                                             float* __restrict__ radiance) {
-  Ctx<false> cx;
-  cx.c = Counters{};
-  const unsigned long long n = min(*count, cap);
-  FT_GRID_STRIDE(i, n) {
-    if (jobs[i].sample == kNoSample) {
-      hits[i].leaf = -2;
-      continue;
-    }
-    const uint32_t it = sample_item(V, jobs[i].sample);
-    wf_march_job(V.scenes[it], V.params[it], jobs[i], &hits[i], radiance, cx);
-  }
-}
-
 __global__ void __launch_bounds__(128) wf_shade_batch_kernel(BatchView V, const uint32_t* __restrict__ max_depth,
                                                              const WJob* __restrict__ jobs,
                                                              const unsigned long long* __restrict__ count,
@@ -284,17 +472,6 @@ __global__ void __launch_bounds__(128) wf_shade_batch_kernel(BatchView V, const 
   }
 }
 
-__global__ void __launch_bounds__(128) wf_shadow_batch_kernel(BatchView V, const WShadow* __restrict__ shadows,
-                                                              const unsigned long long* __restrict__ count,
-                                                              unsigned long long cap, float* __restrict__ radiance) {
-  Ctx<false> cx;
-  cx.c = Counters{};
-  const unsigned long long n = min(*count, cap);
-  FT_GRID_STRIDE(i, n) {
-    const uint32_t it = sample_item(V, shadows[i].sample);
-    wf_shadow_job(V.scenes[it], V.params[it], shadows[i], radiance, cx);
-  }
-}
 #endif  // FT_JIT
 
 #undef FT_GRID_STRIDE
