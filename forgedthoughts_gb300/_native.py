@@ -29,6 +29,7 @@ FT_ERR_JIT = 12
 FT_FLAG_DEVICE_POINTERS = 1
 FT_FLAG_FP16_BRICKS = 2
 FT_BRICK_FREE_FAR_STEPS = 1
+FT_MAT_STANDARD, FT_MAT_LAMBERT, FT_MAT_METAL, FT_MAT_DIELECTRIC = 0, 1, 2, 3  # ft_material_kind
 FT_ABI_VERSION = 1
 FT_MAX_PROGRAM_REGS = 64
 

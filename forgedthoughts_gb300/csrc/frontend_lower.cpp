@@ -237,6 +237,32 @@ class HookCompiler {
     return prog;
   }
 
+ // eval_material_properties_with_overrides (E:2804-2858): the definition's
+  // bindings and property assignments in order, an instance field of the same
+  // name replacing either; property values must fold to constants.  Returns
+  // false when the evaluation fails (the reference then applies none).
+  bool eval_properties(const BlockDef& def, const ObjectData& overrides, std::map<std::string, Value>* props) {
+    what_ = "material property";
+    try {
+      std::map<std::string, SVal> locals;
+      for (const auto& kv : overrides.fields) locals[kv.first] = cst(kv.second);
+      for (const BlockStmt& s : def.statements) {
+        if (s.kind == BlockStmt::Function || !s.expr) continue;
+        const Value* ov = overrides.get(s.name);
+        SVal v = ov ? cst(*ov) : eval(*s.expr, locals, 0);
+        if (s.kind == BlockStmt::Binding) {
+          locals[s.name] = v;
+        } else {
+          if (!v.is_const) return false;
+          (*props)[s.name] = v.cv;
+        }
+      }
+      return true;
+    } catch (const FrontendError&) {
+      return false;
+    }
+  }
+
  private:
   const EvalState& st_;
   std::vector<ft_instr>& code_;
@@ -637,15 +663,7 @@ class Lowerer {
       if (!read_spectrum(o, "color", &col) && !read_spectrum(o, "base_color", &col)) col = def;
       mm.color[0] = col.x; mm.color[1] = col.y; mm.color[2] = col.z;
     };
-    if (st_.material_defs.count(t)) {
-      const BlockDef& def = *st_.material_defs.at(t);
-      std::string model = lower(def.model);
-      int kind = model == "lambert" ? FT_MAT_LAMBERT : model == "metal" ? FT_MAT_METAL
-                 : model == "dielectric" ? FT_MAT_DIELECTRIC : FT_MAT_STANDARD;
-      m = material_defaults(kind);
-      if (kind == FT_MAT_LAMBERT) m.roughness = 1.0f;
-      return m;
-    }
+    if (st_.material_defs.count(t)) return material_from_dynamic_def(*st_.material_defs.at(t), o);
     if (lt == "lambert") {
       m = material_defaults(FT_MAT_LAMBERT);
       set_color(m, v3(0.8f, 0.8f, 0.8f));
@@ -690,6 +708,69 @@ class Lowerer {
     m.clearcoat = clampf(number_or(o, {"clearcoat"}, 0.0f), 0.0f, 1.0f);
     m.clearcoat_roughness = clampf(number_or(o, {"clearcoat_roughness"}, 0.1f), 0.0f, 1.0f);
     emission(m);
+    return m;
+  }
+
+  // material_from_dynamic_def (R:6633-6690) with apply_dynamic_material_
+  // properties (R:6692-6770): the model's parameters, then the definition's
+  // property assignments.  Metal and Dielectric definitions keep their kind;
+  // every other model (Lambert included) is a Standard material, with the
+  // Lambert parameters unless the model is Standard or Layered.  The
+  // definition's functions (`fn color(ctx)` and the other per-hit hooks) are
+  // not evaluated.
+  ft_material material_from_dynamic_def(const BlockDef& def, const ObjectData& overrides) {
+    ft_material m;
+    const std::string& model = def.model;
+    if (model == "Metal") {
+      m = material_defaults(FT_MAT_METAL);  // MaterialParams::metal (materials/mod.rs:154-181)
+      m.color[0] = m.color[1] = m.color[2] = 0.9f;
+      m.roughness = 0.1f;
+      m.metallic = 1.0f;
+      m.specular = 1.0f;
+    } else if (model == "Dielectric") {
+      m = material_defaults(FT_MAT_DIELECTRIC);  // MaterialParams::dielectric (materials/mod.rs:183-212)
+      m.color[0] = m.color[1] = m.color[2] = 1.0f;
+      m.ior = 1.5f;
+      m.roughness = 0.0f;
+      m.transmission = 1.0f;
+    } else {
+      m = material_defaults(FT_MAT_STANDARD);
+      if (model != "Standard" && model != "Layered") m.roughness = 1.0f;  // MaterialParams::lambert
+    }
+    std::vector<ft_instr> scratch;
+    HookCompiler hc(st_, scratch);
+    std::map<std::string, Value> props;
+    if (!hc.eval_properties(def, overrides, &props)) return m;
+    auto num = [&](const char* k, float* out) {
+      auto it = props.find(k);
+      if (it == props.end() || it->second.kind != Value::Number) return false;
+      *out = it->second.num;
+      return true;
+    };
+    auto spec = [&](const char* k, float* out3) {
+      auto it = props.find(k);
+      if (it == props.end()) return false;
+      ObjectData holder;
+      holder.fields[k] = it->second;
+      V3 c;
+      if (!read_spectrum(holder, k, &c)) return false;
+      out3[0] = c.x; out3[1] = c.y; out3[2] = c.z;
+      return true;
+    };
+    float v;
+    spec("color", m.color);
+    if (num("roughness", &v)) m.roughness = clampf(v, 0.0f, 1.0f);
+    if (num("ior", &v)) m.ior = clampf(v, 1.0f, 3.0f);
+    if (num("metallic", &v)) m.metallic = clampf(v, 0.0f, 1.0f);
+    if (num("specular", &v)) m.specular = clampf(v, 0.0f, 1.0f);
+    if (num("specular_weight", &v)) m.specular_weight = clampf(v, 0.0f, 1.0f);
+    spec("specular_color", m.specular_color);
+    if (num("clearcoat", &v)) m.clearcoat = clampf(v, 0.0f, 1.0f);
+    if (num("clearcoat_roughness", &v)) m.clearcoat_roughness = clampf(v, 0.0f, 1.0f);
+    if (num("transmission", &v)) m.transmission = clampf(v, 0.0f, 1.0f);
+    if (num("thin_walled", &v)) m.thin_walled = v >= 0.5f;
+    spec("emission_color", m.emission_color);
+    if (num("emission_strength", &v)) m.emission_strength = std::max(v, 0.0f);
     return m;
   }
 

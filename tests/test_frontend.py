@@ -116,3 +116,65 @@ def test_workload_generators_are_deterministic():
     b = workloads.union_round_field(n=32, width=16, height=16).source
     assert a == b
     assert "e-" not in a and "e+" not in a  # the lexer has no exponent syntax
+
+
+def _sphere_material(source: str):
+    st = ft.parse_and_eval(source)
+    d = st.desc
+    sph = [d.nodes[i] for i in range(d.n_nodes) if d.nodes[i].kind == 0]
+    assert len(sph) == 1
+    return _native.MaterialC.from_buffer_copy(d.materials[sph[0].material_id])  # outlives the description
+
+
+def test_material_definition_static_color_property():
+    """The reference's resolves_ft_material_static_color_property
+    (renderer.rs tests): a Lambert-model definition assigning `color` from a
+    binding is a Standard material with that colour and the Lambert
+    parameters (material_from_dynamic_def, R:6633-6690)."""
+    m = _sphere_material("""
+        material Solid {
+          model: Lambert;
+          let tint = vec3(0.24, 0.5, 0.82);
+          color = tint;
+        };
+        let scene = Sphere { material: Solid {} };
+    """)
+    assert m.kind == _native.FT_MAT_STANDARD
+    assert abs(m.color[0] - 0.24) < 1e-6 and abs(m.color[1] - 0.5) < 1e-6 and abs(m.color[2] - 0.82) < 1e-6
+    assert m.roughness == 1.0 and m.metallic == 0.0 and abs(m.specular - 0.5) < 1e-7
+
+
+def test_material_definition_properties_clamps_and_overrides():
+    """Metal and Dielectric definitions keep their kind; properties are
+    clamped as apply_dynamic_material_properties (R:6692-6770); an instance
+    field replaces the binding of the same name (material_override_value,
+    eval.rs:3761-3766)."""
+    metal = _sphere_material("""
+        material Brushed {
+          model: Metal;
+          color = vec3(0.8, 0.72, 0.3);
+          roughness = 1.7;
+        };
+        let scene = Sphere { material: Brushed {} };
+    """)
+    assert metal.kind == _native.FT_MAT_METAL and metal.metallic == 1.0
+    assert abs(metal.color[1] - 0.72) < 1e-6 and metal.roughness == 1.0
+    glass = _sphere_material("""
+        material Glass {
+          model: Dielectric;
+          ior = 5.0;
+        };
+        let scene = Sphere { material: Glass {} };
+    """)
+    assert glass.kind == _native.FT_MAT_DIELECTRIC and glass.ior == 3.0 and glass.transmission == 1.0
+    over = _sphere_material("""
+        material Solid {
+          model: Standard;
+          let tint = vec3(0.24, 0.5, 0.82);
+          color = tint;
+          metallic = 0.25;
+        };
+        let scene = Sphere { material: Solid { tint: vec3(0.1, 0.2, 0.3) } };
+    """)
+    assert over.kind == _native.FT_MAT_STANDARD and over.roughness == 0.5 and over.metallic == 0.25
+    assert abs(over.color[0] - 0.1) < 1e-6 and abs(over.color[2] - 0.3) < 1e-6

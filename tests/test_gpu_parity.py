@@ -6,7 +6,7 @@ import pytest
 import forgedthoughts_gb300 as ft
 import oracle
 from conftest import FIXTURES
-from forgedthoughts_gb300 import workloads
+from forgedthoughts_gb300 import _native, workloads
 from parity import DEPTH_TOL, assert_depth_parity, compare_depth
 
 pytestmark = pytest.mark.gpu
@@ -194,3 +194,42 @@ def test_gpu_trace_union_round_field_reduced():
     assert within >= 0.99, within
     assert radiance_rmse(lin, ref32) <= max(1e-3, radiance_rmse(ref32, ref64)), (
         radiance_rmse(lin, ref32), radiance_rmse(ref32, ref64))
+
+
+MATERIAL_DEFS_SCENE = """
+material Solid {
+  model: Lambert;
+  let tint = vec3(0.24, 0.5, 0.82);
+  color = tint;
+};
+material Brushed {
+  model: Metal;
+  color = vec3(0.8, 0.72, 0.3);
+  roughness = 0.15;
+};
+material Glass {
+  model: Dielectric;
+  ior = 1.45;
+};
+let camera = Camera { origin: vec3(0.0, 1.2, -4.5), target: vec3(0.0, 0.4, 0.0), fov_y: 45.0 };
+let light = PointLight { position: vec3(3.0, 6.0, -3.0), intensity: 60.0 };
+let ground = Box { size: vec3(20.0, 1.0, 20.0), pos: vec3(0.0, -0.5, 0.0), material: Solid { tint: vec3(0.7, 0.7, 0.68) } };
+let a = Sphere { radius: 0.5, pos: vec3(-1.1, 0.5, 0.0), material: Solid {} };
+let b = Sphere { radius: 0.5, pos: vec3(0.0, 0.5, 0.3), material: Brushed {} };
+let c = Sphere { radius: 0.5, pos: vec3(1.1, 0.5, 0.0), material: Glass {} };
+let scene = ground + a + b + c;
+"""
+
+
+def test_gpu_trace_material_definitions():
+    """User material definitions (Lambert-model definitions become Standard
+    materials, Metal and Dielectric keep their kind, properties and instance
+    overrides applied): Whitted radiance against the f32 oracle."""
+    st = ft.parse_and_eval(MATERIAL_DEFS_SCENE)
+    opts = ft.RenderOptions(width=160, height=120, max_steps=256, max_dist=50.0, epsilon=1e-4, step_scale=0.7)
+    kinds = sorted({st.desc.materials[i].kind for i in range(st.desc.n_materials)})
+    assert kinds == [_native.FT_MAT_STANDARD, _native.FT_MAT_METAL, _native.FT_MAT_DIELECTRIC]
+    for depth in (1, 3):
+        lin, _ = ft.render_trace(st, opts, ft.AccelMode.Bvh, 1, depth)
+        ref, _, _ = oracle.render_trace(st, opts, 1, 1, depth, 32)
+        assert radiance_rmse(lin, ref) <= 1e-3, (depth, radiance_rmse(lin, ref))
