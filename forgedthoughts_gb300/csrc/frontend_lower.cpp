@@ -771,6 +771,18 @@ class Lowerer {
     if (num("thin_walled", &v)) m.thin_walled = v >= 0.5f;
     spec("emission_color", m.emission_color);
     if (num("emission_strength", &v)) m.emission_strength = std::max(v, 0.0f);
+    if (model == "Standard" || model == "Layered") {
+      // resolve_leaf_material (R:7258-7470) then sets the coat at every hit:
+      // specular colour, IOR, clearcoat and its roughness come from the
+      // coat_* properties (defaults 1, 1.33, 0 and 0.08; coat_mask, a
+      // per-hit hook only, is 1 without one).
+      float cc[3] = {1.0f, 1.0f, 1.0f};
+      spec("coat_color", cc);
+      std::memcpy(m.specular_color, cc, sizeof(cc));
+      m.ior = clampf(num("coat_ior", &v) ? v : 1.33f, 1.0f, 3.0f);
+      m.clearcoat = clampf(num("coat_weight", &v) ? v : 0.0f, 0.0f, 1.0f);
+      m.clearcoat_roughness = clampf(num("coat_roughness", &v) ? v : 0.08f, 0.0f, 1.0f);
+    }
     return m;
   }
 

@@ -178,3 +178,17 @@ def test_material_definition_properties_clamps_and_overrides():
     """)
     assert over.kind == _native.FT_MAT_STANDARD and over.roughness == 0.5 and over.metallic == 0.25
     assert abs(over.color[0] - 0.1) < 1e-6 and abs(over.color[2] - 0.3) < 1e-6
+    # Standard-model definitions get the coat of resolve_leaf_material
+    # (R:7396-7470): IOR 1.33 and clearcoat roughness 0.08 by default
+    assert abs(over.ior - 1.33) < 1e-6 and abs(over.clearcoat_roughness - 0.08) < 1e-6 and over.clearcoat == 0.0
+    coat = _sphere_material("""
+        material Coated {
+          model: Standard;
+          ior = 1.7;
+          coat_ior = 1.5;
+          coat_weight = 0.6;
+          coat_color = vec3(0.9, 0.95, 1.0);
+        };
+        let scene = Sphere { material: Coated {} };
+    """)
+    assert abs(coat.ior - 1.5) < 1e-6 and abs(coat.clearcoat - 0.6) < 1e-6 and abs(coat.specular_color[1] - 0.95) < 1e-6
