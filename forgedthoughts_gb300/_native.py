@@ -30,7 +30,8 @@ FT_FLAG_DEVICE_POINTERS = 1
 FT_FLAG_FP16_BRICKS = 2
 FT_BRICK_FREE_FAR_STEPS = 1
 FT_MAT_STANDARD, FT_MAT_LAMBERT, FT_MAT_METAL, FT_MAT_DIELECTRIC = 0, 1, 2, 3  # ft_material_kind
-FT_ABI_VERSION = 1
+FT_MATERIAL_HOOK_PARAMS = 7
+FT_ABI_VERSION = 2
 FT_MAX_PROGRAM_REGS = 64
 
 
@@ -73,7 +74,9 @@ class MaterialC(ctypes.Structure):
                 ("medium_ior", ctypes.c_float), ("medium_absorption", ctypes.c_float * 3),
                 ("medium_density", ctypes.c_float), ("specular", ctypes.c_float),
                 ("specular_weight", ctypes.c_float), ("specular_color", ctypes.c_float * 3),
-                ("clearcoat", ctypes.c_float), ("clearcoat_roughness", ctypes.c_float)]
+                ("clearcoat", ctypes.c_float), ("clearcoat_roughness", ctypes.c_float),
+                ("roughness_program", ctypes.c_int32), ("ior_program", ctypes.c_int32),
+                ("thin_walled_program", ctypes.c_int32)]
 
 
 class CameraC(ctypes.Structure):

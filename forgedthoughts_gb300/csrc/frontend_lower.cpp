@@ -157,7 +157,7 @@ ft_material material_defaults(int kind) {
   ft_material m;
   std::memset(&m, 0, sizeof(m));
   m.kind = kind;
-  m.color_program = -1;
+  m.color_program = m.roughness_program = m.ior_program = m.thin_walled_program = -1;
   m.color[0] = m.color[1] = m.color[2] = 0.8f;
   m.roughness = 0.5f;
   m.ior = 1.5f;
@@ -181,6 +181,8 @@ struct SVal {
   Value cv;
   int reg = -1;
   bool vec3 = false;
+  // a record of run-time fields (the shading context of material hooks)
+  std::shared_ptr<std::map<std::string, SVal>> rec;
 };
 
 class HookCompiler {
@@ -237,7 +239,67 @@ class HookCompiler {
     return prog;
   }
 
- // eval_material_properties_with_overrides (E:2804-2858): the definition's
+ // A material hook `fn name(ctx)` (eval_material_function_with_overrides,
+  // E:2860-2940): the definition's bindings (an instance field of the same
+  // name replacing one) are constants, `ctx` is the shading context record of
+  // seven parameters (FT_MATERIAL_HOOK_PARAMS).  want: 0 a number, 1 a vec3,
+  // 2 either.  Returns false, emitting nothing, when the body does not fold to
+  // a program of the wanted type.
+  bool compile_ctx(const BlockStmt& fn, const BlockDef& def, const ObjectData& overrides, int want,
+                   ft_program* out) {
+    const size_t mark = code_.size();
+    first_ = static_cast<uint32_t>(mark);
+    nregs_ = 0;
+    what_ = "material";
+    block_ = &def;
+    try {
+      std::map<std::string, SVal> locals;
+      for (const auto& kv : overrides.fields) locals[kv.first] = cst(kv.second);
+      for (const BlockStmt& s : def.statements) {
+        if (s.kind != BlockStmt::Binding || !s.expr) continue;
+        const Value* ov = overrides.get(s.name);
+        locals[s.name] = ov ? cst(*ov) : eval(*s.expr, locals, 0);
+      }
+      static const char* const kFields[FT_MATERIAL_HOOK_PARAMS] = {
+          "position", "local_position", "normal", "view_dir", "front_face", "object_id", "material_id"};
+      SVal ctx;
+      ctx.is_const = false;
+      ctx.rec = std::make_shared<std::map<std::string, SVal>>();
+      for (int k = 0; k < FT_MATERIAL_HOOK_PARAMS; ++k) (*ctx.rec)[kFields[k]] = reg(nregs_++, k < 4);
+      locals[fn.params[0]] = ctx;
+      SVal result = run_body(fn.body, locals, 0);
+      if (result.rec) fail("returns the context");
+      int r = materialize(result);
+      bool rv = reg_vec3(result);
+      if ((want == 0 && rv) || (want == 1 && !rv)) {
+        code_.resize(mark);
+        return false;
+      }
+      ft_instr ret{};
+      ret.op = FT_OP_RET;
+      ret.a = static_cast<uint8_t>(r);
+      ret.flags = rv ? FT_INSTR_VEC3 : 0;
+      code_.push_back(ret);
+      ft_program prog{};
+      prog.first_instr = first_;
+      prog.n_instr = static_cast<uint32_t>(code_.size()) - first_;
+      prog.n_params = FT_MATERIAL_HOOK_PARAMS;
+      prog.param_is_vec3 = 0xfu;
+      prog.n_regs = static_cast<uint32_t>(nregs_);
+      prog.result_is_vec3 = rv ? 1u : 0u;
+      if (nregs_ > FT_MAX_PROGRAM_REGS) {
+        code_.resize(mark);
+        return false;
+      }
+      *out = prog;
+      return true;
+    } catch (const FrontendError&) {
+      code_.resize(mark);
+      return false;
+    }
+  }
+
+  // eval_material_properties_with_overrides (E:2804-2858): the definition's
   // bindings and property assignments in order, an instance field of the same
   // name replacing either; property values must fold to constants.  Returns
   // false when the evaluation fails (the reference then applies none).
@@ -371,6 +433,11 @@ class HookCompiler {
       }
       case Expr::Member: {
         SVal base = eval(*e.lhs, locals, depth);
+        if (base.rec) {
+          auto it = base.rec->find(e.text);
+          if (it == base.rec->end()) fail("undefined identifier '" + e.text + "'");
+          return it->second;
+        }
         if (base.is_const) {
           if (base.cv.kind != Value::Object) fail("member access requires object value");
           const Value* v = base.cv.obj->get(e.text);
@@ -771,6 +838,26 @@ class Lowerer {
     if (num("thin_walled", &v)) m.thin_walled = v >= 0.5f;
     spec("emission_color", m.emission_color);
     if (num("emission_strength", &v)) m.emission_strength = std::max(v, 0.0f);
+    // Per-hit hooks: colour, roughness, IOR and thin_walled
+    // (resolve_leaf_material, R:7164-7600); the other hookable properties are
+    // not lowered.  A Standard or Layered definition's IOR is the coat's
+    // whatever its hook returns, so that hook is left out.
+    const bool coated = model == "Standard" || model == "Layered";
+    for (const BlockStmt& st : def.statements) {
+      if (st.kind != BlockStmt::Function || st.params.size() != 1) continue;
+      int want = st.name == "color" ? 2
+                 : (st.name == "roughness" || (st.name == "ior" && !coated) || st.name == "thin_walled") ? 0 : -1;
+      if (want < 0) continue;
+      HookCompiler hook(st_, out_.instrs);
+      ft_program prog;
+      if (!hook.compile_ctx(st, def, overrides, want, &prog)) continue;
+      out_.programs.push_back(prog);
+      int32_t idx = static_cast<int32_t>(out_.programs.size()) - 1;
+      if (st.name == "color") m.color_program = idx;
+      else if (st.name == "roughness") m.roughness_program = idx;
+      else if (st.name == "ior") m.ior_program = idx;
+      else m.thin_walled_program = idx;
+    }
     if (model == "Standard" || model == "Layered") {
       // resolve_leaf_material (R:7258-7470) then sets the coat at every hit:
       // specular colour, IOR, clearcoat and its roughness come from the

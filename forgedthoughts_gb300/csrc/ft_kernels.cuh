@@ -1166,10 +1166,11 @@ template <bool kStats, class Sink>
 __device__ __forceinline__ void shade_hit(const DevScene& S, const RayParams& P, const RayJob& J, const TraceHit& h,
                                           Sink& sink, Ctx<kStats>& cx) {
   const float eps = P.eps;
-  Resolved rs;
-  resolve_hit(S, h.leaf, h.pos, &rs, cx);
   bool front = ftd::dot3(h.normal, J.d) < 0.0f;
   F3 normal = front ? ftd::normalize3(h.normal) : ftd::normalize3(h.normal * -1.0f);
+  const HookCtx hc{h.pos, normal, ftd::normalize3(J.d * -1.0f), front ? 1.0f : 0.0f};
+  Resolved rs;
+  resolve_hit(S, h.leaf, h.pos, hc, &rs, cx);
   F3 shading_n = normal;
   if (rs.ok) shading_n = ftd::normalize3(front ? rs.normal : rs.normal * -1.0f);
   DMat mats[2];

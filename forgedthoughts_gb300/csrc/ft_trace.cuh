@@ -76,6 +76,40 @@ __device__ DMat mat_of_id(const DevScene& S, uint32_t id) {
   return m;
 }
 
+// The shading context of a hit for material hooks (make_shading_context,
+// R:7875-7911): position, the normal facing the ray, view_dir = -ray
+// direction, front_face.
+struct HookCtx {
+  F3 pos, normal, view_dir;
+  float front_face;
+};
+
+// resolve_leaf_material (R:7164-7600) for a leaf primitive: its material,
+// with the colour, roughness, IOR and thin_walled hooks evaluated on the hit
+// in the primitive's frame.  Roughness is clamped to [0, 1] and the IOR to
+// [1, 3]; a Metal takes neither IOR nor thin_walled.  A numeric colour is
+// grey (spectrum_from_value, R:7924-7935).
+__device__ DMat mat_of_leaf(const DevScene& S, const DevNode& pn, const HookCtx& hc) {
+  DMat m = mat_of_id(S, pn.material_id);
+  const ft_material& fm = S.materials[pn.material_id < static_cast<uint32_t>(S.n_materials) ? pn.material_id : 0u];
+  if (fm.color_program < 0 && fm.roughness_program < 0 && fm.ior_program < 0 && fm.thin_walled_program < 0) return m;
+  const float obj = static_cast<float>(pn.object_id), mat = static_cast<float>(pn.material_id);
+  F3 args[FT_MATERIAL_HOOK_PARAMS] = {hc.pos, ftd::to_local(hc.pos, pn), hc.normal, hc.view_dir,
+                                      f3(hc.front_face, hc.front_face, hc.front_face), f3(obj, obj, obj),
+                                      f3(mat, mat, mat)};
+  if (fm.color_program >= 0) {
+    F3 c = scene_program(S, fm.color_program, args, nullptr);
+    m.a.color = S.programs[fm.color_program].result_is_vec3 ? c : f3(c.x, c.x, c.x);
+  }
+  if (fm.roughness_program >= 0) m.a.roughness = clamp01(scene_program(S, fm.roughness_program, args, nullptr).x);
+  if (fm.kind != FT_MAT_METAL) {
+    if (fm.ior_program >= 0) m.a.ior = ftd::rclamp(scene_program(S, fm.ior_program, args, nullptr).x, 1.0f, 3.0f);
+    if (fm.thin_walled_program >= 0) m.a.thin = scene_program(S, fm.thin_walled_program, args, nullptr).x >= 0.5f;
+  }
+  m.b = m.a;
+  return m;
+}
+
 __device__ __forceinline__ int dom_model(const DMat& m) {
   if (m.kind != kBlendKind) return m.kind;
   return m.t < 0.5f ? m.a_model : m.b_model;
@@ -276,7 +310,8 @@ struct GEntry {
 // resolved normal and material (R:4462-4552, R:6945-7113).  Subtree values of
 // modifiers come from their postfix op range.
 template <bool kStats>
-__device__ __noinline__ void resolve_generic(const DevScene& S, int root, F3 p, Resolved* out, Ctx<kStats>& cx) {
+__device__ __noinline__ void resolve_generic(const DevScene& S, int root, F3 p, const HookCtx& hc, Resolved* out,
+                                             Ctx<kStats>& cx) {
   GEntry st[8];
   int sp = 0;
   int node_stack[24];
@@ -306,7 +341,7 @@ __device__ __noinline__ void resolve_generic(const DevScene& S, int root, F3 p, 
     if (is_prim) {
       e.d = ftd::prim_distance(n, p);
       e.n = prim_normal(n, p);
-      e.m = mat_of_id(S, n.material_id);
+      e.m = mat_of_leaf(S, n, hc);
     } else if (n.kind == FT_NODE_DOMAIN || n.kind == FT_NODE_DISTANCE_POST || n.kind == FT_NODE_NOISE) {
       GEntry base = st[--sp];
       int b = S.node_op_begin[ni], c = S.node_op_end[ni] - S.node_op_begin[ni];
@@ -465,7 +500,8 @@ struct NEntry {
 // weight t; a child with weight exactly 0 is skipped.  A child without
 // gathered primitives is provably weightless when reach >= (other value) + r;
 // otherwise *need receives the reach required.
-__device__ __noinline__ bool resolve_urtree_reach(const DevScene& S, const DevUrTree& t, F3 p, float reach,
+__device__ __noinline__ bool resolve_urtree_reach(const DevScene& S, const DevUrTree& t, F3 p, const HookCtx& hc,
+                                                  float reach,
                                                   Resolved* out, float* need) {
   int gpos[kGather];
   float gdist[kGather];
@@ -520,7 +556,7 @@ __device__ __noinline__ bool resolve_urtree_reach(const DevScene& S, const DevUr
       if (c < 0) {
         const DevNode& pn = S.nodes[S.ur_prims[t.prim_first + (-c - 1)]];
         F.slot[F.stage].n = prim_normal(pn, p);
-        F.slot[F.stage].m = mat_of_id(S, pn.material_id);
+        F.slot[F.stage].m = mat_of_leaf(S, pn, hc);
         ++F.stage;
         continue;
       }
@@ -559,12 +595,12 @@ __device__ __noinline__ bool resolve_urtree_reach(const DevScene& S, const DevUr
   return false;
 }
 
-__device__ void resolve_urtree(const DevScene& S, const DevUrTree& t, F3 p, Resolved* out) {
+__device__ void resolve_urtree(const DevScene& S, const DevUrTree& t, F3 p, const HookCtx& hc, Resolved* out) {
   float reach = 3.0f * t.r;
   out->ok = false;
   for (int attempt = 0; attempt < 6; ++attempt) {
     float need = 0.0f;
-    if (resolve_urtree_reach(S, t, p, reach, out, &need)) return;
+    if (resolve_urtree_reach(S, t, p, hc, reach, out, &need)) return;
     if (need < 0.0f) return;  // capacity exceeded
     reach = fmaxf(1.5f * reach, need * 1.0001f + 1.0e-6f);
   }
@@ -572,22 +608,22 @@ __device__ void resolve_urtree(const DevScene& S, const DevUrTree& t, F3 p, Reso
 
 // Normal and material at a hit on leaf `li`.
 template <bool kStats>
-__device__ void resolve_hit(const DevScene& S, int li, F3 p, Resolved* out, Ctx<kStats>& cx) {
+__device__ void resolve_hit(const DevScene& S, int li, F3 p, const HookCtx& hc, Resolved* out, Ctx<kStats>& cx) {
   const DevLeaf& lf = S.leaves[li];
   out->split = false;
   out->ok = false;
   if (lf.kind == ftgpu::kLeafPrim) {
     const DevNode& n = S.nodes[lf.node];
     out->normal = prim_normal(n, p);
-    out->m = mat_of_id(S, n.material_id);
+    out->m = mat_of_leaf(S, n, hc);
     out->ok = true;
     return;
   }
   if (lf.kind == ftgpu::kLeafUrTree) {
-    resolve_urtree(S, S.urtrees[lf.first], p, out);
+    resolve_urtree(S, S.urtrees[lf.first], p, hc, out);
     if (out->ok) return;
   }
-  resolve_generic(S, lf.node, p, out, cx);
+  resolve_generic(S, lf.node, p, hc, out, cx);
 }
 
 // ---------------------------------------------------------------- lights and shadows

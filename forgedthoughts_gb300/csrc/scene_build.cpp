@@ -76,7 +76,7 @@ class Builder {
       ft_material m;
       std::memset(&m, 0, sizeof(m));
       m.kind = FT_MAT_STANDARD;
-      m.color_program = -1;
+      m.color_program = m.roughness_program = m.ior_program = m.thin_walled_program = -1;
       m.color[0] = m.color[1] = m.color[2] = 0.8f;
       m.roughness = 0.5f;
       m.ior = 1.5f;
@@ -164,8 +164,19 @@ class Builder {
       if (d_.lights[i].samples > 4096) return fail("light " + std::to_string(i) + " has too many samples");
     }
     for (uint32_t i = 0; i < d_.n_materials; ++i) {
-      if (d_.materials[i].kind < FT_MAT_STANDARD || d_.materials[i].kind > FT_MAT_DIELECTRIC)
+      const ft_material& m = d_.materials[i];
+      if (m.kind < FT_MAT_STANDARD || m.kind > FT_MAT_DIELECTRIC)
         return fail("material " + std::to_string(i) + " has an unknown kind");
+      const int32_t progs[4] = {m.color_program, m.roughness_program, m.ior_program, m.thin_walled_program};
+      for (int k = 0; k < 4; ++k) {
+        if (progs[k] < 0) continue;
+        if (static_cast<uint32_t>(progs[k]) >= d_.n_programs)
+          return fail("material " + std::to_string(i) + " has an invalid hook program index");
+        const ft_program& p = d_.programs[progs[k]];
+        if (p.n_params != FT_MATERIAL_HOOK_PARAMS || p.param_is_vec3 != 0xfu || (k > 0 && p.result_is_vec3))
+          return fail("material " + std::to_string(i) + " hook must map the shading context to " +
+                      (k == 0 ? "a colour" : "a number"));
+      }
     }
     // The node graph must be a DAG reachable from the root (no cycles).
     std::vector<char> state(d_.n_nodes, 0);

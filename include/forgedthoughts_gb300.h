@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define FT_ABI_VERSION 1u
+#define FT_ABI_VERSION 2u
 
 /* Status codes.  FT_ERR_MISSING_SCENE_ROOT / UNSUPPORTED_OBJECT /
  * EXPECTED_OBJECT mirror `enum RenderError` (R:159-168); PARSE / EVAL mirror
@@ -218,7 +218,7 @@ typedef struct ft_material {
   int32_t kind;            /* ft_material_kind */
   int32_t has_medium;
   int32_t thin_walled;
-  int32_t color_program;   /* dynamic `fn color(ctx)` hook, -1 if none */
+  int32_t color_program;   /* per-hit `fn color(ctx)` hook (vec3 or number), -1 if none */
   float color[3];
   float roughness;
   float metallic;
@@ -234,7 +234,17 @@ typedef struct ft_material {
   float specular_color[3];
   float clearcoat;
   float clearcoat_roughness;
+  int32_t roughness_program;  /* per-hit `fn roughness(ctx)` hook (number), -1 if none */
+  int32_t ior_program;        /* per-hit `fn ior(ctx)` hook (number), -1 if none */
+  int32_t thin_walled_program; /* per-hit `fn thin_walled(ctx)` hook (number, >= 0.5 thin), -1 if none */
 } ft_material;
+
+/* Material hook programs take the shading context of a hit
+ * (make_shading_context, R:7875-7911) as seven parameters: position,
+ * local_position (the hit in the leaf primitive's frame), normal (facing the
+ * ray), view_dir (-ray direction) as vec3s, then front_face (1 or 0),
+ * object_id and material_id as numbers. */
+#define FT_MATERIAL_HOOK_PARAMS 7
 
 typedef struct ft_camera {
   float origin[3];

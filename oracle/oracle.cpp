@@ -1215,17 +1215,19 @@ class Tracer {
       return attenuate(environment(d), med, R(op_.max_dist));
     }
     V<R> view = normalize(d * R(-1));
+    // make_shading_context (R:7875-7911); front_face as raymarch_hit (R:4122)
+    const bool front = dot(h.normal, d) < R(0);
+    const HookCtx hc{h.pos, front ? normalize(h.normal) : normalize(h.normal * R(-1)), view, front ? R(1) : R(0)};
     Mat<R> ma, mb;
     R t;
     int root = S.desc().root;
-    if (split_material(root, h.pos, &ma, &mb, &t)) {
+    if (split_material(root, h.pos, hc, &ma, &mb, &t)) {
       Sp<R> a = trace_hit(h, d, med, depth, ma, evals);
       Sp<R> b = trace_hit(h, d, med, depth, mb, evals);
       return lerp_sp(a, b, t);
     }
     Mat<R> m;
-    if (!material_from_node(root, h.pos, &m)) m = material_for_id<R>(S.desc(), h.mat);
-    (void)view;
+    if (!material_from_node(root, h.pos, hc, &m)) m = material_for_id<R>(S.desc(), h.mat);
     return trace_hit(h, d, med, depth, m, evals);
   }
 
@@ -1347,27 +1349,67 @@ class Tracer {
     return true;
   }
 
+  struct HookCtx {
+    V<R> pos, normal, view;
+    R front;
+  };
+
+  // resolve_leaf_material (R:7164-7600) for a leaf primitive: the colour,
+  // roughness, IOR and thin_walled hooks of its material evaluated on the
+  // hit in the primitive's frame (to_local with its transform, R:7172-7177);
+  // roughness clamped to [0, 1], IOR to [1, 3] and neither IOR nor
+  // thin_walled for a Metal (R:7472-7530); a numeric colour grey.
+  Mat<R> leaf_material(const ft_node& n, const HookCtx& hc) const {
+    Mat<R> m = material_for_id<R>(S.desc(), n.material_id);
+    const ft_scene_desc& d = S.desc();
+    if (d.n_materials == 0) return m;
+    const ft_material& fm = d.materials[n.material_id < d.n_materials ? n.material_id : 0];
+    if (fm.color_program < 0 && fm.roughness_program < 0 && fm.ior_program < 0 && fm.thin_walled_program < 0)
+      return m;
+    const R obj = R(n.object_id), mid = R(n.material_id);
+    V<R> args[FT_MATERIAL_HOOK_PARAMS] = {hc.pos, S.to_local(hc.pos, n), hc.normal, hc.view,
+                                          mk(hc.front, hc.front, hc.front), mk(obj, obj, obj), mk(mid, mid, mid)};
+    V<R> o;
+    if (fm.color_program >= 0) {
+      S.run_program(fm.color_program, args, &o);
+      m.p.color = d.programs[fm.color_program].result_is_vec3 ? sp(o.x, o.y, o.z) : sp(o.x, o.x, o.x);
+    }
+    if (fm.roughness_program >= 0) {
+      S.run_program(fm.roughness_program, args, &o);
+      m.p.roughness = rclamp(o.x, R(0), R(1));
+    }
+    if (fm.kind != FT_MAT_METAL && fm.ior_program >= 0) {
+      S.run_program(fm.ior_program, args, &o);
+      m.p.ior = rclamp(o.x, R(1), R(3));
+    }
+    if (fm.kind != FT_MAT_METAL && fm.thin_walled_program >= 0) {
+      S.run_program(fm.thin_walled_program, args, &o);
+      m.p.thin_walled = o.x >= R(0.5);
+    }
+    return m;
+  }
+
   // resolve_material_from_node (R:6945-7050) / blend_node_materials (R:7093-7113)
-  bool material_from_node(int idx, V<R> p, Mat<R>* out) const {
+  bool material_from_node(int idx, V<R> p, const HookCtx& hc, Mat<R>* out) const {
     const ft_node& n = S.node(idx);
     if (n.kind <= FT_NODE_EXTRUDE_POLYGON) {
-      *out = material_for_id<R>(S.desc(), n.material_id);
+      *out = leaf_material(n, hc);
       return true;
     }
     switch (n.kind) {
       case FT_NODE_DOMAIN: case FT_NODE_DISTANCE_POST: case FT_NODE_NOISE: case FT_NODE_SLICE: case FT_NODE_SMOOTH:
-        return material_from_node(n.a, p, out);
+        return material_from_node(n.a, p, hc, out);
       case FT_NODE_UNION: {
         Info<R> l = S.info(n.a, p), r = S.info(n.b, p);
-        return material_from_node(l.d <= r.d ? n.a : n.b, p, out);
+        return material_from_node(l.d <= r.d ? n.a : n.b, p, hc, out);
       }
       case FT_NODE_INTERSECT: {
         Info<R> l = S.info(n.a, p), r = S.info(n.b, p);
-        return material_from_node(l.d >= r.d ? n.a : n.b, p, out);
+        return material_from_node(l.d >= r.d ? n.a : n.b, p, hc, out);
       }
       case FT_NODE_SUBTRACT: {
         Info<R> l = S.info(n.a, p), r = S.info(n.b, p);
-        return material_from_node(l.d >= -r.d ? n.a : n.b, p, out);
+        return material_from_node(l.d >= -r.d ? n.a : n.b, p, hc, out);
       }
       default: break;
     }
@@ -1375,35 +1417,35 @@ class Tracer {
     R radius;
     blend_kind(n.kind, &diff, &radius, n);
     Mat<R> left, right;
-    if (!material_from_node(n.a, p, &left) || !material_from_node(n.b, p, &right)) return false;
+    if (!material_from_node(n.a, p, hc, &left) || !material_from_node(n.b, p, hc, &right)) return false;
     *out = blend_materials(left, right, blend_t(n, p, diff, radius));
     return true;
   }
 
   // resolve_split_material_from_node (R:7052-7091)
-  bool split_material(int idx, V<R> p, Mat<R>* a, Mat<R>* b, R* t) const {
+  bool split_material(int idx, V<R> p, const HookCtx& hc, Mat<R>* a, Mat<R>* b, R* t) const {
     const ft_node& n = S.node(idx);
     switch (n.kind) {
       case FT_NODE_UNION: {
         Info<R> l = S.info(n.a, p), r = S.info(n.b, p);
-        return split_material(l.d <= r.d ? n.a : n.b, p, a, b, t);
+        return split_material(l.d <= r.d ? n.a : n.b, p, hc, a, b, t);
       }
       case FT_NODE_INTERSECT: {
         Info<R> l = S.info(n.a, p), r = S.info(n.b, p);
-        return split_material(l.d >= r.d ? n.a : n.b, p, a, b, t);
+        return split_material(l.d >= r.d ? n.a : n.b, p, hc, a, b, t);
       }
       case FT_NODE_SUBTRACT: {
         Info<R> l = S.info(n.a, p), r = S.info(n.b, p);
-        return split_material(l.d >= -r.d ? n.a : n.b, p, a, b, t);
+        return split_material(l.d >= -r.d ? n.a : n.b, p, hc, a, b, t);
       }
       case FT_NODE_SMOOTH:
-      case FT_NODE_NOISE: return split_material(n.a, p, a, b, t);
+      case FT_NODE_NOISE: return split_material(n.a, p, hc, a, b, t);
       default: break;
     }
     bool diff;
     R radius;
     if (!blend_kind(n.kind, &diff, &radius, n)) return false;
-    if (!material_from_node(n.a, p, a) || !material_from_node(n.b, p, b)) return false;
+    if (!material_from_node(n.a, p, hc, a) || !material_from_node(n.b, p, hc, b)) return false;
     *t = blend_t(n, p, diff, radius);
     return true;
   }

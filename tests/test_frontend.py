@@ -192,3 +192,85 @@ def test_material_definition_properties_clamps_and_overrides():
         let scene = Sphere { material: Coated {} };
     """)
     assert abs(coat.ior - 1.5) < 1e-6 and abs(coat.clearcoat - 0.6) < 1e-6 and abs(coat.specular_color[1] - 0.95) < 1e-6
+
+
+HOOK_MATERIALS = """
+material Stripe {
+  model: Lambert;
+  let warm = vec3(0.9, 0.72, 0.3);
+  let dark = vec3(0.12, 0.14, 0.18);
+  fn color(ctx) {
+    let phase = sin(ctx.local_position.x * 8.0);
+    let mask = step(0.0, phase);
+    return mix(warm, dark, mask);
+  }
+};
+material RoughStripe {
+  model: Metal;
+  color = vec3(0.8, 0.72, 0.3);
+  roughness = 0.15;
+  fn roughness(ctx) {
+    let phase = sin(ctx.local_position.x * 6.0);
+    let mask = step(0.0, phase);
+    return mix(0.12, 0.48, mask);
+  }
+};
+material RippleGlass {
+  model: Dielectric;
+  color = vec3(1.0);
+  ior = 1.52;
+  roughness = 0.02;
+  thin_walled = 0.0;
+  fn ior(ctx) {
+    let phase = sin(ctx.local_position.x * 6.0);
+    let mask = step(0.0, phase);
+    return mix(1.45, 1.6, mask);
+  }
+  fn thin_walled(ctx) {
+    let phase = sin(ctx.local_position.y * 6.0);
+    return step(0.0, phase);
+  }
+};
+"""
+
+
+def _hook_ctx(pos):
+    a = np.zeros((1, _native.FT_MATERIAL_HOOK_PARAMS, 3), np.float32)
+    a[0, 0] = a[0, 1] = pos          # position; local_position (sphere at the origin)
+    a[0, 2] = (0.0, 1.0, 0.0)        # normal
+    a[0, 3] = (0.0, 0.0, 1.0)        # view_dir
+    a[0, 4] = a[0, 5] = a[0, 6] = 1  # front_face, object_id, material_id
+    return a
+
+
+def _materials_of(st):
+    d = st.desc
+    return {int(d.materials[i].kind): _native.MaterialC.from_buffer_copy(d.materials[i])
+            for i in range(d.n_materials)}
+
+
+@pytest.mark.parametrize("material,kind", [("Stripe", "FT_MAT_STANDARD"), ("RoughStripe", "FT_MAT_METAL"),
+                                           ("RippleGlass", "FT_MAT_DIELECTRIC")])
+def test_material_hooks_reference_known_answers(material, kind):
+    """The reference's resolves_ft_material_color_from_local_hit_position,
+    resolves_ft_material_dynamic_roughness_hook and
+    resolves_ft_material_dynamic_dielectric_hooks (renderer.rs tests): the
+    lowered hook programs evaluated on the same hits."""
+    st = ft.parse_and_eval(HOOK_MATERIALS + f"let scene = Sphere {{ material: {material} {{}} }};\n")
+    m = _materials_of(st)[getattr(_native, kind)]
+    if material == "Stripe":
+        assert m.roughness_program < 0 and m.ior_program < 0
+        warm = oracle.eval_program(st, m.color_program, _hook_ctx((-0.1, 0.0, 0.0)))[0]
+        dark = oracle.eval_program(st, m.color_program, _hook_ctx((0.1, 0.0, 0.0)))[0]
+        assert np.allclose(warm, (0.9, 0.72, 0.3), atol=1e-6) and np.allclose(dark, (0.12, 0.14, 0.18), atol=1e-6)
+    elif material == "RoughStripe":
+        assert m.color_program < 0 and abs(m.color[0] - 0.8) < 1e-6
+        smooth = oracle.eval_program(st, m.roughness_program, _hook_ctx((-0.1, 0.0, 0.0)))[0, 0]
+        rough = oracle.eval_program(st, m.roughness_program, _hook_ctx((0.1, 0.0, 0.0)))[0, 0]
+        assert abs(smooth - 0.12) < 1e-6 and abs(rough - 0.48) < 1e-6
+    else:
+        solid, thin = _hook_ctx((-0.1, -0.1, 0.0)), _hook_ctx((0.1, 0.1, 0.0))
+        assert abs(oracle.eval_program(st, m.ior_program, solid)[0, 0] - 1.45) < 1e-6
+        assert abs(oracle.eval_program(st, m.ior_program, thin)[0, 0] - 1.6) < 1e-6
+        assert oracle.eval_program(st, m.thin_walled_program, solid)[0, 0] < 0.5
+        assert oracle.eval_program(st, m.thin_walled_program, thin)[0, 0] >= 0.5

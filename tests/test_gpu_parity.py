@@ -233,3 +233,39 @@ def test_gpu_trace_material_definitions():
         lin, _ = ft.render_trace(st, opts, ft.AccelMode.Bvh, 1, depth)
         ref, _, _ = oracle.render_trace(st, opts, 1, 1, depth, 32)
         assert radiance_rmse(lin, ref) <= 1e-3, (depth, radiance_rmse(lin, ref))
+
+
+def test_gpu_trace_material_hooks():
+    """Per-hit material hooks (colour, roughness, IOR, thin_walled, evaluated
+    on the hit's shading context in the primitive's frame): Whitted radiance
+    against the f32 oracle, with the interpreter and with the run-time
+    compiled kernels."""
+    from test_frontend import HOOK_MATERIALS
+
+    src = HOOK_MATERIALS + """
+let camera = Camera { origin: vec3(0.0, 1.0, -4.0), target: vec3(0.0, 0.4, 0.0), fov_y: 45.0 };
+let light = PointLight { position: vec3(3.0, 6.0, -3.0), intensity: 60.0 };
+let ground = Box { size: vec3(20.0, 1.0, 20.0), pos: vec3(0.0, -0.5, 0.0), material: Stripe {} };
+let a = Sphere { radius: 0.5, pos: vec3(-1.1, 0.5, 0.0), material: Stripe {} };
+let b = Sphere { radius: 0.5, pos: vec3(0.0, 0.5, 0.3), material: RoughStripe {} };
+let c = Sphere { radius: 0.5, pos: vec3(1.1, 0.5, 0.0), material: RippleGlass {} };
+let scene = ground + a + b + c;
+"""
+    st = ft.parse_and_eval(src)
+    d = st.desc
+    assert any(d.materials[i].color_program >= 0 for i in range(d.n_materials))
+    opts = ft.RenderOptions(width=160, height=120, max_steps=256, max_dist=50.0, epsilon=1e-4, step_scale=0.7)
+    interp = {}
+    for depth in (1, 3):
+        lin, _ = ft.render_trace(st, opts, ft.AccelMode.Bvh, 1, depth)
+        ref, _, _ = oracle.render_trace(st, opts, 1, 1, depth, 32)
+        assert radiance_rmse(lin, ref) <= 1e-3, (depth, radiance_rmse(lin, ref))
+        interp[depth] = lin
+    # the stripes are visible: the hooked colours differ from the static ones
+    flat = ft.parse_and_eval(src.replace("fn color(ctx)", "fn unused_color(ctx)"))
+    lin_flat, _ = ft.render_trace(flat, opts, ft.AccelMode.Bvh, 1, 1)
+    assert radiance_rmse(interp[1], lin_flat) > 1e-2
+    st.gpu().jit()
+    for depth in (1, 3):
+        lin, _ = ft.render_trace(st, opts, ft.AccelMode.Bvh, 1, depth)
+        assert radiance_rmse(lin, interp[depth]) <= 1e-3, (depth, radiance_rmse(lin, interp[depth]))
