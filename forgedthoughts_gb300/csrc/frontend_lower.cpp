@@ -88,7 +88,7 @@ void set_bounds(ft_node& n, const Aabb& b) {
   n.bounds_max[0] = b.mx.x; n.bounds_max[1] = b.mx.y; n.bounds_max[2] = b.mx.z;
 }
 
-bool is_primitive(int k) { return k <= FT_NODE_EXTRUDE_POLYGON; }
+bool is_primitive(int k) { return k <= FT_NODE_EXTRUDE_POLYGON || k == FT_NODE_CUSTOM; }
 bool is_modifier(int k) { return k == FT_NODE_DOMAIN || k == FT_NODE_DISTANCE_POST || k == FT_NODE_NOISE; }
 bool is_binary(int k) { return k >= FT_NODE_UNION && k <= FT_NODE_TONGUE; }
 
@@ -239,7 +239,69 @@ class HookCompiler {
     return prog;
   }
 
- // A material hook `fn name(ctx)` (eval_material_function_with_overrides,
+ // A function of a block definition (an `sdf` definition's distance, domain
+  // or distance_post, eval_sdf_function_with_overrides, E:2960-3050): its
+  // parameters are registers (vec3 where param_vec3 says so), the
+  // definition's bindings (an instance field of the same name replacing one)
+  // constants, its helper functions callable.  want: 0 a number, 1 a vec3.
+  // Returns false, emitting nothing, when it does not fold to such a program.
+  bool compile_block_fn(const BlockStmt& fn, const BlockDef& def, const ObjectData& overrides,
+                        const std::vector<bool>& param_vec3, int want, ft_program* out) {
+    const size_t mark = code_.size();
+    first_ = static_cast<uint32_t>(mark);
+    nregs_ = 0;
+    what_ = "sdf";
+    block_ = &def;
+    try {
+      std::map<std::string, SVal> locals = block_scope(def, overrides);
+      ft_program prog{};
+      prog.first_instr = first_;
+      prog.n_params = static_cast<uint32_t>(fn.params.size());
+      for (size_t i = 0; i < fn.params.size(); ++i) {
+        locals[fn.params[i]] = reg(nregs_++, param_vec3[i]);
+        if (param_vec3[i]) prog.param_is_vec3 |= 1u << i;
+      }
+      SVal result = run_body(fn.body, locals, 0);
+      if (result.rec) fail("returns a record");
+      int r = materialize(result);
+      bool rv = reg_vec3(result);
+      if (rv != (want == 1) || nregs_ > FT_MAX_PROGRAM_REGS) {
+        code_.resize(mark);
+        return false;
+      }
+      ft_instr ret{};
+      ret.op = FT_OP_RET;
+      ret.a = static_cast<uint8_t>(r);
+      ret.flags = rv ? FT_INSTR_VEC3 : 0;
+      code_.push_back(ret);
+      prog.n_instr = static_cast<uint32_t>(code_.size()) - first_;
+      prog.n_regs = static_cast<uint32_t>(nregs_);
+      prog.result_is_vec3 = rv ? 1u : 0u;
+      *out = prog;
+      return true;
+    } catch (const FrontendError&) {
+      code_.resize(mark);
+      return false;
+    }
+  }
+
+  // A zero-argument function of a block definition folded to a constant
+  // (eval_sdf_zero_arg_function_with_overrides); false if it does not fold.
+  bool const_block_fn(const BlockStmt& fn, const BlockDef& def, const ObjectData& overrides, Value* out) {
+    what_ = "sdf";
+    block_ = &def;
+    try {
+      std::map<std::string, SVal> locals = block_scope(def, overrides);
+      SVal v = run_body(fn.body, locals, 0);
+      if (!v.is_const || v.rec) return false;
+      *out = v.cv;
+      return true;
+    } catch (const FrontendError&) {
+      return false;
+    }
+  }
+
+  // A material hook `fn name(ctx)` (eval_material_function_with_overrides,
   // E:2860-2940): the definition's bindings (an instance field of the same
   // name replacing one) are constants, `ctx` is the shading context record of
   // seven parameters (FT_MATERIAL_HOOK_PARAMS).  want: 0 a number, 1 a vec3,
@@ -253,13 +315,7 @@ class HookCompiler {
     what_ = "material";
     block_ = &def;
     try {
-      std::map<std::string, SVal> locals;
-      for (const auto& kv : overrides.fields) locals[kv.first] = cst(kv.second);
-      for (const BlockStmt& s : def.statements) {
-        if (s.kind != BlockStmt::Binding || !s.expr) continue;
-        const Value* ov = overrides.get(s.name);
-        locals[s.name] = ov ? cst(*ov) : eval(*s.expr, locals, 0);
-      }
+      std::map<std::string, SVal> locals = block_scope(def, overrides);
       static const char* const kFields[FT_MATERIAL_HOOK_PARAMS] = {
           "position", "local_position", "normal", "view_dir", "front_face", "object_id", "material_id"};
       SVal ctx;
@@ -326,6 +382,22 @@ class HookCompiler {
   }
 
  private:
+  // The scope of a block definition's functions: instance fields, then the
+  // bindings in order (an instance field of the same name replacing one);
+  // helper functions see the same bindings.
+  std::map<std::string, SVal> block_scope(const BlockDef& def, const ObjectData& overrides) {
+    std::map<std::string, SVal> locals;
+    for (const auto& kv : overrides.fields) locals[kv.first] = cst(kv.second);
+    block_locals_.clear();
+    for (const BlockStmt& s : def.statements) {
+      if (s.kind != BlockStmt::Binding || !s.expr) continue;
+      const Value* ov = overrides.get(s.name);
+      locals[s.name] = ov ? cst(*ov) : eval(*s.expr, locals, 0);
+      block_locals_[s.name] = locals[s.name];
+    }
+    return locals;
+  }
+
   const EvalState& st_;
   std::vector<ft_instr>& code_;
   uint32_t first_ = 0;
@@ -924,6 +996,7 @@ class Lowerer {
       case FT_NODE_DOMAIN:
       case FT_NODE_DISTANCE_POST:
       case FT_NODE_NOISE:
+      case FT_NODE_CUSTOM:
         return Aabb{v3(n.bounds_min[0], n.bounds_min[1], n.bounds_min[2]),
                     v3(n.bounds_max[0], n.bounds_max[1], n.bounds_max[2])};
       case FT_NODE_SUBTRACT: return bounds(n.a);
@@ -978,7 +1051,7 @@ class Lowerer {
   int split_modifier_base(int idx, Xf* xf, Aabb* bb) {
     *bb = bounds(idx);
     ft_node n = out_.nodes[idx];
-    if (is_primitive(n.kind) || n.kind == FT_NODE_NOISE) {
+    if ((is_primitive(n.kind) && n.kind != FT_NODE_CUSTOM) || n.kind == FT_NODE_NOISE) {
       *xf = node_xf(n);
       set_xf(n, Xf{});
       if (n.kind == FT_NODE_NOISE) set_bounds(n, *bb);
@@ -1042,6 +1115,7 @@ class Lowerer {
     ft_node n = out_.nodes[idx];
     if (is_primitive(n.kind)) {
       set_xf(n, map(node_xf(n)));
+      if (n.kind == FT_NODE_CUSTOM) set_custom_box(n);
       n.object_id = alloc_object_id();
       return push(n);
     }
@@ -1114,6 +1188,78 @@ class Lowerer {
         n.f[1] = number_or(o, {"minor_radius", "r"}, 0.25f);
         break;
     }
+    n.object_id = alloc_object_id();
+    n.material_id = primitive_material_id(o);
+    return push(n);
+  }
+
+  // World box of a Custom node: its half-extent box's corners through the
+  // transform (sdf_bounds, R:5304-5326).
+  static void set_custom_box(ft_node& n) {
+    const float inf = std::numeric_limits<float>::infinity();
+    Xf xf = node_xf(n);
+    Aabb box{v3(inf, inf, inf), v3(-inf, -inf, -inf)};
+    for (int c = 0; c < 8; ++c) {
+      V3 corner = v3((c & 4) ? n.f[0] : -n.f[0], (c & 2) ? n.f[1] : -n.f[1], (c & 1) ? n.f[2] : -n.f[2]);
+      V3 w = add(xf.c, transform_offset(xf, corner));
+      box.mn = v3(std::min(box.mn.x, w.x), std::min(box.mn.y, w.y), std::min(box.mn.z, w.z));
+      box.mx = v3(std::max(box.mx.x, w.x), std::max(box.mx.y, w.y), std::max(box.mx.z, w.z));
+    }
+    set_bounds(n, box);
+  }
+
+  // A user `sdf` definition as a Custom leaf (compile_sdf, R:1528-1550): its
+  // distance / domain / distance_post functions lowered to hook programs, the
+  // half extents of `bounds()` (eval_custom_sdf_bounds_half_extents,
+  // R:6182-6204: a vec3 or a radius, each at least 1e-3, else 10,000), the
+  // object's transform and material.  The world box is the transformed
+  // corners of the half-extent box (sdf_bounds, R:5304-5326).
+  int custom_sdf(const ObjectData& o, const BlockDef& def) {
+    ft_node n = blank(FT_NODE_CUSTOM);
+    Xf xf = read_transform(o);
+    set_xf(n, xf);
+    n.ival = n.reserved = -1;
+    auto find_fn = [&](const char* name, size_t nparams) -> const BlockStmt* {
+      for (const BlockStmt& st : def.statements)
+        if (st.kind == BlockStmt::Function && st.name == name && st.params.size() == nparams) return &st;
+      return nullptr;
+    };
+    auto lower_fn = [&](const BlockStmt* fn, const std::vector<bool>& vec, int want) -> int {
+      if (!fn) return -1;
+      HookCompiler hc(st_, out_.instrs);
+      ft_program prog;
+      if (!hc.compile_block_fn(*fn, def, o, vec, want, &prog)) return -2;
+      out_.programs.push_back(prog);
+      return static_cast<int>(out_.programs.size()) - 1;
+    };
+    n.program = lower_fn(find_fn("distance", 1), {true}, 0);
+    if (n.program < 0)
+      lower_fail(FT_ERR_UNSUPPORTED, "sdf '" + def.name + "': distance(p) must fold to a number program");
+    n.ival = lower_fn(find_fn("domain", 1), {true}, 1);
+    n.reserved = lower_fn(find_fn("distance_post", 2), {false, true}, 0);
+    if (n.ival == -2 || n.reserved == -2)
+      lower_fail(FT_ERR_UNSUPPORTED, "sdf '" + def.name + "': domain / distance_post hook cannot be lowered");
+    V3 half = v3(10000.0f, 10000.0f, 10000.0f);
+    if (const BlockStmt* bf = find_fn("bounds", 0)) {
+      HookCompiler hc(st_, out_.instrs);
+      Value bv;
+      if (hc.const_block_fn(*bf, def, o, &bv)) {
+        float t[3];
+        if (bv.kind == Value::Number) {
+          float r = std::max(std::fabs(bv.num), 1.0e-3f);
+          half = v3(r, r, r);
+        } else if (bv.kind == Value::Object) {
+          float x = 0.0f, y = 0.0f, z = 0.0f;
+          read_number(*bv.obj, {"x"}, &x);
+          read_number(*bv.obj, {"y"}, &y);
+          read_number(*bv.obj, {"z"}, &z);
+          half = v3(std::max(std::fabs(x), 1.0e-3f), std::max(std::fabs(y), 1.0e-3f), std::max(std::fabs(z), 1.0e-3f));
+          (void)t;
+        }
+      }
+    }
+    n.f[0] = half.x; n.f[1] = half.y; n.f[2] = half.z;
+    set_custom_box(n);
     n.object_id = alloc_object_id();
     n.material_id = primitive_material_id(o);
     return push(n);
@@ -1231,6 +1377,8 @@ class Lowerer {
         n.a = b;
         n.f[0] = required_number(o, "k", 0.0f);
         node = push(n);
+      } else if (st_.sdf_defs.count(t)) {
+        node = custom_sdf(o, *st_.sdf_defs.at(t));
       } else {
         lower_fail(FT_ERR_UNSUPPORTED_OBJECT, "unsupported object type '" + t + "' for rendering");
       }

@@ -140,6 +140,23 @@ struct Ctx {
 
 __device__ __forceinline__ float node_lb(F3 p, const float* mn, const float* mx) { return ftd::aabb_lb(p, mn, mx); }
 
+// eval_custom_sdf_distance (R:6139-6180) of a Custom node (a user `sdf`
+// definition): the point in its frame, through domain(p) when present, into
+// distance(p), then distance_post(d, p) when present.  The device node keeps
+// the distance program in `program`, domain in `ival`, distance_post in `b`.
+template <bool kStats>
+__device__ __noinline__ float custom_distance(const DevScene& S, const DevNode& n, F3 p, Ctx<kStats>& cx) {
+  cx.prim();
+  F3 q = ftd::to_local(p, n);
+  if (n.ival >= 0) q = scene_program(S, n.ival, &q, cx.hooks());
+  float d = scene_program(S, n.program, &q, cx.hooks()).x;
+  if (n.b >= 0) {
+    F3 args[2] = {f3(d, d, d), q};
+    d = scene_program(S, n.b, args, cx.hooks()).x;
+  }
+  return d;
+}
+
 // Generic leaf: postfix program over the leaf's node tree (exact).
 template <bool kStats>
 __device__ __noinline__ Info eval_generic(const DevScene& S, int first, int count, F3 p, Ctx<kStats>& cx) {
@@ -192,6 +209,7 @@ __device__ __noinline__ Info eval_generic(const DevScene& S, int first, int coun
         break;
       }
       case ftgpu::kGSmooth: vs[vsp - 1].d -= n.f[0] * 0.1f; break;
+      case ftgpu::kGCustom: vs[vsp++] = Info{custom_distance(S, n, ps[psp], cx), n.object_id, n.material_id}; break;
     }
   }
   return vs[0];
@@ -402,6 +420,17 @@ __device__ __forceinline__ Info eval_leaf(const DevScene& S, const DevLeaf& lf, 
     return Info{ftd::prim_distance(n, p), n.object_id, n.material_id};
   }
   if (lf.kind == ftgpu::kLeafUrTree) return eval_urtree(S, S.urtrees[lf.first], p, cutoff, cx);
+  if (S.nodes[lf.node].kind == FT_NODE_CUSTOM) {
+    // accel_leaf_distance_info (R:635-657): a Custom leaf farther from its box
+    // than a tenth of the box diagonal (clamped to [0.05, 0.5]) is that box
+    // bound, not its program
+    const DevNode& n = S.nodes[lf.node];
+    cx.box();
+    float lb = node_lb(p, lf.bmin, lf.bmax);
+    float ex = lf.bmax[0] - lf.bmin[0], ey = lf.bmax[1] - lf.bmin[1], ez = lf.bmax[2] - lf.bmin[2];
+    float far = ftd::rclamp(sqrtf(ex * ex + ey * ey + ez * ez) * 0.1f, 0.05f, 0.5f);
+    if (lb > far) return Info{lb, n.object_id, n.material_id};
+  }
   return eval_generic(S, lf.first, lf.count, p, cx);
 }
 

@@ -24,7 +24,8 @@ enum GenericOp : uint32_t {
   kGPop = 5,         // pop point (after a domain base)
   kGBinary = 6,      // combine the two top values with the node's operator
   kGSlice = 7,
-  kGSmooth = 8
+  kGSmooth = 8,
+  kGCustom = 9       // push a user `sdf` definition's distance at the current point
 };
 constexpr uint32_t kGOpShift = 27;
 constexpr uint32_t kGNodeMask = (1u << kGOpShift) - 1u;

@@ -288,6 +288,17 @@ __device__ F3 prim_normal(const DevNode& n, F3 p) {
   return ftd::len3(nn) > 1.0e-6f ? ftd::normalize3(nn) : f3(0.0f, 1.0f, 0.0f);
 }
 
+// estimate_node_normal (R:4554-4570) of a Custom node.
+__device__ F3 custom_normal(const DevScene& S, const DevNode& n, F3 p) {
+  const float e = kNormalEps;
+  Ctx<false> cx;
+  cx.c = Counters{};
+  F3 k1 = f3(1.0f, -1.0f, -1.0f), k2 = f3(-1.0f, -1.0f, 1.0f), k3 = f3(-1.0f, 1.0f, -1.0f), k4 = f3(1.0f, 1.0f, 1.0f);
+  F3 nn = k1 * custom_distance(S, n, p + k1 * e, cx) + k2 * custom_distance(S, n, p + k2 * e, cx) +
+          k3 * custom_distance(S, n, p + k3 * e, cx) + k4 * custom_distance(S, n, p + k4 * e, cx);
+  return ftd::len3(nn) > 1.0e-6f ? ftd::normalize3(nn) : f3(0.0f, 1.0f, 0.0f);
+}
+
 // Result of resolving a hit against the tree: geometric normal (not yet
 // oriented to the front face), material, and the optional root split.
 struct Resolved {
@@ -324,7 +335,7 @@ __device__ __noinline__ void resolve_generic(const DevScene& S, int root, F3 p, 
   for (int walk = 0; top >= 0 && walk < ftgpu::kMaxWalk; ++walk) {  // each node is visited once
     int ni = node_stack[top];
     const DevNode& n = S.nodes[ni];
-    bool is_prim = n.kind <= FT_NODE_EXTRUDE_POLYGON;
+    bool is_prim = n.kind <= FT_NODE_EXTRUDE_POLYGON || n.kind == FT_NODE_CUSTOM;
     bool unary = n.kind == FT_NODE_DOMAIN || n.kind == FT_NODE_DISTANCE_POST || n.kind == FT_NODE_NOISE ||
                  n.kind == FT_NODE_SLICE || n.kind == FT_NODE_SMOOTH;
     int nchild = is_prim ? 0 : (unary ? 1 : 2);
@@ -339,8 +350,13 @@ __device__ __noinline__ void resolve_generic(const DevScene& S, int root, F3 p, 
     }
     GEntry e;
     if (is_prim) {
-      e.d = ftd::prim_distance(n, p);
-      e.n = prim_normal(n, p);
+      if (n.kind == FT_NODE_CUSTOM) {
+        e.d = custom_distance(S, n, p, cx);
+        e.n = custom_normal(S, n, p);
+      } else {
+        e.d = ftd::prim_distance(n, p);
+        e.n = prim_normal(n, p);
+      }
       e.m = mat_of_leaf(S, n, hc);
     } else if (n.kind == FT_NODE_DOMAIN || n.kind == FT_NODE_DISTANCE_POST || n.kind == FT_NODE_NOISE) {
       GEntry base = st[--sp];

@@ -56,7 +56,7 @@ class Builder {
     for (uint32_t i = 0; i < d_.n_nodes; ++i) node_bounds(static_cast<int>(i));
     // Primitive nodes carry their culling box in bmin/bmax.
     for (uint32_t i = 0; i < d_.n_nodes; ++i) {
-      if (is_prim(d_.nodes[i].kind)) {
+      if (is_prim(d_.nodes[i].kind) || d_.nodes[i].kind == FT_NODE_CUSTOM) {
         std::memcpy(img_->nodes[i].bmin, bounds_[i].mn, sizeof(float) * 3);
         std::memcpy(img_->nodes[i].bmax, bounds_[i].mx, sizeof(float) * 3);
       }
@@ -148,6 +148,20 @@ class Builder {
           return fail("distance_post hook must map (f32, vec3) -> f32");
       }
       if (n.kind == FT_NODE_SLICE && (n.ival < 0 || n.ival > 2)) return fail("slice axis out of range");
+      if (n.kind == FT_NODE_CUSTOM) {
+        // distance(p) -> f32, domain(p) -> vec3, distance_post(d, p) -> f32
+        auto prog_ok = [&](int32_t idx, uint32_t np, uint32_t vec_mask, bool vec_result, bool required) {
+          if (idx < 0) return !required;
+          if (static_cast<uint32_t>(idx) >= d_.n_programs) return false;
+          const ft_program& p = d_.programs[idx];
+          return p.n_params == np && p.param_is_vec3 == vec_mask && (p.result_is_vec3 != 0) == vec_result;
+        };
+        if (!prog_ok(n.program, 1, 1u, false, true) || !prog_ok(n.ival, 1, 1u, true, false) ||
+            !prog_ok(n.reserved, 2, 2u, false, false))
+          return fail("custom sdf node " + std::to_string(i) + " has an invalid program");
+        if (!(n.f[0] > 0.0f && n.f[1] > 0.0f && n.f[2] > 0.0f))
+          return fail("custom sdf node " + std::to_string(i) + " has invalid bounds");
+      }
     }
     if (d_.environment_program >= 0) {
       if (static_cast<uint32_t>(d_.environment_program) >= d_.n_programs)
@@ -218,6 +232,10 @@ class Builder {
       std::memcpy(n.f, s.f, sizeof(n.f));
       std::memcpy(n.bmin, s.bounds_min, sizeof(n.bmin));
       std::memcpy(n.bmax, s.bounds_max, sizeof(n.bmax));
+      if (s.kind == FT_NODE_CUSTOM) {  // a leaf: program distance, ival domain, b distance_post
+        n.a = -1;
+        n.b = s.reserved;
+      }
     }
   }
 
@@ -241,6 +259,7 @@ class Builder {
       case FT_NODE_DOMAIN:
       case FT_NODE_DISTANCE_POST:
       case FT_NODE_NOISE:
+      case FT_NODE_CUSTOM:
         std::memcpy(b.mn, n.bounds_min, sizeof(b.mn));
         std::memcpy(b.mx, n.bounds_max, sizeof(b.mx));
         break;
@@ -341,6 +360,11 @@ class Builder {
     if (static_cast<uint32_t>(i) > kGNodeMask) return fail("scene has too many nodes for the generic evaluator");
     if (is_prim(n.kind)) {
       op(kGPrim);
+      *vmax = std::max(*vmax, vdepth + 1);
+      return true;
+    }
+    if (n.kind == FT_NODE_CUSTOM) {
+      op(kGCustom);
       *vmax = std::max(*vmax, vdepth + 1);
       return true;
     }

@@ -105,7 +105,10 @@ typedef enum ft_node_kind {
   FT_NODE_TONGUE = 27,         /* f0 ra, f1 rb */
   FT_NODE_SLICE = 28,          /* a base, ival axis, f0 min, f1 max */
   FT_NODE_SMOOTH = 29,         /* a base, f0 k */
-  FT_NODE_KIND_COUNT = 30
+  FT_NODE_CUSTOM = 30,         /* user `sdf` definition (SdfNode::Custom, R:213-220): program = distance(p),
+                                  ival = domain(p) program or -1, reserved = distance_post(d, p) program or
+                                  -1, f0..f2 bounds() half extents, transform, bounds = world box; no children */
+  FT_NODE_KIND_COUNT = 31
 } ft_node_kind;
 
 typedef struct ft_node {

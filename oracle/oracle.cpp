@@ -248,6 +248,7 @@ class Scene {
       case FT_NODE_DOMAIN:
       case FT_NODE_DISTANCE_POST:
       case FT_NODE_NOISE:
+      case FT_NODE_CUSTOM:  // the lowering stores the transformed half-extent box (R:5304-5326)
         return Aabb<R>{mk(R(n.bounds_min[0]), R(n.bounds_min[1]), R(n.bounds_min[2])),
                        mk(R(n.bounds_max[0]), R(n.bounds_max[1]), R(n.bounds_max[2]))};
       case FT_NODE_SUBTRACT: return bounds(n.a);
@@ -310,6 +311,10 @@ class Scene {
   R lower_bound(int idx, V<R> p) const {
     const ft_node& n = node(idx);
     if (n.kind <= FT_NODE_EXTRUDE_POLYGON) return prim_distance(n, p);
+    if (n.kind == FT_NODE_CUSTOM) {  // the half-extent box in the node's frame (R:5506-5515)
+      V<R> h = mk(R(n.f[0]), R(n.f[1]), R(n.f[2]));
+      return point_aabb_lb(to_local(p, n), Aabb<R>{h * R(-1), h});
+    }
     switch (n.kind) {
       case FT_NODE_UNION: return rmin(lower_bound(n.a, p), lower_bound(n.b, p));
       case FT_NODE_INTERSECT: return rmax(lower_bound(n.a, p), lower_bound(n.b, p));
@@ -393,6 +398,23 @@ class Scene {
   Info<R> info(int idx, V<R> p) const {
     const ft_node& n = node(idx);
     if (n.kind <= FT_NODE_EXTRUDE_POLYGON) return Info<R>{prim_distance(n, p), n.object_id, n.material_id};
+    if (n.kind == FT_NODE_CUSTOM) {
+      // eval_custom_sdf_distance (R:6139-6180): domain, distance, distance_post
+      V<R> q = to_local(p, n), t;
+      if (n.ival >= 0) {
+        run_program(n.ival, &q, &t);
+        q = t;
+      }
+      V<R> o;
+      run_program(n.program, &q, &o);
+      R d = o.x;
+      if (n.reserved >= 0) {
+        V<R> args[2] = {mk(d, d, d), q};
+        run_program(n.reserved, args, &o);
+        d = o.x;
+      }
+      return Info<R>{d, n.object_id, n.material_id};
+    }
     switch (n.kind) {
       case FT_NODE_DOMAIN: {
         V<R> q = to_local(p, n), out;
@@ -569,8 +591,17 @@ struct Accel {
     return static_cast<int>(bvh.size()) - 1;
   }
 
-  // accel_leaf_distance_info (R:635-657); Custom leaves are not in the IR.
-  Info<R> leaf_info(const Leaf<R>& l, V<R> p) const { return scene.info(l.node, p); }
+  // accel_leaf_distance_info (R:635-657): a Custom leaf farther from its box
+  // than a tenth of the box diagonal (clamped to [0.05, 0.5]) is that bound.
+  Info<R> leaf_info(const Leaf<R>& l, V<R> p) const {
+    const ft_node& n = scene.node(l.node);
+    if (n.kind == FT_NODE_CUSTOM) {
+      R lb = point_aabb_lb(p, l.bounds);
+      R far = rclamp(len(l.bounds.mx - l.bounds.mn) * R(0.1), R(0.05), R(0.5));
+      if (lb > far) return Info<R>{lb, n.object_id, n.material_id};
+    }
+    return scene.info(l.node, p);
+  }
 
   // bvh_distance_info (R:743-786)
   bool bvh_info(int ni, V<R> p, R& best, Info<R>& out) const {
@@ -1309,7 +1340,7 @@ class Tracer {
   // resolve_surface_normal_from_node (R:4462-4527) / blend_surface_normals (R:4529-4552)
   bool surface_normal(int idx, V<R> p, R eps, V<R>* out) const {
     const ft_node& n = S.node(idx);
-    if (n.kind <= FT_NODE_NOISE) {  // primitives and modifiers
+    if (n.kind <= FT_NODE_NOISE || n.kind == FT_NODE_CUSTOM) {  // primitives, Custom and modifiers
       *out = node_normal(idx, p, eps);
       return true;
     }
@@ -1392,7 +1423,7 @@ class Tracer {
   // resolve_material_from_node (R:6945-7050) / blend_node_materials (R:7093-7113)
   bool material_from_node(int idx, V<R> p, const HookCtx& hc, Mat<R>* out) const {
     const ft_node& n = S.node(idx);
-    if (n.kind <= FT_NODE_EXTRUDE_POLYGON) {
+    if (n.kind <= FT_NODE_EXTRUDE_POLYGON || n.kind == FT_NODE_CUSTOM) {
       *out = leaf_material(n, hc);
       return true;
     }

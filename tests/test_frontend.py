@@ -274,3 +274,102 @@ def test_material_hooks_reference_known_answers(material, kind):
         assert abs(oracle.eval_program(st, m.ior_program, thin)[0, 0] - 1.6) < 1e-6
         assert oracle.eval_program(st, m.thin_walled_program, solid)[0, 0] < 0.5
         assert oracle.eval_program(st, m.thin_walled_program, thin)[0, 0] >= 0.5
+
+
+# The reference's custom sdf test sources (lib.rs tests
+# evaluates_custom_sdf_distance_with_helper_functions,
+# supports_programmable_sdf_domain_and_distance_post_hooks,
+# jits_vec3_box_style_sdf_distance), with bounds() added where they have none.
+CUSTOM_SDFS = """
+sdf SoftBlob {
+  let warp_scale = 0.25;
+  fn bounds() {
+    return vec3(1.2, 1.2, 1.2);
+  }
+  fn warp(p) {
+    return vec3(p.x, p.y + sin(p.x * 3.0) * warp_scale, p.z);
+  }
+  fn distance(p) {
+    let q = warp(p);
+    return length(q) - 1.0;
+  }
+};
+sdf TwistedShell {
+  let radius = 0.5;
+  let thickness = 0.05;
+  fn bounds() {
+    return 0.6;
+  }
+  fn domain(p) {
+    return rotate_y(p, p.y * 90.0);
+  }
+  fn distance(p) {
+    return length(p) - radius;
+  }
+  fn distance_post(d, p) {
+    return abs(d) - thickness;
+  }
+};
+sdf ShellBox {
+  let width = 1.6;
+  let height = 2.0;
+  let depth = 0.6;
+  let wall_thickness = 0.05;
+  fn bounds() {
+    return vec3(0.8, 1.0, 0.3);
+  }
+  fn sd_box(p, half_size) {
+    let q = abs(p) - half_size;
+    let outside = length(max(q, vec3(0.0)));
+    let inside = min(max(q.x, max(q.y, q.z)), 0.0);
+    return outside + inside;
+  }
+  fn distance(p) {
+    let half_outer = vec3(width * 0.5, height * 0.5, depth * 0.5);
+    let outer = sd_box(p, half_outer);
+    let inner_half = max(half_outer - vec3(wall_thickness, wall_thickness, wall_thickness), vec3(0.001));
+    let cavity = sd_box(vec3(p.x, p.y, p.z - wall_thickness), inner_half);
+    return max(outer, -cavity);
+  }
+};
+"""
+
+CUSTOM_SCENE = CUSTOM_SDFS + """
+let camera = Camera { origin: vec3(0.0, 1.5, -6.0), target: vec3(0.0, 0.8, 0.0), fov_y: 45.0 };
+let light = PointLight { position: vec3(3.0, 6.0, -3.0), intensity: 60.0 };
+let ground = Box { size: vec3(20.0, 1.0, 20.0), pos: vec3(0.0, -0.5, 0.0) };
+let blob = SoftBlob { pos: vec3(-1.8, 1.2, 0.0), material: Lambert { color: vec3(0.8, 0.3, 0.2) } };
+let shell = TwistedShell { pos: vec3(0.0, 0.6, -0.5), rot: vec3(0.0, 30.0, 0.0), material: Metal { roughness: 0.1 } };
+let box = ShellBox { pos: vec3(1.8, 1.0, 0.5), rot: vec3(0.0, -20.0, 0.0) };
+let scene = ground + blob + shell + box;
+"""
+
+
+def test_custom_sdf_definitions_lower_to_programs():
+    """User `sdf` definitions become Custom leaves (R:1528-1550): the
+    reference's known answer (lib.rs, evaluates_custom_sdf_distance_with_
+    helper_functions: distance(0, 1, 0) is exactly 0, bounds x is 1.2), the
+    domain and distance_post hooks, vec3 helper functions, and the world box
+    of the rotated half extents (sdf_bounds, R:5304-5326)."""
+    st = ft.parse_and_eval(CUSTOM_SCENE)
+    d = st.desc
+    custom = [_native.NodeC.from_buffer_copy(d.nodes[i]) for i in range(d.n_nodes) if d.nodes[i].kind == 30]
+    assert len(custom) == 3
+    blob, shell, box = custom
+    assert oracle.eval_program(st, blob.program, np.array([[[0.0, 1.0, 0.0]]], np.float32))[0, 0] == 0.0
+    assert blob.f[0] == np.float32(1.2) and blob.ival < 0 and blob.reserved < 0
+    assert shell.ival >= 0 and shell.reserved >= 0 and shell.f[0] == np.float32(0.6)
+    # TwistedShell at its local point (0.5, 0, 0): |p| - 0.5 = 0, post abs(0) - 0.05
+    q = oracle.eval_program(st, shell.ival, np.array([[[0.5, 0.0, 0.0]]], np.float32))[0]
+    assert np.allclose(q, (0.5, 0.0, 0.0), atol=1e-6)
+    post = oracle.eval_program(st, shell.reserved, np.array([[[0.0, 0.0, 0.0], [0.5, 0.0, 0.0]]], np.float32))
+    assert abs(post[0, 0] + 0.05) < 1e-7
+    # ShellBox wall: 0.05 inside the outer x face, well inside the cavity's z
+    assert abs(oracle.eval_program(st, box.program, np.array([[[0.75, 0.0, 0.0]]], np.float32))[0, 0]) < 1e-6
+    # rotated by -20 degrees about y: the world box holds the rotated corners
+    c, s = np.cos(np.radians(20.0)), np.sin(np.radians(20.0))
+    half_x = 0.8 * c + 0.3 * s
+    assert abs((box.bounds_max[0] - box.bounds_min[0]) / 2 - half_x) < 1e-5
+    # an sdf without distance(p) is refused
+    with pytest.raises(ft.RenderError, match="distance"):
+        ft.parse_and_eval("sdf Empty { fn bounds() { return 1.0; } };\nlet scene = Empty {};\n")

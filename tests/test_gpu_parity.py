@@ -269,3 +269,43 @@ let scene = ground + a + b + c;
     for depth in (1, 3):
         lin, _ = ft.render_trace(st, opts, ft.AccelMode.Bvh, 1, depth)
         assert radiance_rmse(lin, interp[depth]) <= 1e-3, (depth, radiance_rmse(lin, interp[depth]))
+
+
+@pytest.mark.parametrize("accel", [ft.AccelMode.Naive, ft.AccelMode.Bvh, ft.AccelMode.Bricks])
+def test_gpu_custom_sdf_depth(accel):
+    """User `sdf` definitions (helper functions, domain and distance_post
+    hooks, vec3 helpers, rotated bounds, the far-box rule of Custom leaves):
+    depth against the f32 and f64 oracle."""
+    from test_frontend import CUSTOM_SCENE
+
+    st = ft.parse_and_eval(CUSTOM_SCENE)
+    opts = ft.RenderOptions(width=160, height=120, max_steps=256, max_dist=50.0, epsilon=1e-4, step_scale=0.7)
+    img = ft.render_depth(st, opts, accel, 1, want_material=True)
+    assert 0.3 < img.mask.mean() < 0.95
+    for prec in (32, 64):
+        t, m, mat, _, _ = oracle.render_depth(st, opts, int(accel), 1, prec)
+        assert_depth_parity(img.t, img.mask, t, m, f"custom sdf f{prec}")
+    both = (img.mask == 1) & (m == 1)
+    assert (img.material[both] == mat[both]).mean() >= 0.999
+
+
+def test_gpu_trace_custom_sdf():
+    """Whitted radiance of the custom sdf scene against the f32 oracle, with
+    the interpreter and with the run-time compiled kernels."""
+    from test_frontend import CUSTOM_SCENE
+
+    st = ft.parse_and_eval(CUSTOM_SCENE)
+    opts = ft.RenderOptions(width=160, height=120, max_steps=256, max_dist=50.0, epsilon=1e-4, step_scale=0.7)
+    interp = {}
+    for depth in (1, 2):
+        lin, _ = ft.render_trace(st, opts, ft.AccelMode.Bvh, 1, depth)
+        ref, _, _ = oracle.render_trace(st, opts, 1, 1, depth, 32)
+        assert radiance_rmse(lin, ref) <= 1e-3, (depth, radiance_rmse(lin, ref))
+        interp[depth] = lin
+    st.gpu().jit()
+    depth_jit = ft.render_depth(st, opts, ft.AccelMode.Bvh, 1)
+    t, m, _, _, _ = oracle.render_depth(st, opts, 1, 1, 32)
+    assert_depth_parity(depth_jit.t, depth_jit.mask, t, m, "custom sdf, compiled kernels")
+    for depth in (1, 2):
+        lin, _ = ft.render_trace(st, opts, ft.AccelMode.Bvh, 1, depth)
+        assert radiance_rmse(lin, interp[depth]) <= 1e-3, (depth, radiance_rmse(lin, interp[depth]))
