@@ -309,3 +309,28 @@ def test_gpu_trace_custom_sdf():
     for depth in (1, 2):
         lin, _ = ft.render_trace(st, opts, ft.AccelMode.Bvh, 1, depth)
         assert radiance_rmse(lin, interp[depth]) <= 1e-3, (depth, radiance_rmse(lin, interp[depth]))
+
+
+def test_gpu_trace_material_hooks_in_union_round():
+    """Hooked materials blended by a union_round tree (the tree resolve walk
+    evaluates each primitive's hooks in its own frame; an instance field
+    overrides a binding): Whitted radiance against the f32 oracle."""
+    from test_frontend import HOOK_MATERIALS
+
+    src = HOOK_MATERIALS + """
+let camera = Camera { origin: vec3(0.0, 1.0, -4.0), target: vec3(0.0, 0.5, 0.0), fov_y: 45.0 };
+let light = PointLight { position: vec3(3.0, 6.0, -3.0), intensity: 60.0 };
+let ground = Box { size: vec3(20.0, 1.0, 20.0), pos: vec3(0.0, -0.5, 0.0) };
+let s0 = Sphere { radius: 0.45, pos: vec3(-0.9, 0.5, 0.0), material: Stripe {} };
+let s1 = Sphere { radius: 0.45, pos: vec3(-0.3, 0.6, 0.1), material: RoughStripe {} };
+let s2 = Sphere { radius: 0.45, pos: vec3(0.3, 0.5, 0.0), material: Stripe { warm: vec3(0.2, 0.8, 0.3) } };
+let s3 = Sphere { radius: 0.45, pos: vec3(0.9, 0.6, -0.1), material: RoughStripe {} };
+let blob = s0.union_round(s1, 0.3).union_round(s2.union_round(s3, 0.3), 0.3);
+let scene = ground + blob;
+"""
+    st = ft.parse_and_eval(src)
+    opts = ft.RenderOptions(width=160, height=120, max_steps=256, max_dist=50.0, epsilon=1e-4, step_scale=0.7)
+    for depth in (1, 2):
+        lin, _ = ft.render_trace(st, opts, ft.AccelMode.Bvh, 1, depth)
+        ref, _, _ = oracle.render_trace(st, opts, 1, 1, depth, 32)
+        assert radiance_rmse(lin, ref) <= 1e-3, (depth, radiance_rmse(lin, ref))
