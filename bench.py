@@ -272,6 +272,19 @@ class Renderer:
         return s
 
 
+def replica_throughput(total_ms: float, items: int, steps: int, world: int, dist=None, device="cpu"):
+    """Whole-job throughput of `world` replicas: the slowest rank's time (a
+    MAX all-reduce when `dist` is given) and every rank's primary samples.
+    Returns (total ms, Mrays/s)."""
+    import torch
+
+    if dist is not None:
+        tt = torch.tensor([float(total_ms)], dtype=torch.float64, device=device)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total_ms = float(tt.item())
+    return total_ms, items * steps * world / (total_ms * 1e-3) / 1e6
+
+
 def _time_steps(fn, steps: int, stream, flush) -> list[float]:
     import torch
 
@@ -672,13 +685,8 @@ def main() -> None:
     if dist:
         dist.barrier()
     clk = clocks.stop()
-    total_ms = sum(step_ms)
-    if dist:
-        tt = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total_ms = float(tt.item())
+    total_ms, value = replica_throughput(sum(step_ms), items, args.steps, world, dist, dev)
     ms_per_step = total_ms / args.steps
-    value = items * args.steps * world / (total_ms * 1e-3) / 1e6
 
     peak = ctypes.c_double(0.0)
     if lib.ft_measure_fp32_peak(ctypes.byref(peak)) != 0:
