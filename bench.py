@@ -725,7 +725,7 @@ def main() -> None:
         fp16["speedup_vs_plain_fp32"] = fp16["value"] / plain["value"]
         line["depth_march_fp16_bricks"] = fp16
     if rank == 0 and not args.no_forms:
-        # the north-star's three chosen forms beside the plain method
+        # the precision, batching and differentiation forms beside the plain method
         forms = {}
         for name, fn in (("precision_fp16_bricks_and_jit", precision_form), ("batched", batched_form),
                          ("differentiation", lambda: differentiation_form(args.adam_steps))):

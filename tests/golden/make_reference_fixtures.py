@@ -3,7 +3,7 @@
 The reference pins its renderer with 96x96 regression PNGs rendered from small
 `.ft` scenes (crates/forgedthoughts/tests/render_regression.rs:27-107) and its
 front-end with parse/eval error fixtures (crates/forgedthoughts/tests/
-golden.rs:9-53).  The GPU machine has no copy of the reference, so the fixtures
+golden.rs:9-53).  Machines that run the tests have no copy of the reference, so the fixtures
 travel with the tests.  Run from the repository root:
 
     python tests/golden/make_reference_fixtures.py /path/to/reference

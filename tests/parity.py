@@ -1,7 +1,7 @@
 """Shared parity metrics: GPU results against the CPU oracle."""
 import numpy as np
 
-DEPTH_TOL = 1e-4        # scene units (spec depth tolerance)
+DEPTH_TOL = 1e-4        # scene units (the benchmark's depth tolerance)
 MASK_AGREEMENT = 0.999  # fraction of samples with identical hit/miss
 
 
