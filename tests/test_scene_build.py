@@ -64,3 +64,75 @@ def test_bad_child_index_is_rejected():
     bad.nodes = ctypes.cast(nodes, ctypes.POINTER(_native.NodeC))
     rc, _ = build_info(ctypes.pointer(bad))
     assert rc == _native.FT_ERR_INVALID_ARGUMENT and "child" in _native.last_error()
+
+
+def _with_materials(st, mutate):
+    d = st.desc
+    mats = (_native.MaterialC * d.n_materials)()
+    ctypes.memmove(mats, d.materials, ctypes.sizeof(mats))
+    mutate(mats, d)
+    bad = _native.SceneDescC.from_buffer_copy(d)
+    bad.materials = ctypes.cast(mats, ctypes.POINTER(_native.MaterialC))
+    return build_info(ctypes.pointer(bad))
+
+
+def test_material_hook_programs_are_validated():
+    """A material hook program must exist and map the shading context to a
+    colour (colour hook) or a number (the others)."""
+    from test_frontend import HOOK_MATERIALS
+
+    st = ft.parse_and_eval(HOOK_MATERIALS + "let scene = Sphere { material: Stripe {} } + "
+                           "Sphere { pos: vec3(3.0, 0.0, 0.0), material: RoughStripe {} };\n")
+    rc, _ = build_info(st.desc_ptr)
+    assert rc == 0
+
+    def bad_index(mats, d):
+        for i in range(d.n_materials):
+            if mats[i].color_program >= 0:
+                mats[i].color_program = d.n_programs + 5
+
+    rc, _ = _with_materials(st, bad_index)
+    assert rc == _native.FT_ERR_INVALID_ARGUMENT and "hook program" in _native.last_error()
+
+    def colour_as_roughness(mats, d):
+        for i in range(d.n_materials):
+            if mats[i].color_program >= 0:
+                mats[i].roughness_program = mats[i].color_program  # returns a vec3
+
+    rc, _ = _with_materials(st, colour_as_roughness)
+    assert rc == _native.FT_ERR_INVALID_ARGUMENT and "number" in _native.last_error()
+
+
+def test_custom_sdf_nodes_are_validated():
+    """A Custom node needs a distance program mapping vec3 to a number,
+    optional domain / distance_post programs of the right shape and positive
+    bounds."""
+    from test_frontend import CUSTOM_SCENE
+
+    st = ft.parse_and_eval(CUSTOM_SCENE)
+    d = st.desc
+    rc, info = build_info(st.desc_ptr)
+    assert rc == 0 and info.generic_leaves == 3
+
+    def mutated(fn):
+        nodes = (_native.NodeC * d.n_nodes)()
+        ctypes.memmove(nodes, d.nodes, ctypes.sizeof(nodes))
+        for i in range(d.n_nodes):
+            if nodes[i].kind == 30 and nodes[i].ival >= 0:
+                fn(nodes[i])
+                break
+        bad = _native.SceneDescC.from_buffer_copy(d)
+        bad.nodes = ctypes.cast(nodes, ctypes.POINTER(_native.NodeC))
+        return build_info(ctypes.pointer(bad))
+
+    for fn in (lambda n: setattr(n, "program", n.ival),      # distance returning a vec3
+               lambda n: setattr(n, "reserved", n.program),  # distance_post with one parameter
+               lambda n: setattr(n, "program", -1)):         # no distance
+        rc, _ = mutated(fn)
+        assert rc == _native.FT_ERR_INVALID_ARGUMENT and "custom sdf" in _native.last_error()
+
+    def no_bounds(n):
+        n.f[0] = 0.0
+
+    rc, _ = mutated(no_bounds)
+    assert rc == _native.FT_ERR_INVALID_ARGUMENT and "bounds" in _native.last_error()
