@@ -321,7 +321,9 @@ def _depth_figures(lib, scene, w, dev, stream, flush, peak: float, flags: int) -
     d_ms = _time_steps(d, 20, stream, flush)
     dk_ms = statistics.mean(_time_steps(lambda: d(full_outputs=False), 10, stream, flush))
     dl = _kernel_roofline(d, dk_ms, peak, "march_depth_persistent")
-    dl["traffic"] = _traffic("march_depth_persistent" + ("_fp16_bricks" if flags else ""), w)
+    dl["traffic"], note = _traffic_summary("march_depth_persistent" + ("_fp16_bricks" if flags else ""), w)
+    if note:
+        dl["traffic_source"] = note
     s = d.stats()
     dl["counts"]["far_steps"] = s.far_steps
     dl["counts"]["brick_fetches"] = s.brick_fetches
@@ -551,16 +553,21 @@ def differentiation_form(adam_steps: int = 200, reps: int = 3) -> dict:
                      "param_rmse_to_target_init": err0, "param_rmse_to_target_final": err1}}
 
 
-def _traffic(kernel: str, w) -> int | None:
-    """Per-launch DRAM bytes of the dominant kernel from a committed ncu summary."""
+def _traffic_summary(kernel: str, w) -> tuple:
+    """Per-launch DRAM bytes of a kernel from its committed ncu summary, and
+    the summary's own note on the state it was captured in (None, None when
+    there is no summary for this workload)."""
     prof = ROOT / "profiles" / f"{kernel}_traffic.txt"
     if not prof.exists() or not w.name.startswith("union_round512"):
-        return None
+        return None, None
     full = w.options.width * w.options.height * w.aa
-    for ln in prof.read_text().splitlines():
+    lines = prof.read_text().splitlines()
+    state = next((ln[2:].strip() for ln in lines if ln.startswith("# State captured:")), None)
+    for ln in lines:
         if ln.startswith(f"bytes_per_full_launch[{full}]:"):
-            return int(ln.split(":", 1)[1])
-    return None
+            return int(ln.split(":", 1)[1]), state
+    return None, None
+
 
 
 def _e2e(lib, st, w, mode: str, steps: int):
@@ -698,7 +705,9 @@ def main() -> None:
     kernel = "wavefront_trace" if args.mode == "trace" else "march_depth_persistent"
     kernel_ms = statistics.mean(_time_steps(lambda: r(full_outputs=False), max(args.steps // 2, 3), stream, flush))
     roofline = _kernel_roofline(r, kernel_ms, peak.value, kernel)
-    roofline["traffic"] = _traffic(kernel, w)
+    roofline["traffic"], note = _traffic_summary(kernel, w)
+    if note:
+        roofline["traffic_source"] = note
 
     _log("roofline done; end-to-end steps")
     line = {
