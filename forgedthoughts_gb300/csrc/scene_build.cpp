@@ -22,6 +22,9 @@
 namespace ftgpu {
 namespace {
 
+// Edge, in cells, of the blocks the candidate grid is built in.
+constexpr int kGridBlock = 4;
+
 struct Box {
   float mn[3], mx[3];
 };
@@ -548,71 +551,140 @@ class Builder {
     std::memcpy(t.dims, dims, sizeof(dims));
     t.cell_first = static_cast<int32_t>(img_->ur_cell_offsets.size());
     const double pad = double(t.cell) * 1.0e-3;
-    // Cells are independent: z-slabs are built on worker threads and
-    // concatenated in cell order.  Each list is sorted by its box gap so the
-    // device meets the likely nearest primitive first and prunes the rest.
-    const int nz = dims[2];
-    std::vector<std::vector<uint32_t>> slab_offsets(nz);
-    std::vector<std::vector<int32_t>> slab_prims(nz);
-    std::vector<std::vector<float>> slab_gaps(nz);
-    auto work = [&](int z) {
-      std::vector<std::pair<double, int32_t>> cand;
-      cand.reserve(64);
-      auto& offs = slab_offsets[z];
-      auto& prims = slab_prims[z];
-      auto& gaps = slab_gaps[z];
-      for (int y = 0; y < dims[1]; ++y)
-        for (int x = 0; x < dims[0]; ++x) {
-          double mn[3], mx[3];
-          int idx[3] = {x, y, z};
-          for (int a = 0; a < 3; ++a) {
-            mn[a] = double(t.gmin[a]) + double(idx[a]) * double(t.cell) - pad;
-            mx[a] = double(t.gmin[a]) + double(idx[a] + 1) * double(t.cell) + pad;
-          }
-          double min_ub = std::numeric_limits<double>::infinity();
-          for (int k = 0; k < np; ++k) {
-            double fx = std::max(std::fabs(double(cx[k]) - mn[0]), std::fabs(double(cx[k]) - mx[0]));
-            double fy = std::max(std::fabs(double(cy[k]) - mn[1]), std::fabs(double(cy[k]) - mx[1]));
-            double fz = std::max(std::fabs(double(cz[k]) - mn[2]), std::fabs(double(cz[k]) - mx[2]));
-            double far = std::sqrt(fx * fx + fy * fy + fz * fz);
-            double u = rho[k] >= 0.0f ? far - rho[k] : far + 2.0 * rad[k];
-            min_ub = std::min(min_ub, u);
-          }
-          // slack of 1e-5 keeps float rounding of the device-side bound on the safe side
-          double thr = std::max(double(t.r), min_ub) * (1.0 + 1e-5) + 1e-6;
-          double thr2 = thr * thr;
-          cand.clear();
-          for (int k = 0; k < np; ++k) {
-            double g2 = 0.0;
-            for (int a = 0; a < 3; ++a) {
-              double gap = std::max({0.0, double(pb[k].mn[a]) - mx[a], mn[a] - double(pb[k].mx[a])});
-              g2 += gap * gap;
-            }
-            if (g2 < thr2) cand.emplace_back(g2, k);
-          }
-          std::sort(cand.begin(), cand.end());
-          offs.push_back(static_cast<uint32_t>(prims.size()));
-          for (const auto& c : cand) {
-            prims.push_back(c.second);
-            // Points of the cell are at least pad inside the padded box, so
-            // the device's float box bound of any of them exceeds this value.
-            gaps.push_back(std::nextafter(static_cast<float>(std::sqrt(c.first) * (1.0 - 1e-6)), 0.0f));
-          }
-        }
+    const double half = 0.5 * double(t.cell);
+    // Absolute rounding allowance of the block bounds below: far above the
+    // error of a few double operations on the scene's coordinates.
+    double scale = 0.0;
+    for (int a = 0; a < 3; ++a) scale = std::max({scale, std::fabs(double(all.mn[a])), std::fabs(double(all.mx[a]))});
+    const double slack = 1e-9 * (1.0 + scale);
+    // Padded extent of the cells [i0, i1) along axis a (one cell: i1 = i0 + 1).
+    auto extent = [&](int a, int i0, int i1, double* lo, double* hi) {
+      *lo = double(t.gmin[a]) + double(i0) * double(t.cell) - pad;
+      *hi = double(t.gmin[a]) + double(i1) * double(t.cell) + pad;
     };
+    // Cells are taken in blocks of kGridBlock^3.  For a block, T bounds every
+    // cell's min_j ub(j, C) from above (the smallest ub of any one primitive
+    // over the whole block), and two subsets of the primitives are kept:
+    //   near:  lb of ub(i, C) over the block's cells < T, with
+    //          ub(i, C) >= |(d_a + cell/2)_a| - rho_i, d_a the distance from
+    //          c_i to the block along axis a (a cell's farthest face is at
+    //          least that far);
+    //   cands: box gap to the block < the largest threshold T allows.
+    // A primitive outside `near` cannot give a cell's minimum and one outside
+    // `cands` cannot pass a cell's threshold, so each cell's minimum and list,
+    // computed over the subsets with the same expressions, are those of all
+    // primitives.  The bounds carry `slack` against rounding.
+    const int blk = kGridBlock;
+    const int nbx = (dims[0] + blk - 1) / blk, nby = (dims[1] + blk - 1) / blk, nbz = (dims[2] + blk - 1) / blk;
+    const size_t nrows = static_cast<size_t>(dims[1]) * dims[2];
+    std::vector<std::vector<uint32_t>> row_offsets(nrows);
+    std::vector<std::vector<int32_t>> row_prims(nrows);
+    std::vector<std::vector<float>> row_gaps(nrows);
+    const float* cen[3] = {cx.data(), cy.data(), cz.data()};
+    auto work = [&](int item) {
+      const int by = item % nby, bz = item / nby;
+      std::vector<int32_t> near, cands;
+      std::vector<std::pair<double, int32_t>> cand;
+      near.reserve(np);
+      cands.reserve(np);
+      cand.reserve(64);
+      for (int bx = 0; bx < nbx; ++bx) {
+        const int i0[3] = {bx * blk, by * blk, bz * blk};
+        const int i1[3] = {std::min(i0[0] + blk, dims[0]), std::min(i0[1] + blk, dims[1]),
+                           std::min(i0[2] + blk, dims[2])};
+        double lo[3], hi[3];
+        for (int a = 0; a < 3; ++a) extent(a, i0[a], i1[a], &lo[a], &hi[a]);
+        double bound = std::numeric_limits<double>::infinity();
+        for (int k = 0; k < np; ++k) {
+          double f2 = 0.0;
+          for (int a = 0; a < 3; ++a) {
+            double f = std::max(std::fabs(double(cen[a][k]) - lo[a]), std::fabs(double(cen[a][k]) - hi[a]));
+            f2 += f * f;
+          }
+          double f = std::sqrt(f2);
+          bound = std::min(bound, rho[k] >= 0.0f ? f - rho[k] : f + 2.0 * rad[k]);
+        }
+        bound += slack + 1e-9 * std::fabs(bound);
+        double thr_max = std::max(double(t.r), bound) * (1.0 + 1e-5) + 1e-6;
+        thr_max += slack + 1e-9 * thr_max;
+        const double thr_max2 = thr_max * thr_max;
+        near.clear();
+        cands.clear();
+        for (int k = 0; k < np; ++k) {
+          double l2 = 0.0, g2 = 0.0;
+          for (int a = 0; a < 3; ++a) {
+            double c = double(cen[a][k]);
+            double d = std::max({0.0, lo[a] - c, c - hi[a]}) + half;
+            l2 += d * d;
+            double gap = std::max({0.0, double(pb[k].mn[a]) - hi[a], lo[a] - double(pb[k].mx[a])});
+            g2 += gap * gap;
+          }
+          double l = std::sqrt(l2);
+          if ((rho[k] >= 0.0f ? l - rho[k] : l + 2.0 * rad[k]) < bound) near.push_back(k);
+          if (g2 < thr_max2) cands.push_back(k);
+        }
+        for (int z = i0[2]; z < i1[2]; ++z)
+          for (int y = i0[1]; y < i1[1]; ++y) {
+            const size_t row = static_cast<size_t>(z) * dims[1] + y;
+            auto& offs = row_offsets[row];
+            auto& prims = row_prims[row];
+            auto& gaps = row_gaps[row];
+            for (int x = i0[0]; x < i1[0]; ++x) {
+              double mn[3], mx[3];
+              const int idx[3] = {x, y, z};
+              for (int a = 0; a < 3; ++a) extent(a, idx[a], idx[a] + 1, &mn[a], &mx[a]);
+              double min_ub = std::numeric_limits<double>::infinity();
+              for (int32_t k : near) {
+                double fx = std::max(std::fabs(double(cx[k]) - mn[0]), std::fabs(double(cx[k]) - mx[0]));
+                double fy = std::max(std::fabs(double(cy[k]) - mn[1]), std::fabs(double(cy[k]) - mx[1]));
+                double fz = std::max(std::fabs(double(cz[k]) - mn[2]), std::fabs(double(cz[k]) - mx[2]));
+                double far = std::sqrt(fx * fx + fy * fy + fz * fz);
+                double u = rho[k] >= 0.0f ? far - rho[k] : far + 2.0 * rad[k];
+                min_ub = std::min(min_ub, u);
+              }
+              // slack of 1e-5 keeps float rounding of the device-side bound on the safe side
+              double thr = std::max(double(t.r), min_ub) * (1.0 + 1e-5) + 1e-6;
+              double thr2 = thr * thr;
+              cand.clear();
+              for (int32_t k : cands) {
+                double g2 = 0.0;
+                for (int a = 0; a < 3; ++a) {
+                  double gap = std::max({0.0, double(pb[k].mn[a]) - mx[a], mn[a] - double(pb[k].mx[a])});
+                  g2 += gap * gap;
+                }
+                if (g2 < thr2) cand.emplace_back(g2, k);
+              }
+              // Sorted by box gap, so the device meets the likely nearest
+              // primitive first and prunes the rest.
+              std::sort(cand.begin(), cand.end());
+              offs.push_back(static_cast<uint32_t>(prims.size()));
+              for (const auto& c : cand) {
+                prims.push_back(c.second);
+                // Points of the cell are at least pad inside the padded box, so
+                // the device's float box bound of any of them exceeds this value.
+                gaps.push_back(std::nextafter(static_cast<float>(std::sqrt(c.first) * (1.0 - 1e-6)), 0.0f));
+              }
+            }
+          }
+      }
+    };
+    // Columns of blocks are independent: they are built on worker threads and
+    // the rows concatenated in cell order.
+    const int items = nby * nbz;
     unsigned nthreads = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    nthreads = std::min<unsigned>(nthreads, static_cast<unsigned>(items));
     std::atomic<int> next{0};
     std::vector<std::thread> pool;
     for (unsigned i = 0; i < nthreads; ++i)
       pool.emplace_back([&]() {
-        for (int z = next.fetch_add(1); z < nz; z = next.fetch_add(1)) work(z);
+        for (int it = next.fetch_add(1); it < items; it = next.fetch_add(1)) work(it);
       });
     for (auto& th : pool) th.join();
-    for (int z = 0; z < nz; ++z) {
+    for (size_t row = 0; row < nrows; ++row) {
       uint32_t base = static_cast<uint32_t>(img_->ur_cell_prims.size());
-      for (uint32_t o : slab_offsets[z]) img_->ur_cell_offsets.push_back(base + o);
-      img_->ur_cell_prims.insert(img_->ur_cell_prims.end(), slab_prims[z].begin(), slab_prims[z].end());
-      img_->ur_cell_gaps.insert(img_->ur_cell_gaps.end(), slab_gaps[z].begin(), slab_gaps[z].end());
+      for (uint32_t o : row_offsets[row]) img_->ur_cell_offsets.push_back(base + o);
+      img_->ur_cell_prims.insert(img_->ur_cell_prims.end(), row_prims[row].begin(), row_prims[row].end());
+      img_->ur_cell_gaps.insert(img_->ur_cell_gaps.end(), row_gaps[row].begin(), row_gaps[row].end());
     }
     img_->ur_cell_offsets.push_back(static_cast<uint32_t>(img_->ur_cell_prims.size()));
   }

@@ -33,6 +33,22 @@ def test_union_round_candidate_grid():
     assert 0 < info.grid_max_list <= 64
 
 
+@pytest.mark.parametrize("n,seed,cells,entries,max_list", [
+    (512, 1, 34592, 230017, 25),
+    (200, 5, 13475, 76626, 21),
+    (64, 3, 4416, 18447, 15),
+])
+def test_candidate_grid_matches_the_full_scan(n, seed, cells, entries, max_list):
+    """The grid is built in blocks whose primitive subsets are pruned by
+    bounds; every cell's list must still be the one a scan of all primitives
+    gives.  The expected counts are those of that full scan (every cell
+    against every primitive) on the same trees."""
+    st = ft.parse_and_eval(workloads.union_round_field(n=n, seed=seed).source)
+    rc, info = build_info(st.desc_ptr)
+    assert rc == 0
+    assert (info.grid_cells, info.grid_entries, info.grid_max_list) == (cells, entries, max_list)
+
+
 def test_polygon_trees_take_the_generic_path():
     src = "let scene = " + ".union_round(".join(
         f"ExtrudePolygon {{ sides: 5, radius: 0.3, pos: vec3({i}, 0, 0) }}" for i in range(4)) + ", 0.1)" * 3 + ";"
