@@ -24,6 +24,9 @@ namespace {
 
 // Edge, in cells, of the blocks the candidate grid is built in.
 constexpr int kGridBlock = 4;
+// Candidate-list entries of all union_round grids of a scene (8 bytes each on
+// the device); trees past it evaluate through their BVH.
+constexpr uint64_t kMaxGridEntries = uint64_t(1) << 26;
 
 struct Box {
   float mn[3], mx[3];
@@ -581,6 +584,12 @@ class Builder {
     std::vector<std::vector<int32_t>> row_prims(nrows);
     std::vector<std::vector<float>> row_gaps(nrows);
     const float* cen[3] = {cx.data(), cy.data(), cz.data()};
+    // Entries left under kMaxGridEntries for the whole image; a tree whose
+    // lists would pass it keeps no grid (its points take the tree BVH).
+    const uint64_t have = img_->ur_cell_prims.size();
+    const uint64_t budget = have < kMaxGridEntries ? kMaxGridEntries - have : 0;
+    std::atomic<uint64_t> produced{0};
+    std::atomic<bool> over{false};
     auto work = [&](int item) {
       const int by = item % nby, bz = item / nby;
       std::vector<int32_t> near, cands;
@@ -589,6 +598,8 @@ class Builder {
       cands.reserve(np);
       cand.reserve(64);
       for (int bx = 0; bx < nbx; ++bx) {
+        if (over.load(std::memory_order_relaxed)) return;
+        uint64_t block_entries = 0;
         const int i0[3] = {bx * blk, by * blk, bz * blk};
         const int i1[3] = {std::min(i0[0] + blk, dims[0]), std::min(i0[1] + blk, dims[1]),
                            std::min(i0[2] + blk, dims[2])};
@@ -658,6 +669,7 @@ class Builder {
               // primitive first and prunes the rest.
               std::sort(cand.begin(), cand.end());
               offs.push_back(static_cast<uint32_t>(prims.size()));
+              block_entries += cand.size();
               for (const auto& c : cand) {
                 prims.push_back(c.second);
                 // Points of the cell are at least pad inside the padded box, so
@@ -666,6 +678,7 @@ class Builder {
               }
             }
           }
+        if (produced.fetch_add(block_entries) + block_entries > budget) over.store(true);
       }
     };
     // Columns of blocks are independent: they are built on worker threads and
@@ -680,6 +693,10 @@ class Builder {
         for (int it = next.fetch_add(1); it < items; it = next.fetch_add(1)) work(it);
       });
     for (auto& th : pool) th.join();
+    if (over.load()) {
+      t.dims[0] = t.dims[1] = t.dims[2] = 0;
+      return;
+    }
     for (size_t row = 0; row < nrows; ++row) {
       uint32_t base = static_cast<uint32_t>(img_->ur_cell_prims.size());
       for (uint32_t o : row_offsets[row]) img_->ur_cell_offsets.push_back(base + o);

@@ -49,6 +49,27 @@ def test_candidate_grid_matches_the_full_scan(n, seed, cells, entries, max_list)
     assert (info.grid_cells, info.grid_entries, info.grid_max_list) == (cells, entries, max_list)
 
 
+def test_candidate_grid_is_dropped_past_its_entry_cap():
+    """1200 nearly concentric spheres: every cell would list every primitive
+    (about 93 M entries).  Past 2^26 entries the tree keeps no grid and is
+    evaluated through its BVH."""
+    n = 1200
+    lines = [f"let p{i} = Sphere {{ radius: {0.5 + 0.0001 * i:.6f}, pos: vec3({0.001 * (i % 7):.4f}, 1, 0) }};"
+             for i in range(n)]
+    cur, lvl = [f"p{i}" for i in range(n)], 0
+    while len(cur) > 1:
+        nxt = []
+        for j in range(0, len(cur) - 1, 2):
+            lines.append(f"let v{lvl}_{j // 2} = {cur[j]}.union_round({cur[j + 1]}, 0.1);")
+            nxt.append(f"v{lvl}_{j // 2}")
+        cur, lvl = nxt + cur[len(cur) - len(cur) % 2:], lvl + 1
+    lines.append(f"let scene = {cur[0]};")
+    st = ft.parse_and_eval("\n".join(lines))
+    rc, info = build_info(st.desc_ptr)
+    assert rc == 0 and info.union_round_leaves == 1
+    assert info.grid_cells == 0 and info.grid_entries == 0
+
+
 def test_polygon_trees_take_the_generic_path():
     src = "let scene = " + ".union_round(".join(
         f"ExtrudePolygon {{ sides: 5, radius: 0.3, pos: vec3({i}, 0, 0) }}" for i in range(4)) + ", 0.1)" * 3 + ";"
