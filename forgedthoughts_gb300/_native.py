@@ -25,6 +25,7 @@ FT_ERR_OUT_OF_MEMORY = 9
 FT_ERR_UNSUPPORTED = 10
 FT_ERR_NO_DEVICE = 11
 FT_ERR_JIT = 12
+FT_ERR_INTERNAL = 13
 
 FT_FLAG_DEVICE_POINTERS = 1
 FT_FLAG_FP16_BRICKS = 2

@@ -4,6 +4,8 @@
 
 #include <cstring>
 #include <new>
+#include <stdexcept>
+#include <system_error>
 
 #include "common.h"
 #include "frontend.h"
@@ -11,10 +13,47 @@
 namespace ftcommon {
 namespace {
 thread_local std::string g_last_error;
+// Set when the message itself could not be stored (no host memory left).
+thread_local bool g_last_error_lost = false;
 }
-void set_last_error(const std::string& message) { g_last_error = message; }
-void clear_last_error() { g_last_error.clear(); }
-const char* last_error_cstr() { return g_last_error.c_str(); }
+void set_last_error(const std::string& message) {
+  try {
+    g_last_error = message;
+    g_last_error_lost = false;
+  } catch (...) {
+    g_last_error.clear();
+    g_last_error_lost = true;
+  }
+}
+void clear_last_error() {
+  g_last_error.clear();
+  g_last_error_lost = false;
+}
+const char* last_error_cstr() { return g_last_error_lost ? "out of host memory" : g_last_error.c_str(); }
+
+ft_status fail_current_exception() noexcept {
+  try {
+    throw;
+  } catch (const std::bad_alloc&) {
+    return fail(FT_ERR_OUT_OF_MEMORY, "out of host memory");
+  } catch (const std::length_error&) {
+    return fail(FT_ERR_OUT_OF_MEMORY, "out of host memory (size limit of a host container)");
+  } catch (const std::system_error& e) {
+    try {
+      return fail(FT_ERR_OUT_OF_MEMORY, std::string("host resources exhausted: ") + e.what());
+    } catch (...) {
+      return fail(FT_ERR_OUT_OF_MEMORY, "host resources exhausted");
+    }
+  } catch (const std::exception& e) {
+    try {
+      return fail(FT_ERR_INTERNAL, std::string("internal error: ") + e.what());
+    } catch (...) {
+      return fail(FT_ERR_INTERNAL, "internal error");
+    }
+  } catch (...) {
+    return fail(FT_ERR_INTERNAL, "internal error: unknown exception");
+  }
+}
 }  // namespace ftcommon
 
 namespace {
@@ -41,6 +80,9 @@ void* run_frontend(void* arg) {
   } catch (const std::exception& e) {
     job->status = FT_ERR_EVAL;
     job->error = e.what();
+  } catch (...) {
+    job->status = FT_ERR_INTERNAL;
+    job->error = "internal error: unknown exception in the scene front-end";
   }
   return nullptr;
 }

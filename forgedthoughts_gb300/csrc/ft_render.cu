@@ -707,6 +707,7 @@ ft_status trace_wavefront(ft_scene* sc, const RayParams& P, uint32_t max_depth, 
 extern "C" {
 
 ft_status ft_scene_create(const ft_scene_desc* desc, ft_scene** out) {
+  FT_API_BEGIN
   if (!desc || !out) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "desc and out must be non-null");
   *out = nullptr;
   int ndev = 0;
@@ -716,12 +717,29 @@ ft_status ft_scene_create(const ft_scene_desc* desc, ft_scene** out) {
   auto* sc = new (std::nothrow) ft_scene();
   if (!sc) return ftcommon::fail(FT_ERR_OUT_OF_MEMORY, "out of host memory");
   std::string err;
-  if (!ftgpu::build_scene_image(*desc, &sc->img, &err)) {
+  bool built = false;
+  try {
+    built = ftgpu::build_scene_image(*desc, &sc->img, &err);
+  } catch (...) {
+    delete sc;
+    throw;
+  }
+  if (!built) {
     delete sc;
     return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, err);
   }
-  FT_CUDA_TRY(cudaGetDevice(&sc->device), "cudaGetDevice");
-  ft_status s = upload_scene(sc);
+  e = cudaGetDevice(&sc->device);
+  if (e != cudaSuccess) {
+    delete sc;
+    return ftcommon::fail(FT_ERR_CUDA, cuda_msg(e, "cudaGetDevice"));
+  }
+  ft_status s = FT_OK;
+  try {
+    s = upload_scene(sc);
+  } catch (...) {
+    ft_scene_destroy(sc);
+    throw;
+  }
   if (s != FT_OK) {
     ft_scene_destroy(sc);
     return s;
@@ -729,9 +747,11 @@ ft_status ft_scene_create(const ft_scene_desc* desc, ft_scene** out) {
   *out = sc;
   ftcommon::clear_last_error();
   return FT_OK;
+  FT_API_END
 }
 
 ft_status ft_scene_build_info(const ft_scene_desc* desc, ft_build_info* info) {
+  FT_API_BEGIN
   if (!desc || !info) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "desc and info must be non-null");
   ftgpu::SceneImage img;
   std::string err;
@@ -761,6 +781,7 @@ ft_status ft_scene_build_info(const ft_scene_desc* desc, ft_build_info* info) {
   info->generic_ops = static_cast<uint32_t>(img.gops.size());
   info->build_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
   return FT_OK;
+  FT_API_END
 }
 
 ft_status ft_scene_last_launches(const ft_scene* sc, uint32_t* launches) {
@@ -802,6 +823,7 @@ void ft_scene_destroy(ft_scene* sc) {
 ft_status ft_render_depth(ft_scene* sc, const ft_render_options* options, ft_accel_mode accel, uint32_t aa_samples,
                           float* t_out, uint8_t* mask_out, uint32_t* material_out, float* normal_out,
                           uint8_t* rgb8_out, uint32_t flags, void* stream) {
+  FT_API_BEGIN
   if (!sc) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "scene must be non-null");
   if (accel < FT_ACCEL_NAIVE || accel > FT_ACCEL_BRICKS) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "unknown accel mode");
   uint32_t aa = std::max(aa_samples, 1u);
@@ -846,6 +868,7 @@ ft_status ft_render_depth(ft_scene* sc, const ft_render_options* options, ft_acc
   if (ft_status s = march_check(march_flags)) return s;
   ftcommon::clear_last_error();
   return FT_OK;
+  FT_API_END
 }
 
 ft_status ft_render_depth_preview_noalloc(ft_scene* sc, const ft_render_options* options, ft_accel_mode accel,
@@ -881,6 +904,7 @@ ft_status ft_render_depth_preview_noalloc(ft_scene* sc, const ft_render_options*
 
 ft_status ft_render_trace(ft_scene* sc, const ft_render_options* options, ft_accel_mode accel, uint32_t aa_samples,
                           uint32_t max_depth, float* rgb_out, uint8_t* rgb8_out, uint32_t flags, void* stream) {
+  FT_API_BEGIN
   if (!sc) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "scene must be non-null");
   if (accel < FT_ACCEL_NAIVE || accel > FT_ACCEL_BRICKS) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "unknown accel mode");
   uint32_t aa = std::max(aa_samples, 1u);
@@ -913,10 +937,12 @@ ft_status ft_render_trace(ft_scene* sc, const ft_render_options* options, ft_acc
   FT_CUDA_TRY(cudaStreamSynchronize(st), "trace");
   ftcommon::clear_last_error();
   return FT_OK;
+  FT_API_END
 }
 
 ft_status ft_render_trace_stats(ft_scene* sc, const ft_render_options* options, ft_accel_mode accel,
                                 uint32_t aa_samples, uint32_t max_depth, ft_render_stats* stats) {
+  FT_API_BEGIN
   if (!sc || !stats) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "scene and stats must be non-null");
   if (accel < FT_ACCEL_NAIVE || accel > FT_ACCEL_BRICKS) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "unknown accel mode");
   uint32_t aa = std::max(aa_samples, 1u);
@@ -943,10 +969,12 @@ ft_status ft_render_trace_stats(ft_scene* sc, const ft_render_options* options, 
   stats->march_steps = h[4];
   ftcommon::clear_last_error();
   return FT_OK;
+  FT_API_END
 }
 
 ft_status ft_render_depth_stats(ft_scene* sc, const ft_render_options* options, ft_accel_mode accel,
                                 uint32_t aa_samples, uint32_t flags, ft_render_stats* stats) {
+  FT_API_BEGIN
   if (!sc || !stats) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "scene and stats must be non-null");
   if (accel < FT_ACCEL_NAIVE || accel > FT_ACCEL_BRICKS) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "unknown accel mode");
   uint32_t aa = std::max(aa_samples, 1u);
@@ -972,9 +1000,11 @@ ft_status ft_render_depth_stats(ft_scene* sc, const ft_render_options* options, 
   stats->march_steps = h[4];
   ftcommon::clear_last_error();
   return FT_OK;
+  FT_API_END
 }
 
 ft_status ft_scene_build_bricks(ft_scene* sc, const ft_brick_options* options, ft_brick_info* info) {
+  FT_API_BEGIN
   if (!sc) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "scene must be non-null");
   ft_brick_options o{};
   if (options) o = *options;
@@ -1156,9 +1186,11 @@ ft_status ft_scene_build_bricks(ft_scene* sc, const ft_brick_options* options, f
   }
   ftcommon::clear_last_error();
   return FT_OK;
+  FT_API_END
 }
 
 ft_status ft_scene_brick_bounds(ft_scene* sc, const float* points, uint32_t n, float* bound_out, float* exact_out) {
+  FT_API_BEGIN
   if (!sc || (n && (!points || !bound_out || !exact_out)))
     return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "scene, points and outputs must be non-null");
   std::lock_guard<std::mutex> lock(sc->mu);
@@ -1177,9 +1209,11 @@ ft_status ft_scene_brick_bounds(ft_scene* sc, const float* points, uint32_t n, f
   FT_CUDA_TRY(cudaMemcpy(exact_out, de, static_cast<size_t>(n) * sizeof(float), cudaMemcpyDeviceToHost), "copy exact");
   ftcommon::clear_last_error();
   return FT_OK;
+  FT_API_END
 }
 
 ft_status ft_batch_create(const ft_batch_item* items, uint32_t n, uint32_t flags, ft_batch** out) {
+  FT_API_BEGIN
   if (!out || (n && !items)) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "items and out must be non-null");
   *out = nullptr;
   if (n == 0) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "a batch needs at least one item");
@@ -1289,9 +1323,11 @@ ft_status ft_batch_create(const ft_batch_item* items, uint32_t n, uint32_t flags
   *out = guard.release();
   ftcommon::clear_last_error();
   return FT_OK;
+  FT_API_END
 }
 
 ft_status ft_batch_set_tuning(ft_batch* b, const ft_batch_tuning* t) {
+  FT_API_BEGIN
   if (!b || !t) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "batch and tuning must be non-null");
   if (ft_status st = check_tuning(*t)) return st;
   std::lock_guard<std::mutex> lock(b->mu);
@@ -1301,9 +1337,11 @@ ft_status ft_batch_set_tuning(ft_batch* b, const ft_batch_tuning* t) {
   if (ft_status st = batch_apply_tuning(b)) return st;
   ftcommon::clear_last_error();
   return FT_OK;
+  FT_API_END
 }
 
 ft_status ft_batch_autotune(ft_batch* b, ft_batch_tuning* best) {
+  FT_API_BEGIN
   if (!b) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "batch must be non-null");
   std::lock_guard<std::mutex> lock(b->mu);
   FT_CUDA_TRY(cudaSetDevice(b->device), "cudaSetDevice");
@@ -1344,19 +1382,23 @@ ft_status ft_batch_autotune(ft_batch* b, ft_batch_tuning* best) {
   if (best) *best = top;
   ftcommon::clear_last_error();
   return FT_OK;
+  FT_API_END
 }
 
 ft_status ft_batch_launch(ft_batch* b, void* stream) {
+  FT_API_BEGIN
   if (!b) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "batch must be non-null");
   std::lock_guard<std::mutex> lock(b->mu);
   FT_CUDA_TRY(cudaSetDevice(b->device), "cudaSetDevice");
   FT_CUDA_TRY(cudaGraphLaunch(b->exec, static_cast<cudaStream_t>(stream)), "cudaGraphLaunch(batch)");
   ftcommon::clear_last_error();
   return FT_OK;
+  FT_API_END
 }
 
 ft_status ft_batch_read(ft_batch* b, uint32_t item, float* t_out, uint8_t* mask_out, float* rgb_out,
                         uint8_t* rgb8_out) {
+  FT_API_BEGIN
   if (!b) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "batch must be non-null");
   if (item >= b->items.size()) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "batch item out of range");
   std::lock_guard<std::mutex> lock(b->mu);
@@ -1379,6 +1421,7 @@ ft_status ft_batch_read(ft_batch* b, uint32_t item, float* t_out, uint8_t* mask_
     FT_CUDA_TRY(cudaMemcpy(rgb8_out, b->d_rgb8 + 3 * pi.pix_first, px * 3, cudaMemcpyDeviceToHost), "copy rgb8");
   ftcommon::clear_last_error();
   return FT_OK;
+  FT_API_END
 }
 
 ft_status ft_batch_samples(const ft_batch* b, uint64_t* primary_samples) {
@@ -1437,6 +1480,7 @@ ft_status check_views(const ft_scene* sc, const ft_view* views, uint32_t n, cons
 
 ft_status ft_render_views(ft_scene* sc, const ft_view* views, uint32_t n_views, const ft_render_options* options,
                           float tau, float* t_out, uint8_t* mask_out, float* sil_out, uint32_t flags, void* stream) {
+  FT_API_BEGIN
   if (ft_status s = check_views(sc, views, n_views, options, tau)) return s;
   std::lock_guard<std::mutex> lock(sc->mu);
   FT_CUDA_TRY(cudaSetDevice(sc->device), "cudaSetDevice");
@@ -1470,11 +1514,13 @@ ft_status ft_render_views(ft_scene* sc, const ft_view* views, uint32_t n_views, 
   FT_CUDA_TRY(cudaStreamSynchronize(st), "views");
   ftcommon::clear_last_error();
   return FT_OK;
+  FT_API_END
 }
 
 ft_status ft_render_backward(ft_scene* sc, const ft_view* views, uint32_t n_views, const ft_render_options* options,
                              float tau, const ft_param* params, uint32_t n_params, const float* dL_dt,
                              const float* dL_dsil, double* dL_dparams, uint32_t flags, void* stream) {
+  FT_API_BEGIN
   if (ft_status s = check_views(sc, views, n_views, options, tau)) return s;
   if (!dL_dparams || (n_params && !params))
     return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "params and dL_dparams must be non-null");
@@ -1563,9 +1609,11 @@ ft_status ft_render_backward(ft_scene* sc, const ft_view* views, uint32_t n_view
                                                      "(or has more than 512 primitives): no adjoint");
   ftcommon::clear_last_error();
   return FT_OK;
+  FT_API_END
 }
 
 ft_status ft_scene_jit(ft_scene* sc, ft_jit_info* info) {
+  FT_API_BEGIN
   if (!sc) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "scene must be non-null");
   std::lock_guard<std::mutex> lock(sc->mu);
   FT_CUDA_TRY(cudaSetDevice(sc->device), "cudaSetDevice");
@@ -1682,9 +1730,11 @@ ft_status ft_scene_jit(ft_scene* sc, ft_jit_info* info) {
   if (info) *info = out;
   ftcommon::clear_last_error();
   return FT_OK;
+  FT_API_END
 }
 
 ft_status ft_measure_fp32_peak(double* tflops) {
+  FT_API_BEGIN
   if (!tflops) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "tflops must be non-null");
   int dev = 0, sms = 0;
   FT_CUDA_TRY(cudaGetDevice(&dev), "cudaGetDevice");
@@ -1710,6 +1760,7 @@ ft_status ft_measure_fp32_peak(double* tflops) {
   double flops = 2.0 * 8.0 * iters * double(threads) * blocks * reps;
   *tflops = flops / (ms * 1e-3) / 1e12;
   return FT_OK;
+  FT_API_END
 }
 
 }  // extern "C"

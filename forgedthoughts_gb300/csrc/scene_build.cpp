@@ -17,6 +17,9 @@
 #include <numeric>
 #include <string>
 #include <atomic>
+#include <exception>
+#include <mutex>
+#include <system_error>
 #include <thread>
 
 namespace ftgpu {
@@ -687,12 +690,32 @@ class Builder {
     unsigned nthreads = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
     nthreads = std::min<unsigned>(nthreads, static_cast<unsigned>(items));
     std::atomic<int> next{0};
-    std::vector<std::thread> pool;
-    for (unsigned i = 0; i < nthreads; ++i)
-      pool.emplace_back([&]() {
+    // A worker's exception (a failed allocation) stops the others and is
+    // rethrown here once all have ended; if no thread can be started, the
+    // calling thread does the work.
+    std::exception_ptr failure;
+    std::mutex failure_mu;
+    auto drain = [&]() {
+      try {
         for (int it = next.fetch_add(1); it < items; it = next.fetch_add(1)) work(it);
-      });
+      } catch (...) {
+        std::lock_guard<std::mutex> lock(failure_mu);
+        if (!failure) failure = std::current_exception();
+        over.store(true);
+      }
+    };
+    std::vector<std::thread> pool;
+    pool.reserve(nthreads);
+    for (unsigned i = 0; i < nthreads; ++i) {
+      try {
+        pool.emplace_back(drain);
+      } catch (const std::system_error&) {
+        break;
+      }
+    }
+    if (pool.empty()) drain();
     for (auto& th : pool) th.join();
+    if (failure) std::rethrow_exception(failure);
     if (over.load()) {
       t.dims[0] = t.dims[1] = t.dims[2] = 0;
       return;
@@ -918,6 +941,7 @@ bool check_param(const ft_scene_desc& d, const ft_param& p) {
 extern "C" {
 
 ft_status ft_scene_param_layout(const ft_scene_desc* desc, uint32_t capacity, ft_param* params, uint32_t* count) {
+  FT_API_BEGIN
   if (!desc || !count || (capacity && !params))
     return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "desc, count and params must be non-null");
   if (desc->root < 0 || static_cast<uint32_t>(desc->root) >= desc->n_nodes || !desc->nodes)
@@ -935,9 +959,11 @@ ft_status ft_scene_param_layout(const ft_scene_desc* desc, uint32_t capacity, ft
   for (uint32_t i = 0; i < std::min<uint32_t>(capacity, *count); ++i) params[i] = out[i];
   ftcommon::clear_last_error();
   return FT_OK;
+  FT_API_END
 }
 
 ft_status ft_scene_desc_get_params(const ft_scene_desc* desc, const ft_param* params, uint32_t n, float* values) {
+  FT_API_BEGIN
   if (!desc || (n && (!params || !values))) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "null argument");
   for (uint32_t i = 0; i < n; ++i) {
     if (!check_param(*desc, params[i]))
@@ -945,9 +971,11 @@ ft_status ft_scene_desc_get_params(const ft_scene_desc* desc, const ft_param* pa
     values[i] = *param_field(const_cast<ft_node&>(desc->nodes[params[i].node]), params[i].field);
   }
   return FT_OK;
+  FT_API_END
 }
 
 ft_status ft_scene_desc_set_params(ft_scene_desc* desc, const ft_param* params, uint32_t n, const float* values) {
+  FT_API_BEGIN
   if (!desc || (n && (!params || !values))) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "null argument");
   for (uint32_t i = 0; i < n; ++i)
     if (!check_param(*desc, params[i]) || !std::isfinite(values[i]))
@@ -971,6 +999,7 @@ ft_status ft_scene_desc_set_params(ft_scene_desc* desc, const ft_param* params, 
     }
   }
   return FT_OK;
+  FT_API_END
 }
 
 }  // extern "C"

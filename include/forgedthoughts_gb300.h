@@ -44,7 +44,8 @@ typedef enum ft_status {
   FT_ERR_OUT_OF_MEMORY = 9,
   FT_ERR_UNSUPPORTED = 10,
   FT_ERR_NO_DEVICE = 11,
-  FT_ERR_JIT = 12           /* run-time compilation (NVRTC) or module load failed */
+  FT_ERR_JIT = 12,          /* run-time compilation (NVRTC) or module load failed */
+  FT_ERR_INTERNAL = 13      /* an unexpected host-side failure; no C++ exception crosses this ABI */
 } ft_status;
 
 /* `enum AccelMode` (R:58-63). */

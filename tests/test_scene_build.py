@@ -49,11 +49,9 @@ def test_candidate_grid_matches_the_full_scan(n, seed, cells, entries, max_list)
     assert (info.grid_cells, info.grid_entries, info.grid_max_list) == (cells, entries, max_list)
 
 
-def test_candidate_grid_is_dropped_past_its_entry_cap():
-    """1200 nearly concentric spheres: every cell would list every primitive
-    (about 93 M entries).  Past 2^26 entries the tree keeps no grid and is
-    evaluated through its BVH."""
-    n = 1200
+def _overlapping_spheres(n: int) -> str:
+    """A balanced union_round tree of n nearly concentric spheres: every grid
+    cell would list every primitive."""
     lines = [f"let p{i} = Sphere {{ radius: {0.5 + 0.0001 * i:.6f}, pos: vec3({0.001 * (i % 7):.4f}, 1, 0) }};"
              for i in range(n)]
     cur, lvl = [f"p{i}" for i in range(n)], 0
@@ -64,10 +62,56 @@ def test_candidate_grid_is_dropped_past_its_entry_cap():
             nxt.append(f"v{lvl}_{j // 2}")
         cur, lvl = nxt + cur[len(cur) - len(cur) % 2:], lvl + 1
     lines.append(f"let scene = {cur[0]};")
-    st = ft.parse_and_eval("\n".join(lines))
+    return "\n".join(lines)
+
+
+def test_candidate_grid_is_dropped_past_its_entry_cap():
+    """1200 overlapping spheres would give about 93 M list entries.  Past 2^26
+    entries the tree keeps no grid and is evaluated through its BVH."""
+    st = ft.parse_and_eval(_overlapping_spheres(1200))
     rc, info = build_info(st.desc_ptr)
     assert rc == 0 and info.union_round_leaves == 1
     assert info.grid_cells == 0 and info.grid_entries == 0
+
+
+_OOM_CHILD = r"""
+import ctypes, resource, sys
+sys.path.insert(0, sys.argv[1])
+import forgedthoughts_gb300 as ft
+from forgedthoughts_gb300 import _native
+sys.path.insert(0, sys.argv[2])
+from test_scene_build import _overlapping_spheres
+st = ft.parse_and_eval(_overlapping_spheres(1200))
+info = _native.BuildInfoC()
+lib = _native.lib()
+soft, hard = resource.getrlimit(resource.RLIMIT_AS)
+vm = int(open("/proc/self/statm").read().split()[0]) * resource.getpagesize()
+resource.setrlimit(resource.RLIMIT_AS, (vm + (256 << 20), hard))
+rc = lib.ft_scene_build_info(st.desc_ptr, ctypes.byref(info))
+resource.setrlimit(resource.RLIMIT_AS, (soft, hard))
+print(rc, _native.last_error())
+"""
+
+
+def test_host_allocation_failure_returns_a_status():
+    """A failed host allocation inside the scene builder, here in its worker
+    threads, comes back as FT_ERR_OUT_OF_MEMORY: no C++ exception crosses the
+    C ABI (an escaping one would abort the process).  The child process caps
+    its address space 256 MB above its size, and the tree's grid needs more
+    than 500 MB before it reaches its entry cap."""
+    import subprocess
+    import sys
+    from pathlib import Path
+
+    if not Path("/proc/self/statm").exists():
+        pytest.skip("needs /proc")
+    here = Path(__file__).resolve().parent
+    p = subprocess.run([sys.executable, "-c", _OOM_CHILD, str(here.parent), str(here)],
+                       capture_output=True, text=True, timeout=300)
+    assert p.returncode == 0, p.stderr[-2000:]
+    rc, msg = p.stdout.strip().split(" ", 1)
+    assert int(rc) == _native.FT_ERR_OUT_OF_MEMORY, p.stdout
+    assert "host" in msg
 
 
 def test_polygon_trees_take_the_generic_path():
