@@ -781,8 +781,32 @@ class Lowerer {
     return static_cast<uint32_t>(out_.materials.size()) - 1;
   }
 
+  // medium_from_value (R:6834-6845): an object value of any type gives an
+  // explicit medium, IOR clamped to [1, 3], absorption colour white and
+  // density 0 (at least 0) unless given; any other value leaves none.
+  static void read_medium(const Value* v, ft_material* m) {
+    if (!v || v->kind != Value::Object) return;
+    const ObjectData& mo = *v->obj;
+    V3 a;
+    if (!read_spectrum(mo, "absorption_color", &a)) a = v3(1.0f, 1.0f, 1.0f);
+    m->has_medium = 1;
+    m->medium_ior = clampf(number_or(mo, {"ior"}, 1.0f), 1.0f, 3.0f);
+    m->medium_absorption[0] = a.x;
+    m->medium_absorption[1] = a.y;
+    m->medium_absorption[2] = a.z;
+    m->medium_density = std::max(number_or(mo, {"density"}, 0.0f), 0.0f);
+  }
+
   // material_from_object (R:6439-6570), without the dynamic-hook machinery.
+  // Every model reads the `medium` field (R:6458, R:6517, R:6535, R:6564).
   ft_material material_from_object(const ObjectData& o) {
+    if (st_.material_defs.count(o.type_name)) return material_from_dynamic_def(*st_.material_defs.at(o.type_name), o);
+    ft_material m = material_from_builtin(o);
+    read_medium(o.get("medium"), &m);
+    return m;
+  }
+
+  ft_material material_from_builtin(const ObjectData& o) {
     const std::string& t = o.type_name;
     auto lower = [](std::string s) {
       for (char& ch : s) ch = static_cast<char>(std::tolower(static_cast<unsigned char>(ch)));
@@ -802,7 +826,6 @@ class Lowerer {
       if (!read_spectrum(o, "color", &col) && !read_spectrum(o, "base_color", &col)) col = def;
       mm.color[0] = col.x; mm.color[1] = col.y; mm.color[2] = col.z;
     };
-    if (st_.material_defs.count(t)) return material_from_dynamic_def(*st_.material_defs.at(t), o);
     if (lt == "lambert") {
       m = material_defaults(FT_MAT_LAMBERT);
       set_color(m, v3(0.8f, 0.8f, 0.8f));
@@ -910,6 +933,8 @@ class Lowerer {
     if (num("thin_walled", &v)) m.thin_walled = v >= 0.5f;
     spec("emission_color", m.emission_color);
     if (num("emission_strength", &v)) m.emission_strength = std::max(v, 0.0f);
+    auto medium = props.find("medium");
+    if (medium != props.end()) read_medium(&medium->second, &m);
     // Per-hit hooks: colour, roughness, IOR and thin_walled
     // (resolve_leaf_material, R:7164-7600); the other hookable properties are
     // not lowered.  A Standard or Layered definition's IOR is the coat's

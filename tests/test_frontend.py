@@ -194,6 +194,64 @@ def test_material_definition_properties_clamps_and_overrides():
     assert abs(coat.ior - 1.5) < 1e-6 and abs(coat.clearcoat - 0.6) < 1e-6 and abs(coat.specular_color[1] - 0.95) < 1e-6
 
 
+def test_material_medium_field():
+    """The reference's parses_medium_and_subsurface_material_fields: a
+    Dielectric's `medium: Medium {...}` field (medium_from_value,
+    R:6834-6845) gives IOR 1.33, absorption blue 1.0 and density 0.35."""
+    m = _sphere_material("""
+        let scene = Sphere {
+          material: Dielectric {
+            color: vec3(0.96, 0.98, 1.0),
+            ior: 1.52,
+            medium: Medium {
+              ior: 1.33,
+              absorption_color: vec3(0.82, 0.91, 1.0),
+              density: 0.35
+            },
+            subsurface: Subsurface {
+              color: vec3(1.0, 0.58, 0.44),
+              radius: vec3(0.8, 0.4, 0.22),
+              anisotropy: 0.15,
+              scale: 1.25
+            }
+          }
+        };
+    """)
+    assert m.kind == _native.FT_MAT_DIELECTRIC and m.has_medium == 1
+    assert abs(m.medium_ior - 1.33) < 1e-6 and abs(m.medium_absorption[2] - 1.0) < 1e-6
+    assert abs(m.medium_absorption[0] - 0.82) < 1e-6 and abs(m.medium_density - 0.35) < 1e-6
+    assert abs(m.ior - 1.52) < 1e-6
+
+
+def test_material_medium_defaults_clamps_and_definitions():
+    """Missing medium fields take medium_from_value's defaults and clamps
+    (IOR 1 within [1, 3], white absorption, density >= 0); any model reads
+    the field; a definition's `medium = ...` property is its static medium
+    (apply_dynamic_material_properties, R:6761-6763); no field, no medium."""
+    m = _sphere_material("let scene = Sphere { material: Lambert { medium: Medium { ior: 7.0, density: -2.0 } } };")
+    assert m.kind == _native.FT_MAT_LAMBERT and m.has_medium == 1
+    assert m.medium_ior == 3.0 and m.medium_density == 0.0 and list(m.medium_absorption) == [1.0, 1.0, 1.0]
+    m = _sphere_material("let scene = Sphere { material: Metal { medium: Fog {} } };")
+    assert m.kind == _native.FT_MAT_METAL and m.has_medium == 1 and m.medium_ior == 1.0
+    m = _sphere_material("let scene = Sphere { material: Dielectric { medium: 0.5 } };")
+    assert m.has_medium == 0
+    m = _sphere_material("""
+        material WaxedGlass {
+          model: Dielectric;
+          color = vec3(1.0);
+          medium = Medium {
+            ior: 1.33,
+            absorption_color: vec3(0.9, 0.95, 1.0),
+            density: 0.05
+          };
+        };
+        let scene = Sphere { material: WaxedGlass {} };
+    """)
+    assert m.kind == _native.FT_MAT_DIELECTRIC and m.has_medium == 1
+    assert abs(m.medium_ior - 1.33) < 1e-6 and abs(m.medium_absorption[1] - 0.95) < 1e-6
+    assert abs(m.medium_density - 0.05) < 1e-6
+
+
 HOOK_MATERIALS = """
 material Stripe {
   model: Lambert;
