@@ -647,6 +647,8 @@ def main() -> None:
         w.options.height = args.height
     if args.aa:
         w.aa = args.aa
+    if args.width or args.height or args.aa:
+        w.name = f"{w.name}_resized_to_{w.options.width}x{w.options.height}_aa{w.aa}"
     if args.max_depth:
         w.max_depth = args.max_depth
     if args.mode == "trace" and w.max_depth <= 0:
