@@ -43,6 +43,10 @@ def lib() -> ctypes.CDLL:
         h.oracle_render_backward.argtypes = [vp, vp, ctypes.c_uint32, vp, ctypes.c_float, vp, ctypes.c_uint32, vp,
                                              vp, ctypes.c_int, ctypes.c_int, vp]
         h.oracle_last_error.restype = ctypes.c_char_p
+        h.oracle_medium_transmittance.restype = None
+        h.oracle_medium_transmittance.argtypes = [vp, ctypes.c_float, vp]
+        h.oracle_transition_medium.restype = None
+        h.oracle_transition_medium.argtypes = [vp, ctypes.c_int, vp, vp]
         _lib = h
     return _lib
 
@@ -111,6 +115,24 @@ def distance(state, points: np.ndarray, accel: int = 1, precision: int = 32):
     _check(lib().oracle_distance(_vp(state.desc_ptr), int(accel), int(precision), _arr(pts), n, _arr(d), _arr(obj),
                                  _arr(mat)))
     return d, obj, mat
+
+
+def medium_transmittance(ior: float, absorption, density: float, distance: float) -> np.ndarray:
+    """medium_transmittance (renderer.rs:5109-5119) in f32: the (3,) transmittance."""
+    m = np.array([ior, *absorption, density], np.float32)
+    out = np.zeros(3, np.float32)
+    lib().oracle_medium_transmittance(_arr(m), float(distance), _arr(out))
+    return out
+
+
+def transition_medium(material, front_face: bool, current) -> np.ndarray:
+    """transition_medium (renderer.rs:5147-5166) in f32 for an ``ft_material``
+    (a ctypes structure): the next medium as (ior, r, g, b, density)."""
+    cur = np.ascontiguousarray(current, np.float32)
+    out = np.zeros(5, np.float32)
+    lib().oracle_transition_medium(ctypes.cast(ctypes.byref(material), ctypes.c_void_p), int(bool(front_face)),
+                                   _arr(cur), _arr(out))
+    return out
 
 
 def eval_program(state, program: int, args: np.ndarray, precision: int = 32) -> np.ndarray:

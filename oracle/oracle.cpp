@@ -1037,6 +1037,11 @@ struct Params {  // MaterialParams (materials/mod.rs:66-86), render-relevant fie
   bool thin_walled;
   Sp<R> emission_color;
   R emission_strength;
+  // MediumParams (materials/mod.rs), present when the material has one
+  bool has_medium = false;
+  R medium_ior = R(1);
+  Sp<R> medium_absorption = Sp<R>{R(1), R(1), R(1)};
+  R medium_density = R(0);
 };
 
 template <class R>
@@ -1063,6 +1068,10 @@ template <class R> Params<R> params_from(const ft_material& m) {
   p.thin_walled = m.thin_walled != 0;
   p.emission_color = sp(R(m.emission_color[0]), R(m.emission_color[1]), R(m.emission_color[2]));
   p.emission_strength = R(m.emission_strength);
+  p.has_medium = m.has_medium != 0;
+  p.medium_ior = R(m.medium_ior);
+  p.medium_absorption = sp(R(m.medium_absorption[0]), R(m.medium_absorption[1]), R(m.medium_absorption[2]));
+  p.medium_density = R(m.medium_density);
   return p;
 }
 
@@ -1109,6 +1118,20 @@ template <class R> Params<R> blend_params(Params<R> a, const Params<R>& b, R t) 
   a.thin_walled = t < R(0.5) ? a.thin_walled : b.thin_walled;
   a.emission_color = lerp_sp(a.emission_color, b.emission_color, t);
   a.emission_strength = a.emission_strength + (b.emission_strength - a.emission_strength) * t;
+  // blend_medium (R:7543-7565): both present blend (the colour through
+  // lerp_spectrum's clamped t); one present is kept on its side of t = 0.5
+  if (a.has_medium && b.has_medium) {
+    a.medium_ior = a.medium_ior + (b.medium_ior - a.medium_ior) * t;
+    a.medium_absorption = lerp_sp(a.medium_absorption, b.medium_absorption, t);
+    a.medium_density = a.medium_density + (b.medium_density - a.medium_density) * t;
+  } else if (a.has_medium) {
+    a.has_medium = t < R(0.5);
+  } else if (b.has_medium && t >= R(0.5)) {
+    a.has_medium = true;
+    a.medium_ior = b.medium_ior;
+    a.medium_absorption = b.medium_absorption;
+    a.medium_density = b.medium_density;
+  }
   return a;
 }
 template <class R> Mat<R> blend_materials(const Mat<R>& a, const Mat<R>& b, R t) {
@@ -1231,6 +1254,30 @@ struct Medium {  // MediumState (R:4372-4387)
   static Medium air() { return Medium{R(1), sp(R(1), R(1), R(1)), R(0)}; }
 };
 
+// medium_transmittance (R:5109-5119): per channel, the clamped absorption
+// colour to the power density * distance; white without density or distance.
+template <class R> Sp<R> medium_transmittance(const Medium<R>& m, R dist) {
+  if (m.density <= R(0) || dist <= R(0)) return sp(R(1), R(1), R(1));
+  R e = m.density * rmax(dist, R(0));
+  return sp(std::pow(rclamp(m.absorption.r, R(0), R(1)), e), std::pow(rclamp(m.absorption.g, R(0), R(1)), e),
+            std::pow(rclamp(m.absorption.b, R(0), R(1)), e));
+}
+
+// transition_medium with medium_state_from_material (R:5125-5166): crossing
+// into a transmissive material enters its explicit medium (IOR clamped to
+// [1, 3], density at least 0), else one of its IOR with no absorption;
+// leaving it returns to air; other materials keep the current medium.
+template <class R> Medium<R> transition_medium(const Mat<R>& m, bool front, Medium<R> cur) {
+  int model = dominant_model(m);
+  Params<R> p = dominant_params(m);
+  bool transmissive = model == kDielectric || (model == kStandard && p.transmission > R(0.01));
+  if (!transmissive) return cur;
+  if (!front) return Medium<R>::air();
+  if (p.has_medium)
+    return Medium<R>{rclamp(p.medium_ior, R(1), R(3)), p.medium_absorption, rmax(p.medium_density, R(0))};
+  return Medium<R>{rclamp(p.ior, R(1), R(3)), sp(R(1), R(1), R(1)), R(0)};
+}
+
 template <class R>
 class Tracer {
  public:
@@ -1292,11 +1339,8 @@ class Tracer {
     return env_radiance();
   }
 
-  static Sp<R> attenuate(Sp<R> c, const Medium<R>& m, R dist) {  // R:5109-5123
-    if (m.density <= R(0) || dist <= R(0)) return c;
-    R e = m.density * rmax(dist, R(0));
-    return c * sp(std::pow(rclamp(m.absorption.r, R(0), R(1)), e), std::pow(rclamp(m.absorption.g, R(0), R(1)), e),
-                  std::pow(rclamp(m.absorption.b, R(0), R(1)), e));
+  static Sp<R> attenuate(Sp<R> c, const Medium<R>& m, R dist) {  // apply_medium_attenuation (R:5121-5123)
+    return c * medium_transmittance(m, dist);
   }
 
   // estimate_node_normal (R:4554-4570)
@@ -1719,13 +1763,8 @@ class Tracer {
     return true;
   }
 
-  static Medium<R> transition(const Mat<R>& m, bool front, Medium<R> cur) {  // R:5125-5175
-    int model = dominant_model(m);
-    Params<R> p = dominant_params(m);
-    bool transmissive = model == kDielectric || (model == kStandard && p.transmission > R(0.01));
-    if (!transmissive) return cur;
-    if (front) return Medium<R>{rclamp(p.ior, R(1), R(3)), sp(R(1), R(1), R(1)), R(0)};
-    return Medium<R>::air();
+  static Medium<R> transition(const Mat<R>& m, bool front, Medium<R> cur) {  // R:5147-5166
+    return transition_medium(m, front, cur);
   }
 };
 
@@ -2269,4 +2308,26 @@ extern "C" int oracle_render_backward(const ft_scene_desc* desc, const ft_view* 
                                 params, n_params, dl_dt, dl_dsil, grad_out);
   return render_views<float>(desc, views, n_views, options, tau, threads, nullptr, nullptr, nullptr, params, n_params,
                              dl_dt, dl_dsil, grad_out);
+}
+
+extern "C" void oracle_medium_transmittance(const float medium[5], float distance, float out_rgb[3]) {
+  const Medium<float> m{medium[0], sp(medium[1], medium[2], medium[3]), medium[4]};
+  const Sp<float> t = medium_transmittance(m, distance);
+  out_rgb[0] = t.r;
+  out_rgb[1] = t.g;
+  out_rgb[2] = t.b;
+}
+
+extern "C" void oracle_transition_medium(const ft_material* material, int front_face, const float current[5],
+                                         float out[5]) {
+  Mat<float> m;
+  m.kind = material->kind;
+  m.p = params_from<float>(*material);
+  const Medium<float> cur{current[0], sp(current[1], current[2], current[3]), current[4]};
+  const Medium<float> next = transition_medium(m, front_face != 0, cur);
+  out[0] = next.ior;
+  out[1] = next.absorption.r;
+  out[2] = next.absorption.g;
+  out[3] = next.absorption.b;
+  out[4] = next.density;
 }

@@ -70,6 +70,14 @@ int oracle_render_backward(const ft_scene_desc* desc, const ft_view* views, uint
 
 const char* oracle_last_error(void);
 
+/* The Whitted trace's medium functions in f32, for their known-answer tests.
+ * A medium is {ior, absorption r, g, b, density}.
+ * oracle_medium_transmittance: medium_transmittance (renderer.rs:5109-5119).
+ * oracle_transition_medium: transition_medium (renderer.rs:5147-5166) for an
+ * unblended material crossed at a front (1) or back (0) face. */
+void oracle_medium_transmittance(const float medium[5], float distance, float out_rgb[3]);
+void oracle_transition_medium(const ft_material* material, int front_face, const float current[5], float out[5]);
+
 #ifdef __cplusplus
 }
 #endif

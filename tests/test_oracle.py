@@ -76,6 +76,66 @@ def test_oracle_matches_reference_trace_golden(name, precision):
     assert diff.max() <= 8 and diff.mean() <= 0.35, (diff.max(), diff.mean())
 
 
+def _sphere_material(source):
+    from forgedthoughts_gb300 import _native
+
+    st = ft.parse_and_eval(source)
+    d = st.desc
+    sph = [d.nodes[i] for i in range(d.n_nodes) if d.nodes[i].kind == 0]  # FT_NODE_SPHERE
+    return _native.MaterialC.from_buffer_copy(d.materials[sph[0].material_id])  # outlives the description
+
+
+def test_medium_transmittance_known_answer():
+    """The reference's applies_medium_transmittance_per_segment: absorption
+    (0.5, 0.8, 1.0) at density 2 over 1.5 units gives (0.125, 0.512, 1)."""
+    t = oracle.medium_transmittance(1.33, (0.5, 0.8, 1.0), 2.0, 1.5)
+    assert np.allclose(t, [0.125, 0.512, 1.0], atol=1e-6), t
+    # no density or no distance: no attenuation
+    assert np.array_equal(oracle.medium_transmittance(1.33, (0.5, 0.8, 1.0), 0.0, 1.5), [1, 1, 1])
+    assert np.array_equal(oracle.medium_transmittance(1.33, (0.5, 0.8, 1.0), 2.0, 0.0), [1, 1, 1])
+
+
+def test_transition_medium_known_answer():
+    """The reference's transitions_medium_when_crossing_dielectric: entering
+    a Dielectric (IOR 1.52) with an explicit medium takes that medium, leaving
+    it returns to air.  The material comes through the `.ft` lowering."""
+    m = _sphere_material("""
+        let scene = Sphere { material: Dielectric { ior: 1.52,
+          medium: Medium { ior: 1.33, absorption_color: vec3(0.9, 0.8, 0.7), density: 0.25 } } };
+    """)
+    air = [1.0, 1.0, 1.0, 1.0, 0.0]
+    entered = oracle.transition_medium(m, True, air)
+    assert abs(entered[0] - 1.33) < 1e-6 and abs(entered[2] - 0.8) < 1e-6 and abs(entered[4] - 0.25) < 1e-6
+    exited = oracle.transition_medium(m, False, entered)
+    assert abs(exited[0] - 1.0) < 1e-6 and abs(exited[1] - 1.0) < 1e-6 and abs(exited[4]) < 1e-6
+    # without an explicit medium the material's IOR is entered, with no absorption
+    plain = _sphere_material("let scene = Sphere { material: Dielectric { ior: 1.52 } };")
+    assert np.allclose(oracle.transition_medium(plain, True, air), [1.52, 1, 1, 1, 0], atol=1e-6)
+    # an opaque material keeps the current medium
+    lam = _sphere_material("let scene = Sphere { material: Lambert { medium: Medium { density: 3.0 } } };")
+    assert np.array_equal(oracle.transition_medium(lam, True, entered), entered)
+
+
+def test_trace_absorbing_medium_darkens_the_refraction():
+    """A glass sphere with a dense blue-absorbing medium in front of a white
+    sky: the pixels seen through it lose blue relative to the same sphere
+    without the medium, and nothing else changes."""
+    base = """
+        environment Sky {{ fn color(dir) {{ return vec3(1.0, 1.0, 1.0); }} }};
+        let scene = Sphere {{ radius: 1.0, material: Dielectric {{ ior: 1.3{medium} }} }};
+    """
+    opts = ft.RenderOptions(width=24, height=24, max_steps=200, max_dist=20.0, epsilon=1e-4, camera_z=4.0)
+    plain = ft.parse_and_eval(base.format(medium=""))
+    dense = ft.parse_and_eval(base.format(
+        medium=", medium: Medium { absorption_color: vec3(0.9, 0.9, 0.2), density: 2.0 }"))
+    a, _, _ = oracle.render_trace(plain, opts, 1, 1, 4, 32)
+    b, _, _ = oracle.render_trace(dense, opts, 1, 1, 4, 32)
+    centre = (slice(9, 15), slice(9, 15))
+    assert (b[centre][..., 2] < 0.5 * a[centre][..., 2]).all()
+    assert (b[centre][..., 0] > 0.5 * a[centre][..., 0]).all()
+    assert np.array_equal(a[0, 0], b[0, 0])  # a corner ray misses the sphere
+
+
 def test_trace_f32_tracks_f64():
     st = ft.load_and_eval_scene(FIXTURES / "render_regression" / "ray_boolean_union_round.ft")
     opts = ft.RenderOptions(**TRACE_CASES["ray_boolean_union_round"])
