@@ -14,10 +14,12 @@
 // inlined.  This takes the role of the Cranelift JIT
 // (crates/forgedthoughts/src/jit.rs:501-747, 2931-3016).
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstring>
 #include <functional>
 #include <limits>
+#include <map>
 
 #include "frontend.h"
 
@@ -751,6 +753,7 @@ class Lowerer {
   uint32_t next_object_id_ = 1;
   ft_material default_material_{};
   std::vector<std::pair<const FunctionData*, int>> hook_cache_;
+  std::map<std::array<float, 7>, int32_t> pattern_programs_;  // (colour a, colour b, scale) -> program
 
   const Value* find_scene_root() {
     for (const char* k : {"scene", "result", "b", "s"}) {
@@ -798,12 +801,69 @@ class Lowerer {
   }
 
   // material_from_object (R:6439-6570), without the dynamic-hook machinery.
-  // Every model reads the `medium` field (R:6458, R:6517, R:6535, R:6564).
+  // Every model reads the `medium` and `pattern` fields (R:6458-6460,
+  // R:6517-6519, R:6535-6537, R:6564-6566).
   ft_material material_from_object(const ObjectData& o) {
     if (st_.material_defs.count(o.type_name)) return material_from_dynamic_def(*st_.material_defs.at(o.type_name), o);
     ft_material m = material_from_builtin(o);
     read_medium(o.get("medium"), &m);
+    m.color_program = pattern_program(o.get("pattern"));
     return m;
+  }
+
+  // read_pattern_field (R:6802-6825) with resolve_pattern_color (R:7233-7250):
+  // a Checker3d (or Checker) pattern gives a hit colour_a or colour_b by the
+  // parity of floor(local position * scale) summed over the axes.  It is
+  // lowered as the material's colour hook, through the hook compiler, so it
+  // runs wherever hooks run and replaces the colour where the reference's
+  // pattern does (resolve_leaf_material, R:7164-7530).  Sums of the floors
+  // in f32 equal the reference's i32 sums while |local * scale| < 2^24.
+  // One program per distinct (colours, scale); -1 for no or another pattern.
+  int32_t pattern_program(const Value* v) {
+    if (!v || v->kind != Value::Object) return -1;
+    const ObjectData& po = *v->obj;
+    std::string kind = po.type_name;
+    for (char& ch : kind) ch = static_cast<char>(std::tolower(static_cast<unsigned char>(ch)));
+    if (kind != "checker3d" && kind != "checker") return -1;
+    V3 a, b;
+    if (!read_spectrum(po, "color_a", &a) && !read_spectrum(po, "color1", &a) && !read_spectrum(po, "a", &a))
+      a = v3(0.15f, 0.15f, 0.15f);
+    if (!read_spectrum(po, "color_b", &b) && !read_spectrum(po, "color2", &b) && !read_spectrum(po, "b", &b))
+      b = v3(0.85f, 0.85f, 0.85f);
+    const float scale = std::max(number_or(po, {"scale", "frequency", "freq"}, 4.0f), 1.0e-4f);
+    const std::array<float, 7> key = {a.x, a.y, a.z, b.x, b.y, b.z, scale};
+    auto hit = pattern_programs_.find(key);
+    if (hit != pattern_programs_.end()) return hit->second;
+    // The pattern's constants enter as instance overrides of the definition's
+    // bindings, so no number is printed into source text.
+    static const std::shared_ptr<BlockDef> def = parse_program(
+        "material Checker3dPattern {\n"
+        "  model: Lambert;\n"
+        "  let color_a = vec3(0.0);\n"
+        "  let color_b = vec3(0.0);\n"
+        "  let scale = 1.0;\n"
+        "  fn color(ctx) {\n"
+        "    let s = floor(ctx.local_position * scale);\n"
+        "    let n = s.x + s.y + s.z;\n"
+        "    return mix(color_a, color_b, n - 2.0 * floor(n * 0.5));\n"
+        "  }\n"
+        "};\n")[0].block;
+    ObjectData overrides;
+    overrides.fields["color_a"] = make_vec3(a.x, a.y, a.z);
+    overrides.fields["color_b"] = make_vec3(b.x, b.y, b.z);
+    overrides.fields["scale"] = Value::number(scale);
+    int32_t idx = -1;
+    for (const BlockStmt& st : def->statements) {
+      if (st.kind != BlockStmt::Function || st.name != "color") continue;
+      HookCompiler hook(st_, out_.instrs);
+      ft_program prog;
+      if (hook.compile_ctx(st, *def, overrides, 1, &prog)) {
+        out_.programs.push_back(prog);
+        idx = static_cast<int32_t>(out_.programs.size()) - 1;
+      }
+    }
+    pattern_programs_[key] = idx;
+    return idx;
   }
 
   ft_material material_from_builtin(const ObjectData& o) {

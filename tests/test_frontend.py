@@ -252,6 +252,80 @@ def test_material_medium_defaults_clamps_and_definitions():
     assert abs(m.medium_density - 0.05) < 1e-6
 
 
+def _hook_args(local_positions):
+    a = np.zeros((len(local_positions), 7, 3), np.float32)
+    for i, lp in enumerate(local_positions):
+        a[i, 0] = a[i, 1] = lp            # position, local_position
+        a[i, 2] = (0.0, 1.0, 0.0)         # normal
+        a[i, 3] = (0.0, 0.0, 1.0)         # view_dir
+        a[i, 4] = a[i, 5] = a[i, 6] = 1   # front_face, object_id, material_id
+    return a
+
+
+def test_checker_pattern_reference_known_answer():
+    """The reference's resolves_checker_pattern_from_local_hit_position: a
+    Lambert with a Checker3d pattern (scale 2) is colour_a at local
+    (0.1, 0.1, 0.1) and colour_b at (0.6, 0.1, 0.1).  The pattern is lowered
+    as the material's colour hook; its static colour stays the given one."""
+    st = ft.parse_and_eval("""
+        let material = Lambert {
+          color: vec3(0.5),
+          pattern: Checker3d { color_a: vec3(0.1, 0.2, 0.3), color_b: vec3(0.9, 0.8, 0.7), scale: 2.0 }
+        };
+        let scene = Sphere { material: material };
+    """)
+    d = st.desc
+    m = d.materials[d.nodes[d.root].material_id]
+    assert m.kind == _native.FT_MAT_LAMBERT and m.color_program >= 0 and list(m.color) == [0.5, 0.5, 0.5]
+    c = oracle.eval_program(st, m.color_program, _hook_args([(0.1, 0.1, 0.1), (0.6, 0.1, 0.1)]))
+    assert np.allclose(c[0], [0.1, 0.2, 0.3], atol=1e-6) and np.allclose(c[1], [0.9, 0.8, 0.7], atol=1e-6)
+    # negative cells follow the integer parity of the floors: floor(-0.2) = -1 is odd
+    c = oracle.eval_program(st, m.color_program, _hook_args([(-0.1, 0.1, 0.1), (-0.6, -0.6, 0.2)]))
+    assert np.allclose(c[0], [0.9, 0.8, 0.7], atol=1e-6) and np.allclose(c[1], [0.1, 0.2, 0.3], atol=1e-6)
+    # colours are exactly the given constants (a select, not a blend)
+    assert np.array_equal(c.astype(np.float32)[1], np.array([0.1, 0.2, 0.3], np.float32))
+
+
+def test_checker_pattern_defaults_aliases_and_sharing():
+    """read_pattern_field's aliases (color1/color2, frequency) and defaults
+    (0.15 / 0.85 grey, scale 4); every model takes a pattern; another pattern
+    type is ignored; primitives with the same pattern share one program."""
+    st = ft.parse_and_eval("""
+        let a = Sphere { material: Metal { pattern: Checker { } } };
+        let b = Sphere { pos: vec3(3, 0, 0), material: Dielectric { pattern: checker3d { color1: vec3(1, 0, 0),
+                                                                               color2: vec3(0, 0, 1), frequency: 1.0 } } };
+        let c = Sphere { pos: vec3(6, 0, 0), material: Metal { pattern: Checker { } } };
+        let d = Sphere { pos: vec3(9, 0, 0), material: Lambert { pattern: Stripes { } } };
+        let scene = a + b + c + d;
+    """)
+    d = st.desc
+    sph = [d.nodes[i] for i in range(d.n_nodes) if d.nodes[i].kind == 0]
+    mats = [d.materials[n.material_id] for n in sph]
+    assert mats[0].kind == _native.FT_MAT_METAL and mats[0].color_program >= 0
+    assert mats[2].color_program == mats[0].color_program and d.n_programs == 2
+    assert mats[3].color_program == -1
+    c = oracle.eval_program(st, mats[0].color_program, _hook_args([(0.1, 0.1, 0.1), (0.3, 0.1, 0.1)]))
+    assert np.allclose(c, [[0.15] * 3, [0.85] * 3], atol=1e-6)  # scale 4: floor(1.2) = 1 is odd
+    c = oracle.eval_program(st, mats[1].color_program, _hook_args([(0.5, 0.5, 0.5), (1.5, 0.5, 0.5)]))
+    assert np.allclose(c, [[1, 0, 0], [0, 0, 1]], atol=1e-6)
+
+
+def test_checker_pattern_renders_both_colours():
+    """Traced through the oracle, a checkered sphere under a white sky shows
+    pixels of both colours."""
+    st = ft.parse_and_eval("""
+        environment Sky { fn color(dir) { return vec3(1.0, 1.0, 1.0); } };
+        let scene = Sphere { radius: 1.0, material: Lambert {
+          pattern: Checker3d { color_a: vec3(1.0, 0.0, 0.0), color_b: vec3(0.0, 0.0, 1.0), scale: 3.0 } } };
+    """)
+    opts = ft.RenderOptions(width=32, height=32, max_steps=200, max_dist=20.0, epsilon=1e-4, camera_z=4.0)
+    rgb, _, _ = oracle.render_trace(st, opts, 1, 1, 2, 32)
+    hit = rgb[8:24, 8:24].reshape(-1, 3)
+    reds = (hit[:, 0] > 0.05) & (hit[:, 2] < 0.01)
+    blues = (hit[:, 2] > 0.05) & (hit[:, 0] < 0.01)
+    assert reds.sum() > 20 and blues.sum() > 20, (reds.sum(), blues.sum())
+
+
 HOOK_MATERIALS = """
 material Stripe {
   model: Lambert;
