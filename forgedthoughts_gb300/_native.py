@@ -27,6 +27,18 @@ FT_ERR_NO_DEVICE = 11
 FT_ERR_JIT = 12
 FT_ERR_INTERNAL = 13
 
+# ft_light_kind
+FT_LIGHT_POINT = 0
+FT_LIGHT_ENV = 1
+FT_LIGHT_SPHERE = 2
+
+# ft_node_kind: the primitives
+FT_NODE_SPHERE = 0
+FT_NODE_BOX = 1
+FT_NODE_CYLINDER = 2
+FT_NODE_TORUS = 3
+FT_NODE_EXTRUDE_POLYGON = 4
+
 FT_FLAG_DEVICE_POINTERS = 1
 FT_FLAG_FP16_BRICKS = 2
 FT_BRICK_FREE_FAR_STEPS = 1
