@@ -147,7 +147,11 @@ class SceneState:
 
     @property
     def desc(self) -> _native.SceneDescC:
-        return self._desc.contents
+        """A view of the native description; it keeps this state (which owns
+        the memory) alive, so ``parse_and_eval(src).desc`` stays valid."""
+        d = self._desc.contents
+        d._owner = self
+        return d
 
     def gpu(self) -> "GpuScene":
         if self._gpu is None:

@@ -38,6 +38,7 @@ FT_NODE_BOX = 1
 FT_NODE_CYLINDER = 2
 FT_NODE_TORUS = 3
 FT_NODE_EXTRUDE_POLYGON = 4
+FT_NODE_CUSTOM = 30
 
 FT_FLAG_DEVICE_POINTERS = 1
 FT_FLAG_FP16_BRICKS = 2

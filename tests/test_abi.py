@@ -47,3 +47,18 @@ def test_null_arguments_are_rejected():
         _native.FT_ERR_INVALID_ARGUMENT
     lib.ft_scene_destroy(None)
     lib.ft_scene_desc_free(None)
+
+
+def test_description_view_keeps_its_state_alive():
+    """`parse_and_eval(src).desc` outlives the temporary state: the view holds
+    the state that owns the native description."""
+    import gc
+
+    import forgedthoughts_gb300 as ft
+
+    d = ft.parse_and_eval("var a = Sphere{}; var b = Box { size: vec3(1.0) }; let scene = a & b;").desc
+    gc.collect()
+    others = [ft.parse_and_eval("let scene = Torus {};") for _ in range(20)]  # reuse freed memory, if any
+    root = d.nodes[d.root]
+    assert root.kind == 9 and d.nodes[root.a].kind == _native.FT_NODE_SPHERE  # FT_NODE_INTERSECT
+    assert d.nodes[root.b].kind == _native.FT_NODE_BOX and len(others) == 20

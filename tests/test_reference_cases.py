@@ -247,3 +247,73 @@ def test_resolves_environment_color_on_miss():
     assert d.environment_program >= 0
     sky = oracle.eval_program(st, d.environment_program, np.array([[[0.0, 1.0, 0.0]]], np.float32))[0]
     assert sky[2] > sky[0]
+
+
+# ---- crates/forgedthoughts/src/lib.rs tests whose values reach the scene description
+
+def test_supports_primitive_round_fields():
+    st = ft.parse_and_eval("let b = Box { size: vec3(1.0, 2.0, 3.0), round: 0.1 };")  # owns the description
+    d = st.desc
+    n = d.nodes[d.root]
+    assert n.kind == _native.FT_NODE_BOX and list(n.f[:3]) == [0.5, 1.0, 1.5] and abs(n.f[3] - 0.1) < 1e-7
+
+
+def test_supports_nested_transform_assignments():
+    st = ft.parse_and_eval("var s = Sphere{}; s.pos.x = 1.5; s.pos.y = -0.25; s.rot.z = 30.0;")
+    d = st.desc
+    n = d.nodes[d.root]
+    assert list(n.center) == [1.5, -0.25, 0.0] and list(n.rot_deg) == [0.0, 0.0, 30.0]
+
+
+@pytest.mark.parametrize("expr,kind,params", [
+    ("a & b", 9, ()),                        # FT_NODE_INTERSECT
+    ("a.union_round(b, 0.2)", 11, (0.2,)),   # FT_NODE_UNION_ROUND, r
+    ("a.diff_stairs(b, 0.3, 5.0)", 23, (0.3, 5.0)),  # FT_NODE_DIFF_STAIRS, r and n
+])
+def test_supports_intersection_and_boolean_variant_calls(expr, kind, params):
+    st = ft.parse_and_eval(f"var a = Sphere{{}}; var b = Box {{ size: vec3(1.0) }}; let scene = {expr};")
+    d = st.desc
+    n = d.nodes[d.root]
+    assert n.kind == kind and np.allclose(list(n.f[:len(params)]), params, atol=1e-7)
+    assert d.nodes[n.a].kind == _native.FT_NODE_SPHERE and d.nodes[n.b].kind == _native.FT_NODE_BOX
+
+
+def test_material_properties_accept_instance_overrides():
+    m = _root_material(ft.parse_and_eval("""
+        material Checker {
+          model: Lambert;
+          let color_a = #ffffff;
+          let scale = 3.4;
+          color = color_a;
+          roughness = scale / 10.0;
+        };
+        let scene = Sphere { material: Checker { color_a: vec3(0.2, 0.4, 0.6), scale: 6.0 } };
+    """))
+    assert np.allclose(list(m.color), [0.2, 0.4, 0.6], atol=1e-6) and abs(m.roughness - 0.6) < 1e-6
+
+
+def test_sdf_functions_accept_instance_overrides():
+    st = ft.parse_and_eval("""
+        sdf SoftBlob {
+          let radius = 1.0;
+          let warp_frequency = 4.0;
+          let warp_amount = 0.16;
+          fn bounds() {
+            return vec3(radius + 0.2, radius + warp_amount + 0.2, radius + 0.1);
+          }
+          fn warp(p) {
+            return vec3(p.x, p.y + sin(p.x * warp_frequency) * warp_amount, p.z);
+          }
+          fn distance(p) {
+            let q = warp(p);
+            return length(q) - radius;
+          }
+        };
+        let scene = SoftBlob { radius: 2.0, warp_frequency: 3.1415926535, warp_amount: 0.0 };
+    """)
+    d = st.desc
+    n = d.nodes[d.root]
+    assert n.kind == _native.FT_NODE_CUSTOM
+    assert abs(n.f[0] - 2.2) < 1e-6 and abs(n.f[1] - 2.2) < 1e-6
+    dist = oracle.eval_program(st, n.program, np.array([[[2.0, 0.0, 0.0]]], np.float32))[0, 0]
+    assert abs(dist) < 1e-6
