@@ -1,5 +1,6 @@
 """The reference renderer's own unit tests (crates/forgedthoughts/src/renderer.rs,
-`mod tests`), one by one under their names, on the CPU.  Where the reference
+`mod tests`), and those of crates/forgedthoughts/src/lib.rs whose values reach
+the scene description, one by one under their names, on the CPU.  Where the reference
 builds an `EvalState` by hand the same bindings are written as `.ft` source.
 Renders go through the oracle, on the scene description the GPU library
 consumes; material resolution goes through the lowered materials and hook
@@ -317,3 +318,71 @@ def test_sdf_functions_accept_instance_overrides():
     assert abs(n.f[0] - 2.2) < 1e-6 and abs(n.f[1] - 2.2) < 1e-6
     dist = oracle.eval_program(st, n.program, np.array([[[2.0, 0.0, 0.0]]], np.float32))[0, 0]
     assert abs(dist) < 1e-6
+
+
+def test_supports_object_level_modifier_function_assignments():
+    """Assigned `domain` / `distance_post` functions become modifier nodes
+    with their hook programs (the F8 double transform keeps both)."""
+    st = ft.parse_and_eval("""
+        var statue = Box { size: vec3(1.0, 2.0, 1.0) };
+        statue.domain = fn(p) {
+          return rotate_y(p, p.y * 10.0);
+        };
+        statue.distance_post = fn(d, p) {
+          return abs(d + sin(p.y * 20.0) * 0.01) - 0.02;
+        };
+        let scene = statue;
+    """)
+    d = st.desc
+    kinds = {d.nodes[i].kind: d.nodes[i] for i in range(d.n_nodes)}
+    assert 5 in kinds and 6 in kinds  # FT_NODE_DOMAIN, FT_NODE_DISTANCE_POST
+    assert kinds[5].program >= 0 and kinds[6].program >= 0
+    post = oracle.eval_program(st, kinds[6].program, np.array([[[0.2, 0.0, 0.0], [0.0, 0.0, 0.0]]], np.float32))
+    assert abs(post[0, 0] - 0.18) < 1e-6  # abs(0.2 + sin(0) * 0.01) - 0.02
+
+
+def test_jits_scalar_material_hook_with_ctx_members():
+    """The reference checks the value is finite; it is also the closed form
+    mix(0.08, 0.32, smoothstep(-0.2, 0.2, sin(3)))."""
+    st = ft.parse_and_eval("""
+        material Stripe {
+          model: Metal;
+          fn roughness(ctx) {
+            let phase = sin(ctx.local_position.y * 12.0);
+            let mask = smoothstep(-0.2, 0.2, phase);
+            return mix(0.08, 0.32, mask);
+          }
+        };
+        let scene = Sphere { material: Stripe {} };
+    """)
+    m = _root_material(st)
+    assert m.kind == _native.FT_MAT_METAL and m.roughness_program >= 0
+    v = oracle.eval_program(st, m.roughness_program, _hook_args((0.0, 0.25, 0.0), (0.0, 0.25, 0.0)))[0, 0]
+    t = min(max((np.sin(3.0) + 0.2) / 0.4, 0.0), 1.0)
+    assert np.isfinite(v) and abs(v - (0.08 + 0.24 * t * t * (3 - 2 * t))) < 1e-5
+
+
+def test_material_functions_accept_instance_overrides():
+    st = ft.parse_and_eval("""
+        material Checker {
+          model: Lambert;
+          let color_a = #ffffff;
+          let color_b = #000000;
+          let scale = 3.4;
+          fn checker(p, scale) {
+            let sx = step(0.0, sin(p.x * scale));
+            let sz = step(0.0, sin(p.z * scale));
+            return abs(sx - sz);
+          }
+          fn color(ctx) {
+            let m = checker(ctx.local_position, scale);
+            return mix(color_a, color_b, m);
+          }
+        };
+        let scene = Sphere { material: Checker { color_a: vec3(1.0, 0.0, 0.0), color_b: vec3(0.0, 0.0, 1.0),
+                                                 scale: 3.1415926535 } };
+    """)
+    m = _root_material(st)
+    a = oracle.eval_program(st, m.color_program, _hook_args((0.5, 0.0, 0.0), (0.5, 0.0, 0.0)))[0]
+    b = oracle.eval_program(st, m.color_program, _hook_args((1.5, 0.0, 0.0), (1.5, 0.0, 0.0)))[0]
+    assert a[0] > 0.9 and a[2] < 0.1 and b[2] > 0.9 and b[0] < 0.1
