@@ -386,3 +386,23 @@ def test_material_functions_accept_instance_overrides():
     a = oracle.eval_program(st, m.color_program, _hook_args((0.5, 0.0, 0.0), (0.5, 0.0, 0.0)))[0]
     b = oracle.eval_program(st, m.color_program, _hook_args((1.5, 0.0, 0.0), (1.5, 0.0, 0.0)))[0]
     assert a[0] > 0.9 and a[2] < 0.1 and b[2] > 0.9 and b[0] < 0.1
+
+
+def test_evaluates_environment_function():
+    """The environment colour straight up is the zenith colour: the reference
+    checks blue > 0.7; the hex literal #4d74c7 is (77, 116, 199) / 255."""
+    st = ft.parse_and_eval("""
+        environment Sky {
+          let zenith = #4d74c7;
+          let horizon = #d8e7ff;
+          fn color(dir) {
+            let t = clamp(dir.y * 0.5 + 0.5, 0.0, 1.0);
+            return mix(horizon, zenith, t);
+          }
+        };
+        let scene = Sphere {};
+    """)
+    d = st.desc
+    c = oracle.eval_program(st, d.environment_program, np.array([[[0.0, 1.0, 0.0]]], np.float32))[0]
+    assert c[2] > 0.7
+    assert np.allclose(c, np.array([77, 116, 199], np.float32) / np.float32(255), atol=1e-6)
