@@ -131,8 +131,11 @@ def build_library(force: bool = False) -> Path:
     for src in CU_SOURCES:
         obj = BUILD / (src + ".o")
         objs.append(obj)
+        # -split-compile 0: cicc and ptxas work on the kernels in parallel on
+        # every host core (ptxas alone is ~3 minutes single-threaded)
         jobs.append([nvcc, "-gencode", GENCODE, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-                     "-Xptxas", "-O3", "-I", str(INCLUDE), "-I", str(CSRC), "-c", str(CSRC / src), "-o", str(obj)])
+                     "-Xptxas", "-O3", "-split-compile", "0", "-I", str(INCLUDE), "-I", str(CSRC), "-c",
+                     str(CSRC / src), "-o", str(obj)])
     with ThreadPoolExecutor(max_workers=max(2, os.cpu_count() or 2)) as ex:
         list(ex.map(_run, jobs))
     tmp = BUILD / (LIB_NAME + ".tmp")

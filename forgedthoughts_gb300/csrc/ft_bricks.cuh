@@ -142,6 +142,26 @@ __device__ __forceinline__ bool plane_jump(const DevBricks& B, F3 q, F3 d, float
          ex > B.plane_lo[0] && ex < B.plane_hi[0] && ez > B.plane_lo[1] && ez < B.plane_hi[1];
 }
 
+// Steps of the plain march's descent onto the plane from height g >= eps on
+// a ray of downward slope sdn, step = scale x distance: the heights are
+// g (1 - c)^k with c = scale sdn, so the first sample inside the eps shell is
+// n = floor(ln(eps / g) / ln(1 - c)) + 1 steps on.  All in FP32: the closed
+// form's n is checked against the heights at n - 1 and n (one powf each) and
+// moved by one where rounding of the logarithms put it on the wrong side.
+// *along = distance travelled in those n steps, g (1 - (1 - c)^n) / sdn.
+// Returns -1 when the count does not fit (grazing rays: n > 2^24).
+__device__ __forceinline__ int plane_descent_steps(float g, float sdn, float scale, float eps, float* along) {
+  const float c = scale * sdn;
+  const float q = 1.0f - c;
+  const float x = logf(eps / g) / log1pf(-c);
+  if (!(x < 16777216.0f)) return -1;
+  int n = static_cast<int>(floorf(x)) + 1;
+  if (n > 1 && g * powf(q, static_cast<float>(n - 1)) < eps) --n;
+  else if (g * powf(q, static_cast<float>(n)) >= eps) ++n;
+  *along = (g - g * powf(q, static_cast<float>(n))) / sdn;
+  return n;
+}
+
 #ifndef FT_JIT  // build and query kernels: precompiled only
 // ------------------------------------------------------------------ build
 

@@ -992,14 +992,11 @@ __global__ void __launch_bounds__(128, 6) march_depth_persistent(DevScene S0, Ra
           // when it would run out of steps or distance on the way.
           const float sdn = -d.y;
           const float g = info.d;
-          const double c = static_cast<double>(scale) * static_cast<double>(sdn);
-          const double x = log(static_cast<double>(eps) / static_cast<double>(g)) / log1p(-c);
-          const double n = floor(x) + 1.0;
-          const double tn = static_cast<double>(traveled) +
-                            (static_cast<double>(g) - static_cast<double>(g) * pow(1.0 - c, n)) / sdn;
+          float along = 0.0f;
+          const int n = plane_descent_steps(g, sdn, scale, eps, &along);
           cx.far_step();
-          if (!(n < 1.0e9) || static_cast<double>(steps) + n >= static_cast<double>(P.max_steps) ||
-              tn > static_cast<double>(max_t)) {
+          if (n < 0 || static_cast<uint64_t>(steps) + static_cast<uint64_t>(n) >= P.max_steps ||
+              traveled + along > max_t) {
             write_miss();
             continue;
           }

@@ -425,6 +425,10 @@ struct ft_batch {
   uint8_t* d_rgb8 = nullptr;
   unsigned long long* d_counters = nullptr;
   cudaStream_t stream = nullptr;
+  // Recorded after every ft_batch_launch on the caller's stream: the calls
+  // that rewrite the tables, counters and queues of a launch wait on it, so
+  // they never touch them under a launch still running on another stream.
+  cudaEvent_t done = nullptr;
   cudaGraphExec_t exec = nullptr;
   ft_batch_tuning tuning{8, 8, 8, 0.0f};
   std::mutex mu;
@@ -873,6 +877,7 @@ ft_status ft_render_depth(ft_scene* sc, const ft_render_options* options, ft_acc
 
 ft_status ft_render_depth_preview_noalloc(ft_scene* sc, const ft_render_options* options, ft_accel_mode accel,
                                           uint32_t aa_samples, uint8_t* rgb8_out, void* stream) {
+  FT_API_BEGIN
   if (!sc || !rgb8_out) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "scene and rgb8_out must be non-null");
   if (accel < FT_ACCEL_NAIVE || accel > FT_ACCEL_BRICKS) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "unknown accel mode");
   uint32_t aa = std::max(aa_samples, 1u);
@@ -900,6 +905,7 @@ ft_status ft_render_depth_preview_noalloc(ft_scene* sc, const ft_render_options*
   FT_CUDA_TRY(cudaGetLastError(), "depth_rgb8_kernel launch");
   ftcommon::clear_last_error();
   return FT_OK;
+  FT_API_END
 }
 
 ft_status ft_render_trace(ft_scene* sc, const ft_render_options* options, ft_accel_mode accel, uint32_t aa_samples,
@@ -1238,6 +1244,7 @@ ft_status ft_batch_create(const ft_batch_item* items, uint32_t n, uint32_t flags
   b->bricks = bricks;
   b->items.assign(items, items + n);
   FT_CUDA_TRY(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  FT_CUDA_TRY(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming), "cudaEventCreate");
   uint64_t pix_total = 0, samples[2] = {0, 0};
   for (uint32_t i = 0; i < n; ++i) {
     const ft_batch_item& it = items[i];
@@ -1332,6 +1339,7 @@ ft_status ft_batch_set_tuning(ft_batch* b, const ft_batch_tuning* t) {
   if (ft_status st = check_tuning(*t)) return st;
   std::lock_guard<std::mutex> lock(b->mu);
   FT_CUDA_TRY(cudaSetDevice(b->device), "cudaSetDevice");
+  FT_CUDA_TRY(cudaEventSynchronize(b->done), "wait for the last batch launch");
   FT_CUDA_TRY(cudaStreamSynchronize(b->stream), "batch");
   b->tuning = *t;
   if (ft_status st = batch_apply_tuning(b)) return st;
@@ -1345,6 +1353,7 @@ ft_status ft_batch_autotune(ft_batch* b, ft_batch_tuning* best) {
   if (!b) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "batch must be non-null");
   std::lock_guard<std::mutex> lock(b->mu);
   FT_CUDA_TRY(cudaSetDevice(b->device), "cudaSetDevice");
+  FT_CUDA_TRY(cudaEventSynchronize(b->done), "wait for the last batch launch");
   const uint32_t tiles[3][2] = {{8, 8}, {16, 8}, {32, 8}};
   const uint32_t refills[3] = {4, 8, 16};
   cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -1390,7 +1399,12 @@ ft_status ft_batch_launch(ft_batch* b, void* stream) {
   if (!b) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "batch must be non-null");
   std::lock_guard<std::mutex> lock(b->mu);
   FT_CUDA_TRY(cudaSetDevice(b->device), "cudaSetDevice");
-  FT_CUDA_TRY(cudaGraphLaunch(b->exec, static_cast<cudaStream_t>(stream)), "cudaGraphLaunch(batch)");
+  // Two launches of one batch share its counters and queues: the graph waits
+  // for the previous launch, wherever that was enqueued.
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  FT_CUDA_TRY(cudaStreamWaitEvent(st, b->done, 0), "order after the last batch launch");
+  FT_CUDA_TRY(cudaGraphLaunch(b->exec, st), "cudaGraphLaunch(batch)");
+  FT_CUDA_TRY(cudaEventRecord(b->done, st), "record batch completion");
   ftcommon::clear_last_error();
   return FT_OK;
   FT_API_END
@@ -1435,6 +1449,7 @@ void ft_batch_destroy(ft_batch* b) {
   int prev = 0;
   cudaGetDevice(&prev);
   cudaSetDevice(b->device);
+  if (b->done) cudaEventSynchronize(b->done);
   if (b->stream) cudaStreamSynchronize(b->stream);
   if (b->exec) cudaGraphExecDestroy(b->exec);
   for (auto& p : b->part) free_part(p);
@@ -1451,6 +1466,7 @@ void ft_batch_destroy(ft_batch* b) {
   cudaFree(b->wf_shadows);
   cudaFree(b->wf_counters);
   if (b->stream) cudaStreamDestroy(b->stream);
+  if (b->done) cudaEventDestroy(b->done);
   cudaSetDevice(prev);
   delete b;
 }

@@ -399,7 +399,10 @@ typedef struct ft_render_stats {
  * width*height*max(aa,1) above FT_NOALLOC_MAX_SAMPLES fail with
  * FT_ERR_INVALID_ARGUMENT and launch nothing.  The first call on a device
  * looks up that array's device address (a one-time set-up); make that first
- * call before any stream capture.  The call allocates nothing, enqueues its
+ * call before any stream capture.  The address is kept for the life of the
+ * process, so do not use this entry point on a device after cudaDeviceReset
+ * (or any other teardown of its primary context), which moves the array.
+ * The call allocates nothing, enqueues its
  * two kernels on `stream` and returns without waiting: the image is ready
  * when the stream's work completes.  All calls share the scratch array and it
  * keeps the last call's contents, so calls whose work can overlap on the GPU
@@ -529,7 +532,10 @@ ft_status ft_batch_create(const ft_batch_item* items, uint32_t n_items, uint32_t
 ft_status ft_batch_set_tuning(ft_batch* batch, const ft_batch_tuning* tuning);
 ft_status ft_batch_autotune(ft_batch* batch, ft_batch_tuning* best);
 /* Enqueue the whole batch (one graph launch) on `stream`; returns without
- * waiting.  Calls on one batch must not overlap on the GPU. */
+ * waiting.  A launch waits on the GPU for the batch's previous launch (on
+ * whatever stream that was), and ft_batch_set_tuning, ft_batch_autotune,
+ * ft_batch_read and ft_batch_destroy wait on the host for the last launch
+ * before they touch the batch's tables, counters and queues. */
 ft_status ft_batch_launch(ft_batch* batch, void* stream);
 /* Host copies of one item's outputs after the launch has completed (the call
  * synchronises the device): t_out / mask_out (w*h*aa, depth items only),

@@ -3,9 +3,10 @@ ground plane by a closed-form step count: from height g above the plane on a
 ray of downward slope s, with step = scale x distance, heights shrink by
 (1 - scale s) per step, so the first sample inside the eps shell is
 n = floor(ln(eps / g) / ln(1 - scale s)) + 1 steps later.  This checks that
-count, in the float64 form the kernel evaluates, against a literal float32
-plain march (raymarch_hit's step rule, R:4100-4137) over random descents:
-equal, or off by one step, never more."""
+count, in the float32 form the kernel evaluates (plane_descent_steps: the
+closed form, then a check of the heights at n - 1 and n), against a literal
+float32 plain march (raymarch_hit's step rule, R:4100-4137) over random
+descents: equal, or off by one step, never more."""
 import numpy as np
 
 
@@ -23,8 +24,18 @@ def plain_steps(oy, dy, t0, top, eps, scale, min_step, limit):
 
 
 def closed_form(g, s, eps, scale):
-    c = float(scale) * float(s)
-    return int(np.floor(np.log(float(eps) / float(g)) / np.log1p(-c))) + 1
+    f = np.float32
+    g, s, eps, scale = f(g), f(s), f(eps), f(scale)
+    c = scale * s
+    q = f(1.0) - c
+    x = np.log(eps / g) / np.log1p(-c)
+    assert x.dtype == np.float32
+    n = int(np.floor(x)) + 1
+    if n > 1 and g * np.power(q, f(n - 1)) < eps:
+        n -= 1
+    elif g * np.power(q, f(n)) >= eps:
+        n += 1
+    return n
 
 
 def test_closed_form_matches_the_plain_march():

@@ -48,10 +48,10 @@ def test_batch_matches_single_renders(fp16):
                 assert np.array_equal(got["mask"], m), (k, tuning)
                 assert np.array_equal(got["rgb8"], rgb8), (k, tuning)
             else:
-                # the batch traces with the per-sample integrator, single
-                # renders with the wavefront: the same terms in another
-                # summation order, which the soft-shadow march's switch between
-                # lower bound and exact distance can amplify to ~1e-5
+                # both run the wavefront, but radiance is summed with float
+                # atomics whose order varies; the soft-shadow march's switch
+                # between lower bound and exact distance can amplify that
+                # last-bit difference to ~1e-5
                 assert np.allclose(got["rgb"], a, rtol=1e-3, atol=1e-4), (k, tuning)
                 assert np.abs(got["rgb8"].astype(int) - rgb8.astype(int)).max() <= 1, (k, tuning)
     best = b.autotune()

@@ -53,3 +53,44 @@ def test_noalloc_rejects_frames_beyond_the_scratch_limit():
     assert "scratch" in _native.last_error()
     assert 1024 * 1024 * 4 > _native.FT_NOALLOC_MAX_SAMPLES
     st.close()
+
+
+def test_noalloc_preview_matches_oracle():
+    """The preview pins to the CPU oracle's gray image, not only to the
+    regular GPU entry point (the two run different march kernels)."""
+    torch = pytest.importorskip("torch")
+    import oracle
+
+    w = workloads.spheres_on_ground(width=256, height=192)
+    st = ft.parse_and_eval(w.source)
+    _, _, _, rgb, _ = oracle.render_depth(st, w.options, int(w.accel), w.aa, 32)
+    out = torch.empty(w.options.width * w.options.height * 3, dtype=torch.uint8, device="cuda")
+    for _ in range(2):
+        out.fill_(7)
+        rc = _noalloc(st.gpu(), w.options, w.accel, w.aa, out, torch.cuda.current_stream())
+        assert rc == _native.FT_OK, _native.last_error()
+        torch.cuda.synchronize()
+        got = out.cpu().numpy().reshape(w.options.height, w.options.width, 3)
+        diff = np.abs(got.astype(int) - rgb.astype(int))
+        # one gray level of rounding where a depth sits on a quantisation edge
+        assert diff.max() <= 1 and (diff == 0).mean() >= 0.999, (diff.max(), (diff == 0).mean())
+    st.close()
+
+
+def test_noalloc_error_paths_return_a_status():
+    torch = pytest.importorskip("torch")
+    w = workloads.spheres_on_ground(width=64, height=64)
+    st = ft.parse_and_eval(w.source)
+    out = torch.empty(64 * 64 * 3, dtype=torch.uint8, device="cuda")
+    lib = _native.lib()
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    rc = lib.ft_render_depth_preview_noalloc(st.gpu().handle, None, int(w.accel), 1,
+                                             ctypes.c_void_p(out.data_ptr()), stream)
+    assert rc == _native.FT_ERR_INVALID_ARGUMENT
+    rc = lib.ft_render_depth_preview_noalloc(st.gpu().handle, ctypes.byref(w.options.to_c()), int(w.accel), 1,
+                                             None, stream)
+    assert rc == _native.FT_ERR_INVALID_ARGUMENT
+    rc = lib.ft_render_depth_preview_noalloc(st.gpu().handle, ctypes.byref(w.options.to_c()), 99, 1,
+                                             ctypes.c_void_p(out.data_ptr()), stream)
+    assert rc == _native.FT_ERR_INVALID_ARGUMENT
+    st.close()
