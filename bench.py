@@ -50,6 +50,19 @@ FLOP_BOX = 15.0
 FLOP_PRIM = 34.0
 # march step bookkeeping: point (6), |d| test, step (4)
 FLOP_STEP = 12.0
+# union_round combine (op_union_round R:6024-6029): two max, two squares, sum,
+# sqrt, min and a subtraction = 9 + 1 sqrt
+FLOP_BLEND = 10.0
+# candidate-list entry: running limit max(r, min(best, cutoff)) and the gap compare
+FLOP_CAND = 3.0
+# hook program instruction (interpreted or compiled): one operation
+FLOP_HOOK = 1.0
+
+
+def flop_count(s) -> float:
+    """FP32 operations of the counted work (an ft_render_stats)."""
+    return (s.box_tests * FLOP_BOX + s.primitive_evals * FLOP_PRIM + s.march_steps * FLOP_STEP
+            + s.blend_ops * FLOP_BLEND + s.candidate_entries * FLOP_CAND + s.hook_instrs * FLOP_HOOK)
 
 L2_FLUSH_BYTES = 256 << 20  # > 129 MB L2
 _T0 = time.perf_counter()
@@ -125,50 +138,76 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def _oracle_rows(st, w, mode: str, threads: int, rows):
+CPU_ROW_STEP = 8  # every 8th row of the frame
+
+
+def _oracle_sample(st, w, mode: str, threads: int, accel: int, col_first: int, col_step: int) -> int:
+    """The oracle over every 8th row (from row 4) and every col_step-th column
+    (from col_first) of the full frame; returns the samples traced."""
     import oracle
 
-    if mode == "trace":
-        oracle.render_trace(st, w.options, int(w.accel), w.aa, w.max_depth, 32, threads, rows=rows)
-    else:
-        oracle.render_depth(st, w.options, int(w.accel), w.aa, 32, threads, rows=rows)
+    oracle.render_sample(st, w.options, accel, w.aa, w.max_depth, mode, threads, rows=(CPU_ROW_STEP // 2, CPU_ROW_STEP),
+                         cols=(col_first, col_step))
+    return len(range(CPU_ROW_STEP // 2, w.options.height, CPU_ROW_STEP)) * \
+        len(range(col_first, w.options.width, col_step)) * w.aa
 
 
-def _row_sample(st, w, mode: str, threads: int, budget_s: float):
-    """Rows (begin, end, step) sized so one oracle pass takes about budget_s."""
-    h = w.options.height
+def _col_step(st, w, mode: str, threads: int, accel: int, budget_s: float) -> int:
+    """Column stride (a power of two, at least 64) for which one sample of
+    every 8th row takes about budget_s, from a small timed probe."""
+    import oracle
+
     t0 = time.perf_counter()
-    _oracle_rows(st, w, mode, threads, (h // 2, h // 2 + 1, 1))
-    per_row = max(time.perf_counter() - t0, 1e-3)
-    n_rows = int(min(max(budget_s / per_row, 1), h))
-    step = max(h // n_rows, 1)
-    # rows centred in their bands (a one-row sample is the middle row, not the sky)
-    return (step // 2, h, step), len(range(step // 2, h, step))
+    oracle.render_sample(st, w.options, accel, w.aa, w.max_depth, mode, threads, rows=(32, 64), cols=(32, 256))
+    probe_s = max(time.perf_counter() - t0, 1e-3)
+    probe_n = len(range(32, w.options.height, 64)) * len(range(32, w.options.width, 256)) * w.aa
+    per_sample = probe_s / max(probe_n, 1)
+    rows = len(range(CPU_ROW_STEP // 2, w.options.height, CPU_ROW_STEP))
+    step = 64
+    while step < w.options.width and rows * (w.options.width / step) * w.aa * per_sample > budget_s:
+        step *= 2
+    return step
 
 
-def _sample_text(w, mode: str, rows: int, step: int) -> str:
+def _sample_text(w, mode: str, col_step: int, n: int) -> str:
     what = (f"Whitted trace depth {w.max_depth}" if mode == "trace" else "depth march")
-    return (f"{rows} of {w.options.height} rows (every {step}th) x {w.options.width} px x {w.aa} AA samples, "
-            f"f32 C++ restatement of the reference {what}, {w.accel.name} accel")
+    frac = CPU_ROW_STEP * col_step
+    return (f"every {CPU_ROW_STEP}th row x every {col_step}th column of the {w.options.width}x{w.options.height} "
+            f"frame x {w.aa} AA samples ({n} samples, 1/{frac} of the frame; the rate extrapolates to the full "
+            f"frame), f32 C++ restatement of the reference {what}, {w.accel.name} accel")
 
 
-def cpu_baseline(w, mode: str, budget_s: float = 12.0) -> dict:
-    """Oracle (f32 restatement of the reference CPU path) on a row sample."""
+def cpu_baseline(w, mode: str, budget_s: float = 20.0) -> dict:
+    """Oracle (f32 restatement of the reference CPU path) on all host cores
+    over a strided sample of the frame: every 8th row, strided columns.  Also
+    the depth march under each accelerator mode, as `ftc bench` times
+    Naive / Bvh / Bricks (crates/ftc/src/main.rs:508-548)."""
     import forgedthoughts_gb300 as ft
 
     st = ft.parse_and_eval(w.source)
     threads = os.cpu_count() or 1
-    rows, n = _row_sample(st, w, mode, threads, budget_s)
+    step = _col_step(st, w, mode, threads, int(w.accel), budget_s)
     t0 = time.perf_counter()
-    _oracle_rows(st, w, mode, threads, rows)
+    n = _oracle_sample(st, w, mode, threads, int(w.accel), (step // 2) % step, step)
     dt = time.perf_counter() - t0
-    rays = n * w.options.width * w.aa
-    return {"value": rays / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": _sample_text(w, mode, n, rows[2]) + f", {dt:.1f} s"}
+    out = {"value": n / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": _sample_text(w, mode, step, n) + f", {dt:.1f} s"}
+    per_accel = {}
+    for accel in (ft.AccelMode.Naive, ft.AccelMode.Bvh, ft.AccelMode.Bricks):
+        dstep = _col_step(st, w, "depth", threads, int(accel), 4.0)
+        t0 = time.perf_counter()
+        dn = _oracle_sample(st, w, "depth", threads, int(accel), (dstep // 2) % dstep, dstep)
+        ddt = time.perf_counter() - t0
+        per_accel[accel.name] = {"value": dn / ddt / 1e6, "unit": UNIT, "samples": dn, "seconds": ddt,
+                                 "col_step": dstep}
+    out["depth_march_per_accel"] = per_accel
+    return out
 
 
 def run_reference(args, w) -> None:
-    """`--impl reference`: the reference algorithm on the host cores."""
+    """`--impl reference`: the reference algorithm on the host cores, each
+    step a strided sample of the frame (every 8th row; the column offset
+    moves from step to step so the steps together cover more of the frame)."""
     import forgedthoughts_gb300 as ft
 
     rank = _env_int("RANK", 0)
@@ -176,25 +215,25 @@ def run_reference(args, w) -> None:
         return
     st = ft.parse_and_eval(w.source)
     threads = os.cpu_count() or 1
-    # bounded sample per step: a fixed set of rows spread over the frame
-    budget = 60.0 / max(args.steps + args.warmup, 1)
-    rows, n = _row_sample(st, w, args.mode, threads, budget)
-    for _ in range(args.warmup):
-        _oracle_rows(st, w, args.mode, threads, rows)
-    times = []
-    for _ in range(args.steps):
+    budget = 150.0 / max(args.steps + args.warmup, 1)
+    step = _col_step(st, w, args.mode, threads, int(w.accel), budget)
+    offsets = [(k * 37 + step // 2) % step for k in range(args.warmup + args.steps)]
+    for k in range(args.warmup):
+        _oracle_sample(st, w, args.mode, threads, int(w.accel), offsets[k], step)
+    times, samples = [], 0
+    for k in range(args.steps):
         t0 = time.perf_counter()
-        _oracle_rows(st, w, args.mode, threads, rows)
+        samples += _oracle_sample(st, w, args.mode, threads, int(w.accel), offsets[args.warmup + k], step)
         times.append(time.perf_counter() - t0)
-    rays = n * w.options.width * w.aa
     total = sum(times)
-    value = rays * len(times) / total / 1e6
+    value = samples / total / 1e6
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total / len(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": _config(w, args.mode, 1) | {"sample_rows": n},
+            "config": _config(w, args.mode, 1) | {"sample_col_step": step, "sample_row_step": CPU_ROW_STEP},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": _sample_text(w, args.mode, n, rows[2]) + " per step"},
+                             "sample": _sample_text(w, args.mode, step, samples // max(len(times), 1))
+                             + " per step, column offset moving per step"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -299,16 +338,74 @@ def _time_steps(fn, steps: int, stream, flush) -> list[float]:
     return [a.elapsed_time(b) for a, b in zip(starts, stops)]
 
 
-def _kernel_roofline(r: Renderer, kernel_ms: float, peak: float, kernel: str) -> dict:
+def _counts(s) -> dict:
+    return {"distance_evals": s.distance_evals, "primitive_evals": s.primitive_evals, "box_tests": s.box_tests,
+            "march_steps": s.march_steps, "blend_ops": s.blend_ops, "candidate_entries": s.candidate_entries,
+            "hook_instrs": s.hook_instrs, "far_steps": s.far_steps, "brick_fetches": s.brick_fetches}
+
+
+def _fp32_line(flops: float, kernel_ms: float, peak: float) -> dict:
+    achieved = flops / (kernel_ms * 1e-3) / 1e12 if kernel_ms > 0 else 0.0
+    return {"achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
+            "flop": flops, "kernel_ms": kernel_ms}
+
+
+PEAK_SOURCE = "measured dependent-FMA kernel (ft_measure_fp32_peak), of measured"
+
+
+def kernel_times(lib, scene, steps: int) -> dict:
+    """Per-kernel CUDA-event times the library recorded on the launch stream
+    since profiling started, per step: {kind: (ms per step, launches per step)}."""
+    from forgedthoughts_gb300 import _native
+
+    kt = _native.KernelTimesC()
+    if lib.ft_scene_kernel_times(scene.handle, ctypes.byref(kt)) != 0:
+        raise RuntimeError(_native.last_error())
+    return {name: (kt.ms[k] / steps, kt.launches[k] / steps) for k, name in enumerate(_native.KERNEL_KIND_NAMES)
+            if kt.launches[k]}
+
+
+def trace_roofline(r: "Renderer", times: dict, peak: float) -> dict:
+    """FP32 roofline of the Whitted trace's dominant kernel (the wavefront ray
+    march), with the shade and shadow kernels and the whole wavefront beside
+    it.  FLOPs: the op counts of the counting variants of the same kernels on
+    the same frame; time: their CUDA-event times inside the timed steps."""
+    from forgedthoughts_gb300 import _native
+
+    m, sh, sd = _native.RenderStatsC(), _native.RenderStatsC(), _native.RenderStatsC()
+    w = r.w
+    if r.lib.ft_render_trace_kernel_stats(r.scene.handle, ctypes.byref(r.opts), int(w.accel), w.aa, w.max_depth,
+                                          ctypes.byref(m), ctypes.byref(sh), ctypes.byref(sd)) != 0:
+        raise RuntimeError(_native.last_error())
+    per = {}
+    total_flop = total_ms = 0.0
+    for name, st in (("wf_march_persistent", m), ("wf_shade_kernel", sh), ("wf_shadow_persistent", sd)):
+        ms, launches = times.get(name, (0.0, 0.0))
+        per[name] = _fp32_line(flop_count(st), ms, peak) | {"launches_per_step": launches,
+                                                              "avg_launch_ms": ms / launches if launches else None,
+                                                              "counts": _counts(st)}
+        total_flop += flop_count(st)
+        total_ms += ms
+    dom = per["wf_march_persistent"]
+    line = {"bound": "fp32", "achieved": dom["achieved"], "peak": peak, "unit": "TFLOP/s", "frac": dom["frac"],
+            "kernel": "wf_march_persistent", "kernel_ms_per_step": dom["kernel_ms"],
+            "avg_launch_ms": dom["avg_launch_ms"], "flop_per_step": dom["flop"], "peak_source": PEAK_SOURCE,
+            "flop_model": {"box": FLOP_BOX, "primitive": FLOP_PRIM, "march_step": FLOP_STEP, "blend": FLOP_BLEND,
+                           "candidate_entry": FLOP_CAND, "hook_instr": FLOP_HOOK},
+            "per_kernel": per, "wavefront": _fp32_line(total_flop, total_ms, peak)}
+    return line
+
+
+def depth_roofline(r: "Renderer", times: dict, peak: float) -> dict:
     s = r.stats()
-    flops = s.box_tests * FLOP_BOX + s.primitive_evals * FLOP_PRIM + s.march_steps * FLOP_STEP
-    achieved = flops / (kernel_ms * 1e-3) / 1e12
-    return {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-            "frac": achieved / peak if peak else None, "kernel": kernel, "kernel_ms": kernel_ms,
-            "flop_per_launch": flops,
-            "peak_source": "measured dependent-FMA kernel (ft_measure_fp32_peak), of measured",
-            "counts": {"distance_evals": s.distance_evals, "primitive_evals": s.primitive_evals,
-                       "box_tests": s.box_tests, "march_steps": s.march_steps}}
+    ms, launches = times.get("march_depth_persistent", (0.0, 0.0))
+    line = {"bound": "fp32", "kernel": "march_depth_persistent", "peak_source": PEAK_SOURCE,
+            "launches_per_step": launches} | _fp32_line(flop_count(s), ms, peak)
+    line["counts"] = _counts(s)
+    if s.brick_fetches:
+        # one trilinear FP16 fetch reads 8 lattice corners x 2 B
+        line["brick_fetch_gbs"] = s.brick_fetches * 16.0 / (ms * 1e-3) / 1e9 if ms > 0 else None
+    return line
 
 
 def _depth_figures(lib, scene, w, dev, stream, flush, peak: float, flags: int) -> dict:
@@ -318,15 +415,14 @@ def _depth_figures(lib, scene, w, dev, stream, flush, peak: float, flags: int) -
     for _ in range(3):
         d()
     torch.cuda.synchronize()
+    lib.ft_scene_profile(scene.handle, 1)
     d_ms = _time_steps(d, 20, stream, flush)
-    dk_ms = statistics.mean(_time_steps(lambda: d(full_outputs=False), 10, stream, flush))
-    dl = _kernel_roofline(d, dk_ms, peak, "march_depth_persistent")
+    times = kernel_times(lib, scene, 20)
+    lib.ft_scene_profile(scene.handle, 0)
+    dl = depth_roofline(d, times, peak)
     dl["traffic"], note = _traffic_summary("march_depth_persistent" + ("_fp16_bricks" if flags else ""), w)
     if note:
         dl["traffic_source"] = note
-    s = d.stats()
-    dl["counts"]["far_steps"] = s.far_steps
-    dl["counts"]["brick_fetches"] = s.brick_fetches
     return {"value": d.items * len(d_ms) / (sum(d_ms) * 1e-3) / 1e6, "unit": UNIT,
             "ms_per_step": statistics.mean(d_ms), "roofline": dl, "gpu_launches_per_step": 2}
 
@@ -689,7 +785,10 @@ def main() -> None:
         dist.barrier()
     torch.cuda.synchronize()
     r.launches = 0
+    lib.ft_scene_profile(scene.handle, 1)  # CUDA events around every launch of the timed steps
     step_ms = _time_steps(r, args.steps, stream, flush)
+    times = kernel_times(lib, scene, args.steps)
+    lib.ft_scene_profile(scene.handle, 0)
     timed_launches = r.launches
     if dist:
         dist.barrier()
@@ -701,15 +800,17 @@ def main() -> None:
     if lib.ft_measure_fp32_peak(ctypes.byref(peak)) != 0:
         raise RuntimeError(_native.last_error())
 
-    # Dominant kernel: the same launch without the output conversion pass.
-    # (the trace's kernel time is the whole wavefront: wf_march, wf_shade and
-    # wf_shadow per bounce level; its FLOP count is the statistics pass's)
-    kernel = "wavefront_trace" if args.mode == "trace" else "march_depth_persistent"
-    kernel_ms = statistics.mean(_time_steps(lambda: r(full_outputs=False), max(args.steps // 2, 3), stream, flush))
-    roofline = _kernel_roofline(r, kernel_ms, peak.value, kernel)
-    roofline["traffic"], note = _traffic_summary(kernel, w)
+    # Dominant kernel: the trace's wavefront ray march (or the depth march),
+    # timed by the CUDA events of the timed steps, FLOPs from the counting
+    # variants of the same kernels.
+    if args.mode == "trace":
+        roofline = trace_roofline(r, times, peak.value)
+    else:
+        roofline = depth_roofline(r, times, peak.value)
+    roofline["traffic"], note = _traffic_summary(roofline["kernel"], w)
     if note:
         roofline["traffic_source"] = note
+    roofline["kernel_times_per_step"] = {k: {"ms": v[0], "launches": v[1]} for k, v in times.items()}
 
     _log("roofline done; end-to-end steps")
     line = {

@@ -45,7 +45,7 @@ FT_FLAG_FP16_BRICKS = 2
 FT_BRICK_FREE_FAR_STEPS = 1
 FT_MAT_STANDARD, FT_MAT_LAMBERT, FT_MAT_METAL, FT_MAT_DIELECTRIC = 0, 1, 2, 3  # ft_material_kind
 FT_MATERIAL_HOOK_PARAMS = 7
-FT_ABI_VERSION = 2
+FT_ABI_VERSION = 3
 FT_MAX_PROGRAM_REGS = 64
 
 
@@ -119,7 +119,18 @@ class BuildInfoC(ctypes.Structure):
 class RenderStatsC(ctypes.Structure):
     _fields_ = [("rays", ctypes.c_uint64), ("distance_evals", ctypes.c_uint64), ("primitive_evals", ctypes.c_uint64),
                 ("box_tests", ctypes.c_uint64), ("hook_instrs", ctypes.c_uint64), ("march_steps", ctypes.c_uint64),
-                ("far_steps", ctypes.c_uint64), ("brick_fetches", ctypes.c_uint64)]
+                ("far_steps", ctypes.c_uint64), ("brick_fetches", ctypes.c_uint64), ("blend_ops", ctypes.c_uint64),
+                ("candidate_entries", ctypes.c_uint64)]
+
+
+FT_KERNEL_PRIMARY, FT_KERNEL_MARCH, FT_KERNEL_SHADE, FT_KERNEL_SHADOW, FT_KERNEL_PIXELS, FT_KERNEL_DEPTH_MARCH = range(6)
+FT_KERNEL_KINDS = 6
+KERNEL_KIND_NAMES = ["wf_primary_kernel", "wf_march_persistent", "wf_shade_kernel", "wf_shadow_persistent",
+                     "pixels", "march_depth_persistent"]
+
+
+class KernelTimesC(ctypes.Structure):
+    _fields_ = [("ms", ctypes.c_double * FT_KERNEL_KINDS), ("launches", ctypes.c_uint64 * FT_KERNEL_KINDS)]
 
 
 class BrickOptionsC(ctypes.Structure):
@@ -189,6 +200,11 @@ SIGNATURES = {
     "ft_measure_fp32_peak": (ctypes.c_int, [ctypes.POINTER(ctypes.c_double)]),
     "ft_render_trace_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RenderOptionsC), ctypes.c_int,
                                              ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(RenderStatsC)]),
+    "ft_render_trace_kernel_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RenderOptionsC), ctypes.c_int,
+                                                    ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(RenderStatsC),
+                                                    ctypes.POINTER(RenderStatsC), ctypes.POINTER(RenderStatsC)]),
+    "ft_scene_profile": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32]),
+    "ft_scene_kernel_times": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(KernelTimesC)]),
     "ft_batch_create": (ctypes.c_int, [ctypes.POINTER(BatchItemC), ctypes.c_uint32, ctypes.c_uint32,
                                        ctypes.POINTER(ctypes.c_void_p)]),
     "ft_batch_set_tuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(BatchTuningC)]),

@@ -110,9 +110,21 @@ struct RayParams {
 
 // Per-thread work counters (only compiled into the statistics variant).
 struct Counters {
-  unsigned long long evals, prims, boxes, hook_instrs, steps, far_steps, fetches;
+  unsigned long long evals, prims, boxes, hook_instrs, steps, far_steps, fetches, blends, cands;
 };
-constexpr int kNumCounters = 7;
+constexpr int kNumCounters = 9;
+
+// Warp sum of every counter into stats[0 .. kNumCounters) (all 32 lanes call it).
+__device__ __forceinline__ void flush_stats(const Counters& c, unsigned long long* stats) {
+  unsigned long long v[kNumCounters] = {c.evals, c.prims, c.boxes, c.hook_instrs, c.steps,
+                                        c.far_steps, c.fetches, c.blends, c.cands};
+#pragma unroll
+  for (int j = 0; j < kNumCounters; ++j) {
+    unsigned long long x = v[j];
+    for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
+    if ((threadIdx.x & 31u) == 0u && x) atomicAdd(&stats[j], x);
+  }
+}
 
 template <bool kStats>
 struct Ctx {
@@ -123,8 +135,8 @@ struct Ctx {
   __device__ void prim() {
     if (kStats) ++c.prims;
   }
-  __device__ void box() {
-    if (kStats) ++c.boxes;
+  __device__ void box(unsigned n = 1) {
+    if (kStats) c.boxes += n;
   }
   __device__ void step() {
     if (kStats) ++c.steps;
@@ -134,6 +146,13 @@ struct Ctx {
   }
   __device__ void fetch() {
     if (kStats) ++c.fetches;
+  }
+  // union_round combines of a restricted fold, candidate-list entries tested
+  __device__ void blend(unsigned n = 1) {
+    if (kStats) c.blends += n;
+  }
+  __device__ void cand() {
+    if (kStats) ++c.cands;
   }
   __device__ unsigned long long* hooks() { return kStats ? &c.hook_instrs : nullptr; }
 };
@@ -227,8 +246,9 @@ __device__ __noinline__ Info eval_generic(const DevScene& S, int first, int coun
 // N is gathered through a BVH over the tree's primitives with pruning bound
 // max(r, min(best so far, cutoff)); primitive AABBs bound their distances from
 // below, so no primitive that can change the result is skipped.
+template <bool kStats>
 __device__ __noinline__ Info ur_fold(const DevScene& S, const DevUrTree& t, const int* near_pos,
-                                     const Info* near_info, int nn);
+                                     const Info* near_info, int nn, Ctx<kStats>& cx);
 
 // Parent value of a node whose only child holding a near primitive is on
 // `side`: the other child is +inf (exact for any far subtree, see above).
@@ -242,8 +262,9 @@ __device__ __forceinline__ Info ur_lift(Info v, int side, float r) {
 // along its parent links to their lowest common ancestor, combine there, and
 // lift the result to the root.  The same operations in the same order as the
 // frame walk of ur_fold.
+template <bool kStats>
 __device__ __forceinline__ Info ur_fold_small(const DevScene& S, const DevUrTree& t, int p0, Info v0, int p1, Info v1,
-                                              int nn) {
+                                              int nn, Ctx<kStats>& cx) {
   const float r = t.r;
   int link = S.ur_prim_up[t.prim_first + p0];
   if (nn == 2) {
@@ -257,19 +278,23 @@ __device__ __forceinline__ Info ur_fold_small(const DevScene& S, const DevUrTree
       const DevUrInner& in = S.ur_inner[link >> 1];
       if (in.lo <= p1 && p1 < in.hi) break;
       v0 = ur_lift(v0, link & 1, r);
+      cx.blend();
       link = S.ur_inner_up[link >> 1];
     }
     const int lca = link >> 1;
     int l1 = S.ur_prim_up[t.prim_first + p1];
     for (int guard = 0; guard <= ftgpu::kMaxUrDepth && (l1 >> 1) != lca; ++guard) {
       v1 = ur_lift(v1, l1 & 1, r);
+      cx.blend();
       l1 = S.ur_inner_up[l1 >> 1];
     }
     v0 = ftd::combine(FT_NODE_UNION_ROUND, r, 0.0f, v0, v1);
+    cx.blend();
     link = S.ur_inner_up[lca];
   }
   for (int guard = 0; guard <= ftgpu::kMaxUrDepth && link >= 0; ++guard) {
     v0 = ur_lift(v0, link & 1, r);
+    cx.blend();
     link = S.ur_inner_up[link >> 1];
   }
   return v0;
@@ -325,6 +350,7 @@ __device__ __forceinline__ Info eval_urtree(const DevScene& S, const DevUrTree& 
     int cell = t.cell_first + ix + t.dims[0] * (iy + t.dims[1] * iz);
     uint32_t beg = S.ur_cell_offsets[cell], end = S.ur_cell_offsets[cell + 1];
     for (uint32_t k = beg; k < end; ++k) {
+      cx.cand();
       if (S.ur_cell_gaps[k] >= ftd::rmax(r, fminf(best.d, cutoff))) break;
       consider(S.ur_cell_prims[k]);
     }
@@ -357,16 +383,17 @@ __device__ __forceinline__ Info eval_urtree(const DevScene& S, const DevUrTree& 
   }
   if (overflow) return eval_generic(S, t.fallback_first, t.fallback_count, p, cx);
   if (nn == 0) return best;
-  if (nn <= 2) return ur_fold_small(S, t, np0, ni0, np1, ni1, nn);
+  if (nn <= 2) return ur_fold_small(S, t, np0, ni0, np1, ni1, nn, cx);
   near_pos[0] = np0; near_info[0] = ni0;
   near_pos[1] = np1; near_info[1] = ni1;
-  return ur_fold(S, t, near_pos, near_info, nn);
+  return ur_fold(S, t, near_pos, near_info, nn, cx);
 }
 
 // Restricted union_round fold over the subtrees holding near primitives
 // (out of line: only points within r of a primitive take it).
+template <bool kStats>
 __device__ __noinline__ Info ur_fold(const DevScene& S, const DevUrTree& t, const int* near_pos,
-                                     const Info* near_info, int nn) {
+                                     const Info* near_info, int nn, Ctx<kStats>& cx) {
   const float r = t.r;
   // Frames hold partially combined inner nodes.
   struct Frame {
@@ -405,6 +432,7 @@ __device__ __noinline__ Info ur_fold(const DevScene& S, const DevUrTree& t, cons
       continue;
     }
     Info res = ftd::combine(FT_NODE_UNION_ROUND, r, 0.0f, F.slot[0], F.slot[1]);
+    cx.blend();
     if (fp == 0) return res;
     --fp;
     fr[fp].slot[fr[fp].stage - 1] = res;
@@ -707,15 +735,7 @@ __global__ void __launch_bounds__(128) march_depth_kernel(DevScene S, RayParams 
       normal_out[3 * idx + 2] = h.normal.z;
     }
   }
-  if (kStats) {
-    unsigned long long v[5] = {cx.c.evals, cx.c.prims, cx.c.boxes, cx.c.hook_instrs, cx.c.steps};
-#pragma unroll
-    for (int k = 0; k < 5; ++k) {
-      unsigned long long x = v[k];
-      for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
-      if ((threadIdx.x & 31) == 0 && x) atomicAdd(&stats[k], x);
-    }
-  }
+  if (kStats) flush_stats(cx.c, stats);
 }
 
 // Primary ray of work item i (pixel_sample_offsets R:4838-4854, NDC map of
@@ -1059,16 +1079,7 @@ __global__ void __launch_bounds__(128, 6) march_depth_persistent(DevScene S0, Ra
       write_hit(info.mat);
     }
   }
-  if (kStats) {
-    unsigned long long v[kNumCounters] = {cx.c.evals, cx.c.prims,     cx.c.boxes,  cx.c.hook_instrs,
-                                          cx.c.steps, cx.c.far_steps, cx.c.fetches};
-#pragma unroll
-    for (int j = 0; j < kNumCounters; ++j) {
-      unsigned long long x = v[j];
-      for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
-      if (lane == 0 && x) atomicAdd(&stats[j], x);
-    }
-  }
+  if (kStats) flush_stats(cx.c, stats);
 }
 
 #ifndef FT_JIT
@@ -1125,49 +1136,6 @@ struct TraceHit {
   uint32_t mat;
   int leaf;
 };
-
-// raymarch_hit (R:4091-4139) from min_t, with the six-tap normal and the
-// winning leaf of the final evaluation.
-template <bool kStats>
-__device__ bool march_hit(const DevScene& S, const RayParams& P, F3 o, F3 d, float min_t, TraceHit* h,
-                          Ctx<kStats>& cx) {
-  float t0, t1;
-  if (!ray_aabb(o, d, S.smin, S.smax, &t0, &t1)) return false;
-  float max_t = fminf(P.max_dist, t1);
-  float traveled = fmaxf(min_t, fmaxf(t0, 0.0f));
-  float prev = traveled;
-  const float eps = P.eps;
-  const float scale = ftd::rclamp(P.step_scale, 0.05f, 1.0f);
-  const float min_step = fmaxf(eps * 0.5f, 1.0e-5f);
-  for (uint32_t s = 0; s < P.max_steps; ++s) {
-    if (traveled > max_t) return false;
-    cx.step();
-    Info info = scene_distance(S, o + d * traveled, cx);
-    if (fabsf(info.d) < eps) {
-      float lo = prev, hi = traveled;
-      for (int k = 0; k < 10; ++k) {
-        float mid = 0.5f * (lo + hi);
-        if (fabsf(scene_d(S, o + d * mid, cx)) < eps) hi = mid;
-        else lo = mid;
-      }
-      F3 pos = o + d * hi;
-      float e = fmaxf(eps * 4.0f, 1.0e-5f);
-      float dx = scene_d(S, f3(pos.x + e, pos.y, pos.z), cx) - scene_d(S, f3(pos.x - e, pos.y, pos.z), cx);
-      float dy = scene_d(S, f3(pos.x, pos.y + e, pos.z), cx) - scene_d(S, f3(pos.x, pos.y - e, pos.z), cx);
-      float dz = scene_d(S, f3(pos.x, pos.y, pos.z + e), cx) - scene_d(S, f3(pos.x, pos.y, pos.z - e), cx);
-      F3 nn = f3(dx, dy, dz);
-      h->normal = ftd::len3(nn) > 1.0e-8f ? ftd::normalize3(nn) : f3(0.0f, 1.0f, 0.0f);
-      Info fin = scene_distance_leaf(S, pos, &h->leaf, cx);
-      h->t = hi;
-      h->pos = pos;
-      h->mat = fin.mat;
-      return true;
-    }
-    prev = traveled;
-    traveled += fmaxf(fabsf(info.d) * scale, min_step);
-  }
-  return false;
-}
 
 // environment_color (R:4328-4333), falling back to the sum of EnvLight
 // radiances (env_radiance, R:4318-4326).
@@ -1306,82 +1274,7 @@ __device__ __forceinline__ void shade_hit(const DevScene& S, const RayParams& P,
   }
 }
 
-// Sink of the per-sample integrator: shadow rays are marched at once and the
-// secondary rays go to the sample's own job stack.
-template <bool kStats>
-struct StackSink {
-  const DevScene& S;
-  float eps;
-  F3 acc;
-  RayJob* stack;
-  int sp;
-  Ctx<kStats>& cx;
-  __device__ void emit(F3 v) { acc = acc + v; }
-  __device__ void light(F3 contrib, F3 o, F3 d, float max_t) {
-    float vis = shadow_visibility(S, o, d, max_t, eps, cx);
-    if (vis > 0.0f) acc = acc + contrib * vis;
-  }
-  __device__ void push(const RayJob& j) {
-    if (sp < kTraceStack) stack[sp++] = j;
-  }
-};
-
-// The full Whitted tree of one primary sample (trace_ray_recursive,
-// ray.rs:3-222), as a stack of ray jobs carrying their throughput weights.
-template <bool kStats>
-__device__ __forceinline__ F3 trace_sample(const DevScene& S, const RayParams& P, uint32_t max_depth, F3 dir,
-                                           Ctx<kStats>& cx) {
-  const float eps = P.eps;
-  RayJob stack[kTraceStack];
-  StackSink<kStats> sink{S, eps, f3(0.0f, 0.0f, 0.0f), stack, 0, cx};
-  stack[sink.sp++] = RayJob{f3(P.origin[0], P.origin[1], P.origin[2]), dir, f3(1.0f, 1.0f, 1.0f), air(), 0};
-  while (sink.sp > 0) {
-    RayJob J = stack[--sink.sp];
-    if (static_cast<uint32_t>(J.depth) >= max_depth) continue;
-    float min_t = J.depth == 0 ? 0.0f : eps * 2.0f;  // secondary_min_t (R:4175-4178)
-    TraceHit h;
-    if (!march_hit(S, P, J.o, J.d, min_t, &h, cx)) {
-      sink.emit(mul3(J.w, mul3(environment(S, J.d), transmittance(J.med, P.max_dist))));
-      continue;
-    }
-    shade_hit(S, P, J, h, sink, cx);
-  }
-  return sink.acc;
-}
-
 #include "ft_wavefront.cuh"
-
-template <bool kStats>
-__device__ __forceinline__ void flush_counters(const Ctx<kStats>& cx, unsigned long long* stats) {
-  if (kStats) {
-    unsigned long long v[5] = {cx.c.evals, cx.c.prims, cx.c.boxes, cx.c.hook_instrs, cx.c.steps};
-#pragma unroll
-    for (int k = 0; k < 5; ++k) {
-      unsigned long long x = v[k];
-      for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(0xffffffffu, x, off);
-      if ((threadIdx.x & 31) == 0 && x) atomicAdd(&stats[k], x);
-    }
-  }
-}
-
-// One thread per (pixel, AA sample).
-template <bool kStats>
-__global__ void __launch_bounds__(128) trace_kernel(DevScene S, RayParams P, uint32_t max_depth,
-                                                    float* __restrict__ sample_rgb,
-                                                    unsigned long long* __restrict__ stats) {
-  uint64_t i = static_cast<uint64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-  Ctx<kStats> cx;
-  cx.c = Counters{};
-  F3 dir;
-  size_t idx = 0;
-  if (i < P.n_items && item_ray(P, i, &dir, &idx)) {
-    F3 acc = trace_sample(S, P, max_depth, dir, cx);
-    sample_rgb[3 * idx] = acc.x;
-    sample_rgb[3 * idx + 1] = acc.y;
-    sample_rgb[3 * idx + 2] = acc.z;
-  }
-  flush_counters(cx, stats);
-}
 
 #ifndef FT_JIT  // batch, pixel, adjoint and measurement kernels: precompiled only
 // AA average per pixel and spectrum_to_rgb8_reinhard (R:3908-3921, R:5229-5239).

@@ -50,6 +50,12 @@ std::string cuda_msg(cudaError_t e, const char* what) {
 
 size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
+// Per-scene counter block: kNumCounters statistics words, then the
+// persistent depth march's work counter and its self-check flags.
+constexpr int kStatWords = 16;
+constexpr int kStatWork = 12;
+static_assert(kNumCounters <= kStatWork, "statistics overlap the work counter");
+
 }  // namespace
 
 // Scratch of ft_render_depth_preview_noalloc: FT_NOALLOC_MAX_SAMPLES refined
@@ -108,7 +114,6 @@ struct ft_scene {
   // Scene JIT (ft_scene_jit): the run-time compiled module and its kernels
   cudaLibrary_t jit_lib = nullptr;
   cudaKernel_t jit_depth[2] = {nullptr, nullptr};  // plain, FP16 bricks
-  cudaKernel_t jit_trace = nullptr;
   cudaKernel_t jit_wf[3] = {nullptr, nullptr, nullptr};  // march, shade, shadow
   int jit_blocks[2] = {1, 1};
   // Wavefront trace queues (grown on demand, reused across calls)
@@ -122,10 +127,56 @@ struct ft_scene {
   // counters, self-check flags (kWfCounters)
   unsigned long long* wf_counters = nullptr;
   uint32_t last_launches = 0;  // kernels launched by the last ft_render_depth / ft_render_trace
+  // Per-kernel CUDA-event timing (ft_scene_profile): an event pair around each
+  // launch since the last collection, and the sums per kernel kind.
+  bool profiling = false;
+  std::vector<cudaEvent_t> prof_pool;             // created on demand, reused
+  std::vector<std::pair<int, int>> prof_pending;  // (kind, first event of the pair)
+  double prof_ms[FT_KERNEL_KINDS] = {};
+  uint64_t prof_launches[FT_KERNEL_KINDS] = {};
   std::mutex mu;
 };
 
 namespace {
+
+// Record the start event of a launch of `kind` on `st` when the scene is
+// profiling; returns the pair's index for prof_end (-1: not profiling).
+int prof_begin(ft_scene* sc, cudaStream_t st, int kind) {
+  if (!sc->profiling) return -1;
+  const size_t first = 2 * sc->prof_pending.size();
+  while (sc->prof_pool.size() < first + 2) {
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) {
+      cudaGetLastError();
+      return -1;
+    }
+    sc->prof_pool.push_back(e);
+  }
+  if (cudaEventRecord(sc->prof_pool[first], st) != cudaSuccess) {
+    cudaGetLastError();
+    return -1;
+  }
+  sc->prof_pending.emplace_back(kind, static_cast<int>(first));
+  return static_cast<int>(first);
+}
+
+void prof_end(ft_scene* sc, cudaStream_t st, int first) {
+  if (first >= 0) cudaEventRecord(sc->prof_pool[first + 1], st);
+}
+
+// After the stream has completed: add the pending launches' times.
+void prof_collect(ft_scene* sc) {
+  for (const auto& pk : sc->prof_pending) {
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, sc->prof_pool[pk.second], sc->prof_pool[pk.second + 1]) == cudaSuccess) {
+      sc->prof_ms[pk.first] += ms;
+      sc->prof_launches[pk.first] += 1;
+    } else {
+      cudaGetLastError();
+    }
+  }
+  sc->prof_pending.clear();
+}
 
 ft_status upload_scene(ft_scene* sc) {
   const ftgpu::SceneImage& im = sc->img;
@@ -198,7 +249,7 @@ ft_status upload_scene(ft_scene* sc) {
   std::memcpy(d.smin, im.scene_min, sizeof(d.smin));
   std::memcpy(d.smax, im.scene_max, sizeof(d.smax));
   // [0, 8): statistics counters; [8]: work-item counter of the persistent march
-  FT_CUDA_TRY(cudaMalloc(&sc->d_stats, 16 * sizeof(unsigned long long)), "cudaMalloc(stats)");
+  FT_CUDA_TRY(cudaMalloc(&sc->d_stats, kStatWords * sizeof(unsigned long long)), "cudaMalloc(stats)");
   int sms = 0, per_sm = 0;
   FT_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, sc->device), "sm count");
   FT_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, march_depth_persistent<false, false, false>, 128, 0),
@@ -289,10 +340,10 @@ ft_status launch_depth(ft_scene* sc, const RayParams& P, cudaStream_t st, bool s
   if (blocks > 0x7fffffffull) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "image too large");
   int resident = bricks ? sc->persistent_blocks_bricks : sc->persistent_blocks;
   unsigned grid = static_cast<unsigned>(std::min<uint64_t>(blocks, static_cast<uint64_t>(resident)));
-  unsigned long long* counter = sc->d_stats + 8;
+  unsigned long long* counter = sc->d_stats + kStatWork;
   unsigned long long* st_ptr = stats ? sc->d_stats : nullptr;
   if (stats)
-    FT_CUDA_TRY(cudaMemsetAsync(sc->d_stats, 0, 16 * sizeof(unsigned long long), st), "cudaMemsetAsync(stats)");
+    FT_CUDA_TRY(cudaMemsetAsync(sc->d_stats, 0, kStatWords * sizeof(unsigned long long), st), "cudaMemsetAsync(stats)");
   else
     FT_CUDA_TRY(cudaMemsetAsync(counter, 0, 2 * sizeof(unsigned long long), st), "cudaMemsetAsync(counter)");
   const DevBricks& B = sc->bricks;
@@ -305,11 +356,14 @@ ft_status launch_depth(ft_scene* sc, const RayParams& P, cudaStream_t st, bool s
     BatchView V{};
     unsigned long long* none = nullptr;
     void* args[] = {&S, &PP, &BB, &V, &t, &mask, &mat, &normal, &none, &counter};
+    int ev = prof_begin(sc, st, FT_KERNEL_DEPTH_MARCH);
     FT_CUDA_TRY(cudaLaunchKernel(reinterpret_cast<const void*>(sc->jit_depth[bricks ? 1 : 0]), dim3(jgrid), dim3(128),
                                  args, 0, st),
                 "launch of the compiled march kernel");
+    prof_end(sc, st, ev);
     return FT_OK;
   }
+  int ev = prof_begin(sc, st, FT_KERNEL_DEPTH_MARCH);
   if (stats && bricks)
     march_depth_persistent<true, true, false><<<grid, 128, 0, st>>>(sc->dev, P, B, BatchView{}, t, mask, mat, normal, st_ptr, counter);
   else if (stats)
@@ -318,6 +372,7 @@ ft_status launch_depth(ft_scene* sc, const RayParams& P, cudaStream_t st, bool s
     march_depth_persistent<false, true, false><<<grid, 128, 0, st>>>(sc->dev, P, B, BatchView{}, t, mask, mat, normal, st_ptr, counter);
   else
     march_depth_persistent<false, false, false><<<grid, 128, 0, st>>>(sc->dev, P, B, BatchView{}, t, mask, mat, normal, st_ptr, counter);
+  prof_end(sc, st, ev);
   FT_CUDA_TRY(cudaGetLastError(), "march_depth_persistent launch");
   return FT_OK;
 }
@@ -552,15 +607,16 @@ ft_status batch_apply_tuning(ft_batch* b) {
       cudaMemsetAsync(c + nxt, 0, sizeof(unsigned long long), b->stream);
       cudaMemsetAsync(c + 2, 0, sizeof(unsigned long long), b->stream);
       cudaMemsetAsync(c + 4, 0, 2 * sizeof(unsigned long long), b->stream);
-      wf_march_persistent<true><<<mgrid, 128, 0, b->stream>>>(DevScene{}, RayParams{}, V, b->wf_jobs[cur], c + cur,
-                                                              b->wf_jobs_cap[cur], b->wf_hits, b->d_srgb, c + 4,
-                                                              c + 6);
+      wf_march_persistent<true, false><<<mgrid, 128, 0, b->stream>>>(DevScene{}, RayParams{}, V, b->wf_jobs[cur],
+                                                                     c + cur, b->wf_jobs_cap[cur], b->wf_hits,
+                                                                     b->d_srgb, c + 4, c + 6, nullptr);
       WQueues Q{b->d_srgb, b->wf_jobs[nxt], c + nxt, b->wf_jobs_cap[nxt], b->wf_shadows, c + 2,
                 b->wf_shadows_cap, reinterpret_cast<unsigned int*>(c + 3), 0};
       wf_shade_batch_kernel<<<grid, 128, 0, b->stream>>>(V, T.d_max_depth, b->wf_jobs[cur], c + cur,
                                                          b->wf_jobs_cap[cur], b->wf_hits, Q);
-      wf_shadow_persistent<true><<<sgrid, 128, 0, b->stream>>>(DevScene{}, RayParams{}, V, b->wf_shadows, c + 2,
-                                                               b->wf_shadows_cap, b->d_srgb, c + 5, c + 6);
+      wf_shadow_persistent<true, false><<<sgrid, 128, 0, b->stream>>>(DevScene{}, RayParams{}, V, b->wf_shadows,
+                                                                      c + 2, b->wf_shadows_cap, b->d_srgb, c + 5,
+                                                                      c + 6, nullptr);
     }
   }
   {
@@ -621,7 +677,7 @@ ft_status check_tuning(const ft_batch_tuning& t) {
 // size the next one; the capacities are exact upper bounds (a job pushes at
 // most two materials x two rays, and two materials x the light samples).
 ft_status trace_wavefront(ft_scene* sc, const RayParams& P, uint32_t max_depth, cudaStream_t st,
-                          uint32_t* launches) {
+                          uint32_t* launches, unsigned long long* const* kind_stats = nullptr) {
   const ftgpu::SceneImage& im = sc->img;
   uint64_t light_samples = 0;
   for (const ft_light& L : im.lights) light_samples += L.kind == FT_LIGHT_SPHERE ? std::max(L.samples, 1u) : 1u;
@@ -636,17 +692,28 @@ ft_status trace_wavefront(ft_scene* sc, const RayParams& P, uint32_t max_depth, 
   FT_CUDA_TRY(cudaMemsetAsync(c, 0, kWfCounters * sizeof(unsigned long long), st), "cudaMemsetAsync(queues)");
   unsigned long long first = n;
   FT_CUDA_TRY(cudaMemcpyAsync(c, &first, sizeof(first), cudaMemcpyHostToDevice, st), "queue count");
+  int ev = prof_begin(sc, st, FT_KERNEL_PRIMARY);
   wf_primary_kernel<<<static_cast<unsigned>((n + 127) / 128), 128, 0, st>>>(P, sc->wf_jobs[0]);
+  prof_end(sc, st, ev);
   FT_CUDA_TRY(cudaGetLastError(), "wf_primary_kernel launch");
   *launches = 1;
   int sms = 0;
   FT_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, sc->device), "sm count");
-  const void* k_march = sc->jit_wf[0] ? reinterpret_cast<const void*>(sc->jit_wf[0])
-                                      : reinterpret_cast<const void*>(wf_march_persistent<false>);
-  const void* k_shade = sc->jit_wf[1] ? reinterpret_cast<const void*>(sc->jit_wf[1])
-                                      : reinterpret_cast<const void*>(wf_shade_kernel);
-  const void* k_shadow = sc->jit_wf[2] ? reinterpret_cast<const void*>(sc->jit_wf[2])
-                                       : reinterpret_cast<const void*>(wf_shadow_persistent<false>);
+  // statistics runs take the precompiled counting variants; the run-time
+  // compiled kernels, when present, serve every other trace
+  const bool stats = kind_stats != nullptr;
+  const void* k_march = stats ? reinterpret_cast<const void*>(wf_march_persistent<false, true>)
+                        : sc->jit_wf[0] ? reinterpret_cast<const void*>(sc->jit_wf[0])
+                                        : reinterpret_cast<const void*>(wf_march_persistent<false, false>);
+  const void* k_shade = stats ? reinterpret_cast<const void*>(wf_shade_kernel<true>)
+                        : sc->jit_wf[1] ? reinterpret_cast<const void*>(sc->jit_wf[1])
+                                        : reinterpret_cast<const void*>(wf_shade_kernel<false>);
+  const void* k_shadow = stats ? reinterpret_cast<const void*>(wf_shadow_persistent<false, true>)
+                         : sc->jit_wf[2] ? reinterpret_cast<const void*>(sc->jit_wf[2])
+                                         : reinterpret_cast<const void*>(wf_shadow_persistent<false, false>);
+  unsigned long long* st_march = stats ? kind_stats[0] : nullptr;
+  unsigned long long* st_shade = stats ? kind_stats[1] : nullptr;
+  unsigned long long* st_shadow = stats ? kind_stats[2] : nullptr;
   DevScene S = sc->dev;
   RayParams PP = P;
   BatchView none{};
@@ -672,13 +739,17 @@ ft_status trace_wavefront(ft_scene* sc, const RayParams& P, uint32_t max_depth, 
     FT_CUDA_TRY(cudaMemsetAsync(march_next, 0, sizeof(unsigned long long), st), "cudaMemsetAsync(queues)");
     unsigned mgrid = static_cast<unsigned>(std::max<uint64_t>(1, std::min<uint64_t>((n + 127) / 128,
                                                                                    static_cast<uint64_t>(sms) * 6)));
-    void* margs[] = {&S, &PP, &none, &jobs, &count, &jcap, &hits, &radiance, &march_next, &flags};
+    void* margs[] = {&S, &PP, &none, &jobs, &count, &jcap, &hits, &radiance, &march_next, &flags, &st_march};
+    ev = prof_begin(sc, st, FT_KERNEL_MARCH);
     FT_CUDA_TRY(cudaLaunchKernel(k_march, dim3(mgrid), dim3(128), margs, 0, st), "wavefront march launch");
+    prof_end(sc, st, ev);
     WQueues Q{radiance, sc->wf_jobs[nxt], c + nxt, sc->wf_jobs_cap[nxt], sc->wf_shadows, c + 2,
               sc->wf_shadows_cap, reinterpret_cast<unsigned int*>(c + 3), max_depth};
     const WHit* chits = hits;
-    void* sargs[] = {&S, &PP, &jobs, &count, &jcap, &chits, &Q};
+    void* sargs[] = {&S, &PP, &jobs, &count, &jcap, &chits, &Q, &st_shade};
+    ev = prof_begin(sc, st, FT_KERNEL_SHADE);
     FT_CUDA_TRY(cudaLaunchKernel(k_shade, dim3(grid), dim3(128), sargs, 0, st), "wavefront shade launch");
+    prof_end(sc, st, ev);
     *launches += 2;
     unsigned long long h[2] = {0, 0};
     FT_CUDA_TRY(cudaMemcpyAsync(&h[0], c + nxt, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st), "queue count");
@@ -691,8 +762,10 @@ ft_status trace_wavefront(ft_scene* sc, const RayParams& P, uint32_t max_depth, 
       const unsigned long long* scount = c + 2;
       unsigned long long scap = sc->wf_shadows_cap;
       FT_CUDA_TRY(cudaMemsetAsync(shadow_next, 0, sizeof(unsigned long long), st), "cudaMemsetAsync(queues)");
-      void* hargs[] = {&S, &PP, &none, &shadows, &scount, &scap, &radiance, &shadow_next, &flags};
+      void* hargs[] = {&S, &PP, &none, &shadows, &scount, &scap, &radiance, &shadow_next, &flags, &st_shadow};
+      ev = prof_begin(sc, st, FT_KERNEL_SHADOW);
       FT_CUDA_TRY(cudaLaunchKernel(k_shadow, dim3(sgrid), dim3(128), hargs, 0, st), "wavefront shadow launch");
+      prof_end(sc, st, ev);
       *launches += 1;
     }
     n = std::min<uint64_t>(h[0], sc->wf_jobs_cap[nxt]);  // an overflowed queue holds its capacity
@@ -820,6 +893,7 @@ void ft_scene_destroy(ft_scene* sc) {
   cudaFree(sc->wf_hits);
   cudaFree(sc->wf_shadows);
   cudaFree(sc->wf_counters);
+  for (cudaEvent_t e : sc->prof_pool) cudaEventDestroy(e);
   cudaSetDevice(prev);
   delete sc;
 }
@@ -850,7 +924,9 @@ ft_status ft_render_depth(ft_scene* sc, const ft_render_options* options, ft_acc
   if (rgb8_out) {
     uint8_t* rgb = dev_ptrs ? rgb8_out : sc->d_rgb;
     uint32_t np = static_cast<uint32_t>(pixels);
+    int ev = prof_begin(sc, st, FT_KERNEL_PIXELS);
     depth_rgb8_kernel<<<(np + 255) / 256, 256, 0, st>>>(t, mask, np, aa, options->max_dist, rgb);
+    prof_end(sc, st, ev);
     FT_CUDA_TRY(cudaGetLastError(), "depth_rgb8_kernel launch");
     if (!dev_ptrs)
       FT_CUDA_TRY(cudaMemcpyAsync(rgb8_out, rgb, pixels * 3, cudaMemcpyDeviceToHost, st), "copy rgb8");
@@ -866,9 +942,10 @@ ft_status ft_render_depth(ft_scene* sc, const ft_render_options* options, ft_acc
                   "copy normal");
   }
   unsigned long long march_flags = 0;
-  FT_CUDA_TRY(cudaMemcpyAsync(&march_flags, sc->d_stats + 9, sizeof(march_flags), cudaMemcpyDeviceToHost, st),
+  FT_CUDA_TRY(cudaMemcpyAsync(&march_flags, sc->d_stats + kStatWork + 1, sizeof(march_flags), cudaMemcpyDeviceToHost, st),
               "march flags");
   FT_CUDA_TRY(cudaStreamSynchronize(st), "render");
+  prof_collect(sc);
   if (ft_status s = march_check(march_flags)) return s;
   ftcommon::clear_last_error();
   return FT_OK;
@@ -932,7 +1009,9 @@ ft_status ft_render_trace(ft_scene* sc, const ft_render_options* options, ft_acc
   float* rgbf = rgb_out ? (dev_ptrs ? rgb_out : sc->d_rgbf) : nullptr;
   uint8_t* rgb8 = rgb8_out ? (dev_ptrs ? rgb8_out : sc->d_rgb) : nullptr;
   uint32_t np = static_cast<uint32_t>(pixels);
+  int ev = prof_begin(sc, st, FT_KERNEL_PIXELS);
   trace_pixels_kernel<<<(np + 255) / 256, 256, 0, st>>>(sc->d_normal, np, aa, rgbf, rgb8);
+  prof_end(sc, st, ev);
   FT_CUDA_TRY(cudaGetLastError(), "trace_pixels_kernel launch");
   sc->last_launches = launches + 1;
   if (!dev_ptrs) {
@@ -941,15 +1020,17 @@ ft_status ft_render_trace(ft_scene* sc, const ft_render_options* options, ft_acc
     if (rgb8_out) FT_CUDA_TRY(cudaMemcpyAsync(rgb8_out, rgb8, pixels * 3, cudaMemcpyDeviceToHost, st), "copy rgb8");
   }
   FT_CUDA_TRY(cudaStreamSynchronize(st), "trace");
+  prof_collect(sc);
   ftcommon::clear_last_error();
   return FT_OK;
   FT_API_END
 }
 
-ft_status ft_render_trace_stats(ft_scene* sc, const ft_render_options* options, ft_accel_mode accel,
-                                uint32_t aa_samples, uint32_t max_depth, ft_render_stats* stats) {
-  FT_API_BEGIN
-  if (!sc || !stats) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "scene and stats must be non-null");
+// Statistics of one Whitted trace, summed per kernel kind of the wavefront
+// (march, shade, shadow) from the counting variants of the same kernels.
+static ft_status trace_kind_stats(ft_scene* sc, const ft_render_options* options, ft_accel_mode accel, uint32_t aa_samples,
+                           uint32_t max_depth, ft_render_stats out[3]) {
+  if (!sc || !out) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "scene and stats must be non-null");
   if (accel < FT_ACCEL_NAIVE || accel > FT_ACCEL_BRICKS) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "unknown accel mode");
   uint32_t aa = std::max(aa_samples, 1u);
   if (ft_status s = check_options(options, aa)) return s;
@@ -960,20 +1041,98 @@ ft_status ft_render_trace_stats(ft_scene* sc, const ft_render_options* options, 
   size_t pixels = static_cast<size_t>(options->width) * options->height;
   if (ft_status s = ensure_buffers(sc, pixels * aa, pixels)) return s;
   RayParams P = make_params(sc, *options, aa);
-  uint64_t blocks = (P.n_items + 127) / 128;
-  FT_CUDA_TRY(cudaMemset(sc->d_stats, 0, 16 * sizeof(unsigned long long)), "cudaMemset(stats)");
-  trace_kernel<true><<<static_cast<unsigned>(blocks), 128>>>(sc->dev, P, depth, sc->d_normal, sc->d_stats);
-  FT_CUDA_TRY(cudaGetLastError(), "trace_kernel launch");
-  unsigned long long h[8] = {0};
-  FT_CUDA_TRY(cudaMemcpy(h, sc->d_stats, sizeof(h), cudaMemcpyDeviceToHost), "copy stats");
+  unsigned long long* d = nullptr;
+  FT_CUDA_TRY(cudaMalloc(&d, 3 * kStatWords * sizeof(unsigned long long)), "cudaMalloc(stats)");
+  std::unique_ptr<unsigned long long, cudaError_t (*)(void*)> guard(d, cudaFree);
+  FT_CUDA_TRY(cudaMemset(d, 0, 3 * kStatWords * sizeof(unsigned long long)), "cudaMemset(stats)");
+  unsigned long long* kinds[3] = {d, d + kStatWords, d + 2 * kStatWords};
+  const bool was = sc->profiling;
+  sc->profiling = false;
+  uint32_t launches = 0;
+  ft_status st = trace_wavefront(sc, P, depth, nullptr, &launches, kinds);
+  sc->profiling = was;
+  if (st) return st;
+  unsigned long long h[3 * kStatWords];
+  FT_CUDA_TRY(cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost), "copy stats");
+  for (int k = 0; k < 3; ++k) {
+    const unsigned long long* v = h + k * kStatWords;
+    ft_render_stats& o = out[k];
+    std::memset(&o, 0, sizeof(o));
+    o.rays = pixels * aa;
+    o.distance_evals = v[0];
+    o.primitive_evals = v[1];
+    o.box_tests = v[2];
+    o.hook_instrs = v[3];
+    o.march_steps = v[4];
+    o.far_steps = v[5];
+    o.brick_fetches = v[6];
+    o.blend_ops = v[7];
+    o.candidate_entries = v[8];
+  }
+  return FT_OK;
+}
+
+ft_status ft_render_trace_stats(ft_scene* sc, const ft_render_options* options, ft_accel_mode accel,
+                                uint32_t aa_samples, uint32_t max_depth, ft_render_stats* stats) {
+  FT_API_BEGIN
+  if (!stats) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "stats must be non-null");
+  ft_render_stats k[3];
+  if (ft_status s = trace_kind_stats(sc, options, accel, aa_samples, max_depth, k)) return s;
   std::memset(stats, 0, sizeof(*stats));
-  stats->rays = pixels * aa;
-  stats->distance_evals = h[0];
-  stats->primitive_evals = h[1];
-  stats->box_tests = h[2];
-  stats->hook_instrs = h[3];
-  stats->march_steps = h[4];
+  stats->rays = k[0].rays;
+  for (const ft_render_stats& v : k) {
+    stats->distance_evals += v.distance_evals;
+    stats->primitive_evals += v.primitive_evals;
+    stats->box_tests += v.box_tests;
+    stats->hook_instrs += v.hook_instrs;
+    stats->march_steps += v.march_steps;
+    stats->far_steps += v.far_steps;
+    stats->brick_fetches += v.brick_fetches;
+    stats->blend_ops += v.blend_ops;
+    stats->candidate_entries += v.candidate_entries;
+  }
   ftcommon::clear_last_error();
+  return FT_OK;
+  FT_API_END
+}
+
+ft_status ft_render_trace_kernel_stats(ft_scene* sc, const ft_render_options* options, ft_accel_mode accel,
+                                       uint32_t aa_samples, uint32_t max_depth, ft_render_stats* march,
+                                       ft_render_stats* shade, ft_render_stats* shadow) {
+  FT_API_BEGIN
+  if (!march || !shade || !shadow) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "stats must be non-null");
+  ft_render_stats k[3];
+  if (ft_status s = trace_kind_stats(sc, options, accel, aa_samples, max_depth, k)) return s;
+  *march = k[0];
+  *shade = k[1];
+  *shadow = k[2];
+  ftcommon::clear_last_error();
+  return FT_OK;
+  FT_API_END
+}
+
+ft_status ft_scene_profile(ft_scene* sc, uint32_t enable) {
+  FT_API_BEGIN
+  if (!sc) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "scene must be non-null");
+  std::lock_guard<std::mutex> lock(sc->mu);
+  sc->profiling = enable != 0;
+  sc->prof_pending.clear();
+  for (int k = 0; k < FT_KERNEL_KINDS; ++k) {
+    sc->prof_ms[k] = 0.0;
+    sc->prof_launches[k] = 0;
+  }
+  return FT_OK;
+  FT_API_END
+}
+
+ft_status ft_scene_kernel_times(ft_scene* sc, ft_kernel_times* out) {
+  FT_API_BEGIN
+  if (!sc || !out) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "scene and out must be non-null");
+  std::lock_guard<std::mutex> lock(sc->mu);
+  for (int k = 0; k < FT_KERNEL_KINDS; ++k) {
+    out->ms[k] = sc->prof_ms[k];
+    out->launches[k] = sc->prof_launches[k];
+  }
   return FT_OK;
   FT_API_END
 }
@@ -991,12 +1150,18 @@ ft_status ft_render_depth_stats(ft_scene* sc, const ft_render_options* options, 
   if (ft_status s = ensure_buffers(sc, pixels * aa, pixels)) return s;
   RayParams P = make_params(sc, *options, aa);
   const bool bricks = (flags & FT_FLAG_FP16_BRICKS) != 0;
-  if (ft_status s = launch_depth(sc, P, nullptr, true, bricks, sc->d_t, sc->d_mask, nullptr, sc->d_normal)) return s;
-  unsigned long long h[10] = {0};
+  const bool was = sc->profiling;
+  sc->profiling = false;  // a statistics pass is not one of the timed launches
+  ft_status ls = launch_depth(sc, P, nullptr, true, bricks, sc->d_t, sc->d_mask, nullptr, sc->d_normal);
+  sc->profiling = was;
+  if (ls) return ls;
+  unsigned long long h[kStatWords] = {0};
   FT_CUDA_TRY(cudaMemcpy(h, sc->d_stats, sizeof(h), cudaMemcpyDeviceToHost), "copy stats");
   std::memset(stats, 0, sizeof(*stats));
-  if (ft_status st = march_check(h[9])) return st;
+  if (ft_status st = march_check(h[kStatWork + 1])) return st;
   stats->rays = pixels * aa;
+  stats->blend_ops = h[7];
+  stats->candidate_entries = h[8];
   stats->far_steps = h[5];
   stats->brick_fetches = h[6];
   stats->distance_evals = h[0];
@@ -1641,13 +1806,14 @@ ft_status ft_scene_jit(ft_scene* sc, ft_jit_info* info) {
                                            im.instrs.data()) +
                     "}  // namespace\n";
   out.source_bytes = src.size();
-  static const char* const kExprs[6] = {"march_depth_persistent<false, false, false>",
-                                        "march_depth_persistent<false, true, false>", "trace_kernel<false>",
-                                        "wf_march_persistent<false>", "wf_shade_kernel",
-                                        "wf_shadow_persistent<false>"};
+  constexpr int kJitKernels = 5;
+  static const char* const kExprs[kJitKernels] = {"march_depth_persistent<false, false, false>",
+                                                  "march_depth_persistent<false, true, false>",
+                                                  "wf_march_persistent<false, false>", "wf_shade_kernel<false>",
+                                                  "wf_shadow_persistent<false, false>"};
   struct Module {
     std::vector<char> cubin;
-    std::string lowered[6];
+    std::string lowered[kJitKernels];
   };
   static std::mutex cache_mu;
   static std::map<std::string, Module> cache;
@@ -1695,7 +1861,7 @@ ft_status ft_scene_jit(ft_scene* sc, ft_jit_info* info) {
     mod.cubin.resize(cubin_size);
     r = nvrtcGetCUBIN(prog, mod.cubin.data());
     if (r != NVRTC_SUCCESS) return ftcommon::fail(FT_ERR_JIT, "nvrtcGetCUBIN failed");
-    for (int k = 0; k < 6; ++k) {
+    for (int k = 0; k < kJitKernels; ++k) {
       const char* lowered = nullptr;
       r = nvrtcGetLoweredName(prog, kExprs[k], &lowered);
       if (r != NVRTC_SUCCESS || !lowered) return ftcommon::fail(FT_ERR_JIT, std::string("no kernel ") + kExprs[k]);
@@ -1708,8 +1874,8 @@ ft_status ft_scene_jit(ft_scene* sc, ft_jit_info* info) {
   cudaLibrary_t lib = nullptr;
   FT_CUDA_TRY(cudaLibraryLoadData(&lib, mod.cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0),
               "cudaLibraryLoadData(scene module)");
-  cudaKernel_t k[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
-  for (int i = 0; i < 6; ++i) {
+  cudaKernel_t k[kJitKernels] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  for (int i = 0; i < kJitKernels; ++i) {
     cudaError_t e = cudaLibraryGetKernel(&k[i], lib, mod.lowered[i].c_str());
     if (e != cudaSuccess) {
       cudaLibraryUnload(lib);
@@ -1732,10 +1898,9 @@ ft_status ft_scene_jit(ft_scene* sc, ft_jit_info* info) {
   sc->jit_lib = lib;
   sc->jit_depth[0] = k[0];
   sc->jit_depth[1] = k[1];
-  sc->jit_trace = k[2];
-  sc->jit_wf[0] = k[3];
-  sc->jit_wf[1] = k[4];
-  sc->jit_wf[2] = k[5];
+  sc->jit_wf[0] = k[2];
+  sc->jit_wf[1] = k[3];
+  sc->jit_wf[2] = k[4];
   sc->jit_blocks[0] = blocks[0];
   sc->jit_blocks[1] = blocks[1];
   auto t2 = std::chrono::steady_clock::now();

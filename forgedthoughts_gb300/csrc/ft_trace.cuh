@@ -16,7 +16,6 @@
 // the hit only.  Whether a subtree's material becomes a Blend depends only on
 // whether its primitives mix material models, a static per-node flag.
 
-constexpr int kTraceStack = 32;
 constexpr int kGather = 32;
 constexpr float kNormalEps = 1.0e-4f;  // resolve_surface_normal_at_hit epsilon (R:4411)
 
@@ -645,8 +644,10 @@ __device__ void resolve_hit(const DevScene& S, int li, F3 p, const HookCtx& hc, 
 // ---------------------------------------------------------------- lights and shadows
 // Accelerator::lower_bound over the leaf BVH (bvh_lower_bound, R:788-822):
 // the nearest leaf box.
-__device__ float scene_lower_bound(const DevScene& S, F3 p) {
+template <bool kStats>
+__device__ float scene_lower_bound(const DevScene& S, F3 p, Ctx<kStats>& cx) {
   float best = kInf;
+  cx.box();
   int stack[64];
   float slb[64];
   int sp = 0;
@@ -663,6 +664,7 @@ __device__ float scene_lower_bound(const DevScene& S, F3 p) {
     }
     if (sp + 2 > 64) break;
     float ll = node_lb(p, S.bvh[n.lhs].bmin, S.bvh[n.lhs].bmax), rl = node_lb(p, S.bvh[n.rhs].bmin, S.bvh[n.rhs].bmax);
+    cx.box(2);
     if (ll <= rl) {
       stack[sp] = n.rhs; slb[sp] = rl; ++sp;
       stack[sp] = n.lhs; slb[sp] = ll; ++sp;
@@ -672,23 +674,6 @@ __device__ float scene_lower_bound(const DevScene& S, F3 p) {
     }
   }
   return best;
-}
-
-// shadow_visibility (R:4706-4733)
-template <bool kStats>
-__device__ float shadow_visibility(const DevScene& S, F3 o, F3 d, float max_t, float eps, Ctx<kStats>& cx) {
-  float t = eps * 2.0f;
-  float vis = 1.0f;
-  for (int i = 0; i < 80; ++i) {
-    if (t >= max_t) return clamp01(vis);
-    F3 p = o + d * t;
-    float lower = fabsf(scene_lower_bound(S, p));
-    float h = lower > fmaxf(eps * 8.0f, 0.02f) ? lower : fabsf(scene_distance(S, p, cx).d);
-    if (h < eps * 4.0f) return 0.0f;
-    vis = fminf(vis, clamp01(10.0f * h / t));
-    t += fmaxf(h, eps * 2.0f);
-  }
-  return clamp01(vis);
 }
 
 // Light::sample_li_indexed (render_api.rs:172-259)

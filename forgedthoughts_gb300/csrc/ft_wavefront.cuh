@@ -128,8 +128,9 @@ __global__ void __launch_bounds__(128) wf_primary_kernel(RayParams P, WJob* __re
 }
 
 // One recorded hit: shade it into the queues.
+template <bool kStats>
 __device__ __forceinline__ void wf_shade_job(const DevScene& S, const RayParams& P, const WJob& wj, const WHit& wh,
-                                             const WQueues& Q, Ctx<false>& cx) {
+                                             const WQueues& Q, Ctx<kStats>& cx) {
   TraceHit h;
   h.t = wh.t;
   h.pos = f3(wh.pos[0], wh.pos[1], wh.pos[2]);
@@ -145,17 +146,20 @@ __device__ __forceinline__ void wf_shade_job(const DevScene& S, const RayParams&
   for (unsigned long long i = static_cast<unsigned long long>(blockIdx.x) * blockDim.x + threadIdx.x; \
        i < (n); i += static_cast<unsigned long long>(gridDim.x) * blockDim.x)
 
+// With kStats the kernel sums its work counters into stats[0 .. kNumCounters).
+template <bool kStats>
 __global__ void __launch_bounds__(128) wf_shade_kernel(DevScene S, RayParams P, const WJob* __restrict__ jobs,
                                                        const unsigned long long* __restrict__ count,
                                                        unsigned long long cap, const WHit* __restrict__ hits,
-                                                       WQueues Q) {
-  Ctx<false> cx;
+                                                       WQueues Q, unsigned long long* __restrict__ stats) {
+  Ctx<kStats> cx;
   cx.c = Counters{};
   const unsigned long long n = min(*count, cap);
   FT_GRID_STRIDE(i, n) {
     if (hits[i].leaf < 0) continue;
     wf_shade_job(S, P, jobs[i], hits[i], Q, cx);
   }
+  if (kStats) flush_stats(cx.c, stats);
 }
 
 
@@ -214,17 +218,18 @@ enum WfPhase : int { kWfMarch = 0, kWfRefine = 1, kWfNormal = 2, kWfFinal = 3 };
 // secondary_min_t (R:4175-4178), ten bisections, the six-tap normal and the
 // hit leaf's lookup (march_hit, one evaluation per iteration); a miss adds
 // the environment seen through the ray's medium.
-template <bool kBatch>
+template <bool kBatch, bool kStats>
 __global__ void __launch_bounds__(128, 6) wf_march_persistent(DevScene S0, RayParams P0, BatchView V,
                                                               const WJob* __restrict__ jobs,
                                                               const unsigned long long* __restrict__ count,
                                                               unsigned long long cap, WHit* __restrict__ hits,
                                                               float* __restrict__ radiance,
                                                               unsigned long long* __restrict__ next_job,
-                                                              unsigned long long* __restrict__ flags) {
+                                                              unsigned long long* __restrict__ flags,
+                                                              unsigned long long* __restrict__ stats) {
   const unsigned lane = threadIdx.x & 31u;
   const unsigned long long n_jobs = min(*count, cap);
-  Ctx<false> cx;
+  Ctx<kStats> cx;
   cx.c = Counters{};
   const unsigned long long t_start = __shfl_sync(0xffffffffu, lane == 0 ? ftd::global_ns() : 0ull, 0);
   uint32_t loop_iters = 0;
@@ -348,20 +353,22 @@ __global__ void __launch_bounds__(128, 6) wf_march_persistent(DevScene S0, RayPa
       if (++k == 6) phase = kWfFinal;
     }
   }
+  if (kStats) flush_stats(cx.c, stats);
 }
 
 // shadow_visibility (R:4706-4733) of every queued shadow job, one step per
 // iteration; the radiance gets contribution x visibility.
-template <bool kBatch>
+template <bool kBatch, bool kStats>
 __global__ void __launch_bounds__(128, 8) wf_shadow_persistent(DevScene S0, RayParams P0, BatchView V,
                                                                const WShadow* __restrict__ shadows,
                                                                const unsigned long long* __restrict__ count,
                                                                unsigned long long cap, float* __restrict__ radiance,
                                                                unsigned long long* __restrict__ next_job,
-                                                               unsigned long long* __restrict__ flags) {
+                                                               unsigned long long* __restrict__ flags,
+                                                               unsigned long long* __restrict__ stats) {
   const unsigned lane = threadIdx.x & 31u;
   const unsigned long long n_jobs = min(*count, cap);
-  Ctx<false> cx;
+  Ctx<kStats> cx;
   cx.c = Counters{};
   const unsigned long long t_start = __shfl_sync(0xffffffffu, lane == 0 ? ftd::global_ns() : 0ull, 0);
   uint32_t loop_iters = 0;
@@ -406,7 +413,7 @@ __global__ void __launch_bounds__(128, 8) wf_shadow_persistent(DevScene S0, RayP
       continue;
     }
     F3 p = o + d * t;
-    float lower = fabsf(scene_lower_bound(S, p));
+    float lower = fabsf(scene_lower_bound(S, p, cx));
     float h = lower > fmaxf(eps * 8.0f, 0.02f) ? lower : fabsf(scene_distance_inl(S, p, cx).d);
     if (h < eps * 4.0f) {
       finish(0.0f);
@@ -416,6 +423,7 @@ __global__ void __launch_bounds__(128, 8) wf_shadow_persistent(DevScene S0, RayP
     t += fmaxf(h, eps * 2.0f);
     ++it;
   }
+  if (kStats) flush_stats(cx.c, stats);
 }
 
 #undef FT_WF_REFILL_TOP

@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define FT_ABI_VERSION 2u
+#define FT_ABI_VERSION 3u
 
 /* Status codes.  FT_ERR_MISSING_SCENE_ROOT / UNSUPPORTED_OBJECT /
  * EXPECTED_OBJECT mirror `enum RenderError` (R:159-168); PARSE / EVAL mirror
@@ -381,6 +381,8 @@ typedef struct ft_render_stats {
   uint64_t march_steps;     /* exact (FP32) march steps */
   uint64_t far_steps;       /* far-field steps on the FP16 brick bound */
   uint64_t brick_fetches;   /* trilinear FP16 texture fetches */
+  uint64_t blend_ops;       /* union_round combines of the restricted folds */
+  uint64_t candidate_entries; /* candidate-grid list entries tested */
 } ft_render_stats;
 
 /* Depth preview for callers that cannot allocate device memory.
@@ -418,10 +420,43 @@ ft_status ft_render_depth_stats(ft_scene* scene, const ft_render_options* option
                                 ft_accel_mode accel, uint32_t aa_samples, uint32_t flags,
                                 ft_render_stats* stats);
 
-/* The same counters for a Whitted trace (ft_render_trace); output discarded. */
+/* The same counters for a Whitted trace (ft_render_trace); output discarded.
+ * They come from counting variants of the wavefront's own kernels (march,
+ * shade, shadow), summed over every bounce level. */
 ft_status ft_render_trace_stats(ft_scene* scene, const ft_render_options* options,
                                 ft_accel_mode accel, uint32_t aa_samples, uint32_t max_depth,
                                 ft_render_stats* stats);
+
+/* The trace's counters per wavefront kernel kind: the ray march
+ * (wf_march_persistent), the shading of the hits (wf_shade_kernel) and the
+ * soft-shadow march (wf_shadow_persistent).  No counterpart in the reference
+ * (measurement). */
+ft_status ft_render_trace_kernel_stats(ft_scene* scene, const ft_render_options* options,
+                                       ft_accel_mode accel, uint32_t aa_samples, uint32_t max_depth,
+                                       ft_render_stats* march, ft_render_stats* shade,
+                                       ft_render_stats* shadow);
+
+/* Per-kernel device time of a scene's renders, measured with a CUDA event
+ * pair around every launch on the launch's own stream.  No counterpart in the
+ * reference (measurement). */
+#define FT_KERNEL_PRIMARY 0     /* wf_primary_kernel: camera rays of a trace */
+#define FT_KERNEL_MARCH 1       /* wf_march_persistent: the trace's ray march */
+#define FT_KERNEL_SHADE 2       /* wf_shade_kernel */
+#define FT_KERNEL_SHADOW 3      /* wf_shadow_persistent */
+#define FT_KERNEL_PIXELS 4      /* AA average / preview pixels */
+#define FT_KERNEL_DEPTH_MARCH 5 /* march_depth_persistent */
+#define FT_KERNEL_KINDS 6
+
+typedef struct ft_kernel_times {
+  double ms[FT_KERNEL_KINDS];          /* summed launch durations */
+  uint64_t launches[FT_KERNEL_KINDS];  /* launches timed */
+} ft_kernel_times;
+
+/* enable != 0 starts timing every kernel that ft_render_depth / ft_render_trace
+ * launch on this scene (the sums restart at zero); 0 stops it. */
+ft_status ft_scene_profile(ft_scene* scene, uint32_t enable);
+/* The sums since the last ft_scene_profile call. */
+ft_status ft_scene_kernel_times(ft_scene* scene, ft_kernel_times* out);
 
 /* FP16 brick distance cache: the precision form of the depth march.
  *

@@ -42,6 +42,10 @@ def lib() -> ctypes.CDLL:
         h.oracle_render_backward.restype = ctypes.c_int
         h.oracle_render_backward.argtypes = [vp, vp, ctypes.c_uint32, vp, ctypes.c_float, vp, ctypes.c_uint32, vp,
                                              vp, ctypes.c_int, ctypes.c_int, vp]
+        h.oracle_render_sample.restype = ctypes.c_int
+        h.oracle_render_sample.argtypes = [vp, vp, ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int,
+                                           ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                           ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint64)]
         h.oracle_last_error.restype = ctypes.c_char_p
         h.oracle_medium_transmittance.restype = None
         h.oracle_medium_transmittance.argtypes = [vp, ctypes.c_float, vp]
@@ -104,6 +108,23 @@ def render_trace(state, options, accel: int, aa: int = 1, max_depth: int = 8, pr
                                      int(accel), max(int(aa), 1), int(max_depth), int(precision), int(threads), r0,
                                      r1, rs, _arr(rgb), _arr(rgb8), ctypes.byref(evals)))
     return rgb, rgb8, int(evals.value)
+
+
+def render_sample(state, options, accel: int, aa: int, max_depth: int, mode: str, threads: int = 0,
+                  rows: tuple[int, int] = (0, 1), cols: tuple[int, int] = (0, 1)) -> int:
+    """Strided pixel sample of a full frame in f32 (outputs discarded): the
+    timed CPU baseline.  ``rows`` / ``cols`` = (first, step).  Returns the
+    distance evaluations it took."""
+    from forgedthoughts_gb300 import _native
+
+    opts = options.to_c() if hasattr(options, "to_c") else options
+    assert isinstance(opts, _native.RenderOptionsC)
+    evals = ctypes.c_uint64(0)
+    _check(lib().oracle_render_sample(_vp(state.desc_ptr), ctypes.cast(ctypes.pointer(opts), ctypes.c_void_p),
+                                      int(accel), max(int(aa), 1), int(max_depth), 0 if mode == "depth" else 1,
+                                      int(threads), int(rows[0]), int(rows[1]), int(cols[0]), int(cols[1]),
+                                      ctypes.byref(evals)))
+    return int(evals.value)
 
 
 def distance(state, points: np.ndarray, accel: int = 1, precision: int = 32):

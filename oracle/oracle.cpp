@@ -933,10 +933,19 @@ Opts resolve(const ft_render_options* o) {
 // sample of a few rows still spreads over every core).
 constexpr uint32_t kSegment = 32;
 
+// Columns of a (possibly strided) pixel sample of each row.
+inline std::vector<uint32_t> sample_columns(uint32_t width, uint32_t col_begin, uint32_t col_step) {
+  std::vector<uint32_t> cols;
+  col_step = std::max(col_step, 1u);
+  for (uint32_t x = col_begin; x < width; x += col_step) cols.push_back(x);
+  return cols;
+}
+
 template <class R>
 int render_depth(const ft_scene_desc* desc, const ft_render_options* options, int accel, uint32_t aa, int threads,
                  uint32_t row_begin, uint32_t row_end, uint32_t row_step, float* t_out, uint8_t* mask_out,
-                 uint32_t* mat_out, float* normal_out, uint8_t* rgb_out, uint64_t* evals_out) {
+                 uint32_t* mat_out, float* normal_out, uint8_t* rgb_out, uint64_t* evals_out,
+                 uint32_t col_begin = 0, uint32_t col_step = 1) {
   Opts op = resolve(options);
   Scene<R> scene(*desc);
   Accel<R> acc(scene, accel);
@@ -950,7 +959,8 @@ int render_depth(const ft_scene_desc* desc, const ft_render_options* options, in
   row_end = std::min(row_end, op.height);
   std::vector<uint32_t> rows;
   for (uint32_t y = row_begin; y < row_end; y += row_step) rows.push_back(y);
-  const size_t segs = (op.width + kSegment - 1) / kSegment;  // work item: one row segment
+  std::vector<uint32_t> cols = sample_columns(op.width, col_begin, col_step);
+  const size_t segs = (cols.size() + kSegment - 1) / kSegment;  // work item: one row segment
   std::atomic<size_t> next{0};
   std::atomic<uint64_t> total{0};
   auto worker = [&]() {
@@ -959,8 +969,9 @@ int render_depth(const ft_scene_desc* desc, const ft_render_options* options, in
       size_t k = next.fetch_add(1);
       if (k >= rows.size() * segs) break;
       uint32_t y = rows[k / segs];
-      uint32_t x0 = static_cast<uint32_t>(k % segs) * kSegment, x1 = std::min(x0 + kSegment, op.width);
-      for (uint32_t x = x0; x < x1; ++x) {
+      size_t c0 = (k % segs) * kSegment, c1 = std::min(c0 + kSegment, cols.size());
+      for (size_t ci = c0; ci < c1; ++ci) {
+        const uint32_t x = cols[ci];
         float sum = 0.0f;
         for (uint32_t s = 0; s < aa; ++s) {
           float px = ((static_cast<float>(x) + offs[s].first) / static_cast<float>(op.width)) * 2.0f - 1.0f;
@@ -1779,7 +1790,8 @@ uint8_t reinhard_u8(float v) {
 template <class R>
 int render_trace(const ft_scene_desc* desc, const ft_render_options* options, int accel, uint32_t aa,
                  uint32_t max_depth, int threads, uint32_t row_begin, uint32_t row_end, uint32_t row_step,
-                 float* rgb_out, uint8_t* rgb8_out, uint64_t* evals_out) {
+                 float* rgb_out, uint8_t* rgb8_out, uint64_t* evals_out, uint32_t col_begin = 0,
+                 uint32_t col_step = 1) {
   Opts op = resolve(options);
   Scene<R> scene(*desc);
   Accel<R> acc(scene, accel);
@@ -1793,7 +1805,8 @@ int render_trace(const ft_scene_desc* desc, const ft_render_options* options, in
   row_end = std::min(row_end, op.height);
   std::vector<uint32_t> rows;
   for (uint32_t y = row_begin; y < row_end; y += row_step) rows.push_back(y);
-  const size_t segs = (op.width + kSegment - 1) / kSegment;  // work item: one row segment
+  std::vector<uint32_t> cols = sample_columns(op.width, col_begin, col_step);
+  const size_t segs = (cols.size() + kSegment - 1) / kSegment;  // work item: one row segment
   std::atomic<size_t> next{0};
   std::atomic<uint64_t> total{0};
   auto worker = [&]() {
@@ -1802,8 +1815,9 @@ int render_trace(const ft_scene_desc* desc, const ft_render_options* options, in
       size_t k = next.fetch_add(1);
       if (k >= rows.size() * segs) break;
       uint32_t y = rows[k / segs];
-      uint32_t x0 = static_cast<uint32_t>(k % segs) * kSegment, x1 = std::min(x0 + kSegment, op.width);
-      for (uint32_t x = x0; x < x1; ++x) {
+      size_t c0 = (k % segs) * kSegment, c1 = std::min(c0 + kSegment, cols.size());
+      for (size_t ci = c0; ci < c1; ++ci) {
+        const uint32_t x = cols[ci];
         Sp<float> sum = sp(0.0f, 0.0f, 0.0f);
         for (uint32_t s = 0; s < aa; ++s) {
           float px = ((static_cast<float>(x) + offs[s].first) / static_cast<float>(op.width)) * 2.0f - 1.0f;
@@ -2276,6 +2290,30 @@ extern "C" int oracle_render_trace(const ft_scene_desc* desc, const ft_render_op
                                 rgb_out, rgb8_out, evals_out);
   return render_trace<float>(desc, options, accel, aa_samples, max_depth, threads, row_begin, row_end, row_step,
                              rgb_out, rgb8_out, evals_out);
+}
+
+// Strided pixel sample (rows row_begin, +row_step ..; columns col_begin,
+// +col_step ..) of the depth march or the Whitted trace: the timed CPU
+// baseline's sample of a full frame.  mode 0: depth, else trace of max_depth.
+extern "C" int oracle_render_sample(const ft_scene_desc* desc, const ft_render_options* options, int accel,
+                                    uint32_t aa_samples, uint32_t max_depth, int mode, int threads,
+                                    uint32_t row_begin, uint32_t row_step, uint32_t col_begin, uint32_t col_step,
+                                    uint64_t* evals_out) {
+  if (int e = check_desc(desc)) return e;
+  if (!options || options->width == 0 || options->height == 0) {
+    g_error = "invalid render options";
+    return FT_ERR_INVALID_ARGUMENT;
+  }
+  const uint32_t w = options->width, h = options->height, aa = std::max(aa_samples, 1u);
+  if (mode == 0) {
+    std::vector<float> t(static_cast<size_t>(w) * h * aa);
+    std::vector<uint8_t> m(t.size());
+    return render_depth<float>(desc, options, accel, aa, threads, row_begin, h, row_step, t.data(), m.data(),
+                               nullptr, nullptr, nullptr, evals_out, col_begin, col_step);
+  }
+  std::vector<float> rgb(static_cast<size_t>(w) * h * 3);
+  return render_trace<float>(desc, options, accel, aa, max_depth, threads, row_begin, h, row_step, rgb.data(),
+                             nullptr, evals_out, col_begin, col_step);
 }
 
 extern "C" int oracle_render_views(const ft_scene_desc* desc, const ft_view* views, uint32_t n_views,

@@ -41,6 +41,15 @@ int oracle_render_trace(const ft_scene_desc* desc, const ft_render_options* opti
                         int threads, uint32_t row_begin, uint32_t row_end, uint32_t row_step,
                         float* rgb_out, uint8_t* rgb8_out, uint64_t* evals_out);
 
+/* Strided pixel sample of a full frame (every row_step-th row from
+ * row_begin, every col_step-th column from col_begin) in f32, outputs
+ * discarded: mode 0 the depth march, else the Whitted trace of max_depth.
+ * The timed CPU baseline. */
+int oracle_render_sample(const ft_scene_desc* desc, const ft_render_options* options, int accel,
+                         uint32_t aa_samples, uint32_t max_depth, int mode, int threads,
+                         uint32_t row_begin, uint32_t row_step, uint32_t col_begin, uint32_t col_step,
+                         uint64_t* evals_out);
+
 /* Accelerator distance query (`Accelerator::distance_info`) at n points
  * (xyz triples).  Outputs are nullable. */
 int oracle_distance(const ft_scene_desc* desc, int accel, int precision,

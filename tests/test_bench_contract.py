@@ -45,3 +45,18 @@ def test_reference_arm_other_ranks_exit_without_work():
     p = _run_reference_arm({"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"})
     assert p.returncode == 0, p.stderr[-2000:]
     assert p.stdout.strip() == ""
+
+
+def test_flop_model_against_hand_counts():
+    """flop_count: each counted event times its FP32 operation count."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+    from forgedthoughts_gb300 import _native
+
+    s = _native.RenderStatsC()
+    s.box_tests, s.primitive_evals, s.march_steps = 3, 2, 5
+    s.blend_ops, s.candidate_entries, s.hook_instrs = 1, 4, 7
+    # 3 boxes x 15 + 2 primitives x 34 + 5 steps x 12 + 1 blend x 10 + 4 entries x 3 + 7 hook ops
+    assert bench.flop_count(s) == 45 + 68 + 60 + 10 + 12 + 7
+    s2 = _native.RenderStatsC()
+    assert bench.flop_count(s2) == 0
