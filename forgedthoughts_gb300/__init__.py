@@ -282,7 +282,8 @@ def _ptr(a: Optional[np.ndarray]):
 
 def render_depth(state: SceneState, options: RenderOptions, accel: AccelMode = AccelMode.Bvh, aa_samples: int = 1,
                  *, want_t: bool = True, want_mask: bool = True, want_material: bool = False,
-                 want_normal: bool = False, want_rgb8: bool = True, fp16_bricks: bool = False) -> DepthImage:
+                 want_normal: bool = False, want_rgb8: bool = True, fp16_bricks: bool = False,
+                 jitter_seed: int | None = None) -> DepthImage:
     """Depth preview of ``state`` on the GPU (host output buffers).  With
     ``fp16_bricks`` the march uses the scene's FP16 brick cache
     (``state.gpu().build_bricks()`` must have run)."""
@@ -296,7 +297,8 @@ def render_depth(state: SceneState, options: RenderOptions, accel: AccelMode = A
     opts = options.to_c()
     _check(_native.lib().ft_render_depth(state.gpu().handle, ctypes.byref(opts), int(accel), aa, _ptr(t), _ptr(mask),
                                          _ptr(mat), _ptr(nrm), _ptr(rgb),
-                                         _native.FT_FLAG_FP16_BRICKS if fp16_bricks else 0, None))
+                                         (_native.FT_FLAG_FP16_BRICKS if fp16_bricks else 0)
+                                         | jitter_flags(jitter_seed), None))
     return DepthImage(w, h, aa, t, mask, mat, nrm, rgb)
 
 
@@ -309,16 +311,24 @@ class RaySettings:
     aa_samples: int = 1
 
 
+def jitter_flags(jitter_seed: int | None) -> int:
+    """Render flags of jittered AA with ``jitter_seed`` (None: the grid)."""
+    if jitter_seed is None:
+        return 0
+    return _native.FT_FLAG_JITTERED_AA | ((int(jitter_seed) & 0xFFFF) << _native.FT_JITTER_SEED_SHIFT)
+
+
 def render_trace(state: SceneState, options: RenderOptions, accel: AccelMode = AccelMode.Bvh, aa_samples: int = 1,
-                 max_depth: int = 8, *, want_linear: bool = True) -> tuple:
+                 max_depth: int = 8, *, want_linear: bool = True, jitter_seed: int | None = None) -> tuple:
     """Whitted trace of ``state`` on the GPU: (linear rgb (H, W, 3) float32 or
-    None, rgb8 (H, W, 3) uint8)."""
+    None, rgb8 (H, W, 3) uint8).  ``jitter_seed`` selects jittered AA offsets
+    (XorShift64 per pixel sample, the seed xor-ed in) instead of the grid."""
     h, w = int(options.height), int(options.width)
     lin = np.empty((h, w, 3), np.float32) if want_linear else None
     rgb8 = np.empty((h, w, 3), np.uint8)
     opts = options.to_c()
     _check(_native.lib().ft_render_trace(state.gpu().handle, ctypes.byref(opts), int(accel), max(int(aa_samples), 1),
-                                         int(max_depth), _ptr(lin), _ptr(rgb8), 0, None))
+                                         int(max_depth), _ptr(lin), _ptr(rgb8), jitter_flags(jitter_seed), None))
     return lin, rgb8
 
 

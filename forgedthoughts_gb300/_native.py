@@ -42,6 +42,8 @@ FT_NODE_CUSTOM = 30
 
 FT_FLAG_DEVICE_POINTERS = 1
 FT_FLAG_FP16_BRICKS = 2
+FT_FLAG_JITTERED_AA = 4
+FT_JITTER_SEED_SHIFT = 16
 FT_BRICK_FREE_FAR_STEPS = 1
 FT_MAT_STANDARD, FT_MAT_LAMBERT, FT_MAT_METAL, FT_MAT_DIELECTRIC = 0, 1, 2, 3  # ft_material_kind
 FT_MATERIAL_HOOK_PARAMS = 7

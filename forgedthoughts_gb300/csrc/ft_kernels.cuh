@@ -104,8 +104,55 @@ struct RayParams {
   uint32_t tiles_x;
   uint32_t tile_w, tile_h;  // pixels per work tile (rays of a tile are consecutive work items)
   uint32_t refill;          // idle lanes that make a warp of the persistent march refill
+  uint32_t jitter;          // 1: jittered AA offsets (XorShift64 per pixel sample), 0: the sqrt(aa) grid
+  uint32_t jitter_seed;     // xor-ed into each pixel sample's seed
   uint64_t n_items;
 };
+
+// XorShift64 (R:4735-4761): the jittered sub-pixel offsets of the progressive
+// renderer, seeded per pixel sample by seed_pixel_sample (R:4763-4774).
+struct XorShift64 {
+  unsigned long long state;
+  __device__ explicit XorShift64(unsigned long long seed) : state(seed == 0ull ? 0x9E3779B97F4A7C15ull : seed) {}
+  __device__ unsigned long long next_u64() {
+    unsigned long long x = state;
+    x ^= x << 13;
+    x ^= x >> 7;
+    x ^= x << 17;
+    state = x;
+    return x;
+  }
+  __device__ float next_f32() {
+    const uint32_t v = static_cast<uint32_t>(next_u64() >> 40);
+    return static_cast<float>(v) / static_cast<float>(1u << 24);
+  }
+};
+
+__device__ __forceinline__ unsigned long long seed_pixel_sample(uint32_t x, uint32_t y, uint32_t width, uint32_t s) {
+  const unsigned long long base = (static_cast<unsigned long long>(y) * width + x) * 0x9E3779B97F4A7C15ull +
+                                  0xBF58476D1CE4E5B9ull;
+  return base ^ (static_cast<unsigned long long>(s) * 0x94D049BB133111EBull) ^ 0xD6E8FEB86659FD93ull;
+}
+
+// NDC of primary sample s of pixel (px, py) before the aspect scale: the
+// sqrt(aa) x sqrt(aa) grid of pixel_sample_offsets (R:4838-4854) in the NDC
+// map of render_depth_tile (R:3951-3955), or the jittered offsets of the
+// progressive renderer (R:4008-4013).
+__device__ __forceinline__ void sample_ndc(const RayParams& P, uint32_t px, uint32_t py, uint32_t s, float* nx,
+                                           float* ny) {
+  if (P.jitter) {
+    XorShift64 rng(seed_pixel_sample(px, py, P.width, s) ^ static_cast<unsigned long long>(P.jitter_seed));
+    const float jx = rng.next_f32() - 0.5f;
+    const float jy = rng.next_f32() - 0.5f;
+    *nx = ((static_cast<float>(px) + 0.5f + jx) / static_cast<float>(P.width)) * 2.0f - 1.0f;
+    *ny = 1.0f - ((static_cast<float>(py) + 0.5f + jy) / static_cast<float>(P.height)) * 2.0f;
+    return;
+  }
+  const float sx = (static_cast<float>(s % P.grid) + 0.5f) / static_cast<float>(P.grid);
+  const float sy = (static_cast<float>(s / P.grid) + 0.5f) / static_cast<float>(P.grid);
+  *nx = ((static_cast<float>(px) + sx) / static_cast<float>(P.width)) * 2.0f - 1.0f;
+  *ny = 1.0f - ((static_cast<float>(py) + sy) / static_cast<float>(P.height)) * 2.0f;
+}
 
 
 // Per-thread work counters (only compiled into the statistics variant).
@@ -713,11 +760,8 @@ __global__ void __launch_bounds__(128) march_depth_kernel(DevScene S, RayParams 
     active = px < P.width && py < P.height;
   }
   if (active) {
-    // pixel_sample_offsets (R:4838-4854) and the NDC map of render_depth_tile.
-    float sx = (static_cast<float>(s % P.grid) + 0.5f) / static_cast<float>(P.grid);
-    float sy = (static_cast<float>(s / P.grid) + 0.5f) / static_cast<float>(P.grid);
-    float ndc_x = ((static_cast<float>(px) + sx) / static_cast<float>(P.width)) * 2.0f - 1.0f;
-    float ndc_y = 1.0f - ((static_cast<float>(py) + sy) / static_cast<float>(P.height)) * 2.0f;
+    float ndc_x, ndc_y;
+    sample_ndc(P, px, py, s, &ndc_x, &ndc_y);
     ndc_x *= P.aspect;
     F3 fwd = f3(P.fwd[0], P.fwd[1], P.fwd[2]), rt = f3(P.right[0], P.right[1], P.right[2]);
     F3 up = f3(P.up[0], P.up[1], P.up[2]);
@@ -745,10 +789,8 @@ __device__ __forceinline__ bool item_ray(const RayParams& P, uint64_t i, F3* dir
   uint32_t px, py, s;
   item_coords(P, i, &px, &py, &s);
   if (px >= P.width || py >= P.height) return false;
-  float sx = (static_cast<float>(s % P.grid) + 0.5f) / static_cast<float>(P.grid);
-  float sy = (static_cast<float>(s / P.grid) + 0.5f) / static_cast<float>(P.grid);
-  float ndc_x = ((static_cast<float>(px) + sx) / static_cast<float>(P.width)) * 2.0f - 1.0f;
-  float ndc_y = 1.0f - ((static_cast<float>(py) + sy) / static_cast<float>(P.height)) * 2.0f;
+  float ndc_x, ndc_y;
+  sample_ndc(P, px, py, s, &ndc_x, &ndc_y);
   ndc_x *= P.aspect;
   F3 fwd = f3(P.fwd[0], P.fwd[1], P.fwd[2]), rt = f3(P.right[0], P.right[1], P.right[2]);
   F3 up = f3(P.up[0], P.up[1], P.up[2]);

@@ -329,7 +329,18 @@ RayParams make_params(const ft_scene* sc, const ft_render_options& o, uint32_t a
   P.step_scale = o.step_scale;
   set_tiles(&P, 8, 4);
   P.refill = 8;
+  P.jitter = 0;
+  P.jitter_seed = 0;
   return P;
+}
+
+// FT_FLAG_JITTERED_AA: jittered sub-pixel offsets with the seed in the flags'
+// upper half.
+void apply_jitter(RayParams* P, uint32_t flags) {
+  if (flags & FT_FLAG_JITTERED_AA) {
+    P->jitter = 1;
+    P->jitter_seed = flags >> FT_JITTER_SEED_SHIFT;
+  }
 }
 
 ft_status launch_depth(ft_scene* sc, const RayParams& P, cudaStream_t st, bool stats, bool bricks, float* t,
@@ -914,6 +925,7 @@ ft_status ft_render_depth(ft_scene* sc, const ft_render_options* options, ft_acc
   size_t items = pixels * aa;
   if (ft_status s = ensure_buffers(sc, items, pixels)) return s;
   RayParams P = make_params(sc, *options, aa);
+  apply_jitter(&P, flags);
   float* t = dev_ptrs && t_out ? t_out : sc->d_t;
   uint8_t* mask = dev_ptrs && mask_out ? mask_out : sc->d_mask;
   uint32_t* mat = material_out ? (dev_ptrs ? material_out : sc->d_mat) : nullptr;
@@ -1002,6 +1014,7 @@ ft_status ft_render_trace(ft_scene* sc, const ft_render_options* options, ft_acc
   size_t items = pixels * aa;
   if (ft_status s = ensure_buffers(sc, items, pixels)) return s;
   RayParams P = make_params(sc, *options, aa);
+  apply_jitter(&P, flags);
   uint64_t blocks = (P.n_items + 127) / 128;
   if (blocks > 0x7fffffffull) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "image too large");
   uint32_t launches = 0;

@@ -27,6 +27,11 @@ struct DParams {  // MaterialParams (materials/mod.rs:66-86)
   int thin;
   F3 emission_color;
   float emission_strength;
+  // explicit medium (medium_from_value R:6826-6845), entered by transmissive
+  // materials in transition()
+  int has_medium;
+  float medium_ior, medium_density;
+  F3 medium_absorption;
 };
 
 struct DMat {  // Material incl. Blend (materials/mod.rs:214-230)
@@ -60,6 +65,10 @@ __device__ DParams params_of(const ft_material& m) {
   p.thin = m.thin_walled;
   p.emission_color = f3(m.emission_color[0], m.emission_color[1], m.emission_color[2]);
   p.emission_strength = m.emission_strength;
+  p.has_medium = m.has_medium != 0;
+  p.medium_ior = m.medium_ior;
+  p.medium_density = m.medium_density;
+  p.medium_absorption = f3(m.medium_absorption[0], m.medium_absorption[1], m.medium_absorption[2]);
   return p;
 }
 
@@ -133,6 +142,20 @@ __device__ DParams blend_params(DParams a, const DParams& b, float t) {
   a.thin = t < 0.5f ? a.thin : b.thin;
   a.emission_color = lerp_sp(a.emission_color, b.emission_color, t);
   a.emission_strength = a.emission_strength + (b.emission_strength - a.emission_strength) * t;
+  // blend_medium (R:7543-7565): two media blend (the colour through
+  // lerp_spectrum's clamped t); a single one stays on its side of t = 0.5
+  if (a.has_medium && b.has_medium) {
+    a.medium_ior = a.medium_ior + (b.medium_ior - a.medium_ior) * t;
+    a.medium_absorption = lerp_sp(a.medium_absorption, b.medium_absorption, t);
+    a.medium_density = a.medium_density + (b.medium_density - a.medium_density) * t;
+  } else if (a.has_medium) {
+    a.has_medium = t < 0.5f;
+  } else if (b.has_medium && t >= 0.5f) {
+    a.has_medium = 1;
+    a.medium_ior = b.medium_ior;
+    a.medium_absorption = b.medium_absorption;
+    a.medium_density = b.medium_density;
+  }
   return a;
 }
 
@@ -775,14 +798,19 @@ __device__ F3 transmittance(const MediumD& m, float dist) {
   return f3(powf(clamp01(m.absorption.x), e), powf(clamp01(m.absorption.y), e), powf(clamp01(m.absorption.z), e));
 }
 
-// transition_medium (R:5147-5175) for materials without an explicit medium
+// transition_medium with medium_state_from_material (R:5125-5175): entering a
+// transmissive material takes its explicit medium (IOR clamped to [1, 3],
+// density at least 0), else a medium of its IOR without absorption; leaving
+// it returns to air; other materials keep the current medium.
 __device__ MediumD transition(const DMat& m, bool front, MediumD cur) {
   int model = dom_model(m);
   const DParams& p = dom_params(m);
   bool transmissive = model == FT_MAT_DIELECTRIC || (model == FT_MAT_STANDARD && p.transmission > 0.01f);
   if (!transmissive) return cur;
-  if (front) return MediumD{ftd::rclamp(p.ior, 1.0f, 3.0f), f3(1.0f, 1.0f, 1.0f), 0.0f};
-  return air();
+  if (!front) return air();
+  if (p.has_medium)
+    return MediumD{ftd::rclamp(p.medium_ior, 1.0f, 3.0f), p.medium_absorption, fmaxf(p.medium_density, 0.0f)};
+  return MediumD{ftd::rclamp(p.ior, 1.0f, 3.0f), f3(1.0f, 1.0f, 1.0f), 0.0f};
 }
 
 struct RayJob {

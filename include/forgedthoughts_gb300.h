@@ -284,6 +284,14 @@ typedef struct ft_scene ft_scene;
 
 /* Render-call flags. */
 #define FT_FLAG_DEVICE_POINTERS 1u  /* output pointers are device memory */
+/* Jittered AA (ft_render_depth / ft_render_trace): sample s of pixel (x, y)
+ * is offset by two draws of XorShift64 seeded with
+ * seed_pixel_sample(x, y, width, s) ^ seed (R:4735-4774, the progressive
+ * renderer's sampling), seed = flags >> FT_JITTER_SEED_SHIFT, instead of the
+ * sqrt(aa) x sqrt(aa) grid of pixel_sample_offsets (R:4838-4854). */
+#define FT_FLAG_JITTERED_AA 4u
+#define FT_JITTER_SEED_SHIFT 16
+#define FT_FLAG_JITTER_SEED(seed) (((uint32_t)(seed) & 0xffffu) << FT_JITTER_SEED_SHIFT)
 #define FT_FLAG_FP16_BRICKS 2u      /* depth march through the FP16 brick cache
                                        (ft_scene_build_bricks must have run) */
 

@@ -42,6 +42,16 @@ def lib() -> ctypes.CDLL:
         h.oracle_render_backward.restype = ctypes.c_int
         h.oracle_render_backward.argtypes = [vp, vp, ctypes.c_uint32, vp, ctypes.c_float, vp, ctypes.c_uint32, vp,
                                              vp, ctypes.c_int, ctypes.c_int, vp]
+        u32, i64 = ctypes.c_uint32, ctypes.c_int64
+        h.oracle_render_depth_strided.restype = ctypes.c_int
+        h.oracle_render_depth_strided.argtypes = [vp, vp, ctypes.c_int, u32, ctypes.c_int, ctypes.c_int, u32, u32, u32,
+                                                  u32, u32, i64, vp, vp, vp, vp, vp, ctypes.POINTER(ctypes.c_uint64)]
+        h.oracle_render_trace_strided.restype = ctypes.c_int
+        h.oracle_render_trace_strided.argtypes = [vp, vp, ctypes.c_int, u32, u32, ctypes.c_int, ctypes.c_int, u32,
+                                                  u32, u32, u32, u32, i64, vp, vp, ctypes.POINTER(ctypes.c_uint64)]
+        h.oracle_render_views_strided.restype = ctypes.c_int
+        h.oracle_render_views_strided.argtypes = [vp, vp, ctypes.c_uint32, vp, ctypes.c_float, ctypes.c_int,
+                                                  ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, vp, vp, vp]
         h.oracle_render_sample.restype = ctypes.c_int
         h.oracle_render_sample.argtypes = [vp, vp, ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int,
                                            ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
@@ -69,8 +79,12 @@ def _check(rc: int) -> None:
 
 
 def render_depth(state, options, accel: int, aa: int = 1, precision: int = 32, threads: int = 0,
-                 rows: tuple[int, int, int] | None = None, normals: bool = False):
-    """Oracle depth preview.  Returns (t, mask, material, rgb8, evals[, normal])."""
+                 rows: tuple[int, int, int] | None = None, normals: bool = False,
+                 cols: tuple[int, int] | None = None, jitter_seed: int | None = None):
+    """Oracle depth preview.  Returns (t, mask, material, rgb8, evals[, normal]).
+    ``rows`` = (begin, end, step) and ``cols`` = (begin, step) restrict it to
+    a strided band (only those pixels of the full-frame outputs are written);
+    ``jitter_seed`` selects the jittered AA offsets."""
     from forgedthoughts_gb300 import _native  # scene description structs only
 
     aa = max(int(aa), 1)
@@ -83,18 +97,23 @@ def render_depth(state, options, accel: int, aa: int = 1, precision: int = 32, t
     opts = options.to_c() if hasattr(options, "to_c") else options
     assert isinstance(opts, _native.RenderOptionsC)
     r0, r1, rs = rows if rows is not None else (0, h, 1)
+    c0, cs = cols if cols is not None else (0, 1)
     evals = ctypes.c_uint64(0)
-    _check(lib().oracle_render_depth(_vp(state.desc_ptr), ctypes.cast(ctypes.pointer(opts), ctypes.c_void_p),
-                                     int(accel), aa, int(precision), int(threads), r0, r1, rs, _arr(t), _arr(mask),
-                                     _arr(mat), _arr(nrm), _arr(rgb), ctypes.byref(evals)))
+    _check(lib().oracle_render_depth_strided(_vp(state.desc_ptr), ctypes.cast(ctypes.pointer(opts), ctypes.c_void_p),
+                                             int(accel), aa, int(precision), int(threads), r0, r1, rs, c0, cs,
+                                             -1 if jitter_seed is None else int(jitter_seed),
+                                             _arr(t), _arr(mask), _arr(mat), _arr(nrm), _arr(rgb),
+                                             ctypes.byref(evals)))
     if normals:
         return t, mask, mat, rgb, int(evals.value), nrm
     return t, mask, mat, rgb, int(evals.value)
 
 
 def render_trace(state, options, accel: int, aa: int = 1, max_depth: int = 8, precision: int = 32,
-                 threads: int = 0, rows: tuple[int, int, int] | None = None):
-    """Oracle Whitted trace.  Returns (rgb linear float (H, W, 3), rgb8, evals)."""
+                 threads: int = 0, rows: tuple[int, int, int] | None = None, cols: tuple[int, int] | None = None,
+                 jitter_seed: int | None = None):
+    """Oracle Whitted trace.  Returns (rgb linear float (H, W, 3), rgb8, evals).
+    ``rows`` / ``cols`` / ``jitter_seed`` as in render_depth."""
     from forgedthoughts_gb300 import _native
 
     h, w = int(options.height), int(options.width)
@@ -103,10 +122,13 @@ def render_trace(state, options, accel: int, aa: int = 1, max_depth: int = 8, pr
     opts = options.to_c() if hasattr(options, "to_c") else options
     assert isinstance(opts, _native.RenderOptionsC)
     r0, r1, rs = rows if rows is not None else (0, h, 1)
+    c0, cs = cols if cols is not None else (0, 1)
     evals = ctypes.c_uint64(0)
-    _check(lib().oracle_render_trace(_vp(state.desc_ptr), ctypes.cast(ctypes.pointer(opts), ctypes.c_void_p),
-                                     int(accel), max(int(aa), 1), int(max_depth), int(precision), int(threads), r0,
-                                     r1, rs, _arr(rgb), _arr(rgb8), ctypes.byref(evals)))
+    _check(lib().oracle_render_trace_strided(_vp(state.desc_ptr), ctypes.cast(ctypes.pointer(opts), ctypes.c_void_p),
+                                             int(accel), max(int(aa), 1), int(max_depth), int(precision),
+                                             int(threads), r0, r1, rs, c0, cs,
+                                             -1 if jitter_seed is None else int(jitter_seed), _arr(rgb), _arr(rgb8),
+                                             ctypes.byref(evals)))
     return rgb, rgb8, int(evals.value)
 
 
@@ -174,10 +196,13 @@ def _views_c(views):
     return arr
 
 
-def render_views(state, views, options, tau: float = 0.05, precision: int = 64, threads: int = 0):
+def render_views(state, views, options, tau: float = 0.05, precision: int = 64, threads: int = 0,
+                 stride: int = 1, offset: int = 0):
     """Multi-view depth / mask / soft silhouette (the definitions of
     ft_render_views).  ``views``: (origin, target, fov) triples or ViewC.
-    Returns (t, mask, sil), each (n_views, H, W)."""
+    Returns (t, mask, sil), each (n_views, H, W).  With ``stride`` > 1 only
+    the pixels (offset + i * stride, offset + j * stride) are rendered (the
+    others stay zero)."""
     from forgedthoughts_gb300 import _native
 
     varr = _views_c(views)
@@ -188,9 +213,10 @@ def render_views(state, views, options, tau: float = 0.05, precision: int = 64, 
     sil = np.zeros((n, h, w), np.float64)
     opts = options.to_c() if hasattr(options, "to_c") else options
     assert isinstance(opts, _native.RenderOptionsC)
-    _check(lib().oracle_render_views(_vp(state.desc_ptr), ctypes.cast(varr, ctypes.c_void_p), n,
-                                     ctypes.cast(ctypes.pointer(opts), ctypes.c_void_p), float(tau), int(precision),
-                                     int(threads), _arr(t), _arr(mask), _arr(sil)))
+    _check(lib().oracle_render_views_strided(_vp(state.desc_ptr), ctypes.cast(varr, ctypes.c_void_p), n,
+                                             ctypes.cast(ctypes.pointer(opts), ctypes.c_void_p), float(tau),
+                                             int(precision), int(threads), int(stride), int(offset), _arr(t),
+                                             _arr(mask), _arr(sil)))
     return t, mask, sil
 
 

@@ -919,6 +919,44 @@ std::vector<std::pair<float, float>> sample_offsets(uint32_t samples) {
   return out;
 }
 
+// XorShift64 (R:4735-4761) and seed_pixel_sample (R:4763-4774): the jittered
+// sub-pixel offsets of the progressive renderer (R:4008-4013).
+struct XorShift64 {
+  uint64_t state;
+  explicit XorShift64(uint64_t seed) : state(seed == 0 ? 0x9E3779B97F4A7C15ull : seed) {}
+  uint64_t next_u64() {
+    uint64_t x = state;
+    x ^= x << 13;
+    x ^= x >> 7;
+    x ^= x << 17;
+    state = x;
+    return x;
+  }
+  float next_f32() { return static_cast<float>(static_cast<uint32_t>(next_u64() >> 40)) / static_cast<float>(1u << 24); }
+};
+
+uint64_t seed_pixel_sample(uint32_t x, uint32_t y, uint32_t width, uint32_t sample) {
+  uint64_t base = (static_cast<uint64_t>(y) * width + x) * 0x9E3779B97F4A7C15ull + 0xBF58476D1CE4E5B9ull;
+  return base ^ (static_cast<uint64_t>(sample) * 0x94D049BB133111EBull) ^ 0xD6E8FEB86659FD93ull;
+}
+
+// NDC (before the aspect scale) of sample s of pixel (x, y): the AA grid, or
+// with jitter_seed >= 0 the jittered offsets seeded with
+// seed_pixel_sample ^ jitter_seed.
+inline void sample_ndc(uint32_t x, uint32_t y, uint32_t s, uint32_t width, uint32_t height,
+                       const std::vector<std::pair<float, float>>& offs, int64_t jitter_seed, float* px, float* py) {
+  if (jitter_seed >= 0) {
+    XorShift64 rng(seed_pixel_sample(x, y, width, s) ^ static_cast<uint64_t>(jitter_seed));
+    const float jx = rng.next_f32() - 0.5f;
+    const float jy = rng.next_f32() - 0.5f;
+    *px = ((static_cast<float>(x) + 0.5f + jx) / static_cast<float>(width)) * 2.0f - 1.0f;
+    *py = 1.0f - ((static_cast<float>(y) + 0.5f + jy) / static_cast<float>(height)) * 2.0f;
+    return;
+  }
+  *px = ((static_cast<float>(x) + offs[s].first) / static_cast<float>(width)) * 2.0f - 1.0f;
+  *py = 1.0f - ((static_cast<float>(y) + offs[s].second) / static_cast<float>(height)) * 2.0f;
+}
+
 // depth_preview_value + spectrum_to_rgb8 (R:5215-5227)
 uint8_t depth_to_u8(float v) {
   float mapped = std::min(std::pow(std::fmax(v, 0.0f), 1.0f / 2.2f), 1.0f);
@@ -945,7 +983,7 @@ template <class R>
 int render_depth(const ft_scene_desc* desc, const ft_render_options* options, int accel, uint32_t aa, int threads,
                  uint32_t row_begin, uint32_t row_end, uint32_t row_step, float* t_out, uint8_t* mask_out,
                  uint32_t* mat_out, float* normal_out, uint8_t* rgb_out, uint64_t* evals_out,
-                 uint32_t col_begin = 0, uint32_t col_step = 1) {
+                 uint32_t col_begin = 0, uint32_t col_step = 1, int64_t jitter_seed = -1) {
   Opts op = resolve(options);
   Scene<R> scene(*desc);
   Accel<R> acc(scene, accel);
@@ -974,8 +1012,8 @@ int render_depth(const ft_scene_desc* desc, const ft_render_options* options, in
         const uint32_t x = cols[ci];
         float sum = 0.0f;
         for (uint32_t s = 0; s < aa; ++s) {
-          float px = ((static_cast<float>(x) + offs[s].first) / static_cast<float>(op.width)) * 2.0f - 1.0f;
-          float py = 1.0f - ((static_cast<float>(y) + offs[s].second) / static_cast<float>(op.height)) * 2.0f;
+          float px, py;
+          sample_ndc(x, y, s, op.width, op.height, offs, jitter_seed, &px, &py);
           V<R> d = cam.dir(R(px * aspect), R(py));
           Hit<R> h;
           bool hit = raymarch(acc, cam.origin, d, op, R(0), R(op.max_dist), &h, &evals);
@@ -1791,7 +1829,7 @@ template <class R>
 int render_trace(const ft_scene_desc* desc, const ft_render_options* options, int accel, uint32_t aa,
                  uint32_t max_depth, int threads, uint32_t row_begin, uint32_t row_end, uint32_t row_step,
                  float* rgb_out, uint8_t* rgb8_out, uint64_t* evals_out, uint32_t col_begin = 0,
-                 uint32_t col_step = 1) {
+                 uint32_t col_step = 1, int64_t jitter_seed = -1) {
   Opts op = resolve(options);
   Scene<R> scene(*desc);
   Accel<R> acc(scene, accel);
@@ -1820,8 +1858,8 @@ int render_trace(const ft_scene_desc* desc, const ft_render_options* options, in
         const uint32_t x = cols[ci];
         Sp<float> sum = sp(0.0f, 0.0f, 0.0f);
         for (uint32_t s = 0; s < aa; ++s) {
-          float px = ((static_cast<float>(x) + offs[s].first) / static_cast<float>(op.width)) * 2.0f - 1.0f;
-          float py = 1.0f - ((static_cast<float>(y) + offs[s].second) / static_cast<float>(op.height)) * 2.0f;
+          float px, py;
+          sample_ndc(x, y, s, op.width, op.height, offs, jitter_seed, &px, &py);
           V<R> d = cam.dir(R(px * aspect), R(py));
           Sp<R> c = tracer.trace(cam.origin, d, Medium<R>::air(), 0, &evals);
           sum = sum + sp(float(c.r), float(c.g), float(c.b));
@@ -2114,14 +2152,18 @@ ViewRay<R> view_ray(const Accel<R>& acc, V<R> o, V<R> d, const Opts& op, R tau) 
 template <class R>
 int render_views(const ft_scene_desc* desc, const ft_view* views, uint32_t n_views, const ft_render_options* options,
                  R tau, int threads, double* t_out, uint8_t* mask_out, double* sil_out, const ft_param* params,
-                 uint32_t n_params, const float* dl_dt, const float* dl_dsil, double* grad_out) {
+                 uint32_t n_params, const float* dl_dt, const float* dl_dsil, double* grad_out,
+                 uint32_t stride = 1, uint32_t offset = 0) {
   Opts op = resolve(options);
+  stride = std::max(stride, 1u);
+  offset %= stride;
+  const uint32_t rows_per_view = (op.height - std::min(offset, op.height) + stride - 1) / stride;
   Scene<R> scene(*desc);
   Accel<R> acc(scene, FT_ACCEL_BVH);
   ParamSlots slots(*desc, params, n_params);
   if (threads <= 0) threads = static_cast<int>(std::max(1u, std::thread::hardware_concurrency()));
   const uint64_t per_view = static_cast<uint64_t>(op.width) * op.height;
-  const uint64_t rows = static_cast<uint64_t>(n_views) * op.height;
+  const uint64_t rows = static_cast<uint64_t>(n_views) * rows_per_view;
   std::atomic<uint64_t> next{0};
   std::atomic<bool> bad{false};
   std::vector<std::vector<R>> partial(threads, std::vector<R>(n_params, R(0)));
@@ -2130,9 +2172,10 @@ int render_views(const ft_scene_desc* desc, const ft_view* views, uint32_t n_vie
     for (;;) {
       uint64_t row = next.fetch_add(1);
       if (row >= rows) break;
-      uint32_t v = static_cast<uint32_t>(row / op.height), y = static_cast<uint32_t>(row % op.height);
+      uint32_t v = static_cast<uint32_t>(row / rows_per_view);
+      uint32_t y = offset + static_cast<uint32_t>(row % rows_per_view) * stride;
       ViewCamera<R> cam(views[v]);
-      for (uint32_t x = 0; x < op.width; ++x) {
+      for (uint32_t x = offset; x < op.width; x += stride) {
         size_t i = v * per_view + static_cast<size_t>(y) * op.width + x;
         V<R> d = cam.dir(x, y, op);
         ViewRay<R> r = view_ray(acc, cam.origin, d, op, tau);
@@ -2292,6 +2335,47 @@ extern "C" int oracle_render_trace(const ft_scene_desc* desc, const ft_render_op
                              rgb_out, rgb8_out, evals_out);
 }
 
+// The depth preview / Whitted trace over every row_step-th row and
+// col_step-th column (a band of a full frame for the parity tests); outputs
+// are full-frame arrays of which only the sampled pixels are written.
+// jitter_seed >= 0 takes the jittered AA offsets instead of the grid.
+extern "C" int oracle_render_depth_strided(const ft_scene_desc* desc, const ft_render_options* options, int accel,
+                                           uint32_t aa_samples, int precision, int threads, uint32_t row_begin,
+                                           uint32_t row_end, uint32_t row_step, uint32_t col_begin,
+                                           uint32_t col_step, int64_t jitter_seed, float* t_out,
+                                           uint8_t* mask_out, uint32_t* material_out, float* normal_out,
+                                           uint8_t* rgb8_out, uint64_t* evals_out) {
+  if (int e = check_desc(desc)) return e;
+  if (!options || options->width == 0 || options->height == 0) {
+    g_error = "invalid render options";
+    return FT_ERR_INVALID_ARGUMENT;
+  }
+  if (precision == 64)
+    return render_depth<double>(desc, options, accel, aa_samples, threads, row_begin, row_end, row_step, t_out,
+                                mask_out, material_out, normal_out, rgb8_out, evals_out, col_begin, col_step,
+                                jitter_seed);
+  return render_depth<float>(desc, options, accel, aa_samples, threads, row_begin, row_end, row_step, t_out,
+                             mask_out, material_out, normal_out, rgb8_out, evals_out, col_begin, col_step,
+                             jitter_seed);
+}
+
+extern "C" int oracle_render_trace_strided(const ft_scene_desc* desc, const ft_render_options* options, int accel,
+                                           uint32_t aa_samples, uint32_t max_depth, int precision, int threads,
+                                           uint32_t row_begin, uint32_t row_end, uint32_t row_step,
+                                           uint32_t col_begin, uint32_t col_step, int64_t jitter_seed,
+                                           float* rgb_out, uint8_t* rgb8_out, uint64_t* evals_out) {
+  if (int e = check_desc(desc)) return e;
+  if (!options || options->width == 0 || options->height == 0) {
+    g_error = "invalid render options";
+    return FT_ERR_INVALID_ARGUMENT;
+  }
+  if (precision == 64)
+    return render_trace<double>(desc, options, accel, aa_samples, max_depth, threads, row_begin, row_end, row_step,
+                                rgb_out, rgb8_out, evals_out, col_begin, col_step, jitter_seed);
+  return render_trace<float>(desc, options, accel, aa_samples, max_depth, threads, row_begin, row_end, row_step,
+                             rgb_out, rgb8_out, evals_out, col_begin, col_step, jitter_seed);
+}
+
 // Strided pixel sample (rows row_begin, +row_step ..; columns col_begin,
 // +col_step ..) of the depth march or the Whitted trace: the timed CPU
 // baseline's sample of a full frame.  mode 0: depth, else trace of max_depth.
@@ -2329,6 +2413,24 @@ extern "C" int oracle_render_views(const ft_scene_desc* desc, const ft_view* vie
                                 nullptr, 0, nullptr, nullptr, nullptr);
   return render_views<float>(desc, views, n_views, options, tau, threads, t_out, mask_out, sil_out, nullptr, 0,
                              nullptr, nullptr, nullptr);
+}
+
+// render_views over the pixels (offset + i * stride, offset + j * stride) of
+// every view: a sparse sample for finite differences at full resolution.
+extern "C" int oracle_render_views_strided(const ft_scene_desc* desc, const ft_view* views, uint32_t n_views,
+                                           const ft_render_options* options, float tau, int precision, int threads,
+                                           uint32_t stride, uint32_t offset, double* t_out, uint8_t* mask_out,
+                                           double* sil_out) {
+  if (int e = check_desc(desc)) return e;
+  if (!options || options->width == 0 || options->height == 0 || !views || !(tau > 0.0f)) {
+    g_error = "invalid view render arguments";
+    return FT_ERR_INVALID_ARGUMENT;
+  }
+  if (precision == 64)
+    return render_views<double>(desc, views, n_views, options, double(tau), threads, t_out, mask_out, sil_out,
+                                nullptr, 0, nullptr, nullptr, nullptr, stride, offset);
+  return render_views<float>(desc, views, n_views, options, tau, threads, t_out, mask_out, sil_out, nullptr, 0,
+                             nullptr, nullptr, nullptr, stride, offset);
 }
 
 extern "C" int oracle_render_backward(const ft_scene_desc* desc, const ft_view* views, uint32_t n_views,

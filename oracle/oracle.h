@@ -41,6 +41,22 @@ int oracle_render_trace(const ft_scene_desc* desc, const ft_render_options* opti
                         int threads, uint32_t row_begin, uint32_t row_end, uint32_t row_step,
                         float* rgb_out, uint8_t* rgb8_out, uint64_t* evals_out);
 
+/* oracle_render_depth / oracle_render_trace over every row_step-th row and
+ * col_step-th column from (col_begin, row_begin); outputs are full-frame
+ * arrays of which only the sampled pixels are written.  jitter_seed >= 0
+ * takes the jittered AA offsets (XorShift64, seed_pixel_sample ^ seed,
+ * R:4735-4774) instead of the sqrt(aa) grid. */
+int oracle_render_depth_strided(const ft_scene_desc* desc, const ft_render_options* options, int accel,
+                                uint32_t aa_samples, int precision, int threads, uint32_t row_begin,
+                                uint32_t row_end, uint32_t row_step, uint32_t col_begin, uint32_t col_step,
+                                int64_t jitter_seed, float* t_out, uint8_t* mask_out, uint32_t* material_out,
+                                float* normal_out, uint8_t* rgb8_out, uint64_t* evals_out);
+int oracle_render_trace_strided(const ft_scene_desc* desc, const ft_render_options* options, int accel,
+                                uint32_t aa_samples, uint32_t max_depth, int precision, int threads,
+                                uint32_t row_begin, uint32_t row_end, uint32_t row_step, uint32_t col_begin,
+                                uint32_t col_step, int64_t jitter_seed, float* rgb_out, uint8_t* rgb8_out,
+                                uint64_t* evals_out);
+
 /* Strided pixel sample of a full frame (every row_step-th row from
  * row_begin, every col_step-th column from col_begin) in f32, outputs
  * discarded: mode 0 the depth march, else the Whitted trace of max_depth.
@@ -69,6 +85,13 @@ int oracle_eval_program(const ft_scene_desc* desc, int program, int precision,
 int oracle_render_views(const ft_scene_desc* desc, const ft_view* views, uint32_t n_views,
                         const ft_render_options* options, float tau, int precision, int threads,
                         double* t_out, uint8_t* mask_out, double* sil_out);
+
+/* oracle_render_views over the pixels (offset + i * stride, offset + j * stride)
+ * of every view; only those pixels of the full outputs are written. */
+int oracle_render_views_strided(const ft_scene_desc* desc, const ft_view* views, uint32_t n_views,
+                                const ft_render_options* options, float tau, int precision, int threads,
+                                uint32_t stride, uint32_t offset, double* t_out, uint8_t* mask_out,
+                                double* sil_out);
 
 /* The adjoint of oracle_render_views (the definitions of ft_render_backward):
  * grad_out[k] = sum over rays of dl_dt dt/dparam_k + dl_dsil dsil/dparam_k. */
