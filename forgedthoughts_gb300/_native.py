@@ -38,6 +38,8 @@ FT_NODE_BOX = 1
 FT_NODE_CYLINDER = 2
 FT_NODE_TORUS = 3
 FT_NODE_EXTRUDE_POLYGON = 4
+FT_NODE_UNION = 8
+FT_NODE_UNION_ROUND = 11
 FT_NODE_CUSTOM = 30
 
 FT_FLAG_DEVICE_POINTERS = 1

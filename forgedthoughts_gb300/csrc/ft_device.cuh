@@ -24,6 +24,8 @@ FT_DEV F3 operator-(F3 a, F3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
 FT_DEV F3 operator*(F3 a, float s) { return f3(a.x * s, a.y * s, a.z * s); }
 FT_DEV float dot3(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 FT_DEV float len3(F3 a) { return sqrtf(a.x * a.x + a.y * a.y + a.z * a.z); }
+// Vec3::cross
+FT_DEV F3 cross3(F3 a, F3 b) { return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
 // Vec3::normalize (R:414-420)
 FT_DEV F3 normalize3(F3 a) {
   float l = len3(a);

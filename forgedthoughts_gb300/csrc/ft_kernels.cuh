@@ -339,9 +339,14 @@ __device__ __forceinline__ Info ur_fold_small(const DevScene& S, const DevUrTree
     cx.blend();
     link = S.ur_inner_up[lca];
   }
+  // Above the last near subtree every ancestor lifts the value the same way
+  // (either side, the other child is inert): once a lift returns its input
+  // unchanged, every further lift does too, so the walk to the root ends.
   for (int guard = 0; guard <= ftgpu::kMaxUrDepth && link >= 0; ++guard) {
-    v0 = ur_lift(v0, link & 1, r);
+    const Info lifted = ur_lift(v0, link & 1, r);
     cx.blend();
+    if (lifted.d == v0.d) break;
+    v0 = lifted;
     link = S.ur_inner_up[link >> 1];
   }
   return v0;
@@ -1296,21 +1301,42 @@ __device__ __forceinline__ void shade_hit(const DevScene& S, const RayParams& P,
     sink.emit(mul3(W, mat_emission(mat)));
     if (reflect_w > 1.0e-4f) {
       F3 rd = ftd::normalize3(J.d - normal * (2.0f * ftd::dot3(J.d, normal)));
-      F3 ro = offset_origin(h.pos, normal, rd, eps * (1.0f + rough * 6.0f));
       F3 tint = lerp_sp(spec_color, base_color, clamp01(metallic));
-      sink.push(RayJob{ro, rd, mul3(W, tint * reflect_w), J.med, J.depth + 1});
+      if (transmission > 1.0e-4f && rough > 0.06f) {
+        // trace_rough_dielectric_reflection (ray.rs:296-322): the average of
+        // the lobe around the mirror direction
+        F3 dirs[kMaxLobes];
+        const int n = rough_lobe_directions(rd, rough, rough_reflection_samples(rough), dirs);
+        const F3 w = mul3(W, tint * (reflect_w / static_cast<float>(n)));
+        for (int k = 0; k < n; ++k)
+          sink.push(RayJob{offset_origin(h.pos, normal, dirs[k], eps * (8.0f + rough * 12.0f)), dirs[k], w, J.med,
+                           J.depth + 1});
+      } else {
+        F3 ro = offset_origin(h.pos, normal, rd, eps * (1.0f + rough * 6.0f));
+        sink.push(RayJob{ro, rd, mul3(W, tint * reflect_w), J.med, J.depth + 1});
+      }
     }
     if (transmission > 1.0e-4f) {
       MediumD next = thin ? J.med : transition(mat, front, J.med);
       next.ior = ftd::rclamp(next_ior, 1.0f, 3.0f);
       F3 td;
       if (refract_dir(J.d, normal, eta_i / eta_t, &td)) {
-        F3 to = offset_origin(h.pos, normal, td, eps * (8.0f + rough * 12.0f));
         float tt = clamp01(transmission);
         F3 tint = f3(1.0f - (1.0f - clamp01(base_color.x)) * tt, 1.0f - (1.0f - clamp01(base_color.y)) * tt,
                      1.0f - (1.0f - clamp01(base_color.z)) * tt);
-        sink.push(RayJob{to, ftd::normalize3(td), mul3(W, tint * (transmission * (1.0f - fresnel))), next,
-                         J.depth + 1});
+        const F3 wt = mul3(W, tint * (transmission * (1.0f - fresnel)));
+        if (rough > 0.06f) {
+          // trace_rough_dielectric_refraction (ray.rs:324-352)
+          F3 dirs[kMaxLobes];
+          const int n = rough_lobe_directions(ftd::normalize3(td), rough, rough_refraction_samples(rough), dirs);
+          const F3 w = wt * (1.0f / static_cast<float>(n));
+          for (int k = 0; k < n; ++k)
+            sink.push(RayJob{offset_origin(h.pos, normal, dirs[k], eps * (8.0f + rough * 12.0f)), dirs[k], w, next,
+                             J.depth + 1});
+        } else {
+          F3 to = offset_origin(h.pos, normal, td, eps * (8.0f + rough * 12.0f));
+          sink.push(RayJob{to, ftd::normalize3(td), wt, next, J.depth + 1});
+        }
       }
     }
   }

@@ -510,6 +510,7 @@ struct ft_batch {
   unsigned long long* wf_counters = nullptr;
   uint32_t wf_levels = 0;
   uint32_t wf_light_samples = 1;
+  uint64_t wf_max_push = 4;  // most rays a hit of any trace item pushes
   int sms = 1;
 };
 
@@ -537,13 +538,26 @@ ft_status grow(T** buf, uint64_t* cap, uint64_t want, const char* what) {
   return FT_OK;
 }
 
+// Most secondary rays one hit can push: two materials (a smooth boolean's
+// split) x (reflection + refraction), or x (3 + 4) lobe rays when a
+// transmissive material may be rough (roughness above 0.06, or set per hit by
+// a hook; blends mix the roughness of any two materials).
+uint64_t max_rays_per_hit(const ftgpu::SceneImage& im) {
+  bool transmissive = false, rough = false;
+  for (const ft_material& m : im.materials) {
+    transmissive |= m.kind == FT_MAT_DIELECTRIC || (m.kind == FT_MAT_STANDARD && m.transmission > 1.0e-4f);
+    rough |= m.roughness > 0.06f || m.roughness_program >= 0;
+  }
+  return transmissive && rough ? 2 * (3 + 4) : 2 * 2;
+}
+
 // Queue capacity of bounce level k of a batch wavefront over n work items: a
-// job pushes at most four (two materials x reflect / refract), so n * 4^k is
-// exact; it is capped at 16 n (Whitted queues shrink fast: diffuse hits push
+// job pushes at most `push` rays (max_rays_per_hit), so n * push^k is exact;
+// it is capped at 16 n (Whitted queues shrink fast: diffuse hits push
 // nothing) and an overflow is reported when the results are read.
-uint64_t level_capacity(uint64_t n, uint32_t k) {
+uint64_t level_capacity(uint64_t n, uint32_t k, uint64_t push) {
   uint64_t f = 1;
-  for (uint32_t i = 0; i < k && f < 16; ++i) f *= 4;
+  for (uint32_t i = 0; i < k && f < 16; ++i) f *= push;
   return n * std::min<uint64_t>(f, 16);
 }
 
@@ -574,7 +588,7 @@ ft_status batch_apply_tuning(ft_batch* b) {
     const uint64_t n = b->part[1].n_rays;
     uint64_t want[2] = {0, 0}, hits = 0;
     for (uint32_t k = 0; k < b->wf_levels; ++k) {
-      uint64_t c = level_capacity(n, k);
+      uint64_t c = level_capacity(n, k, b->wf_max_push);
       want[k & 1] = std::max(want[k & 1], c);
       hits = std::max(hits, c);
     }
@@ -686,11 +700,12 @@ ft_status check_tuning(const ft_batch_tuning& t) {
 // shade and one shadow kernel over queues (ft_wavefront.cuh).  Radiance per
 // sample lands in sc->d_normal.  Queue sizes are read back once per level to
 // size the next one; the capacities are exact upper bounds (a job pushes at
-// most two materials x two rays, and two materials x the light samples).
+// most max_rays_per_hit rays, and two materials x the light samples).
 ft_status trace_wavefront(ft_scene* sc, const RayParams& P, uint32_t max_depth, cudaStream_t st,
                           uint32_t* launches, unsigned long long* const* kind_stats = nullptr) {
   const ftgpu::SceneImage& im = sc->img;
   uint64_t light_samples = 0;
+  const uint64_t max_push = max_rays_per_hit(im);
   for (const ft_light& L : im.lights) light_samples += L.kind == FT_LIGHT_SPHERE ? std::max(L.samples, 1u) : 1u;
   uint64_t n = P.n_items;  // work items, tile padding included
   if (!sc->wf_counters)
@@ -735,7 +750,7 @@ ft_status trace_wavefront(ft_scene* sc, const RayParams& P, uint32_t max_depth, 
   for (uint32_t level = 0; level < max_depth && n > 0; ++level) {
     const int nxt = 1 - cur;
     if (ft_status s = grow(&sc->wf_hits, &sc->wf_hits_cap, n, "cudaMalloc(hits)")) return s;
-    if (ft_status s = grow(&sc->wf_jobs[nxt], &sc->wf_jobs_cap[nxt], 4 * n, "cudaMalloc(ray jobs)")) return s;
+    if (ft_status s = grow(&sc->wf_jobs[nxt], &sc->wf_jobs_cap[nxt], max_push * n, "cudaMalloc(ray jobs)")) return s;
     if (ft_status s = grow(&sc->wf_shadows, &sc->wf_shadows_cap, std::max<uint64_t>(2 * n * light_samples, 1),
                            "cudaMalloc(shadow jobs)"))
       return s;
@@ -1484,6 +1499,7 @@ ft_status ft_batch_create(const ft_batch_item* items, uint32_t n, uint32_t flags
         for (const ft_light& L : b->items[it].scene->img.lights)
           ls += L.kind == FT_LIGHT_SPHERE ? std::max(L.samples, 1u) : 1u;
         b->wf_light_samples = std::max(b->wf_light_samples, ls);
+        b->wf_max_push = std::max(b->wf_max_push, max_rays_per_hit(b->items[it].scene->img));
       }
     }
     part.blocks = std::max(1, sms * std::max(per_sm, 1));

@@ -784,6 +784,28 @@ __device__ bool refract_dir(F3 inc, F3 nrm, float eta, F3* out) {
   return true;
 }
 
+// rough_lobe_directions (ray.rs:376-411): the ideal direction, then up to six
+// directions offset by the roughness spread along a tangent frame.
+constexpr int kMaxLobes = 4;  // rough_dielectric_refraction_samples' largest count
+__device__ int rough_lobe_directions(F3 ideal_dir, float roughness, int count, F3* dirs) {
+  const F3 ideal = ftd::normalize3(ideal_dir);
+  const F3 seed = fabsf(ideal.y) < 0.99f ? f3(0.0f, 1.0f, 0.0f) : f3(1.0f, 0.0f, 0.0f);
+  const F3 tangent = ftd::normalize3(ftd::cross3(ideal, seed));
+  const F3 bitangent = ftd::normalize3(ftd::cross3(tangent, ideal));
+  const float spread = ftd::rclamp(roughness, 0.0f, 0.5f) * 0.35f;
+  dirs[0] = ideal;
+  if (count <= 1 || spread <= 1.0e-4f) return 1;
+  const float ox[kMaxLobes - 1] = {1.0f, -1.0f, 0.0f};
+  const float oy[kMaxLobes - 1] = {0.0f, 0.0f, 1.0f};
+  const int n = count < kMaxLobes ? count : kMaxLobes;
+  for (int k = 1; k < n; ++k)
+    dirs[k] = ftd::normalize3((ideal + tangent * (ox[k - 1] * spread)) + bitangent * (oy[k - 1] * spread));
+  return n;
+}
+// rough_dielectric_reflection_samples / _refraction_samples (ray.rs:413-435)
+__device__ __forceinline__ int rough_reflection_samples(float r) { return r < 0.12f ? 1 : (r < 0.28f ? 2 : 3); }
+__device__ __forceinline__ int rough_refraction_samples(float r) { return r < 0.1f ? 2 : (r < 0.24f ? 3 : 4); }
+
 struct MediumD {
   float ior;
   F3 absorption;

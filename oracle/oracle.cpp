@@ -1333,6 +1333,39 @@ class Tracer {
   Tracer(const Scene<R>& s, const Accel<R>& a, const Opts& op, uint32_t max_depth)
       : S(s), A(a), op_(op), max_depth_(std::max(max_depth, 1u)) {}
 
+  // rough_lobe_directions (ray.rs:376-411)
+  static int lobe_directions(V<R> ideal_dir, R roughness, int count, V<R>* dirs) {
+    V<R> ideal = normalize(ideal_dir);
+    V<R> seed = std::fabs(ideal.y) < R(0.99) ? mk(R(0), R(1), R(0)) : mk(R(1), R(0), R(0));
+    V<R> tangent = normalize(cross(ideal, seed));
+    V<R> bitangent = normalize(cross(tangent, ideal));
+    R spread = rclamp(roughness, R(0), R(0.5)) * R(0.35);
+    dirs[0] = ideal;
+    if (count <= 1 || spread <= R(1.0e-4)) return 1;
+    const R ox[6] = {R(1), R(-1), R(0), R(0), R(0.707), R(-0.707)};
+    const R oy[6] = {R(0), R(0), R(1), R(-1), R(0.707), R(0.707)};
+    int n = 1;
+    for (int k = 0; k < 6 && k < count - 1; ++k)
+      dirs[n++] = normalize((ideal + tangent * (ox[k] * spread)) + bitangent * (oy[k] * spread));
+    return n;
+  }
+  // rough_dielectric_reflection_samples / _refraction_samples (ray.rs:413-435)
+  static int rough_reflection_samples(R r) { return r < R(0.12) ? 1 : (r < R(0.28) ? 2 : 3); }
+  static int rough_refraction_samples(R r) { return r < R(0.1) ? 2 : (r < R(0.24) ? 3 : 4); }
+  // trace_lobe_average (ray.rs:354-374)
+  Sp<R> lobe_average(V<R> hit_point, V<R> gn, V<R> ideal, Medium<R> med, uint32_t depth, R rough, int count,
+                     uint64_t* evals) const {
+    V<R> dirs[7];
+    int n = lobe_directions(ideal, rough, count, dirs);
+    R inv = R(1) / R(n);
+    Sp<R> sum = black<R>();
+    for (int k = 0; k < n; ++k) {
+      V<R> o = offset_origin(hit_point, gn, dirs[k], R(op_.epsilon) * (R(8) + rough * R(12)));
+      sum = sum + scale(trace(o, dirs[k], med, depth + 1, evals), inv);
+    }
+    return sum;
+  }
+
   // trace_ray_recursive (ray.rs:3-39)
   Sp<R> trace(V<R> o, V<R> d, Medium<R> med, uint32_t depth, uint64_t* evals) const {
     if (depth >= max_depth_) return black<R>();
@@ -1771,10 +1804,15 @@ class Tracer {
     color = color + emission(mat);
     R eps = R(op_.epsilon);
     if (reflect_w > R(1.0e-4)) {
-      // trace_rough_dielectric_reflection is not restated (roughness <= 0.06 here)
       V<R> rd = normalize(dir - normal * (R(2) * dot(dir, normal)));
-      V<R> ro = offset_origin(h.pos, gn, rd, eps * (R(1) + rough * R(6)));
-      Sp<R> refl = trace(ro, rd, med, depth + 1, evals);
+      Sp<R> refl;
+      if (transmission > R(1.0e-4) && rough > R(0.06)) {
+        // trace_rough_dielectric_reflection (ray.rs:296-322)
+        refl = lobe_average(h.pos, gn, rd, med, depth, rough, rough_reflection_samples(rough), evals);
+      } else {
+        V<R> ro = offset_origin(h.pos, gn, rd, eps * (R(1) + rough * R(6)));
+        refl = trace(ro, rd, med, depth + 1, evals);
+      }
       Sp<R> tint = lerp_sp(spec_color, base_color, rclamp(metallic, R(0), R(1)));
       color = color + scale(refl * tint, reflect_w);
     }
@@ -1785,8 +1823,13 @@ class Tracer {
       Sp<R> refr = black<R>();
       V<R> td;
       if (refract_dir(dir, normal, eta_i / eta_t, &td)) {
-        V<R> to = offset_origin(h.pos, gn, td, eps * (R(8) + rough * R(12)));
-        refr = trace(to, normalize(td), next, depth + 1, evals);
+        if (rough > R(0.06)) {
+          // trace_rough_dielectric_refraction (ray.rs:324-352)
+          refr = lobe_average(h.pos, gn, normalize(td), next, depth, rough, rough_refraction_samples(rough), evals);
+        } else {
+          V<R> to = offset_origin(h.pos, gn, td, eps * (R(8) + rough * R(12)));
+          refr = trace(to, normalize(td), next, depth + 1, evals);
+        }
       }
       if (!(refr.r == R(0) && refr.g == R(0) && refr.b == R(0))) {
         R tt = rclamp(transmission, R(0), R(1));

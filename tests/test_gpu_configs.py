@@ -27,6 +27,7 @@ pytestmark = pytest.mark.gpu
 
 ROWS = (22, 1080, 45)  # 24 rows of the 1080
 COLS = (8, 16)         # 120 columns of the 1920
+COLS6 = (8, 32)        # 60 columns: the depth-6 tree costs the oracle about 3x a depth-2 one
 
 
 def _band(a, rows=ROWS, cols=COLS):
@@ -69,9 +70,9 @@ def test_c2_trace_full_frame_depth6(field):
     """The headline configuration itself: 1920x1080, 2x2 AA, depth 6."""
     w, st = field
     lin, _ = ft.render_trace(st, w.options, w.accel, w.aa, 6)
-    ref32, _, _ = oracle.render_trace(st, w.options, int(w.accel), w.aa, 6, 32, rows=ROWS, cols=COLS)
-    ref64, _, _ = oracle.render_trace(st, w.options, int(w.accel), w.aa, 6, 64, rows=ROWS, cols=COLS)
-    e, gap = _chaotic_bar(_band(lin), _band(ref32), _band(ref64))
+    ref32, _, _ = oracle.render_trace(st, w.options, int(w.accel), w.aa, 6, 32, rows=ROWS, cols=COLS6)
+    ref64, _, _ = oracle.render_trace(st, w.options, int(w.accel), w.aa, 6, 64, rows=ROWS, cols=COLS6)
+    e, gap = _chaotic_bar(_band(lin, cols=COLS6), _band(ref32, cols=COLS6), _band(ref64, cols=COLS6))
     print(f"C2 depth 6: RMSE vs f32 oracle {e:.2e}, oracle f32 vs f64 {gap:.2e}")
 
 
@@ -89,9 +90,9 @@ def test_c2_jittered_seed1(field):
     ref, _, _ = oracle.render_trace(st, w.options, int(w.accel), w.aa, 2, 32, rows=ROWS, cols=COLS, jitter_seed=1)
     assert radiance_rmse(_band(lin), _band(ref)) <= 1e-3
     lin6, _ = ft.render_trace(st, w.options, w.accel, w.aa, 6, jitter_seed=1)
-    ref32, _, _ = oracle.render_trace(st, w.options, int(w.accel), w.aa, 6, 32, rows=ROWS, cols=COLS, jitter_seed=1)
-    ref64, _, _ = oracle.render_trace(st, w.options, int(w.accel), w.aa, 6, 64, rows=ROWS, cols=COLS, jitter_seed=1)
-    _chaotic_bar(_band(lin6), _band(ref32), _band(ref64))
+    ref32, _, _ = oracle.render_trace(st, w.options, int(w.accel), w.aa, 6, 32, rows=ROWS, cols=COLS6, jitter_seed=1)
+    ref64, _, _ = oracle.render_trace(st, w.options, int(w.accel), w.aa, 6, 64, rows=ROWS, cols=COLS6, jitter_seed=1)
+    _chaotic_bar(_band(lin6, cols=COLS6), _band(ref32, cols=COLS6), _band(ref64, cols=COLS6))
 
 
 def test_c3_hooked_shells_full_frame_depth():
@@ -129,12 +130,20 @@ def test_c3_shaded_full_frame():
     assert radiance_rmse(_band(lin2, rows, cols), _band(ref, rows, cols)) <= 1e-3
 
 
+def _spheres(w):
+    return int(w.name.split("_spheres")[1].split("_")[0])
+
+
 def test_c4_batch_items_against_oracle():
     """Eight items of the 256-scene batch (four depth previews, four Whitted
-    depth 2), rendered in one batch launch: each against the oracle."""
+    depth 2), rendered in one batch launch: each against the oracle.  The
+    Whitted items are the batch's smallest hard unions: the oracle restates
+    the reference's normal and material walks, which visit both children of
+    every union, so a shaded hit on an n-sphere union costs it O(n^2)."""
     ws = workloads.batch_scenes()
     depth = [w for w in ws if w.max_depth == 0 and w.options.width <= 256][:4]
-    trace = [w for w in ws if w.max_depth > 0 and w.options.width <= 128][:4]
+    trace = sorted((w for w in ws if w.max_depth > 0 and w.options.width <= 256), key=_spheres)[:4]
+    assert max(_spheres(w) for w in trace) <= 64
     picked = depth + trace
     states = [ft.parse_and_eval(w.source) for w in picked]
     b = ft.Batch([(st, w.options, w.aa, w.max_depth) for st, w in zip(states, picked)])

@@ -44,3 +44,33 @@ def test_gpu_trace_explicit_media(join):
     clear = ft.parse_and_eval(src.replace("density: 1.5", "density: 0.0").replace("density: 0.8", "density: 0.0"))
     lin_clear, _ = ft.render_trace(clear, opts, ft.AccelMode.Bvh, 1, 4)
     assert radiance_rmse(lin, lin_clear) > 5e-3
+
+
+ROUGH_SCENE = """
+environment Sky { fn color(dir) { return mix(vec3(0.95, 0.9, 0.8), vec3(0.3, 0.5, 1.0), clamp(dir.y, 0.0, 1.0)); } };
+let camera = Camera { origin: vec3(0.0, 1.0, -4.0), target: vec3(0.0, 0.5, 0.0), fov_y: 45.0 };
+let light = PointLight { position: vec3(3.0, 6.0, -3.0), intensity: 60.0 };
+let ground = Box { size: vec3(20.0, 1.0, 20.0), pos: vec3(0.0, -0.5, 0.0), material: Lambert { color: vec3(0.7, 0.3, 0.2) } };
+let a = Sphere { radius: 0.5, pos: vec3(-1.1, 0.55, 0.0), material: Dielectric { ior: 1.5, roughness: 0.09 } };
+let b = Sphere { radius: 0.5, pos: vec3(0.0, 0.55, 0.2), material: Dielectric { ior: 1.45, roughness: 0.2 } };
+let c = Sphere { radius: 0.5, pos: vec3(1.1, 0.55, 0.0), material: Dielectric { ior: 1.4, roughness: 0.35 } };
+let scene = ground + a + b + c;
+"""
+
+
+def test_gpu_trace_rough_dielectric_lobes():
+    """Dielectrics with roughness above 0.06 average a lobe of reflected and
+    refracted rays (trace_rough_dielectric_reflection / _refraction,
+    ray.rs:296-435): 1 to 3 reflection and 2 to 4 refraction rays by
+    roughness.  GPU against the f32 oracle, and the lobes visibly change the
+    image against the same spheres made smooth."""
+    opts = ft.RenderOptions(width=160, height=120, max_steps=256, max_dist=50.0, epsilon=1e-4, step_scale=0.7)
+    st = ft.parse_and_eval(ROUGH_SCENE)
+    for depth in (2, 3):
+        lin, _ = ft.render_trace(st, opts, ft.AccelMode.Bvh, 1, depth)
+        ref, _, _ = oracle.render_trace(st, opts, 1, 1, depth, 32)
+        assert radiance_rmse(lin, ref) <= 1e-3, (depth, radiance_rmse(lin, ref))
+    smooth = ft.parse_and_eval(ROUGH_SCENE.replace("roughness: 0.09", "roughness: 0.0")
+                               .replace("roughness: 0.2", "roughness: 0.0").replace("roughness: 0.35", "roughness: 0.0"))
+    lin_s, _ = ft.render_trace(smooth, opts, ft.AccelMode.Bvh, 1, 3)
+    assert radiance_rmse(lin, lin_s) > 5e-3

@@ -142,3 +142,22 @@ def test_trace_f32_tracks_f64():
     a, _, _ = oracle.render_trace(st, opts, 1, 1, 4, 32)
     b, _, _ = oracle.render_trace(st, opts, 1, 1, 4, 64)
     assert np.sqrt(np.mean((a - b) ** 2)) <= 1e-3
+
+
+def test_rough_dielectric_lobes_average_traced_rays():
+    """A roughness-0.35 glass sphere (2 reflection and 4 refraction lobe rays
+    per hit) traces more rays than the same sphere smooth, and its image is
+    a blur of the smooth one: the sky seen through it keeps its mean."""
+    src = """
+        environment Sky {{ fn color(dir) {{ return mix(vec3(1.0, 0.9, 0.8), vec3(0.2, 0.4, 1.0), clamp(dir.y, 0.0, 1.0)); }} }};
+        let scene = Sphere {{ radius: 1.0, material: Dielectric {{ ior: 1.4, roughness: {r} }} }};
+    """
+    opts = ft.RenderOptions(width=24, height=24, max_steps=200, max_dist=20.0, epsilon=1e-4, camera_z=4.0)
+    smooth = ft.parse_and_eval(src.format(r="0.0"))
+    rough = ft.parse_and_eval(src.format(r="0.35"))
+    a, _, ea = oracle.render_trace(smooth, opts, 1, 1, 3, 32)
+    b, _, eb = oracle.render_trace(rough, opts, 1, 1, 3, 32)
+    assert eb > 2 * ea
+    centre = (slice(8, 16), slice(8, 16))
+    assert np.abs(b[centre] - a[centre]).max() > 1e-3
+    assert abs(b[centre].mean() - a[centre].mean()) < 0.1 * a[centre].mean()
