@@ -332,6 +332,34 @@ def render_trace(state: SceneState, options: RenderOptions, accel: AccelMode = A
     return lin, rgb8
 
 
+@dataclasses.dataclass
+class PathtraceSettings:
+    """``PathtraceSettings`` (R:107-125)."""
+
+    spp: int = 16
+    max_bounces: int = 4
+    preview_every: int = 5
+    min_spp: int = 8
+    noise_threshold: float = 0.03
+
+
+def render_pathtrace(state: SceneState, options: RenderOptions, accel: AccelMode = AccelMode.Bvh,
+                     settings: PathtraceSettings | None = None) -> tuple:
+    """The MIS path tracer on the GPU (render_pathtrace_with_accel_progressive,
+    R:3974-4045): (linear rgb (H, W, 3) float32, rgb8 (H, W, 3) uint8,
+    samples per pixel (H, W) uint32)."""
+    ps = settings or PathtraceSettings()
+    h, w = int(options.height), int(options.width)
+    lin = np.empty((h, w, 3), np.float32)
+    rgb8 = np.empty((h, w, 3), np.uint8)
+    count = np.empty((h, w), np.uint32)
+    c = _native.PathtraceSettingsC(int(ps.spp), int(ps.max_bounces), int(ps.min_spp), float(ps.noise_threshold))
+    opts = options.to_c()
+    _check(_native.lib().ft_render_pathtrace(state.gpu().handle, ctypes.byref(opts), int(accel), ctypes.byref(c),
+                                             _ptr(lin), _ptr(rgb8), _ptr(count), 0, None))
+    return lin, rgb8, count
+
+
 def render_ray_progressive_with_accel(state: SceneState, options: RenderOptions, accel: AccelMode,
                                       settings: RaySettings, on_tile) -> np.ndarray:
     """Whitted render with the reference's per-tile progress callback (R:1201-1236)."""

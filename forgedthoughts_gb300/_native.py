@@ -133,6 +133,11 @@ KERNEL_KIND_NAMES = ["wf_primary_kernel", "wf_march_persistent", "wf_shade_kerne
                      "pixels", "march_depth_persistent"]
 
 
+class PathtraceSettingsC(ctypes.Structure):
+    _fields_ = [("spp", ctypes.c_uint32), ("max_bounces", ctypes.c_uint32), ("min_spp", ctypes.c_uint32),
+                ("noise_threshold", ctypes.c_float)]
+
+
 class KernelTimesC(ctypes.Structure):
     _fields_ = [("ms", ctypes.c_double * FT_KERNEL_KINDS), ("launches", ctypes.c_uint64 * FT_KERNEL_KINDS)]
 
@@ -208,6 +213,9 @@ SIGNATURES = {
                                                     ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(RenderStatsC),
                                                     ctypes.POINTER(RenderStatsC), ctypes.POINTER(RenderStatsC)]),
     "ft_scene_profile": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32]),
+    "ft_render_pathtrace": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(RenderOptionsC), ctypes.c_int,
+                                           ctypes.POINTER(PathtraceSettingsC), ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p]),
     "ft_scene_kernel_times": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(KernelTimesC)]),
     "ft_batch_create": (ctypes.c_int, [ctypes.POINTER(BatchItemC), ctypes.c_uint32, ctypes.c_uint32,
                                        ctypes.POINTER(ctypes.c_void_p)]),

@@ -38,10 +38,10 @@ CPP_SOURCES = ["frontend_parse.cpp", "frontend_eval.cpp", "frontend_lower.cpp", 
                "scene_build.cpp", "jit_codegen.cpp"]
 CU_SOURCES = ["ft_render.cu"]
 HEADERS = ["frontend.h", "common.h", "scene_build.h", "ft_device.cuh", "ft_trace.cuh", "ft_bricks.cuh", "ft_diff.cuh",
-           "ft_kernels.cuh", "ft_layout.h", "jit.h", "ft_wavefront.cuh"]
+           "ft_kernels.cuh", "ft_layout.h", "jit.h", "ft_wavefront.cuh", "ft_path.cuh"]
 # Device headers embedded for run-time compilation (NVRTC) of scene kernels.
 JIT_HEADERS = ["ft_kernels.cuh", "ft_device.cuh", "ft_layout.h", "ft_bricks.cuh", "ft_trace.cuh", "ft_diff.cuh",
-               "ft_wavefront.cuh"]
+               "ft_wavefront.cuh", "ft_path.cuh"]
 
 # Minimal C headers for the run-time compile unit (NVRTC ships no C library).
 _JIT_SHIMS = {

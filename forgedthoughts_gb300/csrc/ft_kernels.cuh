@@ -391,31 +391,42 @@ __device__ __forceinline__ Info eval_urtree(const DevScene& S, const DevUrTree& 
   };
   int stack[48];
   int sp = 0;
-  // Inside the candidate grid one cell list replaces the BVH walk.  The list
-  // is sorted by a lower bound of the box bound of its points, so the first
-  // entry at or above the running limit ends it: every later primitive
-  // would be skipped by that test.
+  // Candidates come from one cell list of the grid or, outside the grid, from
+  // the tree's BVH.  Both feed a single `consider` site, so the primitive
+  // evaluator is inlined once.  The cell list is sorted by a lower bound of
+  // the box bound of its points, so the first entry at or above the running
+  // limit ends it: every later primitive would be skipped by that test.
   float gx = (p.x - t.gmin[0]) * t.inv_cell, gy = (p.y - t.gmin[1]) * t.inv_cell, gz = (p.z - t.gmin[2]) * t.inv_cell;
-  if (t.dims[0] > 0 && gx >= 0.0f && gy >= 0.0f && gz >= 0.0f && gx < (float)t.dims[0] && gy < (float)t.dims[1] &&
-      gz < (float)t.dims[2]) {
+  const bool in_grid = t.dims[0] > 0 && gx >= 0.0f && gy >= 0.0f && gz >= 0.0f && gx < (float)t.dims[0] &&
+                       gy < (float)t.dims[1] && gz < (float)t.dims[2];
+  uint32_t k = 0, end = 0;  // the cell list, or the primitives of the BVH leaf being walked
+  const int32_t* list = S.ur_bvh_prims;
+  if (in_grid) {
     int ix = min((int)gx, t.dims[0] - 1), iy = min((int)gy, t.dims[1] - 1), iz = min((int)gz, t.dims[2] - 1);
     int cell = t.cell_first + ix + t.dims[0] * (iy + t.dims[1] * iz);
-    uint32_t beg = S.ur_cell_offsets[cell], end = S.ur_cell_offsets[cell + 1];
-    for (uint32_t k = beg; k < end; ++k) {
-      cx.cand();
-      if (S.ur_cell_gaps[k] >= ftd::rmax(r, fminf(best.d, cutoff))) break;
-      consider(S.ur_cell_prims[k]);
-    }
+    k = S.ur_cell_offsets[cell];
+    end = S.ur_cell_offsets[cell + 1];
+    list = S.ur_cell_prims;
   } else {
     stack[sp++] = t.bvh_root;
   }
-  for (int walk = 0; sp > 0 && walk < ftgpu::kMaxWalk; ++walk) {  // a tree walk pops each node once
+  for (int walk = 0; walk < ftgpu::kMaxWalk; ++walk) {  // each list entry and BVH node is visited once
+    if (k < end) {
+      if (in_grid) {
+        cx.cand();
+        if (S.ur_cell_gaps[k] >= ftd::rmax(r, fminf(best.d, cutoff))) break;
+      }
+      consider(list[k++]);
+      continue;
+    }
+    if (in_grid || sp == 0) break;
     const DevUrBvh& bn = S.ur_bvh[stack[--sp]];
     cx.box();
     float bound = ftd::rmax(r, fminf(best.d, cutoff));
     if (node_lb(p, bn.bmin, bn.bmax) >= bound) continue;
     if (bn.prim_count > 0) {
-      for (int k = 0; k < bn.prim_count; ++k) consider(S.ur_bvh_prims[bn.prim_begin + k]);
+      k = static_cast<uint32_t>(bn.prim_begin);
+      end = k + static_cast<uint32_t>(bn.prim_count);
       continue;
     }
     const DevUrBvh& L = S.ur_bvh[bn.left];
@@ -565,20 +576,29 @@ template <bool kStats>
 __device__ __forceinline__ Info scene_distance_inl(const DevScene& S, F3 p, Ctx<kStats>& cx) {
   cx.eval();
   const DevBvhNode& root = S.bvh[S.bvh_root];
-  if (root.leaf >= 0) return eval_leaf(S, S.leaves[root.leaf], p, kInf, cx);
-  const DevBvhNode& L = S.bvh[root.lhs];
-  const DevBvhNode& R = S.bvh[root.rhs];
-  if (L.leaf < 0 || R.leaf < 0) return scene_distance_bvh(S, p, cx);
-  cx.box();
-  cx.box();
-  float ll = node_lb(p, L.bmin, L.bmax), rl = node_lb(p, R.bmin, R.bmax);
-  const bool lfirst = ll <= rl;
-  const DevLeaf& first = S.leaves[lfirst ? L.leaf : R.leaf];
-  const DevLeaf& second = S.leaves[lfirst ? R.leaf : L.leaf];
-  Info cur = eval_leaf(S, first, p, kInf, cx);
-  if ((lfirst ? rl : ll) <= cur.d) {
-    Info in = eval_leaf(S, second, p, cur.d, cx);
-    if (in.d < cur.d) cur = in;
+  int leaf = root.leaf, second = -1;
+  float second_lb = kInf;
+  if (leaf < 0) {
+    const DevBvhNode& L = S.bvh[root.lhs];
+    const DevBvhNode& R = S.bvh[root.rhs];
+    if (L.leaf < 0 || R.leaf < 0) return scene_distance_bvh(S, p, cx);
+    cx.box(2);
+    const float ll = node_lb(p, L.bmin, L.bmax), rl = node_lb(p, R.bmin, R.bmax);
+    const bool lfirst = ll <= rl;
+    leaf = lfirst ? L.leaf : R.leaf;
+    second = lfirst ? R.leaf : L.leaf;
+    second_lb = lfirst ? rl : ll;
+  }
+  // One evaluation site for both leaves: the leaf evaluator (with the whole
+  // union_round path) is inlined once, which keeps the march loops' code
+  // within the instruction cache.
+  Info cur{kInf, 0u, 0u};
+#pragma unroll 1
+  for (int k = 0; k < 2; ++k) {
+    const Info in = eval_leaf(S, S.leaves[leaf], p, k == 0 ? kInf : cur.d, cx);
+    if (k == 0 || in.d < cur.d) cur = in;
+    if (second < 0 || !(second_lb <= cur.d)) break;
+    leaf = second;
   }
   return cur;
 }
@@ -823,10 +843,12 @@ __device__ __forceinline__ bool item_ray(const RayParams& P, uint64_t i, F3* dir
 // as one step against max_steps).  It then continues from that point with the
 // plain method's exact FP32 march (same step rule), and goes back to the far
 // field whenever an exact step finds
-// |d| > band_exit.  At the hit the eps-shell crossing between the last two
-// exact points is found by secant steps on the exact distance (each verified
-// by an exact evaluation) instead of ten bisections, and the material comes
-// from the accepted point's evaluation; the normal is the plain method's.
+// |d| > band_exit.  A hit found by the exact march takes the plain method's
+// ten bisections between its last two samples (the reference's depth); a
+// hit reached by the counted descent onto the ground plane, whose bracket
+// ends at the plane crossing rather than at a sample, finds the eps-shell
+// crossing by secant steps on the exact distance (each verified by an exact
+// evaluation).  The normal is the plain method's.
 enum Phase : int { kMarch = 0, kRefine = 1, kNormal = 2, kFinal = 3, kFar = 4, kSecant = 5 };
 constexpr unsigned long long kMarchWallNs = 20ull * 1000000000ull;  // per warp
 
@@ -878,9 +900,9 @@ __global__ void __launch_bounds__(128, 6) march_depth_persistent(DevScene S0, Ra
   float nx = 0.0f, ny = 0.0f, nz = 0.0f;  // estimate_normal differences
   uint32_t steps = 0;
   int phase = kMarch, k = 0;
-  // precision form: exact distance at `prev` (< 0: unknown), secant bracket
-  // values, material of the accepted hit point
-  float dprev = -1.0f, dlo = 0.0f, dhi = 0.0f;
+  // precision form: secant bracket values of the counted descent, material
+  // of the accepted hit point
+  float dlo = 0.0f, dhi = 0.0f;
   uint32_t hit_mat = 0u;
   bool mat_known = false;
   auto write_miss = [&]() {
@@ -959,7 +981,6 @@ __global__ void __launch_bounds__(128, 6) march_depth_persistent(DevScene S0, Ra
             prev = traveled;
             steps = 0;
             phase = kBricks && B_of_lane.free_far ? kFar : kMarch;
-            dprev = -1.0f;
             mat_known = false;
           } else {
             write_miss();
@@ -1004,7 +1025,6 @@ __global__ void __launch_bounds__(128, 6) march_depth_persistent(DevScene S0, Ra
       if (!exact) continue;
       phase = kMarch;  // exact evaluation at `traveled` in this iteration
       prev = traveled;
-      dprev = -1.0f;
     }
 
     // The point this lane evaluates in this iteration.
@@ -1036,18 +1056,12 @@ __global__ void __launch_bounds__(128, 6) march_depth_persistent(DevScene S0, Ra
 
     if (phase == kMarch) {
       if (fabsf(info.d) < eps) {
+        // the plain method's ten bisections between the last two samples: the
+        // reference's depth (the eps-shell crossing found by bisection)
         lo = prev;
         hi = traveled;
         k = 0;
-        if (kBricks && dprev >= eps) {
-          phase = kSecant;
-          dlo = dprev;
-          dhi = info.d;
-          hit_mat = info.mat;
-          mat_known = true;  // the march's own sample at hi
-        } else {
-          phase = kRefine;
-        }
+        phase = kRefine;
       } else {
         // the nearest leaf is the ground and the ray descends: the cached
         // bound decides whether the rest of the approach is a plane descent
@@ -1078,7 +1092,6 @@ __global__ void __launch_bounds__(128, 6) march_depth_persistent(DevScene S0, Ra
           continue;
         }
         prev = traveled;
-        if (kBricks) dprev = info.d;
         traveled += fmaxf(fabsf(info.d) * scale, min_step);
         ++steps;
         if (kBricks && B.free_far && fabsf(info.d) > B.band_exit) phase = kFar;
@@ -1421,6 +1434,8 @@ __global__ void fma_peak_kernel(float* out, int iters, float a, float b) {
   float s = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
   if (s == 12345.678f) out[0] = s;
 }
+
+#include "ft_path.cuh"
 
 #endif  // FT_JIT
 

@@ -1012,6 +1012,49 @@ ft_status ft_render_depth_preview_noalloc(ft_scene* sc, const ft_render_options*
   FT_API_END
 }
 
+ft_status ft_render_pathtrace(ft_scene* sc, const ft_render_options* options, ft_accel_mode accel,
+                              const ft_pathtrace_settings* settings, float* rgb_out, uint8_t* rgb8_out,
+                              uint32_t* samples_out, uint32_t flags, void* stream) {
+  FT_API_BEGIN
+  if (!sc || !settings) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "scene and settings must be non-null");
+  if (accel < FT_ACCEL_NAIVE || accel > FT_ACCEL_BRICKS) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "unknown accel mode");
+  if (ft_status s = check_options(options, 1)) return s;
+  if (settings->spp > 65536 || settings->max_bounces > 64 || !(settings->noise_threshold >= 0.0f))
+    return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "spp must be <= 65536, max_bounces <= 64, noise_threshold >= 0");
+  std::lock_guard<std::mutex> lock(sc->mu);
+  FT_CUDA_TRY(cudaSetDevice(sc->device), "cudaSetDevice");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const bool dev_ptrs = (flags & FT_FLAG_DEVICE_POINTERS) != 0;
+  const size_t pixels = static_cast<size_t>(options->width) * options->height;
+  if (ft_status s = ensure_buffers(sc, pixels, pixels)) return s;
+  RayParams P = make_params(sc, *options, 1);
+  PathSettingsD ps;
+  // PathtraceSettings' clamps (R:3986-3990)
+  ps.spp = std::max(settings->spp, 1u);
+  ps.max_bounces = std::max(settings->max_bounces, 1u);
+  ps.min_spp = std::min(std::max(settings->min_spp, 1u), ps.spp);
+  ps.noise_threshold = std::max(settings->noise_threshold, 0.0f);
+  float* rgbf = rgb_out ? (dev_ptrs ? rgb_out : sc->d_rgbf) : nullptr;
+  uint8_t* rgb8 = rgb8_out ? (dev_ptrs ? rgb8_out : sc->d_rgb) : nullptr;
+  uint32_t* cnt = samples_out ? (dev_ptrs ? samples_out : sc->d_mat) : nullptr;
+  const unsigned blocks = static_cast<unsigned>((pixels + 127) / 128);
+  path_pixel_kernel<false><<<blocks, 128, 0, st>>>(sc->dev, P, ps, rgbf, rgb8, cnt, nullptr);
+  FT_CUDA_TRY(cudaGetLastError(), "path_pixel_kernel launch");
+  sc->last_launches = 1;
+  if (!dev_ptrs) {
+    if (rgb_out) FT_CUDA_TRY(cudaMemcpyAsync(rgb_out, rgbf, pixels * 3 * sizeof(float), cudaMemcpyDeviceToHost, st),
+                             "copy rgb");
+    if (rgb8_out) FT_CUDA_TRY(cudaMemcpyAsync(rgb8_out, rgb8, pixels * 3, cudaMemcpyDeviceToHost, st), "copy rgb8");
+    if (samples_out)
+      FT_CUDA_TRY(cudaMemcpyAsync(samples_out, cnt, pixels * sizeof(uint32_t), cudaMemcpyDeviceToHost, st),
+                  "copy samples");
+  }
+  FT_CUDA_TRY(cudaStreamSynchronize(st), "path trace");
+  ftcommon::clear_last_error();
+  return FT_OK;
+  FT_API_END
+}
+
 ft_status ft_render_trace(ft_scene* sc, const ft_render_options* options, ft_accel_mode accel, uint32_t aa_samples,
                           uint32_t max_depth, float* rgb_out, uint8_t* rgb8_out, uint32_t flags, void* stream) {
   FT_API_BEGIN

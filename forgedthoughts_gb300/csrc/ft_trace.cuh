@@ -344,7 +344,7 @@ struct GEntry {
 // modifiers come from their postfix op range.
 template <bool kStats>
 __device__ __noinline__ void resolve_generic(const DevScene& S, int root, F3 p, const HookCtx& hc, Resolved* out,
-                                             Ctx<kStats>& cx) {
+                                             Ctx<kStats>& cx, bool split_root) {
   GEntry st[8];
   int sp = 0;
   int node_stack[24];
@@ -419,7 +419,7 @@ __device__ __noinline__ void resolve_generic(const DevScene& S, int root, F3 p, 
       } else if (blend_kind(n.kind, &diff)) {
         float t = blend_weight(l.d, r.d, blend_radius(n), diff);
         e.n = blend_normals(l.n, r.n, t, diff);
-        if (top == 0) {  // smooth boolean at the leaf root: material split
+        if (top == 0 && split_root) {  // smooth boolean at the leaf root: material split
           out->m = l.m;
           out->mb = r.m;
           out->t = t;
@@ -539,8 +539,7 @@ struct NEntry {
 // gathered primitives is provably weightless when reach >= (other value) + r;
 // otherwise *need receives the reach required.
 __device__ __noinline__ bool resolve_urtree_reach(const DevScene& S, const DevUrTree& t, F3 p, const HookCtx& hc,
-                                                  float reach,
-                                                  Resolved* out, float* need) {
+                                                  float reach, Resolved* out, float* need, bool split_root) {
   int gpos[kGather];
   float gdist[kGather];
   int ng = 0;
@@ -548,13 +547,16 @@ __device__ __noinline__ bool resolve_urtree_reach(const DevScene& S, const DevUr
     *need = -1.0f;
     return false;
   }
+  // A frame holds its left child's result while the right subtree is
+  // resolved; a completed right child is combined at once from `carry`.
   struct Frame {
     int inner, stage;
     float tw;
     bool useL, useR;
-    NEntry slot[2];
+    NEntry left;
   };
   Frame fr[20];
+  NEntry carry;
   int fp = 0;
   const float r = t.r;
   // Set up a frame: child values, exact weight, which children carry weight.
@@ -593,8 +595,9 @@ __device__ __noinline__ bool resolve_urtree_reach(const DevScene& S, const DevUr
       }
       if (c < 0) {
         const DevNode& pn = S.nodes[S.ur_prims[t.prim_first + (-c - 1)]];
-        F.slot[F.stage].n = prim_normal(pn, p);
-        F.slot[F.stage].m = mat_of_leaf(S, pn, hc);
+        NEntry& e = F.stage == 0 ? F.left : carry;
+        e.n = prim_normal(pn, p);
+        e.m = mat_of_leaf(S, pn, hc);
         ++F.stage;
         continue;
       }
@@ -607,46 +610,62 @@ __device__ __noinline__ bool resolve_urtree_reach(const DevScene& S, const DevUr
       if (!open(fp, c)) return false;
       continue;
     }
+    // both children done: the left result in F.left, the right one in carry
+    if (fp == 0 && split_root) {
+      out->normal = F.useL && F.useR ? blend_normals(F.left.n, carry.n, F.tw, false)
+                                     : blend_normals(F.useL ? F.left.n : carry.n, F.useL ? F.left.n : carry.n,
+                                                     F.tw, false);
+      out->t = F.tw;
+      out->split = true;
+      out->m = F.useL ? F.left.m : carry.m;
+      out->mb = F.useR ? carry.m : F.left.m;
+      out->ok = true;
+      return true;
+    }
     NEntry res;
     bool mixes = S.ur_inner_blend[F.inner] != 0;
     if (F.useL && F.useR) {
-      res.n = blend_normals(F.slot[0].n, F.slot[1].n, F.tw, false);
-      res.m = blend_materials(F.slot[0].m, F.slot[1].m, F.tw);
+      res.n = blend_normals(F.left.n, carry.n, F.tw, false);
+      res.m = blend_materials(F.left.m, carry.m, F.tw);
     } else {
-      const NEntry& e = F.useL ? F.slot[0] : F.slot[1];
+      const NEntry& e = F.useL ? F.left : carry;
       res.n = blend_normals(e.n, e.n, F.tw, false);
       res.m = blend_with_far(e.m, F.useL, mixes);
     }
-    if (fp == 0) {
+    if (fp == 0) {  // the root's blended material (resolve_material_at_hit)
       out->normal = res.n;
-      out->t = F.tw;
-      out->split = true;
-      out->m = F.useL ? F.slot[0].m : F.slot[1].m;
-      out->mb = F.useR ? F.slot[1].m : F.slot[0].m;
+      out->m = res.m;
+      out->split = false;
       out->ok = true;
       return true;
     }
     --fp;
-    fr[fp].slot[fr[fp].stage - 1] = res;
+    if (fr[fp].stage == 1) fr[fp].left = res;  // a left child completed
+    else carry = res;
   }
   *need = -1.0f;  // only a corrupted tree gets here
   return false;
 }
 
-__device__ void resolve_urtree(const DevScene& S, const DevUrTree& t, F3 p, const HookCtx& hc, Resolved* out) {
+__device__ void resolve_urtree(const DevScene& S, const DevUrTree& t, F3 p, const HookCtx& hc, Resolved* out,
+                               bool split_root) {
   float reach = 3.0f * t.r;
   out->ok = false;
   for (int attempt = 0; attempt < 6; ++attempt) {
     float need = 0.0f;
-    if (resolve_urtree_reach(S, t, p, hc, reach, out, &need)) return;
+    if (resolve_urtree_reach(S, t, p, hc, reach, out, &need, split_root)) return;
     if (need < 0.0f) return;  // capacity exceeded
     reach = fmaxf(1.5f * reach, need * 1.0001f + 1.0e-6f);
   }
 }
 
-// Normal and material at a hit on leaf `li`.
+// Normal and material at a hit on leaf `li`.  With split_root a smooth
+// boolean at the root gives its two materials and weight (the Whitted
+// tracer's split, ray.rs:31-35); without it, the root's blended material
+// (resolve_material_at_hit, as the path tracer shades).
 template <bool kStats>
-__device__ void resolve_hit(const DevScene& S, int li, F3 p, const HookCtx& hc, Resolved* out, Ctx<kStats>& cx) {
+__device__ void resolve_hit(const DevScene& S, int li, F3 p, const HookCtx& hc, Resolved* out, Ctx<kStats>& cx,
+                            bool split_root = true) {
   const DevLeaf& lf = S.leaves[li];
   out->split = false;
   out->ok = false;
@@ -658,10 +677,10 @@ __device__ void resolve_hit(const DevScene& S, int li, F3 p, const HookCtx& hc, 
     return;
   }
   if (lf.kind == ftgpu::kLeafUrTree) {
-    resolve_urtree(S, S.urtrees[lf.first], p, hc, out);
+    resolve_urtree(S, S.urtrees[lf.first], p, hc, out, split_root);
     if (out->ok) return;
   }
-  resolve_generic(S, lf.node, p, hc, out, cx);
+  resolve_generic(S, lf.node, p, hc, out, cx, split_root);
 }
 
 // ---------------------------------------------------------------- lights and shadows

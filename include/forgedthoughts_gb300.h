@@ -435,6 +435,29 @@ ft_status ft_render_trace_stats(ft_scene* scene, const ft_render_options* option
                                 ft_accel_mode accel, uint32_t aa_samples, uint32_t max_depth,
                                 ft_render_stats* stats);
 
+/* `PathtraceSettings` (R:107-125): samples per pixel, bounces, and the
+ * adaptive stop (a pixel stops after min_spp samples once the relative
+ * standard error of its luminance is at most noise_threshold; 0 disables). */
+typedef struct ft_pathtrace_settings {
+  uint32_t spp;             /* default 16 */
+  uint32_t max_bounces;     /* default 4 */
+  uint32_t min_spp;         /* default 8 */
+  float noise_threshold;    /* default 0.03 */
+} ft_pathtrace_settings;
+
+/* The reference's MIS path tracer (render_pathtrace_with_accel_progressive,
+ * R:3974-4045; trace_path renderer/path.rs:3-112; estimate_direct_mis
+ * R:4572-4704).  Dead code in the reference (no CLI entry); here a render
+ * entry point.  Every pixel sample draws from its own XorShift64 seeded by
+ * seed_pixel_sample (R:4735-4774), so the image is deterministic.  Outputs
+ * (each nullable): the average linear radiance (width*height*3 floats), its
+ * spectrum_to_rgb8 (R:5221-5227) and the samples each pixel took.  The
+ * reference's preview callback (preview_every) is left to the caller: the
+ * call returns the final image. */
+ft_status ft_render_pathtrace(ft_scene* scene, const ft_render_options* options, ft_accel_mode accel,
+                              const ft_pathtrace_settings* settings, float* rgb_out, uint8_t* rgb8_out,
+                              uint32_t* samples_out, uint32_t flags, void* stream);
+
 /* The trace's counters per wavefront kernel kind: the ray march
  * (wf_march_persistent), the shading of the hits (wf_shade_kernel) and the
  * soft-shadow march (wf_shadow_persistent).  No counterpart in the reference

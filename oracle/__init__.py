@@ -52,6 +52,10 @@ def lib() -> ctypes.CDLL:
         h.oracle_render_views_strided.restype = ctypes.c_int
         h.oracle_render_views_strided.argtypes = [vp, vp, ctypes.c_uint32, vp, ctypes.c_float, ctypes.c_int,
                                                   ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, vp, vp, vp]
+        h.oracle_render_path.restype = ctypes.c_int
+        h.oracle_render_path.argtypes = [vp, vp, ctypes.c_int, u32, u32, u32, ctypes.c_float, ctypes.c_int,
+                                         ctypes.c_int, u32, u32, u32, u32, u32, vp, vp, vp,
+                                         ctypes.POINTER(ctypes.c_uint64)]
         h.oracle_render_sample.restype = ctypes.c_int
         h.oracle_render_sample.argtypes = [vp, vp, ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int,
                                            ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
@@ -147,6 +151,30 @@ def render_sample(state, options, accel: int, aa: int, max_depth: int, mode: str
                                       int(threads), int(rows[0]), int(rows[1]), int(cols[0]), int(cols[1]),
                                       ctypes.byref(evals)))
     return int(evals.value)
+
+
+def render_path(state, options, accel: int, spp: int = 16, max_bounces: int = 4, min_spp: int = 8,
+                noise_threshold: float = 0.03, precision: int = 32, threads: int = 0,
+                rows: tuple[int, int, int] | None = None, cols: tuple[int, int] | None = None):
+    """Oracle MIS path tracer (the progressive renderer with adaptive
+    sampling).  Returns (rgb linear (H, W, 3), rgb8, samples per pixel (H, W),
+    evals); ``rows`` / ``cols`` restrict it to a strided band."""
+    from forgedthoughts_gb300 import _native
+
+    h, w = int(options.height), int(options.width)
+    rgb = np.zeros((h, w, 3), np.float32)
+    rgb8 = np.zeros((h, w, 3), np.uint8)
+    count = np.zeros((h, w), np.uint32)
+    opts = options.to_c() if hasattr(options, "to_c") else options
+    assert isinstance(opts, _native.RenderOptionsC)
+    r0, r1, rs = rows if rows is not None else (0, h, 1)
+    c0, cs = cols if cols is not None else (0, 1)
+    evals = ctypes.c_uint64(0)
+    _check(lib().oracle_render_path(_vp(state.desc_ptr), ctypes.cast(ctypes.pointer(opts), ctypes.c_void_p),
+                                    int(accel), int(spp), int(max_bounces), int(min_spp), float(noise_threshold),
+                                    int(precision), int(threads), r0, r1, rs, c0, cs, _arr(rgb), _arr(rgb8),
+                                    _arr(count), ctypes.byref(evals)))
+    return rgb, rgb8, count, int(evals.value)
 
 
 def distance(state, points: np.ndarray, accel: int = 1, precision: int = 32):

@@ -1290,6 +1290,199 @@ template <class R> Sp<R> mat_eval(const Mat<R>& m, V<R> n, V<R> wi, V<R> wo) {
   return lerp_sp(model_eval(m.a_model, m.p, n, wi, wo), model_eval(m.b_model, m.pb, n, wi, wo), m.t);
 }
 
+// ---------------------------------------------------------------- BSDF sampling
+// Material::sample / Material::pdf for the MIS path tracer (materials/mod.rs:
+// 312-340, 399-432; lambert.rs, metal.rs, dielectric.rs, standard.rs).
+template <class R> struct BsdfSampleT {
+  V<R> wi;
+  Sp<R> f;
+  R pdf;
+  bool delta, apply_cos, transmission, thin_walled;
+  R next_ior;
+};
+template <class R> struct SampleInputT {
+  bool front_face;
+  R current_ior, u1, u2, u3;
+};
+// to_world (lambert.rs:52-61, metal.rs:65-74)
+template <class R> V<R> to_world(V<R> normal, R x, R y, R z) {
+  V<R> n = normalize(normal);
+  V<R> helper = std::fabs(n.y) < R(0.99) ? mk(R(0), R(1), R(0)) : mk(R(1), R(0), R(0));
+  V<R> t = normalize(cross(helper, n));
+  V<R> b = normalize(cross(n, t));
+  return normalize((t * x + b * y) + n * z);
+}
+template <class R> R lambert_pdf(V<R> n, V<R> wi) { return rmax(dot(n, wi), R(0)) / pi_<R>(); }
+template <class R> BsdfSampleT<R> lambert_sample(const Params<R>& m, V<R> n, const SampleInputT<R>& in) {
+  R uu1 = rclamp(in.u1, R(1.0e-6), R(1) - R(1.0e-6)), uu2 = rclamp(in.u2, R(1.0e-6), R(1) - R(1.0e-6));
+  R r = std::sqrt(uu1), phi = R(2) * pi_<R>() * uu2;
+  V<R> wi = to_world(n, r * std::cos(phi), r * std::sin(phi), std::sqrt(R(1) - uu1));
+  return BsdfSampleT<R>{wi, lambert_eval(m, n, wi), rmax(lambert_pdf(n, wi), R(1.0e-6)), false, true, false, false,
+                        in.current_ior};
+}
+template <class R> R metal_pdf_of(R roughness, V<R> n, V<R> wi, V<R> wo) {
+  if (dot(n, wi) <= R(0) || dot(n, wo) <= R(0)) return R(0);
+  V<R> h = normalize(wi + wo);
+  R ndoth = rmax(dot(n, h), R(0)), vdoth = rmax(std::fabs(dot(wo, h)), R(1.0e-6));
+  R rr = rclamp(roughness, R(0.02), R(1));
+  R d = ggx_d(ndoth, rr * rr);
+  return rmax(d * ndoth / (R(4) * vdoth), R(0));
+}
+template <class R> V<R> reflect_about(V<R> v, V<R> n) { return v - n * (R(2) * dot(v, n)); }
+template <class R> BsdfSampleT<R> metal_sample(const Params<R>& m, V<R> n, V<R> wo, const SampleInputT<R>& in) {
+  R rr = rclamp(m.roughness, R(0.02), R(1));
+  R alpha = rr * rr;
+  R uu1 = rclamp(in.u1, R(1.0e-6), R(1) - R(1.0e-6)), uu2 = rclamp(in.u2, R(1.0e-6), R(1) - R(1.0e-6));
+  R phi = R(2) * pi_<R>() * uu2;
+  R cos_t = std::sqrt((R(1) - uu1) / (R(1) + (alpha * alpha - R(1)) * uu1));
+  R sin_t = std::sqrt(rmax(R(1) - cos_t * cos_t, R(0)));
+  V<R> h = to_world(n, sin_t * std::cos(phi), sin_t * std::sin(phi), cos_t);
+  V<R> wi = normalize(reflect_about(wo * R(-1), h));
+  return BsdfSampleT<R>{wi, metal_eval(m, n, wi, wo), rmax(metal_pdf_of(m.roughness, n, wi, wo), R(1.0e-6)), false,
+                        true, false, false, in.current_ior};
+}
+template <class R> R fresnel_dielectric_of(R ci, R eta_i, R eta_t) {  // R:5188-5204
+  R ei = rmax(eta_i, R(1.0e-4)), et = rmax(eta_t, R(1.0e-4));
+  if (std::fabs(ei - et) < R(1.0e-6)) return R(0);
+  ci = rclamp(ci, R(0), R(1));
+  R eta = ei / et;
+  R sin2 = eta * eta * (R(1) - ci * ci);
+  if (sin2 >= R(1)) return R(1);
+  R ct = std::sqrt(R(1) - sin2);
+  R rs = ((ei * ci) - (et * ct)) / rmax((ei * ci) + (et * ct), R(1.0e-6));
+  R rp = ((et * ci) - (ei * ct)) / rmax((et * ci) + (ei * ct), R(1.0e-6));
+  return R(0.5) * (rs * rs + rp * rp);
+}
+// dielectric.rs refract (lines 81-94)
+template <class R> bool refract_of(V<R> incident, V<R> normal, R eta, V<R>* out) {
+  V<R> i = normalize(incident), n = normalize(normal);
+  R cosi = rclamp(dot(i, n), R(-1), R(1));
+  if (cosi > R(0)) n = n * R(-1);
+  else cosi = -cosi;
+  R sin2 = eta * eta * (R(1) - cosi * cosi);
+  if (sin2 > R(1)) return false;
+  R cost = std::sqrt(R(1) - sin2);
+  *out = normalize(i * eta + n * (eta * cosi - cost));
+  return true;
+}
+template <class R> BsdfSampleT<R> dielectric_sample(Sp<R> color, R ior_in, bool thin, V<R> normal, V<R> wo,
+                                                   const SampleInputT<R>& in) {
+  R ior = rclamp(ior_in, R(1), R(3));
+  R eta_i, eta_t, next_ior;
+  if (thin) { eta_i = R(1); eta_t = R(1); next_ior = in.current_ior; }
+  else if (in.front_face) { eta_i = in.current_ior; eta_t = ior; next_ior = ior; }
+  else { eta_i = in.current_ior; eta_t = R(1); next_ior = R(1); }
+  V<R> n = normalize(normal), incident = wo * R(-1);
+  R fresnel = rclamp(fresnel_dielectric_of(std::fabs(dot(n, wo)), eta_i, eta_t), R(0), R(1));
+  if (in.u1 < fresnel)
+    return BsdfSampleT<R>{normalize(reflect_about(incident, n)), sp(R(1), R(1), R(1)), rmax(fresnel, R(1.0e-6)), true,
+                          false, false, thin, in.current_ior};
+  V<R> wt;
+  if (refract_of(incident, n, eta_i / eta_t, &wt))
+    return BsdfSampleT<R>{normalize(wt), color, rmax(R(1) - fresnel, R(1.0e-6)), true, false, true, thin, next_ior};
+  return BsdfSampleT<R>{normalize(reflect_about(incident, n)), sp(R(1), R(1), R(1)), R(1), true, false, false, thin,
+                        in.current_ior};
+}
+// standard.rs:45-160
+template <class R> void standard_weights(const Params<R>& m, V<R> n, V<R> wo, R* dw, R* sw, R* cw) {
+  R metallic = rclamp(m.metallic, R(0), R(1)), transmission = rclamp(m.transmission, R(0), R(1));
+  R clearcoat = rclamp(m.clearcoat, R(0), R(1));
+  R ndotv = rmax(dot(n, wo), R(0));
+  R cx = rclamp(R(1) - rclamp(ndotv, R(0), R(1)), R(0), R(1));
+  R x2 = cx * cx;
+  R coat_cover = rclamp(clearcoat * (R(0.2) + R(0.8) * (x2 * x2 * cx)) * R(0.65), R(0), R(0.95));
+  *dw = rmax((R(1) - metallic) * (R(1) - transmission), R(0)) * (R(1) - coat_cover);
+  *sw = rclamp((m.specular * m.specular_weight) * (R(1) - transmission), R(0), R(1)) * (R(1) - coat_cover * R(0.85));
+  *cw = clearcoat * R(0.18);
+}
+template <class R> R standard_pdf(const Params<R>& m, V<R> n, V<R> wi, V<R> wo) {
+  R dw, sw, cw;
+  standard_weights(m, n, wo, &dw, &sw, &cw);
+  R sum = dw + sw + cw;
+  if (sum <= R(1.0e-6)) return lambert_pdf(n, wi);
+  return (dw / sum) * lambert_pdf(n, wi) + (sw / sum) * metal_pdf_of(m.roughness, n, wi, wo) +
+         (cw / sum) * metal_pdf_of(rclamp(m.clearcoat_roughness, R(0.02), R(1)), n, wi, wo);
+}
+template <class R> BsdfSampleT<R> standard_sample(const Params<R>& m, V<R> n, V<R> wo, const SampleInputT<R>& in) {
+  R dw, sw, cw;
+  standard_weights(m, n, wo, &dw, &sw, &cw);
+  R tw = rclamp(m.transmission, R(0), R(1));
+  R sum = dw + sw + cw + tw;
+  if (sum <= R(1.0e-6)) return lambert_sample(m, n, in);
+  R pick = rclamp(in.u3, R(0), R(1)) * sum;
+  if (pick < dw) {
+    BsdfSampleT<R> s = lambert_sample(m, n, in);
+    s.f = standard_eval(m, n, s.wi, wo);
+    s.pdf = rmax(standard_pdf(m, n, s.wi, wo), R(1.0e-6));
+    return s;
+  }
+  if (pick < dw + sw || pick < dw + sw + cw) {
+    Params<R> mp = m;
+    if (pick < dw + sw) {
+      // blended_f0 (standard.rs:168-175), lerp unclamped as standard.rs
+      R f0d = rclamp(f0_from_ior(m.ior), R(0), R(1));
+      Sp<R> base = scale(sp(f0d, f0d, f0d), rclamp(m.specular, R(0), R(1)) * rclamp(m.specular_weight, R(0), R(1))) *
+                   m.specular_color;
+      R met = rclamp(m.metallic, R(0), R(1));
+      mp.color = scale(base, R(1) - met) + scale(m.color, met);
+    } else {
+      mp.color = sp(R(1), R(1), R(1));
+      mp.roughness = rclamp(m.clearcoat_roughness, R(0.02), R(1));
+    }
+    BsdfSampleT<R> s = metal_sample(mp, n, wo, in);
+    s.f = standard_eval(m, n, s.wi, wo);
+    s.pdf = rmax(standard_pdf(m, n, s.wi, wo), R(1.0e-6));
+    return s;
+  }
+  BsdfSampleT<R> s = dielectric_sample(m.color, m.ior, m.thin_walled, n, wo, in);
+  s.f = s.transmission ? m.color : standard_eval(m, n, s.wi, wo);
+  s.pdf = s.delta ? rmax(s.pdf, R(1.0e-6)) : rmax(standard_pdf(m, n, s.wi, wo), R(1.0e-6));
+  return s;
+}
+template <class R> R model_pdf(int model, const Params<R>& p, V<R> n, V<R> wi, V<R> wo) {
+  switch (model) {
+    case kStandard: return standard_pdf(p, n, wi, wo);
+    case kLambert: return lambert_pdf(n, wi);
+    case kMetal: return metal_pdf_of(p.roughness, n, wi, wo);
+    default: return R(0);  // dielectric.rs:9-11
+  }
+}
+template <class R> BsdfSampleT<R> model_sample(int model, const Params<R>& p, V<R> n, V<R> wo,
+                                              const SampleInputT<R>& in) {
+  switch (model) {
+    case kStandard: return standard_sample(p, n, wo, in);
+    case kLambert: return lambert_sample(p, n, in);
+    case kMetal: return metal_sample(p, n, wo, in);
+    default: return dielectric_sample(p.color, p.ior, p.thin_walled, n, wo, in);
+  }
+}
+template <class R> R mat_pdf(const Mat<R>& m, V<R> n, V<R> wi, V<R> wo) {
+  if (m.kind != kBlend) return model_pdf(m.kind, m.p, n, wi, wo);
+  R t = rclamp(m.t, R(0), R(1));
+  return model_pdf(m.a_model, m.p, n, wi, wo) * (R(1) - t) + model_pdf(m.b_model, m.pb, n, wi, wo) * t;
+}
+// Material::sample incl. sample_blend (materials/mod.rs:399-432)
+template <class R> BsdfSampleT<R> mat_sample(const Mat<R>& m, V<R> n, V<R> wo, const SampleInputT<R>& in) {
+  if (m.kind != kBlend) return model_sample(m.kind, m.p, n, wo, in);
+  R t = rclamp(m.t, R(0), R(1));
+  BsdfSampleT<R> c = in.u3 < t ? model_sample(m.b_model, m.pb, n, wo, in) : model_sample(m.a_model, m.p, n, wo, in);
+  Sp<R> f = lerp_sp(model_eval(m.a_model, m.p, n, c.wi, wo), model_eval(m.b_model, m.pb, n, c.wi, wo), t);
+  R pdf = rmax(model_pdf(m.a_model, m.p, n, c.wi, wo) * (R(1) - t) + model_pdf(m.b_model, m.pb, n, c.wi, wo) * t,
+               R(1.0e-6));
+  bool all_delta = m.a_model == kDielectric && m.b_model == kDielectric;
+  return BsdfSampleT<R>{c.wi, f, pdf, c.delta && all_delta, c.apply_cos, c.transmission, c.thin_walled, c.next_ior};
+}
+template <class R> R luminance(const Sp<R>& s) { return R(0.2126) * s.r + R(0.7152) * s.g + R(0.0722) * s.b; }
+template <class R> Sp<R> clamp_luma(const Sp<R>& s, R max_luma) {  // clamp_spectrum (R:5168-5175)
+  R l = luminance(s);
+  if (l <= max_luma || l <= R(1.0e-6)) return s;
+  return scale(s, max_luma / l);
+}
+template <class R> R power_heuristic(R pa, R pb) {  // R:5098-5102
+  R a2 = pa * pa, b2 = pb * pb;
+  return a2 / rmax(a2 + b2, R(1.0e-6));
+}
+
 template <class R> R smoothstepf(R e0, R e1, R x) {  // R:7538-7541
   R t = rclamp((x - e0) / rmax(e1 - e0, R(1.0e-6)), R(0), R(1));
   return t * t * (R(3) - R(2) * t);
@@ -1364,6 +1557,145 @@ class Tracer {
       sum = sum + scale(trace(o, dirs[k], med, depth + 1, evals), inv);
     }
     return sum;
+  }
+
+  // ---------------------------------------------------------------- MIS path tracer
+  // trace_path (renderer/path.rs:3-112) with estimate_direct_mis and
+  // sample_one_light (R:4572-4704).  The path lights are the scene's lights
+  // with sphere lights as points (parse_lights R:6288-6388), in binding-name
+  // order.
+  struct PathCtx {  // BsdfContextBase (R:4397-4449) without hooks
+    V<R> normal, wo, hit_normal;
+    bool front;
+    R current_ior;
+  };
+  R env_light_pdf_for_dir(const Mat<R>& m, const PathCtx& c, V<R> wi) const {  // R:4336-4355
+    const ft_scene_desc& d = S.desc();
+    if (d.n_lights == 0) return R(0);
+    R env = 0;
+    for (uint32_t i = 0; i < d.n_lights; ++i) env += d.lights[i].kind == FT_LIGHT_ENV ? R(1) : R(0);
+    if (env <= R(0)) return R(0);
+    return (env / R(d.n_lights)) * rmax(mat_pdf(m, c.normal, wi, c.wo), R(1.0e-6));
+  }
+  // cosine_sample_hemisphere (R:4676-4695): two draws of the path's generator
+  static V<R> cosine_hemisphere(V<R> normal, XorShift64& rng) {
+    R u1 = rclamp(R(rng.next_f32()), R(1.0e-6), R(1) - R(1.0e-6));
+    R u2 = rclamp(R(rng.next_f32()), R(1.0e-6), R(1) - R(1.0e-6));
+    R r = std::sqrt(u1), phi = R(2) * pi_<R>() * u2;
+    return to_world(normal, r * std::cos(phi), r * std::sin(phi), std::sqrt(R(1) - u1));
+  }
+  Sp<R> estimate_direct_mis(const Mat<R>& m, V<R> p, const PathCtx& c, XorShift64& rng, uint64_t* evals) const {
+    const ft_scene_desc& d = S.desc();
+    if (d.n_lights == 0) return black<R>();
+    // sample_one_light
+    const R count = R(d.n_lights);
+    size_t idx = std::min(static_cast<size_t>(std::floor(R(rng.next_f32()) * count)), size_t(d.n_lights - 1));
+    const ft_light& L = d.lights[idx];
+    const R select_pdf = R(1) / count;
+    V<R> wi;
+    Sp<R> rad;
+    R pdf, max_t;
+    bool delta;
+    if (L.kind == FT_LIGHT_ENV) {
+      wi = cosine_hemisphere(c.normal, rng);
+      R env_pdf = rmax(rmax(dot(c.normal, wi), R(0)) / pi_<R>(), R(1.0e-6));
+      rad = sp(R(L.intensity[0]), R(L.intensity[1]), R(L.intensity[2]));
+      pdf = select_pdf * rmax(env_pdf, R(1.0e-6));
+      max_t = std::numeric_limits<R>::infinity();
+      delta = false;
+    } else {
+      V<R> to_light = mk(R(L.position[0]), R(L.position[1]), R(L.position[2])) - p;
+      R dist = rmax(std::sqrt(dot(to_light, to_light)), R(1.0e-4));
+      wi = to_light * (R(1) / dist);
+      rad = scale(sp(R(L.intensity[0]), R(L.intensity[1]), R(L.intensity[2])), R(1) / (dist * dist));
+      pdf = select_pdf;
+      max_t = dist - R(1.0e-4);
+      delta = true;
+    }
+    if (pdf <= R(1.0e-6)) return black<R>();
+    R cos_t = rmax(dot(c.normal, wi), R(0));
+    if (cos_t <= R(0)) return black<R>();
+    V<R> so = offset_origin(p, c.hit_normal, wi, R(op_.epsilon));
+    R vis = shadow(so, wi, max_t, evals);
+    if (vis <= R(0)) return black<R>();
+    Sp<R> f = mat_eval(m, c.normal, wi, c.wo);
+    R bsdf_pdf = rmax(mat_pdf(m, c.normal, wi, c.wo), R(1.0e-6));
+    R w = delta ? R(1) : power_heuristic(pdf, bsdf_pdf);
+    return scale(f * rad, (cos_t * vis * w) / rmax(pdf, R(1.0e-6)));
+  }
+  Sp<R> trace_path(V<R> origin, V<R> dir, uint32_t max_bounces, XorShift64& rng, uint64_t* evals) const {
+    Sp<R> throughput = sp(R(1), R(1), R(1)), radiance = black<R>();
+    bool have_prev = false;
+    R prev_pdf = 0;
+    PathCtx prev_ctx{};
+    Mat<R> prev_mat;
+    Medium<R> medium = Medium<R>::air();
+    const R eps = R(op_.epsilon);
+    for (uint32_t bounce = 0; bounce < max_bounces; ++bounce) {
+      R min_t = bounce == 0 ? R(0) : eps * R(2);
+      Hit<R> h;
+      if (!raymarch(A, origin, dir, op_, min_t, R(op_.max_dist), &h, evals)) {
+        Sp<R> env = attenuate(environment(dir), medium, R(op_.max_dist));
+        R weight = R(1);
+        if (have_prev)
+          weight = power_heuristic(rmax(prev_pdf, R(1.0e-6)),
+                                   rmax(env_light_pdf_for_dir(prev_mat, prev_ctx, dir), R(1.0e-6)));
+        radiance = radiance + scale(throughput * env, weight);
+        break;
+      }
+      throughput = throughput * medium_transmittance(medium, h.t);
+      const bool front = dot(h.normal, dir) < R(0);
+      V<R> wo = normalize(dir * R(-1));
+      const HookCtx hc{h.pos, front ? normalize(h.normal) : normalize(h.normal * R(-1)), wo, front ? R(1) : R(0)};
+      Mat<R> m;
+      if (!material_from_node(S.desc().root, h.pos, hc, &m)) m = material_for_id<R>(S.desc(), h.mat);
+      PathCtx c;
+      c.front = front;
+      c.hit_normal = front ? normalize(h.normal) : normalize(h.normal * R(-1));
+      c.normal = c.hit_normal;
+      V<R> gnode;
+      if (surface_normal(S.desc().root, h.pos, R(1.0e-4), &gnode)) c.normal = normalize(front ? gnode : gnode * R(-1));
+      c.wo = wo;
+      c.current_ior = medium.ior;
+      Sp<R> em = emission(m);
+      if (em.r > R(0) || em.g > R(0) || em.b > R(0)) radiance = radiance + throughput * em;
+      Sp<R> direct = estimate_direct_mis(m, h.pos, c, rng, evals);
+      radiance = radiance + clamp_luma(throughput * direct, R(12));
+      // sample_bsdf_lobe (R:4870-4903)
+      SampleInputT<R> in{front, c.current_ior, R(rng.next_f32()), R(rng.next_f32()), R(rng.next_f32())};
+      BsdfSampleT<R> smp = mat_sample(m, c.normal, c.wo, in);
+      if (smp.pdf <= R(1.0e-6)) break;
+      if (smp.apply_cos) {
+        R ct = rmax(dot(c.normal, smp.wi), R(0));
+        if (ct <= R(0)) break;
+        throughput = throughput * scale(smp.f, ct / rmax(smp.pdf, R(1.0e-6)));
+      } else {
+        throughput = throughput * scale(smp.f, R(1) / rmax(smp.pdf, R(1.0e-6)));
+      }
+      throughput = clamp_luma(throughput, R(8));
+      if (smp.delta) {
+        have_prev = false;
+      } else {
+        have_prev = true;
+        prev_pdf = rmax(smp.pdf, R(1.0e-6));
+        prev_ctx = c;
+        prev_mat = m;
+      }
+      if (bounce >= 2) {
+        R pr = rclamp(luminance(throughput), R(0.05), R(0.98));
+        if (R(rng.next_f32()) > pr) break;
+        throughput = scale(throughput, R(1) / pr);
+      }
+      dir = normalize(smp.wi);
+      if (smp.transmission && !smp.thin_walled) {
+        medium = transition(m, front, medium);
+        medium.ior = rclamp(smp.next_ior, R(1), R(3));
+        origin = offset_origin(h.pos, c.hit_normal, dir, eps * R(8));
+      } else {
+        origin = offset_origin(h.pos, c.hit_normal, dir, eps);
+      }
+    }
+    return radiance;
   }
 
   // trace_ray_recursive (ray.rs:3-39)
@@ -1931,6 +2263,97 @@ int render_trace(const ft_scene_desc* desc, const ft_render_options* options, in
   return 0;
 }
 
+// The progressive MIS path tracer (render_pathtrace_with_accel_progressive,
+// R:3974-4045): per pixel, samples 0, 1, ... each with its own XorShift64
+// seeded by seed_pixel_sample and jittered, until spp or until the pixel's
+// relative error falls to noise_threshold after min_spp samples
+// (PixelAccumulator R:4778-4817).  Pixels are independent, so one pass per
+// pixel gives the reference's result.  Outputs: the average (linear), its
+// spectrum_to_rgb8 (R:5221-5227) and the sample count per pixel.
+template <class R>
+int render_path(const ft_scene_desc* desc, const ft_render_options* options, int accel, uint32_t spp,
+                uint32_t max_bounces, uint32_t min_spp, float noise_threshold, int threads, uint32_t row_begin,
+                uint32_t row_end, uint32_t row_step, uint32_t col_begin, uint32_t col_step, float* rgb_out,
+                uint8_t* rgb8_out, uint32_t* count_out, uint64_t* evals_out) {
+  Opts op = resolve(options);
+  Scene<R> scene(*desc);
+  Accel<R> acc(scene, accel);
+  Camera<R> cam(*desc, op);
+  Tracer<R> tracer(scene, acc, op, 1);
+  spp = std::max(spp, 1u);
+  max_bounces = std::max(max_bounces, 1u);
+  min_spp = std::min(std::max(min_spp, 1u), spp);
+  const float threshold = std::max(noise_threshold, 0.0f);
+  float aspect = static_cast<float>(op.width) / static_cast<float>(op.height);
+  if (threads <= 0) threads = static_cast<int>(std::max(1u, std::thread::hardware_concurrency()));
+  row_step = std::max(row_step, 1u);
+  row_end = std::min(row_end, op.height);
+  std::vector<uint32_t> rows;
+  for (uint32_t y = row_begin; y < row_end; y += row_step) rows.push_back(y);
+  std::vector<uint32_t> cols = sample_columns(op.width, col_begin, col_step);
+  const size_t segs = (cols.size() + kSegment - 1) / kSegment;
+  std::atomic<size_t> next{0};
+  std::atomic<uint64_t> total{0};
+  auto worker = [&]() {
+    uint64_t evals = 0;
+    for (;;) {
+      size_t k = next.fetch_add(1);
+      if (k >= rows.size() * segs) break;
+      uint32_t y = rows[k / segs];
+      size_t c0 = (k % segs) * kSegment, c1 = std::min(c0 + kSegment, cols.size());
+      for (size_t ci = c0; ci < c1; ++ci) {
+        const uint32_t x = cols[ci];
+        Sp<float> sum = sp(0.0f, 0.0f, 0.0f);
+        uint32_t count = 0;
+        float mean = 0.0f, m2 = 0.0f;
+        for (uint32_t s = 0; s < spp; ++s) {
+          XorShift64 rng(seed_pixel_sample(x, y, op.width, s));
+          const float jx = rng.next_f32() - 0.5f;
+          const float jy = rng.next_f32() - 0.5f;
+          float px = (((static_cast<float>(x) + 0.5f + jx) / static_cast<float>(op.width)) * 2.0f - 1.0f) * aspect;
+          float py = 1.0f - ((static_cast<float>(y) + 0.5f + jy) / static_cast<float>(op.height)) * 2.0f;
+          V<R> d = cam.dir(R(px), R(py));
+          Sp<R> c = tracer.trace_path(cam.origin, d, max_bounces, rng, &evals);
+          Sp<float> cs = sp(float(c.r), float(c.g), float(c.b));
+          // PixelAccumulator::add_sample
+          sum = sum + cs;
+          count += 1;
+          float xl = luminance(cs);
+          float delta = xl - mean;
+          mean += delta / static_cast<float>(count);
+          m2 += delta * (xl - mean);
+          if (threshold > 0.0f && count >= min_spp && count >= 2) {
+            float n = static_cast<float>(count);
+            float var = std::max(m2 / (n - 1.0f), 0.0f);
+            float rel = std::sqrt(var / n) / std::max(std::fabs(mean), 1.0e-4f);
+            if (rel <= threshold) break;
+          }
+        }
+        Sp<float> avg = count ? scale(sum, 1.0f / static_cast<float>(count)) : sp(0.0f, 0.0f, 0.0f);
+        size_t pi = static_cast<size_t>(y) * op.width + x;
+        if (rgb_out) {
+          rgb_out[3 * pi] = avg.r;
+          rgb_out[3 * pi + 1] = avg.g;
+          rgb_out[3 * pi + 2] = avg.b;
+        }
+        if (rgb8_out) {
+          rgb8_out[3 * pi] = depth_to_u8(avg.r);
+          rgb8_out[3 * pi + 1] = depth_to_u8(avg.g);
+          rgb8_out[3 * pi + 2] = depth_to_u8(avg.b);
+        }
+        if (count_out) count_out[pi] = count;
+      }
+    }
+    total.fetch_add(evals);
+  };
+  std::vector<std::thread> pool;
+  for (int i = 1; i < threads; ++i) pool.emplace_back(worker);
+  worker();
+  for (auto& t : pool) t.join();
+  if (evals_out) *evals_out = total.load();
+  return 0;
+}
+
 // ============================================================ differentiation
 // Multi-view depth + soft silhouette and its adjoint: the definitions of
 // ft_render_views / ft_render_backward (include/forgedthoughts_gb300.h),
@@ -2417,6 +2840,23 @@ extern "C" int oracle_render_trace_strided(const ft_scene_desc* desc, const ft_r
                                 rgb_out, rgb8_out, evals_out, col_begin, col_step, jitter_seed);
   return render_trace<float>(desc, options, accel, aa_samples, max_depth, threads, row_begin, row_end, row_step,
                              rgb_out, rgb8_out, evals_out, col_begin, col_step, jitter_seed);
+}
+
+extern "C" int oracle_render_path(const ft_scene_desc* desc, const ft_render_options* options, int accel,
+                                  uint32_t spp, uint32_t max_bounces, uint32_t min_spp, float noise_threshold,
+                                  int precision, int threads, uint32_t row_begin, uint32_t row_end,
+                                  uint32_t row_step, uint32_t col_begin, uint32_t col_step, float* rgb_out,
+                                  uint8_t* rgb8_out, uint32_t* count_out, uint64_t* evals_out) {
+  if (int e = check_desc(desc)) return e;
+  if (!options || options->width == 0 || options->height == 0) {
+    g_error = "invalid render options";
+    return FT_ERR_INVALID_ARGUMENT;
+  }
+  if (precision == 64)
+    return render_path<double>(desc, options, accel, spp, max_bounces, min_spp, noise_threshold, threads, row_begin,
+                               row_end, row_step, col_begin, col_step, rgb_out, rgb8_out, count_out, evals_out);
+  return render_path<float>(desc, options, accel, spp, max_bounces, min_spp, noise_threshold, threads, row_begin,
+                            row_end, row_step, col_begin, col_step, rgb_out, rgb8_out, count_out, evals_out);
 }
 
 // Strided pixel sample (rows row_begin, +row_step ..; columns col_begin,

@@ -74,3 +74,31 @@ def test_gpu_trace_rough_dielectric_lobes():
                                .replace("roughness: 0.2", "roughness: 0.0").replace("roughness: 0.35", "roughness: 0.0"))
     lin_s, _ = ft.render_trace(smooth, opts, ft.AccelMode.Bvh, 1, 3)
     assert radiance_rmse(lin, lin_s) > 5e-3
+
+
+def test_gpu_path_tracer_matches_oracle():
+    """The MIS path tracer (trace_path with estimate_direct_mis, every pixel
+    sample seeded by seed_pixel_sample): GPU against the f32 oracle on the
+    same samples, with and without adaptive stopping.  Lambert, Metal,
+    Dielectric and the default Standard material, a point and an environment
+    light, a sky environment."""
+    import sys
+    sys.path.insert(0, __file__.rsplit("/", 1)[0])
+    from test_oracle import PATH_SCENE
+
+    st = ft.parse_and_eval(PATH_SCENE)
+    opts = ft.RenderOptions(width=96, height=72, max_steps=256, max_dist=50.0, epsilon=1e-4, step_scale=0.7)
+    for spp, min_spp, thr in ((8, 8, 0.0), (16, 4, 0.05)):
+        s = ft.PathtraceSettings(spp=spp, max_bounces=4, min_spp=min_spp, noise_threshold=thr)
+        lin, rgb8, n = ft.render_pathtrace(st, opts, ft.AccelMode.Bvh, s)
+        ref, ref8, nref, _ = oracle.render_path(st, opts, 1, spp=spp, max_bounces=4, min_spp=min_spp,
+                                                noise_threshold=thr)
+        # the sample counts follow the same per-pixel statistics
+        assert (n == nref).mean() >= 0.99, (n != nref).sum()
+        same = n == nref
+        # a path is a chain of random decisions: a last-bit difference can
+        # send one sample elsewhere, so compare per pixel with the Whitted
+        # chaotic bar
+        diff = np.abs(lin[same].astype(np.float64) - ref[same]).max(axis=-1)
+        assert (diff <= 1e-3).mean() >= 0.99, (diff <= 1e-3).mean()
+        assert radiance_rmse(lin[same], ref[same]) <= 2e-2, radiance_rmse(lin[same], ref[same])

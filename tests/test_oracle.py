@@ -161,3 +161,39 @@ def test_rough_dielectric_lobes_average_traced_rays():
     centre = (slice(8, 16), slice(8, 16))
     assert np.abs(b[centre] - a[centre]).max() > 1e-3
     assert abs(b[centre].mean() - a[centre].mean()) < 0.1 * a[centre].mean()
+
+
+PATH_SCENE = """
+environment Sky { fn color(dir) { return mix(vec3(0.9, 0.9, 0.95), vec3(0.3, 0.5, 1.0), clamp(dir.y, 0.0, 1.0)); } };
+let camera = Camera { origin: vec3(0.0, 1.0, -4.0), target: vec3(0.0, 0.5, 0.0), fov_y: 45.0 };
+let light = PointLight { position: vec3(3.0, 6.0, -3.0), intensity: 40.0 };
+let env = EnvLight { radiance: 0.3 };
+let ground = Box { size: vec3(20.0, 1.0, 20.0), pos: vec3(0.0, -0.5, 0.0), material: Lambert { color: vec3(0.6, 0.6, 0.6) } };
+let a = Sphere { radius: 0.5, pos: vec3(-1.1, 0.5, 0.0), material: Metal { roughness: 0.3 } };
+let b = Sphere { radius: 0.5, pos: vec3(0.0, 0.5, 0.3), material: Dielectric { ior: 1.5 } };
+let c = Sphere { radius: 0.5, pos: vec3(1.1, 0.5, 0.0) };
+let scene = ground + a + b + c;
+"""
+
+
+def test_path_tracer_is_deterministic_and_adaptive():
+    """The MIS path tracer seeds every pixel sample's generator from the pixel
+    and sample index: two runs are identical; with a noise threshold, pixels
+    stop between min_spp and spp samples and a pixel of the flat sky stops
+    at min_spp; more samples move the image less than fewer do."""
+    st = ft.parse_and_eval(PATH_SCENE)
+    opts = ft.RenderOptions(width=32, height=24, max_steps=256, max_dist=50.0, epsilon=1e-4, step_scale=0.7)
+    a, a8, na, _ = oracle.render_path(st, opts, 1, spp=16, max_bounces=4, min_spp=4, noise_threshold=0.05)
+    b, b8, nb, _ = oracle.render_path(st, opts, 1, spp=16, max_bounces=4, min_spp=4, noise_threshold=0.05)
+    assert np.array_equal(a, b) and np.array_equal(na, nb)
+    assert na.min() >= 4 and na.max() <= 16 and (na < 16).any() and (na == 16).any()
+    assert na[0, 0] == 4  # sky corner: the environment only, no variance
+    full, _, nf, _ = oracle.render_path(st, opts, 1, spp=16, max_bounces=4, min_spp=16, noise_threshold=0.0)
+    assert (nf == 16).all()
+    assert np.isfinite(full).all() and full.mean() > 0.05
+    few, _, _, _ = oracle.render_path(st, opts, 1, spp=4, max_bounces=4, min_spp=4, noise_threshold=0.0)
+    more, _, _, _ = oracle.render_path(st, opts, 1, spp=64, max_bounces=4, min_spp=64, noise_threshold=0.0)
+    assert np.abs(more - full).mean() < np.abs(few - full).mean()
+    f64, _, _, _ = oracle.render_path(st, opts, 1, spp=16, max_bounces=4, min_spp=16, noise_threshold=0.0,
+                                      precision=64)
+    assert np.abs(f64 - full).mean() < 0.02
