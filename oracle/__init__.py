@@ -39,6 +39,10 @@ def lib() -> ctypes.CDLL:
         h.oracle_render_views.restype = ctypes.c_int
         h.oracle_render_views.argtypes = [vp, vp, ctypes.c_uint32, vp, ctypes.c_float, ctypes.c_int, ctypes.c_int,
                                           vp, vp, vp]
+        h.oracle_render_backward_strided.restype = ctypes.c_int
+        h.oracle_render_backward_strided.argtypes = [vp, vp, ctypes.c_uint32, vp, ctypes.c_float, vp,
+                                                     ctypes.c_uint32, vp, vp, ctypes.c_int, ctypes.c_int,
+                                                     ctypes.c_uint32, ctypes.c_uint32, vp]
         h.oracle_render_backward.restype = ctypes.c_int
         h.oracle_render_backward.argtypes = [vp, vp, ctypes.c_uint32, vp, ctypes.c_float, vp, ctypes.c_uint32, vp,
                                              vp, ctypes.c_int, ctypes.c_int, vp]
@@ -249,7 +253,7 @@ def render_views(state, views, options, tau: float = 0.05, precision: int = 64, 
 
 
 def render_backward(state, views, options, params, dl_dt=None, dl_dsil=None, tau: float = 0.05,
-                    precision: int = 64, threads: int = 0) -> np.ndarray:
+                    precision: int = 64, threads: int = 0, stride: int = 1, offset: int = 0) -> np.ndarray:
     """The adjoint of render_views: dL/dparams (float64) for the upstream
     gradients dl_dt / dl_dsil (each (n_views, H, W) or None)."""
     from forgedthoughts_gb300 import _native
@@ -260,8 +264,8 @@ def render_backward(state, views, options, params, dl_dt=None, dl_dsil=None, tau
     a = None if dl_dt is None else np.ascontiguousarray(dl_dt, np.float32)
     b = None if dl_dsil is None else np.ascontiguousarray(dl_dsil, np.float32)
     g = np.zeros(len(parr), np.float64)
-    _check(lib().oracle_render_backward(_vp(state.desc_ptr), ctypes.cast(varr, ctypes.c_void_p), len(views),
-                                        ctypes.cast(ctypes.pointer(opts), ctypes.c_void_p), float(tau),
-                                        ctypes.cast(parr, ctypes.c_void_p), len(parr), _arr(a), _arr(b),
-                                        int(precision), int(threads), _arr(g)))
+    _check(lib().oracle_render_backward_strided(_vp(state.desc_ptr), ctypes.cast(varr, ctypes.c_void_p), len(views),
+                                                ctypes.cast(ctypes.pointer(opts), ctypes.c_void_p), float(tau),
+                                                ctypes.cast(parr, ctypes.c_void_p), len(parr), _arr(a), _arr(b),
+                                                int(precision), int(threads), int(stride), int(offset), _arr(g)))
     return g

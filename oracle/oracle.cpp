@@ -2933,6 +2933,26 @@ extern "C" int oracle_render_backward(const ft_scene_desc* desc, const ft_view* 
                              dl_dt, dl_dsil, grad_out);
 }
 
+// oracle_render_backward over the pixels (offset + i * stride, offset + j *
+// stride) of every view (the upstream gradients elsewhere are not read).
+extern "C" int oracle_render_backward_strided(const ft_scene_desc* desc, const ft_view* views, uint32_t n_views,
+                                              const ft_render_options* options, float tau, const ft_param* params,
+                                              uint32_t n_params, const float* dl_dt, const float* dl_dsil,
+                                              int precision, int threads, uint32_t stride, uint32_t offset,
+                                              double* grad_out) {
+  if (int e = check_desc(desc)) return e;
+  if (!options || options->width == 0 || options->height == 0 || !views || !(tau > 0.0f) || !grad_out ||
+      (n_params && !params)) {
+    g_error = "invalid backward arguments";
+    return FT_ERR_INVALID_ARGUMENT;
+  }
+  if (precision == 64)
+    return render_views<double>(desc, views, n_views, options, double(tau), threads, nullptr, nullptr, nullptr,
+                                params, n_params, dl_dt, dl_dsil, grad_out, stride, offset);
+  return render_views<float>(desc, views, n_views, options, tau, threads, nullptr, nullptr, nullptr, params, n_params,
+                             dl_dt, dl_dsil, grad_out, stride, offset);
+}
+
 extern "C" void oracle_medium_transmittance(const float medium[5], float distance, float out_rgb[3]) {
   const Medium<float> m{medium[0], sp(medium[1], medium[2], medium[3]), medium[4]};
   const Sp<float> t = medium_transmittance(m, distance);

@@ -93,6 +93,13 @@ int oracle_render_views_strided(const ft_scene_desc* desc, const ft_view* views,
                                 uint32_t stride, uint32_t offset, double* t_out, uint8_t* mask_out,
                                 double* sil_out);
 
+/* oracle_render_backward over the pixels (offset + i * stride, offset + j *
+ * stride) of every view. */
+int oracle_render_backward_strided(const ft_scene_desc* desc, const ft_view* views, uint32_t n_views,
+                                   const ft_render_options* options, float tau, const ft_param* params,
+                                   uint32_t n_params, const float* dl_dt, const float* dl_dsil, int precision,
+                                   int threads, uint32_t stride, uint32_t offset, double* grad_out);
+
 /* The adjoint of oracle_render_views (the definitions of ft_render_backward):
  * grad_out[k] = sum over rays of dl_dt dt/dparam_k + dl_dsil dsil/dparam_k. */
 int oracle_render_backward(const ft_scene_desc* desc, const ft_view* views, uint32_t n_views,
