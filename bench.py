@@ -500,10 +500,19 @@ def precision_form(reps: int = 2) -> dict:
     ft.render_depth(st, w.options, w.accel, 1)
     jit_ms = _cuda_ms(lambda: ft.render_depth(st, w.options, w.accel, 1, want_rgb8=False), reps)
     jimg = ft.render_depth(st, w.options, w.accel, 1)
+    # 1-bounce shading (Whitted depth 2) of the compiled scene
+    shade = lambda bricks: ft.render_trace(st, w.options, w.accel, 1, 2, fp16_bricks=bricks)  # noqa: E731
+    shade(False)
+    jit_shaded_ms = _cuda_ms(lambda: shade(False), reps)
+    jlin = shade(False)[0]
     info = g.build_bricks()
     ft.render_depth(st, w.options, w.accel, 1, fp16_bricks=True)
     b_ms = _cuda_ms(lambda: ft.render_depth(st, w.options, w.accel, 1, want_rgb8=False, fp16_bricks=True), reps)
     bimg = ft.render_depth(st, w.options, w.accel, 1, fp16_bricks=True)
+    shade(True)
+    b_shaded_ms = _cuda_ms(lambda: shade(True), reps)
+    blin = shade(True)[0]
+    _log(f"  shaded: compiled {jit_shaded_ms:.0f} ms, compiled + bricks {b_shaded_ms:.0f} ms")
 
     def agree(a, b):
         both = (a.mask == 1) & (b.mask == 1)
@@ -519,7 +528,14 @@ def precision_form(reps: int = 2) -> dict:
             "jit_fp16_bricks": {"value": mr(b_ms), "ms": b_ms, "speedup_vs_plain": plain_ms / b_ms,
                                 "vs_plain": agree(ref, bimg),
                                 "bricks": {"build_ms": info.build_ms, "device_bytes": info.device_bytes,
-                                           "max_lipschitz": info.max_lipschitz, "near_bricks": info.near_bricks}}}
+                                           "max_lipschitz": info.max_lipschitz, "near_bricks": info.near_bricks}},
+            "shaded_1_bounce": {
+                "what": "Whitted depth 2 (primary hit, lights, shadows, one bounce), 1 spp",
+                "jit_nvrtc": {"value": mr(jit_shaded_ms), "ms": jit_shaded_ms},
+                "jit_fp16_bricks": {"value": mr(b_shaded_ms), "ms": b_shaded_ms,
+                                    "speedup_vs_jit": jit_shaded_ms / b_shaded_ms,
+                                    "radiance_rmse_vs_jit": float(np.sqrt(np.mean(
+                                        (blin.astype(np.float64) - jlin) ** 2)))}}}
 
 
 def batched_form(reps: int = 3) -> dict:

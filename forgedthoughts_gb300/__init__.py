@@ -319,16 +319,21 @@ def jitter_flags(jitter_seed: int | None) -> int:
 
 
 def render_trace(state: SceneState, options: RenderOptions, accel: AccelMode = AccelMode.Bvh, aa_samples: int = 1,
-                 max_depth: int = 8, *, want_linear: bool = True, jitter_seed: int | None = None) -> tuple:
+                 max_depth: int = 8, *, want_linear: bool = True, jitter_seed: int | None = None,
+                 fp16_bricks: bool = False) -> tuple:
     """Whitted trace of ``state`` on the GPU: (linear rgb (H, W, 3) float32 or
     None, rgb8 (H, W, 3) uint8).  ``jitter_seed`` selects jittered AA offsets
-    (XorShift64 per pixel sample, the seed xor-ed in) instead of the grid."""
+    (XorShift64 per pixel sample, the seed xor-ed in) instead of the grid.
+    With ``fp16_bricks`` the primary hits come from the FP16 brick depth march
+    (``SceneState.gpu().build_bricks()`` first)."""
     h, w = int(options.height), int(options.width)
     lin = np.empty((h, w, 3), np.float32) if want_linear else None
     rgb8 = np.empty((h, w, 3), np.uint8)
     opts = options.to_c()
     _check(_native.lib().ft_render_trace(state.gpu().handle, ctypes.byref(opts), int(accel), max(int(aa_samples), 1),
-                                         int(max_depth), _ptr(lin), _ptr(rgb8), jitter_flags(jitter_seed), None))
+                                         int(max_depth), _ptr(lin), _ptr(rgb8),
+                                         jitter_flags(jitter_seed) | (_native.FT_FLAG_FP16_BRICKS if fp16_bricks else 0),
+                                         None))
     return lin, rgb8
 
 

@@ -858,12 +858,12 @@ constexpr unsigned long long kMarchWallNs = 20ull * 1000000000ull;  // per warp
 // brick cache from the batch tables (otherwise they are the kernel's own
 // parameters); outputs are the concatenated arrays of all items.
 //
-// Six resident blocks per SM (at most 80 registers): measured on the
-// 512-primitive field at 1920x1080, 165 Mrays/s against 148 with the
-// compiler's own choice (64 registers and more spills) and 132 with one block
-// (123 registers).
+// Five resident blocks per SM (at most 102 registers): measured on the
+// 512-primitive field at 1920x1080, 167 Mrays/s against 165 with six blocks
+// (80 registers), 161 with four, 148 with the compiler's own choice (64
+// registers and more spills) and 132 with one block (123 registers).
 template <bool kStats, bool kBricks, bool kBatch>
-__global__ void __launch_bounds__(128, 6) march_depth_persistent(DevScene S0, RayParams P0, DevBricks B0, BatchView V,
+__global__ void __launch_bounds__(128, 5) march_depth_persistent(DevScene S0, RayParams P0, DevBricks B0, BatchView V,
                                                               float* __restrict__ t_out,
                                                               uint8_t* __restrict__ mask_out,
                                                               uint32_t* __restrict__ mat_out,

@@ -123,6 +123,8 @@ struct ft_scene {
   uint64_t wf_hits_cap = 0;
   WShadow* wf_shadows = nullptr;
   uint64_t wf_shadows_cap = 0;
+  float* wf_primary_normal = nullptr;  // per-sample normals of a depth-marched primary level
+  uint64_t wf_primary_normal_cap = 0;
   // job counts (2), shadow count, overflow flag, march and shadow work
   // counters, self-check flags (kWfCounters)
   unsigned long long* wf_counters = nullptr;
@@ -701,8 +703,12 @@ ft_status check_tuning(const ft_batch_tuning& t) {
 // sample lands in sc->d_normal.  Queue sizes are read back once per level to
 // size the next one; the capacities are exact upper bounds (a job pushes at
 // most max_rays_per_hit rays, and two materials x the light samples).
+// With primary_bricks the level-0 hits come from the FP16 brick depth march of
+// the primary samples (launch_depth, then wf_hits_from_depth_kernel) instead
+// of the wavefront march; every later level is unchanged.
 ft_status trace_wavefront(ft_scene* sc, const RayParams& P, uint32_t max_depth, cudaStream_t st,
-                          uint32_t* launches, unsigned long long* const* kind_stats = nullptr) {
+                          uint32_t* launches, unsigned long long* const* kind_stats = nullptr,
+                          bool primary_bricks = false) {
   const ftgpu::SceneImage& im = sc->img;
   uint64_t light_samples = 0;
   const uint64_t max_push = max_rays_per_hit(im);
@@ -764,11 +770,25 @@ ft_status trace_wavefront(ft_scene* sc, const RayParams& P, uint32_t max_depth, 
     unsigned long long jcap = sc->wf_jobs_cap[cur];
     FT_CUDA_TRY(cudaMemsetAsync(march_next, 0, sizeof(unsigned long long), st), "cudaMemsetAsync(queues)");
     unsigned mgrid = static_cast<unsigned>(std::max<uint64_t>(1, std::min<uint64_t>((n + 127) / 128,
-                                                                                   static_cast<uint64_t>(sms) * 6)));
-    void* margs[] = {&S, &PP, &none, &jobs, &count, &jcap, &hits, &radiance, &march_next, &flags, &st_march};
-    ev = prof_begin(sc, st, FT_KERNEL_MARCH);
-    FT_CUDA_TRY(cudaLaunchKernel(k_march, dim3(mgrid), dim3(128), margs, 0, st), "wavefront march launch");
-    prof_end(sc, st, ev);
+                                                                                   static_cast<uint64_t>(sms) * 5)));
+    if (level == 0 && primary_bricks) {
+      const uint64_t samples3 = 3 * static_cast<uint64_t>(samples);
+      if (ft_status s = grow(&sc->wf_primary_normal, &sc->wf_primary_normal_cap, samples3, "cudaMalloc(normals)"))
+        return s;
+      if (ft_status s = launch_depth(sc, P, st, false, true, sc->d_t, sc->d_mask, nullptr, sc->wf_primary_normal))
+        return s;
+      ev = prof_begin(sc, st, FT_KERNEL_MARCH);
+      wf_hits_from_depth_kernel<<<grid, 128, 0, st>>>(S, PP, jobs, n, sc->d_t, sc->d_mask, sc->wf_primary_normal,
+                                                       hits, radiance);
+      prof_end(sc, st, ev);
+      FT_CUDA_TRY(cudaGetLastError(), "wf_hits_from_depth_kernel launch");
+      *launches += 1;
+    } else {
+      void* margs[] = {&S, &PP, &none, &jobs, &count, &jcap, &hits, &radiance, &march_next, &flags, &st_march};
+      ev = prof_begin(sc, st, FT_KERNEL_MARCH);
+      FT_CUDA_TRY(cudaLaunchKernel(k_march, dim3(mgrid), dim3(128), margs, 0, st), "wavefront march launch");
+      prof_end(sc, st, ev);
+    }
     WQueues Q{radiance, sc->wf_jobs[nxt], c + nxt, sc->wf_jobs_cap[nxt], sc->wf_shadows, c + 2,
               sc->wf_shadows_cap, reinterpret_cast<unsigned int*>(c + 3), max_depth};
     const WHit* chits = hits;
@@ -802,6 +822,14 @@ ft_status trace_wavefront(ft_scene* sc, const RayParams& P, uint32_t max_depth, 
   FT_CUDA_TRY(cudaStreamSynchronize(st), "wavefront");
   if (tail[0]) return ftcommon::fail(FT_ERR_CUDA, "wavefront queue overflow");
   if (ft_status s = march_check(tail[3])) return s;
+  if (primary_bricks) {
+    unsigned long long depth_flags = 0;
+    FT_CUDA_TRY(cudaMemcpyAsync(&depth_flags, sc->d_stats + kStatWork + 1, sizeof(depth_flags), cudaMemcpyDeviceToHost,
+                                st),
+                "march flags");
+    FT_CUDA_TRY(cudaStreamSynchronize(st), "march flags");
+    if (ft_status s = march_check(depth_flags)) return s;
+  }
   return FT_OK;
 }
 
@@ -918,6 +946,7 @@ void ft_scene_destroy(ft_scene* sc) {
   cudaFree(sc->wf_jobs[1]);
   cudaFree(sc->wf_hits);
   cudaFree(sc->wf_shadows);
+  cudaFree(sc->wf_primary_normal);
   cudaFree(sc->wf_counters);
   for (cudaEvent_t e : sc->prof_pool) cudaEventDestroy(e);
   cudaSetDevice(prev);
@@ -1065,6 +1094,9 @@ ft_status ft_render_trace(ft_scene* sc, const ft_render_options* options, ft_acc
   uint32_t depth = std::max(max_depth, 1u);  // RaySettings::max_depth.max(1)
   if (depth > 10) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "max_depth must be <= 10");
   std::lock_guard<std::mutex> lock(sc->mu);
+  const bool primary_bricks = (flags & FT_FLAG_FP16_BRICKS) != 0;
+  if (primary_bricks && !sc->has_bricks)
+    return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "FT_FLAG_FP16_BRICKS needs ft_scene_build_bricks first");
   FT_CUDA_TRY(cudaSetDevice(sc->device), "cudaSetDevice");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const bool dev_ptrs = (flags & FT_FLAG_DEVICE_POINTERS) != 0;
@@ -1076,7 +1108,8 @@ ft_status ft_render_trace(ft_scene* sc, const ft_render_options* options, ft_acc
   uint64_t blocks = (P.n_items + 127) / 128;
   if (blocks > 0x7fffffffull) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "image too large");
   uint32_t launches = 0;
-  if (ft_status s = trace_wavefront(sc, P, depth, st, &launches)) return s;
+  if (ft_status s = trace_wavefront(sc, P, depth, st, &launches, nullptr, primary_bricks))
+    return s;
   float* rgbf = rgb_out ? (dev_ptrs ? rgb_out : sc->d_rgbf) : nullptr;
   uint8_t* rgb8 = rgb8_out ? (dev_ptrs ? rgb8_out : sc->d_rgb) : nullptr;
   uint32_t np = static_cast<uint32_t>(pixels);

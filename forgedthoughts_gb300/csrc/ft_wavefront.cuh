@@ -217,9 +217,11 @@ enum WfPhase : int { kWfMarch = 0, kWfRefine = 1, kWfNormal = 2, kWfFinal = 3 };
 // raymarch_hit (R:4091-4139) of every queued ray: march from the ray's
 // secondary_min_t (R:4175-4178), ten bisections, the six-tap normal and the
 // hit leaf's lookup (march_hit, one evaluation per iteration); a miss adds
-// the environment seen through the ray's medium.
+// the environment seen through the ray's medium.  Five resident blocks per SM
+// (the launch is five per SM): on the 512-primitive field's depth-6 trace,
+// 181 ms of march per frame against 185 with six and 195 with four.
 template <bool kBatch, bool kStats>
-__global__ void __launch_bounds__(128, 6) wf_march_persistent(DevScene S0, RayParams P0, BatchView V,
+__global__ void __launch_bounds__(128, 5) wf_march_persistent(DevScene S0, RayParams P0, BatchView V,
                                                               const WJob* __restrict__ jobs,
                                                               const unsigned long long* __restrict__ count,
                                                               unsigned long long cap, WHit* __restrict__ hits,
@@ -429,6 +431,45 @@ __global__ void __launch_bounds__(128, 8) wf_shadow_persistent(DevScene S0, RayP
 #undef FT_WF_REFILL_TOP
 
 #ifndef FT_JIT
+// Level-0 hits from a depth march of the same primary samples (the FP16 brick
+// form of a trace): the depth march gives t, the hit mask and the six-tap
+// normal per sample; the hit record takes the point o + d t and the leaf
+// lookup there, as the wavefront march's final phase does, and a miss adds
+// the environment.
+__global__ void __launch_bounds__(128) wf_hits_from_depth_kernel(DevScene S, RayParams P,
+                                                                 const WJob* __restrict__ jobs, unsigned long long n,
+                                                                 const float* __restrict__ t_in,
+                                                                 const uint8_t* __restrict__ mask_in,
+                                                                 const float* __restrict__ normal_in,
+                                                                 WHit* __restrict__ hits, float* __restrict__ radiance) {
+  Ctx<false> cx;
+  FT_GRID_STRIDE(i, n) {
+    const WJob& wj = jobs[i];
+    if (wj.sample == kNoSample) {
+      hits[i].leaf = -2;
+      continue;
+    }
+    const uint32_t s = wj.sample;
+    const F3 o = f3(wj.o[0], wj.o[1], wj.o[2]);
+    const F3 d = f3(wj.d[0], wj.d[1], wj.d[2]);
+    if (!mask_in[s]) {
+      RayJob J = job_of(wj);
+      add_radiance(radiance, s, mul3(J.w, mul3(environment(S, J.d), transmittance(J.med, P.max_dist))));
+      hits[i].leaf = -1;
+      continue;
+    }
+    WHit h{};
+    const float t = t_in[s];
+    const F3 pos = o + d * t;
+    Info fin = scene_distance_leaf(S, pos, &h.leaf, cx);
+    h.t = t;
+    h.pos[0] = pos.x; h.pos[1] = pos.y; h.pos[2] = pos.z;
+    h.normal[0] = normal_in[3 * s]; h.normal[1] = normal_in[3 * s + 1]; h.normal[2] = normal_in[3 * s + 2];
+    h.mat = fin.mat;
+    hits[i] = h;
+  }
+}
+
 // ---------------------------------------------------------------- batches
 // The same kernels over the queues of many renders at once (ft_batch): every
 // job carries its global sample index, and the render it belongs to is the

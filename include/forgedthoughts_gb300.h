@@ -293,7 +293,10 @@ typedef struct ft_scene ft_scene;
 #define FT_JITTER_SEED_SHIFT 16
 #define FT_FLAG_JITTER_SEED(seed) (((uint32_t)(seed) & 0xffffu) << FT_JITTER_SEED_SHIFT)
 #define FT_FLAG_FP16_BRICKS 2u      /* depth march through the FP16 brick cache
-                                       (ft_scene_build_bricks must have run) */
+                                       (ft_scene_build_bricks must have run);
+                                       for ft_render_trace, the primary hits
+                                       come from that march and every later
+                                       bounce is the plain march */
 
 /* ---------------------------------------------------------------------------
  * Entry points.

@@ -25,3 +25,8 @@ def assert_depth_parity(t_gpu, m_gpu, t_ref, m_ref, what=""):
     assert r["mask_agreement"] >= MASK_AGREEMENT, (what, r)
     assert r["depth_within_tol"] >= MASK_AGREEMENT, (what, r)
     return r
+
+
+def radiance_rmse(a, b):
+    """Root mean square of the radiance difference, in FP64."""
+    return float(np.sqrt(np.mean((np.asarray(a, np.float64) - np.asarray(b, np.float64)) ** 2)))

@@ -6,7 +6,7 @@ import pytest
 import forgedthoughts_gb300 as ft
 import oracle
 from forgedthoughts_gb300 import workloads
-from parity import DEPTH_TOL, MASK_AGREEMENT, compare_depth
+from parity import DEPTH_TOL, MASK_AGREEMENT, compare_depth, radiance_rmse
 
 pytestmark = pytest.mark.gpu
 
@@ -132,6 +132,37 @@ def test_twisted_shells_fp16_vs_plain_and_oracle():
     # no worse than the plain FP32 march against the FP64 oracle
     assert r64["mask_agreement"] >= min(MASK_AGREEMENT, p64["mask_agreement"]), (r64, p64)
     assert r64["depth_within_tol"] >= min(MASK_AGREEMENT, p64["depth_within_tol"]), (r64, p64)
+
+
+def test_trace_primary_hits_from_bricks():
+    """A Whitted trace (depth 2) whose primary hits come from the FP16 brick
+    march: where its primary hit agrees with the plain march's, the radiance
+    is the plain trace's; against the f32 oracle, radiance RMSE <= 1e-3."""
+    w = workloads.union_round_field(width=320, height=180, aa=1)
+    st = ft.parse_and_eval(w.source)
+    st.gpu().build_bricks()
+    plain, fp16 = _both(st, w, w.accel)
+    lin_p, _ = ft.render_trace(st, w.options, w.accel, 1, 2)
+    lin_b, rgb8_b = ft.render_trace(st, w.options, w.accel, 1, 2, fp16_bricks=True)
+    same = (plain.mask[..., 0] == fp16.mask[..., 0]) & (plain.t[..., 0] == fp16.t[..., 0])
+    close = (plain.mask[..., 0] == fp16.mask[..., 0]) & (np.abs(plain.t[..., 0] - fp16.t[..., 0]) <= 1e-4)
+    assert close.mean() >= MASK_AGREEMENT
+    # identical primary hit: identical shading up to FMA contraction
+    assert np.abs(lin_b[same] - lin_p[same]).max() <= 1e-4
+    ref, _, _ = oracle.render_trace(st, w.options, int(w.accel), 1, 2, 32)
+    assert radiance_rmse(lin_b, ref) <= 1e-3, radiance_rmse(lin_b, ref)
+    assert radiance_rmse(lin_b[close], ref[close]) <= radiance_rmse(lin_p, ref) + 1e-4
+    # deterministic, and the 8-bit image is the linear one's tone map
+    again, _ = ft.render_trace(st, w.options, w.accel, 1, 2, fp16_bricks=True)
+    assert np.array_equal(again, lin_b)
+    assert rgb8_b.shape == (w.options.height, w.options.width, 3)
+
+
+def test_trace_bricks_flag_needs_a_brick_cache():
+    w = workloads.spheres_on_ground(8, 0, 64, 64)
+    st = ft.parse_and_eval(w.source)
+    with pytest.raises(ft.RenderError, match="ft_scene_build_bricks"):
+        ft.render_trace(st, w.options, w.accel, 1, 2, fp16_bricks=True)
 
 
 def test_brick_stats_count_far_steps():

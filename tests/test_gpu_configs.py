@@ -21,7 +21,7 @@ import pytest
 import forgedthoughts_gb300 as ft
 import oracle
 from forgedthoughts_gb300 import workloads
-from parity import assert_depth_parity, compare_depth
+from parity import assert_depth_parity, compare_depth, radiance_rmse
 
 pytestmark = pytest.mark.gpu
 
@@ -32,10 +32,6 @@ COLS6 = (8, 32)        # 60 columns: the depth-6 tree costs the oracle about 3x 
 
 def _band(a, rows=ROWS, cols=COLS):
     return a[rows[0]:rows[1]:rows[2], cols[0]::cols[1]]
-
-
-def radiance_rmse(a, b):
-    return float(np.sqrt(np.mean((a.astype(np.float64) - b.astype(np.float64)) ** 2)))
 
 
 @pytest.fixture(scope="module")
@@ -117,9 +113,9 @@ def test_c3_hooked_shells_full_frame_depth():
 
 def test_c3_shaded_full_frame():
     """C3's 1-bounce shading (Whitted depth 2) at 1920x1080, with 256 of the
-    hooked shells, interpreted and compiled: against the f32 oracle, 98.5 %
-    of the pixels within 1e-3 and radiance RMSE <= 1e-3 where the primary
-    hits agree."""
+    hooked shells, interpreted, compiled, and compiled with the primary hits
+    from the FP16 brick march: against the f32 oracle, 98.5 % of the pixels
+    within 1e-3 and radiance RMSE <= 1e-3 where the primary hits agree."""
     w = workloads.twisted_shells(n=256)
     st = ft.parse_and_eval(w.source)
     rows, cols = (22, 1080, 90), (8, 64)
@@ -131,16 +127,23 @@ def test_c3_shaded_full_frame():
     # hits agree, and 98.5 % of all pixels must be within 1e-3 (4 of the 360
     # band pixels differ by more, though the oracle's own f32 and f64 agree
     # to 1e-6 there)
-    agree = _band((img.mask[..., 0] == m[..., 0]) & (np.abs(img.t[..., 0] - t[..., 0]) <= 1e-4), rows, cols)
+    def agreement(img):
+        return _band((img.mask[..., 0] == m[..., 0]) & (np.abs(img.t[..., 0] - t[..., 0]) <= 1e-4), rows, cols)
+
+    agree = agreement(img)
     assert agree.mean() >= 0.99
-    results = {"interpreter": ft.render_trace(st, w.options, w.accel, 1, 2)[0]}
+    results = {"interpreter": (ft.render_trace(st, w.options, w.accel, 1, 2)[0], agree)}
     st.gpu().jit()
-    results["compiled"] = ft.render_trace(st, w.options, w.accel, 1, 2)[0]
-    for label, lin in results.items():
+    results["compiled"] = (ft.render_trace(st, w.options, w.accel, 1, 2)[0], agree)
+    st.gpu().build_bricks()
+    bagree = agreement(ft.render_depth(st, w.options, w.accel, 1, fp16_bricks=True))
+    assert bagree.mean() >= 0.99
+    results["compiled_fp16_bricks"] = (ft.render_trace(st, w.options, w.accel, 1, 2, fp16_bricks=True)[0], bagree)
+    for label, (lin, ok) in results.items():
         a, b = _band(lin, rows, cols), _band(ref, rows, cols)
         within = float((np.abs(a.astype(np.float64) - b).max(axis=-1) <= 1e-3).mean())
         assert within >= 0.985, (label, within)
-        assert radiance_rmse(a[agree], b[agree]) <= 1e-3, (label, radiance_rmse(a[agree], b[agree]))
+        assert radiance_rmse(a[ok], b[ok]) <= 1e-3, (label, radiance_rmse(a[ok], b[ok]))
 
 
 def _spheres(w):
