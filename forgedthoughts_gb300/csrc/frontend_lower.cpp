@@ -160,6 +160,7 @@ ft_material material_defaults(int kind) {
   std::memset(&m, 0, sizeof(m));
   m.kind = kind;
   m.color_program = m.roughness_program = m.ior_program = m.thin_walled_program = -1;
+  for (int32_t& h : m.hook_program) h = -1;
   m.color[0] = m.color[1] = m.color[2] = 0.8f;
   m.roughness = 0.5f;
   m.ior = 1.5f;
@@ -309,8 +310,16 @@ class HookCompiler {
   // seven parameters (FT_MATERIAL_HOOK_PARAMS).  want: 0 a number, 1 a vec3,
   // 2 either.  Returns false, emitting nothing, when the body does not fold to
   // a program of the wanted type.
+  //
+  // With bsdf set the context is the BSDF context of bsdf_context_value
+  // (R:5006-5030), FT_BSDF_HOOK_PARAMS parameters: the seven (normal = the
+  // shading normal, view_dir = wo), then wo, wi, current_ior and, when
+  // sample_randoms, u1, u2, u3 (the registers exist either way; eval and pdf
+  // see no u fields).  With field set the body returns a record (a
+  // BsdfSample) and the program computes that field of it; a record without
+  // the field emits nothing and returns false.
   bool compile_ctx(const BlockStmt& fn, const BlockDef& def, const ObjectData& overrides, int want,
-                   ft_program* out) {
+                   ft_program* out, bool bsdf = false, bool sample_randoms = false, const char* field = nullptr) {
     const size_t mark = code_.size();
     first_ = static_cast<uint32_t>(mark);
     nregs_ = 0;
@@ -318,14 +327,40 @@ class HookCompiler {
     block_ = &def;
     try {
       std::map<std::string, SVal> locals = block_scope(def, overrides);
-      static const char* const kFields[FT_MATERIAL_HOOK_PARAMS] = {
-          "position", "local_position", "normal", "view_dir", "front_face", "object_id", "material_id"};
+      static const char* const kFields[FT_BSDF_HOOK_PARAMS] = {
+          "position", "local_position", "normal", "view_dir", "front_face", "object_id", "material_id",
+          "wo", "wi", "current_ior", "u1", "u2", "u3"};
+      const int n_params = bsdf ? FT_BSDF_HOOK_PARAMS : FT_MATERIAL_HOOK_PARAMS;
       SVal ctx;
       ctx.is_const = false;
       ctx.rec = std::make_shared<std::map<std::string, SVal>>();
-      for (int k = 0; k < FT_MATERIAL_HOOK_PARAMS; ++k) (*ctx.rec)[kFields[k]] = reg(nregs_++, k < 4);
+      for (int k = 0; k < n_params; ++k) {
+        SVal r = reg(nregs_++, k < 4 || k == 7 || k == 8);
+        if (k < 10 || sample_randoms) (*ctx.rec)[kFields[k]] = r;
+      }
       locals[fn.params[0]] = ctx;
       SVal result = run_body(fn.body, locals, 0);
+      if (field) {
+        SVal picked;
+        if (result.rec) {
+          auto it = result.rec->find(field);
+          if (it == result.rec->end()) {
+            code_.resize(mark);
+            return false;
+          }
+          picked = it->second;
+        } else if (result.is_const && result.cv.kind == Value::Object) {
+          const Value* v = result.cv.obj->get(field);
+          if (!v) {
+            code_.resize(mark);
+            return false;
+          }
+          picked = cst(*v);
+        } else {
+          fail("sample does not return a record");
+        }
+        result = picked;
+      }
       if (result.rec) fail("returns the context");
       int r = materialize(result);
       bool rv = reg_vec3(result);
@@ -341,8 +376,8 @@ class HookCompiler {
       ft_program prog{};
       prog.first_instr = first_;
       prog.n_instr = static_cast<uint32_t>(code_.size()) - first_;
-      prog.n_params = FT_MATERIAL_HOOK_PARAMS;
-      prog.param_is_vec3 = 0xfu;
+      prog.n_params = static_cast<uint32_t>(n_params);
+      prog.param_is_vec3 = bsdf ? 0x18fu : 0xfu;
       prog.n_regs = static_cast<uint32_t>(nregs_);
       prog.result_is_vec3 = rv ? 1u : 0u;
       if (nregs_ > FT_MAX_PROGRAM_REGS) {
@@ -494,16 +529,28 @@ class HookCompiler {
         return cst(b->second.value);
       }
       case Expr::ObjectLiteral: {
-        std::map<std::string, Value> f;
+        // A literal whose fields all fold is a constant object; one with
+        // run-time fields is a record (a BsdfSample returned by a sample
+        // hook), whose fields are read by member access.
+        std::map<std::string, SVal> vals;
+        bool all_const = true;
         for (const auto& kv : e.fields) {
           SVal v = eval(*kv.second, locals, depth);
           if (!v.is_const) {
             if (e.text == "vec3") return vec3_literal(e, locals, depth);
-            fail("object literal with non-constant field");
+            all_const = false;
           }
-          f[kv.first] = v.cv;
+          vals[kv.first] = v;
         }
-        return cst(make_object(e.text, std::move(f)));
+        if (all_const) {
+          std::map<std::string, Value> f;
+          for (auto& kv : vals) f[kv.first] = kv.second.cv;
+          return cst(make_object(e.text, std::move(f)));
+        }
+        SVal r;
+        r.is_const = false;
+        r.rec = std::make_shared<std::map<std::string, SVal>>(std::move(vals));
+        return r;
       }
       case Expr::Member: {
         SVal base = eval(*e.lhs, locals, depth);
@@ -995,25 +1042,82 @@ class Lowerer {
     if (num("emission_strength", &v)) m.emission_strength = std::max(v, 0.0f);
     auto medium = props.find("medium");
     if (medium != props.end()) read_medium(&medium->second, &m);
-    // Per-hit hooks: colour, roughness, IOR and thin_walled
-    // (resolve_leaf_material, R:7164-7600); the other hookable properties are
-    // not lowered.  A Standard or Layered definition's IOR is the coat's
-    // whatever its hook returns, so that hook is left out.
+    // Per-hit hooks (resolve_leaf_material, R:7164-7530; build_bsdf_context
+    // R:4397-4449; the BSDF functions R:4905-4950).  A Standard or Layered
+    // definition's specular colour, IOR, clearcoat and clearcoat roughness are
+    // the coat's at every hit whatever their own hooks return, so those hooks
+    // are left out; metallic, specular, specular_weight, transmission and the
+    // coat hooks are read for those two models only.  `fn medium(ctx)` and
+    // `fn subsurface(ctx)` are not lowered.
     const bool coated = model == "Standard" || model == "Layered";
-    for (const BlockStmt& st : def.statements) {
-      if (st.kind != BlockStmt::Function || st.params.size() != 1) continue;
-      int want = st.name == "color" ? 2
-                 : (st.name == "roughness" || (st.name == "ior" && !coated) || st.name == "thin_walled") ? 0 : -1;
-      if (want < 0) continue;
+    struct Slot {
+      const char* name;
+      int slot;
+      int want;  // 0 number, 1 vec3, 2 either
+      bool coated_only;
+    };
+    static const Slot kSlots[] = {
+        {"emission_color", FT_HOOK_EMISSION_COLOR, 2, false},
+        {"emission_strength", FT_HOOK_EMISSION_STRENGTH, 0, false},
+        {"metallic", FT_HOOK_METALLIC, 0, true},
+        {"specular", FT_HOOK_SPECULAR, 0, true},
+        {"specular_weight", FT_HOOK_SPECULAR_WEIGHT, 0, true},
+        {"transmission", FT_HOOK_TRANSMISSION, 0, true},
+        {"coat_color", FT_HOOK_COAT_COLOR, 2, true},
+        {"coat_roughness", FT_HOOK_COAT_ROUGHNESS, 0, true},
+        {"coat_ior", FT_HOOK_COAT_IOR, 0, true},
+        {"coat_weight", FT_HOOK_COAT_WEIGHT, 0, true},
+        {"coat_mask", FT_HOOK_COAT_MASK, 0, true},
+        {"bump", FT_HOOK_BUMP, 0, false},
+        {"normal", FT_HOOK_NORMAL, 1, false},
+    };
+    // bsdf_sample_from_value (R:5032-5060): wi and f are required
+    static const Slot kSample[] = {
+        {"wi", FT_HOOK_SAMPLE_WI, 1, false},
+        {"f", FT_HOOK_SAMPLE_F, 2, false},
+        {"pdf", FT_HOOK_SAMPLE_PDF, 0, false},
+        {"delta", FT_HOOK_SAMPLE_DELTA, 0, false},
+        {"apply_cos", FT_HOOK_SAMPLE_APPLY_COS, 0, false},
+        {"transmission", FT_HOOK_SAMPLE_TRANSMISSION, 0, false},
+        {"thin_walled", FT_HOOK_SAMPLE_THIN_WALLED, 0, false},
+        {"next_ior", FT_HOOK_SAMPLE_NEXT_IOR, 0, false},
+    };
+    auto add = [&](const BlockStmt& st, int want, bool bsdf, bool randoms, const char* field) -> int32_t {
       HookCompiler hook(st_, out_.instrs);
       ft_program prog;
-      if (!hook.compile_ctx(st, def, overrides, want, &prog)) continue;
+      if (!hook.compile_ctx(st, def, overrides, want, &prog, bsdf, randoms, field)) return -1;
       out_.programs.push_back(prog);
-      int32_t idx = static_cast<int32_t>(out_.programs.size()) - 1;
-      if (st.name == "color") m.color_program = idx;
-      else if (st.name == "roughness") m.roughness_program = idx;
-      else if (st.name == "ior") m.ior_program = idx;
-      else m.thin_walled_program = idx;
+      return static_cast<int32_t>(out_.programs.size()) - 1;
+    };
+    for (const BlockStmt& st : def.statements) {
+      if (st.kind != BlockStmt::Function || st.params.size() != 1) continue;
+      if (st.name == "color") {
+        m.color_program = add(st, 2, false, false, nullptr);
+      } else if (st.name == "roughness") {
+        m.roughness_program = add(st, 0, false, false, nullptr);
+      } else if (st.name == "ior") {
+        if (!coated) m.ior_program = add(st, 0, false, false, nullptr);
+      } else if (st.name == "thin_walled") {
+        m.thin_walled_program = add(st, 0, false, false, nullptr);
+      } else if (st.name == "eval") {
+        m.hook_program[FT_HOOK_EVAL] = add(st, 2, true, false, nullptr);
+      } else if (st.name == "pdf") {
+        m.hook_program[FT_HOOK_PDF] = add(st, 0, true, false, nullptr);
+      } else if (st.name == "sample") {
+        int32_t progs[8];
+        bool ok = true;
+        for (int k = 0; k < 8; ++k) {
+          progs[k] = add(st, kSample[k].want, true, true, kSample[k].name);
+          if (k == 1 && progs[k] < 0) progs[k] = add(st, kSample[k].want, true, true, "color");
+          if (k < 2 && progs[k] < 0) ok = false;
+        }
+        if (ok)
+          for (int k = 0; k < 8; ++k) m.hook_program[kSample[k].slot] = progs[k];
+      } else {
+        for (const Slot& sl : kSlots)
+          if (st.name == sl.name && (coated || !sl.coated_only))
+            m.hook_program[sl.slot] = add(st, sl.want, false, false, nullptr);
+      }
     }
     if (model == "Standard" || model == "Layered") {
       // resolve_leaf_material (R:7258-7470) then sets the coat at every hit:

@@ -74,6 +74,8 @@ struct DevScene {
   const float* __restrict__ ur_cell_gaps;   // per cell entry: box gap lower bound (ascending per cell)
   const int32_t* __restrict__ ur_inner_up;  // parent link (parent << 1 | side), -1 at the root
   const int32_t* __restrict__ ur_prim_up;   // per primitive position: parent link
+  const int32_t* __restrict__ obj_node;     // per object id: the node carrying its transform, -1 none
+  int32_t n_obj_node;
   int32_t n_materials, n_lights, env_program;
   int32_t bvh_root;
   float smin[3], smax[3];
@@ -1193,7 +1195,7 @@ __global__ void depth_rgb8_kernel(const float* __restrict__ t, const uint8_t* __
 struct TraceHit {
   float t;
   F3 pos, normal;
-  uint32_t mat;
+  uint32_t mat, obj;  // the hit's material and object ids (RayHit, R:440-452)
   int leaf;
 };
 
@@ -1227,22 +1229,37 @@ __device__ __forceinline__ void shade_hit(const DevScene& S, const RayParams& P,
   resolve_hit(S, h.leaf, h.pos, hc, &rs, cx);
   F3 shading_n = normal;
   if (rs.ok) shading_n = ftd::normalize3(front ? rs.normal : rs.normal * -1.0f);
-  DMat mats[2];
+  // build_bsdf_context (R:4397-4449): the shading normal through the hit
+  // material's bump and normal hooks, and the context of the BSDF hooks
+  BsdfCtx bc;
+  bc.pos = h.pos;
+  bc.local = object_local(S, h.obj, h.pos);
+  bc.normal = shading_n;
+  bc.wo = ftd::normalize3(J.d * -1.0f);
+  bc.front = front ? 1.0f : 0.0f;
+  bc.obj = static_cast<float>(h.obj);
+  bc.mat = static_cast<float>(h.mat);
+  bc.current_ior = J.med.ior;
+  shading_n = hooked_shading_normal(S, bc, J.d * -1.0f, h.mat);
+  bc.normal = shading_n;
+  // The hit's materials are read where resolve_hit left them (no copies).
+  const DMat* mats[2];
   float ws[2];
   int nm = 0;
   if (rs.ok && rs.split) {
     float tt = clamp01(rs.t);  // lerp_spectrum(a, b, t): a (1 - t) + b t
-    if (tt != 1.0f) { mats[nm] = rs.m; ws[nm++] = 1.0f - tt; }
-    if (tt != 0.0f) { mats[nm] = rs.mb; ws[nm++] = tt; }
+    if (tt != 1.0f) { mats[nm] = &rs.m; ws[nm++] = 1.0f - tt; }
+    if (tt != 0.0f) { mats[nm] = &rs.mb; ws[nm++] = tt; }
   } else {
-    mats[0] = rs.ok ? rs.m : mat_of_id(S, h.mat);
+    if (!rs.ok) rs.m = mat_of_id(S, h.mat);
+    mats[0] = &rs.m;
     ws[0] = 1.0f;
     nm = 1;
   }
   F3 att = transmittance(J.med, h.t);
   F3 wo = ftd::normalize3(J.d * -1.0f);
   for (int mi = 0; mi < nm; ++mi) {
-    const DMat& mat = mats[mi];
+    const DMat& mat = *mats[mi];
     F3 W = mul3(J.w * ws[mi], att);
     const DParams& Pm = dom_params(mat);
     float rough = clamp01(Pm.roughness);
@@ -1306,7 +1323,7 @@ __device__ __forceinline__ void shade_hit(const DevScene& S, const RayParams& P,
           F3 so = offset_origin(h.pos, normal, wi, eps);
           float max_t = isfinite(dist) ? fmaxf(dist - eps * 8.0f, 0.0f) : P.max_dist;
           if (max_t <= 0.0f) continue;
-          F3 f = mat_eval(mat, shading_n, wi, wo);
+          F3 f = bsdf_eval(S, mat, bc, wi);
           sink.light(mul3(W, mul3(f, rad) * (ndotl * inv * local_w)), so, wi, max_t);
         }
       }

@@ -53,6 +53,7 @@ __device__ bool march_hit(const DevScene& S, const RayParams& P, F3 o, F3 d, flo
       h->t = hi;
       h->pos = pos;
       h->mat = fin.mat;
+      h->obj = fin.obj;
       return true;
     }
     prev = traveled;
@@ -241,12 +242,46 @@ __device__ __forceinline__ float power_heuristic(float pa, float pb) {  // R:509
   return a2 / fmaxf(a2 + b2, 1.0e-6f);
 }
 
-// BsdfContextBase (R:4397-4449) without the bump / normal hooks
+// BsdfContextBase (R:4397-4449): the BSDF context with its shading normal
+// and wo, and the geometric normal of the hit facing the ray
 struct PathCtxD {
   F3 normal, wo, hit_normal;
   bool front;
   float current_ior;
+  BsdfCtx b;
 };
+
+// pdf_bsdf (R:4922-4933): the material definition's `fn pdf(ctx)` (at least
+// 0), else Material::pdf.
+__device__ float bsdf_pdf(const DevScene& S, const DMat& m, const PathCtxD& c, F3 wi) {
+  const int prog = bsdf_hook(S, m, FT_HOOK_PDF);
+  if (prog < 0) return mat_pdf(m, c.normal, wi, c.wo);
+  F3 a[FT_BSDF_HOOK_PARAMS];
+  bsdf_args(c.b, wi, 0.0f, 0.0f, 0.0f, a);
+  return fmaxf(scene_program(S, prog, a, nullptr).x, 0.0f);
+}
+
+// sample_bsdf_lobe (R:4869-4903): the material definition's `fn sample(ctx)`
+// (sample_bsdf_ft R:4934-4950, its context's wi the normal), read as
+// bsdf_sample_from_value (R:5032-5060) does, else Material::sample.
+__device__ BsdfSampleD bsdf_sample(const DevScene& S, const DMat& m, const PathCtxD& c, const SampleInD& in) {
+  const int dyn = dom_params(m).dyn;
+  const int32_t* hp = dyn >= 0 ? S.materials[dyn].hook_program : nullptr;
+  if (!hp || hp[FT_HOOK_SAMPLE_WI] < 0 || hp[FT_HOOK_SAMPLE_F] < 0) return mat_sample(m, c.normal, c.wo, in);
+  F3 a[FT_BSDF_HOOK_PARAMS];
+  bsdf_args(c.b, c.b.normal, in.u1, in.u2, in.u3, a);
+  auto num = [&](int slot, float dflt) { return hp[slot] >= 0 ? scene_program(S, hp[slot], a, nullptr).x : dflt; };
+  BsdfSampleD r;
+  r.wi = scene_program(S, hp[FT_HOOK_SAMPLE_WI], a, nullptr);
+  r.f = hook_colour(S, hp[FT_HOOK_SAMPLE_F], a);
+  r.pdf = fmaxf(num(FT_HOOK_SAMPLE_PDF, 0.0f), 0.0f);
+  r.delta = num(FT_HOOK_SAMPLE_DELTA, 0.0f) >= 0.5f;
+  r.apply_cos = num(FT_HOOK_SAMPLE_APPLY_COS, 1.0f) >= 0.5f;
+  r.transmission = num(FT_HOOK_SAMPLE_TRANSMISSION, 0.0f) >= 0.5f;
+  r.thin_walled = num(FT_HOOK_SAMPLE_THIN_WALLED, 0.0f) >= 0.5f;
+  r.next_ior = ftd::rclamp(num(FT_HOOK_SAMPLE_NEXT_IOR, 1.0f), 1.0f, 3.0f);
+  return r;
+}
 
 // env_light_pdf_for_dir (R:4336-4355)
 __device__ float env_light_pdf(const DevScene& S, const DMat& m, const PathCtxD& c, F3 wi) {
@@ -254,7 +289,7 @@ __device__ float env_light_pdf(const DevScene& S, const DMat& m, const PathCtxD&
   float env = 0.0f;
   for (int i = 0; i < S.n_lights; ++i) env += S.lights[i].kind == FT_LIGHT_ENV ? 1.0f : 0.0f;
   if (env <= 0.0f) return 0.0f;
-  return (env / static_cast<float>(S.n_lights)) * fmaxf(mat_pdf(m, c.normal, wi, c.wo), 1.0e-6f);
+  return (env / static_cast<float>(S.n_lights)) * fmaxf(bsdf_pdf(S, m, c, wi), 1.0e-6f);
 }
 
 // estimate_direct_mis with sample_one_light (R:4572-4675): one light chosen
@@ -296,9 +331,9 @@ __device__ F3 estimate_direct_mis(const DevScene& S, const RayParams& P, const D
   const F3 so = offset_origin(p, c.hit_normal, wi, P.eps);
   const float vis = shadow_visibility(S, so, wi, max_t, P.eps, cx);
   if (vis <= 0.0f) return f3(0.0f, 0.0f, 0.0f);
-  const F3 f = mat_eval(m, c.normal, wi, c.wo);
-  const float bsdf_pdf = fmaxf(mat_pdf(m, c.normal, wi, c.wo), 1.0e-6f);
-  const float w = delta ? 1.0f : power_heuristic(pdf, bsdf_pdf);
+  const F3 f = bsdf_eval(S, m, c.b, wi);
+  const float bpdf = fmaxf(bsdf_pdf(S, m, c, wi), 1.0e-6f);
+  const float w = delta ? 1.0f : power_heuristic(pdf, bpdf);
   return mul3(f, rad) * ((cos_t * vis * w) / fmaxf(pdf, 1.0e-6f));
 }
 
@@ -335,6 +370,16 @@ __device__ F3 trace_path(const DevScene& S, const RayParams& P, F3 origin, F3 di
     Resolved rs;
     resolve_hit(S, h.leaf, h.pos, hc, &rs, cx, false);
     c.normal = rs.ok ? ftd::normalize3(front ? rs.normal : rs.normal * -1.0f) : c.hit_normal;
+    c.b.pos = h.pos;
+    c.b.local = object_local(S, h.obj, h.pos);
+    c.b.normal = c.normal;
+    c.b.wo = c.wo;
+    c.b.front = front ? 1.0f : 0.0f;
+    c.b.obj = static_cast<float>(h.obj);
+    c.b.mat = static_cast<float>(h.mat);
+    c.b.current_ior = c.current_ior;
+    c.normal = hooked_shading_normal(S, c.b, dir * -1.0f, h.mat);
+    c.b.normal = c.normal;
     const DMat m = rs.ok ? rs.m : mat_of_id(S, h.mat);
     const F3 em = mat_emission(m);
     if (em.x > 0.0f || em.y > 0.0f || em.z > 0.0f) radiance = radiance + mul3(throughput, em);
@@ -347,7 +392,7 @@ __device__ F3 trace_path(const DevScene& S, const RayParams& P, F3 origin, F3 di
     in.u1 = rng.next_f32();
     in.u2 = rng.next_f32();
     in.u3 = rng.next_f32();
-    const BsdfSampleD smp = mat_sample(m, c.normal, c.wo, in);
+    const BsdfSampleD smp = bsdf_sample(S, m, c, in);
     if (smp.pdf <= 1.0e-6f) break;
     if (smp.apply_cos) {
       const float ct = fmaxf(ftd::dot3(c.normal, smp.wi), 0.0f);

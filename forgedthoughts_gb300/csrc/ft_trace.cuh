@@ -32,6 +32,9 @@ struct DParams {  // MaterialParams (materials/mod.rs:66-86)
   int has_medium;
   float medium_ior, medium_density;
   F3 medium_absorption;
+  // dynamic_material_id (R:6669): the ft_material whose BSDF hooks apply to
+  // these parameters, -1 for none (a blend of two parameter sets keeps none)
+  int dyn;
 };
 
 struct DMat {  // Material incl. Blend (materials/mod.rs:214-230)
@@ -69,17 +72,20 @@ __device__ DParams params_of(const ft_material& m) {
   p.medium_ior = m.medium_ior;
   p.medium_density = m.medium_density;
   p.medium_absorption = f3(m.medium_absorption[0], m.medium_absorption[1], m.medium_absorption[2]);
+  p.dyn = -1;
   return p;
 }
 
 // material_for_id (R:6895-6900)
 __device__ DMat mat_of_id(const DevScene& S, uint32_t id) {
-  const ft_material& fm = S.materials[id < static_cast<uint32_t>(S.n_materials) ? id : 0u];
+  const uint32_t k = id < static_cast<uint32_t>(S.n_materials) ? id : 0u;
+  const ft_material& fm = S.materials[k];
   DMat m;
   m.kind = fm.kind;
   m.a_model = m.b_model = fm.kind;
   m.t = 0.0f;
   m.a = params_of(fm);
+  m.a.dyn = static_cast<int>(k);
   m.b = m.a;
   return m;
 }
@@ -97,22 +103,54 @@ struct HookCtx {
 // in the primitive's frame.  Roughness is clamped to [0, 1] and the IOR to
 // [1, 3]; a Metal takes neither IOR nor thin_walled.  A numeric colour is
 // grey (spectrum_from_value, R:7924-7935).
+//
+// The further property hooks (ft_material_hook): the emission of every
+// definition, and for Standard / Layered definitions metallic, specular,
+// specular_weight, transmission and the coat, whose colour, roughness and IOR
+// replace the specular colour, clearcoat roughness and IOR, and whose weight
+// times mask the clearcoat (R:7258-7470).  The lowering compiles the latter
+// only for those two models.
+__device__ __forceinline__ bool has_leaf_hooks(const ft_material& fm) {
+  if (fm.color_program >= 0 || fm.roughness_program >= 0 || fm.ior_program >= 0 || fm.thin_walled_program >= 0)
+    return true;
+  for (int k = FT_HOOK_EMISSION_COLOR; k <= FT_HOOK_COAT_MASK; ++k)
+    if (fm.hook_program[k] >= 0) return true;
+  return false;
+}
+__device__ __forceinline__ F3 hook_colour(const DevScene& S, int prog, const F3* args) {
+  const F3 c = scene_program(S, prog, args, nullptr);
+  return S.programs[prog].result_is_vec3 ? c : f3(c.x, c.x, c.x);
+}
 __device__ DMat mat_of_leaf(const DevScene& S, const DevNode& pn, const HookCtx& hc) {
   DMat m = mat_of_id(S, pn.material_id);
   const ft_material& fm = S.materials[pn.material_id < static_cast<uint32_t>(S.n_materials) ? pn.material_id : 0u];
-  if (fm.color_program < 0 && fm.roughness_program < 0 && fm.ior_program < 0 && fm.thin_walled_program < 0) return m;
+  if (!has_leaf_hooks(fm)) return m;
   const float obj = static_cast<float>(pn.object_id), mat = static_cast<float>(pn.material_id);
   F3 args[FT_MATERIAL_HOOK_PARAMS] = {hc.pos, ftd::to_local(hc.pos, pn), hc.normal, hc.view_dir,
                                       f3(hc.front_face, hc.front_face, hc.front_face), f3(obj, obj, obj),
                                       f3(mat, mat, mat)};
-  if (fm.color_program >= 0) {
-    F3 c = scene_program(S, fm.color_program, args, nullptr);
-    m.a.color = S.programs[fm.color_program].result_is_vec3 ? c : f3(c.x, c.x, c.x);
-  }
+  if (fm.color_program >= 0) m.a.color = hook_colour(S, fm.color_program, args);
   if (fm.roughness_program >= 0) m.a.roughness = clamp01(scene_program(S, fm.roughness_program, args, nullptr).x);
   if (fm.kind != FT_MAT_METAL) {
     if (fm.ior_program >= 0) m.a.ior = ftd::rclamp(scene_program(S, fm.ior_program, args, nullptr).x, 1.0f, 3.0f);
     if (fm.thin_walled_program >= 0) m.a.thin = scene_program(S, fm.thin_walled_program, args, nullptr).x >= 0.5f;
+  }
+  const int32_t* hp = fm.hook_program;
+  auto num = [&](int slot) { return scene_program(S, hp[slot], args, nullptr).x; };
+  if (hp[FT_HOOK_EMISSION_COLOR] >= 0) m.a.emission_color = hook_colour(S, hp[FT_HOOK_EMISSION_COLOR], args);
+  if (hp[FT_HOOK_EMISSION_STRENGTH] >= 0) m.a.emission_strength = fmaxf(num(FT_HOOK_EMISSION_STRENGTH), 0.0f);
+  if (hp[FT_HOOK_METALLIC] >= 0) m.a.metallic = clamp01(num(FT_HOOK_METALLIC));
+  if (hp[FT_HOOK_SPECULAR] >= 0) m.a.specular = clamp01(num(FT_HOOK_SPECULAR));
+  if (hp[FT_HOOK_SPECULAR_WEIGHT] >= 0) m.a.specular_weight = clamp01(num(FT_HOOK_SPECULAR_WEIGHT));
+  if (hp[FT_HOOK_TRANSMISSION] >= 0) m.a.transmission = clamp01(num(FT_HOOK_TRANSMISSION));
+  if (hp[FT_HOOK_COAT_COLOR] >= 0) m.a.spec_color = hook_colour(S, hp[FT_HOOK_COAT_COLOR], args);
+  if (hp[FT_HOOK_COAT_ROUGHNESS] >= 0) m.a.clearcoat_roughness = clamp01(num(FT_HOOK_COAT_ROUGHNESS));
+  if (hp[FT_HOOK_COAT_IOR] >= 0) m.a.ior = ftd::rclamp(num(FT_HOOK_COAT_IOR), 1.0f, 3.0f);
+  if (hp[FT_HOOK_COAT_WEIGHT] >= 0 || hp[FT_HOOK_COAT_MASK] >= 0) {
+    // the static clearcoat is the clamped static coat_weight
+    const float w = hp[FT_HOOK_COAT_WEIGHT] >= 0 ? clamp01(num(FT_HOOK_COAT_WEIGHT)) : m.a.clearcoat;
+    const float k = hp[FT_HOOK_COAT_MASK] >= 0 ? clamp01(num(FT_HOOK_COAT_MASK)) : 1.0f;
+    m.a.clearcoat = clamp01(w * k);
   }
   m.b = m.a;
   return m;
@@ -156,6 +194,7 @@ __device__ DParams blend_params(DParams a, const DParams& b, float t) {
     a.medium_absorption = b.medium_absorption;
     a.medium_density = b.medium_density;
   }
+  a.dyn = -1;  // dynamic_material_id = None (R:7624)
   return a;
 }
 
@@ -265,6 +304,103 @@ __device__ F3 model_eval(int model, const DParams& p, F3 n, F3 wi, F3 wo) {
 __device__ F3 mat_eval(const DMat& m, F3 n, F3 wi, F3 wo) {
   if (m.kind != kBlendKind) return model_eval(m.kind, m.a, n, wi, wo);
   return lerp_sp(model_eval(m.a_model, m.a, n, wi, wo), model_eval(m.b_model, m.b, n, wi, wo), m.t);
+}
+
+// The BSDF context of a hit (BsdfContextBase, build_bsdf_context
+// R:4397-4449): position, local position in the hit object's frame, the
+// shading normal (after the bump and normal hooks), wo, front face, the hit's
+// object and material ids and the current medium's IOR.
+struct BsdfCtx {
+  F3 pos, local, normal, wo;
+  float front, obj, mat, current_ior;
+};
+
+// Arguments of a BSDF hook program (bsdf_context_value, R:5006-5030).
+__device__ __forceinline__ void bsdf_args(const BsdfCtx& c, F3 wi, float u1, float u2, float u3, F3* a) {
+  a[0] = c.pos;
+  a[1] = c.local;
+  a[2] = c.normal;
+  a[3] = c.wo;  // view_dir of the context is wo
+  a[4] = f3(c.front, c.front, c.front);
+  a[5] = f3(c.obj, c.obj, c.obj);
+  a[6] = f3(c.mat, c.mat, c.mat);
+  a[7] = c.wo;
+  a[8] = wi;
+  a[9] = f3(c.current_ior, c.current_ior, c.current_ior);
+  a[10] = f3(u1, u1, u1);
+  a[11] = f3(u2, u2, u2);
+  a[12] = f3(u3, u3, u3);
+}
+
+// The BSDF hook `slot` of the shaded material's dominant parameters, -1 if
+// none (dynamic_material_name, R:4996-5002).
+__device__ __forceinline__ int bsdf_hook(const DevScene& S, const DMat& m, int slot) {
+  const int dyn = dom_params(m).dyn;
+  return dyn >= 0 ? S.materials[dyn].hook_program[slot] : -1;
+}
+
+// eval_bsdf (R:4905-4920): the material definition's `fn eval(ctx)`, else
+// Material::eval with the context's normal and wo.
+__device__ F3 bsdf_eval(const DevScene& S, const DMat& m, const BsdfCtx& c, F3 wi) {
+  const int prog = bsdf_hook(S, m, FT_HOOK_EVAL);
+  if (prog < 0) return mat_eval(m, c.normal, wi, c.wo);
+  F3 a[FT_BSDF_HOOK_PARAMS];
+  bsdf_args(c, wi, 0.0f, 0.0f, 0.0f, a);
+  return hook_colour(S, prog, a);
+}
+
+// orthonormal_tangent (R:7820-7827)
+__device__ __forceinline__ F3 orthonormal_tangent(F3 n) {
+  const F3 up = fabsf(n.y) < 0.999f ? f3(0.0f, 1.0f, 0.0f) : f3(1.0f, 0.0f, 0.0f);
+  return ftd::normalize3(ftd::cross3(n, up));
+}
+
+// The shading normal of build_bsdf_context (R:4418-4439): the geometric
+// normal through the hit material's `fn bump(ctx)` (resolve_dynamic_bump,
+// R:7776-7818: a height field differentiated by forward differences of 0.01
+// along a tangent frame) and then its `fn normal(ctx)` (resolve_dynamic_normal,
+// R:7749-7774), each normalised, turned to the side of its input and dropped
+// when degenerate.  c.normal holds the geometric normal on entry; the hook
+// context is the hit's shading context with that normal and view_dir.
+__device__ F3 hooked_shading_normal(const DevScene& S, const BsdfCtx& c, F3 view_dir, uint32_t hit_mat) {
+  const ft_material& fm = S.materials[hit_mat < static_cast<uint32_t>(S.n_materials) ? hit_mat : 0u];
+  F3 n = c.normal;
+  const int bump = fm.hook_program[FT_HOOK_BUMP], nrm = fm.hook_program[FT_HOOK_NORMAL];
+  if (bump < 0 && nrm < 0) return n;
+  F3 a[FT_MATERIAL_HOOK_PARAMS] = {c.pos, c.local, n, view_dir, f3(c.front, c.front, c.front),
+                                   f3(c.obj, c.obj, c.obj), f3(c.mat, c.mat, c.mat)};
+  if (bump >= 0) {
+    const float eps = 0.01f;
+    const float center = scene_program(S, bump, a, nullptr).x;
+    const F3 tangent = orthonormal_tangent(n);
+    const F3 bitangent = ftd::normalize3(ftd::cross3(n, tangent));
+    a[1] = c.local + tangent * eps;
+    const float dx = scene_program(S, bump, a, nullptr).x - center;
+    a[1] = c.local + bitangent * eps;
+    const float dy = scene_program(S, bump, a, nullptr).x - center;
+    a[1] = c.local;
+    F3 b = ftd::normalize3((n - tangent * (dx / eps)) - bitangent * (dy / eps));
+    if (ftd::len3(b) > 1.0e-6f) {
+      if (ftd::dot3(b, n) < 0.0f) b = b * -1.0f;
+      n = b;
+    }
+    a[2] = n;
+  }
+  if (nrm >= 0) {
+    F3 b = ftd::normalize3(scene_program(S, nrm, a, nullptr));
+    if (ftd::len3(b) > 1.0e-6f) {
+      if (ftd::dot3(b, n) < 0.0f) b = b * -1.0f;
+      n = b;
+    }
+  }
+  return n;
+}
+
+// The hit's position in its object's frame (object_transforms, identity for
+// an object without one).
+__device__ __forceinline__ F3 object_local(const DevScene& S, uint32_t obj, F3 p) {
+  const int ni = obj < static_cast<uint32_t>(S.n_obj_node) ? S.obj_node[obj] : -1;
+  return ni >= 0 ? ftd::to_local(p, S.nodes[ni]) : p;
 }
 
 // smoothstepf (R:7538-7541) of the blend weight (R:4540-4545, R:7105-7110)
@@ -538,6 +674,12 @@ struct NEntry {
 // weight t; a child with weight exactly 0 is skipped.  A child without
 // gathered primitives is provably weightless when reach >= (other value) + r;
 // otherwise *need receives the reach required.
+//
+// The result of the child completed last travels up in `carry` (registers).
+// Only a node that uses both children keeps its left child's result while the
+// right subtree resolves, on the `pend` stack; the chain of single-child
+// nodes between the root and the hit's primitives (most of the walk) touches
+// no per-thread memory beyond the frames' few scalars.
 __device__ __noinline__ bool resolve_urtree_reach(const DevScene& S, const DevUrTree& t, F3 p, const HookCtx& hc,
                                                   float reach, Resolved* out, float* need, bool split_root) {
   int gpos[kGather];
@@ -547,15 +689,14 @@ __device__ __noinline__ bool resolve_urtree_reach(const DevScene& S, const DevUr
     *need = -1.0f;
     return false;
   }
-  // A frame holds its left child's result while the right subtree is
-  // resolved; a completed right child is combined at once from `carry`.
   struct Frame {
     int inner, stage;
     float tw;
     bool useL, useR;
-    NEntry left;
   };
   Frame fr[20];
+  NEntry pend[20];  // left results of two-child nodes whose right subtree is open
+  int np = 0;
   NEntry carry;
   int fp = 0;
   const float r = t.r;
@@ -586,6 +727,7 @@ __device__ __noinline__ bool resolve_urtree_reach(const DevScene& S, const DevUr
   if (!open(0, t.inner_root)) return false;
   for (int walk = 0; walk < ftgpu::kMaxWalk; ++walk) {  // each inner node is opened once
     Frame& F = fr[fp];
+    bool child_done = false;  // carry holds the result of fr[fp]'s child (stage - 1)
     if (F.stage < 2) {
       bool use = F.stage == 0 ? F.useL : F.useR;
       int c = S.ur_inner[F.inner].child[F.stage];
@@ -595,53 +737,61 @@ __device__ __noinline__ bool resolve_urtree_reach(const DevScene& S, const DevUr
       }
       if (c < 0) {
         const DevNode& pn = S.nodes[S.ur_prims[t.prim_first + (-c - 1)]];
-        NEntry& e = F.stage == 0 ? F.left : carry;
-        e.n = prim_normal(pn, p);
-        e.m = mat_of_leaf(S, pn, hc);
+        carry.n = prim_normal(pn, p);
+        carry.m = mat_of_leaf(S, pn, hc);
         ++F.stage;
+        child_done = true;
+      } else {
+        if (fp + 1 >= 20) {
+          *need = -1.0f;
+          return false;
+        }
+        ++F.stage;
+        ++fp;
+        if (!open(fp, c)) return false;
         continue;
       }
-      if (fp + 1 >= 20) {
-        *need = -1.0f;
-        return false;
-      }
-      ++F.stage;
-      ++fp;
-      if (!open(fp, c)) return false;
-      continue;
-    }
-    // both children done: the left result in F.left, the right one in carry
-    if (fp == 0 && split_root) {
-      out->normal = F.useL && F.useR ? blend_normals(F.left.n, carry.n, F.tw, false)
-                                     : blend_normals(F.useL ? F.left.n : carry.n, F.useL ? F.left.n : carry.n,
-                                                     F.tw, false);
-      out->t = F.tw;
-      out->split = true;
-      out->m = F.useL ? F.left.m : carry.m;
-      out->mb = F.useR ? carry.m : F.left.m;
-      out->ok = true;
-      return true;
-    }
-    NEntry res;
-    bool mixes = S.ur_inner_blend[F.inner] != 0;
-    if (F.useL && F.useR) {
-      res.n = blend_normals(F.left.n, carry.n, F.tw, false);
-      res.m = blend_materials(F.left.m, carry.m, F.tw);
     } else {
-      const NEntry& e = F.useL ? F.left : carry;
-      res.n = blend_normals(e.n, e.n, F.tw, false);
-      res.m = blend_with_far(e.m, F.useL, mixes);
+      // both children done: a two-child node's left result is on pend, the
+      // right one (or a single child's) in carry
+      const bool both = F.useL && F.useR;
+      if (fp == 0 && split_root) {
+        if (both) {
+          const NEntry& L = pend[--np];
+          out->normal = blend_normals(L.n, carry.n, F.tw, false);
+          out->m = L.m;
+          out->mb = carry.m;
+        } else {
+          out->normal = blend_normals(carry.n, carry.n, F.tw, false);
+          out->m = carry.m;
+          out->mb = carry.m;
+        }
+        out->t = F.tw;
+        out->split = true;
+        out->ok = true;
+        return true;
+      }
+      if (both) {
+        const NEntry& L = pend[--np];
+        carry.n = blend_normals(L.n, carry.n, F.tw, false);
+        carry.m = blend_materials(L.m, carry.m, F.tw);
+      } else {
+        carry.n = blend_normals(carry.n, carry.n, F.tw, false);
+        carry.m = blend_with_far(carry.m, F.useL, S.ur_inner_blend[F.inner] != 0);
+      }
+      if (fp == 0) {  // the root's blended material (resolve_material_at_hit)
+        out->normal = carry.n;
+        out->m = carry.m;
+        out->split = false;
+        out->ok = true;
+        return true;
+      }
+      --fp;
+      child_done = true;
     }
-    if (fp == 0) {  // the root's blended material (resolve_material_at_hit)
-      out->normal = res.n;
-      out->m = res.m;
-      out->split = false;
-      out->ok = true;
-      return true;
-    }
-    --fp;
-    if (fr[fp].stage == 1) fr[fp].left = res;  // a left child completed
-    else carry = res;
+    // A left child completed under a node that also uses its right child:
+    // keep its result until the right subtree is done.
+    if (child_done && fr[fp].stage == 1 && fr[fp].useR) pend[np++] = carry;
   }
   *need = -1.0f;  // only a corrupted tree gets here
   return false;
@@ -688,6 +838,22 @@ __device__ void resolve_hit(const DevScene& S, int li, F3 p, const HookCtx& hc, 
 // the nearest leaf box.
 template <bool kStats>
 __device__ float scene_lower_bound(const DevScene& S, F3 p, Ctx<kStats>& cx) {
+  // One- and two-leaf BVHs (a single object, or a ground plus one composite
+  // object) without a stack: the walk below returns the root leaf's box
+  // bound, or the smaller of two leaf children's.
+  const DevBvhNode& root = S.bvh[S.bvh_root];
+  if (root.leaf >= 0) {
+    cx.box();
+    return node_lb(p, root.bmin, root.bmax);
+  }
+  {
+    const DevBvhNode& L = S.bvh[root.lhs];
+    const DevBvhNode& R = S.bvh[root.rhs];
+    if (L.leaf >= 0 && R.leaf >= 0) {
+      cx.box(3);
+      return fminf(node_lb(p, L.bmin, L.bmax), node_lb(p, R.bmin, R.bmax));
+    }
+  }
   float best = kInf;
   cx.box();
   int stack[64];

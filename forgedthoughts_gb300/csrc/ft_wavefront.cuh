@@ -33,7 +33,7 @@ struct WJob {
 
 struct WHit {
   float t, pos[3], normal[3];
-  uint32_t mat;
+  uint32_t mat, obj;
   int32_t leaf;  // -1: missed (environment added), -2: no job
 };
 
@@ -136,6 +136,7 @@ __device__ __forceinline__ void wf_shade_job(const DevScene& S, const RayParams&
   h.pos = f3(wh.pos[0], wh.pos[1], wh.pos[2]);
   h.normal = f3(wh.normal[0], wh.normal[1], wh.normal[2]);
   h.mat = wh.mat;
+  h.obj = wh.obj;
   h.leaf = wh.leaf;
   RayJob J = job_of(wj);
   QueueSink sink{Q, wj.sample};
@@ -214,6 +215,16 @@ constexpr unsigned kWfRefill = 8;
 
 enum WfPhase : int { kWfMarch = 0, kWfRefine = 1, kWfNormal = 2, kWfFinal = 3 };
 
+// A missed ray adds the environment seen through its medium.  Out of line:
+// the environment program's interpreter would otherwise be inlined at every
+// miss site of the march loop, whose body has to stay within the
+// instruction cache; a ray misses once, after all its steps.
+__device__ __noinline__ void wf_add_miss(const DevScene& S, const RayParams& P, const WJob& wj,
+                                         float* __restrict__ radiance) {
+  RayJob J = job_of(wj);
+  add_radiance(radiance, wj.sample, mul3(J.w, mul3(environment(S, J.d), transmittance(J.med, P.max_dist))));
+}
+
 // raymarch_hit (R:4091-4139) of every queued ray: march from the ray's
 // secondary_min_t (R:4175-4178), ten bisections, the six-tap normal and the
 // hit leaf's lookup (march_hit, one evaluation per iteration); a miss adds
@@ -242,9 +253,7 @@ __global__ void __launch_bounds__(128, 5) wf_march_persistent(DevScene S0, RayPa
   F3 o = f3(0.0f, 0.0f, 0.0f), d = o, pos = o;
   float traveled = 0.0f, prev = 0.0f, max_t = 0.0f, lo = 0.0f, hi = 0.0f, nx = 0.0f, ny = 0.0f, nz = 0.0f;
   auto miss = [&](const DevScene& S, const RayParams& P) {
-    const WJob& wj = jobs[job];
-    RayJob J = job_of(wj);
-    add_radiance(radiance, wj.sample, mul3(J.w, mul3(environment(S, J.d), transmittance(J.med, P.max_dist))));
+    wf_add_miss(S, P, jobs[job], radiance);
     hits[job].leaf = -1;
     live = false;
   };
@@ -320,6 +329,7 @@ __global__ void __launch_bounds__(128, 5) wf_march_persistent(DevScene S0, RayPa
       h.pos[0] = pos.x; h.pos[1] = pos.y; h.pos[2] = pos.z;
       h.normal[0] = nr.x; h.normal[1] = nr.y; h.normal[2] = nr.z;
       h.mat = fin.mat;
+      h.obj = fin.obj;
       hits[job] = h;
       live = false;
       continue;
@@ -466,6 +476,7 @@ __global__ void __launch_bounds__(128) wf_hits_from_depth_kernel(DevScene S, Ray
     h.pos[0] = pos.x; h.pos[1] = pos.y; h.pos[2] = pos.z;
     h.normal[0] = normal_in[3 * s]; h.normal[1] = normal_in[3 * s + 1]; h.normal[2] = normal_in[3 * s + 2];
     h.mat = fin.mat;
+    h.obj = fin.obj;
     hits[i] = h;
   }
 }

@@ -70,6 +70,14 @@ class Builder {
         std::memcpy(img_->nodes[i].bmax, bounds_[i].mx, sizeof(float) * 3);
       }
     }
+    // Object id -> the node carrying its transform (the shading context's
+    // local position of a hit, build_bsdf_context R:4403-4408).
+    for (uint32_t i = 0; i < d_.n_nodes; ++i) {
+      const ft_node& n = d_.nodes[i];
+      if (!(is_prim(n.kind) || n.kind == FT_NODE_CUSTOM) || n.object_id >= (1u << 20)) continue;
+      if (img_->obj_node.size() <= n.object_id) img_->obj_node.resize(n.object_id + 1, -1);
+      if (img_->obj_node[n.object_id] < 0) img_->obj_node[n.object_id] = static_cast<int32_t>(i);
+    }
     const Box& sb = bounds_[d_.root];
     std::memcpy(img_->scene_min, sb.mn, sizeof(sb.mn));
     std::memcpy(img_->scene_max, sb.mx, sizeof(sb.mx));
@@ -86,6 +94,7 @@ class Builder {
       std::memset(&m, 0, sizeof(m));
       m.kind = FT_MAT_STANDARD;
       m.color_program = m.roughness_program = m.ior_program = m.thin_walled_program = -1;
+      for (int32_t& h : m.hook_program) h = -1;
       m.color[0] = m.color[1] = m.color[2] = 0.8f;
       m.roughness = 0.5f;
       m.ior = 1.5f;
@@ -190,15 +199,33 @@ class Builder {
       const ft_material& m = d_.materials[i];
       if (m.kind < FT_MAT_STANDARD || m.kind > FT_MAT_DIELECTRIC)
         return fail("material " + std::to_string(i) + " has an unknown kind");
-      const int32_t progs[4] = {m.color_program, m.roughness_program, m.ior_program, m.thin_walled_program};
-      for (int k = 0; k < 4; ++k) {
-        if (progs[k] < 0) continue;
-        if (static_cast<uint32_t>(progs[k]) >= d_.n_programs)
+      // Each hook slot: the program index, then its context (7 shading or 13
+      // BSDF parameters) and result (0 number, 1 vec3, 2 either).
+      struct Want {
+        int32_t prog;
+        bool bsdf;
+        int result;
+      };
+      std::vector<Want> wants = {{m.color_program, false, 2}, {m.roughness_program, false, 0},
+                                 {m.ior_program, false, 0}, {m.thin_walled_program, false, 0}};
+      static const int kResult[FT_MATERIAL_HOOKS] = {2, 0, 0, 0, 0, 0, 2, 0, 0, 0, 0, 0, 1,  // properties, bump, normal
+                                                     2, 0,                                  // eval, pdf
+                                                     1, 2, 0, 0, 0, 0, 0, 0};               // sample fields
+      for (int k = 0; k < FT_MATERIAL_HOOKS; ++k) wants.push_back({m.hook_program[k], k >= FT_HOOK_EVAL, kResult[k]});
+      for (int k = FT_MATERIAL_HOOKS; k < 24; ++k)
+        if (m.hook_program[k] != -1) return fail("material " + std::to_string(i) + " uses a reserved hook slot");
+      for (const Want& w : wants) {
+        if (w.prog < 0) continue;
+        if (static_cast<uint32_t>(w.prog) >= d_.n_programs)
           return fail("material " + std::to_string(i) + " has an invalid hook program index");
-        const ft_program& p = d_.programs[progs[k]];
-        if (p.n_params != FT_MATERIAL_HOOK_PARAMS || p.param_is_vec3 != 0xfu || (k > 0 && p.result_is_vec3))
-          return fail("material " + std::to_string(i) + " hook must map the shading context to " +
-                      (k == 0 ? "a colour" : "a number"));
+        const ft_program& p = d_.programs[w.prog];
+        const uint32_t np = w.bsdf ? FT_BSDF_HOOK_PARAMS : FT_MATERIAL_HOOK_PARAMS;
+        const uint32_t vec_mask = w.bsdf ? 0x18fu : 0xfu;
+        if (p.n_params != np || p.param_is_vec3 != vec_mask || (w.result == 0 && p.result_is_vec3) ||
+            (w.result == 1 && !p.result_is_vec3))
+          return fail("material " + std::to_string(i) + " hook must map the " +
+                      (w.bsdf ? "BSDF" : "shading") + " context to " +
+                      (w.result == 0 ? "a number" : w.result == 1 ? "a vec3" : "a colour"));
       }
     }
     // The node graph must be a DAG reachable from the root (no cycles).

@@ -90,6 +90,9 @@ struct SceneImage {
   // (blend_materials then yields a Blend whatever the weights)
   std::vector<int32_t> ur_inner_blend;
   std::vector<int32_t> node_op_begin, node_op_end;  // postfix op range of each node's subtree
+  // per object id: the primitive or Custom node carrying it (its transform is
+  // the object's, object_transforms R:485-555), -1 for none
+  std::vector<int32_t> obj_node;
   std::vector<ft_material> materials;
   std::vector<ft_light> lights;
   int32_t environment_program = -1;

@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define FT_ABI_VERSION 3u
+#define FT_ABI_VERSION 4u
 
 /* Status codes.  FT_ERR_MISSING_SCENE_ROOT / UNSUPPORTED_OBJECT /
  * EXPECTED_OBJECT mirror `enum RenderError` (R:159-168); PARSE / EVAL mirror
@@ -241,7 +241,59 @@ typedef struct ft_material {
   int32_t roughness_program;  /* per-hit `fn roughness(ctx)` hook (number), -1 if none */
   int32_t ior_program;        /* per-hit `fn ior(ctx)` hook (number), -1 if none */
   int32_t thin_walled_program; /* per-hit `fn thin_walled(ctx)` hook (number, >= 0.5 thin), -1 if none */
+  int32_t hook_program[24];   /* the further hooks, indexed by ft_material_hook (23 used); -1 if none */
 } ft_material;
+
+/* The further hooks of a material definition (crates/forgedthoughts/src/
+ * renderer.rs, "R:" below), by slot of ft_material.hook_program.  The
+ * property hooks take the shading context (FT_MATERIAL_HOOK_PARAMS) and are
+ * applied where a leaf's material is resolved (resolve_leaf_material,
+ * R:7164-7530), with the reference's clamps:
+ *   every definition    emission_color (vec3 or number), emission_strength
+ *                       (>= 0);
+ *   Standard / Layered  metallic, specular, specular_weight, transmission
+ *                       ([0, 1]) and the coat: coat_color, coat_roughness
+ *                       ([0, 1]), coat_ior ([1, 3]), coat_weight and
+ *                       coat_mask ([0, 1]), which replace the specular
+ *                       colour, IOR, clearcoat (weight x mask) and clearcoat
+ *                       roughness at every hit (R:7397-7468).
+ * The shading-normal hooks (build_bsdf_context, R:4397-4449) belong to the
+ * hit's own material: `fn bump(ctx)` (number, a height field differentiated
+ * along a tangent frame, R:7776-7818), then `fn normal(ctx)` (vec3,
+ * R:7749-7774), each seeing the normal so far as ctx.normal.
+ * The BSDF hooks (R:4905-4950) belong to the dominant parameters of the
+ * shaded material (a blend of two parameter sets keeps none) and take the
+ * BSDF context (FT_BSDF_HOOK_PARAMS): `fn eval(ctx)` replaces Material::eval
+ * in the Whitted light loop and the path tracer, `fn pdf(ctx)`
+ * Material::pdf, and `fn sample(ctx)` Material::sample in the path tracer;
+ * the sample's record fields are one program each (wi and f are required,
+ * the others default as bsdf_sample_from_value, R:5032-5060, reads them). */
+typedef enum ft_material_hook {
+  FT_HOOK_EMISSION_COLOR = 0,
+  FT_HOOK_EMISSION_STRENGTH = 1,
+  FT_HOOK_METALLIC = 2,
+  FT_HOOK_SPECULAR = 3,
+  FT_HOOK_SPECULAR_WEIGHT = 4,
+  FT_HOOK_TRANSMISSION = 5,
+  FT_HOOK_COAT_COLOR = 6,
+  FT_HOOK_COAT_ROUGHNESS = 7,
+  FT_HOOK_COAT_IOR = 8,
+  FT_HOOK_COAT_WEIGHT = 9,
+  FT_HOOK_COAT_MASK = 10,
+  FT_HOOK_BUMP = 11,
+  FT_HOOK_NORMAL = 12,
+  FT_HOOK_EVAL = 13,
+  FT_HOOK_PDF = 14,
+  FT_HOOK_SAMPLE_WI = 15,
+  FT_HOOK_SAMPLE_F = 16,
+  FT_HOOK_SAMPLE_PDF = 17,
+  FT_HOOK_SAMPLE_DELTA = 18,
+  FT_HOOK_SAMPLE_APPLY_COS = 19,
+  FT_HOOK_SAMPLE_TRANSMISSION = 20,
+  FT_HOOK_SAMPLE_THIN_WALLED = 21,
+  FT_HOOK_SAMPLE_NEXT_IOR = 22,
+  FT_MATERIAL_HOOKS = 23
+} ft_material_hook;
 
 /* Material hook programs take the shading context of a hit
  * (make_shading_context, R:7875-7911) as seven parameters: position,
@@ -249,6 +301,11 @@ typedef struct ft_material {
  * ray), view_dir (-ray direction) as vec3s, then front_face (1 or 0),
  * object_id and material_id as numbers. */
 #define FT_MATERIAL_HOOK_PARAMS 7
+/* BSDF hook programs (bsdf_context_value, R:5006-5030) take those seven with
+ * normal = the shading normal, then wo, wi (vec3s), current_ior and, for
+ * `fn sample`, the random numbers u1, u2, u3 (numbers): thirteen parameters,
+ * of which eval and pdf read the first ten. */
+#define FT_BSDF_HOOK_PARAMS 13
 
 typedef struct ft_camera {
   float origin[3];

@@ -69,6 +69,8 @@ def lib() -> ctypes.CDLL:
         h.oracle_medium_transmittance.argtypes = [vp, ctypes.c_float, vp]
         h.oracle_transition_medium.restype = None
         h.oracle_transition_medium.argtypes = [vp, ctypes.c_int, vp, vp]
+        h.oracle_bsdf_hit.restype = ctypes.c_int
+        h.oracle_bsdf_hit.argtypes = [vp, vp, vp, ctypes.c_float, vp, vp, vp]
         _lib = h
     return _lib
 
@@ -208,6 +210,23 @@ def transition_medium(material, front_face: bool, current) -> np.ndarray:
     lib().oracle_transition_medium(ctypes.cast(ctypes.byref(material), ctypes.c_void_p), int(bool(front_face)),
                                    _arr(cur), _arr(out))
     return out
+
+
+def bsdf_hit(state, position, normal, front_face: bool, object_id: int, material_id: int, view_dir,
+             current_ior: float, wi, u=(0.5, 0.5, 0.5)) -> dict:
+    """The BSDF context of one hit (build_bsdf_context, renderer.rs:4397-4449)
+    and the BSDF of the material resolved there, hooks included (eval_bsdf,
+    pdf_bsdf, sample_bsdf_lobe, renderer.rs:4869-4950), in f32: the shading
+    normal, eval(wi), pdf(wi) and the sample drawn with the randoms ``u``."""
+    hit = np.array(list(position) + list(normal) + [1.0 if front_face else 0.0, object_id, material_id], np.float32)
+    out = np.zeros(19, np.float32)
+    _check(lib().oracle_bsdf_hit(state.desc_ptr, _arr(hit), _arr(np.asarray(view_dir, np.float32)),
+                                 float(current_ior), _arr(np.asarray(wi, np.float32)),
+                                 _arr(np.asarray(u, np.float32)), _arr(out)))
+    return {"normal": out[0:3], "eval": out[3:6], "pdf": float(out[6]), "sample_wi": out[7:10],
+            "sample_f": out[10:13], "sample_pdf": float(out[13]), "sample_delta": bool(out[14]),
+            "sample_apply_cos": bool(out[15]), "sample_transmission": bool(out[16]),
+            "sample_thin_walled": bool(out[17]), "sample_next_ior": float(out[18])}
 
 
 def eval_program(state, program: int, args: np.ndarray, precision: int = 32) -> np.ndarray:

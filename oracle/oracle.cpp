@@ -218,10 +218,20 @@ template <class R> R sd_regular_ngon(V<R> p, int sides, R radius) {
 template <class R>
 class Scene {
  public:
-  explicit Scene(const ft_scene_desc& d) : d_(d) {}
+  explicit Scene(const ft_scene_desc& d) : d_(d) {
+    // object id -> the primitive or Custom node carrying its transform
+    // (object_transforms, R:485-555)
+    for (uint32_t i = 0; i < d_.n_nodes; ++i) {
+      const ft_node& n = d_.nodes[i];
+      if (!(n.kind <= FT_NODE_EXTRUDE_POLYGON || n.kind == FT_NODE_CUSTOM) || n.object_id >= (1u << 20)) continue;
+      if (obj_node_.size() <= n.object_id) obj_node_.resize(n.object_id + 1, -1);
+      if (obj_node_[n.object_id] < 0) obj_node_[n.object_id] = static_cast<int>(i);
+    }
+  }
 
   const ft_scene_desc& desc() const { return d_; }
   const ft_node& node(int i) const { return d_.nodes[i]; }
+  int object_node(uint32_t obj) const { return obj < obj_node_.size() ? obj_node_[obj] : -1; }
 
   V<R> center(const ft_node& n) const { return mk(R(n.center[0]), R(n.center[1]), R(n.center[2])); }
 
@@ -505,6 +515,7 @@ class Scene {
 
  private:
   const ft_scene_desc& d_;
+  std::vector<int> obj_node_;
 };
 
 // ------------------------------------------------------------ accelerators
@@ -1091,6 +1102,8 @@ struct Params {  // MaterialParams (materials/mod.rs:66-86), render-relevant fie
   R medium_ior = R(1);
   Sp<R> medium_absorption = Sp<R>{R(1), R(1), R(1)};
   R medium_density = R(0);
+  // dynamic_material_id (R:6669): the material whose BSDF hooks apply, -1 none
+  int dyn = -1;
 };
 
 template <class R>
@@ -1140,6 +1153,7 @@ template <class R> Mat<R> material_for_id(const ft_scene_desc& d, uint32_t id) {
   const ft_material& fm = d.materials[id < d.n_materials ? id : 0];
   m.kind = fm.kind;
   m.p = params_from<R>(fm);
+  m.p.dyn = static_cast<int>(id < d.n_materials ? id : 0);
   return m;
 }
 
@@ -1181,6 +1195,7 @@ template <class R> Params<R> blend_params(Params<R> a, const Params<R>& b, R t) 
     a.medium_absorption = b.medium_absorption;
     a.medium_density = b.medium_density;
   }
+  a.dyn = -1;  // dynamic_material_id = None (R:7624)
   return a;
 }
 template <class R> Mat<R> blend_materials(const Mat<R>& a, const Mat<R>& b, R t) {
@@ -1523,6 +1538,13 @@ template <class R> Medium<R> transition_medium(const Mat<R>& m, bool front, Medi
 template <class R>
 class Tracer {
  public:
+  // BsdfContextBase (build_bsdf_context, R:4397-4449): position, local
+  // position in the hit object's frame (object_transforms), shading normal,
+  // wo, front face, object and material ids, current IOR.
+  struct BsdfCtx {
+    V<R> pos, local, normal, wo;
+    R front, obj, mat, current_ior;
+  };
   Tracer(const Scene<R>& s, const Accel<R>& a, const Opts& op, uint32_t max_depth)
       : S(s), A(a), op_(op), max_depth_(std::max(max_depth, 1u)) {}
 
@@ -1564,10 +1586,11 @@ class Tracer {
   // sample_one_light (R:4572-4704).  The path lights are the scene's lights
   // with sphere lights as points (parse_lights R:6288-6388), in binding-name
   // order.
-  struct PathCtx {  // BsdfContextBase (R:4397-4449) without hooks
+  struct PathCtx {  // BsdfContextBase (R:4397-4449) and the hit's geometric normal
     V<R> normal, wo, hit_normal;
     bool front;
     R current_ior;
+    BsdfCtx b;
   };
   R env_light_pdf_for_dir(const Mat<R>& m, const PathCtx& c, V<R> wi) const {  // R:4336-4355
     const ft_scene_desc& d = S.desc();
@@ -1575,7 +1598,7 @@ class Tracer {
     R env = 0;
     for (uint32_t i = 0; i < d.n_lights; ++i) env += d.lights[i].kind == FT_LIGHT_ENV ? R(1) : R(0);
     if (env <= R(0)) return R(0);
-    return (env / R(d.n_lights)) * rmax(mat_pdf(m, c.normal, wi, c.wo), R(1.0e-6));
+    return (env / R(d.n_lights)) * rmax(bsdf_pdf(m, c.b, wi), R(1.0e-6));
   }
   // cosine_sample_hemisphere (R:4676-4695): two draws of the path's generator
   static V<R> cosine_hemisphere(V<R> normal, XorShift64& rng) {
@@ -1618,9 +1641,9 @@ class Tracer {
     V<R> so = offset_origin(p, c.hit_normal, wi, R(op_.epsilon));
     R vis = shadow(so, wi, max_t, evals);
     if (vis <= R(0)) return black<R>();
-    Sp<R> f = mat_eval(m, c.normal, wi, c.wo);
-    R bsdf_pdf = rmax(mat_pdf(m, c.normal, wi, c.wo), R(1.0e-6));
-    R w = delta ? R(1) : power_heuristic(pdf, bsdf_pdf);
+    Sp<R> f = bsdf_eval(m, c.b, wi);
+    R bpdf = rmax(bsdf_pdf(m, c.b, wi), R(1.0e-6));
+    R w = delta ? R(1) : power_heuristic(pdf, bpdf);
     return scale(f * rad, (cos_t * vis * w) / rmax(pdf, R(1.0e-6)));
   }
   Sp<R> trace_path(V<R> origin, V<R> dir, uint32_t max_bounces, XorShift64& rng, uint64_t* evals) const {
@@ -1657,13 +1680,15 @@ class Tracer {
       if (surface_normal(S.desc().root, h.pos, R(1.0e-4), &gnode)) c.normal = normalize(front ? gnode : gnode * R(-1));
       c.wo = wo;
       c.current_ior = medium.ior;
+      c.b = bsdf_context(h, front, c.normal, dir * R(-1), medium.ior);
+      c.normal = c.b.normal;
       Sp<R> em = emission(m);
       if (em.r > R(0) || em.g > R(0) || em.b > R(0)) radiance = radiance + throughput * em;
       Sp<R> direct = estimate_direct_mis(m, h.pos, c, rng, evals);
       radiance = radiance + clamp_luma(throughput * direct, R(12));
       // sample_bsdf_lobe (R:4870-4903)
       SampleInputT<R> in{front, c.current_ior, R(rng.next_f32()), R(rng.next_f32()), R(rng.next_f32())};
-      BsdfSampleT<R> smp = mat_sample(m, c.normal, c.wo, in);
+      BsdfSampleT<R> smp = bsdf_sample(m, c.b, in);
       if (smp.pdf <= R(1.0e-6)) break;
       if (smp.apply_cos) {
         R ct = rmax(dot(c.normal, smp.wi), R(0));
@@ -1853,8 +1878,9 @@ class Tracer {
     const ft_scene_desc& d = S.desc();
     if (d.n_materials == 0) return m;
     const ft_material& fm = d.materials[n.material_id < d.n_materials ? n.material_id : 0];
-    if (fm.color_program < 0 && fm.roughness_program < 0 && fm.ior_program < 0 && fm.thin_walled_program < 0)
-      return m;
+    bool any = fm.color_program >= 0 || fm.roughness_program >= 0 || fm.ior_program >= 0 || fm.thin_walled_program >= 0;
+    for (int k = FT_HOOK_EMISSION_COLOR; k <= FT_HOOK_COAT_MASK; ++k) any = any || fm.hook_program[k] >= 0;
+    if (!any) return m;
     const R obj = R(n.object_id), mid = R(n.material_id);
     V<R> args[FT_MATERIAL_HOOK_PARAMS] = {hc.pos, S.to_local(hc.pos, n), hc.normal, hc.view,
                                           mk(hc.front, hc.front, hc.front), mk(obj, obj, obj), mk(mid, mid, mid)};
@@ -1875,7 +1901,172 @@ class Tracer {
       S.run_program(fm.thin_walled_program, args, &o);
       m.p.thin_walled = o.x >= R(0.5);
     }
+    // The further property hooks (R:7258-7470): emission for every
+    // definition; metallic, specular, specular_weight, transmission and the
+    // coat (compiled for Standard / Layered definitions only), the coat's
+    // colour, roughness and IOR replacing the specular colour, clearcoat
+    // roughness and IOR and its weight x mask the clearcoat.
+    const int32_t* hp = fm.hook_program;
+    auto num = [&](int slot) {
+      S.run_program(hp[slot], args, &o);
+      return o.x;
+    };
+    auto colour = [&](int slot) {
+      S.run_program(hp[slot], args, &o);
+      return d.programs[hp[slot]].result_is_vec3 ? sp(o.x, o.y, o.z) : sp(o.x, o.x, o.x);
+    };
+    if (hp[FT_HOOK_EMISSION_COLOR] >= 0) m.p.emission_color = colour(FT_HOOK_EMISSION_COLOR);
+    if (hp[FT_HOOK_EMISSION_STRENGTH] >= 0) m.p.emission_strength = rmax(num(FT_HOOK_EMISSION_STRENGTH), R(0));
+    if (hp[FT_HOOK_METALLIC] >= 0) m.p.metallic = rclamp(num(FT_HOOK_METALLIC), R(0), R(1));
+    if (hp[FT_HOOK_SPECULAR] >= 0) m.p.specular = rclamp(num(FT_HOOK_SPECULAR), R(0), R(1));
+    if (hp[FT_HOOK_SPECULAR_WEIGHT] >= 0) m.p.specular_weight = rclamp(num(FT_HOOK_SPECULAR_WEIGHT), R(0), R(1));
+    if (hp[FT_HOOK_TRANSMISSION] >= 0) m.p.transmission = rclamp(num(FT_HOOK_TRANSMISSION), R(0), R(1));
+    if (hp[FT_HOOK_COAT_COLOR] >= 0) m.p.specular_color = colour(FT_HOOK_COAT_COLOR);
+    if (hp[FT_HOOK_COAT_ROUGHNESS] >= 0) m.p.clearcoat_roughness = rclamp(num(FT_HOOK_COAT_ROUGHNESS), R(0), R(1));
+    if (hp[FT_HOOK_COAT_IOR] >= 0) m.p.ior = rclamp(num(FT_HOOK_COAT_IOR), R(1), R(3));
+    if (hp[FT_HOOK_COAT_WEIGHT] >= 0 || hp[FT_HOOK_COAT_MASK] >= 0) {
+      R w = hp[FT_HOOK_COAT_WEIGHT] >= 0 ? rclamp(num(FT_HOOK_COAT_WEIGHT), R(0), R(1)) : m.p.clearcoat;
+      R k = hp[FT_HOOK_COAT_MASK] >= 0 ? rclamp(num(FT_HOOK_COAT_MASK), R(0), R(1)) : R(1);
+      m.p.clearcoat = rclamp(w * k, R(0), R(1));
+    }
     return m;
+  }
+
+  // ---------------------------------------------------------------- BSDF context and hooks
+  // The BSDF context of a hit: the geometric normal through the hit
+  // material's bump and normal hooks.
+  BsdfCtx bsdf_context(const Hit<R>& h, bool front, V<R> geometric_normal, V<R> view_dir, R current_ior) const {
+    BsdfCtx c;
+    c.pos = h.pos;
+    int ni = S.object_node(h.obj);
+    c.local = ni >= 0 ? S.to_local(h.pos, S.node(ni)) : h.pos;
+    c.normal = geometric_normal;
+    c.wo = normalize(view_dir);
+    c.front = front ? R(1) : R(0);
+    c.obj = R(h.obj);
+    c.mat = R(h.mat);
+    c.current_ior = current_ior;
+    c.normal = hooked_normal(c, view_dir, h.mat);
+    return c;
+  }
+  // resolve_dynamic_bump then resolve_dynamic_normal (R:7749-7818) of the
+  // hit's material (material_for_id, R:4418): a forward-difference gradient
+  // of the bump height (step 0.01) along the normal's tangent frame, then the
+  // normal hook; each normalised, turned to its input's side, dropped when
+  // degenerate.
+  V<R> hooked_normal(const BsdfCtx& c, V<R> view_dir, uint32_t hit_mat) const {
+    const ft_scene_desc& d = S.desc();
+    V<R> n = c.normal;
+    if (d.n_materials == 0) return n;
+    const ft_material& fm = d.materials[hit_mat < d.n_materials ? hit_mat : 0];
+    const int bump = fm.hook_program[FT_HOOK_BUMP], nrm = fm.hook_program[FT_HOOK_NORMAL];
+    V<R> a[FT_MATERIAL_HOOK_PARAMS] = {c.pos, c.local, n, view_dir, mk(c.front, c.front, c.front),
+                                       mk(c.obj, c.obj, c.obj), mk(c.mat, c.mat, c.mat)};
+    V<R> o;
+    if (bump >= 0) {
+      const R eps = R(0.01);
+      S.run_program(bump, a, &o);
+      const R center = o.x;
+      V<R> up = std::fabs(n.y) < R(0.999) ? mk(R(0), R(1), R(0)) : mk(R(1), R(0), R(0));
+      V<R> tangent = normalize(cross(n, up));
+      V<R> bitangent = normalize(cross(n, tangent));
+      a[1] = c.local + tangent * eps;
+      S.run_program(bump, a, &o);
+      const R dx = o.x - center;
+      a[1] = c.local + bitangent * eps;
+      S.run_program(bump, a, &o);
+      const R dy = o.x - center;
+      a[1] = c.local;
+      V<R> b = normalize((n - tangent * (dx / eps)) - bitangent * (dy / eps));
+      if (len(b) > R(1.0e-6)) n = dot(b, n) < R(0) ? b * R(-1) : b;
+      a[2] = n;
+    }
+    if (nrm >= 0) {
+      S.run_program(nrm, a, &o);
+      V<R> b = normalize(o);
+      if (len(b) > R(1.0e-6)) n = dot(b, n) < R(0) ? b * R(-1) : b;
+    }
+    return n;
+  }
+  // bsdf_context_value (R:5006-5030) as hook arguments
+  static void bsdf_args(const BsdfCtx& c, V<R> wi, R u1, R u2, R u3, V<R>* a) {
+    a[0] = c.pos; a[1] = c.local; a[2] = c.normal; a[3] = c.wo;
+    a[4] = mk(c.front, c.front, c.front); a[5] = mk(c.obj, c.obj, c.obj); a[6] = mk(c.mat, c.mat, c.mat);
+    a[7] = c.wo; a[8] = wi; a[9] = mk(c.current_ior, c.current_ior, c.current_ior);
+    a[10] = mk(u1, u1, u1); a[11] = mk(u2, u2, u2); a[12] = mk(u3, u3, u3);
+  }
+  int bsdf_hook(const Mat<R>& m, int slot) const {
+    const int dyn = dominant_params(m).dyn;
+    return dyn >= 0 && S.desc().n_materials ? S.desc().materials[dyn].hook_program[slot] : -1;
+  }
+  // eval_bsdf (R:4905-4920)
+  Sp<R> bsdf_eval(const Mat<R>& m, const BsdfCtx& c, V<R> wi) const {
+    const int prog = bsdf_hook(m, FT_HOOK_EVAL);
+    if (prog < 0) return mat_eval(m, c.normal, wi, c.wo);
+    V<R> a[FT_BSDF_HOOK_PARAMS], o;
+    bsdf_args(c, wi, R(0), R(0), R(0), a);
+    S.run_program(prog, a, &o);
+    return S.desc().programs[prog].result_is_vec3 ? sp(o.x, o.y, o.z) : sp(o.x, o.x, o.x);
+  }
+ public:
+  // Test probe (oracle_bsdf_hit): the context of one hit with the given
+  // geometric normal, and the hooks of the material resolved at the hit
+  // (resolve_material_at_hit, R:6926-6935).
+  int bsdf_probe(const Hit<R>& h, bool front, V<R> gn, V<R> view, R current_ior, V<R> wi, const float* u,
+                 float* out) const {
+    const HookCtx hc{h.pos, gn, normalize(view), front ? R(1) : R(0)};
+    Mat<R> m;
+    if (!material_from_node(S.desc().root, h.pos, hc, &m)) m = material_for_id<R>(S.desc(), h.mat);
+    const BsdfCtx c = bsdf_context(h, front, gn, view, current_ior);
+    const Sp<R> f = bsdf_eval(m, c, wi);
+    const R pdf = bsdf_pdf(m, c, wi);
+    SampleInputT<R> in{front, current_ior, R(u[0]), R(u[1]), R(u[2])};
+    const BsdfSampleT<R> smp = bsdf_sample(m, c, in);
+    const float vals[19] = {float(c.normal.x), float(c.normal.y), float(c.normal.z), float(f.r), float(f.g),
+                            float(f.b), float(pdf), float(smp.wi.x), float(smp.wi.y), float(smp.wi.z),
+                            float(smp.f.r), float(smp.f.g), float(smp.f.b), float(smp.pdf), smp.delta ? 1.0f : 0.0f,
+                            smp.apply_cos ? 1.0f : 0.0f, smp.transmission ? 1.0f : 0.0f,
+                            smp.thin_walled ? 1.0f : 0.0f, float(smp.next_ior)};
+    for (int k = 0; k < 19; ++k) out[k] = vals[k];
+    return 0;
+  }
+
+ private:
+
+  // pdf_bsdf (R:4922-4933)
+  R bsdf_pdf(const Mat<R>& m, const BsdfCtx& c, V<R> wi) const {
+    const int prog = bsdf_hook(m, FT_HOOK_PDF);
+    if (prog < 0) return mat_pdf(m, c.normal, wi, c.wo);
+    V<R> a[FT_BSDF_HOOK_PARAMS], o;
+    bsdf_args(c, wi, R(0), R(0), R(0), a);
+    S.run_program(prog, a, &o);
+    return rmax(o.x, R(0));
+  }
+  // sample_bsdf_lobe (R:4869-4903) with sample_bsdf_ft / bsdf_sample_from_value
+  // (R:4934-4950, R:5032-5060)
+  BsdfSampleT<R> bsdf_sample(const Mat<R>& m, const BsdfCtx& c, const SampleInputT<R>& in) const {
+    const int dyn = dominant_params(m).dyn;
+    const int32_t* hp = dyn >= 0 && S.desc().n_materials ? S.desc().materials[dyn].hook_program : nullptr;
+    if (!hp || hp[FT_HOOK_SAMPLE_WI] < 0 || hp[FT_HOOK_SAMPLE_F] < 0) return mat_sample(m, c.normal, c.wo, in);
+    V<R> a[FT_BSDF_HOOK_PARAMS], o;
+    bsdf_args(c, c.normal, in.u1, in.u2, in.u3, a);
+    auto num = [&](int slot, R dflt) {
+      if (hp[slot] < 0) return dflt;
+      S.run_program(hp[slot], a, &o);
+      return o.x;
+    };
+    BsdfSampleT<R> r;
+    S.run_program(hp[FT_HOOK_SAMPLE_WI], a, &o);
+    r.wi = o;
+    S.run_program(hp[FT_HOOK_SAMPLE_F], a, &o);
+    r.f = S.desc().programs[hp[FT_HOOK_SAMPLE_F]].result_is_vec3 ? sp(o.x, o.y, o.z) : sp(o.x, o.x, o.x);
+    r.pdf = rmax(num(FT_HOOK_SAMPLE_PDF, R(0)), R(0));
+    r.delta = num(FT_HOOK_SAMPLE_DELTA, R(0)) >= R(0.5);
+    r.apply_cos = num(FT_HOOK_SAMPLE_APPLY_COS, R(1)) >= R(0.5);
+    r.transmission = num(FT_HOOK_SAMPLE_TRANSMISSION, R(0)) >= R(0.5);
+    r.thin_walled = num(FT_HOOK_SAMPLE_THIN_WALLED, R(0)) >= R(0.5);
+    r.next_ior = rclamp(num(FT_HOOK_SAMPLE_NEXT_IOR, R(1)), R(1), R(3));
+    return r;
   }
 
   // resolve_material_from_node (R:6945-7050) / blend_node_materials (R:7093-7113)
@@ -2021,7 +2212,8 @@ class Tracer {
   }
 
   // shade_color (R:4217-4276)
-  Sp<R> shade(const Mat<R>& mat, const Hit<R>& h, bool front, V<R> n_shade, V<R> wo, uint64_t* evals) const {
+  Sp<R> shade(const Mat<R>& mat, const Hit<R>& h, bool front, const BsdfCtx& bc, uint64_t* evals) const {
+    const V<R> n_shade = bc.normal;
     const ft_scene_desc& d = S.desc();
     if (d.n_lights == 0) return sp(R(1), R(1), R(1));
     V<R> n = normalize(n_shade);
@@ -2046,7 +2238,7 @@ class Tracer {
         R vis = shadow(so, wi, max_t, evals);
         if (vis <= R(0)) continue;
         // eval_bsdf passes the context normal as stored (R:4905-4919)
-        Sp<R> f = mat_eval(mat, n_shade, wi, wo);
+        Sp<R> f = bsdf_eval(mat, bc, wi);
         color = color + scale(f * rad, ndotl * vis * inv);
       }
     }
@@ -2079,6 +2271,9 @@ class Tracer {
       gnode = front ? gnode : gnode * R(-1);
       shading_n = normalize(gnode);
     }
+    // the bump and normal hooks of the hit's material, and the BSDF context
+    const BsdfCtx bc = bsdf_context(h, front, shading_n, dir * R(-1), med.ior);
+    shading_n = bc.normal;
     Params<R> P = dominant_params(mat);
     R rough = rclamp(P.roughness, R(0), R(1));
     int model = dominant_model(mat);
@@ -2132,7 +2327,7 @@ class Tracer {
       reflect_w = rclamp(base * fresnel + metallic * R(0.8) + clearcoat * R(0.2), R(0), R(1));
     }
     R local_w = rclamp((R(1) - transmission) * (R(1) - reflect_w), R(0), R(1));
-    Sp<R> color = scale(shade(mat, h, front, shading_n, wo, evals), local_w);
+    Sp<R> color = scale(shade(mat, h, front, bc, evals), local_w);
     color = color + emission(mat);
     R eps = R(op_.epsilon);
     if (reflect_w > R(1.0e-4)) {
@@ -2766,8 +2961,8 @@ int oracle_eval_program(const ft_scene_desc* desc, int program, int precision, c
     Scene<R> scene(*desc);
     uint32_t np = desc->programs[program].n_params;
     for (size_t i = 0; i < n; ++i) {
-      V<R> a[8];
-      for (uint32_t k = 0; k < np && k < 8; ++k) {
+      V<R> a[16];
+      for (uint32_t k = 0; k < np && k < 16; ++k) {
         const float* s = args + (i * np + k) * 3;
         a[k] = mk(R(s[0]), R(s[1]), R(s[2]));
       }
@@ -2973,4 +3168,29 @@ extern "C" void oracle_transition_medium(const ft_material* material, int front_
   out[2] = next.absorption.g;
   out[3] = next.absorption.b;
   out[4] = next.density;
+}
+
+// Test-only: the BSDF context of one hit and the BSDF hooks (or built-in
+// BSDF) of the material resolved there, for the reference's unit tests of
+// build_bsdf_context (R:4397-4449), eval_bsdf, pdf_bsdf and sample_bsdf_lobe
+// (R:4869-4950).  hit = position (3), normal (3), front_face, object_id,
+// material_id; out = shading normal (3), eval (3), pdf, then the sample: wi
+// (3), f (3), pdf, delta, apply_cos, transmission, thin_walled, next_ior.
+extern "C" int oracle_bsdf_hit(const ft_scene_desc* desc, const float hit[9], const float view_dir[3],
+                               float current_ior, const float wi[3], const float u[3], float out[19]) {
+  if (int e = check_desc(desc)) return e;
+  Scene<float> scene(*desc);
+  Accel<float> acc(scene, FT_ACCEL_NAIVE);
+  const Opts op{1, 1, 128, 40.0f, 1.0e-3f, 0.7f, 6.0f, 45.0f};
+  Tracer<float> tr(scene, acc, op, 1);
+  Hit<float> h;
+  h.t = 1.0f;
+  h.pos = mk(hit[0], hit[1], hit[2]);
+  h.normal = mk(hit[3], hit[4], hit[5]);
+  h.obj = static_cast<uint32_t>(hit[7]);
+  h.mat = static_cast<uint32_t>(hit[8]);
+  const bool front = hit[6] >= 0.5f;
+  const V<float> view = mk(view_dir[0], view_dir[1], view_dir[2]);
+  const V<float> gn = front ? normalize(h.normal) : normalize(h.normal * -1.0f);
+  return tr.bsdf_probe(h, front, gn, view, current_ior, mk(wi[0], wi[1], wi[2]), u, out);
 }
