@@ -78,8 +78,10 @@ FT_DEV F3 to_local(F3 p, const DevNode& n) {
 
 FT_DEV float shell(float d, float sh) { return sh > 0.0f ? rmax(d, -(d + sh)) : d; }
 
-// sd_regular_ngon (R:6206-6214)
-FT_DEV float sd_regular_ngon(float px, float pz, int sides, float radius) {
+// sd_regular_ngon (R:6206-6214).  Out of line: its trigonometry would
+// otherwise be inlined at every primitive evaluation site of the march loops,
+// whose bodies have to stay within the instruction cache.
+__device__ __noinline__ float sd_regular_ngon(float px, float pz, int sides, float radius) {
   float n = (float)(sides > 3 ? sides : 3);
   float an = 3.14159265358979323846f / n;
   float apothem = radius * cosf(an);

@@ -69,6 +69,8 @@ def lib() -> ctypes.CDLL:
         h.oracle_medium_transmittance.argtypes = [vp, ctypes.c_float, vp]
         h.oracle_transition_medium.restype = None
         h.oracle_transition_medium.argtypes = [vp, ctypes.c_int, vp, vp]
+        h.oracle_set_resolve_mode.restype = None
+        h.oracle_set_resolve_mode.argtypes = [ctypes.c_int]
         h.oracle_bsdf_hit.restype = ctypes.c_int
         h.oracle_bsdf_hit.argtypes = [vp, vp, vp, ctypes.c_float, vp, vp, vp]
         _lib = h
@@ -227,6 +229,23 @@ def bsdf_hit(state, position, normal, front_face: bool, object_id: int, material
             "sample_f": out[10:13], "sample_pdf": float(out[13]), "sample_delta": bool(out[14]),
             "sample_apply_cos": bool(out[15]), "sample_transmission": bool(out[16]),
             "sample_thin_walled": bool(out[17]), "sample_next_ior": float(out[18])}
+
+
+class resolve_at_hit_leaf:
+    """Context manager: while active, the oracle resolves a hit's normal and
+    material from the hard-union leaf holding the hit's object (the leaf its
+    accelerator found, as the GPU does) instead of walking the scene root's
+    unions as the reference does.  The two differ only where the reference's
+    union culling skips the hit's leaf (an object with both domain and
+    distance_post hooks, whose surface leaves its box)."""
+
+    def __enter__(self):
+        lib().oracle_set_resolve_mode(1)
+        return self
+
+    def __exit__(self, *exc):
+        lib().oracle_set_resolve_mode(0)
+        return False
 
 
 def eval_program(state, program: int, args: np.ndarray, precision: int = 32) -> np.ndarray:

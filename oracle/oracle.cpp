@@ -232,6 +232,39 @@ class Scene {
   const ft_scene_desc& desc() const { return d_; }
   const ft_node& node(int i) const { return d_.nodes[i]; }
   int object_node(uint32_t obj) const { return obj < obj_node_.size() ? obj_node_[obj] : -1; }
+  // The hard-union leaf (collect_accel_leaves, R:659-671) holding object
+  // `obj`, -1 if none.
+  int object_leaf(uint32_t obj) const {
+    if (!leaves_done_) {
+      std::vector<int> stack{d_.root};
+      while (!stack.empty()) {
+        int i = stack.back();
+        stack.pop_back();
+        if (d_.nodes[i].kind == FT_NODE_UNION) {
+          stack.push_back(d_.nodes[i].a);
+          stack.push_back(d_.nodes[i].b);
+          continue;
+        }
+        std::vector<int> sub{i};
+        while (!sub.empty()) {
+          int k = sub.back();
+          sub.pop_back();
+          const ft_node& n = d_.nodes[k];
+          if (n.kind <= FT_NODE_EXTRUDE_POLYGON || n.kind == FT_NODE_CUSTOM) {
+            if (n.object_id < (1u << 20)) {
+              if (obj_leaf_.size() <= n.object_id) obj_leaf_.resize(n.object_id + 1, -1);
+              if (obj_leaf_[n.object_id] < 0) obj_leaf_[n.object_id] = i;
+            }
+            continue;
+          }
+          if (n.a >= 0) sub.push_back(n.a);
+          if (n.b >= 0 && n.kind >= FT_NODE_UNION && n.kind <= FT_NODE_TONGUE) sub.push_back(n.b);
+        }
+      }
+      leaves_done_ = true;
+    }
+    return obj < obj_leaf_.size() ? obj_leaf_[obj] : -1;
+  }
 
   V<R> center(const ft_node& n) const { return mk(R(n.center[0]), R(n.center[1]), R(n.center[2])); }
 
@@ -516,6 +549,8 @@ class Scene {
  private:
   const ft_scene_desc& d_;
   std::vector<int> obj_node_;
+  mutable std::vector<int> obj_leaf_;
+  mutable bool leaves_done_ = false;
 };
 
 // ------------------------------------------------------------ accelerators
@@ -1535,6 +1570,16 @@ template <class R> Medium<R> transition_medium(const Mat<R>& m, bool front, Medi
   return Medium<R>{rclamp(p.ior, R(1), R(3)), sp(R(1), R(1), R(1)), R(0)};
 }
 
+// Where a hit's normal and material are resolved from: 0 = the scene root,
+// walking its unions with sdf_distance_info as the reference does
+// (resolve_surface_normal_at_hit / resolve_material_at_hit); 1 = the
+// hard-union leaf holding the hit's object, the leaf the accelerator's
+// distance evaluation found (the GPU's resolution).  The two differ only
+// where a union's culling in sdf_distance_info skips the hit's leaf: a leaf
+// whose surface lies outside its box (an object with both hooks, whose
+// transform applies twice).  Test-only switch (oracle_set_resolve_mode).
+int g_resolve_mode = 0;
+
 template <class R>
 class Tracer {
  public:
@@ -1671,13 +1716,13 @@ class Tracer {
       V<R> wo = normalize(dir * R(-1));
       const HookCtx hc{h.pos, front ? normalize(h.normal) : normalize(h.normal * R(-1)), wo, front ? R(1) : R(0)};
       Mat<R> m;
-      if (!material_from_node(S.desc().root, h.pos, hc, &m)) m = material_for_id<R>(S.desc(), h.mat);
+      if (!material_from_node(resolve_root(h), h.pos, hc, &m)) m = material_for_id<R>(S.desc(), h.mat);
       PathCtx c;
       c.front = front;
       c.hit_normal = front ? normalize(h.normal) : normalize(h.normal * R(-1));
       c.normal = c.hit_normal;
       V<R> gnode;
-      if (surface_normal(S.desc().root, h.pos, R(1.0e-4), &gnode)) c.normal = normalize(front ? gnode : gnode * R(-1));
+      if (surface_normal(resolve_root(h), h.pos, R(1.0e-4), &gnode)) c.normal = normalize(front ? gnode : gnode * R(-1));
       c.wo = wo;
       c.current_ior = medium.ior;
       c.b = bsdf_context(h, front, c.normal, dir * R(-1), medium.ior);
@@ -1737,7 +1782,7 @@ class Tracer {
     const HookCtx hc{h.pos, front ? normalize(h.normal) : normalize(h.normal * R(-1)), view, front ? R(1) : R(0)};
     Mat<R> ma, mb;
     R t;
-    int root = S.desc().root;
+    int root = resolve_root(h);
     if (split_material(root, h.pos, hc, &ma, &mb, &t)) {
       Sp<R> a = trace_hit(h, d, med, depth, ma, evals);
       Sp<R> b = trace_hit(h, d, med, depth, mb, evals);
@@ -1930,6 +1975,14 @@ class Tracer {
       m.p.clearcoat = rclamp(w * k, R(0), R(1));
     }
     return m;
+  }
+
+  int resolve_root(const Hit<R>& h) const {
+    if (g_resolve_mode == 1) {
+      const int leaf = S.object_leaf(h.obj);
+      if (leaf >= 0) return leaf;
+    }
+    return S.desc().root;
   }
 
   // ---------------------------------------------------------------- BSDF context and hooks
@@ -2267,7 +2320,7 @@ class Tracer {
     // build_bsdf_context: tree-resolved geometric normal (epsilon 1e-4)
     V<R> gnode;
     V<R> shading_n = normal;
-    if (surface_normal(S.desc().root, h.pos, R(1.0e-4), &gnode)) {
+    if (surface_normal(resolve_root(h), h.pos, R(1.0e-4), &gnode)) {
       gnode = front ? gnode : gnode * R(-1);
       shading_n = normalize(gnode);
     }
@@ -3194,3 +3247,6 @@ extern "C" int oracle_bsdf_hit(const ft_scene_desc* desc, const float hit[9], co
   const V<float> gn = front ? normalize(h.normal) : normalize(h.normal * -1.0f);
   return tr.bsdf_probe(h, front, gn, view, current_ior, mk(wi[0], wi[1], wi[2]), u, out);
 }
+
+// Test-only: where hits resolve their normal and material (g_resolve_mode).
+extern "C" void oracle_set_resolve_mode(int mode) { g_resolve_mode = mode; }

@@ -114,19 +114,29 @@ def test_c3_hooked_shells_full_frame_depth():
 def test_c3_shaded_full_frame():
     """C3's 1-bounce shading (Whitted depth 2) at 1920x1080, with 256 of the
     hooked shells, interpreted, compiled, and compiled with the primary hits
-    from the FP16 brick march: against the f32 oracle, 98.5 % of the pixels
-    within 1e-3 and radiance RMSE <= 1e-3 where the primary hits agree."""
+    from the FP16 brick march.
+
+    The reference resolves a hit's normal and material by walking the scene
+    root's hard unions with sdf_distance_info, whose union culling trusts each
+    subtree's box lower bound.  A shell carries both hooks, so its transform
+    applies twice and its surface lies partly outside its box: at a few hits
+    that walk is culled away from the shell the march hit and takes another
+    shell's normal.  The GPU resolves at the leaf its accelerator hit.  So:
+    against the f32 oracle resolving at that leaf, radiance RMSE <= 1e-3
+    where the primary hits agree; against the reference-resolving oracle,
+    98.5 % of the pixels within 1e-3 (4 of the 360 band pixels take the other
+    shell's normal there)."""
     w = workloads.twisted_shells(n=256)
     st = ft.parse_and_eval(w.source)
     rows, cols = (22, 1080, 90), (8, 64)
     ref, _, _ = oracle.render_trace(st, w.options, int(w.accel), 1, 2, 32, rows=rows, cols=cols)
+    with oracle.resolve_at_hit_leaf():
+        ref_leaf, _, _ = oracle.render_trace(st, w.options, int(w.accel), 1, 2, 32, rows=rows, cols=cols)
     t, m, _, _, _ = oracle.render_depth(st, w.options, int(w.accel), 1, 32, rows=rows, cols=cols)
     img = ft.render_depth(st, w.options, w.accel, 1)
     # the thin banded shells put a primary hit on another shell now and then
     # (within the depth bar's 0.1 %); radiance is compared where the primary
-    # hits agree, and 98.5 % of all pixels must be within 1e-3 (4 of the 360
-    # band pixels differ by more, though the oracle's own f32 and f64 agree
-    # to 1e-6 there)
+    # hits agree
     def agreement(img):
         return _band((img.mask[..., 0] == m[..., 0]) & (np.abs(img.t[..., 0] - t[..., 0]) <= 1e-4), rows, cols)
 
@@ -139,11 +149,12 @@ def test_c3_shaded_full_frame():
     bagree = agreement(ft.render_depth(st, w.options, w.accel, 1, fp16_bricks=True))
     assert bagree.mean() >= 0.99
     results["compiled_fp16_bricks"] = (ft.render_trace(st, w.options, w.accel, 1, 2, fp16_bricks=True)[0], bagree)
+    b, bl = _band(ref, rows, cols), _band(ref_leaf, rows, cols)
     for label, (lin, ok) in results.items():
-        a, b = _band(lin, rows, cols), _band(ref, rows, cols)
+        a = _band(lin, rows, cols)
+        assert radiance_rmse(a[ok], bl[ok]) <= 1e-3, (label, radiance_rmse(a[ok], bl[ok]))
         within = float((np.abs(a.astype(np.float64) - b).max(axis=-1) <= 1e-3).mean())
-        assert within >= 0.985, (label, within)
-        assert radiance_rmse(a[ok], b[ok]) <= 1e-3, (label, radiance_rmse(a[ok], b[ok]))
+        assert within >= 0.985, (label, within, radiance_rmse(a[ok], b[ok]))
 
 
 def _spheres(w):
