@@ -75,6 +75,7 @@ struct DevScene {
   const int32_t* __restrict__ ur_inner_up;  // parent link (parent << 1 | side), -1 at the root
   const int32_t* __restrict__ ur_prim_up;   // per primitive position: parent link
   const int32_t* __restrict__ obj_node;     // per object id: the node carrying its transform, -1 none
+  const int32_t* __restrict__ ur_cell_nodes;  // per cell entry: the primitive's node index
   int32_t n_obj_node;
   int32_t n_materials, n_lights, env_program;
   int32_t bvh_root;
@@ -368,8 +369,8 @@ __device__ __forceinline__ Info eval_urtree(const DevScene& S, const DevUrTree& 
   Info best{kInf, 0u, 0u};
   // Test one primitive against the running bound; evaluate it if it can
   // matter and record it in the near set when closer than r.
-  auto consider = [&](int pos) {
-    const DevNode& pn = S.nodes[S.ur_prims[t.prim_first + pos]];
+  auto consider = [&](int pos, int node) {
+    const DevNode& pn = S.nodes[node];
     cx.box();
     float lim = ftd::rmax(r, fminf(best.d, cutoff));
     if (node_lb(p, pn.bmin, pn.bmax) >= lim) return;
@@ -418,7 +419,10 @@ __device__ __forceinline__ Info eval_urtree(const DevScene& S, const DevUrTree& 
         cx.cand();
         if (S.ur_cell_gaps[k] >= ftd::rmax(r, fminf(best.d, cutoff))) break;
       }
-      consider(list[k++]);
+      // a cell entry carries its node index; a BVH leaf's goes through ur_prims
+      const int pos = list[k];
+      consider(pos, in_grid ? S.ur_cell_nodes[k] : S.ur_prims[t.prim_first + pos]);
+      ++k;
       continue;
     }
     if (in_grid || sp == 0) break;
@@ -572,6 +576,25 @@ __device__ __noinline__ Info scene_distance_bvh(const DevScene& S, F3 p, Ctx<kSt
   return cur;
 }
 
+// The nearer leaf, then the other when its box bound is not above the
+// distance found (the strictly-closer replace of bvh_distance_info).  One
+// evaluation site for both leaves: the leaf evaluator (with the whole
+// union_round path) is inlined once, which keeps the march loops' code within
+// the instruction cache.
+template <bool kStats>
+__device__ __forceinline__ Info scene_distance_leaves(const DevScene& S, F3 p, int leaf, int second, float second_lb,
+                                                      Ctx<kStats>& cx) {
+  Info cur{kInf, 0u, 0u};
+#pragma unroll 1
+  for (int k = 0; k < 2; ++k) {
+    const Info in = eval_leaf(S, S.leaves[leaf], p, k == 0 ? kInf : cur.d, cx);
+    if (k == 0 || in.d < cur.d) cur = in;
+    if (second < 0 || !(second_lb <= cur.d)) break;
+    leaf = second;
+  }
+  return cur;
+}
+
 // Same traversal, with the one- and two-leaf BVHs (a single object, or a
 // ground plus one composite object) walked without a stack.
 template <bool kStats>
@@ -591,18 +614,7 @@ __device__ __forceinline__ Info scene_distance_inl(const DevScene& S, F3 p, Ctx<
     second = lfirst ? R.leaf : L.leaf;
     second_lb = lfirst ? rl : ll;
   }
-  // One evaluation site for both leaves: the leaf evaluator (with the whole
-  // union_round path) is inlined once, which keeps the march loops' code
-  // within the instruction cache.
-  Info cur{kInf, 0u, 0u};
-#pragma unroll 1
-  for (int k = 0; k < 2; ++k) {
-    const Info in = eval_leaf(S, S.leaves[leaf], p, k == 0 ? kInf : cur.d, cx);
-    if (k == 0 || in.d < cur.d) cur = in;
-    if (second < 0 || !(second_lb <= cur.d)) break;
-    leaf = second;
-  }
-  return cur;
+  return scene_distance_leaves(S, p, leaf, second, second_lb, cx);
 }
 
 template <bool kStats>

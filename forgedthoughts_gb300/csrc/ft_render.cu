@@ -210,6 +210,7 @@ ft_status upload_scene(ft_scene* sc) {
       {im.ur_inner_up.data(), im.ur_inner_up.size() * sizeof(int32_t), 0},
       {im.ur_prim_up.data(), im.ur_prim_up.size() * sizeof(int32_t), 0},
       {im.obj_node.data(), im.obj_node.size() * sizeof(int32_t), 0},
+      {im.ur_cell_nodes.data(), im.ur_cell_nodes.size() * sizeof(int32_t), 0},
   };
   size_t total = 0;
   for (Part& p : parts) {
@@ -247,6 +248,7 @@ ft_status upload_scene(ft_scene* sc) {
   d.ur_prim_up = reinterpret_cast<const int32_t*>(base + parts[20].off);
   d.obj_node = reinterpret_cast<const int32_t*>(base + parts[21].off);
   d.n_obj_node = static_cast<int32_t>(im.obj_node.size());
+  d.ur_cell_nodes = reinterpret_cast<const int32_t*>(base + parts[22].off);
   d.n_materials = static_cast<int32_t>(im.materials.size());
   d.n_lights = static_cast<int32_t>(im.lights.size());
   d.env_program = im.environment_program;

@@ -368,6 +368,42 @@ __global__ void __launch_bounds__(128, 5) wf_march_persistent(DevScene S0, RayPa
   if (kStats) flush_stats(cx.c, stats);
 }
 
+// A step of shadow_visibility (R:4706-4733): the leaf-box lower bound when it
+// exceeds max(8 eps, 0.02), else the exact distance.  With one or two leaves
+// the lower bound's box bounds are the ones the exact evaluation orders its
+// leaves by, so they are computed once; the values are those of
+// scene_lower_bound and scene_distance_inl.
+template <bool kStats>
+__device__ __forceinline__ float shadow_step_h(const DevScene& S, F3 p, float eps, Ctx<kStats>& cx) {
+  const DevBvhNode& root = S.bvh[S.bvh_root];
+  int leaf = root.leaf, second = -1;
+  float second_lb = kInf, lower;
+  bool small = true;
+  if (leaf >= 0) {
+    cx.box();
+    lower = node_lb(p, root.bmin, root.bmax);
+  } else {
+    const DevBvhNode& L = S.bvh[root.lhs];
+    const DevBvhNode& R = S.bvh[root.rhs];
+    if (L.leaf >= 0 && R.leaf >= 0) {
+      cx.box(3);
+      const float ll = node_lb(p, L.bmin, L.bmax), rl = node_lb(p, R.bmin, R.bmax);
+      lower = fminf(ll, rl);
+      const bool lfirst = ll <= rl;
+      leaf = lfirst ? L.leaf : R.leaf;
+      second = lfirst ? R.leaf : L.leaf;
+      second_lb = lfirst ? rl : ll;
+    } else {
+      small = false;
+      lower = scene_lower_bound(S, p, cx);
+    }
+  }
+  lower = fabsf(lower);
+  if (lower > fmaxf(eps * 8.0f, 0.02f)) return lower;
+  cx.eval();
+  return fabsf(small ? scene_distance_leaves(S, p, leaf, second, second_lb, cx).d : scene_distance_bvh(S, p, cx).d);
+}
+
 // shadow_visibility (R:4706-4733) of every queued shadow job, one step per
 // iteration; the radiance gets contribution x visibility.
 template <bool kBatch, bool kStats>
@@ -425,8 +461,7 @@ __global__ void __launch_bounds__(128, 8) wf_shadow_persistent(DevScene S0, RayP
       continue;
     }
     F3 p = o + d * t;
-    float lower = fabsf(scene_lower_bound(S, p, cx));
-    float h = lower > fmaxf(eps * 8.0f, 0.02f) ? lower : fabsf(scene_distance_inl(S, p, cx).d);
+    const float h = shadow_step_h(S, p, eps, cx);
     if (h < eps * 4.0f) {
       finish(0.0f);
       continue;

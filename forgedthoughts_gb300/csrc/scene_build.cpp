@@ -752,6 +752,7 @@ class Builder {
       for (uint32_t o : row_offsets[row]) img_->ur_cell_offsets.push_back(base + o);
       img_->ur_cell_prims.insert(img_->ur_cell_prims.end(), row_prims[row].begin(), row_prims[row].end());
       img_->ur_cell_gaps.insert(img_->ur_cell_gaps.end(), row_gaps[row].begin(), row_gaps[row].end());
+      for (int32_t pos : row_prims[row]) img_->ur_cell_nodes.push_back(img_->ur_prims[t.prim_first + pos]);
     }
     img_->ur_cell_offsets.push_back(static_cast<uint32_t>(img_->ur_cell_prims.size()));
   }

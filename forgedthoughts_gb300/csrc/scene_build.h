@@ -82,6 +82,9 @@ struct SceneImage {
   // per ur_cell_prims entry: a lower bound of the distance from any point of
   // the cell to the primitive's box (the lists are sorted by it)
   std::vector<float> ur_cell_gaps;
+  // per ur_cell_prims entry: the primitive's node index (ur_prims of it), so
+  // the candidate walk loads it beside the position instead of after it
+  std::vector<int32_t> ur_cell_nodes;
   // parent links of the union_round trees, (parent ur_inner index << 1) |
   // side, -1 at the root: per ur_inner node and per primitive position
   std::vector<int32_t> ur_inner_up;
