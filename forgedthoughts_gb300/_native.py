@@ -125,7 +125,8 @@ class BuildInfoC(ctypes.Structure):
     _fields_ = [("leaves", ctypes.c_uint32), ("primitive_leaves", ctypes.c_uint32),
                 ("generic_leaves", ctypes.c_uint32), ("union_round_leaves", ctypes.c_uint32),
                 ("bvh_nodes", ctypes.c_uint32), ("grid_cells", ctypes.c_uint64), ("grid_entries", ctypes.c_uint64),
-                ("grid_max_list", ctypes.c_uint32), ("generic_ops", ctypes.c_uint32), ("build_ms", ctypes.c_double)]
+                ("grid_max_list", ctypes.c_uint32), ("generic_ops", ctypes.c_uint32), ("build_ms", ctypes.c_double),
+                ("outer_grid_cells", ctypes.c_uint64), ("outer_grid_entries", ctypes.c_uint64)]
 
 
 class RenderStatsC(ctypes.Structure):

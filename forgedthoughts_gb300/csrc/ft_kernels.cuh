@@ -42,6 +42,10 @@ struct DevUrTree {
   float cell, inv_cell;
   int32_t dims[3];
   int32_t cell_first, pad;
+  float ogmin[3];
+  float ocell, oinv_cell;
+  int32_t odims[3];
+  int32_t ocell_first, opad;
 };
 struct DevUrBvh {
   float bmin[3], bmax[3];
@@ -399,14 +403,27 @@ __device__ __forceinline__ Info eval_urtree(const DevScene& S, const DevUrTree& 
   // evaluator is inlined once.  The cell list is sorted by a lower bound of
   // the box bound of its points, so the first entry at or above the running
   // limit ends it: every later primitive would be skipped by that test.
+  // Outside the fine grid, the coarser outer grid around it (its cells list
+  // the primitives that can be the nearest there), else the BVH.
   float gx = (p.x - t.gmin[0]) * t.inv_cell, gy = (p.y - t.gmin[1]) * t.inv_cell, gz = (p.z - t.gmin[2]) * t.inv_cell;
-  const bool in_grid = t.dims[0] > 0 && gx >= 0.0f && gy >= 0.0f && gz >= 0.0f && gx < (float)t.dims[0] &&
-                       gy < (float)t.dims[1] && gz < (float)t.dims[2];
+  int gd0 = t.dims[0], gd1 = t.dims[1], gd2 = t.dims[2], gfirst = t.cell_first;
+  bool in_grid = gd0 > 0 && gx >= 0.0f && gy >= 0.0f && gz >= 0.0f && gx < (float)gd0 && gy < (float)gd1 &&
+                 gz < (float)gd2;
+  if (!in_grid && t.odims[0] > 0) {
+    gx = (p.x - t.ogmin[0]) * t.oinv_cell;
+    gy = (p.y - t.ogmin[1]) * t.oinv_cell;
+    gz = (p.z - t.ogmin[2]) * t.oinv_cell;
+    gd0 = t.odims[0];
+    gd1 = t.odims[1];
+    gd2 = t.odims[2];
+    gfirst = t.ocell_first;
+    in_grid = gx >= 0.0f && gy >= 0.0f && gz >= 0.0f && gx < (float)gd0 && gy < (float)gd1 && gz < (float)gd2;
+  }
   uint32_t k = 0, end = 0;  // the cell list, or the primitives of the BVH leaf being walked
   const int32_t* list = S.ur_bvh_prims;
   if (in_grid) {
-    int ix = min((int)gx, t.dims[0] - 1), iy = min((int)gy, t.dims[1] - 1), iz = min((int)gz, t.dims[2] - 1);
-    int cell = t.cell_first + ix + t.dims[0] * (iy + t.dims[1] * iz);
+    int ix = min((int)gx, gd0 - 1), iy = min((int)gy, gd1 - 1), iz = min((int)gz, gd2 - 1);
+    int cell = gfirst + ix + gd0 * (iy + gd1 * iz);
     k = S.ur_cell_offsets[cell];
     end = S.ur_cell_offsets[cell + 1];
     list = S.ur_cell_prims;

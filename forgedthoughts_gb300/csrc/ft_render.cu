@@ -912,6 +912,10 @@ ft_status ft_scene_build_info(const ft_scene_desc* desc, ft_build_info* info) {
         info->grid_entries += len;
         info->grid_max_list = std::max(info->grid_max_list, len);
       }
+      if (t.odims[0] <= 0) continue;
+      uint64_t ocells = static_cast<uint64_t>(t.odims[0]) * t.odims[1] * t.odims[2];
+      info->outer_grid_cells += ocells;
+      info->outer_grid_entries += img.ur_cell_offsets[t.ocell_first + ocells] - img.ur_cell_offsets[t.ocell_first];
     }
   }
   info->generic_ops = static_cast<uint32_t>(img.gops.size());

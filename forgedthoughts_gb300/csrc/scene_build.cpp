@@ -553,8 +553,12 @@ class Builder {
   // size against rounding in the device's cell lookup.
   void build_ur_grid(HostUrTree& t) {
     const int np = t.n_prims;
-    std::vector<Box> pb(np);
-    std::vector<float> cx(np), cy(np), cz(np), rho(np), rad(np);
+    GridPrims g;
+    g.np = np;
+    g.pb.resize(np);
+    g.cx.resize(np); g.cy.resize(np); g.cz.resize(np); g.rho.resize(np); g.rad.resize(np);
+    std::vector<Box>& pb = g.pb;
+    std::vector<float>&cx = g.cx, &cy = g.cy, &cz = g.cz, &rho = g.rho, &rad = g.rad;
     Box all{};
     for (int k = 0; k < np; ++k) {
       const HostNode& n = img_->nodes[img_->ur_prims[t.prim_first + k]];
@@ -578,22 +582,71 @@ class Builder {
     int dims[3];
     for (int a = 0; a < 3; ++a) dims[a] = std::max(1, static_cast<int>(std::ceil(ext[a] / cell)));
     if (static_cast<int64_t>(dims[0]) * dims[1] * dims[2] > 2 * 262144) return;
+    int32_t first = 0;
+    if (!build_cells(t, g, all.mn, static_cast<float>(cell), dims, &first)) return;
     t.cell = static_cast<float>(cell);
     t.inv_cell = 1.0f / t.cell;
     std::memcpy(t.gmin, all.mn, sizeof(t.gmin));
     std::memcpy(t.dims, dims, sizeof(dims));
-    t.cell_first = static_cast<int32_t>(img_->ur_cell_offsets.size());
-    const double pad = double(t.cell) * 1.0e-3;
-    const double half = 0.5 * double(t.cell);
+    t.cell_first = first;
+    // The outer grid: the first grid's box widened by half its largest extent
+    // on every side, in coarser cells.  Points there are outside the first
+    // grid, hence at least 2r from every primitive box: each cell lists the
+    // primitives that can be the nearest, sorted by gap, as above (a walk of
+    // the tree's BVH from such points tests about six times as many boxes).
+    // Points outside both grids take the tree BVH.
+    const double widen = 0.5 * std::max({ext[0], ext[1], ext[2]});
+    Box outer = all;
+    for (int a = 0; a < 3; ++a) {
+      outer.mn[a] = static_cast<float>(double(all.mn[a]) - widen);
+      outer.mx[a] = static_cast<float>(double(all.mx[a]) + widen);
+    }
+    double oext[3] = {double(outer.mx[0]) - outer.mn[0], double(outer.mx[1]) - outer.mn[1],
+                      double(outer.mx[2]) - outer.mn[2]};
+    double otarget = std::min(double(1 << 19), std::max(32768.0, 256.0 * np));
+    double ocell = std::cbrt(oext[0] * oext[1] * oext[2] / otarget);
+    if (!(ocell > 0.0) || !std::isfinite(ocell)) return;
+    int odims[3];
+    for (int a = 0; a < 3; ++a) odims[a] = std::max(1, static_cast<int>(std::ceil(oext[a] / ocell)));
+    if (static_cast<int64_t>(odims[0]) * odims[1] * odims[2] > 2 * (1 << 19)) return;
+    if (!build_cells(t, g, outer.mn, static_cast<float>(ocell), odims, &first)) return;
+    t.ocell = static_cast<float>(ocell);
+    t.oinv_cell = 1.0f / t.ocell;
+    std::memcpy(t.ogmin, outer.mn, sizeof(t.ogmin));
+    std::memcpy(t.odims, odims, sizeof(odims));
+    t.ocell_first = first;
+  }
+
+  // Primitive data of one union_round tree for its candidate grids.
+  struct GridPrims {
+    int np = 0;
+    std::vector<Box> pb;
+    std::vector<float> cx, cy, cz, rho, rad;
+  };
+
+  // Candidate lists of the dims[0] x dims[1] x dims[2] cells of size `cell`
+  // from `gmin`: each cell lists every primitive that can be the nearest or
+  // lie within r of one of its points, sorted by a lower bound of its box gap.
+  // Appended to the image's cell arrays, the first cell's offset index in
+  // *cell_first; false, with nothing appended, when the image's entry cap
+  // would be passed.
+  bool build_cells(const HostUrTree& t, const GridPrims& g, const float gmin[3], float cell, const int dims[3],
+                   int32_t* cell_first) {
+    const int np = g.np;
+    const std::vector<Box>& pb = g.pb;
+    const std::vector<float>&cx = g.cx, &cy = g.cy, &cz = g.cz, &rho = g.rho, &rad = g.rad;
+    const double pad = double(cell) * 1.0e-3;
+    const double half = 0.5 * double(cell);
     // Absolute rounding allowance of the block bounds below: far above the
     // error of a few double operations on the scene's coordinates.
     double scale = 0.0;
-    for (int a = 0; a < 3; ++a) scale = std::max({scale, std::fabs(double(all.mn[a])), std::fabs(double(all.mx[a]))});
+    for (int a = 0; a < 3; ++a)
+      scale = std::max({scale, std::fabs(double(gmin[a])), std::fabs(double(gmin[a]) + double(dims[a]) * double(cell))});
     const double slack = 1e-9 * (1.0 + scale);
     // Padded extent of the cells [i0, i1) along axis a (one cell: i1 = i0 + 1).
     auto extent = [&](int a, int i0, int i1, double* lo, double* hi) {
-      *lo = double(t.gmin[a]) + double(i0) * double(t.cell) - pad;
-      *hi = double(t.gmin[a]) + double(i1) * double(t.cell) + pad;
+      *lo = double(gmin[a]) + double(i0) * double(cell) - pad;
+      *hi = double(gmin[a]) + double(i1) * double(cell) + pad;
     };
     // Cells are taken in blocks of kGridBlock^3.  For a block, T bounds every
     // cell's min_j ub(j, C) from above (the smallest ub of any one primitive
@@ -743,10 +796,8 @@ class Builder {
     if (pool.empty()) drain();
     for (auto& th : pool) th.join();
     if (failure) std::rethrow_exception(failure);
-    if (over.load()) {
-      t.dims[0] = t.dims[1] = t.dims[2] = 0;
-      return;
-    }
+    if (over.load()) return false;
+    *cell_first = static_cast<int32_t>(img_->ur_cell_offsets.size());
     for (size_t row = 0; row < nrows; ++row) {
       uint32_t base = static_cast<uint32_t>(img_->ur_cell_prims.size());
       for (uint32_t o : row_offsets[row]) img_->ur_cell_offsets.push_back(base + o);
@@ -755,6 +806,7 @@ class Builder {
       for (int32_t pos : row_prims[row]) img_->ur_cell_nodes.push_back(img_->ur_prims[t.prim_first + pos]);
     }
     img_->ur_cell_offsets.push_back(static_cast<uint32_t>(img_->ur_cell_prims.size()));
+    return true;
   }
 
   bool build_urtree(HostLeaf& leaf, float r, int depth) {

@@ -53,6 +53,14 @@ struct HostUrTree {
   int32_t dims[3];
   int32_t cell_first;  // into ur_cell_offsets (dims product + 1 entries)
   int32_t pad;
+  // Outer grid: coarser cells over a box around the first grid, for points
+  // outside it (there every primitive is at least 2r away, so a cell lists
+  // the primitives that can be the nearest).  odims[0] == 0: none.
+  float ogmin[3];
+  float ocell, oinv_cell;
+  int32_t odims[3];
+  int32_t ocell_first;
+  int32_t opad;
 };
 
 struct HostUrBvh {

@@ -393,6 +393,8 @@ typedef struct ft_build_info {
   uint32_t grid_max_list;
   uint32_t generic_ops;
   double build_ms;            /* host time to build the structures */
+  uint64_t outer_grid_cells;  /* the coarser grids around the union_round trees' grids */
+  uint64_t outer_grid_entries;
 } ft_build_info;
 
 ft_status ft_scene_build_info(const ft_scene_desc* desc, ft_build_info* info);

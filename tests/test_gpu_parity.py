@@ -53,6 +53,31 @@ def test_union_round_field_reduced(accel):
     assert (img.material[both] == mat[both]).mean() >= 0.999
 
 
+def test_union_round_distance_in_every_grid_region():
+    """The union_round tree's value at points inside its fine candidate grid,
+    in the coarser outer grid around it and beyond both (the tree BVH): the
+    GPU's exact FP32 distance against the f32 oracle, which folds all 512
+    primitives at every point."""
+    import ctypes
+
+    w = workloads.union_round_field(width=64, height=36, aa=1)
+    st = ft.parse_and_eval(w.source)
+    info = _native.BuildInfoC()
+    assert _native.lib().ft_scene_build_info(st.desc_ptr, ctypes.byref(info)) == 0
+    assert info.grid_cells > 0 and info.outer_grid_cells > 0
+    g = st.gpu()
+    g.build_bricks()
+    rng = np.random.default_rng(11)
+    inner = rng.uniform([-7.0, -0.5, -7.0], [7.0, 4.0, 7.0], size=(40_000, 3))
+    outer = rng.uniform([-13.0, -0.5, -13.0], [13.0, 10.0, 13.0], size=(40_000, 3))
+    beyond = rng.uniform([-40.0, -0.5, -40.0], [40.0, 30.0, 40.0], size=(20_000, 3))
+    pts = np.concatenate([inner, outer, beyond]).astype(np.float32)
+    _, exact = g.brick_bounds(pts)
+    ref, _, _ = oracle.distance(st, pts, accel=1, precision=32)
+    err = np.abs(exact.astype(np.float64) - ref)
+    assert (err <= 1e-5 * np.maximum(1.0, np.abs(ref))).all(), float(err.max())
+
+
 def test_union_round_field_full_size_rows():
     """1920x1080 with the 2x2 AA grid: GPU frame against oracle rows."""
     w = workloads.union_round_field()
