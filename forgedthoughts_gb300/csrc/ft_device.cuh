@@ -91,8 +91,27 @@ __device__ __noinline__ float sd_regular_ngon(float px, float pz, int sides, flo
   return hypotf(px, pz) * cosf(wrapped) - apothem;
 }
 
+__device__ __noinline__ float prim_local_rare(int kind, const float* f, int ival, F3 q);
+
 // Primitive arms of sdf_distance_info (R:5547-5663), point already local.
+// Spheres and boxes inline; the other kinds out of line.
 FT_DEV float prim_local(int kind, const float* f, int ival, F3 q) {
+  switch (kind) {
+    case FT_NODE_SPHERE: return shell(len3(q) - f[0], f[1]);
+    case FT_NODE_BOX: {
+      float rd = f[3];
+      float ix = rmax(f[0] - rd, 0.0f), iy = rmax(f[1] - rd, 0.0f), iz = rmax(f[2] - rd, 0.0f);
+      float qx = fabsf(q.x) - ix, qy = fabsf(q.y) - iy, qz = fabsf(q.z) - iz;
+      float ox = rmax(qx, 0.0f), oy = rmax(qy, 0.0f), oz = rmax(qz, 0.0f);
+      float outside = sqrtf(ox * ox + oy * oy + oz * oz);
+      float inside = rmin(rmax(rmax(qx, qy), qz), 0.0f);
+      return shell(outside + inside - rd, f[4]);
+    }
+    default: return prim_local_rare(kind, f, ival, q);
+  }
+}
+
+__device__ __noinline__ float prim_local_rare(int kind, const float* f, int ival, F3 q) {
   switch (kind) {
     case FT_NODE_SPHERE: return shell(len3(q) - f[0], f[1]);
     case FT_NODE_BOX: {

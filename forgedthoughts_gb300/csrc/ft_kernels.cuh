@@ -359,9 +359,11 @@ __device__ __forceinline__ Info ur_fold_small(const DevScene& S, const DevUrTree
   return v0;
 }
 
-template <bool kStats>
-__device__ __forceinline__ Info eval_urtree(const DevScene& S, const DevUrTree& t, F3 p, float cutoff,
-                                            Ctx<kStats>& cx) {
+// The candidate walk and fold of eval_urtree: over the cell list [k, end)
+// (kFar false) or over the tree's BVH (kFar true).
+template <bool kStats, bool kFar>
+__device__ __forceinline__ Info eval_urtree_walk(const DevScene& S, const DevUrTree& t, F3 p, float cutoff,
+                                                 uint32_t k, uint32_t end, Ctx<kStats>& cx) {
   const float r = t.r;
   // near set: the first two entries in registers, the rest (rare) in arrays
   int np0 = 0, np1 = 0;
@@ -398,38 +400,15 @@ __device__ __forceinline__ Info eval_urtree(const DevScene& S, const DevUrTree& 
   };
   int stack[48];
   int sp = 0;
-  // Candidates come from one cell list of the grid or, outside the grid, from
-  // the tree's BVH.  Both feed a single `consider` site, so the primitive
-  // evaluator is inlined once.  The cell list is sorted by a lower bound of
-  // the box bound of its points, so the first entry at or above the running
-  // limit ends it: every later primitive would be skipped by that test.
-  // Outside the fine grid, the coarser outer grid around it (its cells list
-  // the primitives that can be the nearest there), else the BVH.
-  float gx = (p.x - t.gmin[0]) * t.inv_cell, gy = (p.y - t.gmin[1]) * t.inv_cell, gz = (p.z - t.gmin[2]) * t.inv_cell;
-  int gd0 = t.dims[0], gd1 = t.dims[1], gd2 = t.dims[2], gfirst = t.cell_first;
-  bool in_grid = gd0 > 0 && gx >= 0.0f && gy >= 0.0f && gz >= 0.0f && gx < (float)gd0 && gy < (float)gd1 &&
-                 gz < (float)gd2;
-  if (!in_grid && t.odims[0] > 0) {
-    gx = (p.x - t.ogmin[0]) * t.oinv_cell;
-    gy = (p.y - t.ogmin[1]) * t.oinv_cell;
-    gz = (p.z - t.ogmin[2]) * t.oinv_cell;
-    gd0 = t.odims[0];
-    gd1 = t.odims[1];
-    gd2 = t.odims[2];
-    gfirst = t.ocell_first;
-    in_grid = gx >= 0.0f && gy >= 0.0f && gz >= 0.0f && gx < (float)gd0 && gy < (float)gd1 && gz < (float)gd2;
-  }
-  uint32_t k = 0, end = 0;  // the cell list, or the primitives of the BVH leaf being walked
-  const int32_t* list = S.ur_bvh_prims;
-  if (in_grid) {
-    int ix = min((int)gx, gd0 - 1), iy = min((int)gy, gd1 - 1), iz = min((int)gz, gd2 - 1);
-    int cell = gfirst + ix + gd0 * (iy + gd1 * iz);
-    k = S.ur_cell_offsets[cell];
-    end = S.ur_cell_offsets[cell + 1];
-    list = S.ur_cell_prims;
-  } else {
-    stack[sp++] = t.bvh_root;
-  }
+  // Candidates come from one cell list of the grid or, outside the grids,
+  // from the tree's BVH.  Both feed a single `consider` site, so the
+  // primitive evaluator is inlined once.  The cell list is sorted by a lower
+  // bound of the box bound of its points, so the first entry at or above the
+  // running limit ends it: every later primitive would be skipped by that
+  // test.
+  constexpr bool in_grid = !kFar;
+  const int32_t* list = kFar ? S.ur_bvh_prims : S.ur_cell_prims;
+  if (kFar) stack[sp++] = t.bvh_root;
   for (int walk = 0; walk < ftgpu::kMaxWalk; ++walk) {  // each list entry and BVH node is visited once
     if (k < end) {
       if (in_grid) {
@@ -473,6 +452,39 @@ __device__ __forceinline__ Info eval_urtree(const DevScene& S, const DevUrTree& 
   near_pos[0] = np0; near_info[0] = ni0;
   near_pos[1] = np1; near_info[1] = ni1;
   return ur_fold(S, t, near_pos, near_info, nn, cx);
+}
+
+// Points outside both candidate grids walk the tree's BVH, out of line: it is
+// rare beside the grids' cell walks, whose code stays in the march loops.
+template <bool kStats>
+__device__ __noinline__ Info eval_urtree_far(const DevScene& S, const DevUrTree& t, F3 p, float cutoff,
+                                             Ctx<kStats>& cx) {
+  return eval_urtree_walk<kStats, true>(S, t, p, cutoff, 0u, 0u, cx);
+}
+
+template <bool kStats>
+__device__ __forceinline__ Info eval_urtree(const DevScene& S, const DevUrTree& t, F3 p, float cutoff,
+                                            Ctx<kStats>& cx) {
+  // The fine grid, outside it the coarser outer grid around it (its cells
+  // list the primitives that can be the nearest there), else the BVH.
+  float gx = (p.x - t.gmin[0]) * t.inv_cell, gy = (p.y - t.gmin[1]) * t.inv_cell, gz = (p.z - t.gmin[2]) * t.inv_cell;
+  int gd0 = t.dims[0], gd1 = t.dims[1], gd2 = t.dims[2], gfirst = t.cell_first;
+  bool in_grid = gd0 > 0 && gx >= 0.0f && gy >= 0.0f && gz >= 0.0f && gx < (float)gd0 && gy < (float)gd1 &&
+                 gz < (float)gd2;
+  if (!in_grid && t.odims[0] > 0) {
+    gx = (p.x - t.ogmin[0]) * t.oinv_cell;
+    gy = (p.y - t.ogmin[1]) * t.oinv_cell;
+    gz = (p.z - t.ogmin[2]) * t.oinv_cell;
+    gd0 = t.odims[0];
+    gd1 = t.odims[1];
+    gd2 = t.odims[2];
+    gfirst = t.ocell_first;
+    in_grid = gx >= 0.0f && gy >= 0.0f && gz >= 0.0f && gx < (float)gd0 && gy < (float)gd1 && gz < (float)gd2;
+  }
+  if (!in_grid) return eval_urtree_far(S, t, p, cutoff, cx);
+  const int ix = min((int)gx, gd0 - 1), iy = min((int)gy, gd1 - 1), iz = min((int)gz, gd2 - 1);
+  const int cell = gfirst + ix + gd0 * (iy + gd1 * iz);
+  return eval_urtree_walk<kStats, false>(S, t, p, cutoff, S.ur_cell_offsets[cell], S.ur_cell_offsets[cell + 1], cx);
 }
 
 // Restricted union_round fold over the subtrees holding near primitives
@@ -1278,7 +1290,7 @@ __device__ __forceinline__ void shade_hit(const DevScene& S, const RayParams& P,
   if (rs.ok && rs.split) {
     float tt = clamp01(rs.t);  // lerp_spectrum(a, b, t): a (1 - t) + b t
     if (tt != 1.0f) { mats[nm] = &rs.m; ws[nm++] = 1.0f - tt; }
-    if (tt != 0.0f) { mats[nm] = &rs.mb; ws[nm++] = tt; }
+    if (tt != 0.0f) { mats[nm] = rs.mb_same ? &rs.m : &rs.mb; ws[nm++] = tt; }
   } else {
     if (!rs.ok) rs.m = mat_of_id(S, h.mat);
     mats[0] = &rs.m;

@@ -461,10 +461,11 @@ __device__ F3 custom_normal(const DevScene& S, const DevNode& n, F3 p) {
 // oriented to the front face), material, and the optional root split.
 struct Resolved {
   F3 normal;
-  DMat m;      // material (or the split's left material)
-  DMat mb;     // split's right material
-  float t;     // split weight
+  DMat m;       // material (or the split's left material)
+  DMat mb;      // split's right material, unless mb_same
+  float t;      // split weight
   bool split;
+  bool mb_same;  // the split's right material is m (a root with one weighted child)
   bool ok;
 };
 
@@ -558,6 +559,7 @@ __device__ __noinline__ void resolve_generic(const DevScene& S, int root, F3 p, 
         if (top == 0 && split_root) {  // smooth boolean at the leaf root: material split
           out->m = l.m;
           out->mb = r.m;
+          out->mb_same = false;
           out->t = t;
           out->split = true;
         }
@@ -761,10 +763,11 @@ __device__ __noinline__ bool resolve_urtree_reach(const DevScene& S, const DevUr
           out->normal = blend_normals(L.n, carry.n, F.tw, false);
           out->m = L.m;
           out->mb = carry.m;
+          out->mb_same = false;
         } else {
           out->normal = blend_normals(carry.n, carry.n, F.tw, false);
-          out->m = carry.m;
-          out->mb = carry.m;
+          out->m = carry.m;  // the one material, not written twice
+          out->mb_same = true;
         }
         out->t = F.tw;
         out->split = true;
