@@ -401,7 +401,8 @@ __device__ __forceinline__ float shadow_step_h(const DevScene& S, F3 p, float ep
   lower = fabsf(lower);
   if (lower > fmaxf(eps * 8.0f, 0.02f)) return lower;
   cx.eval();
-  return fabsf(small ? scene_distance_leaves(S, p, leaf, second, second_lb, cx).d : scene_distance_bvh(S, p, cx).d);
+  return fabsf(small ? scene_distance_leaves<kStats, false>(S, p, leaf, second, second_lb, cx).d
+                     : scene_distance_bvh(S, p, cx).d);
 }
 
 // shadow_visibility (R:4706-4733) of every queued shadow job, one step per
