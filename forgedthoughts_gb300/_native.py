@@ -53,8 +53,9 @@ FT_MAT_STANDARD, FT_MAT_LAMBERT, FT_MAT_METAL, FT_MAT_DIELECTRIC = 0, 1, 2, 3  #
  FT_HOOK_TRANSMISSION, FT_HOOK_COAT_COLOR, FT_HOOK_COAT_ROUGHNESS, FT_HOOK_COAT_IOR, FT_HOOK_COAT_WEIGHT,
  FT_HOOK_COAT_MASK, FT_HOOK_BUMP, FT_HOOK_NORMAL, FT_HOOK_EVAL, FT_HOOK_PDF, FT_HOOK_SAMPLE_WI, FT_HOOK_SAMPLE_F,
  FT_HOOK_SAMPLE_PDF, FT_HOOK_SAMPLE_DELTA, FT_HOOK_SAMPLE_APPLY_COS, FT_HOOK_SAMPLE_TRANSMISSION,
- FT_HOOK_SAMPLE_THIN_WALLED, FT_HOOK_SAMPLE_NEXT_IOR) = range(23)
-FT_MATERIAL_HOOKS = 23
+ FT_HOOK_SAMPLE_THIN_WALLED, FT_HOOK_SAMPLE_NEXT_IOR, FT_HOOK_MEDIUM_IOR, FT_HOOK_MEDIUM_ABSORPTION,
+ FT_HOOK_MEDIUM_DENSITY) = range(26)
+FT_MATERIAL_HOOKS, FT_MATERIAL_HOOK_SLOTS = 26, 32
 FT_MATERIAL_HOOK_PARAMS, FT_BSDF_HOOK_PARAMS = 7, 13
 FT_MATERIAL_HOOK_PARAMS = 7
 FT_ABI_VERSION = 4
@@ -102,7 +103,7 @@ class MaterialC(ctypes.Structure):
                 ("specular_weight", ctypes.c_float), ("specular_color", ctypes.c_float * 3),
                 ("clearcoat", ctypes.c_float), ("clearcoat_roughness", ctypes.c_float),
                 ("roughness_program", ctypes.c_int32), ("ior_program", ctypes.c_int32),
-                ("thin_walled_program", ctypes.c_int32), ("hook_program", ctypes.c_int32 * 24)]
+                ("thin_walled_program", ctypes.c_int32), ("hook_program", ctypes.c_int32 * 32)]
 
 
 class CameraC(ctypes.Structure):

@@ -1047,8 +1047,11 @@ class Lowerer {
     // definition's specular colour, IOR, clearcoat and clearcoat roughness are
     // the coat's at every hit whatever their own hooks return, so those hooks
     // are left out; metallic, specular, specular_weight, transmission and the
-    // coat hooks are read for those two models only.  `fn medium(ctx)` and
-    // `fn subsurface(ctx)` are not lowered.
+    // coat hooks are read for those two models only.  `fn medium(ctx)`'s record
+    // is one program per field; a record with none of the three fields is not
+    // lowered (the reference would take a medium of the defaults).
+    // `fn subsurface(ctx)` is not lowered: no renderer path reads subsurface
+    // parameters.
     const bool coated = model == "Standard" || model == "Layered";
     struct Slot {
       const char* name;
@@ -1103,6 +1106,15 @@ class Lowerer {
         m.hook_program[FT_HOOK_EVAL] = add(st, 2, true, false, nullptr);
       } else if (st.name == "pdf") {
         m.hook_program[FT_HOOK_PDF] = add(st, 0, true, false, nullptr);
+      } else if (st.name == "medium") {
+        // medium_from_value (R:6834-6845): ior, absorption_color and density,
+        // each defaulted when the record lacks it
+        const int32_t ior = add(st, 0, false, false, "ior");
+        const int32_t absorption = add(st, 2, false, false, "absorption_color");
+        const int32_t density = add(st, 0, false, false, "density");
+        m.hook_program[FT_HOOK_MEDIUM_IOR] = ior;
+        m.hook_program[FT_HOOK_MEDIUM_ABSORPTION] = absorption;
+        m.hook_program[FT_HOOK_MEDIUM_DENSITY] = density;
       } else if (st.name == "sample") {
         int32_t progs[8];
         bool ok = true;

@@ -115,6 +115,8 @@ __device__ __forceinline__ bool has_leaf_hooks(const ft_material& fm) {
     return true;
   for (int k = FT_HOOK_EMISSION_COLOR; k <= FT_HOOK_COAT_MASK; ++k)
     if (fm.hook_program[k] >= 0) return true;
+  for (int k = FT_HOOK_MEDIUM_IOR; k <= FT_HOOK_MEDIUM_DENSITY; ++k)
+    if (fm.hook_program[k] >= 0) return true;
   return false;
 }
 __device__ __forceinline__ F3 hook_colour(const DevScene& S, int prog, const F3* args) {
@@ -151,6 +153,14 @@ __device__ DMat mat_of_leaf(const DevScene& S, const DevNode& pn, const HookCtx&
     const float w = hp[FT_HOOK_COAT_WEIGHT] >= 0 ? clamp01(num(FT_HOOK_COAT_WEIGHT)) : m.a.clearcoat;
     const float k = hp[FT_HOOK_COAT_MASK] >= 0 ? clamp01(num(FT_HOOK_COAT_MASK)) : 1.0f;
     m.a.clearcoat = clamp01(w * k);
+  }
+  if (hp[FT_HOOK_MEDIUM_IOR] >= 0 || hp[FT_HOOK_MEDIUM_ABSORPTION] >= 0 || hp[FT_HOOK_MEDIUM_DENSITY] >= 0) {
+    // `fn medium(ctx)` replaces the material's medium (medium_from_value, R:6834-6845)
+    m.a.has_medium = 1;
+    m.a.medium_ior = hp[FT_HOOK_MEDIUM_IOR] >= 0 ? ftd::rclamp(num(FT_HOOK_MEDIUM_IOR), 1.0f, 3.0f) : 1.0f;
+    m.a.medium_absorption =
+        hp[FT_HOOK_MEDIUM_ABSORPTION] >= 0 ? hook_colour(S, hp[FT_HOOK_MEDIUM_ABSORPTION], args) : f3(1.0f, 1.0f, 1.0f);
+    m.a.medium_density = hp[FT_HOOK_MEDIUM_DENSITY] >= 0 ? fmaxf(num(FT_HOOK_MEDIUM_DENSITY), 0.0f) : 0.0f;
   }
   m.b = m.a;
   return m;

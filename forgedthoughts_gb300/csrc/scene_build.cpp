@@ -210,9 +210,11 @@ class Builder {
                                  {m.ior_program, false, 0}, {m.thin_walled_program, false, 0}};
       static const int kResult[FT_MATERIAL_HOOKS] = {2, 0, 0, 0, 0, 0, 2, 0, 0, 0, 0, 0, 1,  // properties, bump, normal
                                                      2, 0,                                  // eval, pdf
-                                                     1, 2, 0, 0, 0, 0, 0, 0};               // sample fields
-      for (int k = 0; k < FT_MATERIAL_HOOKS; ++k) wants.push_back({m.hook_program[k], k >= FT_HOOK_EVAL, kResult[k]});
-      for (int k = FT_MATERIAL_HOOKS; k < 24; ++k)
+                                                     1, 2, 0, 0, 0, 0, 0, 0,                // sample fields
+                                                     0, 2, 0};                              // medium fields
+      for (int k = 0; k < FT_MATERIAL_HOOKS; ++k)
+        wants.push_back({m.hook_program[k], k >= FT_HOOK_EVAL && k <= FT_HOOK_SAMPLE_NEXT_IOR, kResult[k]});
+      for (int k = FT_MATERIAL_HOOKS; k < FT_MATERIAL_HOOK_SLOTS; ++k)
         if (m.hook_program[k] != -1) return fail("material " + std::to_string(i) + " uses a reserved hook slot");
       for (const Want& w : wants) {
         if (w.prog < 0) continue;

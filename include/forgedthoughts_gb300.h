@@ -216,6 +216,9 @@ typedef enum ft_material_kind {
   FT_MAT_DIELECTRIC = 3
 } ft_material_kind;
 
+/* Slots of ft_material.hook_program (FT_MATERIAL_HOOKS used, the rest -1). */
+#define FT_MATERIAL_HOOK_SLOTS 32
+
 /* Subset of `MaterialParams` (crates/forgedthoughts/src/materials/mod.rs:66-86)
  * read by the Whitted integrator. */
 typedef struct ft_material {
@@ -241,7 +244,7 @@ typedef struct ft_material {
   int32_t roughness_program;  /* per-hit `fn roughness(ctx)` hook (number), -1 if none */
   int32_t ior_program;        /* per-hit `fn ior(ctx)` hook (number), -1 if none */
   int32_t thin_walled_program; /* per-hit `fn thin_walled(ctx)` hook (number, >= 0.5 thin), -1 if none */
-  int32_t hook_program[24];   /* the further hooks, indexed by ft_material_hook (23 used); -1 if none */
+  int32_t hook_program[FT_MATERIAL_HOOK_SLOTS]; /* the further hooks by ft_material_hook; -1 if none */
 } ft_material;
 
 /* The further hooks of a material definition (crates/forgedthoughts/src/
@@ -256,7 +259,11 @@ typedef struct ft_material {
  *                       ([0, 1]), coat_ior ([1, 3]), coat_weight and
  *                       coat_mask ([0, 1]), which replace the specular
  *                       colour, IOR, clearcoat (weight x mask) and clearcoat
- *                       roughness at every hit (R:7397-7468).
+ *                       roughness at every hit (R:7397-7468);
+ *   every definition    `fn medium(ctx)` (a Medium record; its ior, absorption_color
+ *                       and density fields one program each, defaulted and clamped
+ *                       as medium_from_value, R:6834-6845), replacing the
+ *                       material's medium (R:7217-7226).
  * The shading-normal hooks (build_bsdf_context, R:4397-4449) belong to the
  * hit's own material: `fn bump(ctx)` (number, a height field differentiated
  * along a tangent frame, R:7776-7818), then `fn normal(ctx)` (vec3,
@@ -292,7 +299,10 @@ typedef enum ft_material_hook {
   FT_HOOK_SAMPLE_TRANSMISSION = 20,
   FT_HOOK_SAMPLE_THIN_WALLED = 21,
   FT_HOOK_SAMPLE_NEXT_IOR = 22,
-  FT_MATERIAL_HOOKS = 23
+  FT_HOOK_MEDIUM_IOR = 23,
+  FT_HOOK_MEDIUM_ABSORPTION = 24,
+  FT_HOOK_MEDIUM_DENSITY = 25,
+  FT_MATERIAL_HOOKS = 26
 } ft_material_hook;
 
 /* Material hook programs take the shading context of a hit

@@ -1925,6 +1925,7 @@ class Tracer {
     const ft_material& fm = d.materials[n.material_id < d.n_materials ? n.material_id : 0];
     bool any = fm.color_program >= 0 || fm.roughness_program >= 0 || fm.ior_program >= 0 || fm.thin_walled_program >= 0;
     for (int k = FT_HOOK_EMISSION_COLOR; k <= FT_HOOK_COAT_MASK; ++k) any = any || fm.hook_program[k] >= 0;
+    for (int k = FT_HOOK_MEDIUM_IOR; k <= FT_HOOK_MEDIUM_DENSITY; ++k) any = any || fm.hook_program[k] >= 0;
     if (!any) return m;
     const R obj = R(n.object_id), mid = R(n.material_id);
     V<R> args[FT_MATERIAL_HOOK_PARAMS] = {hc.pos, S.to_local(hc.pos, n), hc.normal, hc.view,
@@ -1973,6 +1974,14 @@ class Tracer {
       R w = hp[FT_HOOK_COAT_WEIGHT] >= 0 ? rclamp(num(FT_HOOK_COAT_WEIGHT), R(0), R(1)) : m.p.clearcoat;
       R k = hp[FT_HOOK_COAT_MASK] >= 0 ? rclamp(num(FT_HOOK_COAT_MASK), R(0), R(1)) : R(1);
       m.p.clearcoat = rclamp(w * k, R(0), R(1));
+    }
+    // `fn medium(ctx)`: runtime_medium.or(base.medium) with medium_from_value's
+    // defaults and clamps (R:7217-7226, R:6834-6845)
+    if (hp[FT_HOOK_MEDIUM_IOR] >= 0 || hp[FT_HOOK_MEDIUM_ABSORPTION] >= 0 || hp[FT_HOOK_MEDIUM_DENSITY] >= 0) {
+      m.p.has_medium = true;
+      m.p.medium_ior = hp[FT_HOOK_MEDIUM_IOR] >= 0 ? rclamp(num(FT_HOOK_MEDIUM_IOR), R(1), R(3)) : R(1);
+      m.p.medium_absorption = hp[FT_HOOK_MEDIUM_ABSORPTION] >= 0 ? colour(FT_HOOK_MEDIUM_ABSORPTION) : sp(R(1), R(1), R(1));
+      m.p.medium_density = hp[FT_HOOK_MEDIUM_DENSITY] >= 0 ? rmax(num(FT_HOOK_MEDIUM_DENSITY), R(0)) : R(0);
     }
     return m;
   }

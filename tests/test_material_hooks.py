@@ -58,7 +58,7 @@ def test_custom_bsdf_hooks():
     # every field of the record is one program; eval and pdf take the BSDF context
     d = st.desc
     m = d.materials[1]
-    for slot in range(_native.FT_HOOK_EVAL, _native.FT_MATERIAL_HOOKS):
+    for slot in range(_native.FT_HOOK_EVAL, _native.FT_HOOK_SAMPLE_NEXT_IOR + 1):
         prog = m.hook_program[slot]
         assert prog >= 0, slot
         assert d.programs[prog].n_params == _native.FT_BSDF_HOOK_PARAMS
@@ -221,7 +221,47 @@ def test_bsdf_and_property_hook_programs_are_validated():
     assert rc == _native.FT_ERR_INVALID_ARGUMENT and "shading context" in _native.last_error()
 
     def reserved(mats, d):
-        mats[0].hook_program[23] = 0
+        mats[0].hook_program[_native.FT_MATERIAL_HOOK_SLOTS - 1] = 0
 
     rc, _ = _with_materials(st, reserved)
     assert rc == _native.FT_ERR_INVALID_ARGUMENT and "reserved" in _native.last_error()
+
+
+MEDIUM_HOOK = """
+material Smoky {
+  model: Dielectric;
+  ior = 1.5;
+  fn medium(ctx) {
+    return Medium {
+      ior: 1.4 + ctx.local_position.y * 0.2,
+      absorption_color: vec3(0.9, 0.5 + ctx.local_position.x, 0.3),
+      density: 2.0 + ctx.local_position.z
+    };
+  }
+};
+material Partial {
+  model: Dielectric;
+  fn medium(ctx) { return Medium { density: 5.0 }; }
+};
+let scene = Sphere { material: Smoky {} } + Sphere { pos: vec3(2.0, 0.0, 0.0), material: Partial {} };
+"""
+
+
+def test_medium_hook_is_lowered_field_by_field():
+    """`fn medium(ctx)` returns a Medium record: each of ior,
+    absorption_color and density is one program over the shading context,
+    and a field the record lacks is left to medium_from_value's default."""
+    st = ft.parse_and_eval(MEDIUM_HOOK)
+    d = st.desc
+    mats = [d.materials[i] for i in range(d.n_materials)]
+    smoky = next(m for m in mats if m.hook_program[_native.FT_HOOK_MEDIUM_ABSORPTION] >= 0)
+    partial = next(m for m in mats if m.hook_program[_native.FT_HOOK_MEDIUM_DENSITY] >= 0
+                   and m.hook_program[_native.FT_HOOK_MEDIUM_ABSORPTION] < 0)
+    assert partial.hook_program[_native.FT_HOOK_MEDIUM_IOR] == -1
+    args = np.zeros((1, _native.FT_MATERIAL_HOOK_PARAMS, 3), np.float32)
+    args[0, 1] = (0.1, 0.5, -0.25)  # local position
+    ev = lambda slot: oracle.eval_program(st, smoky.hook_program[slot], args)[0]
+    assert ev(_native.FT_HOOK_MEDIUM_IOR)[0] == pytest.approx(1.5, abs=1e-6)
+    assert np.allclose(ev(_native.FT_HOOK_MEDIUM_ABSORPTION), [0.9, 0.6, 0.3], atol=1e-6)
+    assert ev(_native.FT_HOOK_MEDIUM_DENSITY)[0] == pytest.approx(1.75, abs=1e-6)
+    assert d.programs[smoky.hook_program[_native.FT_HOOK_MEDIUM_IOR]].n_params == _native.FT_MATERIAL_HOOK_PARAMS

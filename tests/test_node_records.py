@@ -50,7 +50,7 @@ def hand_built_desc():
     m.specular_color[:] = [1.0, 1.0, 1.0]
     m.clearcoat_roughness = 0.1
     m.color_program = m.roughness_program = m.ior_program = m.thin_walled_program = -1
-    m.hook_program[:] = [-1] * 24
+    m.hook_program[:] = [-1] * _native.FT_MATERIAL_HOOK_SLOTS
     lights = (_native.LightC * 1)()
     lights[0].kind, lights[0].samples = _native.FT_LIGHT_POINT, 1
     lights[0].position[:] = [3.0, 6.0, -3.0]
