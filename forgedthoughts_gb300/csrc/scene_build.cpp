@@ -578,7 +578,7 @@ class Builder {
       all.mx[a] += 2.0f * t.r;
     }
     double ext[3] = {double(all.mx[0]) - all.mn[0], double(all.mx[1]) - all.mn[1], double(all.mx[2]) - all.mn[2]};
-    double target = std::min(262144.0, std::max(4096.0, 64.0 * np));
+    double target = std::min(262144.0, std::max(4096.0, 256.0 * np));
     double cell = std::cbrt(ext[0] * ext[1] * ext[2] / target);
     if (!(cell > 0.0) || !std::isfinite(cell)) return;
     int dims[3];

@@ -34,9 +34,9 @@ def test_union_round_candidate_grid():
 
 
 @pytest.mark.parametrize("n,seed,cells,entries,max_list", [
-    (512, 1, 34592, 230017, 25),
-    (200, 5, 13475, 76626, 21),
-    (64, 3, 4416, 18447, 15),
+    (512, 1, 135050, 639791, 23),
+    (200, 5, 54450, 218559, 17),
+    (64, 3, 18252, 54592, 12),
 ])
 def test_candidate_grid_matches_the_full_scan(n, seed, cells, entries, max_list):
     """The grid is built in blocks whose primitive subsets are pruned by
