@@ -777,7 +777,17 @@ class Builder {
     // calling thread does the work.
     std::exception_ptr failure;
     std::mutex failure_mu;
+    // Workers start together once all are running.  Each, and the calling
+    // thread, which rethrows a worker's failure, first touches the C++
+    // runtime's per-thread exception state: glibc allocates a loaded
+    // library's thread-local block on first use and aborts the process when
+    // that allocation fails, so it must not first happen in a throw after
+    // the workers have used up the memory.
+    (void)std::uncaught_exceptions();
+    std::atomic<bool> go{false};
     auto drain = [&]() {
+      (void)std::uncaught_exceptions();
+      while (!go.load(std::memory_order_acquire)) std::this_thread::yield();
       try {
         for (int it = next.fetch_add(1); it < items; it = next.fetch_add(1)) work(it);
       } catch (...) {
@@ -791,10 +801,11 @@ class Builder {
     for (unsigned i = 0; i < nthreads; ++i) {
       try {
         pool.emplace_back(drain);
-      } catch (const std::system_error&) {
+      } catch (...) {  // no thread (system_error) or no memory for its state
         break;
       }
     }
+    go.store(true, std::memory_order_release);
     if (pool.empty()) drain();
     for (auto& th : pool) th.join();
     if (failure) std::rethrow_exception(failure);

@@ -98,7 +98,14 @@ def test_host_allocation_failure_returns_a_status():
     threads, comes back as FT_ERR_OUT_OF_MEMORY: no C++ exception crosses the
     C ABI (an escaping one would abort the process).  The child process caps
     its address space 256 MB above its size, and the tree's grid needs more
-    than 500 MB before it reaches its entry cap."""
+    than 500 MB before it reaches its entry cap.  The child's allocator keeps
+    one arena: with one per worker thread, each reserving 64 MB of address
+    space under the cap, the allocation of a new thread's thread-local block
+    could be the one that fails, which glibc answers by ending the process
+    ("cannot allocate memory for thread-local data") rather than with a
+    status.  The builder's workers and its calling thread touch that block
+    before any of them allocates for the grid."""
+    import os
     import subprocess
     import sys
     from pathlib import Path
@@ -106,8 +113,9 @@ def test_host_allocation_failure_returns_a_status():
     if not Path("/proc/self/statm").exists():
         pytest.skip("needs /proc")
     here = Path(__file__).resolve().parent
+    env = dict(os.environ, MALLOC_ARENA_MAX="1", GLIBC_TUNABLES="glibc.malloc.arena_max=1")
     p = subprocess.run([sys.executable, "-c", _OOM_CHILD, str(here.parent), str(here)],
-                       capture_output=True, text=True, timeout=300)
+                       capture_output=True, text=True, timeout=300, env=env)
     assert p.returncode == 0, p.stderr[-2000:]
     rc, msg = p.stdout.strip().split(" ", 1)
     assert int(rc) == _native.FT_ERR_OUT_OF_MEMORY, p.stdout
