@@ -21,6 +21,7 @@ from __future__ import annotations
 import ctypes
 import dataclasses
 import enum
+import os
 import struct
 import zlib
 from pathlib import Path
@@ -33,6 +34,7 @@ from . import _native
 __all__ = [
     "AccelMode", "RenderOptions", "SceneState", "GpuScene", "DepthImage", "PreviewProgress", "RenderError",
     "MissingSceneRoot", "UnsupportedObjectType", "ExpectedObject", "ParseError", "EvalError", "CudaError",
+    "SceneIoError", "MissingImport", "ImportCycle",
     "parse_and_eval", "load_and_eval_scene", "extract_scene_render_settings", "render_depth",
     "render_depth_png_with_accel", "render_preview_progressive_with_accel", "write_png", "read_png",
 ]
@@ -98,8 +100,26 @@ class CudaError(RenderError):
     status = _native.FT_ERR_CUDA
 
 
+class SceneIoError(RenderError):
+    """A scene file could not be read (``CoreError::Io``, lib.rs:251-256)."""
+
+    status = _native.FT_ERR_IO
+
+
+class MissingImport(RenderError):
+    """A relative import names no file (``CoreError::MissingImport``)."""
+
+    status = _native.FT_ERR_MISSING_IMPORT
+
+
+class ImportCycle(RenderError):
+    """A file imports itself through a chain of imports (``CoreError::ImportCycle``)."""
+
+    status = _native.FT_ERR_IMPORT_CYCLE
+
+
 _ERRORS = {cls.status: cls for cls in (MissingSceneRoot, UnsupportedObjectType, ExpectedObject, ParseError,
-                                       EvalError, CudaError, JitError)}
+                                       EvalError, CudaError, JitError, SceneIoError, MissingImport, ImportCycle)}
 
 
 def _check(status: int) -> None:
@@ -133,13 +153,18 @@ class SceneState:
     GPU copy is created on first use and cached.
     """
 
-    def __init__(self, source: str):
+    def __init__(self, source: Optional[str] = None, path=None):
         lib = _native.lib()
         ptr = ctypes.POINTER(_native.SceneDescC)()
-        _check(lib.ft_scene_desc_from_source(source.encode("utf-8"), ctypes.byref(ptr)))
         self._desc = ptr
         self._gpu: Optional[GpuScene] = None
+        if path is not None:
+            _check(lib.ft_scene_desc_from_file(os.fsencode(path), ctypes.byref(ptr)))
+        else:
+            _check(lib.ft_scene_desc_from_source(source.encode("utf-8"), ctypes.byref(ptr)))
+        self._desc = ptr
         self.source = source
+        self.path = path
 
     @property
     def desc_ptr(self):
@@ -178,7 +203,8 @@ def parse_and_eval(source: str) -> SceneState:
 
 
 def load_and_eval_scene(path) -> SceneState:
-    return SceneState(Path(path).read_text())
+    """A scene file with its relative imports resolved (lib.rs:280-284)."""
+    return SceneState(path=path)
 
 
 def extract_scene_render_settings(state: SceneState) -> SceneRenderSettings:

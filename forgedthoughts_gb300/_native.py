@@ -26,6 +26,9 @@ FT_ERR_UNSUPPORTED = 10
 FT_ERR_NO_DEVICE = 11
 FT_ERR_JIT = 12
 FT_ERR_INTERNAL = 13
+FT_ERR_IO = 14
+FT_ERR_MISSING_IMPORT = 15
+FT_ERR_IMPORT_CYCLE = 16
 
 # ft_light_kind
 FT_LIGHT_POINT = 0
@@ -198,6 +201,7 @@ SIGNATURES = {
     "ft_abi_version": (ctypes.c_uint32, []),
     "ft_last_error": (ctypes.c_char_p, []),
     "ft_scene_desc_from_source": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.POINTER(SceneDescC))]),
+    "ft_scene_desc_from_file": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.POINTER(SceneDescC))]),
     "ft_scene_desc_free": (None, [ctypes.POINTER(SceneDescC)]),
     "ft_scene_create": (ctypes.c_int, [ctypes.POINTER(SceneDescC), ctypes.POINTER(ctypes.c_void_p)]),
     "ft_scene_destroy": (None, [ctypes.c_void_p]),

@@ -6,8 +6,10 @@
 // eval}.rs): literals, hex colours, let/var bindings, path assignment, object
 // literals, `+ - &` on objects, SDF member operators (`union_round`, ...),
 // vector arithmetic and builtins, `fn` literals and top-level functions,
-// `material`, `environment` and `sdf` blocks.  Layout/skeleton/anchor
-// authoring features and file imports are not part of the render hot path.
+// `material`, `environment` and `sdf` blocks, and relative file imports with
+// aliases and export lists (crates/forgedthoughts/src/lib.rs:286-1304).
+// Layout/skeleton/anchor authoring features are not part of the render hot
+// path.
 #pragma once
 
 #include <cstdint>
@@ -76,7 +78,8 @@ struct FunctionDef {
 struct Stmt {  // Statement (ast.rs:108-130)
   enum Kind { Import, Export, Binding, Assign, Function, Material, Sdf, Skeleton, Environment };
   Kind kind = Binding;
-  std::string name;
+  std::string name;   // bound name; the path of an import
+  std::string alias;  // `import "..." as alias;` (empty: none)
   bool mutable_ = false;
   ExprP expr;
   std::vector<std::string> path;
@@ -85,6 +88,19 @@ struct Stmt {  // Statement (ast.rs:108-130)
 };
 
 std::vector<Stmt> parse_program(const std::string& source);
+
+// Reads `scene_path` and splices every `import` in place, recursively:
+// relative paths resolve from the importing file's directory, an import
+// with `as alias` has its top-level names qualified as `alias.name`, a file
+// with `export { ... }` contributes only the exported names and what they
+// depend on, and a file is spliced once per (file, alias) pair.  Throws
+// FrontendError with FT_ERR_IO, FT_ERR_MISSING_IMPORT, FT_ERR_IMPORT_CYCLE,
+// FT_ERR_UNSUPPORTED (a built-in library import) or FT_ERR_PARSE.
+std::vector<Stmt> load_program_with_imports(const std::string& scene_path);
+
+// `a.b.c` as the dotted name "a.b.c" (false for any other expression).  A
+// qualified name from an aliased import is looked up this way.
+bool flatten_member(const Expr& e, std::string* out);
 
 // ----------------------------------------------------------------- values
 // Mirrors `enum Value` (E:22-28).  Objects and arrays are shared and copied on

@@ -1,5 +1,6 @@
-// C ABI of the `.ft` front-end: ft_scene_desc_from_source / ft_scene_desc_free
-// and the thread-local error string shared by every entry point.
+// C ABI of the `.ft` front-end: ft_scene_desc_from_source / _from_file /
+// ft_scene_desc_free and the thread-local error string shared by every entry
+// point.
 #include <pthread.h>
 
 #include <cstring>
@@ -59,7 +60,8 @@ ft_status fail_current_exception() noexcept {
 namespace {
 
 struct FrontendJob {
-  const char* source = nullptr;
+  const char* source = nullptr;  // a scene source, or
+  const char* path = nullptr;    // a scene file whose imports are resolved
   std::unique_ptr<ftfe::OwnedSceneDesc> result;
   ft_status status = FT_OK;
   std::string error;
@@ -68,7 +70,8 @@ struct FrontendJob {
 void* run_frontend(void* arg) {
   auto* job = static_cast<FrontendJob*>(arg);
   try {
-    std::vector<ftfe::Stmt> program = ftfe::parse_program(job->source);
+    std::vector<ftfe::Stmt> program =
+        job->path ? ftfe::load_program_with_imports(job->path) : ftfe::parse_program(job->source);
     ftfe::EvalState state = ftfe::eval_program(program);
     job->result = ftfe::lower_scene(state);
   } catch (const ftfe::FrontendError& e) {
@@ -87,21 +90,8 @@ void* run_frontend(void* arg) {
   return nullptr;
 }
 
-}  // namespace
-
-extern "C" {
-
-uint32_t ft_abi_version(void) { return FT_ABI_VERSION; }
-
-// The string lives in thread-local storage and stays valid until the next
-// call on this thread that sets or clears it.
-const char* ft_last_error(void) { return ftcommon::last_error_cstr(); }
-
-ft_status ft_scene_desc_from_source(const char* source, ft_scene_desc** out) {
-  if (!source || !out) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "source and out must be non-null");
+ft_status run_frontend_job(FrontendJob& job, ft_scene_desc** out) {
   *out = nullptr;
-  FrontendJob job;
-  job.source = source;
   // Scenes such as `a + b + c + ...` over thousands of objects nest deeply;
   // the recursive evaluator runs on a thread with a large stack.
   pthread_attr_t attr;
@@ -120,6 +110,30 @@ ft_status ft_scene_desc_from_source(const char* source, ft_scene_desc** out) {
   *out = &owned->desc;
   ftcommon::clear_last_error();
   return FT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+uint32_t ft_abi_version(void) { return FT_ABI_VERSION; }
+
+// The string lives in thread-local storage and stays valid until the next
+// call on this thread that sets or clears it.
+const char* ft_last_error(void) { return ftcommon::last_error_cstr(); }
+
+ft_status ft_scene_desc_from_source(const char* source, ft_scene_desc** out) {
+  if (!source || !out) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "source and out must be non-null");
+  FrontendJob job;
+  job.source = source;
+  return run_frontend_job(job, out);
+}
+
+ft_status ft_scene_desc_from_file(const char* path, ft_scene_desc** out) {
+  if (!path || !out) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "path and out must be non-null");
+  FrontendJob job;
+  job.path = path;
+  return run_frontend_job(job, out);
 }
 
 void ft_scene_desc_free(ft_scene_desc* desc) {

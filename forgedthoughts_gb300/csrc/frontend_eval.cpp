@@ -166,6 +166,18 @@ void arity(const char* name, const std::vector<Value>& args, size_t n) {
 
 }  // namespace
 
+// flatten_member_expr (E:537-545).
+bool flatten_member(const Expr& e, std::string* out) {
+  if (e.kind == Expr::Ident) { *out = e.text; return true; }
+  if (e.kind == Expr::Member) {
+    std::string t;
+    if (!flatten_member(*e.lhs, &t)) return false;
+    *out = t + "." + e.text;
+    return true;
+  }
+  return false;
+}
+
 // eval_ident_call (E:2223-2690), render-relevant builtins.
 Value eval_builtin(const std::string& name, const std::vector<Value>& args, bool* found) {
   *found = true;
@@ -257,17 +269,6 @@ struct Scope {
 Value eval_expr(const Expr& e, const EvalState& st, const Scope& sc);
 Value call_user_body(const EvalState& st, const std::vector<std::string>& params, const std::vector<FnStmt>& body,
                      const std::vector<Value>& args, std::map<std::string, Value> locals, const Scope& sc);
-
-bool flatten_member(const Expr& e, std::string* out) {
-  if (e.kind == Expr::Ident) { *out = e.text; return true; }
-  if (e.kind == Expr::Member) {
-    std::string t;
-    if (!flatten_member(*e.lhs, &t)) return false;
-    *out = t + "." + e.text;
-    return true;
-  }
-  return false;
-}
 
 Value eval_binary(const Value& l, char op, const Value& r) {
   if (l.kind == Value::Number && r.kind == Value::Number) {
@@ -583,7 +584,10 @@ EvalState eval_program(const std::vector<Stmt>& program) {
   for (const Stmt& s : program) {
     switch (s.kind) {
       case Stmt::Import:
-        throw FrontendError(FT_ERR_UNSUPPORTED, "imports are not supported by this front-end: \"" + s.name + "\"");
+        // A source string has no directory to resolve an import from; the
+        // file loader splices imports before evaluation.
+        throw FrontendError(FT_ERR_UNSUPPORTED, "import \"" + s.name +
+                                                    "\" needs a scene file: load it with ft_scene_desc_from_file");
       case Stmt::Export:
       case Stmt::Skeleton:
         break;

@@ -553,6 +553,13 @@ class HookCompiler {
         return r;
       }
       case Expr::Member: {
+        // A dotted name bound at top level (`alias.name` of an aliased
+        // import) is read before member access (E:494-499).
+        std::string flat;
+        if (flatten_member(e, &flat)) {
+          auto b = st_.bindings.find(flat);
+          if (b != st_.bindings.end()) return cst(b->second.value);
+        }
         SVal base = eval(*e.lhs, locals, depth);
         if (base.rec) {
           auto it = base.rec->find(e.text);
@@ -692,6 +699,12 @@ class HookCompiler {
         return call_user(fn.params, fn.body, args, inner, depth);
       }
       fail("call to unknown function '" + name + "'");
+    }
+    // `alias.fn(...)`: a function of an aliased import (E:1855-1866).
+    std::string flat;
+    if (flatten_member(callee, &flat)) {
+      auto fi = st_.function_defs.find(flat);
+      if (fi != st_.function_defs.end()) return call_user(fi->second->params, fi->second->body, args, {}, depth);
     }
     fail("call on unsupported callee");
   }

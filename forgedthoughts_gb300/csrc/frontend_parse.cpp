@@ -185,7 +185,7 @@ class Parser {
     if (match(Tok::Import)) {
       s.kind = Stmt::Import;
       s.name = expect_string();
-      if (match_ident("as")) expect_ident();
+      if (match_ident("as")) s.alias = expect_ident();
       expect(Tok::Semicolon, ";");
       return s;
     }

@@ -45,7 +45,12 @@ typedef enum ft_status {
   FT_ERR_UNSUPPORTED = 10,
   FT_ERR_NO_DEVICE = 11,
   FT_ERR_JIT = 12,          /* run-time compilation (NVRTC) or module load failed */
-  FT_ERR_INTERNAL = 13      /* an unexpected host-side failure; no C++ exception crosses this ABI */
+  FT_ERR_INTERNAL = 13,     /* an unexpected host-side failure; no C++ exception crosses this ABI */
+  /* Scene-file loading, `CoreError::{Io,MissingImport,ImportCycle}`
+   * (crates/forgedthoughts/src/lib.rs:251-262). */
+  FT_ERR_IO = 14,             /* a scene file could not be read */
+  FT_ERR_MISSING_IMPORT = 15, /* a relative import names no file */
+  FT_ERR_IMPORT_CYCLE = 16    /* a file imports itself through a chain of imports */
 } ft_status;
 
 /* `enum AccelMode` (R:58-63). */
@@ -381,6 +386,19 @@ const char* ft_last_error(void);
  * crate.  The returned description is owned by the library; release it with
  * ft_scene_desc_free. */
 ft_status ft_scene_desc_from_source(const char* source, ft_scene_desc** out);
+
+/* The same for a scene file, with its imports resolved: replaces
+ * `load_and_eval_scene` / `load_program_with_imports`
+ * (crates/forgedthoughts/src/lib.rs:280-383).  `import "./x.ft";` and
+ * `import "../x.ft" as name;` load from the importing file's directory; an
+ * aliased import's top-level names become `name.binding`; a file with an
+ * `export { ... };` list contributes only those names and their
+ * dependencies; each (file, alias) pair is loaded once.  Imports that name
+ * the reference's built-in library (paths without ./ or ../) return
+ * FT_ERR_UNSUPPORTED: that library is not shipped.  A source passed to
+ * ft_scene_desc_from_source has no directory, so an import there returns
+ * FT_ERR_UNSUPPORTED as well. */
+ft_status ft_scene_desc_from_file(const char* path, ft_scene_desc** out);
 void ft_scene_desc_free(ft_scene_desc* desc);
 
 /* Upload a scene to the current CUDA device and build its culling structures
