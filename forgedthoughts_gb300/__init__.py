@@ -34,7 +34,7 @@ from . import _native
 __all__ = [
     "AccelMode", "RenderOptions", "SceneState", "GpuScene", "DepthImage", "PreviewProgress", "RenderError",
     "MissingSceneRoot", "UnsupportedObjectType", "ExpectedObject", "ParseError", "EvalError", "CudaError",
-    "SceneIoError", "MissingImport", "ImportCycle",
+    "SceneIoError", "MissingImport", "ImportCycle", "AmbiguousImport", "LibraryItem", "library_from_dir",
     "parse_and_eval", "load_and_eval_scene", "extract_scene_render_settings", "render_depth",
     "render_depth_png_with_accel", "render_preview_progressive_with_accel", "write_png", "read_png",
 ]
@@ -118,8 +118,15 @@ class ImportCycle(RenderError):
     status = _native.FT_ERR_IMPORT_CYCLE
 
 
+class AmbiguousImport(RenderError):
+    """A library name matches several items (``CoreError::AmbiguousBuiltinImport``)."""
+
+    status = _native.FT_ERR_AMBIGUOUS_IMPORT
+
+
 _ERRORS = {cls.status: cls for cls in (MissingSceneRoot, UnsupportedObjectType, ExpectedObject, ParseError,
-                                       EvalError, CudaError, JitError, SceneIoError, MissingImport, ImportCycle)}
+                                       EvalError, CudaError, JitError, SceneIoError, MissingImport, ImportCycle,
+                                       AmbiguousImport)}
 
 
 def _check(status: int) -> None:
@@ -153,12 +160,21 @@ class SceneState:
     GPU copy is created on first use and cached.
     """
 
-    def __init__(self, source: Optional[str] = None, path=None):
+    def __init__(self, source: Optional[str] = None, path=None, library=None):
         lib = _native.lib()
         ptr = ctypes.POINTER(_native.SceneDescC)()
         self._desc = ptr
         self._gpu: Optional[GpuScene] = None
-        if path is not None:
+        if path is not None and library is not None:
+            items = list(library)
+            arr = (_native.LibraryItemC * max(1, len(items)))()
+            keep = []
+            for i, it in enumerate(items):
+                fields = [x.encode("utf-8") for x in (it.name, it.path, it.source)]
+                keep.append(fields)
+                arr[i] = _native.LibraryItemC(*fields)
+            _check(lib.ft_scene_desc_from_file_with_library(os.fsencode(path), arr, len(items), ctypes.byref(ptr)))
+        elif path is not None:
             _check(lib.ft_scene_desc_from_file(os.fsencode(path), ctypes.byref(ptr)))
         else:
             _check(lib.ft_scene_desc_from_source(source.encode("utf-8"), ctypes.byref(ptr)))
@@ -202,9 +218,39 @@ def parse_and_eval(source: str) -> SceneState:
     return SceneState(source)
 
 
-def load_and_eval_scene(path) -> SceneState:
-    """A scene file with its relative imports resolved (lib.rs:280-284)."""
-    return SceneState(path=path)
+@dataclasses.dataclass(frozen=True)
+class LibraryItem:
+    """An asset library item (``BuiltinLibraryItem``, lib.rs:54-61)."""
+
+    name: str
+    path: str
+    source: str
+
+
+def library_from_dir(root) -> list:
+    """Library items for every ``.ft`` file under ``root``: ``path`` is the
+    file's path below ``root`` with ``/`` separators, ``name`` its stem in
+    CamelCase (``materials/checker_floor.ft`` -> ``CheckerFloor``), the
+    naming of the reference's library directory."""
+    root = Path(root)
+    items = []
+    for f in sorted(root.rglob("*.ft")):
+        name = "".join(part[:1].upper() + part[1:] for part in f.stem.split("_") if part)
+        items.append(LibraryItem(name, f.relative_to(root).as_posix(), f.read_text()))
+    return items
+
+
+def load_and_eval_scene(path, library=None) -> SceneState:
+    """A scene file with its imports resolved (``load_and_eval_scene``,
+    lib.rs:280-284).  ``library`` gives the items that non-relative imports
+    select: a sequence of :class:`LibraryItem`, or a directory read with
+    :func:`library_from_dir`.  Without it, ``FT_LIBRARY_DIR`` names the
+    directory if set; otherwise such an import raises ``RenderError``."""
+    if library is None and os.environ.get("FT_LIBRARY_DIR"):
+        library = os.environ["FT_LIBRARY_DIR"]
+    if isinstance(library, (str, os.PathLike)):
+        library = library_from_dir(library)
+    return SceneState(path=path, library=library)
 
 
 def extract_scene_render_settings(state: SceneState) -> SceneRenderSettings:

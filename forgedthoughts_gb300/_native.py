@@ -29,6 +29,7 @@ FT_ERR_INTERNAL = 13
 FT_ERR_IO = 14
 FT_ERR_MISSING_IMPORT = 15
 FT_ERR_IMPORT_CYCLE = 16
+FT_ERR_AMBIGUOUS_IMPORT = 17
 
 # ft_light_kind
 FT_LIGHT_POINT = 0
@@ -125,6 +126,10 @@ class SceneDescC(ctypes.Structure):
                 ("settings", RenderOptionsC), ("settings_accel", ctypes.c_int32)]
 
 
+class LibraryItemC(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char_p), ("path", ctypes.c_char_p), ("source", ctypes.c_char_p)]
+
+
 class BuildInfoC(ctypes.Structure):
     _fields_ = [("leaves", ctypes.c_uint32), ("primitive_leaves", ctypes.c_uint32),
                 ("generic_leaves", ctypes.c_uint32), ("union_round_leaves", ctypes.c_uint32),
@@ -202,6 +207,9 @@ SIGNATURES = {
     "ft_last_error": (ctypes.c_char_p, []),
     "ft_scene_desc_from_source": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.POINTER(SceneDescC))]),
     "ft_scene_desc_from_file": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.POINTER(SceneDescC))]),
+    "ft_scene_desc_from_file_with_library": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(LibraryItemC),
+                                                             ctypes.c_uint32,
+                                                             ctypes.POINTER(ctypes.POINTER(SceneDescC))]),
     "ft_scene_desc_free": (None, [ctypes.POINTER(SceneDescC)]),
     "ft_scene_create": (ctypes.c_int, [ctypes.POINTER(SceneDescC), ctypes.POINTER(ctypes.c_void_p)]),
     "ft_scene_destroy": (None, [ctypes.c_void_p]),

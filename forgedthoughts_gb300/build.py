@@ -35,7 +35,7 @@ GENCODE = "arch=compute_103a,code=sm_103a"
 CXXFLAGS = ["-std=c++17", "-O2", "-fPIC", "-Wall", "-Wextra", "-Wno-unused-parameter"]
 
 CPP_SOURCES = ["frontend_parse.cpp", "frontend_eval.cpp", "frontend_lower.cpp", "frontend_import.cpp",
-               "frontend_api.cpp", "scene_build.cpp", "jit_codegen.cpp"]
+               "frontend_layout.cpp", "frontend_api.cpp", "scene_build.cpp", "jit_codegen.cpp"]
 CU_SOURCES = ["ft_render.cu"]
 HEADERS = ["frontend.h", "common.h", "scene_build.h", "ft_device.cuh", "ft_trace.cuh", "ft_bricks.cuh", "ft_diff.cuh",
            "ft_kernels.cuh", "ft_layout.h", "jit.h", "ft_wavefront.cuh", "ft_path.cuh"]

@@ -89,14 +89,22 @@ struct Stmt {  // Statement (ast.rs:108-130)
 
 std::vector<Stmt> parse_program(const std::string& source);
 
+// An asset library item (`BuiltinLibraryItem`, lib.rs:54-61).
+struct LibraryItem {
+  std::string name, path, source;
+};
+
 // Reads `scene_path` and splices every `import` in place, recursively:
-// relative paths resolve from the importing file's directory, an import
-// with `as alias` has its top-level names qualified as `alias.name`, a file
-// with `export { ... }` contributes only the exported names and what they
-// depend on, and a file is spliced once per (file, alias) pair.  Throws
-// FrontendError with FT_ERR_IO, FT_ERR_MISSING_IMPORT, FT_ERR_IMPORT_CYCLE,
-// FT_ERR_UNSUPPORTED (a built-in library import) or FT_ERR_PARSE.
-std::vector<Stmt> load_program_with_imports(const std::string& scene_path);
+// relative paths resolve from the importing file's directory, other paths
+// and names select an item of `library`, an import with `as alias` has its
+// top-level names qualified as `alias.name`, a file with `export { ... }`
+// contributes only the exported names and what they depend on, and a file
+// is spliced once per (file, alias) pair.  Throws FrontendError with
+// FT_ERR_IO, FT_ERR_MISSING_IMPORT, FT_ERR_IMPORT_CYCLE,
+// FT_ERR_AMBIGUOUS_IMPORT, FT_ERR_UNSUPPORTED (a library import with no
+// library given) or FT_ERR_PARSE.
+std::vector<Stmt> load_program_with_imports(const std::string& scene_path,
+                                            const std::vector<LibraryItem>* library = nullptr);
 
 // `a.b.c` as the dotted name "a.b.c" (false for any other expression).  A
 // qualified name from an aliased import is looked up this way.
@@ -163,6 +171,14 @@ EvalState eval_program(const std::vector<Stmt>& program);
 
 // Evaluation helpers shared with the lowering step.
 Value eval_builtin(const std::string& name, const std::vector<Value>& args, bool* found);
+
+// Layout member operators and anchor symbols (frontend_layout.cpp).
+bool is_anchor_symbol(const std::string& name);
+Value anchor_symbol(const std::string& name, float offset);
+// `Top + 0.3`: an anchor symbol with an offset; false for other operands.
+bool anchor_arithmetic(const Value& l, char op, const Value& r, Value* out);
+bool is_layout_member_operator(const std::string& field);
+Value build_layout_member(const std::string& field, Value base, const std::vector<Value>& args);
 
 // ---------------------------------------------------------------- lowering
 // Owned storage behind an ft_scene_desc returned to C callers.

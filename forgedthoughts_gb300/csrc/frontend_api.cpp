@@ -62,6 +62,7 @@ namespace {
 struct FrontendJob {
   const char* source = nullptr;  // a scene source, or
   const char* path = nullptr;    // a scene file whose imports are resolved
+  const std::vector<ftfe::LibraryItem>* library = nullptr;
   std::unique_ptr<ftfe::OwnedSceneDesc> result;
   ft_status status = FT_OK;
   std::string error;
@@ -71,7 +72,7 @@ void* run_frontend(void* arg) {
   auto* job = static_cast<FrontendJob*>(arg);
   try {
     std::vector<ftfe::Stmt> program =
-        job->path ? ftfe::load_program_with_imports(job->path) : ftfe::parse_program(job->source);
+        job->path ? ftfe::load_program_with_imports(job->path, job->library) : ftfe::parse_program(job->source);
     ftfe::EvalState state = ftfe::eval_program(program);
     job->result = ftfe::lower_scene(state);
   } catch (const ftfe::FrontendError& e) {
@@ -123,17 +124,36 @@ uint32_t ft_abi_version(void) { return FT_ABI_VERSION; }
 const char* ft_last_error(void) { return ftcommon::last_error_cstr(); }
 
 ft_status ft_scene_desc_from_source(const char* source, ft_scene_desc** out) {
+  FT_API_BEGIN
   if (!source || !out) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "source and out must be non-null");
   FrontendJob job;
   job.source = source;
   return run_frontend_job(job, out);
+  FT_API_END
 }
 
 ft_status ft_scene_desc_from_file(const char* path, ft_scene_desc** out) {
+  return ft_scene_desc_from_file_with_library(path, nullptr, 0, out);
+}
+
+ft_status ft_scene_desc_from_file_with_library(const char* path, const ft_library_item* items, uint32_t n_items,
+                                               ft_scene_desc** out) {
+  FT_API_BEGIN
   if (!path || !out) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "path and out must be non-null");
+  if (n_items && !items) return ftcommon::fail(FT_ERR_INVALID_ARGUMENT, "items is null but n_items is not 0");
+  std::vector<ftfe::LibraryItem> library;
+  library.reserve(n_items);
+  for (uint32_t i = 0; i < n_items; ++i) {
+    if (!items[i].name || !items[i].path || !items[i].source)
+      return ftcommon::fail(FT_ERR_INVALID_ARGUMENT,
+                            "library item " + std::to_string(i) + " has a null name, path or source");
+    library.push_back({items[i].name, items[i].path, items[i].source});
+  }
   FrontendJob job;
   job.path = path;
+  job.library = items ? &library : nullptr;
   return run_frontend_job(job, out);
+  FT_API_END
 }
 
 void ft_scene_desc_free(ft_scene_desc* desc) {

@@ -291,6 +291,7 @@ Value eval_binary(const Value& l, char op, const Value& r) {
       }
     }
   }
+  if (Value anchored; anchor_arithmetic(l, op, r, &anchored)) return anchored;
   if (op == '+' || op == '-' || op == '&') {
     std::map<std::string, Value> f;
     f["lhs"] = l;
@@ -451,6 +452,11 @@ Value eval_call(const Expr& e, const EvalState& st, const Scope& sc) {
     std::vector<Value> args = eval_args(e.items, st, sc);
     return build_sdf_member(field, base, args);
   }
+  if (is_layout_member_operator(field)) {
+    Value base = eval_expr(*callee.lhs, st, sc);
+    std::vector<Value> args = eval_args(e.items, st, sc);
+    return build_layout_member(field, std::move(base), args);
+  }
   std::string flat;
   if (flatten_member(callee, &flat)) {
     std::vector<Value> args = eval_args(e.items, st, sc);
@@ -458,6 +464,43 @@ Value eval_call(const Expr& e, const EvalState& st, const Scope& sc) {
     if (fit != st.function_defs.end()) return call_top_level(st, *fit->second, args, sc.depth + 1);
   }
   eval_fail("call on unsupported callee");
+}
+
+// augment_object_literal_fields (E:547-575) for an instance of an `sdf`
+// definition: its layout bounds `__bounds` (the definition's `bounds()`) and
+// its `anchors` binding, each evaluated with the instance's fields replacing
+// the definition's bindings, and each left out when its evaluation fails.
+void augment_sdf_instance(const EvalState& st, const BlockDef& def, std::map<std::string, Value>& fields,
+                          int depth) {
+  if (depth >= 32) return;
+  std::map<std::string, Value> locals = fields;  // sdf_override_locals (E:3338-3342)
+  bool have_anchors = false, locals_ok = false;
+  Value anchors;
+  try {
+    Scope bs{&locals, &def, nullptr, depth + 1};
+    for (const BlockStmt& s : def.statements) {
+      if (s.kind != BlockStmt::Binding) continue;
+      auto it = fields.find(s.name);
+      locals[s.name] = it != fields.end() ? it->second : eval_expr(*s.expr, st, bs);
+      if (s.name == "anchors" && !have_anchors) {
+        anchors = locals[s.name];
+        have_anchors = true;
+      }
+    }
+    locals_ok = true;
+  } catch (const FrontendError&) {
+  }
+  if (!fields.count("__bounds") && locals_ok) {
+    const BlockStmt* fn = find_block_fn(&def, "bounds");
+    if (fn && fn->params.empty()) {
+      try {
+        Scope inner{nullptr, &def, nullptr, depth + 1};
+        fields["__bounds"] = call_user_body(st, {}, fn->body, {}, locals, inner);
+      } catch (const FrontendError&) {
+      }
+    }
+  }
+  if (!fields.count("anchors") && have_anchors) fields["anchors"] = anchors;
 }
 
 Value eval_expr(const Expr& e, const EvalState& st, const Scope& sc) {
@@ -490,6 +533,8 @@ Value eval_expr(const Expr& e, const EvalState& st, const Scope& sc) {
         auto it = sc.locals->find(e.text);
         if (it != sc.locals->end()) return it->second;
       }
+      // Anchor symbols come before bindings (E:454-466).
+      if (is_anchor_symbol(e.text)) return anchor_symbol(e.text, 0.0f);
       auto it = st.bindings.find(e.text);
       if (it == st.bindings.end()) eval_fail("undefined identifier '" + e.text + "'");
       return it->second.value;
@@ -497,6 +542,8 @@ Value eval_expr(const Expr& e, const EvalState& st, const Scope& sc) {
     case Expr::ObjectLiteral: {
       std::map<std::string, Value> f;
       for (const auto& kv : e.fields) f[kv.first] = eval_expr(*kv.second, st, sc);
+      auto def = st.sdf_defs.find(e.text);
+      if (def != st.sdf_defs.end()) augment_sdf_instance(st, *def->second, f, sc.depth);
       return make_object(e.text, std::move(f));
     }
     case Expr::Binary: {

@@ -7,8 +7,10 @@
 //   namespace_statements / namespace_expr / _path    lib.rs:623-914, 1228-1304
 //   collect_export_names / filter_exported_statements lib.rs:916-986
 //   statement_dependencies / expr_dependencies       lib.rs:988-1226
-// The reference's built-in library (imports without ./ or ../) is not part of
-// this front-end; such an import fails with FT_ERR_UNSUPPORTED.
+//   resolve_builtin_library_name                     lib.rs:432-451
+// The reference's built-in library is not part of this front-end: a caller
+// passes its items (name, path, source) in; without them an import that is
+// not a relative path fails with FT_ERR_UNSUPPORTED.
 #include <limits.h>
 #include <stdlib.h>
 #include <sys/stat.h>
@@ -309,43 +311,72 @@ std::string read_file(const std::string& path) {
   return ss.str();
 }
 
+// An import's identity (`ImportKey`, lib.rs:293-297): a file's canonical
+// path, or "builtin:" + a library item's path, which is also how a cycle
+// report names it (lib.rs:418-422).
+const char kBuiltin[] = "builtin:";
+
 struct Loader {
-  // (file, alias) pairs already spliced (lib.rs:321); "" is "no alias",
+  const std::vector<LibraryItem>* library = nullptr;
+  // (key, alias) pairs already spliced (lib.rs:321); "" is "no alias",
   // which no identifier can spell.
   std::set<std::pair<std::string, std::string>> loaded;
-  std::vector<std::string> stack;  // files being loaded, for cycle reports
+  std::vector<std::string> stack;  // keys being loaded, for cycle reports
 
-  // resolve_import (lib.rs:385-416) for relative paths.
+  const LibraryItem* item_by_path(const std::string& path) const {
+    for (const LibraryItem& it : *library)
+      if (it.path == path) return &it;
+    return nullptr;
+  }
+
+  // resolve_import (lib.rs:385-416): relative paths are files; anything
+  // else is a library item's path, then a library item's name.
   std::string resolve(const std::string& path, const std::string& base_dir) {
-    if (!starts_with(path, "./") && !starts_with(path, "../"))
+    if (starts_with(path, "./") || starts_with(path, "../")) {
+      std::string joined = base_dir + "/" + path, out;
+      if (!canonicalize(joined, &out)) {
+        if (errno == ENOENT || errno == ENOTDIR)
+          load_fail(FT_ERR_MISSING_IMPORT, "missing import '" + path + "' from " + base_dir);
+        load_fail(FT_ERR_IO, "failed to read scene file " + joined + ": " + std::strerror(errno));
+      }
+      return out;
+    }
+    if (!library)
       load_fail(FT_ERR_UNSUPPORTED, "import '" + path + "' from " + base_dir +
                                         " names the built-in library, which this front-end does not ship;"
-                                        " only ./ and ../ imports are resolved");
-    std::string joined = base_dir + "/" + path, out;
-    if (!canonicalize(joined, &out)) {
-      if (errno == ENOENT || errno == ENOTDIR)
-        load_fail(FT_ERR_MISSING_IMPORT, "missing import '" + path + "' from " + base_dir);
-      load_fail(FT_ERR_IO, "failed to read scene file " + joined + ": " + std::strerror(errno));
+                                        " pass the library's items to load it");
+    if (item_by_path(path)) return kBuiltin + path;
+    std::vector<const LibraryItem*> named;
+    for (const LibraryItem& it : *library)
+      if (it.name == path) named.push_back(&it);
+    if (named.size() == 1) return kBuiltin + named[0]->path;
+    if (named.size() > 1) {
+      std::string paths;
+      for (const LibraryItem* it : named) paths += (paths.empty() ? "" : ", ") + it->path;
+      load_fail(FT_ERR_AMBIGUOUS_IMPORT, "ambiguous built-in import '" + path + "' matches: " + paths);
     }
-    return out;
+    load_fail(FT_ERR_MISSING_IMPORT, "missing import '" + path + "' from " + base_dir);
   }
 
   // load_import_source (lib.rs:317-383).
-  std::vector<Stmt> load(const std::string& file, const std::string& alias) {
-    if (loaded.count({file, alias})) return {};
-    if (std::find(stack.begin(), stack.end(), file) != stack.end()) {
+  std::vector<Stmt> load(const std::string& key, const std::string& alias) {
+    if (loaded.count({key, alias})) return {};
+    if (std::find(stack.begin(), stack.end(), key) != stack.end()) {
       std::string cycle;
-      for (const std::string& f : stack) cycle += f + " -> ";
-      load_fail(FT_ERR_IMPORT_CYCLE, "import cycle detected: " + cycle + file);
+      for (const std::string& k : stack) cycle += k + " -> ";
+      load_fail(FT_ERR_IMPORT_CYCLE, "import cycle detected: " + cycle + key);
     }
-    stack.push_back(file);
-    const std::string base_dir = directory_of(file);
+    stack.push_back(key);
+    const bool builtin = starts_with(key, kBuiltin);
+    // A library item has no directory: its relative imports resolve from
+    // the working directory (lib.rs:342, 387).
+    const std::string base_dir = builtin ? "." : directory_of(key);
     std::vector<Stmt> program;
     try {
-      program = parse_program(read_file(file));
+      program = parse_program(builtin ? item_by_path(key.substr(sizeof kBuiltin - 1))->source : read_file(key));
     } catch (const FrontendError& e) {
       if (e.status != FT_ERR_PARSE) throw;
-      load_fail(FT_ERR_PARSE, file + ": " + e.what());
+      load_fail(FT_ERR_PARSE, key + ": " + e.what());
     }
     const std::optional<NameSet> exported = export_names(program);
     std::vector<Stmt> stmts;
@@ -360,18 +391,19 @@ struct Loader {
     if (exported) stmts = filter_exported(std::move(stmts), *exported);
     stack.pop_back();
     if (!alias.empty()) stmts = namespace_statements(std::move(stmts), alias);
-    loaded.insert({file, alias});
+    loaded.insert({key, alias});
     return stmts;
   }
 };
 
 }  // namespace
 
-std::vector<Stmt> load_program_with_imports(const std::string& scene_path) {
+std::vector<Stmt> load_program_with_imports(const std::string& scene_path, const std::vector<LibraryItem>* library) {
   std::string file;
   if (!canonicalize(scene_path, &file))
     load_fail(FT_ERR_IO, "failed to read scene file " + scene_path + ": " + std::strerror(errno));
   Loader loader;
+  loader.library = library;
   return loader.load(file, "");
 }
 

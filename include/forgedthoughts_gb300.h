@@ -50,7 +50,8 @@ typedef enum ft_status {
    * (crates/forgedthoughts/src/lib.rs:251-262). */
   FT_ERR_IO = 14,             /* a scene file could not be read */
   FT_ERR_MISSING_IMPORT = 15, /* a relative import names no file */
-  FT_ERR_IMPORT_CYCLE = 16    /* a file imports itself through a chain of imports */
+  FT_ERR_IMPORT_CYCLE = 16,   /* a file imports itself through a chain of imports */
+  FT_ERR_AMBIGUOUS_IMPORT = 17 /* a library name matches several items (`AmbiguousBuiltinImport`) */
 } ft_status;
 
 /* `enum AccelMode` (R:58-63). */
@@ -399,6 +400,25 @@ ft_status ft_scene_desc_from_source(const char* source, ft_scene_desc** out);
  * ft_scene_desc_from_source has no directory, so an import there returns
  * FT_ERR_UNSUPPORTED as well. */
 ft_status ft_scene_desc_from_file(const char* path, ft_scene_desc** out);
+
+/* One item of an asset library, the role of `BuiltinLibraryItem`
+ * (crates/forgedthoughts/src/lib.rs:54-61): `import "materials/gold.ft";`
+ * selects an item by `path`, `import "Gold";` by `name` (a name that several
+ * items share is FT_ERR_AMBIGUOUS_IMPORT). */
+typedef struct ft_library_item {
+  const char* name;
+  const char* path;
+  const char* source; /* the item's `.ft` text */
+} ft_library_item;
+
+/* ft_scene_desc_from_file with an asset library for imports that are not
+ * relative paths (`resolve_import`, lib.rs:385-416): the reference passes its
+ * built-in library table here.  With a library, an import that matches no
+ * item is FT_ERR_MISSING_IMPORT; imports inside an item resolve relative
+ * paths from the working directory, as the reference's do.  The strings are
+ * read during the call only. */
+ft_status ft_scene_desc_from_file_with_library(const char* path, const ft_library_item* items, uint32_t n_items,
+                                               ft_scene_desc** out);
 void ft_scene_desc_free(ft_scene_desc* desc);
 
 /* Upload a scene to the current CUDA device and build its culling structures

@@ -273,3 +273,66 @@ def test_c_entry_point_rejects_null_arguments():
     out = ctypes.POINTER(_native.SceneDescC)()
     assert lib.ft_scene_desc_from_file(None, ctypes.byref(out)) == _native.FT_ERR_INVALID_ARGUMENT
     assert lib.ft_scene_desc_from_file(b"x.ft", None) == _native.FT_ERR_INVALID_ARGUMENT
+
+
+LIB_GOLD = "material Gold {\n  model: Metal;\n  color = vec3(0.95, 0.75, 0.3);\n  roughness = 0.2;\n};\nexport { Gold };\n"
+LIB_FLOOR = ("let floor_mat = Lambert { color: vec3(0.8) };\n"
+             "let Floor = Box { size: vec3(8.0, 0.5, 8.0), pos: vec3(0.0, -0.25, 0.0), material: floor_mat };\n"
+             "export { Floor };\n")
+
+
+def _library():
+    return [ft.LibraryItem("Gold", "materials/gold.ft", LIB_GOLD),
+            ft.LibraryItem("StageFloor", "objects/stage_floor.ft", LIB_FLOOR)]
+
+
+def test_library_imports_by_path_and_by_name(tmp_path):
+    """Imports that are not relative paths select a library item by path or
+    by name (resolve_import, lib.rs:385-416); the caller supplies the items,
+    as the reference supplies its built-in table."""
+    _write(tmp_path, {
+        "by_path.ft": 'import "materials/gold.ft" as gold;\nimport "objects/stage_floor.ft";\n'
+                      "let scene = Floor + Sphere { pos: vec3(0.0, 1.0, 0.0), material: gold.Gold {} };\n",
+        "by_name.ft": 'import "Gold";\nimport "StageFloor";\n'
+                      "let scene = Floor + Sphere { pos: vec3(0.0, 1.0, 0.0), material: Gold {} };\n",
+    })
+    single = (LIB_GOLD.replace("export { Gold };", "") + LIB_FLOOR.replace("export { Floor };", "")
+              + "let scene = Floor + Sphere { pos: vec3(0.0, 1.0, 0.0), material: Gold {} };\n")
+    ref = _dump(ft.parse_and_eval(single))
+    assert _dump(ft.load_and_eval_scene(tmp_path / "by_path.ft", library=_library())) == ref
+    assert _dump(ft.load_and_eval_scene(tmp_path / "by_name.ft", library=_library())) == ref
+
+
+def test_library_directory_naming(tmp_path, monkeypatch):
+    """library_from_dir names each file's item by its stem in CamelCase;
+    FT_LIBRARY_DIR supplies the directory when no library is passed."""
+    _write(tmp_path / "lib", {"materials/gold.ft": LIB_GOLD, "objects/stage_floor.ft": LIB_FLOOR})
+    items = ft.library_from_dir(tmp_path / "lib")
+    assert [(i.name, i.path) for i in items] == [("Gold", "materials/gold.ft"),
+                                                ("StageFloor", "objects/stage_floor.ft")]
+    _write(tmp_path, {"main.ft": 'import "Gold";\nlet scene = Sphere { material: Gold {} };\n'})
+    monkeypatch.setenv("FT_LIBRARY_DIR", str(tmp_path / "lib"))
+    _same_scene(tmp_path / "main.ft", LIB_GOLD.replace("export { Gold };", "")
+                + "let scene = Sphere { material: Gold {} };\n")
+
+
+def test_library_import_errors(tmp_path):
+    twin = _library() + [ft.LibraryItem("Gold", "materials/gold_leaf.ft", LIB_GOLD)]
+    loop = [ft.LibraryItem("Loop", "scenes/loop.ft", 'import "Loop";\nlet x = 1.0;\n')]
+    _write(tmp_path, {
+        "twin.ft": 'import "Gold";\nlet scene = Sphere {};\n',
+        "unknown.ft": 'import "Silver";\nlet scene = Sphere {};\n',
+        "loop.ft": 'import "Loop";\nlet scene = Sphere {};\n',
+    })
+    with pytest.raises(ft.AmbiguousImport,
+                       match="ambiguous built-in import 'Gold' matches: materials/gold.ft, materials/gold_leaf.ft"):
+        ft.load_and_eval_scene(tmp_path / "twin.ft", library=twin)
+    with pytest.raises(ft.MissingImport, match="missing import 'Silver' from "):
+        ft.load_and_eval_scene(tmp_path / "unknown.ft", library=_library())
+    with pytest.raises(ft.ImportCycle, match="builtin:scenes/loop.ft -> builtin:scenes/loop.ft"):
+        ft.load_and_eval_scene(tmp_path / "loop.ft", library=loop)
+    lib = _native.lib()
+    out = ctypes.POINTER(_native.SceneDescC)()
+    bad = (_native.LibraryItemC * 1)(_native.LibraryItemC(b"X", None, b""))
+    assert lib.ft_scene_desc_from_file_with_library(str(tmp_path / "loop.ft").encode(), bad, 1,
+                                                    ctypes.byref(out)) == _native.FT_ERR_INVALID_ARGUMENT
